@@ -1,0 +1,189 @@
+"""blaze_gb300 — GB300 (sm_103a) backend for Blaze's dense matrix multiplication.
+
+The product is the C-ABI shared library ``libgb300blas.so`` (headers in ``include/``): a drop-in
+CBLAS ``cblas_dgemm``/``cblas_sgemm`` for Blaze's BLAS mode plus the extended ``gb300_*`` API.
+This module is a thin ctypes binding over that library, used by the tests and the benchmark the
+way Blaze's own blazetest/blazemark programs use ``blaze::gemm``.  There is no CPU path here: if
+the library is missing, importing the binding raises.
+"""
+from __future__ import annotations
+
+import ctypes as ct
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libgb300blas.so")
+
+# CBLAS enums (standard ABI values)
+RowMajor, ColMajor = 101, 102
+NoTrans, Trans, ConjTrans = 111, 112, 113
+
+# gb300_status
+OK, ERR_INVALID_ARG, ERR_CUDA, ERR_NO_MEMORY, ERR_DEVICE_TIMEOUT, ERR_NOT_SUPPORTED, ERR_NO_DEVICE, ERR_ADMISSION = range(8)
+# gb300_method
+METHOD_AUTO, METHOD_NATIVE, METHOD_SPLIT, METHOD_BF16X3, METHOD_BF16 = range(5)
+METHODS = {"auto": METHOD_AUTO, "native": METHOD_NATIVE, "split": METHOD_SPLIT, "bf16x3": METHOD_BF16X3,
+           "bf16": METHOD_BF16}
+# gb300_residency
+PTR_DETECT, PTR_DEVICE, PTR_HOST = range(3)
+
+
+class GemmOpts(ct.Structure):
+    _fields_ = [
+        ("method", ct.c_int),
+        ("slices", ct.c_int),
+        ("target_error", ct.c_double),
+        ("residency", ct.c_int),
+        ("stream", ct.c_void_p),
+        ("synchronous", ct.c_int),
+        ("method_used", ct.c_int),
+        ("slices_used", ct.c_int),
+        ("error_bound", ct.c_double),
+    ]
+
+
+class Gb300Error(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"[status {status}] {message}")
+        self.status = status
+
+
+_lib = None
+
+
+def build(force: bool = False) -> str:
+    from . import build as _b
+    return _b.build(force=force)
+
+
+def lib() -> ct.CDLL:
+    """Load libgb300blas.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"{LIB_PATH} is missing: run `python -m blaze_gb300.build` (needs nvcc)")
+    L = ct.CDLL(LIB_PATH)
+    I32, I64, D, F, VP = ct.c_int32, ct.c_int64, ct.c_double, ct.c_float, ct.c_void_p
+    L.cblas_dgemm.argtypes = [ct.c_int, ct.c_int, ct.c_int, I32, I32, I32, D, VP, I32, VP, I32, D, VP, I32]
+    L.cblas_dgemm.restype = None
+    L.cblas_sgemm.argtypes = [ct.c_int, ct.c_int, ct.c_int, I32, I32, I32, F, VP, I32, VP, I32, F, VP, I32]
+    L.cblas_sgemm.restype = None
+    L.cblas_dgemm_64.argtypes = [ct.c_int, ct.c_int, ct.c_int, I64, I64, I64, D, VP, I64, VP, I64, D, VP, I64]
+    L.cblas_dgemm_64.restype = None
+    L.cblas_sgemm_64.argtypes = [ct.c_int, ct.c_int, ct.c_int, I64, I64, I64, F, VP, I64, VP, I64, F, VP, I64]
+    L.cblas_sgemm_64.restype = None
+    L.gb300_dgemm_ex.argtypes = [ct.c_int, ct.c_int, ct.c_int, I64, I64, I64, D, VP, I64, VP, I64, D, VP, I64,
+                                 ct.POINTER(GemmOpts)]
+    L.gb300_dgemm_ex.restype = ct.c_int
+    L.gb300_sgemm_ex.argtypes = [ct.c_int, ct.c_int, ct.c_int, I64, I64, I64, F, VP, I64, VP, I64, F, VP, I64,
+                                 ct.POINTER(GemmOpts)]
+    L.gb300_sgemm_ex.restype = ct.c_int
+    L.gb300_gemm_opts_init.argtypes = [ct.POINTER(GemmOpts)]
+    L.gb300_gemm_opts_init.restype = None
+    L.gb300_last_error.restype = ct.c_int
+    L.gb300_last_error_message.restype = ct.c_char_p
+    L.gb300_clear_error.restype = None
+    L.gb300_set_default_method.argtypes = [ct.c_int]
+    L.gb300_set_default_method.restype = ct.c_int
+    L.gb300_device_info.argtypes = [ct.POINTER(ct.c_int), ct.POINTER(I64), ct.POINTER(I64)]
+    L.gb300_device_info.restype = ct.c_int
+    L.gb300_launch_count.restype = I64
+    L.gb300_measure_fp64_peak.argtypes = [ct.POINTER(ct.c_double)]
+    L.gb300_measure_fp64_peak.restype = ct.c_int
+    L.gb300_synchronize.restype = ct.c_int
+    L.gb300_debug_inject_stall.argtypes = [ct.c_int, ct.c_uint64]
+    L.gb300_debug_inject_stall.restype = None
+    _lib = L
+    return L
+
+
+def last_error() -> tuple[int, str]:
+    L = lib()
+    msg = L.gb300_last_error_message()
+    return L.gb300_last_error(), (msg.decode() if msg else "")
+
+
+def check(status: int) -> None:
+    if status != OK:
+        st, msg = last_error()
+        raise Gb300Error(status, msg)
+
+
+def opts(method: str | int = "auto", slices: int = 0, target_error: float = 0.0, residency: int = PTR_DETECT,
+         stream: int | None = None, synchronous: bool = True) -> GemmOpts:
+    o = GemmOpts()
+    lib().gb300_gemm_opts_init(ct.byref(o))
+    o.method = METHODS[method] if isinstance(method, str) else int(method)
+    o.slices = slices
+    o.target_error = target_error
+    o.residency = residency
+    o.stream = stream
+    o.synchronous = 1 if synchronous else 0
+    return o
+
+
+def _addr(x) -> int:
+    """Address of a numpy array, torch tensor or raw integer pointer."""
+    if x is None:
+        return 0
+    if isinstance(x, int):
+        return x
+    if hasattr(x, "data_ptr"):
+        return x.data_ptr()
+    return x.ctypes.data
+
+
+def dgemm_ex(order, transA, transB, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, o: GemmOpts | None = None) -> GemmOpts:
+    o = o if o is not None else opts()
+    st = lib().gb300_dgemm_ex(order, transA, transB, m, n, k, alpha, _addr(A), lda, _addr(B), ldb, beta, _addr(C),
+                              ldc, ct.byref(o))
+    check(st)
+    return o
+
+
+def sgemm_ex(order, transA, transB, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, o: GemmOpts | None = None) -> GemmOpts:
+    o = o if o is not None else opts(method="native")
+    st = lib().gb300_sgemm_ex(order, transA, transB, m, n, k, alpha, _addr(A), lda, _addr(B), ldb, beta, _addr(C),
+                              ldc, ct.byref(o))
+    check(st)
+    return o
+
+
+def cblas_dgemm(order, transA, transB, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc) -> None:
+    """The exact call Blaze's BLAS mode makes (32-bit integers); raises on a recorded error."""
+    L = lib()
+    L.gb300_clear_error()
+    L.cblas_dgemm(order, transA, transB, m, n, k, alpha, _addr(A), lda, _addr(B), ldb, beta, _addr(C), ldc)
+    st, msg = last_error()
+    if st != OK:
+        raise Gb300Error(st, msg)
+
+
+def cblas_sgemm(order, transA, transB, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc) -> None:
+    L = lib()
+    L.gb300_clear_error()
+    L.cblas_sgemm(order, transA, transB, m, n, k, alpha, _addr(A), lda, _addr(B), ldb, beta, _addr(C), ldc)
+    st, msg = last_error()
+    if st != OK:
+        raise Gb300Error(st, msg)
+
+
+def device_info() -> tuple[int, int, int]:
+    sms, fr, tot = ct.c_int(0), ct.c_int64(0), ct.c_int64(0)
+    check(lib().gb300_device_info(ct.byref(sms), ct.byref(fr), ct.byref(tot)))
+    return sms.value, fr.value, tot.value
+
+
+def measure_fp64_peak() -> float:
+    v = ct.c_double(0.0)
+    check(lib().gb300_measure_fp64_peak(ct.byref(v)))
+    return v.value
+
+
+def launch_count() -> int:
+    return int(lib().gb300_launch_count())
+
+
+def synchronize() -> None:
+    check(lib().gb300_synchronize())

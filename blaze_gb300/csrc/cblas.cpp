@@ -1,0 +1,141 @@
+// cblas.cpp — the CBLAS symbols Blaze's BLAS mode links against (include/gb300_cblas.h).
+//
+// Compiled twice: once with 32-bit integers (the standard names) and once with
+// -DGB300_BLAS_ILP64 (names with a _64 suffix), matching blaze/math/blas/Types.h:56-64.
+//
+// cblas_dgemm / cblas_sgemm run on the GPU (api.cpp).  The remaining routines exist so that every
+// function Blaze's wrappers name (the headers under blaze/math/blas/cblas/) resolves; they compute nothing and
+// record GB300_ERR_NOT_SUPPORTED, so a caller reaching them learns it at once instead of
+// receiving a silent CPU result.
+#include <string>
+
+#include "../../include/gb300_blas.h"
+#include "../../include/gb300_cblas.h"
+#include "gb300_internal.h"
+#include "runtime.h"
+
+namespace {
+void not_supported(const char* name) {
+    gb::set_error(GB300_ERR_NOT_SUPPORTED,
+                  std::string(name) + ": not provided by libgb300blas (only ?gemm runs on the GPU)");
+}
+}  // namespace
+
+extern "C" {
+
+void cblas_sgemm(CBLAS_ORDER order, CBLAS_TRANSPOSE transA, CBLAS_TRANSPOSE transB, gb300_blas_int m,
+                 gb300_blas_int n, gb300_blas_int k, float alpha, const float* A, gb300_blas_int lda, const float* B,
+                 gb300_blas_int ldb, float beta, float* C, gb300_blas_int ldc) {
+    gb::gemm_entry<float>(int(order), int(transA), int(transB), int64_t(m), int64_t(n), int64_t(k), alpha, A,
+                          int64_t(lda), B, int64_t(ldb), beta, C, int64_t(ldc), nullptr, "cblas_sgemm");
+}
+
+void cblas_dgemm(CBLAS_ORDER order, CBLAS_TRANSPOSE transA, CBLAS_TRANSPOSE transB, gb300_blas_int m,
+                 gb300_blas_int n, gb300_blas_int k, double alpha, const double* A, gb300_blas_int lda,
+                 const double* B, gb300_blas_int ldb, double beta, double* C, gb300_blas_int ldc) {
+    gb::gemm_entry<double>(int(order), int(transA), int(transB), int64_t(m), int64_t(n), int64_t(k), alpha, A,
+                           int64_t(lda), B, int64_t(ldb), beta, C, int64_t(ldc), nullptr, "cblas_dgemm");
+}
+
+// Aliases used by the throwing C++ wrappers of gb300_cblas.h (GB300_BLAS_THROW).
+__attribute__((visibility("default"))) void gb300_cblas_sgemm_checked(CBLAS_ORDER order, CBLAS_TRANSPOSE transA, CBLAS_TRANSPOSE transB, gb300_blas_int m,
+                               gb300_blas_int n, gb300_blas_int k, float alpha, const float* A, gb300_blas_int lda,
+                               const float* B, gb300_blas_int ldb, float beta, float* C, gb300_blas_int ldc) {
+    cblas_sgemm(order, transA, transB, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+}
+
+__attribute__((visibility("default"))) void gb300_cblas_dgemm_checked(CBLAS_ORDER order, CBLAS_TRANSPOSE transA, CBLAS_TRANSPOSE transB, gb300_blas_int m,
+                               gb300_blas_int n, gb300_blas_int k, double alpha, const double* A, gb300_blas_int lda,
+                               const double* B, gb300_blas_int ldb, double beta, double* C, gb300_blas_int ldc) {
+    cblas_dgemm(order, transA, transB, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+}
+
+// ---- stubs ------------------------------------------------------------------------------------
+void cblas_cgemm(CBLAS_ORDER, CBLAS_TRANSPOSE, CBLAS_TRANSPOSE, gb300_blas_int, gb300_blas_int, gb300_blas_int,
+                 const void*, const void*, gb300_blas_int, const void*, gb300_blas_int, const void*, void*,
+                 gb300_blas_int) { not_supported("cblas_cgemm"); }
+void cblas_zgemm(CBLAS_ORDER, CBLAS_TRANSPOSE, CBLAS_TRANSPOSE, gb300_blas_int, gb300_blas_int, gb300_blas_int,
+                 const void*, const void*, gb300_blas_int, const void*, gb300_blas_int, const void*, void*,
+                 gb300_blas_int) { not_supported("cblas_zgemm"); }
+void cblas_sgemv(CBLAS_ORDER, CBLAS_TRANSPOSE, gb300_blas_int, gb300_blas_int, float, const float*, gb300_blas_int,
+                 const float*, gb300_blas_int, float, float*, gb300_blas_int) { not_supported("cblas_sgemv"); }
+void cblas_dgemv(CBLAS_ORDER, CBLAS_TRANSPOSE, gb300_blas_int, gb300_blas_int, double, const double*, gb300_blas_int,
+                 const double*, gb300_blas_int, double, double*, gb300_blas_int) { not_supported("cblas_dgemv"); }
+void cblas_cgemv(CBLAS_ORDER, CBLAS_TRANSPOSE, gb300_blas_int, gb300_blas_int, const void*, const void*,
+                 gb300_blas_int, const void*, gb300_blas_int, const void*, void*, gb300_blas_int) {
+    not_supported("cblas_cgemv");
+}
+void cblas_zgemv(CBLAS_ORDER, CBLAS_TRANSPOSE, gb300_blas_int, gb300_blas_int, const void*, const void*,
+                 gb300_blas_int, const void*, gb300_blas_int, const void*, void*, gb300_blas_int) {
+    not_supported("cblas_zgemv");
+}
+void cblas_strmm(CBLAS_ORDER, CBLAS_SIDE, CBLAS_UPLO, CBLAS_TRANSPOSE, CBLAS_DIAG, gb300_blas_int, gb300_blas_int,
+                 float, const float*, gb300_blas_int, float*, gb300_blas_int) { not_supported("cblas_strmm"); }
+void cblas_dtrmm(CBLAS_ORDER, CBLAS_SIDE, CBLAS_UPLO, CBLAS_TRANSPOSE, CBLAS_DIAG, gb300_blas_int, gb300_blas_int,
+                 double, const double*, gb300_blas_int, double*, gb300_blas_int) { not_supported("cblas_dtrmm"); }
+void cblas_ctrmm(CBLAS_ORDER, CBLAS_SIDE, CBLAS_UPLO, CBLAS_TRANSPOSE, CBLAS_DIAG, gb300_blas_int, gb300_blas_int,
+                 const void*, const void*, gb300_blas_int, void*, gb300_blas_int) { not_supported("cblas_ctrmm"); }
+void cblas_ztrmm(CBLAS_ORDER, CBLAS_SIDE, CBLAS_UPLO, CBLAS_TRANSPOSE, CBLAS_DIAG, gb300_blas_int, gb300_blas_int,
+                 const void*, const void*, gb300_blas_int, void*, gb300_blas_int) { not_supported("cblas_ztrmm"); }
+void cblas_strmv(CBLAS_ORDER, CBLAS_UPLO, CBLAS_TRANSPOSE, CBLAS_DIAG, gb300_blas_int, const float*, gb300_blas_int,
+                 float*, gb300_blas_int) { not_supported("cblas_strmv"); }
+void cblas_dtrmv(CBLAS_ORDER, CBLAS_UPLO, CBLAS_TRANSPOSE, CBLAS_DIAG, gb300_blas_int, const double*, gb300_blas_int,
+                 double*, gb300_blas_int) { not_supported("cblas_dtrmv"); }
+void cblas_ctrmv(CBLAS_ORDER, CBLAS_UPLO, CBLAS_TRANSPOSE, CBLAS_DIAG, gb300_blas_int, const void*, gb300_blas_int,
+                 void*, gb300_blas_int) { not_supported("cblas_ctrmv"); }
+void cblas_ztrmv(CBLAS_ORDER, CBLAS_UPLO, CBLAS_TRANSPOSE, CBLAS_DIAG, gb300_blas_int, const void*, gb300_blas_int,
+                 void*, gb300_blas_int) { not_supported("cblas_ztrmv"); }
+void cblas_strsm(CBLAS_ORDER, CBLAS_SIDE, CBLAS_UPLO, CBLAS_TRANSPOSE, CBLAS_DIAG, gb300_blas_int, gb300_blas_int,
+                 float, const float*, gb300_blas_int, float*, gb300_blas_int) { not_supported("cblas_strsm"); }
+void cblas_dtrsm(CBLAS_ORDER, CBLAS_SIDE, CBLAS_UPLO, CBLAS_TRANSPOSE, CBLAS_DIAG, gb300_blas_int, gb300_blas_int,
+                 double, const double*, gb300_blas_int, double*, gb300_blas_int) { not_supported("cblas_dtrsm"); }
+void cblas_ctrsm(CBLAS_ORDER, CBLAS_SIDE, CBLAS_UPLO, CBLAS_TRANSPOSE, CBLAS_DIAG, gb300_blas_int, gb300_blas_int,
+                 const void*, const void*, gb300_blas_int, void*, gb300_blas_int) { not_supported("cblas_ctrsm"); }
+void cblas_ztrsm(CBLAS_ORDER, CBLAS_SIDE, CBLAS_UPLO, CBLAS_TRANSPOSE, CBLAS_DIAG, gb300_blas_int, gb300_blas_int,
+                 const void*, const void*, gb300_blas_int, void*, gb300_blas_int) { not_supported("cblas_ztrsm"); }
+void cblas_saxpy(gb300_blas_int, float, const float*, gb300_blas_int, float*, gb300_blas_int) {
+    not_supported("cblas_saxpy");
+}
+void cblas_daxpy(gb300_blas_int, double, const double*, gb300_blas_int, double*, gb300_blas_int) {
+    not_supported("cblas_daxpy");
+}
+void cblas_caxpy(gb300_blas_int, const void*, const void*, gb300_blas_int, void*, gb300_blas_int) {
+    not_supported("cblas_caxpy");
+}
+void cblas_zaxpy(gb300_blas_int, const void*, const void*, gb300_blas_int, void*, gb300_blas_int) {
+    not_supported("cblas_zaxpy");
+}
+float cblas_sdot(gb300_blas_int, const float*, gb300_blas_int, const float*, gb300_blas_int) {
+    not_supported("cblas_sdot");
+    return 0.0f;
+}
+double cblas_ddot(gb300_blas_int, const double*, gb300_blas_int, const double*, gb300_blas_int) {
+    not_supported("cblas_ddot");
+    return 0.0;
+}
+void cblas_cdotu_sub(gb300_blas_int, const void*, gb300_blas_int, const void*, gb300_blas_int, void*) {
+    not_supported("cblas_cdotu_sub");
+}
+void cblas_zdotu_sub(gb300_blas_int, const void*, gb300_blas_int, const void*, gb300_blas_int, void*) {
+    not_supported("cblas_zdotu_sub");
+}
+void cblas_cdotc_sub(gb300_blas_int, const void*, gb300_blas_int, const void*, gb300_blas_int, void*) {
+    not_supported("cblas_cdotc_sub");
+}
+void cblas_zdotc_sub(gb300_blas_int, const void*, gb300_blas_int, const void*, gb300_blas_int, void*) {
+    not_supported("cblas_zdotc_sub");
+}
+void cblas_cdotu(gb300_blas_int, const void*, gb300_blas_int, const void*, gb300_blas_int, void*) {
+    not_supported("cblas_cdotu");
+}
+void cblas_zdotu(gb300_blas_int, const void*, gb300_blas_int, const void*, gb300_blas_int, void*) {
+    not_supported("cblas_zdotu");
+}
+void cblas_cdotc(gb300_blas_int, const void*, gb300_blas_int, const void*, gb300_blas_int, void*) {
+    not_supported("cblas_cdotc");
+}
+void cblas_zdotc(gb300_blas_int, const void*, gb300_blas_int, const void*, gb300_blas_int, void*) {
+    not_supported("cblas_zdotc");
+}
+
+}  // extern "C"

@@ -1,0 +1,339 @@
+// native_gemm.cu — K1: native FP64 (DFMA) and FP32 (FFMA) GEMM for sm_103a.
+//
+// Replaces the CBLAS dgemm/sgemm that Blaze's BLAS path calls (blaze/math/blas/cblas/gemm.h:116-162,
+// reached from DMatDMatMultExpr.h:2021-2037 and its three storage-order siblings), i.e. the work
+// that Blaze's own large kernel `mmm` (blaze/math/dense/MMM.h:105-600) does on the CPU.
+//
+// Design (one CTA per 128x128 tile of C, 256 threads, 8x8 outputs per thread):
+//   * operand tiles are staged in shared memory by TMA (cp.async.bulk.tensor) as 128-byte
+//     swizzled boxes, a 4-deep mbarrier pipeline (one "full" barrier with transaction bytes and
+//     one "empty" barrier released by the eight warps per stage);
+//   * each k-panel is 128 bytes deep (16 doubles / 32 floats): a K-contiguous operand arrives as
+//     one 128-row box, an M- or N-contiguous operand as 128-byte-wide boxes of k-rows;
+//   * thread (tx,ty) owns rows ty+16r and columns tx+16c, so a warp's B reads are 16 consecutive
+//     elements (conflict-free) and its A reads are two broadcast addresses in different banks
+//     thanks to the swizzle;
+//   * out-of-range parts of edge tiles are zero-filled by TMA, so only the epilogue checks bounds;
+//   * optional split-k writes unscaled partial tiles to a workspace that a second kernel reduces
+//     in a fixed order (deterministic), then applies alpha and beta.
+// beta == 0 never reads C (CBLAS semantics; NaN in C does not propagate).
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <string>
+
+#include "gb300_internal.h"
+#include "ptx.cuh"
+#include "runtime.h"
+
+namespace gb {
+namespace {
+
+constexpr int BM = kNativeTileM;
+constexpr int BN = kNativeTileN;
+constexpr int STAGES = 4;
+constexpr int THREADS = 256;
+constexpr int PANEL_BYTES = 128;                         // k-panel depth in bytes
+constexpr int TILE_BYTES = BM * PANEL_BYTES;             // 16 KB per operand per stage
+
+template <typename T>
+struct NativeParams {
+    int64_t m, n, k;
+    int64_t k_per_split;     // multiple of the panel depth
+    T alpha, beta;
+    T* C;
+    int64_t ldc;
+    T* ws;                   // split-k partials (splits x m x n) or nullptr
+    int* status;
+    uint64_t limit_ns;
+    int inject_stall;
+};
+
+struct __align__(8) NativeBarriers {
+    uint64_t full[STAGES];
+    uint64_t empty[STAGES];
+};
+
+// Shared-memory byte offset of A(m, kk) / B(kk, n) inside one stage's operand tile.
+template <typename T, bool TRANS_A>
+__device__ __forceinline__ uint32_t a_off(int m, int kk) {
+    constexpr int BK = PANEL_BYTES / sizeof(T);
+    constexpr int E = PANEL_BYTES / sizeof(T);            // elements per 128-byte row
+    if (!TRANS_A) return swz128(uint32_t(m * PANEL_BYTES + kk * sizeof(T)));
+    return uint32_t((m / E) * BK * PANEL_BYTES) + swz128(uint32_t(kk * PANEL_BYTES + (m % E) * sizeof(T)));
+}
+
+template <typename T, bool TRANS_B>
+__device__ __forceinline__ uint32_t b_off(int kk, int n) {
+    constexpr int BK = PANEL_BYTES / sizeof(T);
+    constexpr int E = PANEL_BYTES / sizeof(T);
+    if (TRANS_B) return swz128(uint32_t(n * PANEL_BYTES + kk * sizeof(T)));
+    return uint32_t((n / E) * BK * PANEL_BYTES) + swz128(uint32_t(kk * PANEL_BYTES + (n % E) * sizeof(T)));
+}
+
+template <typename T, bool TRANS_A, bool TRANS_B>
+__global__ void __launch_bounds__(THREADS, 1)
+native_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                   const NativeParams<T> p) {
+    constexpr int BK = PANEL_BYTES / sizeof(T);
+    constexpr int E = PANEL_BYTES / sizeof(T);
+    extern __shared__ __align__(1024) uint8_t smem_raw[];
+    // 1024-byte alignment for the swizzle atoms
+    uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    uint8_t* tilesA = smem;
+    uint8_t* tilesB = smem + STAGES * TILE_BYTES;
+    NativeBarriers* bars = reinterpret_cast<NativeBarriers*>(smem + 2 * STAGES * TILE_BYTES);
+
+    const int tid = threadIdx.x;
+    const int lane = tid & 31;
+    const int tx = tid & 15, ty = tid >> 4;
+    const int64_t m0 = int64_t(blockIdx.y) * BM;
+    const int64_t n0 = int64_t(blockIdx.x) * BN;
+    const int64_t kbeg = int64_t(blockIdx.z) * p.k_per_split;
+    const int64_t kend = min(p.k, kbeg + p.k_per_split);
+    const int KT = kend > kbeg ? int((kend - kbeg + BK - 1) / BK) : 0;
+
+    if (tid == 0) {
+        tma_prefetch_desc(&tmA);
+        tma_prefetch_desc(&tmB);
+        for (int s = 0; s < STAGES; ++s) {
+            mbar_init(smem_u32(&bars->full[s]), 1);
+            mbar_init(smem_u32(&bars->empty[s]), THREADS / 32);
+        }
+        fence_mbar_init();
+    }
+    __syncthreads();
+
+    auto issue = [&](int t, int s) {
+        const uint32_t full = smem_u32(&bars->full[s]);
+        mbar_arrive_expect_tx(full, 2 * TILE_BYTES);
+        const int32_t kx = int32_t(kbeg + int64_t(t) * BK);
+        const uint32_t dA = smem_u32(tilesA + s * TILE_BYTES);
+        const uint32_t dB = smem_u32(tilesB + s * TILE_BYTES);
+        if (!TRANS_A) {
+            tma_load_2d(dA, &tmA, kx, int32_t(m0), full);
+        } else {
+#pragma unroll
+            for (int b = 0; b < BM / E; ++b)
+                tma_load_2d(dA + b * BK * PANEL_BYTES, &tmA, int32_t(m0 + b * E), kx, full);
+        }
+        if (TRANS_B) {
+            tma_load_2d(dB, &tmB, kx, int32_t(n0), full);
+        } else {
+#pragma unroll
+            for (int b = 0; b < BN / E; ++b)
+                tma_load_2d(dB + b * BK * PANEL_BYTES, &tmB, int32_t(n0 + b * E), kx, full);
+        }
+    };
+
+    int issued = 0;
+    if (tid == 0 && !p.inject_stall) {
+        for (; issued < min(STAGES, KT); ++issued) issue(issued, issued);
+    }
+
+    T acc[8][8];
+#pragma unroll
+    for (int r = 0; r < 8; ++r)
+#pragma unroll
+        for (int c = 0; c < 8; ++c) acc[r][c] = T(0);
+
+    bool ok = true;
+    int kt = 0;
+    for (; kt < KT; ++kt) {
+        const int s = kt % STAGES;
+        const uint32_t ph = (kt / STAGES) & 1;
+        if (!mbar_wait(smem_u32(&bars->full[s]), ph, p.status, kDevTimeoutFull, p.limit_ns)) {
+            ok = false;
+            break;
+        }
+        const uint8_t* As = tilesA + s * TILE_BYTES;
+        const uint8_t* Bs = tilesB + s * TILE_BYTES;
+#pragma unroll 4
+        for (int kk = 0; kk < BK; ++kk) {
+            T a[8], b[8];
+#pragma unroll
+            for (int r = 0; r < 8; ++r) a[r] = *reinterpret_cast<const T*>(As + a_off<T, TRANS_A>(ty + 16 * r, kk));
+#pragma unroll
+            for (int c = 0; c < 8; ++c) b[c] = *reinterpret_cast<const T*>(Bs + b_off<T, TRANS_B>(kk, tx + 16 * c));
+#pragma unroll
+            for (int r = 0; r < 8; ++r)
+#pragma unroll
+                for (int c = 0; c < 8; ++c) acc[r][c] = fma(a[r], b[c], acc[r][c]);
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(smem_u32(&bars->empty[s]));
+        if (tid == 0 && issued < KT) {
+            // the stage is refilled once all eight warps have released it
+            if (!mbar_wait(smem_u32(&bars->empty[s]), ph, p.status, kDevTimeoutEmpty, p.limit_ns)) {
+                ok = false;
+                ++kt;
+                break;
+            }
+            issue(issued, s);
+            ++issued;
+        }
+    }
+
+    if (!ok) {
+        // drain the copies this CTA issued but did not consume, with the same bounded wait
+        if (tid == 0) {
+            for (int t = kt; t < issued; ++t)
+                mbar_wait_drain(smem_u32(&bars->full[t % STAGES]), (t / STAGES) & 1, p.limit_ns);
+        }
+        return;
+    }
+
+    // epilogue
+    if (p.ws != nullptr) {
+        T* w = p.ws + int64_t(blockIdx.z) * p.m * p.n;
+#pragma unroll
+        for (int r = 0; r < 8; ++r) {
+            const int64_t i = m0 + ty + 16 * r;
+            if (i >= p.m) continue;
+#pragma unroll
+            for (int c = 0; c < 8; ++c) {
+                const int64_t j = n0 + tx + 16 * c;
+                if (j < p.n) w[i * p.n + j] = acc[r][c];
+            }
+        }
+        return;
+    }
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+        const int64_t i = m0 + ty + 16 * r;
+        if (i >= p.m) continue;
+        T* crow = p.C + i * p.ldc;
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+            const int64_t j = n0 + tx + 16 * c;
+            if (j >= p.n) continue;
+            const T v = p.alpha * acc[r][c];
+            crow[j] = (p.beta == T(0)) ? v : fma(p.beta, crow[j], v);
+        }
+    }
+}
+
+// Fixed-order reduction of split-k partials: C = alpha * sum_z W[z] + beta * C.
+template <typename T>
+__global__ void splitk_reduce_kernel(const T* __restrict__ ws, int splits, int64_t m, int64_t n, T alpha,
+                                     T beta, T* __restrict__ C, int64_t ldc) {
+    const int64_t total = m * n;
+    for (int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; e < total;
+         e += int64_t(gridDim.x) * blockDim.x) {
+        T s = ws[e];
+        for (int z = 1; z < splits; ++z) s += ws[int64_t(z) * total + e];
+        const int64_t i = e / n, j = e % n;
+        T* c = C + i * ldc + j;
+        const T v = alpha * s;
+        *c = (beta == T(0)) ? v : fma(beta, *c, v);
+    }
+}
+
+// C = beta * C (k == 0); beta == 0 writes zeros without reading C.
+template <typename T>
+__global__ void scale_c_kernel(int64_t m, int64_t n, T beta, T* __restrict__ C, int64_t ldc) {
+    const int64_t total = m * n;
+    for (int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; e < total;
+         e += int64_t(gridDim.x) * blockDim.x) {
+        const int64_t i = e / n, j = e % n;
+        T* c = C + i * ldc + j;
+        *c = (beta == T(0)) ? T(0) : beta * *c;
+    }
+}
+
+template <typename T>
+constexpr CUtensorMapDataType tmap_type() {
+    return sizeof(T) == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+}
+
+constexpr size_t kSmemBytes = 2 * STAGES * TILE_BYTES + sizeof(NativeBarriers) + 1024;
+
+template <typename T, bool TA, bool TB>
+cudaError_t launch_variant(const CUtensorMap& a, const CUtensorMap& b, const NativeParams<T>& p, dim3 grid,
+                           cudaStream_t s) {
+    auto kern = native_gemm_kernel<T, TA, TB>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kSmemBytes));
+    if (e != cudaSuccess) return e;
+    kern<<<grid, THREADS, kSmemBytes, s>>>(a, b, p);
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+int native_choose_splits(int64_t m, int64_t n, int64_t k, int elem_bytes, int num_sms) {
+    const int64_t bk = PANEL_BYTES / elem_bytes;
+    const int64_t tiles = ((m + BM - 1) / BM) * ((n + BN - 1) / BN);
+    if (tiles >= num_sms || k < 4 * bk) return 1;
+    // enough splits to cover every SM once, each at least four panels deep
+    int64_t splits = (num_sms + tiles - 1) / tiles;
+    splits = std::min<int64_t>(splits, k / (4 * bk));
+    return int(std::max<int64_t>(splits, 1));
+}
+
+template <typename T>
+cudaError_t native_gemm(const Gemm& g, int splits, T* workspace, const LaunchCtl& ctl, cudaStream_t s,
+                        std::string* err) {
+    if (g.m <= 0 || g.n <= 0) return cudaSuccess;
+    const int64_t BK = PANEL_BYTES / sizeof(T);
+    const int E = PANEL_BYTES / sizeof(T);
+    if (g.k == 0) {
+        const int64_t total = g.m * g.n;
+        const int blocks = int(std::min<int64_t>((total + 255) / 256, 4096));
+        scale_c_kernel<T><<<blocks, 256, 0, s>>>(g.m, g.n, T(g.beta), static_cast<T*>(g.C), g.ldc);
+        count_launches(1);
+        return cudaGetLastError();
+    }
+    CUtensorMap ta, tb;
+    const CUtensorMapDataType dt = tmap_type<T>();
+    // A: rows x cols as stored (row-major storage, ld = lda)
+    bool ok;
+    if (!g.ta)
+        ok = encode_tmap_2d(&ta, dt, sizeof(T), g.A, g.m, g.k, g.lda, BM, BK, CU_TENSOR_MAP_SWIZZLE_128B, err);
+    else
+        ok = encode_tmap_2d(&ta, dt, sizeof(T), g.A, g.k, g.m, g.lda, BK, E, CU_TENSOR_MAP_SWIZZLE_128B, err);
+    if (!ok) return cudaErrorInvalidValue;
+    if (g.tb)
+        ok = encode_tmap_2d(&tb, dt, sizeof(T), g.B, g.n, g.k, g.ldb, BN, BK, CU_TENSOR_MAP_SWIZZLE_128B, err);
+    else
+        ok = encode_tmap_2d(&tb, dt, sizeof(T), g.B, g.k, g.n, g.ldb, BK, E, CU_TENSOR_MAP_SWIZZLE_128B, err);
+    if (!ok) return cudaErrorInvalidValue;
+
+    splits = std::max(1, splits);
+    int64_t kps = (g.k + splits - 1) / splits;
+    kps = (kps + BK - 1) / BK * BK;
+    splits = int((g.k + kps - 1) / kps);
+
+    NativeParams<T> p;
+    p.m = g.m; p.n = g.n; p.k = g.k;
+    p.k_per_split = kps;
+    p.alpha = T(g.alpha); p.beta = T(g.beta);
+    p.C = static_cast<T*>(g.C); p.ldc = g.ldc;
+    p.ws = splits > 1 ? workspace : nullptr;
+    p.status = ctl.status;
+    p.limit_ns = ctl.wait_limit_ns;
+    p.inject_stall = ctl.inject_stall;
+    if (splits > 1 && workspace == nullptr) {
+        if (err) *err = "split-k needs a workspace";
+        return cudaErrorInvalidValue;
+    }
+    dim3 grid(unsigned((g.n + BN - 1) / BN), unsigned((g.m + BM - 1) / BM), unsigned(splits));
+    cudaError_t e;
+    if (!g.ta && !g.tb) e = launch_variant<T, false, false>(ta, tb, p, grid, s);
+    else if (!g.ta && g.tb) e = launch_variant<T, false, true>(ta, tb, p, grid, s);
+    else if (g.ta && !g.tb) e = launch_variant<T, true, false>(ta, tb, p, grid, s);
+    else e = launch_variant<T, true, true>(ta, tb, p, grid, s);
+    if (e != cudaSuccess || splits == 1) return e;
+    const int64_t total = g.m * g.n;
+    const int blocks = int(std::min<int64_t>((total + 255) / 256, 152 * 16));
+    splitk_reduce_kernel<T><<<blocks, 256, 0, s>>>(workspace, splits, g.m, g.n, T(g.alpha), T(g.beta),
+                                                   static_cast<T*>(g.C), g.ldc);
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+template cudaError_t native_gemm<double>(const Gemm&, int, double*, const LaunchCtl&, cudaStream_t, std::string*);
+template cudaError_t native_gemm<float>(const Gemm&, int, float*, const LaunchCtl&, cudaStream_t, std::string*);
+
+}  // namespace gb

@@ -1,0 +1,62 @@
+// runtime.h — process-wide state of libgb300blas: the device, the library stream, grow-only
+// device buffers, the device status word, the thread-local last error and launch accounting.
+#pragma once
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstdint>
+#include <mutex>
+#include <string>
+
+namespace gb {
+
+// Buffer slots of the grow-only device pool.  A slot keeps its high-water allocation for the
+// life of the process, so repeated calls of similar size allocate nothing.
+enum Slot : int {
+    kSlotA = 0,        // staged / realigned A
+    kSlotB,            // staged / realigned B
+    kSlotC,            // staged / realigned C
+    kSlotWork,         // split-k partials
+    kSlotSliceA,       // split-precision digit planes of A
+    kSlotSliceB,       // split-precision digit planes of B
+    kSlotScaleA,       // per-row exponents of A
+    kSlotScaleB,       // per-column exponents of B
+    kSlotLevels,       // split-precision per-level integer sums
+    kSlotMisc,         // small reductions (norms, bounds)
+    kSlotCount
+};
+
+struct Runtime {
+    std::mutex mu;                 // one queue: GPU work submitted through the library is serialized
+    bool inited = false;
+    int device = -1;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    int* d_status = nullptr;       // device status word written by kernels (DeviceStatus)
+    void* pool[kSlotCount] = {};
+    size_t pool_bytes[kSlotCount] = {};
+    std::atomic<int64_t> launches{0};
+    int inject_stall_count = 0;
+    uint64_t inject_limit_ns = 0;
+};
+
+Runtime& runtime();
+
+// Initialise the device state once (thread-safe).  Returns a gb300_status.
+int ensure_init(std::string* err);
+
+// Device buffer of at least `bytes` in slot `s` (caller holds runtime().mu).  nullptr on failure.
+void* pool_get(int s, size_t bytes, std::string* err);
+
+// Thread-local last error.
+void set_error(int status, const std::string& msg);
+void clear_error();
+int last_error();
+const char* last_error_message();
+
+// Count kernel launches issued by the library.
+inline void count_launches(int n) { runtime().launches.fetch_add(n, std::memory_order_relaxed); }
+
+}  // namespace gb

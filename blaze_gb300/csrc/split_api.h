@@ -1,0 +1,29 @@
+// split_api.h — host interface of the tensor-core forms (split-precision, BF16x3, BF16).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+
+#include "gb300_internal.h"
+
+namespace gb {
+
+struct SplitRequest {
+    int method = 0;            // gb300_method (AUTO, SPLIT, BF16X3 or BF16)
+    int slices = 0;            // slices per operand; 0 = choose from target_error
+    double target_error = 0;   // normwise target; <= 0 means k * 2^-53
+};
+
+struct SplitResult {
+    int method_used = 0;
+    int slices = 0;
+    double error_bound = 0;
+};
+
+// Runs the double-precision product g with one of the tensor-core forms (or, for AUTO, picks
+// between the split form and the native kernel).  Returns a gb300_status.
+int split_gemm(const Gemm& g, const SplitRequest& req, const LaunchCtl& ctl, cudaStream_t s, SplitResult* out,
+               std::string* err);
+
+}  // namespace gb

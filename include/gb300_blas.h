@@ -1,0 +1,112 @@
+/*
+ * gb300_blas.h — extended C-ABI of libgb300blas (GB300 / sm_103a dense matrix multiplication).
+ *
+ * The drop-in CBLAS surface is include/gb300_cblas.h.  This header adds what CBLAS cannot say:
+ * the choice between the native FP64 kernel and the split-precision tensor-core forms, device-
+ * resident operands and streams, and status reporting.  All signatures use plain pointers,
+ * sizes and enums; no CUDA or C++ types appear.
+ */
+#ifndef GB300_BLAS_H
+#define GB300_BLAS_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+#if defined(__GNUC__)
+#pragma GCC visibility push(default)
+#endif
+
+/* Status codes (returned by the *_ex functions and recorded for the CBLAS entry points). */
+enum gb300_status {
+    GB300_OK = 0,
+    GB300_ERR_INVALID_ARG = 1,     /* an argument violates the CBLAS contract (see message) */
+    GB300_ERR_CUDA = 2,            /* a CUDA runtime call failed */
+    GB300_ERR_NO_MEMORY = 3,       /* device or pinned-host allocation failed */
+    GB300_ERR_DEVICE_TIMEOUT = 4,  /* a kernel's bounded wait ran out; the launch was abandoned */
+    GB300_ERR_NOT_SUPPORTED = 5,   /* routine declared for Blaze but not provided on the GPU */
+    GB300_ERR_NO_DEVICE = 6,       /* no CUDA device is visible */
+    GB300_ERR_ADMISSION = 7        /* a request exceeds the server's memory budget */
+};
+
+/* Arithmetic forms of the product. */
+enum gb300_method {
+    GB300_METHOD_AUTO = 0,    /* FP64-accurate: split-precision where it is faster, else native */
+    GB300_METHOD_NATIVE = 1,  /* native FP64 DFMA (FP32 FFMA for sgemm) */
+    GB300_METHOD_SPLIT = 2,   /* Ozaki-style BF16 slices on tcgen05, FP64 recombination (double only) */
+    GB300_METHOD_BF16X3 = 3,  /* three BF16 products (hi*hi + hi*lo + lo*hi), FP32 accumulation */
+    GB300_METHOD_BF16 = 4     /* one BF16 product, FP32 accumulation */
+};
+
+/* Where the operand pointers live. */
+enum gb300_residency {
+    GB300_PTR_DETECT = 0,     /* ask the CUDA driver (cudaPointerGetAttributes) */
+    GB300_PTR_DEVICE = 1,     /* device or managed memory: used in place, no copies */
+    GB300_PTR_HOST = 2        /* host memory: staged to the device and back inside the call */
+};
+
+typedef struct gb300_gemm_opts {
+    int method;            /* gb300_method */
+    int slices;            /* GB300_METHOD_SPLIT: slices per operand (0 = choose from target) */
+    double target_error;   /* GB300_METHOD_SPLIT: normwise bound to reach; <= 0 means k * 2^-53 */
+    int residency;         /* gb300_residency */
+    void* stream;          /* cudaStream_t to run on; NULL = the library's stream */
+    int synchronous;       /* non-zero: return after the result is in C */
+    /* outputs */
+    int method_used;       /* the form that ran */
+    int slices_used;       /* GB300_METHOD_SPLIT: slices per operand */
+    double error_bound;    /* a-priori normwise bound ||C-AB||_F/(||A||_F||B||_F) of the form
+                              that ran (split: computed from the operands' exponents; other forms:
+                              the textbook bound of their arithmetic) */
+} gb300_gemm_opts;
+
+/* Fill `opts` with defaults: method from the library default, target k*2^-53, detect residency,
+ * library stream, synchronous. */
+void gb300_gemm_opts_init(gb300_gemm_opts* opts);
+
+/* C = alpha*op(A)*op(B) + beta*C with CBLAS argument conventions and 64-bit sizes.
+ * Returns a gb300_status (also recorded as the thread's last error). */
+int gb300_dgemm_ex(int order, int transA, int transB, int64_t m, int64_t n, int64_t k, double alpha,
+                   const double* A, int64_t lda, const double* B, int64_t ldb, double beta, double* C,
+                   int64_t ldc, gb300_gemm_opts* opts);
+int gb300_sgemm_ex(int order, int transA, int transB, int64_t m, int64_t n, int64_t k, float alpha,
+                   const float* A, int64_t lda, const float* B, int64_t ldb, float beta, float* C,
+                   int64_t ldc, gb300_gemm_opts* opts);
+
+/* Default method used by cblas_dgemm (initially GB300_METHOD_AUTO, or the GB300_DGEMM_METHOD
+ * environment variable: auto|native|split|bf16x3|bf16).  Returns the previous value. */
+int gb300_set_default_method(int method);
+
+/* Last status of the calling thread (also declared in gb300_cblas.h). */
+int gb300_last_error(void);
+const char* gb300_last_error_message(void);
+void gb300_clear_error(void);
+
+/* Device facts the library uses: SM count, free and total device memory in bytes.
+ * Returns GB300_ERR_NO_DEVICE when no GPU is visible. */
+int gb300_device_info(int* num_sms, int64_t* free_bytes, int64_t* total_bytes);
+
+/* Measure the device's sustained FP64 FMA rate (TFLOP/s) with independent DFMA chains on every
+ * SM.  The automatic method choice uses it; benchmarks report it as the FP64 roofline. */
+int gb300_measure_fp64_peak(double* tflops);
+
+/* Count of kernel launches the library has issued in this process (all entry points). */
+int64_t gb300_launch_count(void);
+
+/* Wait until all work the library queued on its own stream has finished. */
+int gb300_synchronize(void);
+
+/* Test hooks for failure detection (no fault is involved): the next `count` native-kernel
+ * launches run with their TMA producer disabled and their waits limited to `limit_ns`, so they
+ * end with GB300_ERR_DEVICE_TIMEOUT.  count = 0 clears the hook. */
+void gb300_debug_inject_stall(int count, uint64_t limit_ns);
+
+#if defined(__GNUC__)
+#pragma GCC visibility pop
+#endif
+#ifdef __cplusplus
+} /* extern "C" */
+#endif
+
+#endif /* GB300_BLAS_H */

@@ -1,0 +1,255 @@
+/*
+ * gb300_cblas.h — drop-in CBLAS header for Blaze's BLAS mode, backed by GB300 (sm_103a) kernels.
+ *
+ * Use with Blaze:
+ *     g++ ... -DBLAZE_BLAS_MODE=1 -DBLAZE_BLAS_IS_PARALLEL=1 \
+ *             -DBLAZE_BLAS_INCLUDE_FILE="<gb300_cblas.h>" -I<this dir> ... -lgb300blas
+ * Blaze includes this file inside `extern "C" { ... }` (blaze/system/BLAS.h:57-58) and its inline
+ * wrappers in blaze/math/blas/cblas/ headers call the cblas_* functions declared here.
+ *
+ * Implemented on the GPU: cblas_dgemm and cblas_sgemm (the dense matrix-multiplication path,
+ * reached from blaze::gemm(), blaze/math/blas/gemm.h:105-131, and blaze/math/blas/cblas/gemm.h:
+ * 116-162).  Every other routine that Blaze's wrappers name is declared so that Blaze compiles;
+ * the library defines them as stubs that record GB300_ERR_NOT_SUPPORTED (see gb300_last_error())
+ * and compute nothing — there is no CPU fallback.
+ *
+ * Integer type: `blas_int_t` is int32 unless BLAZE_BLAS_IS_64BIT is set, matching
+ * blaze/math/blas/Types.h:56-64.  The library exports the 32-bit ABI under the standard names;
+ * the 64-bit (ILP64) variants are exported as cblas_*_64 and selected here when
+ * BLAZE_BLAS_IS_64BIT (or GB300_BLAS_ILP64) is defined.
+ *
+ * Errors: CBLAS routines return void.  Invalid arguments and device failures are recorded in a
+ * thread-local status readable with gb300_last_error() / gb300_last_error_message().
+ * Defining GB300_BLAS_THROW before inclusion in C++ wraps cblas_dgemm / cblas_sgemm so that a
+ * non-zero status throws std::runtime_error right after the call (the behaviour of Blaze's own
+ * BLAZE_THROW_RUNTIME_ERROR, blaze/util/Exception.h).
+ */
+#ifndef GB300_CBLAS_H
+#define GB300_CBLAS_H
+
+#include <stdint.h>
+
+/* Standard CBLAS enumerations (values are the CBLAS ABI). */
+#ifndef CBLAS_ENUM_DEFINED_H
+#define CBLAS_ENUM_DEFINED_H
+typedef enum CBLAS_ORDER { CblasRowMajor = 101, CblasColMajor = 102 } CBLAS_ORDER;
+typedef enum CBLAS_TRANSPOSE { CblasNoTrans = 111, CblasTrans = 112, CblasConjTrans = 113 } CBLAS_TRANSPOSE;
+typedef enum CBLAS_UPLO { CblasUpper = 121, CblasLower = 122 } CBLAS_UPLO;
+typedef enum CBLAS_DIAG { CblasNonUnit = 131, CblasUnit = 132 } CBLAS_DIAG;
+typedef enum CBLAS_SIDE { CblasLeft = 141, CblasRight = 142 } CBLAS_SIDE;
+typedef CBLAS_ORDER CBLAS_LAYOUT;
+#endif
+
+#if defined(BLAZE_BLAS_IS_64BIT) && BLAZE_BLAS_IS_64BIT
+#define GB300_BLAS_ILP64 1
+#endif
+
+#ifdef GB300_BLAS_ILP64
+typedef int64_t gb300_blas_int;
+#define GB300_CBLAS_NAME(x) x##_64
+#else
+typedef int32_t gb300_blas_int;
+#define GB300_CBLAS_NAME(x) x
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+#if defined(__GNUC__)
+#pragma GCC visibility push(default)
+#endif
+
+/* ---- status of the calling thread's last call --------------------------------------------- */
+int gb300_last_error(void);
+const char* gb300_last_error_message(void);
+void gb300_clear_error(void);
+
+#if defined(GB300_BLAS_ILP64)
+#define cblas_sgemm cblas_sgemm_64
+#define cblas_dgemm cblas_dgemm_64
+#define cblas_cgemm cblas_cgemm_64
+#define cblas_zgemm cblas_zgemm_64
+#define cblas_sgemv cblas_sgemv_64
+#define cblas_dgemv cblas_dgemv_64
+#define cblas_cgemv cblas_cgemv_64
+#define cblas_zgemv cblas_zgemv_64
+#define cblas_strmm cblas_strmm_64
+#define cblas_dtrmm cblas_dtrmm_64
+#define cblas_ctrmm cblas_ctrmm_64
+#define cblas_ztrmm cblas_ztrmm_64
+#define cblas_strmv cblas_strmv_64
+#define cblas_dtrmv cblas_dtrmv_64
+#define cblas_ctrmv cblas_ctrmv_64
+#define cblas_ztrmv cblas_ztrmv_64
+#define cblas_strsm cblas_strsm_64
+#define cblas_dtrsm cblas_dtrsm_64
+#define cblas_ctrsm cblas_ctrsm_64
+#define cblas_ztrsm cblas_ztrsm_64
+#define cblas_saxpy cblas_saxpy_64
+#define cblas_daxpy cblas_daxpy_64
+#define cblas_caxpy cblas_caxpy_64
+#define cblas_zaxpy cblas_zaxpy_64
+#define cblas_sdot cblas_sdot_64
+#define cblas_ddot cblas_ddot_64
+#define cblas_cdotu cblas_cdotu_64
+#define cblas_zdotu cblas_zdotu_64
+#define cblas_cdotc cblas_cdotc_64
+#define cblas_zdotc cblas_zdotc_64
+#define cblas_cdotu_sub cblas_cdotu_sub_64
+#define cblas_zdotu_sub cblas_zdotu_sub_64
+#define cblas_cdotc_sub cblas_cdotc_sub_64
+#define cblas_zdotc_sub cblas_zdotc_sub_64
+#define gb300_cblas_sgemm_checked gb300_cblas_sgemm_checked_64
+#define gb300_cblas_dgemm_checked gb300_cblas_dgemm_checked_64
+#endif
+
+/* ---- GEMM: implemented on the GPU ---------------------------------------------------------- */
+/* C = alpha*op(A)*op(B) + beta*C.  Replaces the cblas_sgemm call of
+ * blaze/math/blas/cblas/gemm.h:121 (float). */
+#if defined(__cplusplus) && defined(GB300_BLAS_THROW)
+void gb300_cblas_sgemm_checked(CBLAS_ORDER order, CBLAS_TRANSPOSE transA, CBLAS_TRANSPOSE transB,
+#else
+void cblas_sgemm(CBLAS_ORDER order, CBLAS_TRANSPOSE transA, CBLAS_TRANSPOSE transB,
+#endif
+                 gb300_blas_int m, gb300_blas_int n, gb300_blas_int k, float alpha, const float* A,
+                 gb300_blas_int lda, const float* B, gb300_blas_int ldb, float beta, float* C,
+                 gb300_blas_int ldc);
+
+/* C = alpha*op(A)*op(B) + beta*C.  Replaces the cblas_dgemm call of
+ * blaze/math/blas/cblas/gemm.h:161 (double). */
+#if defined(__cplusplus) && defined(GB300_BLAS_THROW)
+void gb300_cblas_dgemm_checked(CBLAS_ORDER order, CBLAS_TRANSPOSE transA, CBLAS_TRANSPOSE transB,
+#else
+void cblas_dgemm(CBLAS_ORDER order, CBLAS_TRANSPOSE transA, CBLAS_TRANSPOSE transB,
+#endif
+                 gb300_blas_int m, gb300_blas_int n, gb300_blas_int k, double alpha, const double* A,
+                 gb300_blas_int lda, const double* B, gb300_blas_int ldb, double beta, double* C,
+                 gb300_blas_int ldc);
+
+/* ---- declared for Blaze's other wrappers; stubs (GB300_ERR_NOT_SUPPORTED) ------------------ */
+/* blaze/math/blas/cblas/gemm.h:201,243 */
+void cblas_cgemm(CBLAS_ORDER order, CBLAS_TRANSPOSE transA, CBLAS_TRANSPOSE transB, gb300_blas_int m,
+                 gb300_blas_int n, gb300_blas_int k, const void* alpha, const void* A, gb300_blas_int lda,
+                 const void* B, gb300_blas_int ldb, const void* beta, void* C, gb300_blas_int ldc);
+void cblas_zgemm(CBLAS_ORDER order, CBLAS_TRANSPOSE transA, CBLAS_TRANSPOSE transB, gb300_blas_int m,
+                 gb300_blas_int n, gb300_blas_int k, const void* alpha, const void* A, gb300_blas_int lda,
+                 const void* B, gb300_blas_int ldb, const void* beta, void* C, gb300_blas_int ldc);
+/* blaze/math/blas/cblas/gemv.h:116,153,193,235 */
+void cblas_sgemv(CBLAS_ORDER order, CBLAS_TRANSPOSE transA, gb300_blas_int m, gb300_blas_int n, float alpha,
+                 const float* A, gb300_blas_int lda, const float* x, gb300_blas_int incX, float beta, float* y,
+                 gb300_blas_int incY);
+void cblas_dgemv(CBLAS_ORDER order, CBLAS_TRANSPOSE transA, gb300_blas_int m, gb300_blas_int n, double alpha,
+                 const double* A, gb300_blas_int lda, const double* x, gb300_blas_int incX, double beta,
+                 double* y, gb300_blas_int incY);
+void cblas_cgemv(CBLAS_ORDER order, CBLAS_TRANSPOSE transA, gb300_blas_int m, gb300_blas_int n,
+                 const void* alpha, const void* A, gb300_blas_int lda, const void* x, gb300_blas_int incX,
+                 const void* beta, void* y, gb300_blas_int incY);
+void cblas_zgemv(CBLAS_ORDER order, CBLAS_TRANSPOSE transA, gb300_blas_int m, gb300_blas_int n,
+                 const void* alpha, const void* A, gb300_blas_int lda, const void* x, gb300_blas_int incX,
+                 const void* beta, void* y, gb300_blas_int incY);
+/* blaze/math/blas/cblas/trmm.h:116,153,... */
+void cblas_strmm(CBLAS_ORDER order, CBLAS_SIDE side, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA, CBLAS_DIAG diag,
+                 gb300_blas_int m, gb300_blas_int n, float alpha, const float* A, gb300_blas_int lda, float* B,
+                 gb300_blas_int ldb);
+void cblas_dtrmm(CBLAS_ORDER order, CBLAS_SIDE side, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA, CBLAS_DIAG diag,
+                 gb300_blas_int m, gb300_blas_int n, double alpha, const double* A, gb300_blas_int lda,
+                 double* B, gb300_blas_int ldb);
+void cblas_ctrmm(CBLAS_ORDER order, CBLAS_SIDE side, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA, CBLAS_DIAG diag,
+                 gb300_blas_int m, gb300_blas_int n, const void* alpha, const void* A, gb300_blas_int lda,
+                 void* B, gb300_blas_int ldb);
+void cblas_ztrmm(CBLAS_ORDER order, CBLAS_SIDE side, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA, CBLAS_DIAG diag,
+                 gb300_blas_int m, gb300_blas_int n, const void* alpha, const void* A, gb300_blas_int lda,
+                 void* B, gb300_blas_int ldb);
+/* blaze/math/blas/cblas/trmv.h */
+void cblas_strmv(CBLAS_ORDER order, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA, CBLAS_DIAG diag, gb300_blas_int n,
+                 const float* A, gb300_blas_int lda, float* x, gb300_blas_int incX);
+void cblas_dtrmv(CBLAS_ORDER order, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA, CBLAS_DIAG diag, gb300_blas_int n,
+                 const double* A, gb300_blas_int lda, double* x, gb300_blas_int incX);
+void cblas_ctrmv(CBLAS_ORDER order, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA, CBLAS_DIAG diag, gb300_blas_int n,
+                 const void* A, gb300_blas_int lda, void* x, gb300_blas_int incX);
+void cblas_ztrmv(CBLAS_ORDER order, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA, CBLAS_DIAG diag, gb300_blas_int n,
+                 const void* A, gb300_blas_int lda, void* x, gb300_blas_int incX);
+/* blaze/math/blas/cblas/trsm.h */
+void cblas_strsm(CBLAS_ORDER order, CBLAS_SIDE side, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA, CBLAS_DIAG diag,
+                 gb300_blas_int m, gb300_blas_int n, float alpha, const float* A, gb300_blas_int lda, float* B,
+                 gb300_blas_int ldb);
+void cblas_dtrsm(CBLAS_ORDER order, CBLAS_SIDE side, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA, CBLAS_DIAG diag,
+                 gb300_blas_int m, gb300_blas_int n, double alpha, const double* A, gb300_blas_int lda,
+                 double* B, gb300_blas_int ldb);
+void cblas_ctrsm(CBLAS_ORDER order, CBLAS_SIDE side, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA, CBLAS_DIAG diag,
+                 gb300_blas_int m, gb300_blas_int n, const void* alpha, const void* A, gb300_blas_int lda,
+                 void* B, gb300_blas_int ldb);
+void cblas_ztrsm(CBLAS_ORDER order, CBLAS_SIDE side, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA, CBLAS_DIAG diag,
+                 gb300_blas_int m, gb300_blas_int n, const void* alpha, const void* A, gb300_blas_int lda,
+                 void* B, gb300_blas_int ldb);
+/* blaze/math/blas/cblas/axpy.h:103,133,165,198 */
+void cblas_saxpy(gb300_blas_int n, float alpha, const float* x, gb300_blas_int incX, float* y, gb300_blas_int incY);
+void cblas_daxpy(gb300_blas_int n, double alpha, const double* x, gb300_blas_int incX, double* y,
+                 gb300_blas_int incY);
+void cblas_caxpy(gb300_blas_int n, const void* alpha, const void* x, gb300_blas_int incX, void* y,
+                 gb300_blas_int incY);
+void cblas_zaxpy(gb300_blas_int n, const void* alpha, const void* x, gb300_blas_int incX, void* y,
+                 gb300_blas_int incY);
+/* blaze/math/blas/cblas/dotu.h:99,127 and dotc.h */
+float cblas_sdot(gb300_blas_int n, const float* x, gb300_blas_int incX, const float* y, gb300_blas_int incY);
+double cblas_ddot(gb300_blas_int n, const double* x, gb300_blas_int incX, const double* y, gb300_blas_int incY);
+/* Both forms of the complex dot products: dotu.h / dotc.h reference each under its own branch. */
+void cblas_cdotu_sub(gb300_blas_int n, const void* x, gb300_blas_int incX, const void* y, gb300_blas_int incY,
+                     void* dotu);
+void cblas_zdotu_sub(gb300_blas_int n, const void* x, gb300_blas_int incX, const void* y, gb300_blas_int incY,
+                     void* dotu);
+void cblas_cdotc_sub(gb300_blas_int n, const void* x, gb300_blas_int incX, const void* y, gb300_blas_int incY,
+                     void* dotc);
+void cblas_zdotc_sub(gb300_blas_int n, const void* x, gb300_blas_int incX, const void* y, gb300_blas_int incY,
+                     void* dotc);
+/* The value-returning complex forms exist in some CBLAS flavours; the library exports them with
+ * the result written through the trailing pointer (interoperable with the _sub forms). */
+void cblas_cdotu(gb300_blas_int n, const void* x, gb300_blas_int incX, const void* y, gb300_blas_int incY,
+                 void* dotu);
+void cblas_zdotu(gb300_blas_int n, const void* x, gb300_blas_int incX, const void* y, gb300_blas_int incY,
+                 void* dotu);
+void cblas_cdotc(gb300_blas_int n, const void* x, gb300_blas_int incX, const void* y, gb300_blas_int incY,
+                 void* dotc);
+void cblas_zdotc(gb300_blas_int n, const void* x, gb300_blas_int incX, const void* y, gb300_blas_int incY,
+                 void* dotc);
+
+#if defined(__GNUC__)
+#pragma GCC visibility pop
+#endif
+#ifdef __cplusplus
+} /* extern "C" */
+#endif
+
+/* ---- optional throwing wrappers for C++ callers (Blaze) ------------------------------------- */
+#if defined(__cplusplus) && defined(GB300_BLAS_THROW)
+extern "C++" {
+#include <stdexcept>
+#include <string>
+inline void gb300_throw_if_error(const char* routine) {
+    const int st = gb300_last_error();
+    if (st != 0) {
+        std::string msg = std::string(routine) + ": " + gb300_last_error_message();
+        gb300_clear_error();
+        throw std::runtime_error(msg);
+    }
+}
+}
+extern "C" {
+static inline void cblas_sgemm(CBLAS_ORDER order, CBLAS_TRANSPOSE transA, CBLAS_TRANSPOSE transB,
+                               gb300_blas_int m, gb300_blas_int n, gb300_blas_int k, float alpha,
+                               const float* A, gb300_blas_int lda, const float* B, gb300_blas_int ldb,
+                               float beta, float* C, gb300_blas_int ldc) {
+    gb300_cblas_sgemm_checked(order, transA, transB, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+    gb300_throw_if_error("cblas_sgemm");
+}
+static inline void cblas_dgemm(CBLAS_ORDER order, CBLAS_TRANSPOSE transA, CBLAS_TRANSPOSE transB,
+                               gb300_blas_int m, gb300_blas_int n, gb300_blas_int k, double alpha,
+                               const double* A, gb300_blas_int lda, const double* B, gb300_blas_int ldb,
+                               double beta, double* C, gb300_blas_int ldc) {
+    gb300_cblas_dgemm_checked(order, transA, transB, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+    gb300_throw_if_error("cblas_dgemm");
+}
+}
+#endif
+
+#endif /* GB300_CBLAS_H */

@@ -1,0 +1,230 @@
+"""CPU oracle for the dense matrix-multiplication path (TEST INFRASTRUCTURE ONLY).
+
+Python bindings (ctypes + numpy) for ``oracle/_build/liboracle.so`` — the C restatement of
+Blaze's CPU GEMM kernels, the seeded generators and the compensated (Dot2) FP64 reference — and,
+when it has been built in a container that has the reference headers, for
+``oracle/_ref/libblazeref.so`` (Blaze itself).
+
+Only the tests, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline legs use this module,
+always as the checker or as the timed CPU baseline.  The shipped library never calls it.
+"""
+from __future__ import annotations
+
+import ctypes as ct
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+REF_PATH = os.path.join(HERE, "_ref", "libblazeref.so")
+
+ROW_MAJOR, COL_MAJOR = 101, 102
+NO_TRANS, TRANS = 111, 112
+
+_lib = None
+_ref = None
+
+
+def build(quiet: bool = True) -> str:
+    """Compile liboracle.so with oracle/Makefile (gcc, a few seconds)."""
+    out = subprocess.run(["make", "-C", HERE], capture_output=True, text=True)
+    if out.returncode != 0:
+        raise RuntimeError("oracle build failed:\n" + out.stdout + out.stderr)
+    if not quiet:
+        print(out.stdout)
+    return LIB_PATH
+
+
+def build_ref(ref_root: str = "/root/reference") -> str | None:
+    """Compile oracle/_ref/libblazeref.so from the reference headers, if they are present."""
+    if os.path.exists(REF_PATH):
+        return REF_PATH
+    if not os.path.isdir(os.path.join(ref_root, "blaze")):
+        return None
+    out = subprocess.run(["make", "-C", HERE, "ref", f"REF={ref_root}"], capture_output=True, text=True)
+    if out.returncode != 0:
+        raise RuntimeError("reference build failed:\n" + out.stdout + out.stderr)
+    return REF_PATH
+
+
+_D = ct.POINTER(ct.c_double)
+_F = ct.POINTER(ct.c_float)
+_I64 = ct.c_int64
+
+
+def _gemm_argtypes(P, S):
+    return [ct.c_int, ct.c_int, ct.c_int, _I64, _I64, _I64, S, P, _I64, P, _I64, S, P, _I64]
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = ct.CDLL(LIB_PATH)
+        L.orc_fill_uniform_d.argtypes = [_D, _I64, ct.c_uint32, ct.c_double, ct.c_double]
+        L.orc_fill_uniform_s.argtypes = [_F, _I64, ct.c_uint32, ct.c_float, ct.c_float]
+        L.orc_fill_spread_d.argtypes = [_D, _I64, ct.c_uint32, ct.c_int, ct.c_int]
+        L.orc_fill_spread_s.argtypes = [_F, _I64, ct.c_uint32, ct.c_int, ct.c_int]
+        L.orc_fill_int_d.argtypes = [_D, _I64, ct.c_uint32, ct.c_int, ct.c_int]
+        L.orc_mt19937_raw.argtypes = [ct.c_uint32, ct.POINTER(ct.c_uint32), _I64]
+        L.orc_gemm_default_d.argtypes = _gemm_argtypes(_D, ct.c_double)
+        L.orc_gemm_default_s.argtypes = _gemm_argtypes(_F, ct.c_float)
+        L.orc_gemm_blocked_d.argtypes = _gemm_argtypes(_D, ct.c_double) + [ct.c_int]
+        L.orc_gemm_blocked_s.argtypes = _gemm_argtypes(_F, ct.c_float) + [ct.c_int]
+        L.orc_product_rows_dot2.argtypes = [ct.c_int, ct.c_int, ct.c_int, _I64, _I64, _I64, _D, _I64,
+                                            _D, _I64, ct.POINTER(ct.c_int64), _I64, _D, ct.c_int]
+        L.orc_fro_norm_d.argtypes = [_D, _I64, _I64, _I64, ct.c_int]
+        L.orc_fro_norm_d.restype = ct.c_double
+        L.orc_fro_norm_s.argtypes = [_F, _I64, _I64, _I64, ct.c_int]
+        L.orc_fro_norm_s.restype = ct.c_double
+        L.orc_max_threads.restype = ct.c_int
+        _lib = L
+    return _lib
+
+
+def ref_lib():
+    """Blaze itself (oracle/_ref), or None when it was not built here."""
+    global _ref
+    if _ref is None and os.path.exists(REF_PATH):
+        R = ct.CDLL(REF_PATH)
+        R.ref_gemm_d.argtypes = _gemm_argtypes(_D, ct.c_double)
+        R.ref_gemm_d.restype = ct.c_int
+        R.ref_gemm_s.argtypes = _gemm_argtypes(_F, ct.c_float)
+        R.ref_gemm_s.restype = ct.c_int
+        _ref = R
+    return _ref
+
+
+def _p(x: np.ndarray):
+    assert x.flags["C_CONTIGUOUS"] or x.flags["F_CONTIGUOUS"]
+    return x.ctypes.data_as(_D if x.dtype == np.float64 else _F)
+
+
+# ---- generators ---------------------------------------------------------------------------------
+def uniform(n: int, seed: int, lo: float = -1.0, hi: float = 1.0, dtype=np.float64) -> np.ndarray:
+    x = np.empty(n, dtype=dtype)
+    if dtype == np.float64:
+        lib().orc_fill_uniform_d(_p(x), n, seed, lo, hi)
+    else:
+        lib().orc_fill_uniform_s(_p(x), n, seed, lo, hi)
+    return x
+
+
+def spread(n: int, seed: int, emin: int = -20, emax: int = 20, dtype=np.float64) -> np.ndarray:
+    x = np.empty(n, dtype=dtype)
+    if dtype == np.float64:
+        lib().orc_fill_spread_d(_p(x), n, seed, emin, emax)
+    else:
+        lib().orc_fill_spread_s(_p(x), n, seed, emin, emax)
+    return x
+
+
+def integers(n: int, seed: int, lo: int = -10, hi: int = 10) -> np.ndarray:
+    x = np.empty(n, dtype=np.float64)
+    lib().orc_fill_int_d(_p(x), n, seed, lo, hi)
+    return x
+
+
+def mt19937_raw(seed: int, n: int) -> np.ndarray:
+    x = np.empty(n, dtype=np.uint32)
+    lib().orc_mt19937_raw(seed, x.ctypes.data_as(ct.POINTER(ct.c_uint32)), n)
+    return x
+
+
+def matrix(rows: int, cols: int, seed: int, dist: str = "uniform", dtype=np.float64,
+           ld: int | None = None, order: int = ROW_MAJOR) -> np.ndarray:
+    """A stored matrix buffer: rows x cols logical, `order` storage, leading dimension `ld`.
+
+    Returns the flat storage buffer (length ld*rows for row-major, ld*cols for column-major);
+    padding elements are filled from the same stream.
+    """
+    if order == ROW_MAJOR:
+        ld = cols if ld is None else ld
+        n = max(ld * rows, 1)
+    else:
+        ld = rows if ld is None else ld
+        n = max(ld * cols, 1)
+    if dist == "uniform":
+        return uniform(n, seed, dtype=dtype)
+    if dist == "spread":
+        return spread(n, seed, dtype=dtype)
+    if dist == "int":
+        return integers(n, seed).astype(dtype)
+    raise ValueError(dist)
+
+
+# ---- kernels -------------------------------------------------------------------------------------
+def gemm(order, transA, transB, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, kernel="blocked",
+         nthreads: int = 0):
+    """CBLAS-semantics C = alpha*op(A)op(B) + beta*C with the Blaze restatement (in place on C)."""
+    L = lib()
+    if C.dtype == np.float64:
+        if kernel == "blocked":
+            L.orc_gemm_blocked_d(order, transA, transB, m, n, k, alpha, _p(A), lda, _p(B), ldb, beta, _p(C), ldc, nthreads)
+        else:
+            L.orc_gemm_default_d(order, transA, transB, m, n, k, alpha, _p(A), lda, _p(B), ldb, beta, _p(C), ldc)
+    else:
+        if kernel == "blocked":
+            L.orc_gemm_blocked_s(order, transA, transB, m, n, k, alpha, _p(A), lda, _p(B), ldb, beta, _p(C), ldc, nthreads)
+        else:
+            L.orc_gemm_default_s(order, transA, transB, m, n, k, alpha, _p(A), lda, _p(B), ldb, beta, _p(C), ldc)
+    return C
+
+
+def ref_gemm(order, transA, transB, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc):
+    """The same call through Blaze itself (oracle/_ref); raises if it was not built."""
+    R = ref_lib()
+    if R is None:
+        raise RuntimeError("oracle/_ref/libblazeref.so not built")
+    f = R.ref_gemm_d if C.dtype == np.float64 else R.ref_gemm_s
+    if f(order, transA, transB, m, n, k, alpha, _p(A), lda, _p(B), ldb, beta, _p(C), ldc) != 0:
+        raise RuntimeError("Blaze raised an exception for this call (see stderr)")
+    return C
+
+
+def product_rows_dot2(order, transA, transB, m, n, k, A, lda, B, ldb, rows=None, nthreads: int = 0):
+    """Rows of op(A)op(B) (logical row-major, nrows x n) in compensated FP64."""
+    A = np.ascontiguousarray(A, dtype=np.float64)
+    B = np.ascontiguousarray(B, dtype=np.float64)
+    if rows is None:
+        nrows, rp = m, None
+    else:
+        rows = np.ascontiguousarray(rows, dtype=np.int64)
+        nrows, rp = len(rows), rows.ctypes.data_as(ct.POINTER(ct.c_int64))
+    P = np.empty((nrows, n), dtype=np.float64)
+    lib().orc_product_rows_dot2(order, transA, transB, m, n, k, _p(A), lda, _p(B), ldb, rp, nrows, _p(P), nthreads)
+    return P
+
+
+def fro_norm_op(order, trans, rows, cols, X, ld) -> float:
+    """Frobenius norm of the logical rows x cols operand op(X) (compensated)."""
+    # the norm is invariant under transposition; walk the storage as it lies
+    sr, sc = (rows, cols) if trans == NO_TRANS else (cols, rows)
+    rm = 1 if order == ROW_MAJOR else 0
+    if X.dtype == np.float64:
+        return lib().orc_fro_norm_d(_p(X), sr, sc, ld, rm)
+    return lib().orc_fro_norm_s(_p(X), sr, sc, ld, rm)
+
+
+def logical(order, trans, rows, cols, X, ld) -> np.ndarray:
+    """The logical rows x cols matrix op(X) as a numpy array (a view when possible)."""
+    t = trans != NO_TRANS
+    if order == ROW_MAJOR:
+        if not t:
+            return np.lib.stride_tricks.as_strided(X, (rows, cols), (ld * X.itemsize, X.itemsize))
+        return np.lib.stride_tricks.as_strided(X, (rows, cols), (X.itemsize, ld * X.itemsize))
+    if not t:
+        return np.lib.stride_tricks.as_strided(X, (rows, cols), (X.itemsize, ld * X.itemsize))
+    return np.lib.stride_tricks.as_strided(X, (rows, cols), (ld * X.itemsize, X.itemsize))
+
+
+def normwise_error(C_logical: np.ndarray, Cref_logical: np.ndarray, normA: float, normB: float,
+                   scale: float = 1.0) -> float:
+    """||C - Cref||_F / (||A||_F ||B||_F), with an optional sqrt(m/nrows) sampling scale."""
+    d = np.asarray(C_logical, dtype=np.float64) - np.asarray(Cref_logical, dtype=np.float64)
+    num = float(np.sqrt(np.sum(d * d))) * scale
+    den = normA * normB
+    return num / den if den > 0 else num

@@ -1,0 +1,212 @@
+/*
+ * oracle_blaze.c — C restatement of Blaze's CPU dense matrix-multiplication kernels.
+ *
+ * TEST INFRASTRUCTURE ONLY (the checker and the timed CPU baseline); see oracle.h.
+ *
+ * Two kernels, both with CBLAS argument semantics:
+ *
+ *  orc_gemm_default_*   blaze/math/expressions/DMatDMatMultExpr.h:590-681
+ *      For each row i:  C(i,j) = A(i,0)*B(0,j)  then  C(i,j) += A(i,k)*B(k,j)  for k = 1..K-1,
+ *      i.e. every element is accumulated sequentially in k order.  (The row x column default
+ *      kernel, DMatTDMatMultExpr.h:566-665, forms the same sequential dot product per element.)
+ *      The alpha/beta update follows Blaze's scaled/add-assign expressions: the product is
+ *      formed first, then C = alpha*P (beta == 0: C is not read) or C = alpha*P + beta*C.
+ *
+ *  orc_gemm_blocked_*   blaze/math/dense/MMM.h:105-600 (`mmm`, row-major C)
+ *      beta == 0 resets C without reading it, beta != 1 scales C (MMM.h:146-151);
+ *      k-panels of KBLOCK = MMM_OUTER_BLOCK_SIZE*16/sizeof(T) = 112*16/sizeof(T) columns
+ *      (blaze/system/Blocking.h:60-61, MMM.h:131) with A's panel packed row-major (A2) and
+ *      JBLOCK = MMM_INNER_BLOCK_SIZE = 96 column panels of B packed column-major (B2);
+ *      each C element of a panel pair is a SIMDSIZE-lane split dot product over the panel,
+ *      reduced by a horizontal sum and added as C(i,j) += sum*alpha (MMM.h:190-330); when K is
+ *      not a multiple of SIMDSIZE the trailing columns are added term by term as
+ *      C(i,j) += A2(i,k)*B2(k,j)*alpha (MMM.h:470-575).  SIMDSIZE is 8 doubles / 16 floats
+ *      (the AVX-512 width Blaze selects on the survey host).
+ *      Column-major C (MMM.h:605-1080) is evaluated through the identity
+ *      C^T = op(B)^T op(A)^T, which maps a column-major call onto the row-major kernel.
+ *      Rows of C are split across OpenMP threads (Blaze's SMP layer splits C into thread
+ *      tiles, blaze/math/smp/openmp/DenseMatrix.h:97-160; every tile runs the same kernel).
+ */
+#include "oracle.h"
+
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define KBLOCK_D (112 * 16 / 8)   /* 224 */
+#define KBLOCK_S (112 * 16 / 4)   /* 448 */
+#define JBLOCK 96
+#define LANES_D 8
+#define LANES_S 16
+
+/* Logical element (r,c) of op(X) for a row-major call: X stored row-major with leading
+ * dimension ld; trans selects X^T. */
+#define OPX(X, ld, trans, r, c) ((trans) ? (X)[(int64_t)(c) * (ld) + (r)] : (X)[(int64_t)(r) * (ld) + (c)])
+
+int orc_max_threads(void) {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+/* ---------------------------------------------------------------------------------------------
+ * default (scalar i-k-j) kernel
+ * ------------------------------------------------------------------------------------------- */
+#define DEFINE_DEFAULT(SUFFIX, T)                                                                  \
+static void default_rm_##SUFFIX(int tA, int tB, int64_t m, int64_t n, int64_t k, T alpha,        \
+                                const T* A, int64_t lda, const T* B, int64_t ldb, T beta, T* C,  \
+                                int64_t ldc) {                                                   \
+    T* row = (T*)malloc(sizeof(T) * (size_t)(n > 0 ? n : 1));                                   \
+    for (int64_t i = 0; i < m; ++i) {                                                            \
+        if (k == 0) {                                                                            \
+            for (int64_t j = 0; j < n; ++j) row[j] = (T)0;                                       \
+        } else {                                                                                 \
+            const T a0 = OPX(A, lda, tA, i, 0);                                                  \
+            for (int64_t j = 0; j < n; ++j) row[j] = a0 * OPX(B, ldb, tB, 0, j);                 \
+            for (int64_t p = 1; p < k; ++p) {                                                    \
+                const T a = OPX(A, lda, tA, i, p);                                               \
+                for (int64_t j = 0; j < n; ++j) row[j] += a * OPX(B, ldb, tB, p, j);             \
+            }                                                                                    \
+        }                                                                                        \
+        T* c = C + i * ldc;                                                                      \
+        if (beta == (T)0) {                                                                      \
+            for (int64_t j = 0; j < n; ++j) c[j] = alpha * row[j];                               \
+        } else {                                                                                 \
+            for (int64_t j = 0; j < n; ++j) c[j] = alpha * row[j] + beta * c[j];                 \
+        }                                                                                        \
+    }                                                                                            \
+    free(row);                                                                                   \
+}                                                                                                \
+void orc_gemm_default_##SUFFIX(int order, int transA, int transB, int64_t m, int64_t n,         \
+                               int64_t k, T alpha, const T* A, int64_t lda, const T* B,          \
+                               int64_t ldb, T beta, T* C, int64_t ldc) {                         \
+    const int tA = (transA != ORC_NO_TRANS), tB = (transB != ORC_NO_TRANS);                      \
+    if (m <= 0 || n <= 0) return;                                                                \
+    if (order == ORC_ROW_MAJOR)                                                                  \
+        default_rm_##SUFFIX(tA, tB, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);               \
+    else                                                                                         \
+        default_rm_##SUFFIX(tB, tA, n, m, k, alpha, B, ldb, A, lda, beta, C, ldc);               \
+}
+
+DEFINE_DEFAULT(d, double)
+DEFINE_DEFAULT(s, float)
+
+/* ---------------------------------------------------------------------------------------------
+ * blocked (mmm) kernel
+ * ------------------------------------------------------------------------------------------- */
+#define DEFINE_BLOCKED(SUFFIX, T, KBLOCK, LANES)                                                   \
+static void blocked_rows_##SUFFIX(int tA, int tB, int64_t i0, int64_t i1, int64_t n, int64_t k,  \
+                                  T alpha, const T* A, int64_t lda, const T* B, int64_t ldb,     \
+                                  T* C, int64_t ldc, T* A2, T* B2) {                             \
+    const int64_t isize = i1 - i0;                                                               \
+    for (int64_t kk = 0; kk < k; kk += KBLOCK) {                                                 \
+        const int64_t kb = (kk + KBLOCK <= k) ? KBLOCK : (k - kk);                               \
+        const int64_t kv = kb - kb % LANES; /* lane-split part of the panel */                  \
+        for (int64_t i = 0; i < isize; ++i)                                                      \
+            for (int64_t p = 0; p < kb; ++p) A2[i * KBLOCK + p] = OPX(A, lda, tA, i0 + i, kk + p);\
+        for (int64_t jj = 0; jj < n; jj += JBLOCK) {                                             \
+            const int64_t jb = (jj + JBLOCK <= n) ? JBLOCK : (n - jj);                           \
+            for (int64_t j = 0; j < jb; ++j)                                                     \
+                for (int64_t p = 0; p < kb; ++p) B2[j * KBLOCK + p] = OPX(B, ldb, tB, kk + p, jj + j);\
+            int64_t i = 0;                                                                       \
+            for (; i + 4 <= isize; i += 4) {                                                     \
+                int64_t j = 0;                                                                   \
+                for (; j + 2 <= jb; j += 2) {                                                    \
+                    T x[4][2][LANES];                                                            \
+                    memset(x, 0, sizeof(x));                                                     \
+                    const T* a0 = A2 + (i + 0) * KBLOCK; const T* a1 = A2 + (i + 1) * KBLOCK;    \
+                    const T* a2 = A2 + (i + 2) * KBLOCK; const T* a3 = A2 + (i + 3) * KBLOCK;    \
+                    const T* b0 = B2 + (j + 0) * KBLOCK; const T* b1 = B2 + (j + 1) * KBLOCK;    \
+                    for (int64_t p = 0; p < kv; p += LANES) {                                    \
+                        for (int l = 0; l < LANES; ++l) {                                        \
+                            x[0][0][l] += a0[p + l] * b0[p + l]; x[0][1][l] += a0[p + l] * b1[p + l];\
+                            x[1][0][l] += a1[p + l] * b0[p + l]; x[1][1][l] += a1[p + l] * b1[p + l];\
+                            x[2][0][l] += a2[p + l] * b0[p + l]; x[2][1][l] += a2[p + l] * b1[p + l];\
+                            x[3][0][l] += a3[p + l] * b0[p + l]; x[3][1][l] += a3[p + l] * b1[p + l];\
+                        }                                                                        \
+                    }                                                                            \
+                    for (int r = 0; r < 4; ++r)                                                  \
+                        for (int c = 0; c < 2; ++c) {                                            \
+                            T s = (T)0;                                                          \
+                            for (int l = 0; l < LANES; ++l) s += x[r][c][l];                     \
+                            T* cij = C + (i0 + i + r) * ldc + jj + j + c;                        \
+                            *cij += s * alpha;                                                   \
+                            const T* ar = A2 + (i + r) * KBLOCK; const T* bc = B2 + (j + c) * KBLOCK;\
+                            for (int64_t p = kv; p < kb; ++p) *cij += ar[p] * bc[p] * alpha;     \
+                        }                                                                        \
+                }                                                                                \
+                for (; j < jb; ++j)                                                              \
+                    for (int r = 0; r < 4; ++r) {                                                \
+                        T x1[LANES];                                                             \
+                        memset(x1, 0, sizeof(x1));                                               \
+                        const T* ar = A2 + (i + r) * KBLOCK; const T* bc = B2 + j * KBLOCK;      \
+                        for (int64_t p = 0; p < kv; p += LANES)                                  \
+                            for (int l = 0; l < LANES; ++l) x1[l] += ar[p + l] * bc[p + l];      \
+                        T s = (T)0;                                                              \
+                        for (int l = 0; l < LANES; ++l) s += x1[l];                              \
+                        T* cij = C + (i0 + i + r) * ldc + jj + j;                                \
+                        *cij += s * alpha;                                                       \
+                        for (int64_t p = kv; p < kb; ++p) *cij += ar[p] * bc[p] * alpha;         \
+                    }                                                                            \
+            }                                                                                    \
+            for (; i < isize; ++i)                                                               \
+                for (int64_t j = 0; j < jb; ++j) {                                               \
+                    T x1[LANES];                                                                 \
+                    memset(x1, 0, sizeof(x1));                                                   \
+                    const T* ar = A2 + i * KBLOCK; const T* bc = B2 + j * KBLOCK;                \
+                    for (int64_t p = 0; p < kv; p += LANES)                                      \
+                        for (int l = 0; l < LANES; ++l) x1[l] += ar[p + l] * bc[p + l];          \
+                    T s = (T)0;                                                                  \
+                    for (int l = 0; l < LANES; ++l) s += x1[l];                                  \
+                    T* cij = C + (i0 + i) * ldc + jj + j;                                        \
+                    *cij += s * alpha;                                                           \
+                    for (int64_t p = kv; p < kb; ++p) *cij += ar[p] * bc[p] * alpha;             \
+                }                                                                                \
+        }                                                                                        \
+    }                                                                                            \
+}                                                                                                \
+static void blocked_rm_##SUFFIX(int tA, int tB, int64_t m, int64_t n, int64_t k, T alpha,        \
+                                const T* A, int64_t lda, const T* B, int64_t ldb, T beta, T* C,  \
+                                int64_t ldc, int nthreads) {                                     \
+    /* beta pre-scale, MMM.h:146-151: reset (no read) for beta == 0, scale for beta != 1 */      \
+    for (int64_t i = 0; i < m; ++i) {                                                            \
+        T* c = C + i * ldc;                                                                      \
+        if (beta == (T)0) { for (int64_t j = 0; j < n; ++j) c[j] = (T)0; }                       \
+        else if (beta != (T)1) { for (int64_t j = 0; j < n; ++j) c[j] *= beta; }                 \
+    }                                                                                            \
+    if (k == 0) return;                                                                          \
+    int nt = nthreads > 0 ? nthreads : orc_max_threads();                                        \
+    if (nt < 1) nt = 1;                                                                          \
+    /* row tiles of at least 20 rows per thread, multiples of the 4-row micro-tile */            \
+    int64_t chunk = (m + nt - 1) / nt;                                                           \
+    chunk = ((chunk + 3) / 4) * 4;                                                               \
+    if (chunk < 20) chunk = 20;                                                                  \
+    const int64_t ntiles = (m + chunk - 1) / chunk;                                              \
+    _Pragma("omp parallel for num_threads(nt) schedule(static)")                                 \
+    for (int64_t t = 0; t < ntiles; ++t) {                                                       \
+        const int64_t i0 = t * chunk;                                                            \
+        const int64_t i1 = (i0 + chunk < m) ? i0 + chunk : m;                                    \
+        T* A2 = (T*)malloc(sizeof(T) * (size_t)(i1 - i0) * KBLOCK);                              \
+        T* B2 = (T*)malloc(sizeof(T) * (size_t)JBLOCK * KBLOCK);                                 \
+        blocked_rows_##SUFFIX(tA, tB, i0, i1, n, k, alpha, A, lda, B, ldb, C, ldc, A2, B2);      \
+        free(A2);                                                                                \
+        free(B2);                                                                                \
+    }                                                                                            \
+}                                                                                                \
+void orc_gemm_blocked_##SUFFIX(int order, int transA, int transB, int64_t m, int64_t n,         \
+                               int64_t k, T alpha, const T* A, int64_t lda, const T* B,          \
+                               int64_t ldb, T beta, T* C, int64_t ldc, int nthreads) {           \
+    const int tA = (transA != ORC_NO_TRANS), tB = (transB != ORC_NO_TRANS);                      \
+    if (m <= 0 || n <= 0) return;                                                                \
+    if (order == ORC_ROW_MAJOR)                                                                  \
+        blocked_rm_##SUFFIX(tA, tB, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, nthreads);     \
+    else                                                                                         \
+        blocked_rm_##SUFFIX(tB, tA, n, m, k, alpha, B, ldb, A, lda, beta, C, ldc, nthreads);     \
+}
+
+DEFINE_BLOCKED(d, double, KBLOCK_D, LANES_D)
+DEFINE_BLOCKED(s, float, KBLOCK_S, LANES_S)

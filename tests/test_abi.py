@@ -1,0 +1,104 @@
+"""The C-ABI library: it loads without a GPU, exports every function the public headers declare,
+and its host-side argument handling follows the CBLAS contract."""
+import ctypes as ct
+import os
+import re
+
+import numpy as np
+import pytest
+
+import blaze_gb300 as G
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADERS = [os.path.join(ROOT, "include", h) for h in sorted(os.listdir(os.path.join(ROOT, "include"))) if h.endswith(".h")]
+
+
+@pytest.fixture(scope="module")
+def lib():
+    if not os.path.exists(G.LIB_PATH):
+        G.build()
+    return G.lib()
+
+
+def declared_functions():
+    names = set()
+    for h in HEADERS:
+        text = open(h).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        text = re.sub(r"//[^\n]*", "", text)
+        for mname in re.findall(r"\b((?:cblas|gb300)_\w+)\s*\(", text):
+            names.add(mname)
+    # the wrappers/macros of the headers themselves are not library symbols
+    names -= {"gb300_throw_if_error"}
+    return sorted(names)
+
+
+def test_headers_declare_the_cblas_surface_blaze_uses():
+    names = declared_functions()
+    for base in ("gemm", "gemv", "trmm", "trmv", "trsm", "axpy"):
+        for p in "sdcz":
+            assert f"cblas_{p}{base}" in names
+    for f in ("cblas_sdot", "cblas_ddot", "cblas_cdotu_sub", "cblas_zdotc_sub", "cblas_cdotu", "cblas_zdotc"):
+        assert f in names
+
+
+def test_library_exports_every_declared_function(lib):
+    missing = []
+    for name in declared_functions():
+        for sym in ([name, name + "_64"] if name.startswith("cblas_") or name.endswith("_checked") else [name]):
+            try:
+                getattr(lib, sym)
+            except AttributeError:
+                missing.append(sym)
+    assert not missing, missing
+
+
+def test_enum_values_are_the_cblas_abi():
+    text = open(os.path.join(ROOT, "include", "gb300_cblas.h")).read()
+    for name, val in (("CblasRowMajor", 101), ("CblasColMajor", 102), ("CblasNoTrans", 111), ("CblasTrans", 112),
+                      ("CblasConjTrans", 113), ("CblasUpper", 121), ("CblasLower", 122), ("CblasNonUnit", 131),
+                      ("CblasUnit", 132), ("CblasLeft", 141), ("CblasRight", 142)):
+        assert re.search(rf"\b{name}\s*=\s*{val}\b", text), name
+
+
+@pytest.mark.parametrize("args,param", [
+    (dict(order=99), 1), (dict(ta=7), 2), (dict(tb=7), 3), (dict(m=-1), 4), (dict(n=-1), 5), (dict(k=-1), 6),
+    (dict(lda=3), 9), (dict(ldb=3), 11), (dict(ldc=3), 14),
+])
+def test_argument_errors_name_the_parameter(lib, args, param):
+    a = dict(order=G.RowMajor, ta=G.NoTrans, tb=G.NoTrans, m=8, n=8, k=8, lda=8, ldb=8, ldc=8)
+    a.update(args)
+    A = np.zeros(64); B = np.zeros(64); C = np.zeros(64)
+    lib.gb300_clear_error()
+    lib.cblas_dgemm(a["order"], a["ta"], a["tb"], a["m"], a["n"], a["k"], 1.0, A.ctypes.data, a["lda"],
+                    B.ctypes.data, a["ldb"], 0.0, C.ctypes.data, a["ldc"])
+    st, msg = G.last_error()
+    assert st == G.ERR_INVALID_ARG
+    assert f"parameter {param} " in msg
+
+
+def test_quick_returns_do_not_touch_the_device(lib):
+    C = np.full(4, 7.0)
+    lib.gb300_clear_error()
+    lib.cblas_dgemm(G.RowMajor, G.NoTrans, G.NoTrans, 0, 2, 2, 1.0, None, 2, None, 2, 0.0, C.ctypes.data, 2)
+    assert G.last_error()[0] == G.OK
+    lib.cblas_dgemm(G.RowMajor, G.NoTrans, G.NoTrans, 2, 2, 0, 1.0, None, 1, None, 2, 1.0, C.ctypes.data, 2)
+    assert G.last_error()[0] == G.OK and np.all(C == 7.0)
+
+
+def test_stub_routines_report_not_supported(lib):
+    lib.gb300_clear_error()
+    lib.cblas_daxpy(4, ct.c_double(1.0), None, 1, None, 1)
+    assert G.last_error()[0] == G.ERR_NOT_SUPPORTED
+
+
+def test_no_device_is_reported_not_faked(lib):
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    A = np.ones(4); B = np.ones(4); C = np.zeros(4)
+    lib.gb300_clear_error()
+    lib.cblas_dgemm(G.RowMajor, G.NoTrans, G.NoTrans, 2, 2, 2, 1.0, A.ctypes.data, 2, B.ctypes.data, 2, 0.0,
+                    C.ctypes.data, 2)
+    assert G.last_error()[0] == G.ERR_NO_DEVICE
+    assert np.all(C == 0.0)  # nothing was computed on the CPU
