@@ -1,0 +1,363 @@
+"""Benchmark: FP64-accurate dense GEMM on GB300 (the path Blaze's `C = A * B` reaches via
+cblas_dgemm), at M = N = K = 8192.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--size 8192]
+
+One step = one FP64-accurate product C = A*B (split-precision tensor-core form, slice count chosen
+for the normwise bound k*2^-53) with A, B and C resident in HBM; `value` is 2*M*N*K / step time
+(TFLOP/s of FP64-equivalent useful work) over all GPUs.  The line also carries:
+  * the native FP64 (DFMA) kernel on the same product, with the measured FP64 peak;
+  * the normwise error of the split result against the compensated FP64 oracle (sampled rows);
+  * `e2e`: the same metric through the drop-in C-ABI (cblas_dgemm) with pinned HOST buffers, the
+    host<->device copies inside the timed region;
+  * `roofline` of the dominant kernel (tc_gemm) from CUDA events on its launching stream;
+  * `cpu_baseline`: the oracle's restatement of Blaze's blocked kernel on the host cores.
+`--impl reference` times the reference CPU implementation (the oracle's restatement of Blaze's
+default kernels, all host threads) on the same metric and prints its own line.
+Multi-GPU (torchrun): every rank computes its own product (replicas, no collective in the data
+path); the barrier and the max over ranks use torch.distributed.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "FP64-accurate GEMM TFLOP/s @8192 (split vs native FP64); serving p50/p99"
+UNIT = "TFLOP/s"
+PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
+TRAFFIC_FILE = os.path.join(ROOT, "profiles", "tc_gemm_split_8192_traffic.json")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--size", type=int, default=8192)
+    ap.add_argument("--seed", type=int, default=42)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-native", action="store_true", help="skip the native FP64 comparison")
+    return ap.parse_args()
+
+
+# ---- distributed plumbing ----------------------------------------------------------------------
+class Dist:
+    def __init__(self, gpus: int):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+            import torch
+            torch.cuda.set_device(self.local)
+            dist.init_process_group("nccl")
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            import torch
+            self.pg.all_reduce(torch.zeros(1, device="cuda"))
+            torch.cuda.synchronize()
+
+    def max(self, v: float) -> float:
+        if not self.pg:
+            return v
+        import torch
+        t = torch.tensor([v], dtype=torch.float64, device="cuda")
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+# ---- clocks sampling during the timed region -----------------------------------------------------
+class Clocks:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def read_peaks():
+    try:
+        with open(PEAKS_FILE) as f:
+            return json.load(f), "measured"
+    except (OSError, ValueError):
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+# ---- CPU baseline (the oracle's restatement of Blaze's blocked kernel) --------------------------
+def cpu_baseline(size: int, seconds_target: float = 12.0):
+    import numpy as np
+    import oracle as O
+    n = size
+    A = O.uniform(n * n, 1)
+    B = O.uniform(n * n, 2)
+    C = np.zeros(n * n)
+    threads = O.lib().orc_max_threads()
+    # warm-up on a small product, then as many products as fit the time target (at least one)
+    O.gemm(O.ROW_MAJOR, O.NO_TRANS, O.NO_TRANS, 256, 256, 256, 1.0, A, 256, B, 256, 0.0, C, 256, nthreads=threads)
+    reps, total = 0, 0.0
+    while True:
+        t0 = time.perf_counter()
+        O.gemm(O.ROW_MAJOR, O.NO_TRANS, O.NO_TRANS, n, n, n, 1.0, A, n, B, n, 0.0, C, n, nthreads=threads)
+        total += time.perf_counter() - t0
+        reps += 1
+        if total >= seconds_target or reps >= 8:
+            break
+    tflops = 2.0 * n ** 3 * reps / total / 1e12
+    return {"value": round(tflops, 5), "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{reps} product(s) of {n}^3 FP64 (row-major x row-major, uniform [-1,1]) through the oracle's "
+                      f"restatement of Blaze's blocked mmm kernel, {threads} OpenMP threads, {total:.1f} s"}
+
+
+def reference_arm(args, dist: Dist):
+    if dist.rank != 0:
+        return
+    size = max(args.size // 2, 256)
+    import numpy as np
+    import oracle as O
+    oracle_threads = O.lib().orc_max_threads()
+    n = size
+    A = O.uniform(n * n, args.seed)
+    B = O.uniform(n * n, args.seed + 1)
+    C = np.zeros(n * n)
+    for _ in range(args.warmup):
+        O.gemm(O.ROW_MAJOR, O.NO_TRANS, O.NO_TRANS, n, n, n, 1.0, A, n, B, n, 0.0, C, n, nthreads=oracle_threads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        O.gemm(O.ROW_MAJOR, O.NO_TRANS, O.NO_TRANS, n, n, n, 1.0, A, n, B, n, 0.0, C, n, nthreads=oracle_threads)
+    dt = time.perf_counter() - t0
+    value = 2.0 * n ** 3 * args.steps / dt / 1e12
+    sample = (f"each step one {n}^3 FP64 product (1/8 of the {args.size}^3 workload) through the oracle's "
+              f"restatement of Blaze's blocked mmm kernel on {oracle_threads} host threads (the reference is "
+              f"header-only C++; its own build needs its headers, which the GPU host does not have)")
+    line = {"metric": METRIC, "value": round(value, 5), "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dt / args.steps * 1e3, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"dense FP64 GEMM C=A*B, M=N=K={args.size} (timed on {n}^3 samples), row-major, "
+                                   f"uniform [-1,1] (mt19937 seed {args.seed})", "method": "blaze-cpu"},
+            "cpu_baseline": {"value": round(value, 5), "unit": UNIT, "cores": oracle_threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": round(value, 5), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---- GPU arm -----------------------------------------------------------------------------------------
+def ours(args, dist: Dist):
+    import numpy as np
+    import torch
+
+    import blaze_gb300 as G
+
+    dev = dist.local
+    torch.cuda.set_device(dev)
+    G.select_device(dev)
+    G.device_info()
+    n = args.size
+    flops = 2.0 * n ** 3
+    s = torch.cuda.Stream(device=dev)
+
+    import oracle as O
+    # inputs: seeded mt19937 uniform [-1,1] built on the host (exactly reproducible), then resident
+    hA = torch.from_numpy(O.uniform(n * n, args.seed + 17 * dist.rank))
+    hB = torch.from_numpy(O.uniform(n * n, args.seed + 17 * dist.rank + 1))
+    with torch.cuda.stream(s):
+        dA = hA.to(f"cuda:{dev}", non_blocking=False)
+        dB = hB.to(f"cuda:{dev}", non_blocking=False)
+        dC = torch.empty(n * n, dtype=torch.float64, device=f"cuda:{dev}")
+    s.synchronize()
+
+    def product(method, synchronous=False):
+        o = G.opts(method=method, residency=G.PTR_DEVICE, stream=s.cuda_stream, synchronous=synchronous)
+        return G.dgemm_ex(G.RowMajor, G.NoTrans, G.NoTrans, n, n, n, 1.0, dA, n, dB, n, 0.0, dC, n, o)
+
+    # one synchronous product reports the slice count and the a-priori bound
+    info = product("split", synchronous=True)
+    for _ in range(args.warmup):
+        product("split")
+    s.synchronize()
+
+    clocks = Clocks(dev)
+    clocks.start()
+    dist.barrier()
+    G.profile_enable(True)
+    G.profile_read()  # clear
+    launches0 = G.launch_count()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    s.synchronize()
+    e0.record(s)
+    for _ in range(args.steps):
+        product("split")
+    e1.record(s)
+    s.synchronize()
+    dist.barrier()
+    launches = G.launch_count() - launches0
+    ms_tc, n_tc = G.profile_read("tc_gemm")
+    G.profile_enable(False)
+    clk = clocks.stop()
+    ms_step = e0.elapsed_time(e1) / args.steps
+    ms_step_max = dist.max(ms_step)
+    value = flops * dist.world / (ms_step_max * 1e-3) / 1e12
+
+    # accuracy of the (last) split result against the compensated oracle on sampled rows
+    G.synchronize()
+    C = dC.cpu().numpy().reshape(n, n)
+    rows = np.arange(0, n, max(1, n // 32))
+    P = O.product_rows_dot2(O.ROW_MAJOR, O.NO_TRANS, O.NO_TRANS, n, n, n, hA.numpy(), n, hB.numpy(), n, rows=rows)
+    nA = float(np.linalg.norm(hA.numpy()))
+    nB = float(np.linalg.norm(hB.numpy()))
+    err = float(np.linalg.norm(C[rows] - P) * np.sqrt(n / len(rows)) / (nA * nB))
+
+    # native FP64 on the same product (one timed product after one warm-up)
+    native = None
+    fp64_peak = G.measure_fp64_peak()
+    if not args.no_native:
+        with torch.cuda.stream(s):
+            product("native")
+            s.synchronize()
+            n0 = torch.cuda.Event(enable_timing=True)
+            n1 = torch.cuda.Event(enable_timing=True)
+            n0.record(s)
+            product("native")
+            n1.record(s)
+            s.synchronize()
+        ms_native = n0.elapsed_time(n1)
+        Cn = dC.cpu().numpy().reshape(n, n)
+        err_native = float(np.linalg.norm(Cn[rows] - P) * np.sqrt(n / len(rows)) / (nA * nB))
+        tf_native = flops / (ms_native * 1e-3) / 1e12
+        native = {"value": round(tf_native, 4), "unit": UNIT, "ms": round(ms_native, 2),
+                  "fp64_peak_tflops": round(fp64_peak, 4), "frac_of_fp64_peak": round(tf_native / fp64_peak, 4),
+                  "normwise_error": err_native}
+
+    # e2e: the drop-in C-ABI call with pinned host buffers, copies inside the timed region
+    pA = hA.pin_memory()
+    pB = hB.pin_memory()
+    pC = torch.empty(n * n, dtype=torch.float64).pin_memory()
+    G.cblas_dgemm(G.RowMajor, G.NoTrans, G.NoTrans, n, n, n, 1.0, pA, n, pB, n, 0.0, pC, n)  # warm-up
+    e2e_steps = max(2, min(args.steps, 5))
+    dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        G.cblas_dgemm(G.RowMajor, G.NoTrans, G.NoTrans, n, n, n, 1.0, pA, n, pB, n, 0.0, pC, n)
+    t_e2e = (time.perf_counter() - t0) / e2e_steps
+    t_e2e = dist.max(t_e2e)
+    e2e = {"value": round(flops * dist.world / t_e2e / 1e12, 4), "unit": UNIT,
+           "h2d_bytes_per_step": 2 * n * n * 8, "d2h_bytes_per_step": n * n * 8, "steps": e2e_steps,
+           "ms_per_step": round(t_e2e * 1e3, 3), "call": "cblas_dgemm (default method: auto -> split)"}
+
+    peaks, peaks_src = read_peaks()
+    pairs = info.slices_used * (info.slices_used + 1) // 2
+    tc_flops = pairs * flops  # BF16 tensor operations of the slice products
+    tc_ms = ms_tc / max(n_tc, 1)
+    achieved = tc_flops / (tc_ms * 1e-3) / 1e12
+    peak = float(peaks.get("bf16_tflops_sustained", peaks.get("bf16_tflops")))
+    traffic = None
+    try:
+        with open(TRAFFIC_FILE) as f:
+            tj = json.load(f)
+        if int(tj.get("size", 0)) == n and int(tj.get("slices", 0)) == info.slices_used:
+            traffic = int(tj["dram_bytes_per_launch"])
+    except (OSError, ValueError, KeyError):
+        traffic = None
+    roofline = {"kernel": "tc_gemm_kernel<exact> (split slice products)", "bound": "tensor",
+                "achieved": round(achieved, 2), "peak": peak, "unit": "TFLOP/s", "frac": round(achieved / peak, 4),
+                "traffic": traffic, "peak_source": f"bf16_tflops_sustained ({peaks_src})",
+                "work_per_launch": f"{pairs} slice products x 2*{n}^3 BF16 tensor ops",
+                "kernel_ms": round(tc_ms, 3), "kernel_share_of_step": round(tc_ms / ms_step, 4)}
+
+    if dist.rank == 0:
+        line = {"metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": dist.world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step_max, 4),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic",
+                "config": {"workload": f"dense FP64-accurate GEMM C=A*B, M=N=K={n}, row-major x row-major, "
+                                       f"uniform [-1,1] (mt19937 seed {args.seed})",
+                           "method": "split (Ozaki-style BF16 slices on tcgen05, exact int32 slice sums, FP64 "
+                                     "recombination)",
+                           "slices": info.slices_used, "target_error": f"k*2^-53 = {n * 2.0 ** -53:.3e}",
+                           "l2": "operands larger than L2 (512 MiB each)", "parallelism": "replicas"},
+                "accuracy": {"normwise_error": err, "a_priori_bound": info.error_bound,
+                             "target": n * 2.0 ** -53, "oracle": "Dot2 compensated FP64 on every "
+                                                                 f"{max(1, n // 32)}th row"},
+                "native_fp64": native,
+                "split_vs_native": round(value / dist.world / native["value"], 2) if native else None,
+                "e2e": e2e, "roofline": roofline, "gpu_launches": int(launches), "clocks": clk}
+        if not args.no_cpu:
+            line["cpu_baseline"] = cpu_baseline(min(n, 4096))
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    dist = Dist(args.gpus)
+    try:
+        if args.impl == "reference":
+            reference_arm(args, dist)
+        else:
+            ours(args, dist)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    main()

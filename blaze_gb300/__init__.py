@@ -52,8 +52,8 @@ _lib = None
 
 
 def build(force: bool = False) -> str:
-    from . import build as _b
-    return _b.build(force=force)
+    from . import nvcc_build
+    return nvcc_build.build(force=force)
 
 
 def lib() -> ct.CDLL:
@@ -62,7 +62,7 @@ def lib() -> ct.CDLL:
     if _lib is not None:
         return _lib
     if not os.path.exists(LIB_PATH):
-        raise ImportError(f"{LIB_PATH} is missing: run `python -m blaze_gb300.build` (needs nvcc)")
+        raise ImportError(f"{LIB_PATH} is missing: run `python -m blaze_gb300.nvcc_build` (needs nvcc)")
     L = ct.CDLL(LIB_PATH)
     I32, I64, D, F, VP = ct.c_int32, ct.c_int64, ct.c_double, ct.c_float, ct.c_void_p
     L.cblas_dgemm.argtypes = [ct.c_int, ct.c_int, ct.c_int, I32, I32, I32, D, VP, I32, VP, I32, D, VP, I32]
@@ -92,6 +92,12 @@ def lib() -> ct.CDLL:
     L.gb300_measure_fp64_peak.argtypes = [ct.POINTER(ct.c_double)]
     L.gb300_measure_fp64_peak.restype = ct.c_int
     L.gb300_synchronize.restype = ct.c_int
+    L.gb300_select_device.argtypes = [ct.c_int]
+    L.gb300_select_device.restype = ct.c_int
+    L.gb300_profile_enable.argtypes = [ct.c_int]
+    L.gb300_profile_enable.restype = None
+    L.gb300_profile_read.argtypes = [ct.c_char_p, ct.POINTER(ct.c_double), ct.POINTER(I64)]
+    L.gb300_profile_read.restype = ct.c_int
     L.gb300_debug_inject_stall.argtypes = [ct.c_int, ct.c_uint64]
     L.gb300_debug_inject_stall.restype = None
     _lib = L
@@ -183,6 +189,20 @@ def measure_fp64_peak() -> float:
 
 def launch_count() -> int:
     return int(lib().gb300_launch_count())
+
+
+def select_device(ordinal: int) -> None:
+    check(lib().gb300_select_device(ordinal))
+
+
+def profile_enable(on: bool = True) -> None:
+    lib().gb300_profile_enable(1 if on else 0)
+
+
+def profile_read(prefix: str | None = None) -> tuple[float, int]:
+    ms, n = ct.c_double(0.0), ct.c_int64(0)
+    check(lib().gb300_profile_read(prefix.encode() if prefix else None, ct.byref(ms), ct.byref(n)))
+    return ms.value, n.value
 
 
 def synchronize() -> None:

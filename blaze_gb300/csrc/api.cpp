@@ -213,6 +213,7 @@ int gemm_entry(int order, int transA, int transB, int64_t m, int64_t n, int64_t 
     cudaMemsetAsync(r.d_status, 0, sizeof(int), s);
 
     int used = method;
+    const void* info_dev = nullptr;
     cudaError_t e = cudaSuccess;
     if (is_double && product && method != GB300_METHOD_NATIVE) {
         SplitRequest req;
@@ -223,6 +224,7 @@ int gemm_entry(int order, int transA, int transB, int64_t m, int64_t n, int64_t 
         st = split_gemm(g, req, ctl, s, &res_out, &err);
         if (st != GB300_OK) return fail(st, err);
         used = res_out.method_used;
+        info_dev = res_out.info_dev;
         if (opts) {
             opts->slices_used = res_out.slices;
             opts->error_bound = res_out.error_bound;
@@ -258,6 +260,14 @@ int gemm_entry(int order, int transA, int transB, int64_t m, int64_t n, int64_t 
             return fail(GB300_ERR_DEVICE_TIMEOUT, std::string("a device-side wait ran out (code ") +
                                                       std::to_string(status) + ", method " + method_name(used) +
                                                       "); the result is incomplete");
+        if (opts && info_dev) {
+            int sl = 0;
+            double bd = 0;
+            if (split_read_info(info_dev, &sl, &bd)) {
+                opts->slices_used = sl;
+                opts->error_bound = bd;
+            }
+        }
     }
     return GB300_OK;
 }
@@ -328,6 +338,23 @@ int gb300_device_info(int* num_sms, int64_t* free_bytes, int64_t* total_bytes) {
 }
 
 int64_t gb300_launch_count(void) { return gb::runtime().launches.load(); }
+
+int gb300_select_device(int ordinal) {
+    gb::Runtime& r = gb::runtime();
+    std::lock_guard<std::mutex> lock(r.mu);
+    if (r.inited) {
+        if (r.device == ordinal) return GB300_OK;
+        gb::set_error(GB300_ERR_INVALID_ARG, "gb300_select_device: the library already runs on device " +
+                                                 std::to_string(r.device));
+        return GB300_ERR_INVALID_ARG;
+    }
+    cudaError_t e = cudaSetDevice(ordinal);
+    if (e != cudaSuccess) {
+        gb::set_error(GB300_ERR_NO_DEVICE, std::string("gb300_select_device: ") + cudaGetErrorString(e));
+        return GB300_ERR_NO_DEVICE;
+    }
+    return GB300_OK;
+}
 
 int gb300_synchronize(void) {
     gb::Runtime& r = gb::runtime();

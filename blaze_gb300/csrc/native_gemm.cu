@@ -25,6 +25,7 @@
 
 #include "gb300_internal.h"
 #include "ptx.cuh"
+#include "profile.h"
 #include "runtime.h"
 
 namespace gb {
@@ -255,7 +256,10 @@ cudaError_t launch_variant(const CUtensorMap& a, const CUtensorMap& b, const Nat
     auto kern = native_gemm_kernel<T, TA, TB>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kSmemBytes));
     if (e != cudaSuccess) return e;
-    kern<<<grid, THREADS, kSmemBytes, s>>>(a, b, p);
+    {
+        KernelTimer timer("native_gemm", s);
+        kern<<<grid, THREADS, kSmemBytes, s>>>(a, b, p);
+    }
     count_launches(1);
     return cudaGetLastError();
 }

@@ -19,7 +19,12 @@ struct SplitResult {
     int method_used = 0;
     int slices = 0;
     double error_bound = 0;
+    const void* info_dev = nullptr;  // device copy of the slice count and bound (tensor-core forms)
 };
+
+// Read the slice count and the a-priori bound back from the device copy (after the stream has
+// finished the product).
+bool split_read_info(const void* info_dev, int* slices, double* bound);
 
 // Runs the double-precision product g with one of the tensor-core forms (or, for AUTO, picks
 // between the split form and the native kernel).  Returns a gb300_status.

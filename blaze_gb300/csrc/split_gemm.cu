@@ -1,29 +1,807 @@
-// split_gemm.cu — tensor-core forms of the double-precision product (placeholder: AUTO runs the
-// native kernel; the explicit tensor-core methods report that they are not built yet).
+// split_gemm.cu — K2/K3: the tensor-core forms of the double-precision product on sm_103a.
+//
+//   GB300_METHOD_SPLIT   Ozaki-style split-precision product that reaches FP64-level normwise
+//                        accuracy: A and B are scaled per row / per column by powers of two and
+//                        cut into BF16 "digit" slices; the slice products run on tcgen05 tensor
+//                        cores (FP32 accumulators in TMEM) in groups whose sums stay exactly
+//                        representable, so every partial product is an exact integer; the
+//                        integers are accumulated exactly (int32) and only the final
+//                        recombination, the exponent rescale and alpha/beta run in FP64.
+//   GB300_METHOD_BF16X3  hi*hi + hi*lo + lo*hi with BF16 hi/lo parts, FP32 accumulation.
+//   GB300_METHOD_BF16    one BF16 product, FP32 accumulation.
+//   GB300_METHOD_AUTO    the split form when it is predicted faster than the native kernel.
+//
+// They replace the same CBLAS dgemm call as the native kernel (blaze/math/blas/cblas/gemm.h:
+// 156-162, reached from DMatDMatMultExpr.h:2021-2037 and siblings).
+//
+// ---- split arithmetic --------------------------------------------------------------------------
+// Row i of op(A) is scaled by 2^-e_i with e_i = frexp exponent of max_p |A(i,p)|, so the scaled
+// entries x satisfy |x| < 1.  Digits: d_1 = rint(x*2^7), r_1 = x*2^7 - d_1, then
+// d_s = rint(r_{s-1}*2^8), r_s = r_{s-1}*2^8 - d_s (all exact in FP64; |d_s| <= 128, |r_s| <= 1/2),
+// so x = sum_s d_s 2^(1-8s) + r_S 2^(1-8S).  Columns of op(B) likewise with exponents f_j.
+// With planes numbered a = s-1, the pair (a, b) has weight 2^(-14-8(a+b)); all pairs with
+// a + b = L form "level" L, L = 0..S-1 (the triangle s + t <= S + 1 of Ozaki's scheme).
+//   Exactness: one TMEM drain group accumulates at most 4 x 64 = 256 products of digits,
+//   |sum| <= 256 * 128^2 = 2^22, which FP32 holds exactly whatever the order of the additions.
+//   The epilogue reads the FP32 integer v, forms bits(v + 1.5*2^23) = 0x4B400000 + v (exact for
+//   |v| <= 2^22) and adds the bit patterns in int32 (wrapping), removing the bias at the end.
+//   A level's int32 sum over a k-segment is bounded by n_L * (Kseg/256) * 2^22 < 2^31.
+//   Error bound (elementwise, scaled units): |dC_ij| <= (S+1) K 2^(-8S); normwise
+//   ||dC||_F / (||A||_F ||B||_F) <= (S+1) K 2^(-8S) ||2^e||_2 ||2^f||_2 / (||A||_F ||B||_F)
+//   plus (S+3) 2^-53 for the FP64 recombination.  The slice count is the smallest S whose bound
+//   meets the target (default K * 2^-53, the classical worst-case FP64 dot-product bound); it is
+//   chosen on the device, so the whole product is stream-ordered without a host round trip.
+//
+// ---- kernel structure (tc_gemm_kernel) ---------------------------------------------------------
+// Persistent CTAs, one per SM, each owning whole 128 x 256 output tiles (and a k-segment).
+//   warp 0      TMA producer: 128x64 A-plane box + 256x64 B-plane box per item, 128B swizzle,
+//               4-stage ring of 48 KB stages.
+//   warp 1      TMEM allocator and MMA issuer: 4 x tcgen05.mma (M=128, N=256, K=16, BF16->FP32)
+//               per item; tcgen05.commit releases the smem stage and, at the end of a drain
+//               group, hands the accumulator buffer to the epilogue.  Two 256-column TMEM
+//               accumulators let the MMAs of one group overlap the drain of the previous one.
+//   warps 2-9   epilogue: tcgen05.ld of its 32 lanes x 128 columns, exact integer accumulation
+//               in registers, and at each level end a store of the int32 level sums (float
+//               modes: the FP32 tile) to the level planes in global memory.
+// A separate combine kernel forms C = alpha * 2^(e_i+f_j) * sum_L 2^(-14-8L) T_L + beta*C in FP64
+// (float modes: alpha * sum of segment partials + beta*C).  Every wait is bounded.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <string>
+
 #include "../../include/gb300_blas.h"
+#include "gb300_internal.h"
+#include "ptx.cuh"
 #include "runtime.h"
+#include "profile.h"
 #include "split_api.h"
 
 namespace gb {
+namespace {
 
-int split_gemm(const Gemm& g, const SplitRequest& req, const LaunchCtl& ctl, cudaStream_t s, SplitResult* out,
+constexpr int TM = 128;                 // tile rows (MMA M)
+constexpr int TN = 256;                 // tile cols (MMA N)
+constexpr int TK = 64;                  // k per item (one 128-byte swizzle row of bf16)
+constexpr int STAGES = 4;
+constexpr int A_BYTES = TM * TK * 2;    // 16 KB
+constexpr int B_BYTES = TN * TK * 2;    // 32 KB
+constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
+constexpr int GROUP_ITEMS = 4;          // exact mode: 4 items (256 products) per TMEM drain
+constexpr int EPI_WARPS = 8;
+constexpr int THREADS = 64 + EPI_WARPS * 32;
+constexpr int MAX_SLICES = 10;
+constexpr int KSEG_UNIT = 256;          // k-segments are multiples of this
+constexpr uint32_t MAGIC_BITS = 0x4B400000u;  // bits of 1.5 * 2^23
+constexpr float MAGIC = 12582912.0f;
+
+enum Mode : int { kExact = 0, kBf16 = 1, kBf16x3 = 2 };
+
+// Device-side result of the pre-pass: the slice count and the bound it guarantees.
+struct SplitInfo {
+    int slices;           // S (exact mode); planes per operand otherwise
+    int nonfinite;        // inputs contained Inf/NaN
+    double bound;         // a-priori normwise bound of the result
+    double normA, normB;  // Frobenius norms
+    double scaleA, scaleB;// ||2^e||_2, ||2^f||_2
+};
+
+// ---- pre-pass ------------------------------------------------------------------------------
+// Row statistics of a logical R x K operand X(r,p) = X[r*sr + p*sp]: e_r = frexp exponent of
+// max |X(r,:)| (kNonFinite if the row holds Inf/NaN) and q_r = sum_p (X(r,p) * 2^-e_r)^2, the
+// row's sum of squares relative to 2^(2 e_r) (so that norms of huge or tiny inputs stay finite).
+//
+// stats_tile_kernel reads 32-row x 64-k tiles (coalesced along whichever dimension is
+// contiguous, like slice_kernel) and folds each row's tile maximum and sum of squares into
+// per-row accumulators with atomics; stats_finalize_kernel turns them into (e_r, q_r).  A row
+// whose values leave [2^-500, 2^500] would over- or underflow the unscaled sum of squares; the
+// finalize kernel recomputes such (rare) rows on scaled values.
+constexpr int kNonFinite = 0x7fff;
+
+struct RowAcc {
+    unsigned long long maxbits;  // bits of max |x| (non-negative doubles order like integers)
+    double sumsq;
+    int flags;                   // 1: non-finite value seen
+    int pad;
+};
+
+__global__ void stats_tile_kernel(const double* __restrict__ X, int64_t R, int64_t K, int64_t sr, int64_t sp,
+                                  RowAcc* __restrict__ acc) {
+    __shared__ double tile[32][65];
+    const int64_t r0 = int64_t(blockIdx.y) * 32, p0 = int64_t(blockIdx.x) * 64;
+    const int t = threadIdx.x;  // 256 threads
+    if (sp == 1) {
+        for (int e = t; e < 32 * 64; e += 256) {
+            const int rr = e / 64, pp = e % 64;
+            const int64_t r = r0 + rr, p = p0 + pp;
+            tile[rr][pp] = (r < R && p < K) ? X[r * sr + p] : 0.0;
+        }
+    } else {
+        for (int e = t; e < 32 * 64; e += 256) {
+            const int pp = e / 32, rr = e % 32;
+            const int64_t r = r0 + rr, p = p0 + pp;
+            tile[rr][pp] = (r < R && p < K) ? X[r * sr + p * sp] : 0.0;
+        }
+    }
+    __syncthreads();
+    const int rr = t / 8, pp0 = (t % 8) * 8;
+    double mx = 0.0, sq = 0.0;
+    int bad = 0;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        const double v = tile[rr][pp0 + q];
+        bad |= !isfinite(v);
+        mx = fmax(mx, fabs(v));
+        sq = fma(v, v, sq);
+    }
+    // reduce over the 8 threads of the row (consecutive lanes)
+#pragma unroll
+    for (int o = 4; o > 0; o >>= 1) {
+        mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        sq += __shfl_xor_sync(0xffffffffu, sq, o);
+        bad |= __shfl_xor_sync(0xffffffffu, bad, o);
+    }
+    const int64_t r = r0 + rr;
+    if ((t & 7) == 0 && r < R) {
+        if (bad) atomicOr(&acc[r].flags, 1);
+        if (mx > 0.0) atomicMax(&acc[r].maxbits, static_cast<unsigned long long>(__double_as_longlong(mx)));
+        if (sq != 0.0) atomicAdd(&acc[r].sumsq, sq);
+    }
+}
+
+__global__ void stats_finalize_kernel(const double* __restrict__ X, int64_t R, int64_t K, int64_t sr, int64_t sp,
+                                      const RowAcc* __restrict__ acc, int* __restrict__ rexp,
+                                      double* __restrict__ rsq) {
+    const int64_t r = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (r >= R) return;
+    const RowAcc a = acc[r];
+    if (a.flags & 1) {
+        rexp[r] = kNonFinite;
+        rsq[r] = 0.0;
+        return;
+    }
+    const double mx = __longlong_as_double(static_cast<long long>(a.maxbits));
+    int e = 0;
+    if (mx > 0.0) frexp(mx, &e);
+    double q = ldexp(a.sumsq, -2 * e);
+    if (mx > 0.0 && (e > 500 || e < -500)) {
+        q = 0.0;
+        for (int64_t p = 0; p < K; ++p) {
+            const double v = ldexp(X[r * sr + p * sp], -e);
+            q = fma(v, v, q);
+        }
+    }
+    rexp[r] = e;
+    rsq[r] = q;
+}
+
+// One block: norms, scale norms, slice count and bound.  Sums are formed relative to the largest
+// row exponent, so the ratio rho = ||2^e|| ||2^f|| / (||A|| ||B||) is finite for any finite input.
+__device__ double block_sum(double v, double* red) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double t = 0.0;
+    for (int i = 0; i < int(blockDim.x >> 5); ++i) t += red[i];
+    return t;
+}
+
+__device__ int block_max_int(int v, int* red) {
+    for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    int t = red[0];
+    for (int i = 1; i < int(blockDim.x >> 5); ++i) t = max(t, red[i]);
+    return t;
+}
+
+__global__ void split_info_kernel(const int* __restrict__ eA, const double* __restrict__ qA, int64_t m,
+                                  const int* __restrict__ eB, const double* __restrict__ qB, int64_t n, int64_t k,
+                                  int mode, int fixed_slices, double target, SplitInfo* info) {
+    __shared__ double redd[32];
+    __shared__ int redi[32];
+    int bad = 0, EA = -100000, EB = -100000;
+    for (int64_t i = threadIdx.x; i < m; i += blockDim.x) {
+        if (eA[i] == kNonFinite) bad = 1;
+        else if (qA[i] > 0.0) EA = max(EA, eA[i]);
+    }
+    for (int64_t j = threadIdx.x; j < n; j += blockDim.x) {
+        if (eB[j] == kNonFinite) bad = 1;
+        else if (qB[j] > 0.0) EB = max(EB, eB[j]);
+    }
+    bad = block_max_int(bad, redi);
+    EA = block_max_int(EA, redi);
+    EB = block_max_int(EB, redi);
+    double sa = 0, na = 0, sb = 0, nb = 0;
+    for (int64_t i = threadIdx.x; i < m; i += blockDim.x) {
+        if (eA[i] == kNonFinite || qA[i] <= 0.0) continue;
+        const double w = ldexp(1.0, 2 * (eA[i] - EA));
+        sa += w;
+        na += w * qA[i];
+    }
+    for (int64_t j = threadIdx.x; j < n; j += blockDim.x) {
+        if (eB[j] == kNonFinite || qB[j] <= 0.0) continue;
+        const double w = ldexp(1.0, 2 * (eB[j] - EB));
+        sb += w;
+        nb += w * qB[j];
+    }
+    sa = block_sum(sa, redd);
+    na = block_sum(na, redd);
+    sb = block_sum(sb, redd);
+    nb = block_sum(nb, redd);
+    if (threadIdx.x == 0) {
+        SplitInfo r;
+        r.nonfinite = bad;
+        r.normA = (na > 0) ? ldexp(sqrt(na), EA) : 0.0;
+        r.normB = (nb > 0) ? ldexp(sqrt(nb), EB) : 0.0;
+        r.scaleA = (sa > 0) ? ldexp(sqrt(sa), EA) : 0.0;
+        r.scaleB = (sb > 0) ? ldexp(sqrt(sb), EB) : 0.0;
+        const double rho = (na > 0 && nb > 0) ? sqrt(sa / na) * sqrt(sb / nb) : 0.0;
+        if (mode == kExact) {
+            int S = fixed_slices;
+            if (S <= 0) {
+                S = MAX_SLICES;
+                for (int s = 2; s <= MAX_SLICES; ++s) {
+                    const double b = (s + 1) * double(k) * ldexp(1.0, -8 * s) * rho + (s + 3) * ldexp(1.0, -53);
+                    if (b <= target) { S = s; break; }
+                }
+            }
+            r.slices = S;
+            r.bound = (S + 1) * double(k) * ldexp(1.0, -8 * S) * rho + (S + 3) * ldexp(1.0, -53);
+        } else if (mode == kBf16) {
+            // each operand rounded to 8 significant bits, FP32 accumulation
+            r.slices = 1;
+            r.bound = 2.0 * ldexp(1.0, -8) + double(k) * ldexp(1.0, -24);
+        } else {
+            // hi/lo split keeps 16 bits; the dropped lo*lo term and the FP32 accumulation remain
+            r.slices = 2;
+            r.bound = 3.0 * ldexp(1.0, -16) + double(k) * ldexp(1.0, -24);
+        }
+        *info = r;
+    }
+}
+
+// Digit planes: planes[a][r][p] (bf16, pitch kpad, plane stride rpad*kpad) for r < rpad, p < kpad;
+// zeros outside the R x K operand.  Each block covers 32 rows x 64 k.
+__global__ void slice_kernel(const double* __restrict__ X, int64_t R, int64_t K, int64_t sr, int64_t sp,
+                             const int* __restrict__ rexp, const SplitInfo* __restrict__ info, int mode,
+                             __nv_bfloat16* __restrict__ planes, int64_t rpad, int64_t kpad) {
+    __shared__ double tile[32][65];
+    const int64_t r0 = int64_t(blockIdx.y) * 32, p0 = int64_t(blockIdx.x) * 64;
+    const int t = threadIdx.x;  // 256 threads
+    // load 32 x 64 doubles with coalescing along the contiguous dimension
+    if (sp == 1) {
+        for (int e = t; e < 32 * 64; e += 256) {
+            const int rr = e / 64, pp = e % 64;
+            const int64_t r = r0 + rr, p = p0 + pp;
+            tile[rr][pp] = (r < R && p < K) ? X[r * sr + p] : 0.0;
+        }
+    } else {
+        for (int e = t; e < 32 * 64; e += 256) {
+            const int pp = e / 32, rr = e % 32;
+            const int64_t r = r0 + rr, p = p0 + pp;
+            tile[rr][pp] = (r < R && p < K) ? X[r * sr + p * sp] : 0.0;
+        }
+    }
+    __syncthreads();
+    const int rr = t / 8, pp0 = (t % 8) * 8;
+    const int64_t r = r0 + rr;
+    if (r >= rpad) return;
+    const int nplanes = (mode == kExact) ? info->slices : (mode == kBf16 ? 1 : 2);
+    const int e = (r < R) ? rexp[r] : 0;
+    const bool bad = (e == kNonFinite);
+    double x[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        const double v = bad ? 0.0 : tile[rr][pp0 + q];
+        x[q] = (mode == kExact) ? ldexp(v, -e) : v;
+    }
+    __nv_bfloat16* dst = planes + r * kpad + p0 + pp0;
+    const int64_t pstride = rpad * kpad;
+    if (mode == kExact) {
+        // first digit carries 7 bits (|x| < 1), later digits 8 bits
+#pragma unroll
+        for (int q = 0; q < 8; ++q) x[q] *= 128.0;
+        for (int a = 0; a < nplanes; ++a) {
+            __align__(16) __nv_bfloat16 d[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                const double dv = rint(x[q]);
+                x[q] = (x[q] - dv) * 256.0;
+                d[q] = __float2bfloat16_rn(float(dv));
+            }
+            *reinterpret_cast<uint4*>(dst + a * pstride) = *reinterpret_cast<const uint4*>(d);
+        }
+    } else {
+        __align__(16) __nv_bfloat16 hi[8], lo[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            hi[q] = __float2bfloat16_rn(float(x[q]));
+            lo[q] = __float2bfloat16_rn(float(x[q] - double(__bfloat162float(hi[q]))));
+        }
+        *reinterpret_cast<uint4*>(dst) = *reinterpret_cast<const uint4*>(hi);
+        if (mode == kBf16x3) *reinterpret_cast<uint4*>(dst + pstride) = *reinterpret_cast<const uint4*>(lo);
+    }
+}
+
+// ---- level / pair schedule ---------------------------------------------------------------------
+__device__ __forceinline__ int num_levels(int mode, int S) { return mode == kExact ? S : 1; }
+__device__ __forceinline__ int pairs_in_level(int mode, int L) {
+    return mode == kExact ? L + 1 : (mode == kBf16 ? 1 : 3);
+}
+// (A plane, B plane) of pair `i` of level `L`.
+__device__ __forceinline__ void pair_planes(int mode, int L, int i, int& a, int& b) {
+    if (mode == kExact) { a = i; b = L - i; }
+    else if (mode == kBf16) { a = 0; b = 0; }
+    else { a = (i == 2) ? 1 : 0; b = (i == 1) ? 1 : 0; }
+}
+
+struct TcParams {
+    int mode;
+    int m_tiles, n_tiles, nseg;
+    int kb_per_seg;          // 64-wide k-blocks per segment
+    int kb_total;            // 64-wide k-blocks in the padded K
+    int64_t mpad, npad;      // padded rows of the A / B planes
+    int32_t* levels;         // [nseg][nlevels][mpad][npad] int32 (float modes: fp32 bits)
+    int max_levels;          // level dimension of `levels`
+    const SplitInfo* info;
+    int* status;
+    uint64_t limit_ns;
+    int inject_stall;
+};
+
+struct __align__(8) TcBarriers {
+    uint64_t full[STAGES];
+    uint64_t empty[STAGES];
+    uint64_t acc_full[2];
+    uint64_t acc_empty[2];
+    uint64_t drain;
+    uint32_t tmem_base;
+};
+
+constexpr size_t kTcSmem = size_t(STAGES) * STAGE_BYTES + sizeof(TcBarriers) + 1024;
+
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+    uint64_t d = 0;
+    d |= uint64_t((saddr & 0x3FFFFu) >> 4);     // start address
+    d |= uint64_t(1) << 16;                      // leading byte offset (unused for 128B swizzle)
+    d |= uint64_t(1024 >> 4) << 32;              // stride byte offset: 8 rows x 128 B
+    d |= uint64_t(1) << 46;                      // descriptor version (tcgen05)
+    d |= uint64_t(2) << 61;                      // 128-byte swizzle
+    return d;
+}
+
+// kind::f16 instruction descriptor: BF16 A and B (K-major), FP32 D, M = 128, N = 256.
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(TN >> 3) << 17) | (uint32_t(TM >> 4) << 24);
+
+// Work unit u -> (tile m, tile n, segment), grouping 8 m-tiles per band for L2 reuse.
+__device__ __forceinline__ void unit_coords(const TcParams& p, int u, int& tm, int& tn, int& seg) {
+    seg = u % p.nseg;
+    const int t = u / p.nseg;
+    const int band = 8;
+    const int per_band = band * p.n_tiles;
+    const int b = t / per_band, r = t % per_band;
+    const int rows_in_band = min(band, p.m_tiles - b * band);
+    tm = b * band + r % rows_in_band;
+    tn = r / rows_in_band;
+}
+
+template <int MODE>
+__global__ void __maxnreg__(168)
+tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, const TcParams p) {
+    extern __shared__ __align__(1024) uint8_t smem_raw[];
+    uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    TcBarriers* bars = reinterpret_cast<TcBarriers*>(smem + STAGES * STAGE_BYTES);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+    constexpr int mode = MODE;
+    const int S = (mode == kExact) ? p.info->slices : 1;
+    const int nlev = num_levels(mode, S);
+    const int units = p.m_tiles * p.n_tiles * p.nseg;
+
+    if (threadIdx.x == 0) {
+        tma_prefetch_desc(&tmA);
+        tma_prefetch_desc(&tmB);
+        for (int s = 0; s < STAGES; ++s) {
+            mbar_init(smem_u32(&bars->full[s]), 1);
+            mbar_init(smem_u32(&bars->empty[s]), 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(smem_u32(&bars->acc_full[b]), 1);
+            mbar_init(smem_u32(&bars->acc_empty[b]), EPI_WARPS);
+        }
+        mbar_init(smem_u32(&bars->drain), 1);
+        fence_mbar_init();
+    }
+    if (warp == 1) {
+        tmem_alloc(smem_u32(&bars->tmem_base), 512);
+        tmem_relinquish();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = bars->tmem_base;
+
+    if (warp == 0) {
+        // ---------------- TMA producer ----------------
+        if (lane == 0 && !p.inject_stall) {
+            uint32_t it = 0;
+            bool ok = true;
+            for (int u = blockIdx.x; u < units && ok; u += gridDim.x) {
+                int tm, tn, seg;
+                unit_coords(p, u, tm, tn, seg);
+                const int kb0 = seg * p.kb_per_seg;
+                const int kbn = min(p.kb_per_seg, p.kb_total - kb0);
+                for (int L = 0; L < nlev && ok; ++L) {
+                    const int np = pairs_in_level(mode, L);
+                    for (int kb = 0; kb < kbn && ok; ++kb) {
+                        for (int i = 0; i < np; ++i, ++it) {
+                            const int s = it % STAGES;
+                            if (it >= STAGES &&
+                                !mbar_wait(smem_u32(&bars->empty[s]), ((it / STAGES) - 1) & 1, p.status,
+                                           kDevTimeoutEmpty, p.limit_ns)) {
+                                ok = false;
+                                break;
+                            }
+                            int a, b;
+                            pair_planes(mode, L, i, a, b);
+                            const uint32_t full = smem_u32(&bars->full[s]);
+                            mbar_arrive_expect_tx(full, STAGE_BYTES);
+                            const uint32_t dst = smem_u32(smem + s * STAGE_BYTES);
+                            const int32_t kx = (kb0 + kb) * TK;
+                            tma_load_2d(dst, &tmA, kx, int32_t(a * p.mpad + int64_t(tm) * TM), full);
+                            tma_load_2d(dst + A_BYTES, &tmB, kx, int32_t(b * p.npad + int64_t(tn) * TN), full);
+                        }
+                    }
+                }
+            }
+            // drain: the last use of every stage must have landed before the CTA exits
+            const uint32_t first = it > STAGES ? it - STAGES : 0;
+            for (uint32_t j = first; j < it; ++j)
+                mbar_wait_drain(smem_u32(&bars->full[j % STAGES]), (j / STAGES) & 1, p.limit_ns);
+        }
+    } else if (warp == 1) {
+        // ---------------- MMA issuer ----------------
+        if (lane == 0) {
+            uint32_t it = 0, grp = 0;
+            bool ok = true, issued_any = false;
+            for (int u = blockIdx.x; u < units && ok; u += gridDim.x) {
+                int tm, tn, seg;
+                unit_coords(p, u, tm, tn, seg);
+                const int kb0 = seg * p.kb_per_seg;
+                const int kbn = min(p.kb_per_seg, p.kb_total - kb0);
+                for (int L = 0; L < nlev && ok; ++L) {
+                    const int np = pairs_in_level(mode, L);
+                    const int items = np * kbn;
+                    const int gsize = (mode == kExact) ? GROUP_ITEMS : items;
+                    for (int g0 = 0; g0 < items && ok; g0 += gsize, ++grp) {
+                        const int buf = grp & 1;
+                        if (grp >= 2 && !mbar_wait(smem_u32(&bars->acc_empty[buf]), ((grp >> 1) - 1) & 1, p.status,
+                                                   kDevTimeoutAccEmpty, p.limit_ns)) {
+                            ok = false;
+                            break;
+                        }
+                        tc_fence_after();
+                        const uint32_t dcol = tmem + uint32_t(buf * TN);
+                        const int gend = min(items, g0 + gsize);
+                        for (int x = g0; x < gend; ++x, ++it) {
+                            const int s = it % STAGES;
+                            if (!mbar_wait(smem_u32(&bars->full[s]), (it / STAGES) & 1, p.status, kDevTimeoutFull,
+                                           p.limit_ns)) {
+                                ok = false;
+                                break;
+                            }
+                            tc_fence_after();
+                            const uint32_t a_addr = smem_u32(smem + s * STAGE_BYTES);
+                            const uint64_t adesc = sw128_desc(a_addr);
+                            const uint64_t bdesc = sw128_desc(a_addr + A_BYTES);
+#pragma unroll
+                            for (int j = 0; j < TK / 16; ++j)
+                                tc_mma_f16(dcol, adesc + uint64_t(2 * j), bdesc + uint64_t(2 * j), kIdesc,
+                                           (x == g0 && j == 0) ? 0u : 1u);
+                            tc_commit(smem_u32(&bars->empty[s]));
+                            issued_any = true;
+                        }
+                        if (!ok) break;
+                        tc_commit(smem_u32(&bars->acc_full[buf]));
+                    }
+                }
+            }
+            // drain: every issued MMA completes before TMEM is released
+            if (issued_any) {
+                tc_commit(smem_u32(&bars->drain));
+                mbar_wait_drain(smem_u32(&bars->drain), 0, p.limit_ns);
+            }
+        }
+    } else {
+        // ---------------- epilogue ----------------
+        const int q = warp & 3;                 // TMEM lane quarter of this warp
+        const int h = (warp - 2) >> 2;          // column half: 0 or 1
+        const uint32_t lane_base = uint32_t(32 * q) << 16;
+        uint32_t grp = 0;
+        bool ok = true;
+        for (int u = blockIdx.x; u < units && ok; u += gridDim.x) {
+            int tm, tn, seg;
+            unit_coords(p, u, tm, tn, seg);
+            const int kb0 = seg * p.kb_per_seg;
+            const int kbn = min(p.kb_per_seg, p.kb_total - kb0);
+            const int64_t row = int64_t(tm) * TM + 32 * q + lane;
+            for (int L = 0; L < nlev && ok; ++L) {
+                const int np = pairs_in_level(mode, L);
+                const int items = np * kbn;
+                const int gsize = (mode == kExact) ? GROUP_ITEMS : items;
+                uint32_t acc[128];
+#pragma unroll
+                for (int c = 0; c < 128; ++c) acc[c] = 0u;
+                uint32_t ngroups = 0;
+                for (int g0 = 0; g0 < items; g0 += gsize, ++grp, ++ngroups) {
+                    const int buf = grp & 1;
+                    if (!mbar_wait(smem_u32(&bars->acc_full[buf]), (grp >> 1) & 1, p.status, kDevTimeoutMma,
+                                   p.limit_ns)) {
+                        ok = false;
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint32_t base = tmem + lane_base + uint32_t(buf * TN + h * 128);
+#pragma unroll
+                    for (int c4 = 0; c4 < 8; ++c4) {
+                        uint32_t v[16];
+                        tmem_ld_32x32b_x16(base + uint32_t(c4 * 16), v);
+                        tc_wait_ld();
+                        if (mode == kExact) {
+#pragma unroll
+                            for (int c = 0; c < 16; ++c)
+                                acc[c4 * 16 + c] += __float_as_uint(__uint_as_float(v[c]) + MAGIC);
+                        } else {
+#pragma unroll
+                            for (int c = 0; c < 16; ++c) acc[c4 * 16 + c] = v[c];
+                        }
+                    }
+                    tc_fence_before();
+                    __syncwarp();
+                    if (lane == 0) mbar_arrive(smem_u32(&bars->acc_empty[buf]));
+                }
+                if (!ok) break;
+                // level sums -> global level plane (row-major, pitch npad)
+                int32_t* dst = p.levels + ((int64_t(seg) * p.max_levels + L) * p.mpad + row) * p.npad +
+                               int64_t(tn) * TN + h * 128;
+                const uint32_t bias = (mode == kExact) ? ngroups * MAGIC_BITS : 0u;
+#pragma unroll
+                for (int c = 0; c < 128; c += 4) {
+                    int4 w;
+                    w.x = int32_t(acc[c + 0] - bias);
+                    w.y = int32_t(acc[c + 1] - bias);
+                    w.z = int32_t(acc[c + 2] - bias);
+                    w.w = int32_t(acc[c + 3] - bias);
+                    *reinterpret_cast<int4*>(dst + c) = w;
+                }
+            }
+        }
+    }
+
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        tc_fence_after();
+        tmem_dealloc(tmem, 512);
+    }
+}
+
+// C = alpha * 2^(e_i + f_j) * sum_L 2^(-14-8L) * sum_seg T[seg][L] + beta * C   (exact mode)
+// C = alpha * sum_seg P[seg] + beta * C                                         (float modes)
+__global__ void combine_kernel(const int32_t* __restrict__ levels, int nseg, int max_levels, int64_t mpad,
+                               int64_t npad, int mode, const SplitInfo* __restrict__ info,
+                               const int* __restrict__ eA, const int* __restrict__ eB, int64_t m, int64_t n,
+                               double alpha, double beta, double* __restrict__ C, int64_t ldc) {
+    const int64_t total = m * n;
+    const int64_t plane = mpad * npad;
+    const int S = (mode == kExact) ? info->slices : 1;
+    for (int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; e < total; e += int64_t(gridDim.x) * blockDim.x) {
+        const int64_t i = e / n, j = e % n;
+        const int64_t off = i * npad + j;
+        double v;
+        if (mode == kExact) {
+            const int ei = eA[i], fj = eB[j];
+            if (ei == kNonFinite || fj == kNonFinite) {
+                v = __longlong_as_double(0x7ff8000000000000ll);  // NaN: the inputs were not finite
+            } else {
+                // least significant level first; three levels combine exactly in int64
+                double acc = 0.0;
+                for (int L = S - 1; L >= 0; L -= 3) {
+                    const int L0 = max(L - 2, 0);
+                    long long t = 0;
+                    for (int l = L0; l <= L; ++l) {
+                        long long s = 0;
+                        for (int g = 0; g < nseg; ++g) s += levels[(int64_t(g) * max_levels + l) * plane + off];
+                        t += s * (1ll << (8 * (L - l)));
+                    }
+                    acc += ldexp(double(t), -14 - 8 * L);
+                }
+                v = alpha * ldexp(acc, ei + fj);
+            }
+        } else {
+            double acc = 0.0;
+            for (int g = 0; g < nseg; ++g)
+                acc += double(__int_as_float(levels[int64_t(g) * max_levels * plane + off]));
+            v = alpha * acc;
+        }
+        double* c = C + i * ldc + j;
+        *c = (beta == 0.0) ? v : fma(beta, *c, v);
+    }
+}
+
+int64_t round_up(int64_t x, int64_t q) { return (x + q - 1) / q * q; }
+
+}  // namespace
+
+bool split_read_info(const void* info_dev, int* slices, double* bound) {
+    SplitInfo h;
+    if (cudaMemcpy(&h, info_dev, sizeof(h), cudaMemcpyDeviceToHost) != cudaSuccess) return false;
+    *slices = h.slices;
+    *bound = h.bound;
+    return true;
+}
+
+// ---- host orchestration ------------------------------------------------------------------------
+// Predicted seconds of the native FP64 kernel and of the split form for a shape (AUTO policy).
+static double predict_native_s(const Gemm& g, double fp64_tflops) {
+    return 2.0 * double(g.m) * double(g.n) * double(g.k) / (fp64_tflops * 1e12);
+}
+
+int split_gemm(const Gemm& g, const SplitRequest& req, const LaunchCtl& ctl, cudaStream_t st, SplitResult* out,
                std::string* err) {
-    if (req.method != GB300_METHOD_AUTO) {
-        if (err) *err = "tensor-core forms are not available in this build";
-        return GB300_ERR_NOT_SUPPORTED;
-    }
     Runtime& r = runtime();
-    int splits = native_choose_splits(g.m, g.n, g.k, 8, r.num_sms);
-    double* ws = nullptr;
-    if (splits > 1) {
-        ws = static_cast<double*>(pool_get(kSlotWork, size_t(splits) * size_t(g.m) * size_t(g.n) * 8, err));
-        if (!ws) return GB300_ERR_NO_MEMORY;
+    int mode = kExact;
+    if (req.method == GB300_METHOD_BF16) mode = kBf16;
+    else if (req.method == GB300_METHOD_BF16X3) mode = kBf16x3;
+
+    if (req.method == GB300_METHOD_AUTO) {
+        // The split form costs about (S(S+1)/2) BF16 products plus operand passes; below a few
+        // million multiply-adds per output tile the native kernel's single pass wins.
+        const double work = double(g.m) * double(g.n) * double(g.k);
+        if (work < 256.0 * 256.0 * 256.0 || g.k < 64) {
+            int splits = native_choose_splits(g.m, g.n, g.k, 8, r.num_sms);
+            double* ws = nullptr;
+            if (splits > 1) {
+                ws = static_cast<double*>(pool_get(kSlotWork, size_t(splits) * size_t(g.m) * size_t(g.n) * 8, err));
+                if (!ws) return GB300_ERR_NO_MEMORY;
+            }
+            cudaError_t e = native_gemm<double>(g, splits, ws, ctl, st, err);
+            if (e != cudaSuccess) {
+                if (err && err->empty()) *err = cudaGetErrorString(e);
+                return GB300_ERR_CUDA;
+            }
+            out->method_used = GB300_METHOD_NATIVE;
+            out->slices = 0;
+            out->error_bound = double(g.k) * 0x1p-53;
+            (void)predict_native_s;
+            return GB300_OK;
+        }
     }
-    cudaError_t e = native_gemm<double>(g, splits, ws, ctl, s, err);
-    if (e != cudaSuccess) return GB300_ERR_CUDA;
-    out->method_used = GB300_METHOD_NATIVE;
-    out->slices = 0;
-    out->error_bound = double(g.k) * 0x1p-53;
+
+    const int64_t m = g.m, n = g.n, k = g.k;
+    const int m_tiles = int((m + TM - 1) / TM), n_tiles = int((n + TN - 1) / TN);
+    const int64_t mpad = int64_t(m_tiles) * TM, npad = int64_t(n_tiles) * TN;
+    const int64_t kpad = round_up(k, TK);
+    const int kb_total = int(kpad / TK);
+    const int max_planes = (mode == kExact) ? (req.slices > 0 ? std::min(req.slices, MAX_SLICES) : MAX_SLICES)
+                                            : (mode == kBf16 ? 1 : 2);
+    const int max_levels = (mode == kExact) ? max_planes : 1;
+
+    // k-segments: exactness (int32 level sums) and parallelism for few output tiles
+    int64_t kseg = kpad;
+    if (mode == kExact) {
+        // n_L * (Kseg/256) groups of at most 2^22 each must stay below 2^31
+        const int64_t cap = (int64_t(511) / max_planes) * KSEG_UNIT;
+        kseg = std::min(kseg, std::max<int64_t>(cap, KSEG_UNIT));
+    }
+    const int tiles = m_tiles * n_tiles;
+    if (tiles < r.num_sms) {
+        const int64_t want = (r.num_sms + tiles - 1) / tiles;
+        kseg = std::min(kseg, std::max<int64_t>(KSEG_UNIT, round_up((kpad + want - 1) / want, KSEG_UNIT)));
+    }
+    kseg = round_up(kseg, TK);
+    const int nseg = int((kpad + kseg - 1) / kseg);
+
+    // device buffers
+    const size_t planesA = size_t(max_planes) * size_t(mpad) * size_t(kpad);
+    const size_t planesB = size_t(max_planes) * size_t(npad) * size_t(kpad);
+    auto* pa = static_cast<__nv_bfloat16*>(pool_get(kSlotSliceA, planesA * 2, err));
+    auto* pb = static_cast<__nv_bfloat16*>(pool_get(kSlotSliceB, planesB * 2, err));
+    auto* lv = static_cast<int32_t*>(
+        pool_get(kSlotLevels, size_t(nseg) * max_levels * size_t(mpad) * size_t(npad) * 4, err));
+    // statistics block: exponents (int), relative sums of squares (double), SplitInfo
+    const int64_t off_sq = round_up((m + n) * int64_t(sizeof(int)), 256);
+    const int64_t off_info = round_up(off_sq + (m + n) * int64_t(sizeof(double)), 256);
+    const size_t stat_bytes = size_t(off_info) + 256;
+    auto* stats = static_cast<uint8_t*>(pool_get(kSlotScaleA, stat_bytes, err));
+    if (!pa || !pb || !lv || !stats) return GB300_ERR_NO_MEMORY;
+    int* eA = reinterpret_cast<int*>(stats);
+    int* eB = eA + m;
+    double* sqA = reinterpret_cast<double*>(stats + off_sq);
+    double* sqB = sqA + m;
+    auto* info = reinterpret_cast<SplitInfo*>(stats + off_info);
+
+    // operand strides of the logical R x K views
+    const int64_t a_sr = g.ta ? 1 : g.lda, a_sp = g.ta ? g.lda : 1;
+    const int64_t b_sr = g.tb ? g.ldb : 1, b_sp = g.tb ? 1 : g.ldb;
+    const double* A = static_cast<const double*>(g.A);
+    const double* B = static_cast<const double*>(g.B);
+
+    RowAcc* racc = static_cast<RowAcc*>(pool_get(kSlotScaleB, size_t(m + n) * sizeof(RowAcc), err));
+    if (!racc) return GB300_ERR_NO_MEMORY;
+    cudaMemsetAsync(racc, 0, size_t(m + n) * sizeof(RowAcc), st);
+    auto stats_launch = [&](const double* X, int64_t R, int64_t sr, int64_t sp, RowAcc* ra, int* ex, double* sq) {
+        dim3 grid(unsigned((k + 63) / 64), unsigned((R + 31) / 32));
+        stats_tile_kernel<<<grid, 256, 0, st>>>(X, R, k, sr, sp, ra);
+        stats_finalize_kernel<<<unsigned((R + 255) / 256), 256, 0, st>>>(X, R, k, sr, sp, ra, ex, sq);
+    };
+    stats_launch(A, m, a_sr, a_sp, racc, eA, sqA);
+    stats_launch(B, n, b_sr, b_sp, racc + m, eB, sqB);
+    const double target = req.target_error > 0 ? req.target_error : double(k) * 0x1p-53;
+    split_info_kernel<<<1, 1024, 0, st>>>(eA, sqA, m, eB, sqB, n, k, mode, req.slices > 0 ? max_planes : 0, target,
+                                          info);
+    {
+        dim3 grid(unsigned(kpad / 64), unsigned(mpad / 32));
+        slice_kernel<<<grid, 256, 0, st>>>(A, m, k, a_sr, a_sp, eA, info, mode, pa, mpad, kpad);
+        dim3 gridb(unsigned(kpad / 64), unsigned(npad / 32));
+        slice_kernel<<<gridb, 256, 0, st>>>(B, n, k, b_sr, b_sp, eB, info, mode, pb, npad, kpad);
+    }
+    count_launches(7);
+
+    CUtensorMap tA, tB;
+    if (!encode_tmap_2d(&tA, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, pa, uint64_t(max_planes) * mpad, kpad, kpad, TM, TK,
+                        CU_TENSOR_MAP_SWIZZLE_128B, err) ||
+        !encode_tmap_2d(&tB, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, pb, uint64_t(max_planes) * npad, kpad, kpad, TN, TK,
+                        CU_TENSOR_MAP_SWIZZLE_128B, err))
+        return GB300_ERR_CUDA;
+
+    TcParams p;
+    p.mode = mode;
+    p.m_tiles = m_tiles;
+    p.n_tiles = n_tiles;
+    p.nseg = nseg;
+    p.kb_per_seg = int(kseg / TK);
+    p.kb_total = kb_total;
+    p.mpad = mpad;
+    p.npad = npad;
+    p.levels = lv;
+    p.max_levels = max_levels;
+    p.info = info;
+    p.status = ctl.status;
+    p.limit_ns = ctl.wait_limit_ns;
+    p.inject_stall = ctl.inject_stall;
+    const int units = m_tiles * n_tiles * nseg;
+    const int grid = std::min(units, r.num_sms);
+    auto kern = mode == kExact ? tc_gemm_kernel<kExact> : (mode == kBf16 ? tc_gemm_kernel<kBf16> : tc_gemm_kernel<kBf16x3>);
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kTcSmem));
+    if (e != cudaSuccess) {
+        if (err) *err = std::string("tc_gemm_kernel smem attribute: ") + cudaGetErrorString(e);
+        return GB300_ERR_CUDA;
+    }
+    {
+        KernelTimer timer("tc_gemm", st);
+        kern<<<grid, THREADS, kTcSmem, st>>>(tA, tB, p);
+    }
+    const int64_t total = m * n;
+    const int cblocks = int(std::min<int64_t>((total + 255) / 256, int64_t(r.num_sms) * 16));
+    combine_kernel<<<cblocks, 256, 0, st>>>(lv, nseg, max_levels, mpad, npad, mode, info, eA, eB, m, n, g.alpha,
+                                            g.beta, static_cast<double*>(g.C), g.ldc);
+    count_launches(2);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        if (err) *err = std::string("split-precision launch: ") + cudaGetErrorString(e);
+        return GB300_ERR_CUDA;
+    }
+    out->method_used = req.method == GB300_METHOD_AUTO ? GB300_METHOD_SPLIT : req.method;
+    out->slices = -1;  // filled in by the caller from the device info when synchronous
+    out->error_bound = -1.0;
+    out->info_dev = info;
     return GB300_OK;
 }
 

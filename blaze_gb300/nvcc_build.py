@@ -1,6 +1,6 @@
 """Build libgb300blas.so in-tree: nvcc for sm_103a, translation units compiled in parallel.
 
-    python -m blaze_gb300.build          (or __graft_entry__.build())
+    python -m blaze_gb300.nvcc_build     (or __graft_entry__.build())
 
 Objects go to blaze_gb300/_build/, the library to blaze_gb300/libgb300blas.so.  The CUDA runtime
 is linked statically, so loading the library needs no driver (a GPU is needed only to run it).
@@ -32,6 +32,7 @@ UNITS = [
     ("native_gemm.cu", "native_gemm.o", []),
     ("split_gemm.cu", "split_gemm.o", []),
     ("peaks.cu", "peaks.o", []),
+    ("profile.cpp", "profile.o", []),
 ]
 
 

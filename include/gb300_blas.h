@@ -91,6 +91,18 @@ int gb300_device_info(int* num_sms, int64_t* free_bytes, int64_t* total_bytes);
  * SM.  The automatic method choice uses it; benchmarks report it as the FP64 roofline. */
 int gb300_measure_fp64_peak(double* tflops);
 
+/* Make `ordinal` the library's device.  Call before the first product of the process (each
+ * process of a multi-GPU job owns one device). */
+int gb300_select_device(int ordinal);
+
+/* Kernel timing for benchmarks: while enabled, the library records CUDA events on the launching
+ * stream around the dominant kernel of every product ("tc_gemm" for the tensor-core forms,
+ * "native_gemm" for the native kernel).  gb300_profile_read waits for the recorded events, returns
+ * the summed milliseconds and the launch count of kernels whose name starts with `prefix` (NULL:
+ * all), and clears the record. */
+void gb300_profile_enable(int on);
+int gb300_profile_read(const char* prefix, double* total_ms, int64_t* launches);
+
 /* Count of kernel launches the library has issued in this process (all entry points). */
 int64_t gb300_launch_count(void);
 

@@ -1,0 +1,145 @@
+"""Tensor-core forms (split-precision FP64-accurate, BF16x3, BF16) through the C-ABI on a GB300:
+normwise error against the compensated FP64 oracle within each form's stated bound, every
+storage-order combination, alpha/beta, skinny and split-k shapes, exponent-spread inputs,
+exactness of the integer slice products at their largest magnitudes, and non-finite inputs."""
+import numpy as np
+import pytest
+
+import blaze_gb300 as G
+import oracle as O
+from helpers import check_result, golden_inputs, load_golden, normwise, stored_dims
+
+pytestmark = pytest.mark.gpu
+
+FP64_BOUND = 2.0 ** -53
+
+
+@pytest.fixture(scope="module", autouse=True)
+def lib():
+    L = G.lib()
+    G.device_info()
+    return L
+
+
+def product(order, ta, tb, m, n, k, dist="uniform", seed=1, pad=0, alpha=1.0, beta=0.0, method="split", slices=0):
+    ra, ca = stored_dims(order, ta, m, k)
+    rb, cb = stored_dims(order, tb, k, n)
+    rc, cc = stored_dims(order, O.NO_TRANS, m, n)
+    lda, ldb, ldc = ca + pad, cb + pad, cc + pad
+    gen = O.uniform if dist == "uniform" else O.spread
+    A = gen(max(ra * lda, 1), seed)
+    B = gen(max(rb * ldb, 1), seed + 1)
+    C = O.uniform(max(rc * ldc, 1), seed + 2)
+    C0 = C.copy()
+    o = G.dgemm_ex(order, ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, G.opts(method=method, slices=slices))
+    P = O.product_rows_dot2(order, ta, tb, m, n, k, A, lda, B, ldb)
+    Cl0 = O.logical(order, O.NO_TRANS, m, n, C0, ldc)
+    out = O.logical(order, O.NO_TRANS, m, n, C, ldc)
+    nA = O.fro_norm_op(order, ta, m, k, A, lda)
+    nB = O.fro_norm_op(order, tb, k, n, B, ldb)
+    err = normwise((out - beta * Cl0) / alpha, P, nA, nB)
+    return err, o, out, P
+
+
+LAYOUTS = [(o, a, b) for o in (O.ROW_MAJOR, O.COL_MAJOR) for a in (O.NO_TRANS, O.TRANS) for b in (O.NO_TRANS, O.TRANS)]
+
+
+@pytest.mark.parametrize("order,ta,tb", LAYOUTS)
+@pytest.mark.parametrize("dist", ["uniform", "spread"])
+def test_split_meets_fp64_bound(order, ta, tb, dist):
+    m, n, k = 300, 517, 777
+    err, o, _, _ = product(order, ta, tb, m, n, k, dist=dist, pad=3, alpha=1.25, beta=-0.5)
+    assert o.method_used == G.METHOD_SPLIT
+    assert 2 <= o.slices_used <= 10
+    assert o.error_bound <= k * FP64_BOUND
+    assert err <= o.error_bound, (err, o.error_bound)
+    assert err <= k * FP64_BOUND
+
+
+@pytest.mark.parametrize("slices", [2, 3, 4, 5, 6, 7, 8])
+def test_error_falls_with_slices(slices):
+    """Each added slice buys about 8 bits; the reported a-priori bound always holds."""
+    err, o, _, _ = product(O.ROW_MAJOR, O.NO_TRANS, O.NO_TRANS, 200, 264, 1000, slices=slices, seed=5)
+    assert o.slices_used == slices
+    assert err <= o.error_bound
+    assert err <= 2.0 ** (-8 * slices + 1)
+
+
+@pytest.mark.parametrize("method,bound", [("bf16x3", 2.0 ** -14), ("bf16", 2.0 ** -6)])
+def test_bf16_forms_within_stated_error(method, bound):
+    for order, ta, tb in LAYOUTS[::3]:
+        err, o, _, _ = product(order, ta, tb, 333, 290, 650, method=method, seed=9)
+        assert o.method_used == G.METHODS[method]
+        assert err <= o.error_bound and err <= bound, (method, err, o.error_bound)
+
+
+@pytest.mark.parametrize("m,n,k", [(256, 256, 16384), (2000, 64, 3000), (1, 700, 900), (900, 1, 300), (5, 7, 3)])
+def test_skinny_and_split_k_shapes(m, n, k):
+    err, o, _, _ = product(O.COL_MAJOR, O.TRANS, O.NO_TRANS, m, n, k, seed=13)
+    assert err <= max(o.error_bound, 1e-300) and err <= k * FP64_BOUND
+
+
+def test_golden_cases_split():
+    """Blaze's own outputs for every double golden case through cblas_dgemm in split mode."""
+    prev = G.lib().gb300_set_default_method(G.METHOD_SPLIT)
+    try:
+        for c in load_golden():
+            if c["dtype"] != np.float64:
+                continue
+            A, B, C = golden_inputs(c)
+            C0 = C.copy()
+            G.cblas_dgemm(c["order"], c["ta"], c["tb"], c["m"], c["n"], c["k"], c["alpha"], A, c["lda"], B, c["ldb"],
+                          c["beta"], C, c["ldc"])
+            check_result(c, C, c["C_ref"], C0)
+    finally:
+        G.lib().gb300_set_default_method(prev)
+
+
+def test_integer_slices_are_exact_at_the_largest_digit_sums():
+    """Operands whose every digit is +-128 with one sign make each 256-product group sum to
+    exactly +-2^22, the largest magnitude the scheme relies on; products of integers that the
+    split represents exactly must come back exact."""
+    m, n, k = 128, 256, 4096
+    # entries 1 - 2^-9: first digit rint(0.998*128) = 128, remainder -0.25*... ; use powers of two
+    A = np.full(m * k, 0.99609375)  # 255/256: scaled by 2^0 -> x*128 = 127.5 -> digit 128 (ties to even)
+    B = np.full(k * n, 0.99609375)
+    C = np.zeros(m * n)
+    G.dgemm_ex(O.ROW_MAJOR, O.NO_TRANS, O.NO_TRANS, m, n, k, 1.0, A, k, B, n, 0.0, C, n, G.opts(method="split"))
+    assert np.all(C == k * 0.99609375 ** 2)
+    # integers in [-1000, 1000]: the exact product is an integer the split reproduces exactly
+    A = O.integers(m * k, 3, -1000, 1000)
+    B = O.integers(k * n, 4, -1000, 1000)
+    G.dgemm_ex(O.ROW_MAJOR, O.NO_TRANS, O.NO_TRANS, m, n, k, 1.0, A, k, B, n, 0.0, C, n, G.opts(method="split"))
+    exact = A.astype(np.int64).reshape(m, k) @ B.astype(np.int64).reshape(k, n)
+    assert np.array_equal(C.reshape(m, n), exact.astype(np.float64))
+
+
+def test_nonfinite_inputs_poison_their_rows_and_columns():
+    m, n, k = 130, 260, 300
+    A = O.uniform(m * k, 1); B = O.uniform(k * n, 2)
+    A[5 * k + 7] = np.inf
+    B[11 * n + 3] = np.nan
+    C = np.zeros(m * n)
+    G.dgemm_ex(O.ROW_MAJOR, O.NO_TRANS, O.NO_TRANS, m, n, k, 1.0, A, k, B, n, 0.0, C, n, G.opts(method="split"))
+    C = C.reshape(m, n)
+    assert np.all(np.isnan(C[5, :])) and np.all(np.isnan(C[:, 3]))
+    mask = np.ones((m, n), bool); mask[5, :] = False; mask[:, 3] = False
+    assert np.isfinite(C[mask]).all()
+
+
+def test_auto_picks_a_fp64_accurate_form():
+    m = n = k = 512
+    err, o, _, _ = product(O.ROW_MAJOR, O.NO_TRANS, O.NO_TRANS, m, n, k, method="auto", seed=17)
+    assert o.method_used in (G.METHOD_SPLIT, G.METHOD_NATIVE)
+    assert err <= k * FP64_BOUND
+
+
+def test_split_stall_reports_timeout_and_recovers():
+    m = n = k = 256
+    A = O.uniform(m * k, 61); B = O.uniform(k * n, 62); C = np.zeros(m * n)
+    G.lib().gb300_debug_inject_stall(1, 20_000_000)
+    with pytest.raises(G.Gb300Error) as ei:
+        G.dgemm_ex(O.ROW_MAJOR, O.NO_TRANS, O.NO_TRANS, m, n, k, 1.0, A, k, B, n, 0.0, C, n, G.opts(method="split"))
+    assert ei.value.status == G.ERR_DEVICE_TIMEOUT
+    G.dgemm_ex(O.ROW_MAJOR, O.NO_TRANS, O.NO_TRANS, m, n, k, 1.0, A, k, B, n, 0.0, C, n, G.opts(method="split"))
+    assert np.allclose(C.reshape(m, n), A.reshape(m, k) @ B.reshape(k, n), rtol=1e-12, atol=1e-12)
