@@ -1,0 +1,46 @@
+"""Compile the Blaze drop-in test program (needs the reference headers; test infrastructure).
+
+    build(kind)   kind = "stub": linked against stub_cblas.cpp (CPU stand-in that logs calls)
+                  kind = "lib":  linked against blaze_gb300/libgb300blas.so
+Returns the executable path, or None when the Blaze headers are not available here.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+OUT = os.path.join(HERE, "_build")
+REF = os.environ.get("BLAZE_INCLUDE", "/root/reference")
+
+FLAGS = ["-std=c++17", "-O1", "-DBLAZE_BLAS_MODE=1", "-DBLAZE_BLAS_IS_PARALLEL=1",
+         "-DBLAZE_BLAS_INCLUDE_FILE=<gb300_cblas.h>", "-DGB300_BLAS_THROW", "-I" + os.path.join(ROOT, "include")]
+
+
+def available() -> bool:
+    return os.path.isdir(os.path.join(REF, "blaze")) and shutil.which("g++") is not None
+
+
+def build(kind: str) -> str | None:
+    if not available():
+        return None
+    os.makedirs(OUT, exist_ok=True)
+    exe = os.path.join(OUT, f"dropin_{kind}")
+    srcs = [os.path.join(HERE, "dropin_main.cpp")]
+    deps = list(srcs) + [os.path.join(ROOT, "include", "gb300_cblas.h")]
+    extra = []
+    if kind == "stub":
+        srcs.append(os.path.join(HERE, "stub_cblas.cpp"))
+        deps.append(srcs[-1])
+    else:
+        lib_dir = os.path.join(ROOT, "blaze_gb300")
+        extra = ["-L" + lib_dir, "-lgb300blas", "-Wl,-rpath," + lib_dir]
+    if os.path.exists(exe) and all(os.path.getmtime(exe) >= os.path.getmtime(d) for d in deps):
+        return exe
+    cmd = ["g++", *FLAGS, "-isystem", REF, *srcs, "-o", exe, *extra]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("Blaze drop-in build failed:\n" + " ".join(cmd) + "\n" + r.stderr[-4000:])
+    return exe

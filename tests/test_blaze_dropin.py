@@ -1,0 +1,81 @@
+"""Blaze itself, built in BLAS mode with include/gb300_cblas.h as its BLAS header.
+
+Where the reference headers exist (the build container), a Blaze program computing
+`C = A*B`, `+=`, `-=` and `s*(A*B)` for every storage-order class and a CustomMatrix is compiled
+(1) against a logging CPU stub, to check that every product reaches cblas_dgemm with the CBLAS
+arguments blaze::gemm() derives (blaze/math/blas/gemm.h:115-131) and that the results are right,
+(2) against the stub with an injected failure and (3) against libgb300blas.so on a host without a
+GPU, to check that a library error reaches the Blaze caller as std::runtime_error (no silent CPU
+result).  The recorded calls are also a committed fixture (tests/golden/blaze_calls.txt) that
+the GPU tests replay."""
+import os
+import subprocess
+import sys
+
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(HERE, "blaze_dropin"))
+import build as dropin  # noqa: E402
+
+pytestmark = pytest.mark.skipif(not dropin.available(), reason="Blaze headers are not present on this host")
+
+EXPECTED_TRANS = {  # label -> (order, transA, transB): order from C, trans = (SO_C != SO_X)
+    "rr_r": (101, 111, 111), "rc_r": (101, 111, 112), "cr_r": (101, 112, 111), "cc_r": (101, 112, 112),
+    "rr_c": (102, 112, 112), "cc_c": (102, 111, 111), "custom": (101, 111, 111),
+}
+EXPECTED_AB = {"assign": (1.0, 0.0), "add": (1.0, 1.0), "sub": (-1.0, 1.0), "scaled": (2.5, 0.0)}
+
+
+def run(exe, env):
+    r = subprocess.run([exe], capture_output=True, text=True, env=dict(os.environ, **env), timeout=120)
+    assert r.returncode == 0, r.stderr
+    return [ln.split() for ln in r.stdout.splitlines() if ln.strip()]
+
+
+def test_blaze_products_reach_cblas_dgemm_with_the_right_arguments(tmp_path):
+    exe = dropin.build("stub")
+    log = tmp_path / "log.txt"
+    out = run(exe, {"GB300_STUB_LOG": str(log)})
+    assert len(out) == 25
+    for fields in out:
+        assert fields[1] == "status=ok", fields
+        assert float(fields[2].split("=")[1]) <= 1e-12, fields
+    calls = [ln.split() for ln in log.read_text().splitlines()]
+    assert len(calls) == len(out)
+    for fields, call in zip(out, calls):
+        label, op = fields[0].split("/")
+        assert call[0] == "dgemm"
+        assert tuple(int(x) for x in call[1:4]) == EXPECTED_TRANS[label], (fields, call)
+        assert (float(call[7]), float(call[10])) == EXPECTED_AB[op], (fields, call)
+
+
+def test_library_errors_surface_as_exceptions_in_blaze():
+    exe = dropin.build("stub")
+    out = run(exe, {"GB300_STUB_FAIL": "1"})
+    assert all(f[1] == "status=exception" for f in out)
+    assert all("injected failure" in " ".join(f) for f in out)
+
+
+def test_real_library_without_gpu_raises_instead_of_computing_on_the_cpu():
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    import blaze_gb300 as G
+    if not os.path.exists(G.LIB_PATH):
+        G.build()
+    exe = dropin.build("lib")
+    out = run(exe, {})
+    assert all(f[1] == "status=exception" for f in out), out
+    assert all("no CUDA device" in " ".join(f) for f in out)
+
+
+def test_recorded_call_fixture_matches_blaze():
+    exe = dropin.build("stub")
+    import tempfile
+    with tempfile.TemporaryDirectory() as d:
+        log = os.path.join(d, "log.txt")
+        run(exe, {"GB300_STUB_LOG": log})
+        fresh = open(log).read().splitlines()
+    committed = open(os.path.join(HERE, "golden", "blaze_calls.txt")).read().splitlines()
+    assert fresh == committed
