@@ -92,6 +92,9 @@ def lib() -> ct.CDLL:
     L.gb300_measure_fp64_peak.argtypes = [ct.POINTER(ct.c_double)]
     L.gb300_measure_fp64_peak.restype = ct.c_int
     L.gb300_synchronize.restype = ct.c_int
+    L.gb300_dgemm_native_noalloc.argtypes = [ct.c_int, ct.c_int, ct.c_int, I64, I64, I64, D, VP, I64, VP, I64, D,
+                                             VP, I64, VP]
+    L.gb300_dgemm_native_noalloc.restype = ct.c_int
     L.gb300_select_device.argtypes = [ct.c_int]
     L.gb300_select_device.restype = ct.c_int
     L.gb300_profile_enable.argtypes = [ct.c_int]
@@ -173,6 +176,13 @@ def cblas_sgemm(order, transA, transB, m, n, k, alpha, A, lda, B, ldb, beta, C, 
     st, msg = last_error()
     if st != OK:
         raise Gb300Error(st, msg)
+
+
+def dgemm_native_noalloc(order, transA, transB, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc,
+                         stream: int | None = None) -> None:
+    """The allocation-free native product (device operands; fixed in-library scratch)."""
+    check(lib().gb300_dgemm_native_noalloc(order, transA, transB, m, n, k, alpha, _addr(A), lda, _addr(B), ldb,
+                                           beta, _addr(C), ldc, stream))
 
 
 def device_info() -> tuple[int, int, int]:

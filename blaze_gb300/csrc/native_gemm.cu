@@ -21,7 +21,10 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <mutex>
 #include <string>
+
+#include "../../include/gb300_blas.h"
 
 #include "gb300_internal.h"
 #include "ptx.cuh"
@@ -341,3 +344,155 @@ template cudaError_t native_gemm<double>(const Gemm&, int, double*, const Launch
 template cudaError_t native_gemm<float>(const Gemm&, int, float*, const LaunchCtl&, cudaStream_t, std::string*);
 
 }  // namespace gb
+
+// =============================================================================================
+//  Allocation-free entry point (gb300_dgemm_native_noalloc)
+// =============================================================================================
+// Some callers must not allocate device memory on their own: a host framework that owns every
+// byte of device memory through its own pool or budget, a latency-critical loop in which
+// cudaMalloc/cudaFree (which can synchronize the device) is not allowed, or a plugin host that
+// forbids allocations after start-up.  For them this entry point runs the native kernel with its
+// split-k scratch taken from a fixed array compiled into the library instead of the device pool.
+//
+//   * The array is a file-scope static __device__ variable of kNoAllocScratchBytes (16 MiB).
+//     Every GPU on which the library's device code is loaded holds it until the process exits.
+//   * Its device address is looked up once per device with cudaGetSymbolAddress, on the first
+//     call made while that device is current; that first call should therefore come before any
+//     stream capture.  Host code must never pass the symbol itself to a kernel: on the host it is
+//     only a stand-in, not a device address.
+//   * The first 256 bytes hold the kernel status word (cleared before every launch); the rest
+//     holds split-k partial tiles, which the kernel writes in full before reading them.
+//   * All calls share the array, so two calls whose kernels overlapped on the GPU would race on
+//     it.  The entry point therefore serializes its callers with a process-wide lock and returns
+//     only after its kernels have finished on `stream`.
+//   * Products whose split-k partials do not fit are rejected with GB300_ERR_INVALID_ARG; nothing
+//     is allocated, including by the CUDA runtime calls made here.
+namespace gb {
+namespace {
+
+constexpr size_t kNoAllocScratchBytes = size_t(16) << 20;
+constexpr size_t kNoAllocStatusBytes = 256;
+constexpr int kNoAllocMaxDevices = 64;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+std::mutex g_noalloc_mu;
+void* g_noalloc_addr[kNoAllocMaxDevices] = {};
+
+// Device address of g_noalloc_scratch on the current device (set up on first use per device).
+int noalloc_scratch(void** out, std::string* err) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) {
+        *err = std::string("cudaGetDevice: ") + cudaGetErrorString(e);
+        return GB300_ERR_NO_DEVICE;
+    }
+    if (dev < 0 || dev >= kNoAllocMaxDevices) {
+        *err = "device ordinal " + std::to_string(dev) + " is beyond the supported " + std::to_string(kNoAllocMaxDevices);
+        return GB300_ERR_NO_DEVICE;
+    }
+    if (!g_noalloc_addr[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || p == nullptr) {
+            cudaGetLastError();
+            *err = std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e);
+            return GB300_ERR_CUDA;
+        }
+        g_noalloc_addr[dev] = p;
+    }
+    *out = g_noalloc_addr[dev];
+    return GB300_OK;
+}
+
+bool device_resident(const void* p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+}  // namespace
+}  // namespace gb
+
+extern "C" int gb300_dgemm_native_noalloc(int order, int transA, int transB, int64_t m, int64_t n, int64_t k,
+                                          double alpha, const double* A, int64_t lda, const double* B, int64_t ldb,
+                                          double beta, double* C, int64_t ldc, void* stream) {
+    using namespace gb;
+    auto fail = [](int st, const std::string& msg) {
+        set_error(st, "gb300_dgemm_native_noalloc: " + msg);
+        return st;
+    };
+    if (order != 101 && order != 102) return fail(GB300_ERR_INVALID_ARG, "parameter 1 (order) is invalid");
+    auto valid_trans = [](int t) { return t == 111 || t == 112 || t == 113; };
+    if (!valid_trans(transA)) return fail(GB300_ERR_INVALID_ARG, "parameter 2 (transA) is invalid");
+    if (!valid_trans(transB)) return fail(GB300_ERR_INVALID_ARG, "parameter 3 (transB) is invalid");
+    if (m < 0 || n < 0 || k < 0) return fail(GB300_ERR_INVALID_ARG, "negative dimension");
+    const bool tA = transA != 111, tB = transB != 111, rm = order == 101;
+    if (lda < std::max<int64_t>(1, rm ? (tA ? m : k) : (tA ? k : m)))
+        return fail(GB300_ERR_INVALID_ARG, "parameter 9 (lda) is too small");
+    if (ldb < std::max<int64_t>(1, rm ? (tB ? k : n) : (tB ? n : k)))
+        return fail(GB300_ERR_INVALID_ARG, "parameter 11 (ldb) is too small");
+    if (ldc < std::max<int64_t>(1, rm ? n : m)) return fail(GB300_ERR_INVALID_ARG, "parameter 14 (ldc) is too small");
+    clear_error();
+    if (m == 0 || n == 0) return GB300_OK;
+    if ((alpha == 0.0 || k == 0) && beta == 1.0) return GB300_OK;
+    const bool product = alpha != 0.0 && k > 0;
+    if (product && (!device_resident(A) || !device_resident(B)))
+        return fail(GB300_ERR_INVALID_ARG, "A and B must be device (or managed) memory");
+    if (!device_resident(C)) return fail(GB300_ERR_INVALID_ARG, "C must be device (or managed) memory");
+
+    Gemm g;
+    if (rm) {
+        g.m = m; g.n = n; g.k = k; g.ta = tA; g.tb = tB;
+        g.A = A; g.lda = lda; g.B = B; g.ldb = ldb;
+    } else {
+        g.m = n; g.n = m; g.k = k; g.ta = tB; g.tb = tA;
+        g.A = B; g.lda = ldb; g.B = A; g.ldb = lda;
+    }
+    g.C = C; g.ldc = ldc;
+    if (!product) g.k = 0;
+    g.alpha = alpha;
+    g.beta = beta;
+    auto tma_ok = [](const void* p, int64_t ld) {
+        return reinterpret_cast<uintptr_t>(p) % 16 == 0 && (ld * 8) % 16 == 0;
+    };
+    if (product && (!tma_ok(g.A, g.lda) || !tma_ok(g.B, g.ldb)))
+        return fail(GB300_ERR_INVALID_ARG,
+                    "A and B need 16-byte aligned bases and even leading dimensions (realigning them would "
+                    "need device memory; use gb300_dgemm_ex)");
+
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    std::string err;
+    void* scratch = nullptr;
+    int st = noalloc_scratch(&scratch, &err);
+    if (st != GB300_OK) return fail(st, err);
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
+        return fail(GB300_ERR_NO_DEVICE, "cannot query the SM count");
+    int splits = g.k > 0 ? native_choose_splits(g.m, g.n, g.k, 8, sms) : 1;
+    const size_t need = splits > 1 ? size_t(splits) * size_t(g.m) * size_t(g.n) * sizeof(double) : 0;
+    if (need > kNoAllocScratchBytes - kNoAllocStatusBytes)
+        return fail(GB300_ERR_INVALID_ARG,
+                    "the product needs " + std::to_string(need) + " bytes of split-k scratch; the allocation-free "
+                    "entry point holds " + std::to_string(kNoAllocScratchBytes - kNoAllocStatusBytes) +
+                    " (use gb300_dgemm_ex)");
+    auto* status = static_cast<int*>(scratch);
+    auto* ws = reinterpret_cast<double*>(static_cast<unsigned char*>(scratch) + kNoAllocStatusBytes);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    cudaError_t e = cudaMemsetAsync(status, 0, sizeof(int), s);
+    if (e != cudaSuccess) return fail(GB300_ERR_CUDA, std::string("status reset: ") + cudaGetErrorString(e));
+    LaunchCtl ctl;
+    ctl.status = status;
+    e = native_gemm<double>(g, splits, splits > 1 ? ws : nullptr, ctl, s, &err);
+    if (e != cudaSuccess) return fail(GB300_ERR_CUDA, err.empty() ? cudaGetErrorString(e) : err);
+    int h = 0;
+    e = cudaMemcpyAsync(&h, status, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return fail(GB300_ERR_CUDA, std::string("kernel failed: ") + cudaGetErrorString(e));
+    if (h != 0) return fail(GB300_ERR_DEVICE_TIMEOUT, "a device-side wait ran out (code " + std::to_string(h) + ")");
+    return GB300_OK;
+}

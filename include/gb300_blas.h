@@ -109,6 +109,20 @@ int64_t gb300_launch_count(void);
 /* Wait until all work the library queued on its own stream has finished. */
 int gb300_synchronize(void);
 
+/* Allocation-free variant of the native FP64 product, for callers that cannot allocate device
+ * memory themselves (a host framework that owns all device memory through its own pool or
+ * budget, or a latency-critical loop where cudaMalloc/cudaFree and their implicit device
+ * synchronization are not allowed).  It has no counterpart in the reference.
+ * Operands and C must be device (or managed) memory with 16-byte aligned bases and even leading
+ * dimensions.  The split-k scratch comes from a fixed 16 MiB array compiled into the library (held
+ * on every GPU that loads the library until exit); products that need more are rejected with
+ * GB300_ERR_INVALID_ARG.  The first call on a device looks up that array's device address, so
+ * make it before any stream capture.  Calls share the array: the function serializes its callers
+ * and returns after its kernels finished on `stream` (NULL: the legacy default stream). */
+int gb300_dgemm_native_noalloc(int order, int transA, int transB, int64_t m, int64_t n, int64_t k,
+                               double alpha, const double* A, int64_t lda, const double* B,
+                               int64_t ldb, double beta, double* C, int64_t ldc, void* stream);
+
 /* Test hooks for failure detection (no fault is involved): the next `count` native-kernel
  * launches run with their TMA producer disabled and their waits limited to `limit_ns`, so they
  * end with GB300_ERR_DEVICE_TIMEOUT.  count = 0 clears the hook. */
