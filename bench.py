@@ -47,6 +47,7 @@ def parse():
     ap.add_argument("--seed", type=int, default=42)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-native", action="store_true", help="skip the native FP64 comparison")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end C-ABI leg")
     return ap.parse_args()
 
 
@@ -202,6 +203,25 @@ def reference_arm(args, dist: Dist):
 
 
 # ---- GPU arm -----------------------------------------------------------------------------------------
+def e2e_leg(G, hA, hB, n, flops, args, dist):
+    """cblas_dgemm on pinned host buffers: H2D of A and B, the product, D2H of C per step."""
+    import torch
+    pA = hA.pin_memory()
+    pB = hB.pin_memory()
+    pC = torch.empty(n * n, dtype=torch.float64).pin_memory()
+    G.cblas_dgemm(G.RowMajor, G.NoTrans, G.NoTrans, n, n, n, 1.0, pA, n, pB, n, 0.0, pC, n)  # warm-up
+    e2e_steps = max(2, min(args.steps, 5))
+    dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        G.cblas_dgemm(G.RowMajor, G.NoTrans, G.NoTrans, n, n, n, 1.0, pA, n, pB, n, 0.0, pC, n)
+    t_e2e = (time.perf_counter() - t0) / e2e_steps
+    t_e2e = dist.max(t_e2e)
+    return {"value": round(flops * dist.world / t_e2e / 1e12, 4), "unit": UNIT,
+            "h2d_bytes_per_step": 2 * n * n * 8, "d2h_bytes_per_step": n * n * 8, "steps": e2e_steps,
+            "ms_per_step": round(t_e2e * 1e3, 3), "call": "cblas_dgemm (default method: auto -> split)"}
+
+
 def ours(args, dist: Dist):
     import numpy as np
     import torch
@@ -270,8 +290,8 @@ def ours(args, dist: Dist):
 
     # native FP64 on the same product (one timed product after one warm-up)
     native = None
-    fp64_peak = G.measure_fp64_peak()
     if not args.no_native:
+        fp64_peak = G.measure_fp64_peak()
         with torch.cuda.stream(s):
             product("native")
             s.synchronize()
@@ -290,22 +310,12 @@ def ours(args, dist: Dist):
                   "normwise_error": err_native}
 
     # e2e: the drop-in C-ABI call with pinned host buffers, copies inside the timed region
-    pA = hA.pin_memory()
-    pB = hB.pin_memory()
-    pC = torch.empty(n * n, dtype=torch.float64).pin_memory()
-    G.cblas_dgemm(G.RowMajor, G.NoTrans, G.NoTrans, n, n, n, 1.0, pA, n, pB, n, 0.0, pC, n)  # warm-up
-    e2e_steps = max(2, min(args.steps, 5))
-    dist.barrier()
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        G.cblas_dgemm(G.RowMajor, G.NoTrans, G.NoTrans, n, n, n, 1.0, pA, n, pB, n, 0.0, pC, n)
-    t_e2e = (time.perf_counter() - t0) / e2e_steps
-    t_e2e = dist.max(t_e2e)
-    e2e = {"value": round(flops * dist.world / t_e2e / 1e12, 4), "unit": UNIT,
-           "h2d_bytes_per_step": 2 * n * n * 8, "d2h_bytes_per_step": n * n * 8, "steps": e2e_steps,
-           "ms_per_step": round(t_e2e * 1e3, 3), "call": "cblas_dgemm (default method: auto -> split)"}
+    e2e = None
+    if not args.no_e2e:
+        e2e = e2e_leg(G, hA, hB, n, flops, args, dist)
 
     peaks, peaks_src = read_peaks()
+
     pairs = info.slices_used * (info.slices_used + 1) // 2
     tc_flops = pairs * flops  # BF16 tensor operations of the slice products
     tc_ms = ms_tc / max(n_tc, 1)

@@ -52,6 +52,7 @@
 #include <algorithm>
 #include <cmath>
 #include <string>
+#include <type_traits>
 
 #include "../../include/gb300_blas.h"
 #include "gb300_internal.h"
@@ -110,45 +111,62 @@ struct RowAcc {
 
 __global__ void stats_tile_kernel(const double* __restrict__ X, int64_t R, int64_t K, int64_t sr, int64_t sp,
                                   RowAcc* __restrict__ acc) {
-    __shared__ double tile[32][65];
+    __shared__ unsigned long long tile[32][65];
     const int64_t r0 = int64_t(blockIdx.y) * 32, p0 = int64_t(blockIdx.x) * 64;
     const int t = threadIdx.x;  // 256 threads
+    const unsigned long long* Xb = reinterpret_cast<const unsigned long long*>(X);
     if (sp == 1) {
         for (int e = t; e < 32 * 64; e += 256) {
             const int rr = e / 64, pp = e % 64;
             const int64_t r = r0 + rr, p = p0 + pp;
-            tile[rr][pp] = (r < R && p < K) ? X[r * sr + p] : 0.0;
+            tile[rr][pp] = (r < R && p < K) ? Xb[r * sr + p] : 0ull;
         }
     } else {
         for (int e = t; e < 32 * 64; e += 256) {
             const int pp = e / 32, rr = e % 32;
             const int64_t r = r0 + rr, p = p0 + pp;
-            tile[rr][pp] = (r < R && p < K) ? X[r * sr + p * sp] : 0.0;
+            tile[rr][pp] = (r < R && p < K) ? Xb[r * sr + p * sp] : 0ull;
         }
     }
     __syncthreads();
     const int rr = t / 8, pp0 = (t % 8) * 8;
-    double mx = 0.0, sq = 0.0;
+    // max |x| and non-finite flag with integer operations on the bit patterns
+    unsigned long long mx = 0;
     int bad = 0;
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
-        const double v = tile[rr][pp0 + q];
-        bad |= !isfinite(v);
-        mx = fmax(mx, fabs(v));
-        sq = fma(v, v, sq);
+        const unsigned long long a = tile[rr][pp0 + q] & 0x7fffffffffffffffull;
+        bad |= (a >> 52) == 0x7ff;
+        mx = a > mx ? a : mx;
     }
-    // reduce over the 8 threads of the row (consecutive lanes)
 #pragma unroll
     for (int o = 4; o > 0; o >>= 1) {
-        mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-        sq += __shfl_xor_sync(0xffffffffu, sq, o);
+        const unsigned long long y = __shfl_xor_sync(0xffffffffu, mx, o);
+        mx = y > mx ? y : mx;
         bad |= __shfl_xor_sync(0xffffffffu, bad, o);
     }
+    // sum of squares in FP32 on values rebased to the tile row's largest exponent (|f| < 2)
+    const int et = int(mx >> 52);  // biased exponent of the tile-row maximum
+    float sq = 0.f;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        const unsigned long long a = tile[rr][pp0 + q] & 0x7fffffffffffffffull;
+        const int ea = int(a >> 52);
+        const int fe = ea - et + 127;  // biased float exponent after rebasing
+        const uint32_t fb = (ea == 0 || fe <= 0) ? 0u : (uint32_t(fe) << 23) | uint32_t((a >> 29) & 0x7fffffu);
+        const float f = __uint_as_float(fb);
+        sq = fmaf(f, f, sq);
+    }
+#pragma unroll
+    for (int o = 4; o > 0; o >>= 1) sq += __shfl_xor_sync(0xffffffffu, sq, o);
     const int64_t r = r0 + rr;
     if ((t & 7) == 0 && r < R) {
         if (bad) atomicOr(&acc[r].flags, 1);
-        if (mx > 0.0) atomicMax(&acc[r].maxbits, static_cast<unsigned long long>(__double_as_longlong(mx)));
-        if (sq != 0.0) atomicAdd(&acc[r].sumsq, sq);
+        if (mx != 0) {
+            atomicMax(&acc[r].maxbits, mx);
+            // sum of squares of the unscaled values: sq * 2^(2*(et - 1023))
+            atomicAdd(&acc[r].sumsq, ldexp(double(sq), 2 * (et - 1023)));
+        }
     }
 }
 
@@ -268,61 +286,107 @@ __global__ void split_info_kernel(const int* __restrict__ eA, const double* __re
 
 // Digit planes: planes[a][r][p] (bf16, pitch kpad, plane stride rpad*kpad) for r < rpad, p < kpad;
 // zeros outside the R x K operand.  Each block covers 32 rows x 64 k.
+//
+// Exact mode: for |a| < 2^e (e the row exponent) the fixed-point integer
+// X = round(|a| * 2^(8S-1-e)) (round half up below the last digit) satisfies X <= 2^(8S-1); its
+// balanced base-256 digits d_S..d_2 in [-128, 127] and the top digit d_1 in [0, 128] give
+// |a| * 2^-e = sum_s d_s 2^(1-8s) + rho, |rho| <= 2^-8S.  Everything is integer arithmetic on the
+// FP64 bit pattern (64-bit for S <= 8, 128-bit beyond); digits become BF16 bit patterns through an
+// exact FP32 add.  Float modes: BF16 hi part and BF16 rounding of the remainder.
+__device__ __forceinline__ uint16_t digit_bf16(int d) {
+    // float(d) exactly via the 1.5*2^23 bias; |d| <= 128 has at most 8 significant bits, so the
+    // upper half of the FP32 pattern is the BF16 pattern
+    const float f = __int_as_float(0x4B400000 + d) - 12582912.0f;
+    return uint16_t(__float_as_uint(f) >> 16);
+}
+
+// Fixed-point magnitude V = X + sum_{s<S-1} 128*256^s of one element: with it, the balanced digit of
+// plane a >= 1 is byte (S-1-a) of V minus 128 and the top digit (plane 0) is V >> 8(S-1); adding the
+// 128s once replaces the digit-by-digit carry chain.
+template <typename U_t>
+__device__ __forceinline__ U_t fixed_point_biased(unsigned long long bits, int e, int S) {
+    const int eb = int((bits >> 52) & 0x7ff);
+    const unsigned long long mant = bits & 0xfffffffffffffull;
+    const unsigned long long M = eb ? (mant | (1ull << 52)) : mant;
+    const int E = (eb ? eb : 1) - 1075;  // |a| = M * 2^E
+    const int sh = E + 8 * S - 1 - e;
+    U_t U;
+    if (M == 0) U = 0;
+    else if (sh >= 0) U = U_t(M) << sh;
+    else if (sh > -64) U = U_t((M + (1ull << (-sh - 1))) >> (-sh));
+    else U = 0;
+    U_t B = 0;
+    for (int s = 0; s < S - 1; ++s) B = (B << 8) | 0x80;
+    return U + B;
+}
+
+template <typename U_t>
+__device__ __forceinline__ void write_planes(const U_t (&V)[8], const bool (&neg)[8], int S, uint16_t* dst,
+                                             int64_t pstride) {
+    for (int a = 0; a < S; ++a) {
+        const int sft = 8 * (S - 1 - a);
+        __align__(16) uint16_t d[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            int v = int(uint32_t(V[q] >> sft) & (a == 0 ? 0x1ffu : 0xffu));
+            if (a != 0) v -= 128;
+            d[q] = digit_bf16(neg[q] ? -v : v);
+        }
+        *reinterpret_cast<uint4*>(dst + a * pstride) = *reinterpret_cast<const uint4*>(d);
+    }
+}
+
 __global__ void slice_kernel(const double* __restrict__ X, int64_t R, int64_t K, int64_t sr, int64_t sp,
                              const int* __restrict__ rexp, const SplitInfo* __restrict__ info, int mode,
                              __nv_bfloat16* __restrict__ planes, int64_t rpad, int64_t kpad) {
-    __shared__ double tile[32][65];
+    __shared__ unsigned long long tile[32][65];
     const int64_t r0 = int64_t(blockIdx.y) * 32, p0 = int64_t(blockIdx.x) * 64;
     const int t = threadIdx.x;  // 256 threads
-    // load 32 x 64 doubles with coalescing along the contiguous dimension
+    const unsigned long long* Xb = reinterpret_cast<const unsigned long long*>(X);
     if (sp == 1) {
         for (int e = t; e < 32 * 64; e += 256) {
             const int rr = e / 64, pp = e % 64;
             const int64_t r = r0 + rr, p = p0 + pp;
-            tile[rr][pp] = (r < R && p < K) ? X[r * sr + p] : 0.0;
+            tile[rr][pp] = (r < R && p < K) ? Xb[r * sr + p] : 0ull;
         }
     } else {
         for (int e = t; e < 32 * 64; e += 256) {
             const int pp = e / 32, rr = e % 32;
             const int64_t r = r0 + rr, p = p0 + pp;
-            tile[rr][pp] = (r < R && p < K) ? X[r * sr + p * sp] : 0.0;
+            tile[rr][pp] = (r < R && p < K) ? Xb[r * sr + p * sp] : 0ull;
         }
     }
     __syncthreads();
     const int rr = t / 8, pp0 = (t % 8) * 8;
     const int64_t r = r0 + rr;
     if (r >= rpad) return;
-    const int nplanes = (mode == kExact) ? info->slices : (mode == kBf16 ? 1 : 2);
-    const int e = (r < R) ? rexp[r] : 0;
-    const bool bad = (e == kNonFinite);
-    double x[8];
-#pragma unroll
-    for (int q = 0; q < 8; ++q) {
-        const double v = bad ? 0.0 : tile[rr][pp0 + q];
-        x[q] = (mode == kExact) ? ldexp(v, -e) : v;
-    }
-    __nv_bfloat16* dst = planes + r * kpad + p0 + pp0;
     const int64_t pstride = rpad * kpad;
+    uint16_t* dst = reinterpret_cast<uint16_t*>(planes) + r * kpad + p0 + pp0;
     if (mode == kExact) {
-        // first digit carries 7 bits (|x| < 1), later digits 8 bits
+        const int S = info->slices;
+        const int e = (r < R) ? rexp[r] : 0;
+        const bool bad = (e == kNonFinite);
+        bool neg[8];
 #pragma unroll
-        for (int q = 0; q < 8; ++q) x[q] *= 128.0;
-        for (int a = 0; a < nplanes; ++a) {
-            __align__(16) __nv_bfloat16 d[8];
+        for (int q = 0; q < 8; ++q) neg[q] = !bad && (tile[rr][pp0 + q] >> 63) != 0;
+        if (S <= 8) {
+            unsigned long long V[8];
 #pragma unroll
-            for (int q = 0; q < 8; ++q) {
-                const double dv = rint(x[q]);
-                x[q] = (x[q] - dv) * 256.0;
-                d[q] = __float2bfloat16_rn(float(dv));
-            }
-            *reinterpret_cast<uint4*>(dst + a * pstride) = *reinterpret_cast<const uint4*>(d);
+            for (int q = 0; q < 8; ++q) V[q] = fixed_point_biased<unsigned long long>(bad ? 0ull : tile[rr][pp0 + q], e, S);
+            write_planes(V, neg, S, dst, pstride);
+        } else {
+            unsigned __int128 V[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) V[q] = fixed_point_biased<unsigned __int128>(bad ? 0ull : tile[rr][pp0 + q], e, S);
+            write_planes(V, neg, S, dst, pstride);
         }
     } else {
         __align__(16) __nv_bfloat16 hi[8], lo[8];
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
-            hi[q] = __float2bfloat16_rn(float(x[q]));
-            lo[q] = __float2bfloat16_rn(float(x[q] - double(__bfloat162float(hi[q]))));
+            const double x = __longlong_as_double(static_cast<long long>(tile[rr][pp0 + q]));
+            hi[q] = __float2bfloat16_rn(float(x));
+            lo[q] = __float2bfloat16_rn(float(x - double(__bfloat162float(hi[q]))));
         }
         *reinterpret_cast<uint4*>(dst) = *reinterpret_cast<const uint4*>(hi);
         if (mode == kBf16x3) *reinterpret_cast<uint4*>(dst + pstride) = *reinterpret_cast<const uint4*>(lo);
@@ -592,8 +656,47 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
     }
 }
 
+// Round the signed 128-bit integer W to the nearest double and multiply by 2^x, with integer
+// operations only whenever the result is a normal number (the usual case); sub- or overflowing
+// results take the FP64 ldexp path.
+__device__ __forceinline__ double int128_to_double_scaled(__int128 W, int x) {
+    if (W == 0) return 0.0;
+    const bool neg = W < 0;
+    const unsigned __int128 U = neg ? (unsigned __int128)(-W) : (unsigned __int128)W;
+    const unsigned long long hi = (unsigned long long)(U >> 64), lo = (unsigned long long)U;
+    const int nbits = hi ? 128 - __clzll((long long)hi) : 64 - __clzll((long long)lo);
+    unsigned long long mant;
+    int shift = 0;
+    if (nbits <= 53) {
+        mant = lo << (53 - nbits);
+        shift = nbits - 53;
+    } else {
+        shift = nbits - 53;
+        const unsigned __int128 m = U >> shift;
+        const unsigned __int128 rem = U - (m << shift);
+        const unsigned __int128 half = (unsigned __int128)1 << (shift - 1);
+        mant = (unsigned long long)m;
+        if (rem > half || (rem == half && (mant & 1))) ++mant;
+        if (mant == (1ull << 53)) {
+            mant >>= 1;
+            ++shift;
+        }
+    }
+    // value = mant * 2^(shift + x), mant in [2^52, 2^53)
+    const int be = 52 + shift + x + 1023;
+    if (be > 0 && be < 2047) {
+        const unsigned long long bits =
+            (neg ? (1ull << 63) : 0ull) | ((unsigned long long)be << 52) | (mant & 0xfffffffffffffull);
+        return __longlong_as_double((long long)bits);
+    }
+    const double v = ldexp(double(mant), shift + x);
+    return neg ? -v : v;
+}
+
 // C = alpha * 2^(e_i + f_j) * sum_L 2^(-14-8L) * sum_seg T[seg][L] + beta * C   (exact mode)
 // C = alpha * sum_seg P[seg] + beta * C                                         (float modes)
+// Exact mode forms W = sum_L T_L * 2^(8(S-1-L)) exactly in 128-bit integers, so the only roundings
+// are the conversion of W to double and the alpha/beta update (skipped when alpha == 1, beta == 0).
 __global__ void combine_kernel(const int32_t* __restrict__ levels, int nseg, int max_levels, int64_t mpad,
                                int64_t npad, int mode, const SplitInfo* __restrict__ info,
                                const int* __restrict__ eA, const int* __restrict__ eB, int64_t m, int64_t n,
@@ -601,6 +704,7 @@ __global__ void combine_kernel(const int32_t* __restrict__ levels, int nseg, int
     const int64_t total = m * n;
     const int64_t plane = mpad * npad;
     const int S = (mode == kExact) ? info->slices : 1;
+    const bool plain = (alpha == 1.0 && beta == 0.0);
     for (int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; e < total; e += int64_t(gridDim.x) * blockDim.x) {
         const int64_t i = e / n, j = e % n;
         const int64_t off = i * npad + j;
@@ -610,28 +714,26 @@ __global__ void combine_kernel(const int32_t* __restrict__ levels, int nseg, int
             if (ei == kNonFinite || fj == kNonFinite) {
                 v = __longlong_as_double(0x7ff8000000000000ll);  // NaN: the inputs were not finite
             } else {
-                // least significant level first; three levels combine exactly in int64
-                double acc = 0.0;
-                for (int L = S - 1; L >= 0; L -= 3) {
-                    const int L0 = max(L - 2, 0);
+                __int128 W = 0;
+                for (int L = 0; L < S; ++L) {
                     long long t = 0;
-                    for (int l = L0; l <= L; ++l) {
-                        long long s = 0;
-                        for (int g = 0; g < nseg; ++g) s += levels[(int64_t(g) * max_levels + l) * plane + off];
-                        t += s * (1ll << (8 * (L - l)));
-                    }
-                    acc += ldexp(double(t), -14 - 8 * L);
+                    for (int g = 0; g < nseg; ++g) t += levels[(int64_t(g) * max_levels + L) * plane + off];
+                    W = (W << 8) + t;
                 }
-                v = alpha * ldexp(acc, ei + fj);
+                v = int128_to_double_scaled(W, ei + fj - 14 - 8 * (S - 1));
             }
         } else {
             double acc = 0.0;
             for (int g = 0; g < nseg; ++g)
                 acc += double(__int_as_float(levels[int64_t(g) * max_levels * plane + off]));
-            v = alpha * acc;
+            v = acc;
         }
         double* c = C + i * ldc + j;
-        *c = (beta == 0.0) ? v : fma(beta, *c, v);
+        if (plain) *c = v;
+        else {
+            v *= alpha;
+            *c = (beta == 0.0) ? v : fma(beta, *c, v);
+        }
     }
 }
 
