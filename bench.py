@@ -48,6 +48,8 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-native", action="store_true", help="skip the native FP64 comparison")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end C-ABI leg")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched small-product leg")
+    ap.add_argument("--batch-count", type=int, default=10000)
     return ap.parse_args()
 
 
@@ -222,6 +224,63 @@ def e2e_leg(G, hA, hB, n, flops, args, dist):
             "ms_per_step": round(t_e2e * 1e3, 3), "call": "cblas_dgemm (default method: auto -> split)"}
 
 
+def batched_leg(G, torch, args, dev):
+    """10,000 independent products, M, N, K log-uniform integers in [4, 256], uniform [-1,1],
+    FP64 and FP32: one persistent grouped launch (CUDA graph) against a loop of per-product
+    launches of the native kernel, both device-resident."""
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from batched import build
+
+    out = {"workload": f"{args.batch_count} products, M,N,K log-uniform integers in [4,256], uniform [-1,1], "
+                       "row-major, device-resident"}
+    s = torch.cuda.Stream(device=dev)
+    for name, dtype, esz in (("fp64", np.float64, 8), ("fp32", np.float32, 4)):
+        specs, A, B, C0, dA, dB, dC = build(torch, args.batch_count, seed=args.seed + 100, dtype=dtype)
+        probs = G.problems(specs)
+        t0 = time.perf_counter()
+        plan = G.GroupedPlan(probs, esz)
+        t_plan = time.perf_counter() - t0
+        ntiles, useful, padded = plan.info()
+        plan.run(s.cuda_stream)
+        s.synchronize()
+        reps = 10
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        for _ in range(reps):
+            plan.run(s.cuda_stream)
+        e1.record(s)
+        s.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        plan.close()
+        # loop of per-product launches (native kernel) on the same stream
+        fx = G.dgemm_ex if dtype == np.float64 else G.sgemm_ex
+        o = G.opts(method="native", residency=G.PTR_DEVICE, stream=s.cuda_stream, synchronous=False)
+        for sp in specs[:50]:
+            fx(sp["order"], sp["transA"], sp["transB"], sp["m"], sp["n"], sp["k"], sp["alpha"], sp["A"], sp["lda"],
+               sp["B"], sp["ldb"], sp["beta"], sp["C"], sp["ldc"], o)
+        s.synchronize()
+        l0 = torch.cuda.Event(enable_timing=True)
+        l1 = torch.cuda.Event(enable_timing=True)
+        t0 = time.perf_counter()
+        l0.record(s)
+        for sp in specs:
+            fx(sp["order"], sp["transA"], sp["transB"], sp["m"], sp["n"], sp["k"], sp["alpha"], sp["A"], sp["lda"],
+               sp["B"], sp["ldb"], sp["beta"], sp["C"], sp["ldc"], o)
+        l1.record(s)
+        s.synchronize()
+        loop_wall = time.perf_counter() - t0
+        loop_ms = l0.elapsed_time(l1)
+        out[name] = {"grouped_ms": round(ms, 4), "grouped_tflops": round(useful / (ms * 1e-3) / 1e12, 4),
+                     "padded_over_useful": round(padded / useful, 4), "tiles": int(ntiles),
+                     "plan_ms": round(t_plan * 1e3, 2), "loop_ms_device": round(loop_ms, 3),
+                     "loop_ms_wall": round(loop_wall * 1e3, 2), "speedup_vs_loop": round(loop_ms / ms, 2),
+                     "useful_gflop": round(useful / 1e9, 4)}
+        del dA, dB, dC
+    return out
+
+
 def ours(args, dist: Dist):
     import numpy as np
     import torch
@@ -351,7 +410,8 @@ def ours(args, dist: Dist):
                                                                  f"{max(1, n // 32)}th row"},
                 "native_fp64": native,
                 "split_vs_native": round(value / dist.world / native["value"], 2) if native else None,
-                "e2e": e2e, "roofline": roofline, "gpu_launches": int(launches), "clocks": clk}
+                "e2e": e2e, "roofline": roofline, "gpu_launches": int(launches), "clocks": clk,
+                "batched": batched}
         if not args.no_cpu:
             line["cpu_baseline"] = cpu_baseline(min(n, 4096))
         print(json.dumps(line), flush=True)

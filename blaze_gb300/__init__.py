@@ -42,6 +42,17 @@ class GemmOpts(ct.Structure):
     ]
 
 
+class GemmProblem(ct.Structure):
+    _fields_ = [
+        ("order", ct.c_int), ("transA", ct.c_int), ("transB", ct.c_int),
+        ("m", ct.c_int64), ("n", ct.c_int64), ("k", ct.c_int64),
+        ("alpha", ct.c_double), ("beta", ct.c_double),
+        ("A", ct.c_void_p), ("lda", ct.c_int64),
+        ("B", ct.c_void_p), ("ldb", ct.c_int64),
+        ("C", ct.c_void_p), ("ldc", ct.c_int64),
+    ]
+
+
 class Gb300Error(RuntimeError):
     def __init__(self, status: int, message: str):
         super().__init__(f"[status {status}] {message}")
@@ -95,6 +106,27 @@ def lib() -> ct.CDLL:
     L.gb300_dgemm_native_noalloc.argtypes = [ct.c_int, ct.c_int, ct.c_int, I64, I64, I64, D, VP, I64, VP, I64, D,
                                              VP, I64, VP]
     L.gb300_dgemm_native_noalloc.restype = ct.c_int
+    PP = ct.POINTER(GemmProblem)
+    L.gb300_grouped_plan_create.argtypes = [ct.c_int, PP, I64, ct.POINTER(VP)]
+    L.gb300_grouped_plan_create.restype = ct.c_int
+    L.gb300_grouped_plan_run.argtypes = [VP, VP]
+    L.gb300_grouped_plan_run.restype = ct.c_int
+    L.gb300_grouped_plan_info.argtypes = [VP, ct.POINTER(I64), ct.POINTER(D), ct.POINTER(D)]
+    L.gb300_grouped_plan_info.restype = ct.c_int
+    L.gb300_grouped_plan_destroy.argtypes = [VP]
+    L.gb300_grouped_plan_destroy.restype = None
+    L.gb300_dgemm_grouped.argtypes = [PP, I64, VP]
+    L.gb300_dgemm_grouped.restype = ct.c_int
+    L.gb300_sgemm_grouped.argtypes = [PP, I64, VP]
+    L.gb300_sgemm_grouped.restype = ct.c_int
+    L.gb300_grouped_autotune.argtypes = [ct.c_int, ct.c_int]
+    L.gb300_grouped_autotune.restype = ct.c_int
+    L.gb300_grouped_tuning_save.argtypes = [ct.c_char_p]
+    L.gb300_grouped_tuning_save.restype = ct.c_int
+    L.gb300_grouped_tuning_load.argtypes = [ct.c_char_p]
+    L.gb300_grouped_tuning_load.restype = ct.c_int
+    L.gb300_grouped_shape_for.argtypes = [ct.c_int, I64, I64, I64, ct.POINTER(ct.c_int), ct.POINTER(ct.c_int)]
+    L.gb300_grouped_shape_for.restype = ct.c_int
     L.gb300_select_device.argtypes = [ct.c_int]
     L.gb300_select_device.restype = ct.c_int
     L.gb300_profile_enable.argtypes = [ct.c_int]
@@ -183,6 +215,68 @@ def dgemm_native_noalloc(order, transA, transB, m, n, k, alpha, A, lda, B, ldb, 
     """The allocation-free native product (device operands; fixed in-library scratch)."""
     check(lib().gb300_dgemm_native_noalloc(order, transA, transB, m, n, k, alpha, _addr(A), lda, _addr(B), ldb,
                                            beta, _addr(C), ldc, stream))
+
+
+def problems(specs) -> ct.Array:
+    """A ctypes array of GemmProblem from dicts with the CBLAS fields
+    (order, transA, transB, m, n, k, alpha, beta, A, lda, B, ldb, C, ldc); pointers may be
+    integers, numpy arrays or torch tensors."""
+    arr = (GemmProblem * len(specs))()
+    for i, sp in enumerate(specs):
+        p = arr[i]
+        p.order, p.transA, p.transB = sp["order"], sp["transA"], sp["transB"]
+        p.m, p.n, p.k = sp["m"], sp["n"], sp["k"]
+        p.alpha, p.beta = sp.get("alpha", 1.0), sp.get("beta", 0.0)
+        p.A, p.lda = _addr(sp["A"]), sp["lda"]
+        p.B, p.ldb = _addr(sp["B"]), sp["ldb"]
+        p.C, p.ldc = _addr(sp["C"]), sp["ldc"]
+    return arr
+
+
+class GroupedPlan:
+    """A captured grouped launch (gb300_grouped_plan_*)."""
+
+    def __init__(self, probs, elem_bytes: int = 8):
+        self.handle = ct.c_void_p()
+        self._probs = probs
+        check(lib().gb300_grouped_plan_create(elem_bytes, probs, len(probs), ct.byref(self.handle)))
+
+    def run(self, stream: int | None = None) -> None:
+        check(lib().gb300_grouped_plan_run(self.handle, stream))
+
+    def info(self) -> tuple[int, float, float]:
+        t, u, p = ct.c_int64(0), ct.c_double(0), ct.c_double(0)
+        check(lib().gb300_grouped_plan_info(self.handle, ct.byref(t), ct.byref(u), ct.byref(p)))
+        return t.value, u.value, p.value
+
+    def close(self) -> None:
+        if self.handle:
+            lib().gb300_grouped_plan_destroy(self.handle)
+            self.handle = ct.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:  # noqa: BLE001
+            pass
+
+
+def dgemm_grouped(probs, stream: int | None = None) -> None:
+    check(lib().gb300_dgemm_grouped(probs, len(probs), stream))
+
+
+def sgemm_grouped(probs, stream: int | None = None) -> None:
+    check(lib().gb300_sgemm_grouped(probs, len(probs), stream))
+
+
+def grouped_autotune(elem_bytes: int = 8, effort: int = 1) -> None:
+    check(lib().gb300_grouped_autotune(elem_bytes, effort))
+
+
+def grouped_shape_for(elem_bytes: int, m: int, n: int, k: int) -> tuple[int, int, int]:
+    r, c = ct.c_int(0), ct.c_int(0)
+    s = lib().gb300_grouped_shape_for(elem_bytes, m, n, k, ct.byref(r), ct.byref(c))
+    return s, r.value, c.value
 
 
 def device_info() -> tuple[int, int, int]:

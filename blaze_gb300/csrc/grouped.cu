@@ -1,0 +1,563 @@
+// grouped.cu — K4: persistent grouped GEMM for many independent, uneven, small products
+// (Blaze's StaticMatrix / HybridMatrix sizes), FP64 (DFMA) and FP32 (FFMA), one launch per batch,
+// captured in a CUDA graph, with warp-tile shapes picked per size class by an autotuner.
+//
+// Blaze evaluates every such product separately on the CPU through its small vectorized kernel
+// (blaze/math/expressions/DMatDMatMultExpr.h:864-1878, DMatTDMatMultExpr.h:1067+); it has no
+// batched product, so this is a new entry point (gb300_?gemm_grouped) with the per-product CBLAS
+// argument conventions.
+//
+// Design:
+//   * Every product is brought to the row-major form (as for the single products) and tiled with
+//     the warp-tile shape chosen for its (m, n, k) class.  Warp tile = (8*R) x (4*C) outputs, lane
+//     (ly, lx) of an 8 x 4 lane grid owning rows ly + 8r and columns lx + 4c, so a warp's B loads
+//     are coalesced runs and its A loads are 8 broadcast rows.
+//   * One flat tile list, sorted by descending work (longest first), is consumed by persistent
+//     warps through a global atomic counter (warp-granular work stealing): uneven products
+//     balance across SMs without a per-product launch.
+//   * Operands are read through L1 (__ldg): a small product's panels stay cache-resident across the
+//     k loop, and on this chip the FP64 pipe (about 2 DFMA/clock/SM) — not the load path — bounds
+//     the FP64 form, so the tile shapes exist to avoid multiply-adds on padding.
+//   * The launch (counter reset + kernel) is captured once into a CUDA graph owned by the plan;
+//     running the plan is one graph launch.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <mutex>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "../../include/gb300_blas.h"
+#include "runtime.h"
+
+namespace gb {
+namespace {
+
+// Warp-tile shapes: (R, C) -> (8R) x (4C) outputs per warp.
+struct Shape {
+    int R, C;
+};
+constexpr Shape kShapes[] = {{1, 2}, {2, 4}, {4, 4}, {2, 8}, {4, 8}, {8, 8}};
+constexpr int kNumShapes = sizeof(kShapes) / sizeof(kShapes[0]);
+__host__ __device__ constexpr int shape_rows(int s) { return s == 0 ? 8 : s == 1 ? 16 : s == 2 ? 32 : s == 3 ? 16 : s == 4 ? 32 : 64; }
+__host__ __device__ constexpr int shape_cols(int s) { return s == 0 ? 8 : s == 1 ? 16 : s == 2 ? 16 : s == 3 ? 32 : s == 4 ? 32 : 32; }
+
+struct DevProblem {
+    const void* A;
+    const void* B;
+    void* C;
+    int64_t lda, ldb, ldc;
+    int m, n, k;
+    int ta, tb;
+    int shape;
+    double alpha, beta;
+};
+
+struct DevTile {
+    int prob;
+    int tm, tn;  // tile coordinates in units of the problem's warp tile
+    int pad;
+};
+
+template <typename T, int R, int C>
+__device__ __forceinline__ void warp_tile(const DevProblem& p, int tm, int tn, int lane) {
+    const int ly = lane >> 2, lx = lane & 3;
+    const int row0 = tm * (8 * R) + ly;
+    const int col0 = tn * (4 * C) + lx;
+    // A(i, kk) = A[i*a_rs + kk*a_ks], B(kk, j) = B[kk*b_ks + j*b_cs]; one running pointer per operand
+    const int64_t a_rs = p.ta ? 1 : p.lda, a_ks = p.ta ? p.lda : 1;
+    const int64_t b_cs = p.tb ? p.ldb : 1, b_ks = p.tb ? 1 : p.ldb;
+    const int64_t a8 = 8 * a_rs, b4 = 4 * b_cs;
+    const T* pa = static_cast<const T*>(p.A) + int64_t(row0) * a_rs;
+    const T* pb = static_cast<const T*>(p.B) + int64_t(col0) * b_cs;
+    uint32_t rmask = 0, cmask = 0;
+#pragma unroll
+    for (int r = 0; r < R; ++r) rmask |= (row0 + 8 * r < p.m) ? (1u << r) : 0u;
+#pragma unroll
+    for (int c = 0; c < C; ++c) cmask |= (col0 + 4 * c < p.n) ? (1u << c) : 0u;
+    T acc[R][C];
+#pragma unroll
+    for (int r = 0; r < R; ++r)
+#pragma unroll
+        for (int c = 0; c < C; ++c) acc[r][c] = T(0);
+#pragma unroll 1
+    for (int kk = 0; kk < p.k; ++kk) {
+        T a0[R], b0[C];
+#pragma unroll
+        for (int r = 0; r < R; ++r) a0[r] = (rmask >> r) & 1u ? __ldg(pa + r * a8) : T(0);
+#pragma unroll
+        for (int c = 0; c < C; ++c) b0[c] = (cmask >> c) & 1u ? __ldg(pb + c * b4) : T(0);
+#pragma unroll
+        for (int r = 0; r < R; ++r)
+#pragma unroll
+            for (int c = 0; c < C; ++c) acc[r][c] = fma(a0[r], b0[c], acc[r][c]);
+        pa += a_ks;
+        pb += b_ks;
+    }
+    T* Cp = static_cast<T*>(p.C);
+    const T alpha = T(p.alpha), beta = T(p.beta);
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        if (!((rmask >> r) & 1u)) continue;
+        T* crow = Cp + int64_t(row0 + 8 * r) * p.ldc;
+#pragma unroll
+        for (int c = 0; c < C; ++c) {
+            if (!((cmask >> c) & 1u)) continue;
+            const int j = col0 + 4 * c;
+            const T v = alpha * acc[r][c];
+            crow[j] = (beta == T(0)) ? v : fma(beta, crow[j], v);
+        }
+    }
+}
+
+// Shapes available per element type: FP64 stops at 16x32 / 32x16 warp tiles (16 accumulators per
+// lane): on the FP64 pipe a larger tile only adds padding, and the smaller register footprint lets an
+// SM hold twice the warps.
+template <typename T>
+__host__ __device__ constexpr int max_shape() { return sizeof(T) == 8 ? 3 : 5; }
+
+template <typename T>
+__global__ void __launch_bounds__(256, sizeof(T) == 8 ? 2 : 1)
+grouped_kernel(const DevProblem* __restrict__ probs, const DevTile* __restrict__ tiles, int ntiles,
+               int* __restrict__ counter) {
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        int t = 0;
+        if (lane == 0) t = atomicAdd(counter, 1);
+        t = __shfl_sync(0xffffffffu, t, 0);
+        if (t >= ntiles) break;
+        const DevTile tl = tiles[t];
+        const DevProblem p = probs[tl.prob];
+        switch (p.shape) {
+            case 0: warp_tile<T, 1, 2>(p, tl.tm, tl.tn, lane); break;
+            case 1: warp_tile<T, 2, 4>(p, tl.tm, tl.tn, lane); break;
+            case 2: warp_tile<T, 4, 4>(p, tl.tm, tl.tn, lane); break;
+            case 3: warp_tile<T, 2, 8>(p, tl.tm, tl.tn, lane); break;
+            case 4:
+                if constexpr (max_shape<T>() >= 4) warp_tile<T, 4, 8>(p, tl.tm, tl.tn, lane);
+                break;
+            default:
+                if constexpr (max_shape<T>() >= 5) warp_tile<T, 8, 8>(p, tl.tm, tl.tn, lane);
+                break;
+        }
+    }
+}
+
+// ---- tuning table ------------------------------------------------------------------------------
+// Size classes: m and n bucketed by powers of two (<=8, <=16, <=32, <=64, <=128, >128), k by
+// (<=16, <=64, >64).  Entry = warp-tile shape index.
+constexpr int kMB = 6, kKB = 3;
+int bucket_mn(int x) { return x <= 8 ? 0 : x <= 16 ? 1 : x <= 32 ? 2 : x <= 64 ? 3 : x <= 128 ? 4 : 5; }
+int bucket_k(int x) { return x <= 16 ? 0 : x <= 64 ? 1 : 2; }
+
+struct TuneTable {
+    int shape[2][kMB][kMB][kKB];  // [dtype: 0 double, 1 float]
+    bool tuned[2] = {false, false};
+};
+
+std::mutex g_tune_mu;
+TuneTable g_tune;
+bool g_tune_init = false;
+
+// Default choice (no measurements): the shape with the least padded work, larger tiles on ties.
+int model_shape(int m, int n, int nshapes) {
+    int best = 0;
+    double best_cost = 1e300;
+    for (int s = 0; s < nshapes; ++s) {
+        const double tr = shape_rows(s), tc = shape_cols(s);
+        const double padded = std::ceil(m / tr) * tr * std::ceil(n / tc) * tc;
+        // a small per-tile overhead favours fewer, larger tiles when the padding is equal
+        const double cost = padded + 64.0 * std::ceil(m / tr) * std::ceil(n / tc);
+        if (cost < best_cost - 1e-9) {
+            best_cost = cost;
+            best = s;
+        }
+    }
+    return best;
+}
+
+void tune_defaults() {
+    if (g_tune_init) return;
+    const int rep[kMB] = {6, 12, 24, 48, 96, 192};
+    for (int d = 0; d < 2; ++d)
+        for (int a = 0; a < kMB; ++a)
+            for (int b = 0; b < kMB; ++b)
+                for (int c = 0; c < kKB; ++c)
+                    g_tune.shape[d][a][b][c] = model_shape(rep[a], rep[b], d == 0 ? max_shape<double>() + 1 : kNumShapes);
+    g_tune_init = true;
+}
+
+int pick_shape(int dtype_idx, int m, int n, int k) {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    tune_defaults();
+    return g_tune.shape[dtype_idx][bucket_mn(m)][bucket_mn(n)][bucket_k(k)];
+}
+
+}  // namespace
+
+// ---- plan ----------------------------------------------------------------------------------
+struct GroupedPlan {
+    int elem = 8;
+    int64_t count = 0;
+    int64_t ntiles = 0;
+    DevProblem* d_probs = nullptr;
+    DevTile* d_tiles = nullptr;
+    int* d_counter = nullptr;
+    cudaStream_t cap_stream = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int grid = 0;
+    double useful_flops = 0, padded_flops = 0;
+};
+
+namespace {
+
+void plan_free(GroupedPlan* p) {
+    if (!p) return;
+    if (p->exec) cudaGraphExecDestroy(p->exec);
+    if (p->graph) cudaGraphDestroy(p->graph);
+    if (p->cap_stream) cudaStreamDestroy(p->cap_stream);
+    if (p->d_probs) cudaFree(p->d_probs);
+    if (p->d_tiles) cudaFree(p->d_tiles);
+    if (p->d_counter) cudaFree(p->d_counter);
+    delete p;
+}
+
+template <typename T>
+int plan_create(const gb300_gemm_problem* probs, int64_t count, int force_shape, GroupedPlan** out, std::string* err) {
+    Runtime& r = runtime();
+    int st = ensure_init(err);
+    if (st != GB300_OK) return st;
+    const int didx = sizeof(T) == 8 ? 0 : 1;
+    std::vector<DevProblem> hp;
+    hp.reserve(size_t(count));
+    std::vector<DevTile> ht;
+    double useful = 0, padded = 0;
+    for (int64_t q = 0; q < count; ++q) {
+        const gb300_gemm_problem& x = probs[q];
+        const bool rm = x.order == 101;
+        if ((x.order != 101 && x.order != 102) || x.m < 0 || x.n < 0 || x.k < 0 || x.m > INT32_MAX ||
+            x.n > INT32_MAX || x.k > INT32_MAX) {
+            if (err) *err = "problem " + std::to_string(q) + ": invalid order or size";
+            return GB300_ERR_INVALID_ARG;
+        }
+        const bool tA = x.transA != 111, tB = x.transB != 111;
+        const int64_t minlda = std::max<int64_t>(1, rm ? (tA ? x.m : x.k) : (tA ? x.k : x.m));
+        const int64_t minldb = std::max<int64_t>(1, rm ? (tB ? x.k : x.n) : (tB ? x.n : x.k));
+        const int64_t minldc = std::max<int64_t>(1, rm ? x.n : x.m);
+        if (x.lda < minlda || x.ldb < minldb || x.ldc < minldc) {
+            if (err) *err = "problem " + std::to_string(q) + ": leading dimension too small";
+            return GB300_ERR_INVALID_ARG;
+        }
+        DevProblem d;
+        if (rm) {
+            d.m = int(x.m); d.n = int(x.n); d.A = x.A; d.lda = x.lda; d.B = x.B; d.ldb = x.ldb;
+            d.ta = tA; d.tb = tB;
+        } else {
+            d.m = int(x.n); d.n = int(x.m); d.A = x.B; d.lda = x.ldb; d.B = x.A; d.ldb = x.lda;
+            d.ta = tB; d.tb = tA;
+        }
+        d.k = int(x.k);
+        d.C = x.C;
+        d.ldc = x.ldc;
+        d.alpha = x.alpha;
+        d.beta = x.beta;
+        if (d.m == 0 || d.n == 0) continue;
+        if (d.k == 0 || x.alpha == 0.0) d.k = 0;  // C = beta*C through the same kernel
+        d.shape = force_shape >= 0 ? force_shape : pick_shape(didx, d.m, d.n, d.k);
+        const int tr = shape_rows(d.shape), tc = shape_cols(d.shape);
+        const int mt = (d.m + tr - 1) / tr, nt = (d.n + tc - 1) / tc;
+        const int pid = int(hp.size());
+        hp.push_back(d);
+        for (int a = 0; a < mt; ++a)
+            for (int b = 0; b < nt; ++b) ht.push_back(DevTile{pid, a, b, 0});
+        useful += 2.0 * d.m * d.n * d.k;
+        padded += 2.0 * double(mt) * tr * double(nt) * tc * d.k;
+    }
+    // longest first: tiles ordered by their k times tile area (descending)
+    std::stable_sort(ht.begin(), ht.end(), [&](const DevTile& a, const DevTile& b) {
+        const DevProblem& pa = hp[a.prob];
+        const DevProblem& pb = hp[b.prob];
+        const double wa = double(pa.k) * shape_rows(pa.shape) * shape_cols(pa.shape);
+        const double wb = double(pb.k) * shape_rows(pb.shape) * shape_cols(pb.shape);
+        return wa > wb;
+    });
+    auto* p = new GroupedPlan();
+    p->elem = sizeof(T);
+    p->count = count;
+    p->ntiles = int64_t(ht.size());
+    p->useful_flops = useful;
+    p->padded_flops = padded;
+    cudaError_t e = cudaSuccess;
+    if (!hp.empty()) {
+        if ((e = cudaMalloc(&p->d_probs, hp.size() * sizeof(DevProblem))) != cudaSuccess ||
+            (e = cudaMalloc(&p->d_tiles, ht.size() * sizeof(DevTile))) != cudaSuccess ||
+            (e = cudaMemcpy(p->d_probs, hp.data(), hp.size() * sizeof(DevProblem), cudaMemcpyHostToDevice)) !=
+                cudaSuccess ||
+            (e = cudaMemcpy(p->d_tiles, ht.data(), ht.size() * sizeof(DevTile), cudaMemcpyHostToDevice)) != cudaSuccess) {
+            plan_free(p);
+            if (err) *err = std::string("grouped plan upload: ") + cudaGetErrorString(e);
+            return GB300_ERR_NO_MEMORY;
+        }
+    }
+    if ((e = cudaMalloc(&p->d_counter, sizeof(int))) != cudaSuccess ||
+        (e = cudaStreamCreateWithFlags(&p->cap_stream, cudaStreamNonBlocking)) != cudaSuccess) {
+        plan_free(p);
+        if (err) *err = std::string("grouped plan set-up: ") + cudaGetErrorString(e);
+        return GB300_ERR_NO_MEMORY;
+    }
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, grouped_kernel<T>, 256, 0);
+    per_sm = std::max(per_sm, 1);
+    const int64_t warps_needed = p->ntiles;
+    p->grid = int(std::max<int64_t>(1, std::min<int64_t>(int64_t(r.num_sms) * per_sm, (warps_needed + 7) / 8)));
+    // capture: counter reset + persistent kernel
+    e = cudaStreamBeginCapture(p->cap_stream, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        cudaMemsetAsync(p->d_counter, 0, sizeof(int), p->cap_stream);
+        if (p->ntiles > 0)
+            grouped_kernel<T><<<p->grid, 256, 0, p->cap_stream>>>(p->d_probs, p->d_tiles, int(p->ntiles), p->d_counter);
+        e = cudaStreamEndCapture(p->cap_stream, &p->graph);
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&p->exec, p->graph, 0);
+    if (e != cudaSuccess) {
+        plan_free(p);
+        if (err) *err = std::string("grouped graph capture: ") + cudaGetErrorString(e);
+        return GB300_ERR_CUDA;
+    }
+    *out = p;
+    return GB300_OK;
+}
+
+// ---- autotuner -----------------------------------------------------------------------------
+// For every size class, time each candidate shape on a synthetic batch of that class (operands
+// uniform [-1,1], sizes drawn inside the class) and keep the fastest; results can be saved to and
+// loaded from a text cache ("gb300-grouped-tune v1" header, one class per line).
+template <typename T>
+int autotune(int didx, int effort, std::string* err) {
+    const int rep_lo[kMB] = {4, 9, 17, 33, 65, 129};
+    const int rep_hi[kMB] = {8, 16, 32, 64, 128, 256};
+    const int k_lo[kKB] = {4, 17, 65}, k_hi[kKB] = {16, 64, 256};
+    const int batch = std::max(32, 64 * effort);
+    uint64_t rng = 0x9E3779B97F4A7C15ull;
+    auto rnd = [&](int lo, int hi) {
+        rng ^= rng << 13; rng ^= rng >> 7; rng ^= rng << 17;
+        return lo + int(rng % uint64_t(hi - lo + 1));
+    };
+    // one pool of operand memory large enough for a class batch
+    const size_t maxel = size_t(256) * 256;
+    T *dA = nullptr, *dB = nullptr, *dC = nullptr;
+    cudaError_t e;
+    if ((e = cudaMalloc(&dA, size_t(batch) * maxel * sizeof(T))) != cudaSuccess ||
+        (e = cudaMalloc(&dB, size_t(batch) * maxel * sizeof(T))) != cudaSuccess ||
+        (e = cudaMalloc(&dC, size_t(batch) * maxel * sizeof(T))) != cudaSuccess) {
+        cudaFree(dA); cudaFree(dB); cudaFree(dC);
+        if (err) *err = std::string("autotune buffers: ") + cudaGetErrorString(e);
+        return GB300_ERR_NO_MEMORY;
+    }
+    cudaMemset(dA, 0, size_t(batch) * maxel * sizeof(T));
+    cudaMemset(dB, 0, size_t(batch) * maxel * sizeof(T));
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    int table[kMB][kMB][kKB];
+    for (int a = 0; a < kMB; ++a)
+        for (int b = 0; b < kMB; ++b)
+            for (int c = 0; c < kKB; ++c) {
+                std::vector<gb300_gemm_problem> ps(static_cast<size_t>(batch));
+                for (int q = 0; q < batch; ++q) {
+                    gb300_gemm_problem& x = ps[size_t(q)];
+                    std::memset(&x, 0, sizeof(x));
+                    x.order = 101; x.transA = 111; x.transB = 111;
+                    x.m = rnd(rep_lo[a], rep_hi[a]); x.n = rnd(rep_lo[b], rep_hi[b]); x.k = rnd(k_lo[c], k_hi[c]);
+                    x.alpha = 1.0; x.beta = 0.0;
+                    x.A = dA + size_t(q) * maxel; x.lda = x.k;
+                    x.B = dB + size_t(q) * maxel; x.ldb = x.n;
+                    x.C = dC + size_t(q) * maxel; x.ldc = x.n;
+                }
+                float best_ms = 1e30f;
+                int best = 0;
+                for (int s = 0; s <= max_shape<T>(); ++s) {
+                    GroupedPlan* p = nullptr;
+                    if (plan_create<T>(ps.data(), batch, s, &p, err) != GB300_OK) continue;
+                    cudaGraphLaunch(p->exec, p->cap_stream);  // warm-up
+                    cudaEventRecord(e0, p->cap_stream);
+                    const int reps = 5;
+                    for (int it = 0; it < reps; ++it) cudaGraphLaunch(p->exec, p->cap_stream);
+                    cudaEventRecord(e1, p->cap_stream);
+                    cudaEventSynchronize(e1);
+                    float ms = 0;
+                    cudaEventElapsedTime(&ms, e0, e1);
+                    count_launches(reps + 1);
+                    plan_free(p);
+                    if (ms < best_ms) { best_ms = ms; best = s; }
+                }
+                table[a][b][c] = best;
+            }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(dA); cudaFree(dB); cudaFree(dC);
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    tune_defaults();
+    std::memcpy(g_tune.shape[didx], table, sizeof(table));
+    g_tune.tuned[didx] = true;
+    return GB300_OK;
+}
+
+}  // namespace
+}  // namespace gb
+
+// ============================================================================================
+//  C-ABI
+// ============================================================================================
+extern "C" {
+
+int gb300_grouped_plan_create(int elem_bytes, const gb300_gemm_problem* problems, int64_t count,
+                              gb300_grouped_plan** plan) {
+    if (!plan || (count > 0 && !problems) || count < 0 || (elem_bytes != 8 && elem_bytes != 4)) {
+        gb::set_error(GB300_ERR_INVALID_ARG, "gb300_grouped_plan_create: invalid arguments");
+        return GB300_ERR_INVALID_ARG;
+    }
+    gb::Runtime& r = gb::runtime();
+    std::lock_guard<std::mutex> lock(r.mu);
+    std::string err;
+    gb::GroupedPlan* p = nullptr;
+    const int st = elem_bytes == 8 ? gb::plan_create<double>(problems, count, -1, &p, &err)
+                                   : gb::plan_create<float>(problems, count, -1, &p, &err);
+    if (st != GB300_OK) {
+        gb::set_error(st, "gb300_grouped_plan_create: " + err);
+        return st;
+    }
+    *plan = reinterpret_cast<gb300_grouped_plan*>(p);
+    gb::clear_error();
+    return GB300_OK;
+}
+
+int gb300_grouped_plan_run(gb300_grouped_plan* plan, void* stream) {
+    auto* p = reinterpret_cast<gb::GroupedPlan*>(plan);
+    if (!p) {
+        gb::set_error(GB300_ERR_INVALID_ARG, "gb300_grouped_plan_run: null plan");
+        return GB300_ERR_INVALID_ARG;
+    }
+    cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : gb::runtime().stream;
+    const cudaError_t e = cudaGraphLaunch(p->exec, s);
+    if (e != cudaSuccess) {
+        gb::set_error(GB300_ERR_CUDA, std::string("gb300_grouped_plan_run: ") + cudaGetErrorString(e));
+        return GB300_ERR_CUDA;
+    }
+    gb::count_launches(p->ntiles > 0 ? 1 : 0);
+    return GB300_OK;
+}
+
+int gb300_grouped_plan_info(const gb300_grouped_plan* plan, int64_t* tiles, double* useful_flops,
+                            double* padded_flops) {
+    auto* p = reinterpret_cast<const gb::GroupedPlan*>(plan);
+    if (!p) return GB300_ERR_INVALID_ARG;
+    if (tiles) *tiles = p->ntiles;
+    if (useful_flops) *useful_flops = p->useful_flops;
+    if (padded_flops) *padded_flops = p->padded_flops;
+    return GB300_OK;
+}
+
+void gb300_grouped_plan_destroy(gb300_grouped_plan* plan) {
+    gb::Runtime& r = gb::runtime();
+    std::lock_guard<std::mutex> lock(r.mu);
+    gb::plan_free(reinterpret_cast<gb::GroupedPlan*>(plan));
+}
+
+int gb300_dgemm_grouped(const gb300_gemm_problem* problems, int64_t count, void* stream) {
+    gb300_grouped_plan* p = nullptr;
+    int st = gb300_grouped_plan_create(8, problems, count, &p);
+    if (st != GB300_OK) return st;
+    st = gb300_grouped_plan_run(p, stream);
+    if (st == GB300_OK) {
+        cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : gb::runtime().stream;
+        if (cudaStreamSynchronize(s) != cudaSuccess) st = GB300_ERR_CUDA;
+    }
+    gb300_grouped_plan_destroy(p);
+    return st;
+}
+
+int gb300_sgemm_grouped(const gb300_gemm_problem* problems, int64_t count, void* stream) {
+    gb300_grouped_plan* p = nullptr;
+    int st = gb300_grouped_plan_create(4, problems, count, &p);
+    if (st != GB300_OK) return st;
+    st = gb300_grouped_plan_run(p, stream);
+    if (st == GB300_OK) {
+        cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : gb::runtime().stream;
+        if (cudaStreamSynchronize(s) != cudaSuccess) st = GB300_ERR_CUDA;
+    }
+    gb300_grouped_plan_destroy(p);
+    return st;
+}
+
+int gb300_grouped_autotune(int elem_bytes, int effort) {
+    if (elem_bytes != 8 && elem_bytes != 4) {
+        gb::set_error(GB300_ERR_INVALID_ARG, "gb300_grouped_autotune: elem_bytes must be 8 or 4");
+        return GB300_ERR_INVALID_ARG;
+    }
+    gb::Runtime& r = gb::runtime();
+    std::string err;
+    int st;
+    {
+        std::lock_guard<std::mutex> lock(r.mu);
+        st = gb::ensure_init(&err);
+        if (st == GB300_OK)
+            st = elem_bytes == 8 ? gb::autotune<double>(0, effort, &err) : gb::autotune<float>(1, effort, &err);
+    }
+    if (st != GB300_OK) gb::set_error(st, "gb300_grouped_autotune: " + err);
+    return st;
+}
+
+int gb300_grouped_tuning_save(const char* path) {
+    std::lock_guard<std::mutex> lock(gb::g_tune_mu);
+    gb::tune_defaults();
+    std::ofstream f(path);
+    if (!f) {
+        gb::set_error(GB300_ERR_INVALID_ARG, std::string("gb300_grouped_tuning_save: cannot write ") + path);
+        return GB300_ERR_INVALID_ARG;
+    }
+    f << "gb300-grouped-tune v1\n";
+    for (int d = 0; d < 2; ++d)
+        for (int a = 0; a < gb::kMB; ++a)
+            for (int b = 0; b < gb::kMB; ++b)
+                for (int c = 0; c < gb::kKB; ++c)
+                    f << d << ' ' << a << ' ' << b << ' ' << c << ' ' << gb::g_tune.shape[d][a][b][c] << '\n';
+    return GB300_OK;
+}
+
+int gb300_grouped_tuning_load(const char* path) {
+    std::ifstream f(path);
+    std::string head;
+    if (!f || !std::getline(f, head) || head != "gb300-grouped-tune v1") {
+        gb::set_error(GB300_ERR_INVALID_ARG, std::string("gb300_grouped_tuning_load: not a tuning file: ") + path);
+        return GB300_ERR_INVALID_ARG;
+    }
+    std::lock_guard<std::mutex> lock(gb::g_tune_mu);
+    gb::tune_defaults();
+    int d, a, b, c, s;
+    while (f >> d >> a >> b >> c >> s) {
+        if (d < 0 || d > 1 || a < 0 || a >= gb::kMB || b < 0 || b >= gb::kMB || c < 0 || c >= gb::kKB || s < 0 ||
+            s > (d == 0 ? gb::max_shape<double>() : gb::max_shape<float>())) {
+            gb::set_error(GB300_ERR_INVALID_ARG, "gb300_grouped_tuning_load: bad entry");
+            return GB300_ERR_INVALID_ARG;
+        }
+        gb::g_tune.shape[d][a][b][c] = s;
+    }
+    return GB300_OK;
+}
+
+int gb300_grouped_shape_for(int elem_bytes, int64_t m, int64_t n, int64_t k, int* rows, int* cols) {
+    const int s = gb::pick_shape(elem_bytes == 8 ? 0 : 1, int(std::min<int64_t>(m, INT32_MAX)),
+                                 int(std::min<int64_t>(n, INT32_MAX)), int(std::min<int64_t>(k, INT32_MAX)));
+    if (rows) *rows = gb::shape_rows(s);
+    if (cols) *cols = gb::shape_cols(s);
+    return s;
+}
+
+}  // extern "C"

@@ -697,43 +697,66 @@ __device__ __forceinline__ double int128_to_double_scaled(__int128 W, int x) {
 // C = alpha * sum_seg P[seg] + beta * C                                         (float modes)
 // Exact mode forms W = sum_L T_L * 2^(8(S-1-L)) exactly in 128-bit integers, so the only roundings
 // are the conversion of W to double and the alpha/beta update (skipped when alpha == 1, beta == 0).
+// Grid: x over groups of 4 consecutive columns (one 16-byte load per level plane), y over rows.
+constexpr int COMBINE_COLS = 4;
+
 __global__ void combine_kernel(const int32_t* __restrict__ levels, int nseg, int max_levels, int64_t mpad,
                                int64_t npad, int mode, const SplitInfo* __restrict__ info,
                                const int* __restrict__ eA, const int* __restrict__ eB, int64_t m, int64_t n,
                                double alpha, double beta, double* __restrict__ C, int64_t ldc) {
-    const int64_t total = m * n;
+    const int64_t j0 = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) * COMBINE_COLS;
+    if (j0 >= n) return;
     const int64_t plane = mpad * npad;
-    const int S = (mode == kExact) ? info->slices : 1;
-    const bool plain = (alpha == 1.0 && beta == 0.0);
-    for (int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; e < total; e += int64_t(gridDim.x) * blockDim.x) {
-        const int64_t i = e / n, j = e % n;
-        const int64_t off = i * npad + j;
-        double v;
-        if (mode == kExact) {
-            const int ei = eA[i], fj = eB[j];
-            if (ei == kNonFinite || fj == kNonFinite) {
-                v = __longlong_as_double(0x7ff8000000000000ll);  // NaN: the inputs were not finite
-            } else {
-                __int128 W = 0;
-                for (int L = 0; L < S; ++L) {
-                    long long t = 0;
-                    for (int g = 0; g < nseg; ++g) t += levels[(int64_t(g) * max_levels + L) * plane + off];
-                    W = (W << 8) + t;
-                }
-                v = int128_to_double_scaled(W, ei + fj - 14 - 8 * (S - 1));
+    for (int64_t i = blockIdx.y; i < m; i += gridDim.y) {
+    const int64_t off = i * npad + j0;
+    double v[COMBINE_COLS];
+    if (mode == kExact) {
+        const int S = info->slices;
+        const int ei = eA[i];
+        __int128 W[COMBINE_COLS] = {0, 0, 0, 0};
+        for (int L = 0; L < S; ++L) {
+            long long t[COMBINE_COLS] = {0, 0, 0, 0};
+            for (int g = 0; g < nseg; ++g) {
+                const int4 q = *reinterpret_cast<const int4*>(levels + (int64_t(g) * max_levels + L) * plane + off);
+                t[0] += q.x; t[1] += q.y; t[2] += q.z; t[3] += q.w;
             }
-        } else {
-            double acc = 0.0;
-            for (int g = 0; g < nseg; ++g)
-                acc += double(__int_as_float(levels[int64_t(g) * max_levels * plane + off]));
-            v = acc;
+#pragma unroll
+            for (int c = 0; c < COMBINE_COLS; ++c) W[c] = (W[c] << 8) + t[c];
         }
-        double* c = C + i * ldc + j;
-        if (plain) *c = v;
+#pragma unroll
+        for (int c = 0; c < COMBINE_COLS; ++c) {
+            const int64_t j = j0 + c;
+            const int fj = (j < n) ? eB[j] : 0;
+            if (ei == kNonFinite || fj == kNonFinite)
+                v[c] = __longlong_as_double(0x7ff8000000000000ll);  // NaN: the inputs were not finite
+            else
+                v[c] = int128_to_double_scaled(W[c], ei + fj - 14 - 8 * (S - 1));
+        }
+    } else {
+        float acc[COMBINE_COLS] = {0.f, 0.f, 0.f, 0.f};
+        double dacc[COMBINE_COLS] = {0.0, 0.0, 0.0, 0.0};
+        for (int g = 0; g < nseg; ++g) {
+            const int4 q = *reinterpret_cast<const int4*>(levels + int64_t(g) * max_levels * plane + off);
+            acc[0] = __int_as_float(q.x); acc[1] = __int_as_float(q.y);
+            acc[2] = __int_as_float(q.z); acc[3] = __int_as_float(q.w);
+#pragma unroll
+            for (int c = 0; c < COMBINE_COLS; ++c) dacc[c] += double(acc[c]);
+        }
+#pragma unroll
+        for (int c = 0; c < COMBINE_COLS; ++c) v[c] = dacc[c];
+    }
+    const bool plain = (alpha == 1.0 && beta == 0.0);
+    double* crow = C + i * ldc;
+#pragma unroll
+    for (int c = 0; c < COMBINE_COLS; ++c) {
+        const int64_t j = j0 + c;
+        if (j >= n) break;
+        if (plain) crow[j] = v[c];
         else {
-            v *= alpha;
-            *c = (beta == 0.0) ? v : fma(beta, *c, v);
+            const double x = alpha * v[c];
+            crow[j] = (beta == 0.0) ? x : fma(beta, crow[j], x);
         }
+    }
     }
 }
 
@@ -890,10 +913,12 @@ int split_gemm(const Gemm& g, const SplitRequest& req, const LaunchCtl& ctl, cud
         KernelTimer timer("tc_gemm", st);
         kern<<<grid, THREADS, kTcSmem, st>>>(tA, tB, p);
     }
-    const int64_t total = m * n;
-    const int cblocks = int(std::min<int64_t>((total + 255) / 256, int64_t(r.num_sms) * 16));
-    combine_kernel<<<cblocks, 256, 0, st>>>(lv, nseg, max_levels, mpad, npad, mode, info, eA, eB, m, n, g.alpha,
-                                            g.beta, static_cast<double*>(g.C), g.ldc);
+    {
+        const int64_t colgroups = (n + COMBINE_COLS - 1) / COMBINE_COLS;
+        dim3 cgrid(unsigned((colgroups + 127) / 128), unsigned(std::min<int64_t>(m, 65535)));
+        combine_kernel<<<cgrid, 128, 0, st>>>(lv, nseg, max_levels, mpad, npad, mode, info, eA, eB, m, n, g.alpha,
+                                              g.beta, static_cast<double*>(g.C), g.ldc);
+    }
     count_launches(2);
     e = cudaGetLastError();
     if (e != cudaSuccess) {

@@ -33,6 +33,7 @@ UNITS = [
     ("split_gemm.cu", "split_gemm.o", []),
     ("peaks.cu", "peaks.o", []),
     ("profile.cpp", "profile.o", []),
+    ("grouped.cu", "grouped.o", []),
 ]
 
 

@@ -109,6 +109,48 @@ int64_t gb300_launch_count(void);
 /* Wait until all work the library queued on its own stream has finished. */
 int gb300_synchronize(void);
 
+/* ---- grouped (batched) products -----------------------------------------------------------
+ * Many independent, uneven products (Blaze's StaticMatrix / HybridMatrix sizes) in one persistent
+ * launch.  Each problem uses the CBLAS conventions of gb300_dgemm_ex; A, B and C must be device (or
+ * managed) memory.  alpha/beta are taken as double (converted for the float form).  Blaze has no
+ * batched product: this replaces a loop of per-product calls (blaze/math/expressions/
+ * DMatDMatMultExpr.h:864-1878, the small kernel each such product runs on the CPU). */
+typedef struct gb300_gemm_problem {
+    int order, transA, transB;
+    int64_t m, n, k;
+    double alpha, beta;
+    const void* A;
+    int64_t lda;
+    const void* B;
+    int64_t ldb;
+    void* C;
+    int64_t ldc;
+} gb300_gemm_problem;
+
+typedef struct gb300_grouped_plan gb300_grouped_plan;
+
+/* Tile every problem with the warp-tile shape of its size class (autotuned, see below), upload the
+ * problem and tile tables and capture the launch in a CUDA graph.  elem_bytes: 8 (double) or 4. */
+int gb300_grouped_plan_create(int elem_bytes, const gb300_gemm_problem* problems, int64_t count,
+                              gb300_grouped_plan** plan);
+/* One graph launch on `stream` (NULL: the library stream); asynchronous. */
+int gb300_grouped_plan_run(gb300_grouped_plan* plan, void* stream);
+/* Tiles of the plan and the useful / padded multiply-add work (2*m*n*k summed, in flops). */
+int gb300_grouped_plan_info(const gb300_grouped_plan* plan, int64_t* tiles, double* useful_flops,
+                            double* padded_flops);
+void gb300_grouped_plan_destroy(gb300_grouped_plan* plan);
+/* Plan, run and destroy in one call; returns after the products finished. */
+int gb300_dgemm_grouped(const gb300_gemm_problem* problems, int64_t count, void* stream);
+int gb300_sgemm_grouped(const gb300_gemm_problem* problems, int64_t count, void* stream);
+/* Autotuner: time every warp-tile shape on synthetic batches of each size class (m, n bucketed by
+ * powers of two up to 256, k in three ranges) and keep the fastest per class.  effort >= 1 scales
+ * the batch size.  Tables persist through save/load ("gb300-grouped-tune v1" text files). */
+int gb300_grouped_autotune(int elem_bytes, int effort);
+int gb300_grouped_tuning_save(const char* path);
+int gb300_grouped_tuning_load(const char* path);
+/* Shape index the planner uses for a product, with its warp-tile rows and columns. */
+int gb300_grouped_shape_for(int elem_bytes, int64_t m, int64_t n, int64_t k, int* rows, int* cols);
+
 /* Allocation-free variant of the native FP64 product, for callers that cannot allocate device
  * memory themselves (a host framework that owns all device memory through its own pool or
  * budget, or a latency-critical loop where cudaMalloc/cudaFree and their implicit device
