@@ -139,6 +139,19 @@ class Clocks:
                 "samples": len(sm)}
 
 
+def uniform(n: int, seed: int, lo: float = -1.0, hi: float = 1.0):
+    """Seeded MT19937 uniform doubles (numpy's legacy stream; the oracle's generator yields the same
+    values, which tests/test_oracle.py pins)."""
+    import numpy as np
+    return lo + (hi - lo) * np.random.RandomState(seed).random_sample(n)
+
+
+def batch_sizes(count: int, seed: int, lo: int = 4, hi: int = 256):
+    import numpy as np
+    u = uniform(3 * count, seed, np.log(lo), np.log(hi))
+    return np.clip(np.rint(np.exp(u)).astype(np.int64), lo, hi).reshape(count, 3)
+
+
 def read_peaks():
     try:
         with open(PEAKS_FILE) as f:
@@ -147,8 +160,9 @@ def read_peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
 
 
-# ---- CPU baseline (the oracle's restatement of Blaze's blocked kernel) --------------------------
+# ---- CPU legs: the timed CPU baseline and the accuracy check, both through the oracle ----------
 def cpu_baseline(size: int, seconds_target: float = 12.0):
+    """Time the oracle's restatement of Blaze's blocked kernel on the host cores."""
     import numpy as np
     import oracle as O
     n = size
@@ -170,6 +184,12 @@ def cpu_baseline(size: int, seconds_target: float = 12.0):
     return {"value": round(tflops, 5), "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"{reps} product(s) of {n}^3 FP64 (row-major x row-major, uniform [-1,1]) through the oracle's "
                       f"restatement of Blaze's blocked mmm kernel, {threads} OpenMP threads, {total:.1f} s"}
+
+
+def cpu_check_rows(hA, hB, n: int, rows):
+    """Compensated (Dot2) FP64 reference rows of A*B from the oracle: the checker of the GPU results."""
+    import oracle as O
+    return O.product_rows_dot2(O.ROW_MAJOR, O.NO_TRANS, O.NO_TRANS, n, n, n, hA, n, hB, n, rows=rows)
 
 
 def reference_arm(args, dist: Dist):
@@ -229,14 +249,30 @@ def batched_leg(G, torch, args, dev):
     FP64 and FP32: one persistent grouped launch (CUDA graph) against a loop of per-product
     launches of the native kernel, both device-resident."""
     import numpy as np
-    sys.path.insert(0, os.path.join(ROOT, "tests"))
-    from batched import build
+
+    def build(count, seed, dtype):
+        mnk = batch_sizes(count, seed)
+        specs, offA, offB, offC = [], 0, 0, 0
+        for q in range(count):
+            m, n, k = (int(x) for x in mnk[q])
+            specs.append(dict(order=101, transA=111, transB=111, m=m, n=n, k=k, alpha=1.0, beta=0.0,
+                              offA=offA, lda=k, offB=offB, ldb=n, offC=offC, ldc=n))
+            offA += m * k; offB += k * n; offC += m * n
+        dA = torch.from_numpy(uniform(offA, seed + 1).astype(dtype)).cuda()
+        dB = torch.from_numpy(uniform(offB, seed + 2).astype(dtype)).cuda()
+        dC = torch.zeros(offC, dtype=dA.dtype, device="cuda")
+        esz = dA.element_size()
+        for sp in specs:
+            sp["A"] = dA.data_ptr() + sp["offA"] * esz
+            sp["B"] = dB.data_ptr() + sp["offB"] * esz
+            sp["C"] = dC.data_ptr() + sp["offC"] * esz
+        return specs, dA, dB, dC
 
     out = {"workload": f"{args.batch_count} products, M,N,K log-uniform integers in [4,256], uniform [-1,1], "
                        "row-major, device-resident"}
     s = torch.cuda.Stream(device=dev)
     for name, dtype, esz in (("fp64", np.float64, 8), ("fp32", np.float32, 4)):
-        specs, A, B, C0, dA, dB, dC = build(torch, args.batch_count, seed=args.seed + 100, dtype=dtype)
+        specs, dA, dB, dC = build(args.batch_count, args.seed + 100, dtype)
         probs = G.problems(specs)
         t0 = time.perf_counter()
         plan = G.GroupedPlan(probs, esz)
@@ -295,10 +331,9 @@ def ours(args, dist: Dist):
     flops = 2.0 * n ** 3
     s = torch.cuda.Stream(device=dev)
 
-    import oracle as O
     # inputs: seeded mt19937 uniform [-1,1] built on the host (exactly reproducible), then resident
-    hA = torch.from_numpy(O.uniform(n * n, args.seed + 17 * dist.rank))
-    hB = torch.from_numpy(O.uniform(n * n, args.seed + 17 * dist.rank + 1))
+    hA = torch.from_numpy(uniform(n * n, args.seed + 17 * dist.rank))
+    hB = torch.from_numpy(uniform(n * n, args.seed + 17 * dist.rank + 1))
     with torch.cuda.stream(s):
         dA = hA.to(f"cuda:{dev}", non_blocking=False)
         dB = hB.to(f"cuda:{dev}", non_blocking=False)
@@ -342,7 +377,7 @@ def ours(args, dist: Dist):
     G.synchronize()
     C = dC.cpu().numpy().reshape(n, n)
     rows = np.arange(0, n, max(1, n // 32))
-    P = O.product_rows_dot2(O.ROW_MAJOR, O.NO_TRANS, O.NO_TRANS, n, n, n, hA.numpy(), n, hB.numpy(), n, rows=rows)
+    P = cpu_check_rows(hA.numpy(), hB.numpy(), n, rows)
     nA = float(np.linalg.norm(hA.numpy()))
     nB = float(np.linalg.norm(hB.numpy()))
     err = float(np.linalg.norm(C[rows] - P) * np.sqrt(n / len(rows)) / (nA * nB))
