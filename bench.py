@@ -408,6 +408,12 @@ def ours(args, dist: Dist):
     if not args.no_e2e:
         e2e = e2e_leg(G, hA, hB, n, flops, args, dist)
 
+    batched = None
+    if not args.no_batched:
+        batched = batched_leg(G, torch, args, dev)
+        if native:
+            batched["fp64"]["frac_of_fp64_peak"] = round(batched["fp64"]["grouped_tflops"] / native["fp64_peak_tflops"], 4)
+
     peaks, peaks_src = read_peaks()
 
     pairs = info.slices_used * (info.slices_used + 1) // 2
