@@ -53,6 +53,37 @@ class GemmProblem(ct.Structure):
     ]
 
 
+class ServerConfig(ct.Structure):
+    _fields_ = [("memory_budget_bytes", ct.c_int64), ("slots", ct.c_int), ("reserve_sms", ct.c_int),
+                ("aging_ms", ct.c_double), ("large_threshold", ct.c_int64)]
+
+
+class ServeRequest(ct.Structure):
+    _fields_ = [
+        ("order", ct.c_int), ("transA", ct.c_int), ("transB", ct.c_int),
+        ("m", ct.c_int64), ("n", ct.c_int64), ("k", ct.c_int64),
+        ("alpha", ct.c_double), ("beta", ct.c_double),
+        ("A", ct.c_void_p), ("lda", ct.c_int64),
+        ("B", ct.c_void_p), ("ldb", ct.c_int64),
+        ("C", ct.c_void_p), ("ldc", ct.c_int64),
+        ("accuracy", ct.c_int), ("target_error", ct.c_double),
+    ]
+
+
+class ServeResult(ct.Structure):
+    _fields_ = [("status", ct.c_int), ("method_used", ct.c_int), ("slices", ct.c_int),
+                ("error_bound", ct.c_double), ("queue_ms", ct.c_double), ("run_ms", ct.c_double),
+                ("latency_ms", ct.c_double)]
+
+
+class ServerStats(ct.Structure):
+    _fields_ = [("submitted", ct.c_int64), ("completed", ct.c_int64), ("rejected", ct.c_int64),
+                ("failed", ct.c_int64), ("queued", ct.c_int64),
+                ("p50_ms", ct.c_double), ("p99_ms", ct.c_double), ("mean_ms", ct.c_double), ("max_ms", ct.c_double),
+                ("wall_s", ct.c_double), ("tflops", ct.c_double),
+                ("bytes_in_use", ct.c_int64), ("peak_bytes", ct.c_int64), ("budget_bytes", ct.c_int64)]
+
+
 class Gb300Error(RuntimeError):
     def __init__(self, status: int, message: str):
         super().__init__(f"[status {status}] {message}")
@@ -127,6 +158,22 @@ def lib() -> ct.CDLL:
     L.gb300_grouped_tuning_load.restype = ct.c_int
     L.gb300_grouped_shape_for.argtypes = [ct.c_int, I64, I64, I64, ct.POINTER(ct.c_int), ct.POINTER(ct.c_int)]
     L.gb300_grouped_shape_for.restype = ct.c_int
+    L.gb300_server_config_init.argtypes = [ct.POINTER(ServerConfig)]
+    L.gb300_server_config_init.restype = None
+    L.gb300_server_create.argtypes = [ct.POINTER(ServerConfig), ct.POINTER(VP)]
+    L.gb300_server_create.restype = ct.c_int
+    L.gb300_server_submit.argtypes = [VP, ct.POINTER(ServeRequest), ct.POINTER(ct.c_uint64)]
+    L.gb300_server_submit.restype = ct.c_int
+    L.gb300_server_wait.argtypes = [VP, ct.c_uint64, ct.c_double, ct.POINTER(ServeResult)]
+    L.gb300_server_wait.restype = ct.c_int
+    L.gb300_server_poll.argtypes = [VP, ct.c_uint64, ct.POINTER(ct.c_int)]
+    L.gb300_server_poll.restype = ct.c_int
+    L.gb300_server_get_stats.argtypes = [VP, ct.POINTER(ServerStats)]
+    L.gb300_server_get_stats.restype = ct.c_int
+    L.gb300_server_reset_stats.argtypes = [VP]
+    L.gb300_server_reset_stats.restype = None
+    L.gb300_server_destroy.argtypes = [VP]
+    L.gb300_server_destroy.restype = None
     L.gb300_select_device.argtypes = [ct.c_int]
     L.gb300_select_device.restype = ct.c_int
     L.gb300_profile_enable.argtypes = [ct.c_int]
@@ -277,6 +324,67 @@ def grouped_shape_for(elem_bytes: int, m: int, n: int, k: int) -> tuple[int, int
     r, c = ct.c_int(0), ct.c_int(0)
     s = lib().gb300_grouped_shape_for(elem_bytes, m, n, k, ct.byref(r), ct.byref(c))
     return s, r.value, c.value
+
+
+class Server:
+    """Continuous-batching request server (gb300_server_*); operands are device-resident."""
+
+    def __init__(self, budget_bytes: int | None = None, slots: int | None = None, reserve_sms: int | None = None,
+                 aging_ms: float | None = None, large_threshold: int | None = None):
+        cfg = ServerConfig()
+        lib().gb300_server_config_init(ct.byref(cfg))
+        if budget_bytes is not None:
+            cfg.memory_budget_bytes = budget_bytes
+        if slots is not None:
+            cfg.slots = slots
+        if reserve_sms is not None:
+            cfg.reserve_sms = reserve_sms
+        if aging_ms is not None:
+            cfg.aging_ms = aging_ms
+        if large_threshold is not None:
+            cfg.large_threshold = large_threshold
+        self.handle = ct.c_void_p()
+        check(lib().gb300_server_create(ct.byref(cfg), ct.byref(self.handle)))
+
+    def submit(self, order, transA, transB, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, accuracy="split",
+               target_error: float = 0.0) -> int:
+        r = ServeRequest()
+        r.order, r.transA, r.transB, r.m, r.n, r.k = order, transA, transB, m, n, k
+        r.alpha, r.beta = alpha, beta
+        r.A, r.lda, r.B, r.ldb, r.C, r.ldc = _addr(A), lda, _addr(B), ldb, _addr(C), ldc
+        r.accuracy = METHODS[accuracy] if isinstance(accuracy, str) else int(accuracy)
+        r.target_error = target_error
+        t = ct.c_uint64(0)
+        st = lib().gb300_server_submit(self.handle, ct.byref(r), ct.byref(t))
+        if st != OK:
+            raise Gb300Error(st, last_error()[1])
+        return t.value
+
+    def wait(self, ticket: int, timeout_ms: float = -1.0) -> ServeResult:
+        res = ServeResult()
+        st = lib().gb300_server_wait(self.handle, ticket, timeout_ms, ct.byref(res))
+        if st != OK:
+            raise Gb300Error(st, last_error()[1] or f"request status {st}")
+        return res
+
+    def stats(self) -> ServerStats:
+        s = ServerStats()
+        check(lib().gb300_server_get_stats(self.handle, ct.byref(s)))
+        return s
+
+    def reset_stats(self) -> None:
+        lib().gb300_server_reset_stats(self.handle)
+
+    def close(self) -> None:
+        if self.handle:
+            lib().gb300_server_destroy(self.handle)
+            self.handle = ct.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:  # noqa: BLE001
+            pass
 
 
 def device_info() -> tuple[int, int, int]:

@@ -221,7 +221,7 @@ int gemm_entry(int order, int transA, int transB, int64_t m, int64_t n, int64_t 
         req.slices = opts ? opts->slices : 0;
         req.target_error = opts ? opts->target_error : 0.0;
         SplitResult res_out;
-        st = split_gemm(g, req, ctl, s, &res_out, &err);
+        st = device_product(g, req, ctl, s, r.ws, &res_out, &err);
         if (st != GB300_OK) return fail(st, err);
         used = res_out.method_used;
         info_dev = res_out.info_dev;

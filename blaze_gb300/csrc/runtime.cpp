@@ -103,22 +103,23 @@ int ensure_init(std::string* err) {
     }
     r.device = dev;
     r.num_sms = prop.multiProcessorCount;
+    r.ws.stream = r.stream;
+    r.ws.d_status = r.d_status;
     r.inited = true;
     return GB300_OK;
 }
 
-void* pool_get(int s, size_t bytes, std::string* err) {
-    Runtime& r = runtime();
-    if (bytes == 0) bytes = 256;
-    if (r.pool_bytes[s] >= bytes) return r.pool[s];
-    if (r.pool[s]) {
-        cudaStreamSynchronize(r.stream);
-        cudaFree(r.pool[s]);
-        r.pool[s] = nullptr;
-        r.pool_bytes[s] = 0;
+void* Workspace::get(int s, size_t n, std::string* err) {
+    if (n == 0) n = 256;
+    if (bytes[s] >= n) return ptr[s];
+    if (ptr[s]) {
+        cudaStreamSynchronize(stream);
+        cudaFree(ptr[s]);
+        ptr[s] = nullptr;
+        bytes[s] = 0;
     }
     // round up to 2 MiB so that slowly growing sizes do not reallocate every call
-    const size_t rounded = (bytes + (size_t(2) << 20) - 1) & ~((size_t(2) << 20) - 1);
+    const size_t rounded = (n + (size_t(2) << 20) - 1) & ~((size_t(2) << 20) - 1);
     void* p = nullptr;
     cudaError_t e = cudaMalloc(&p, rounded);
     if (e != cudaSuccess) {
@@ -126,10 +127,27 @@ void* pool_get(int s, size_t bytes, std::string* err) {
         if (err) *err = "device allocation of " + std::to_string(rounded) + " bytes failed: " + cudaGetErrorString(e);
         return nullptr;
     }
-    r.pool[s] = p;
-    r.pool_bytes[s] = rounded;
+    ptr[s] = p;
+    bytes[s] = rounded;
     return p;
 }
+
+size_t Workspace::total() const {
+    size_t t = 0;
+    for (int s = 0; s < kSlotCount; ++s) t += bytes[s];
+    return t;
+}
+
+void Workspace::release() {
+    if (stream) cudaStreamSynchronize(stream);
+    for (int s = 0; s < kSlotCount; ++s) {
+        if (ptr[s]) cudaFree(ptr[s]);
+        ptr[s] = nullptr;
+        bytes[s] = 0;
+    }
+}
+
+void* pool_get(int s, size_t bytes, std::string* err) { return runtime().ws.get(s, bytes, err); }
 
 bool encode_tmap_2d(CUtensorMap* map, CUtensorMapDataType dtype, size_t elem_bytes, const void* base,
                     uint64_t rows, uint64_t cols, uint64_t ld, uint32_t box_rows, uint32_t box_cols,

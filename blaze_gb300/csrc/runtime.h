@@ -28,15 +28,28 @@ enum Slot : int {
     kSlotCount
 };
 
+// Grow-only device buffers of one execution context (the library's default context, or one slot
+// of a server), used on that context's stream.  A slot keeps its high-water allocation, so
+// repeated calls of similar size allocate nothing.
+struct Workspace {
+    cudaStream_t stream = nullptr;
+    int* d_status = nullptr;       // device status word written by kernels (DeviceStatus)
+    void* ptr[kSlotCount] = {};
+    size_t bytes[kSlotCount] = {};
+    // Buffer of at least `n` bytes in slot `s`; nullptr (and *err) on allocation failure.
+    void* get(int s, size_t n, std::string* err);
+    size_t total() const;
+    void release();                // frees every buffer (after the stream drained)
+};
+
 struct Runtime {
     std::mutex mu;                 // one queue: GPU work submitted through the library is serialized
     bool inited = false;
     int device = -1;
     int num_sms = 0;
     cudaStream_t stream = nullptr;
-    int* d_status = nullptr;       // device status word written by kernels (DeviceStatus)
-    void* pool[kSlotCount] = {};
-    size_t pool_bytes[kSlotCount] = {};
+    int* d_status = nullptr;       // device status word of the default context
+    Workspace ws;                  // default context (stream = `stream`)
     std::atomic<int64_t> launches{0};
     int inject_stall_count = 0;
     uint64_t inject_limit_ns = 0;
@@ -47,7 +60,8 @@ Runtime& runtime();
 // Initialise the device state once (thread-safe).  Returns a gb300_status.
 int ensure_init(std::string* err);
 
-// Device buffer of at least `bytes` in slot `s` (caller holds runtime().mu).  nullptr on failure.
+// Device buffer of at least `bytes` in slot `s` of the default context (caller holds
+// runtime().mu).  nullptr on failure.
 void* pool_get(int s, size_t bytes, std::string* err);
 
 // Thread-local last error.

@@ -1,0 +1,455 @@
+// serve.cpp — request loop with continuous batching for dense products on one GB300.
+//
+// Blaze has no server; this is the serving form of the same C = alpha*op(A)*op(B) + beta*C path
+// (one request = one product, CBLAS argument conventions, device-resident operands).
+//
+// Model:
+//   * Requests arrive at any time (gb300_server_submit) and wait in a queue.
+//   * A scheduler thread admits them while a stream slot is free and the device memory the
+//     request needs (its scratch, from device_product_footprint) fits the server's budget next to
+//     what running requests hold; a request that cannot fit even on an idle server is rejected.
+//     Admission is FIFO with backfill: a smaller request may pass a head request that does not fit
+//     yet, unless the head has waited longer than the aging limit.
+//   * Each slot owns a stream and a grow-only workspace, so admitted requests run concurrently
+//     and their kernels overlap on the device.  While a large tensor-core product runs, a share of
+//     the SMs is kept out of its persistent grid so that small requests keep flowing.
+//   * Completion is detected with a CUDA event per request; latency = completion - submission.
+//   * Results do not depend on the mix: the split form accumulates exact integers (its k-segments
+//     depend only on the shape), BF16 forms have a fixed accumulation order per tile, and the
+//     native kernel's split-k choice depends only on the shape.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/gb300_blas.h"
+#include "gb300_internal.h"
+#include "ptx.cuh"
+#include "runtime.h"
+#include "split_api.h"
+
+namespace gb {
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+double ms_between(Clock::time_point a, Clock::time_point b) {
+    return std::chrono::duration<double, std::milli>(b - a).count();
+}
+
+struct ServeRequest {
+    uint64_t id = 0;
+    gb300_serve_request req{};
+    Gemm g;
+    SplitRequest sreq;
+    size_t footprint = 0;
+    bool large = false;
+    Clock::time_point t_submit, t_start, t_end;
+    int slot = -1;
+    int state = 0;  // 0 queued, 1 running, 2 done
+    gb300_serve_result res{};
+    cudaEvent_t done = nullptr;
+    const void* info_dev = nullptr;
+};
+
+struct ServeSlot {
+    cudaStream_t stream = nullptr;
+    Workspace ws;
+    ServeRequest* cur = nullptr;
+};
+
+}  // namespace
+
+class Server {
+  public:
+    gb300_server_config cfg{};
+    std::vector<ServeSlot> slots;
+    std::deque<ServeRequest*> queue;
+    std::unordered_map<uint64_t, ServeRequest*> reqs;
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    std::thread worker;
+    bool stop = false;
+    uint64_t next_id = 1;
+    size_t budget = 0;
+    int num_sms = 0;
+    // statistics
+    std::vector<double> latencies;
+    int64_t submitted = 0, completed = 0, rejected = 0, failed = 0;
+    double useful_flops = 0;
+    Clock::time_point t_first;
+    bool any = false;
+    size_t peak_bytes = 0;
+
+    size_t bytes_held() const {
+        size_t t = 0;
+        for (const auto& s : slots) t += s.ws.total();
+        return t;
+    }
+
+    bool large_running() const {
+        for (const auto& s : slots)
+            if (s.cur && s.cur->large) return true;
+        return false;
+    }
+
+    // Try to start `r` on a free slot; returns true when launched.
+    bool try_admit(ServeRequest* r) {
+        int free_slot = -1;
+        for (size_t i = 0; i < slots.size(); ++i)
+            if (!slots[i].cur) { free_slot = int(i); break; }
+        if (free_slot < 0) return false;
+        ServeSlot& sl = slots[size_t(free_slot)];
+        size_t others = 0;
+        for (size_t i = 0; i < slots.size(); ++i)
+            if (int(i) != free_slot) others += slots[i].ws.total();
+        size_t mine = std::max(sl.ws.total(), r->footprint);
+        if (others + mine > budget) {
+            // give back memory of idle slots before refusing
+            for (size_t i = 0; i < slots.size(); ++i)
+                if (!slots[i].cur && slots[i].ws.total() > 0) slots[i].ws.release();
+            others = 0;
+            for (size_t i = 0; i < slots.size(); ++i)
+                if (int(i) != free_slot) others += slots[i].ws.total();
+            mine = std::max(sl.ws.total(), r->footprint);
+            if (others + mine > budget) return false;
+        }
+        launch(r, free_slot);
+        return true;
+    }
+
+    void launch(ServeRequest* r, int si) {
+        ServeSlot& sl = slots[size_t(si)];
+        r->slot = si;
+        r->state = 1;
+        r->t_start = Clock::now();
+        sl.cur = r;
+        LaunchCtl ctl;
+        ctl.status = sl.ws.d_status;
+        SplitRequest sreq = r->sreq;
+        // keep SMs for small requests while a large tensor-core product runs
+        if (r->large && cfg.reserve_sms > 0) sreq.max_sms = std::max(1, num_sms - cfg.reserve_sms);
+        std::string err;
+        cudaMemsetAsync(sl.ws.d_status, 0, sizeof(int), sl.stream);
+        SplitResult res;
+        const int st = device_product(r->g, sreq, ctl, sl.stream, sl.ws, &res, &err);
+        r->res.status = st;
+        r->res.method_used = res.method_used;
+        r->res.slices = res.slices;
+        r->res.error_bound = res.error_bound;
+        r->info_dev = res.info_dev;
+        cudaEventRecord(r->done, sl.stream);
+        peak_bytes = std::max(peak_bytes, bytes_held());
+        if (st != GB300_OK) r->res.status = st;
+    }
+
+    void complete(ServeSlot& sl) {
+        ServeRequest* r = sl.cur;
+        r->t_end = Clock::now();
+        int status = 0;
+        cudaMemcpy(&status, sl.ws.d_status, sizeof(int), cudaMemcpyDeviceToHost);
+        if (r->res.status == GB300_OK && status != 0) r->res.status = GB300_ERR_DEVICE_TIMEOUT;
+        if (r->info_dev) {
+            int sl_ = 0;
+            double bd = 0;
+            if (split_read_info(r->info_dev, &sl_, &bd)) {
+                r->res.slices = sl_;
+                r->res.error_bound = bd;
+            }
+        }
+        r->res.queue_ms = ms_between(r->t_submit, r->t_start);
+        r->res.latency_ms = ms_between(r->t_submit, r->t_end);
+        r->res.run_ms = ms_between(r->t_start, r->t_end);
+        r->state = 2;
+        if (r->res.status == GB300_OK) {
+            ++completed;
+            latencies.push_back(r->res.latency_ms);
+            useful_flops += 2.0 * double(r->g.m) * double(r->g.n) * double(r->g.k);
+        } else {
+            ++failed;
+        }
+        sl.cur = nullptr;
+    }
+
+    void loop() {
+        std::unique_lock<std::mutex> lock(mu);
+        while (!stop) {
+            bool progressed = false;
+            // completions
+            for (auto& sl : slots) {
+                if (sl.cur && cudaEventQuery(sl.cur->done) == cudaSuccess) {
+                    complete(sl);
+                    progressed = true;
+                }
+            }
+            if (progressed) cv_done.notify_all();
+            // admissions: FIFO with backfill, unless the head has aged past the limit
+            const auto now = Clock::now();
+            bool head_blocked = false;
+            for (auto it = queue.begin(); it != queue.end();) {
+                ServeRequest* r = *it;
+                if (head_blocked) break;
+                if (try_admit(r)) {
+                    it = queue.erase(it);
+                    progressed = true;
+                } else {
+                    if (it == queue.begin() && ms_between(r->t_submit, now) > cfg.aging_ms) head_blocked = true;
+                    ++it;
+                }
+            }
+            bool busy = false;
+            for (const auto& sl : slots) busy |= (sl.cur != nullptr);
+            if (!progressed) {
+                // running work is polled every 20 us; an idle server sleeps until a submission
+                if (busy) cv_work.wait_for(lock, std::chrono::microseconds(20));
+                else cv_work.wait(lock, [&] { return stop || !queue.empty(); });
+            }
+        }
+    }
+};
+
+}  // namespace gb
+
+// ============================================================================================
+//  C-ABI
+// ============================================================================================
+extern "C" {
+
+void gb300_server_config_init(gb300_server_config* c) {
+    if (!c) return;
+    std::memset(c, 0, sizeof(*c));
+    c->memory_budget_bytes = int64_t(150) << 30;
+    c->slots = 8;
+    c->reserve_sms = 16;
+    c->aging_ms = 50.0;
+    c->large_threshold = 2048;
+}
+
+int gb300_server_create(const gb300_server_config* cfg, gb300_server** out) {
+    if (!out) return GB300_ERR_INVALID_ARG;
+    gb::Runtime& r = gb::runtime();
+    std::string err;
+    {
+        std::lock_guard<std::mutex> lock(r.mu);
+        const int st = gb::ensure_init(&err);
+        if (st != GB300_OK) {
+            gb::set_error(st, "gb300_server_create: " + err);
+            return st;
+        }
+    }
+    auto* s = new gb::Server();
+    if (cfg) s->cfg = *cfg;
+    else gb300_server_config_init(&s->cfg);
+    if (s->cfg.slots <= 0) s->cfg.slots = 1;
+    size_t fr = 0, tot = 0;
+    cudaMemGetInfo(&fr, &tot);
+    s->budget = size_t(std::max<int64_t>(s->cfg.memory_budget_bytes, 0));
+    s->budget = std::min(s->budget, size_t(double(fr) * 0.95));
+    s->num_sms = r.num_sms;
+    s->slots.resize(size_t(s->cfg.slots));
+    for (auto& sl : s->slots) {
+        cudaError_t e = cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaMalloc(&sl.ws.d_status, 64);
+        if (e != cudaSuccess) {
+            gb::set_error(GB300_ERR_CUDA, std::string("gb300_server_create: ") + cudaGetErrorString(e));
+            delete s;
+            return GB300_ERR_CUDA;
+        }
+        cudaMemset(sl.ws.d_status, 0, 64);
+        sl.ws.stream = sl.stream;
+    }
+    s->worker = std::thread([s] { s->loop(); });
+    *out = reinterpret_cast<gb300_server*>(s);
+    return GB300_OK;
+}
+
+int gb300_server_submit(gb300_server* srv, const gb300_serve_request* q, uint64_t* ticket) {
+    auto* s = reinterpret_cast<gb::Server*>(srv);
+    if (!s || !q || !ticket) return GB300_ERR_INVALID_ARG;
+    const bool rm = q->order == 101;
+    const bool tA = q->transA != 111, tB = q->transB != 111;
+    if ((q->order != 101 && q->order != 102) || q->m < 0 || q->n < 0 || q->k < 0 ||
+        q->lda < std::max<int64_t>(1, rm ? (tA ? q->m : q->k) : (tA ? q->k : q->m)) ||
+        q->ldb < std::max<int64_t>(1, rm ? (tB ? q->k : q->n) : (tB ? q->n : q->k)) ||
+        q->ldc < std::max<int64_t>(1, rm ? q->n : q->m) || q->accuracy < GB300_METHOD_AUTO ||
+        q->accuracy > GB300_METHOD_BF16) {
+        gb::set_error(GB300_ERR_INVALID_ARG, "gb300_server_submit: invalid request");
+        return GB300_ERR_INVALID_ARG;
+    }
+    auto* r = new gb::ServeRequest();
+    r->req = *q;
+    gb::Gemm& g = r->g;
+    if (rm) {
+        g.m = q->m; g.n = q->n; g.ta = tA; g.tb = tB; g.A = q->A; g.lda = q->lda; g.B = q->B; g.ldb = q->ldb;
+    } else {
+        g.m = q->n; g.n = q->m; g.ta = tB; g.tb = tA; g.A = q->B; g.lda = q->ldb; g.B = q->A; g.ldb = q->lda;
+    }
+    g.k = (q->alpha == 0.0) ? 0 : q->k;
+    g.C = q->C;
+    g.ldc = q->ldc;
+    g.alpha = q->alpha;
+    g.beta = q->beta;
+    auto aligned = [](const void* p, int64_t ld) { return reinterpret_cast<uintptr_t>(p) % 16 == 0 && (ld * 8) % 16 == 0; };
+    if (g.k > 0 && (!aligned(g.A, g.lda) || !aligned(g.B, g.ldb))) {
+        delete r;
+        gb::set_error(GB300_ERR_INVALID_ARG, "gb300_server_submit: operands need 16-byte aligned bases and even "
+                                             "leading dimensions");
+        return GB300_ERR_INVALID_ARG;
+    }
+    r->sreq.method = q->accuracy;
+    r->sreq.target_error = q->target_error;
+    r->sreq.slices = 0;
+    r->large = std::max(q->m, q->n) >= s->cfg.large_threshold && q->accuracy != GB300_METHOD_NATIVE;
+    r->footprint = (g.m > 0 && g.n > 0) ? gb::device_product_footprint(g, r->sreq) : 0;
+    if (cudaEventCreateWithFlags(&r->done, cudaEventDisableTiming) != cudaSuccess) {
+        delete r;
+        gb::set_error(GB300_ERR_CUDA, "gb300_server_submit: event creation failed");
+        return GB300_ERR_CUDA;
+    }
+    std::lock_guard<std::mutex> lock(s->mu);
+    r->id = s->next_id++;
+    r->t_submit = gb::Clock::now();
+    if (!s->any) {
+        s->any = true;
+        s->t_first = r->t_submit;
+    }
+    ++s->submitted;
+    s->reqs[r->id] = r;
+    *ticket = r->id;
+    if (r->footprint > s->budget) {
+        r->state = 2;
+        r->res.status = GB300_ERR_ADMISSION;
+        r->t_start = r->t_end = r->t_submit;
+        ++s->rejected;
+        s->cv_done.notify_all();
+        gb::set_error(GB300_ERR_ADMISSION, "gb300_server_submit: the request needs " + std::to_string(r->footprint) +
+                                               " bytes of device memory, above the server budget of " +
+                                               std::to_string(s->budget));
+        return GB300_ERR_ADMISSION;
+    }
+    if (g.m == 0 || g.n == 0) {
+        r->state = 2;
+        r->res.status = GB300_OK;
+        r->t_start = r->t_end = r->t_submit;
+        ++s->completed;
+        s->cv_done.notify_all();
+        return GB300_OK;
+    }
+    s->queue.push_back(r);
+    s->cv_work.notify_one();
+    return GB300_OK;
+}
+
+int gb300_server_wait(gb300_server* srv, uint64_t ticket, double timeout_ms, gb300_serve_result* res) {
+    auto* s = reinterpret_cast<gb::Server*>(srv);
+    if (!s) return GB300_ERR_INVALID_ARG;
+    std::unique_lock<std::mutex> lock(s->mu);
+    auto it = s->reqs.find(ticket);
+    if (it == s->reqs.end()) {
+        gb::set_error(GB300_ERR_INVALID_ARG, "gb300_server_wait: unknown ticket");
+        return GB300_ERR_INVALID_ARG;
+    }
+    gb::ServeRequest* r = it->second;
+    const auto pred = [&] { return r->state == 2; };
+    if (timeout_ms < 0) s->cv_done.wait(lock, pred);
+    else if (!s->cv_done.wait_for(lock, std::chrono::duration<double, std::milli>(timeout_ms), pred)) {
+        gb::set_error(GB300_ERR_DEVICE_TIMEOUT, "gb300_server_wait: the request has not finished yet");
+        return GB300_ERR_DEVICE_TIMEOUT;
+    }
+    if (res) *res = r->res;
+    cudaEventDestroy(r->done);
+    s->reqs.erase(it);
+    const int st = r->res.status;
+    delete r;
+    return st;
+}
+
+int gb300_server_poll(gb300_server* srv, uint64_t ticket, int* done) {
+    auto* s = reinterpret_cast<gb::Server*>(srv);
+    if (!s || !done) return GB300_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> lock(s->mu);
+    auto it = s->reqs.find(ticket);
+    if (it == s->reqs.end()) return GB300_ERR_INVALID_ARG;
+    *done = it->second->state == 2;
+    return GB300_OK;
+}
+
+int gb300_server_get_stats(gb300_server* srv, gb300_server_stats* out) {
+    auto* s = reinterpret_cast<gb::Server*>(srv);
+    if (!s || !out) return GB300_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> lock(s->mu);
+    std::memset(out, 0, sizeof(*out));
+    out->submitted = s->submitted;
+    out->completed = s->completed;
+    out->rejected = s->rejected;
+    out->failed = s->failed;
+    out->queued = int64_t(s->queue.size());
+    std::vector<double> l = s->latencies;
+    if (!l.empty()) {
+        std::sort(l.begin(), l.end());
+        auto pct = [&](double p) {
+            const double pos = p * double(l.size() - 1);
+            const size_t lo = size_t(pos);
+            const size_t hi = std::min(lo + 1, l.size() - 1);
+            return l[lo] + (l[hi] - l[lo]) * (pos - double(lo));
+        };
+        out->p50_ms = pct(0.50);
+        out->p99_ms = pct(0.99);
+        out->max_ms = l.back();
+        double sum = 0;
+        for (double v : l) sum += v;
+        out->mean_ms = sum / double(l.size());
+    }
+    if (s->any) {
+        const double wall = gb::ms_between(s->t_first, gb::Clock::now()) * 1e-3;
+        out->wall_s = wall;
+        out->tflops = wall > 0 ? s->useful_flops / wall / 1e12 : 0.0;
+    }
+    out->bytes_in_use = int64_t(s->bytes_held());
+    out->peak_bytes = int64_t(s->peak_bytes);
+    out->budget_bytes = int64_t(s->budget);
+    return GB300_OK;
+}
+
+void gb300_server_reset_stats(gb300_server* srv) {
+    auto* s = reinterpret_cast<gb::Server*>(srv);
+    if (!s) return;
+    std::lock_guard<std::mutex> lock(s->mu);
+    s->latencies.clear();
+    s->submitted = s->completed = s->rejected = s->failed = 0;
+    s->useful_flops = 0;
+    s->any = false;
+    s->peak_bytes = s->bytes_held();
+}
+
+void gb300_server_destroy(gb300_server* srv) {
+    auto* s = reinterpret_cast<gb::Server*>(srv);
+    if (!s) return;
+    {
+        std::lock_guard<std::mutex> lock(s->mu);
+        s->stop = true;
+        s->cv_work.notify_all();
+    }
+    if (s->worker.joinable()) s->worker.join();
+    for (auto& sl : s->slots) {
+        if (sl.stream) cudaStreamSynchronize(sl.stream);
+        sl.ws.release();
+        if (sl.ws.d_status) cudaFree(sl.ws.d_status);
+        if (sl.stream) cudaStreamDestroy(sl.stream);
+    }
+    for (auto& kv : s->reqs) {
+        if (kv.second->done) cudaEventDestroy(kv.second->done);
+        delete kv.second;
+    }
+    delete s;
+}
+
+}  // extern "C"

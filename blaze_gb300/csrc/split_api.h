@@ -10,9 +10,10 @@
 namespace gb {
 
 struct SplitRequest {
-    int method = 0;            // gb300_method (AUTO, SPLIT, BF16X3 or BF16)
+    int method = 0;            // gb300_method (AUTO, NATIVE, SPLIT, BF16X3 or BF16)
     int slices = 0;            // slices per operand; 0 = choose from target_error
     double target_error = 0;   // normwise target; <= 0 means k * 2^-53
+    int max_sms = 0;           // cap on the persistent tensor-core grid (0: every SM)
 };
 
 struct SplitResult {
@@ -26,9 +27,15 @@ struct SplitResult {
 // finished the product).
 bool split_read_info(const void* info_dev, int* slices, double* bound);
 
-// Runs the double-precision product g with one of the tensor-core forms (or, for AUTO, picks
-// between the split form and the native kernel).  Returns a gb300_status.
-int split_gemm(const Gemm& g, const SplitRequest& req, const LaunchCtl& ctl, cudaStream_t s, SplitResult* out,
-               std::string* err);
+struct Workspace;
+
+// Runs the double-precision product g (operands on the device, TMA-aligned) with the requested
+// form on stream `s`, taking scratch from `ws`.  AUTO picks between the split form and the native
+// kernel.  Returns a gb300_status.
+int device_product(const Gemm& g, const SplitRequest& req, const LaunchCtl& ctl, cudaStream_t s, Workspace& ws,
+                   SplitResult* out, std::string* err);
+
+// Device scratch bytes device_product needs for g (an upper bound used for admission control).
+size_t device_product_footprint(const Gemm& g, const SplitRequest& req);
 
 }  // namespace gb

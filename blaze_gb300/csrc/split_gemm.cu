@@ -773,78 +773,118 @@ bool split_read_info(const void* info_dev, int* slices, double* bound) {
 }
 
 // ---- host orchestration ------------------------------------------------------------------------
-// Predicted seconds of the native FP64 kernel and of the split form for a shape (AUTO policy).
-static double predict_native_s(const Gemm& g, double fp64_tflops) {
-    return 2.0 * double(g.m) * double(g.n) * double(g.k) / (fp64_tflops * 1e12);
+namespace {
+
+int native_product(const Gemm& g, const LaunchCtl& ctl, cudaStream_t st, Workspace& ws, SplitResult* out,
+                   std::string* err) {
+    Runtime& r = runtime();
+    const int splits = g.k > 0 ? native_choose_splits(g.m, g.n, g.k, 8, r.num_sms) : 1;
+    double* w = nullptr;
+    if (splits > 1) {
+        w = static_cast<double*>(ws.get(kSlotWork, size_t(splits) * size_t(g.m) * size_t(g.n) * 8, err));
+        if (!w) return GB300_ERR_NO_MEMORY;
+    }
+    cudaError_t e = native_gemm<double>(g, splits, w, ctl, st, err);
+    if (e != cudaSuccess) {
+        if (err && err->empty()) *err = cudaGetErrorString(e);
+        return GB300_ERR_CUDA;
+    }
+    out->method_used = GB300_METHOD_NATIVE;
+    out->slices = 0;
+    out->error_bound = double(g.k) * 0x1p-53;
+    out->info_dev = nullptr;
+    return GB300_OK;
 }
 
-int split_gemm(const Gemm& g, const SplitRequest& req, const LaunchCtl& ctl, cudaStream_t st, SplitResult* out,
-               std::string* err) {
-    Runtime& r = runtime();
-    int mode = kExact;
-    if (req.method == GB300_METHOD_BF16) mode = kBf16;
-    else if (req.method == GB300_METHOD_BF16X3) mode = kBf16x3;
+// The AUTO policy: the split form costs about S(S+1)/2 BF16 products plus operand passes; below a
+// few million multiply-adds, or for very short k, the native kernel's single pass wins.
+bool auto_uses_native(const Gemm& g) {
+    const double work = double(g.m) * double(g.n) * double(g.k);
+    return work < 256.0 * 256.0 * 256.0 || g.k < 64;
+}
 
-    if (req.method == GB300_METHOD_AUTO) {
-        // The split form costs about (S(S+1)/2) BF16 products plus operand passes; below a few
-        // million multiply-adds per output tile the native kernel's single pass wins.
-        const double work = double(g.m) * double(g.n) * double(g.k);
-        if (work < 256.0 * 256.0 * 256.0 || g.k < 64) {
-            int splits = native_choose_splits(g.m, g.n, g.k, 8, r.num_sms);
-            double* ws = nullptr;
-            if (splits > 1) {
-                ws = static_cast<double*>(pool_get(kSlotWork, size_t(splits) * size_t(g.m) * size_t(g.n) * 8, err));
-                if (!ws) return GB300_ERR_NO_MEMORY;
-            }
-            cudaError_t e = native_gemm<double>(g, splits, ws, ctl, st, err);
-            if (e != cudaSuccess) {
-                if (err && err->empty()) *err = cudaGetErrorString(e);
-                return GB300_ERR_CUDA;
-            }
-            out->method_used = GB300_METHOD_NATIVE;
-            out->slices = 0;
-            out->error_bound = double(g.k) * 0x1p-53;
-            (void)predict_native_s;
-            return GB300_OK;
-        }
-    }
+struct SplitGeometry {
+    int mode, m_tiles, n_tiles, nseg, kb_total, max_planes, max_levels;
+    int64_t mpad, npad, kpad, kseg;
+};
 
-    const int64_t m = g.m, n = g.n, k = g.k;
-    const int m_tiles = int((m + TM - 1) / TM), n_tiles = int((n + TN - 1) / TN);
-    const int64_t mpad = int64_t(m_tiles) * TM, npad = int64_t(n_tiles) * TN;
-    const int64_t kpad = round_up(k, TK);
-    const int kb_total = int(kpad / TK);
-    const int max_planes = (mode == kExact) ? (req.slices > 0 ? std::min(req.slices, MAX_SLICES) : MAX_SLICES)
-                                            : (mode == kBf16 ? 1 : 2);
-    const int max_levels = (mode == kExact) ? max_planes : 1;
-
-    // k-segments: exactness (int32 level sums) and parallelism for few output tiles
-    int64_t kseg = kpad;
-    if (mode == kExact) {
+SplitGeometry split_geometry(const Gemm& g, const SplitRequest& req, int num_sms) {
+    SplitGeometry G;
+    G.mode = kExact;
+    if (req.method == GB300_METHOD_BF16) G.mode = kBf16;
+    else if (req.method == GB300_METHOD_BF16X3) G.mode = kBf16x3;
+    G.m_tiles = int((g.m + TM - 1) / TM);
+    G.n_tiles = int((g.n + TN - 1) / TN);
+    G.mpad = int64_t(G.m_tiles) * TM;
+    G.npad = int64_t(G.n_tiles) * TN;
+    G.kpad = round_up(g.k, TK);
+    G.kb_total = int(G.kpad / TK);
+    G.max_planes = (G.mode == kExact) ? (req.slices > 0 ? std::min(req.slices, MAX_SLICES) : MAX_SLICES)
+                                      : (G.mode == kBf16 ? 1 : 2);
+    G.max_levels = (G.mode == kExact) ? G.max_planes : 1;
+    // k-segments: exactness (int32 level sums) and parallelism for few output tiles; decided from the
+    // device's SM count only, so a capped grid computes the same segments (and the same result)
+    int64_t kseg = G.kpad;
+    if (G.mode == kExact) {
         // n_L * (Kseg/256) groups of at most 2^22 each must stay below 2^31
-        const int64_t cap = (int64_t(511) / max_planes) * KSEG_UNIT;
+        const int64_t cap = (int64_t(511) / G.max_planes) * KSEG_UNIT;
         kseg = std::min(kseg, std::max<int64_t>(cap, KSEG_UNIT));
     }
-    const int tiles = m_tiles * n_tiles;
-    if (tiles < r.num_sms) {
-        const int64_t want = (r.num_sms + tiles - 1) / tiles;
-        kseg = std::min(kseg, std::max<int64_t>(KSEG_UNIT, round_up((kpad + want - 1) / want, KSEG_UNIT)));
+    const int tiles = G.m_tiles * G.n_tiles;
+    if (tiles < num_sms) {
+        const int64_t want = (num_sms + tiles - 1) / tiles;
+        kseg = std::min(kseg, std::max<int64_t>(KSEG_UNIT, round_up((G.kpad + want - 1) / want, KSEG_UNIT)));
     }
-    kseg = round_up(kseg, TK);
-    const int nseg = int((kpad + kseg - 1) / kseg);
+    G.kseg = round_up(kseg, TK);
+    G.nseg = int((G.kpad + G.kseg - 1) / G.kseg);
+    return G;
+}
+
+size_t split_scratch_bytes(const Gemm& g, const SplitGeometry& G) {
+    const size_t planes = size_t(G.max_planes) * (size_t(G.mpad) + size_t(G.npad)) * size_t(G.kpad) * 2;
+    const size_t levels = size_t(G.nseg) * G.max_levels * size_t(G.mpad) * size_t(G.npad) * 4;
+    const size_t stats = size_t(g.m + g.n) * (sizeof(int) + sizeof(double) + 32) + 4096;
+    return planes + levels + stats;
+}
+
+}  // namespace
+
+size_t device_product_footprint(const Gemm& g, const SplitRequest& req) {
+    Runtime& r = runtime();
+    if (g.k == 0 || req.method == GB300_METHOD_NATIVE || (req.method == GB300_METHOD_AUTO && auto_uses_native(g))) {
+        const int splits = g.k > 0 ? native_choose_splits(g.m, g.n, g.k, 8, r.num_sms) : 1;
+        return splits > 1 ? size_t(splits) * size_t(g.m) * size_t(g.n) * 8 : 0;
+    }
+    return split_scratch_bytes(g, split_geometry(g, req, r.num_sms));
+}
+
+int device_product(const Gemm& g, const SplitRequest& req, const LaunchCtl& ctl, cudaStream_t st, Workspace& ws,
+                   SplitResult* out, std::string* err) {
+    Runtime& r = runtime();
+    if (g.k == 0 || req.method == GB300_METHOD_NATIVE || (req.method == GB300_METHOD_AUTO && auto_uses_native(g)))
+        return native_product(g, ctl, st, ws, out, err);
+
+    const SplitGeometry G = split_geometry(g, req, r.num_sms);
+    const int mode = G.mode;
+    const int64_t m = g.m, n = g.n, k = g.k;
+    const int m_tiles = G.m_tiles, n_tiles = G.n_tiles;
+    const int64_t mpad = G.mpad, npad = G.npad, kpad = G.kpad;
+    const int kb_total = G.kb_total, max_planes = G.max_planes, max_levels = G.max_levels;
+    const int64_t kseg = G.kseg;
+    const int nseg = G.nseg;
 
     // device buffers
     const size_t planesA = size_t(max_planes) * size_t(mpad) * size_t(kpad);
     const size_t planesB = size_t(max_planes) * size_t(npad) * size_t(kpad);
-    auto* pa = static_cast<__nv_bfloat16*>(pool_get(kSlotSliceA, planesA * 2, err));
-    auto* pb = static_cast<__nv_bfloat16*>(pool_get(kSlotSliceB, planesB * 2, err));
+    auto* pa = static_cast<__nv_bfloat16*>(ws.get(kSlotSliceA, planesA * 2, err));
+    auto* pb = static_cast<__nv_bfloat16*>(ws.get(kSlotSliceB, planesB * 2, err));
     auto* lv = static_cast<int32_t*>(
-        pool_get(kSlotLevels, size_t(nseg) * max_levels * size_t(mpad) * size_t(npad) * 4, err));
+        ws.get(kSlotLevels, size_t(nseg) * max_levels * size_t(mpad) * size_t(npad) * 4, err));
     // statistics block: exponents (int), relative sums of squares (double), SplitInfo
     const int64_t off_sq = round_up((m + n) * int64_t(sizeof(int)), 256);
     const int64_t off_info = round_up(off_sq + (m + n) * int64_t(sizeof(double)), 256);
     const size_t stat_bytes = size_t(off_info) + 256;
-    auto* stats = static_cast<uint8_t*>(pool_get(kSlotScaleA, stat_bytes, err));
+    auto* stats = static_cast<uint8_t*>(ws.get(kSlotScaleA, stat_bytes, err));
     if (!pa || !pb || !lv || !stats) return GB300_ERR_NO_MEMORY;
     int* eA = reinterpret_cast<int*>(stats);
     int* eB = eA + m;
@@ -858,7 +898,7 @@ int split_gemm(const Gemm& g, const SplitRequest& req, const LaunchCtl& ctl, cud
     const double* A = static_cast<const double*>(g.A);
     const double* B = static_cast<const double*>(g.B);
 
-    RowAcc* racc = static_cast<RowAcc*>(pool_get(kSlotScaleB, size_t(m + n) * sizeof(RowAcc), err));
+    RowAcc* racc = static_cast<RowAcc*>(ws.get(kSlotScaleB, size_t(m + n) * sizeof(RowAcc), err));
     if (!racc) return GB300_ERR_NO_MEMORY;
     cudaMemsetAsync(racc, 0, size_t(m + n) * sizeof(RowAcc), st);
     auto stats_launch = [&](const double* X, int64_t R, int64_t sr, int64_t sp, RowAcc* ra, int* ex, double* sq) {
@@ -902,7 +942,7 @@ int split_gemm(const Gemm& g, const SplitRequest& req, const LaunchCtl& ctl, cud
     p.limit_ns = ctl.wait_limit_ns;
     p.inject_stall = ctl.inject_stall;
     const int units = m_tiles * n_tiles * nseg;
-    const int grid = std::min(units, r.num_sms);
+    const int grid = std::min(units, req.max_sms > 0 ? std::min(req.max_sms, r.num_sms) : r.num_sms);
     auto kern = mode == kExact ? tc_gemm_kernel<kExact> : (mode == kBf16 ? tc_gemm_kernel<kBf16> : tc_gemm_kernel<kBf16x3>);
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kTcSmem));
     if (e != cudaSuccess) {

@@ -34,6 +34,7 @@ UNITS = [
     ("peaks.cu", "peaks.o", []),
     ("profile.cpp", "profile.o", []),
     ("grouped.cu", "grouped.o", []),
+    ("serve.cpp", "serve.o", []),
 ]
 
 

@@ -151,6 +151,67 @@ int gb300_grouped_tuning_load(const char* path);
 /* Shape index the planner uses for a product, with its warp-tile rows and columns. */
 int gb300_grouped_shape_for(int elem_bytes, int64_t m, int64_t n, int64_t k, int* rows, int* cols);
 
+/* ---- serving: continuous batching of product requests ---------------------------------------
+ * A server admits requests as stream slots and device memory free up (FIFO with backfill under a
+ * device-memory budget), runs admitted requests concurrently on their own streams and workspaces,
+ * and records per-request latency.  Operands are resident: A, B and C are device (or managed)
+ * memory owned by the caller, 16-byte aligned with even leading dimensions.  Blaze has no server;
+ * each request is the same product as gb300_dgemm_ex with the accuracy class as its method. */
+typedef struct gb300_server_config {
+    int64_t memory_budget_bytes;  /* scratch the server may hold (default 150 GiB, capped by free memory) */
+    int slots;                    /* requests running at once (default 8) */
+    int reserve_sms;              /* SMs kept out of large tensor-core products for small requests (16) */
+    double aging_ms;              /* a queue head older than this stops backfilling (50 ms) */
+    int64_t large_threshold;      /* max(m, n) from which a request counts as large (2048) */
+} gb300_server_config;
+
+typedef struct gb300_serve_request {
+    int order, transA, transB;
+    int64_t m, n, k;
+    double alpha, beta;
+    const double* A;
+    int64_t lda;
+    const double* B;
+    int64_t ldb;
+    double* C;
+    int64_t ldc;
+    int accuracy;          /* gb300_method: NATIVE, SPLIT (<= target_error), BF16X3, BF16, AUTO */
+    double target_error;   /* SPLIT: normwise target; <= 0 means k * 2^-53 */
+} gb300_serve_request;
+
+typedef struct gb300_serve_result {
+    int status;            /* gb300_status of the request */
+    int method_used;
+    int slices;
+    double error_bound;    /* a-priori normwise bound of the form that ran */
+    double queue_ms;       /* submission -> start */
+    double run_ms;         /* start -> completion seen */
+    double latency_ms;     /* submission -> completion seen */
+} gb300_serve_result;
+
+typedef struct gb300_server_stats {
+    int64_t submitted, completed, rejected, failed, queued;
+    double p50_ms, p99_ms, mean_ms, max_ms;   /* latency of completed requests */
+    double wall_s;                            /* since the first submission (or the last reset) */
+    double tflops;                            /* 2*m*n*k of completed requests / wall_s */
+    int64_t bytes_in_use, peak_bytes, budget_bytes;
+} gb300_server_stats;
+
+typedef struct gb300_server gb300_server;
+
+void gb300_server_config_init(gb300_server_config* config);
+int gb300_server_create(const gb300_server_config* config, gb300_server** server);
+/* Queue a request; the ticket identifies it.  GB300_ERR_ADMISSION when it can never fit the budget. */
+int gb300_server_submit(gb300_server* server, const gb300_serve_request* request, uint64_t* ticket);
+/* Wait for a request (timeout_ms < 0: no limit), fill `result` and forget the ticket; returns the
+ * request's status (GB300_ERR_DEVICE_TIMEOUT if the timeout passed first; the ticket stays valid). */
+int gb300_server_wait(gb300_server* server, uint64_t ticket, double timeout_ms, gb300_serve_result* result);
+int gb300_server_poll(gb300_server* server, uint64_t ticket, int* done);
+int gb300_server_get_stats(gb300_server* server, gb300_server_stats* stats);
+void gb300_server_reset_stats(gb300_server* server);
+/* Stop the scheduler after the running requests finished and free the server's memory. */
+void gb300_server_destroy(gb300_server* server);
+
 /* Allocation-free variant of the native FP64 product, for callers that cannot allocate device
  * memory themselves (a host framework that owns all device memory through its own pool or
  * budget, or a latency-critical loop where cudaMalloc/cudaFree and their implicit device
