@@ -50,6 +50,9 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end C-ABI leg")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched small-product leg")
     ap.add_argument("--batch-count", type=int, default=10000)
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving leg")
+    ap.add_argument("--serve-requests", type=int, default=240)
+    ap.add_argument("--serve-rates", default="40,160", help="Poisson arrival rates (requests/s) to sweep")
     return ap.parse_args()
 
 
@@ -317,6 +320,69 @@ def batched_leg(G, torch, args, dev):
     return out
 
 
+def serving_leg(G, torch, args, dev):
+    """Poisson stream of square FP64 requests: 70 % n log-uniform in [8,128], 25 % in [512,2048],
+    5 % in [4096,8192], accuracy class drawn uniformly from {native FP64, split <= k*2^-53, BF16},
+    operands resident; admission by a 150 GiB budget.  Reports p50/p99 latency and TFLOP/s per rate."""
+    import numpy as np
+    import threading
+
+    rs = np.random.RandomState(args.seed + 7)
+    nmax = 8192
+    pool = torch.empty(nmax * nmax, dtype=torch.float64, device=f"cuda:{dev}").uniform_(-1.0, 1.0)
+    poolB = torch.empty(nmax * nmax, dtype=torch.float64, device=f"cuda:{dev}").uniform_(-1.0, 1.0)
+    classes = ["native", "split", "bf16"]
+    out = {"workload": "Poisson stream, square FP64 n: 70% logU[8,128], 25% logU[512,2048], 5% logU[4096,8192]; "
+                       "class uniform over {native, split<=k*2^-53, bf16}; operands resident; budget 150 GiB",
+           "rates": []}
+    srv = G.Server(budget_bytes=150 << 30, slots=8, reserve_sms=16, large_threshold=2048)
+    try:
+        for rate in [float(x) for x in args.serve_rates.split(",") if x]:
+            nreq = args.serve_requests
+            u = rs.random_sample(nreq)
+            n = np.where(u < 0.70, np.exp(rs.uniform(np.log(8), np.log(128), nreq)),
+                         np.where(u < 0.95, np.exp(rs.uniform(np.log(512), np.log(2048), nreq)),
+                                  np.exp(rs.uniform(np.log(4096), np.log(8192), nreq))))
+            n = (np.rint(n).astype(np.int64) + 1) // 2 * 2  # even leading dimensions
+            cls = rs.randint(0, 3, nreq)
+            gaps = rs.exponential(1.0 / rate, nreq)
+            Cs = [torch.empty(int(x) * int(x), dtype=torch.float64, device=f"cuda:{dev}") for x in n]
+            tickets = [None] * nreq
+            srv.reset_stats()
+            t0 = time.perf_counter()
+
+            def producer():
+                t_next = t0
+                for i in range(nreq):
+                    t_next += gaps[i]
+                    d = t_next - time.perf_counter()
+                    if d > 0:
+                        time.sleep(d)
+                    k = int(n[i])
+                    tickets[i] = srv.submit(101, 111, 111, k, k, k, 1.0, pool, k, poolB, k, 0.0, Cs[i], k,
+                                            accuracy=classes[int(cls[i])])
+
+            th = threading.Thread(target=producer)
+            th.start()
+            th.join()
+            lat = {c: [] for c in classes}
+            for i in range(nreq):
+                res = srv.wait(tickets[i])
+                lat[classes[int(cls[i])]].append(res.latency_ms)
+            st = srv.stats()
+            flops = float(np.sum(2.0 * n.astype(np.float64) ** 3))
+            entry = {"rate_per_s": rate, "requests": nreq, "completed": int(st.completed),
+                     "rejected": int(st.rejected), "p50_ms": round(st.p50_ms, 3), "p99_ms": round(st.p99_ms, 3),
+                     "max_ms": round(st.max_ms, 3), "tflops": round(st.tflops, 3), "wall_s": round(st.wall_s, 3),
+                     "useful_tflop": round(flops / 1e12, 3), "peak_gib": round(st.peak_bytes / 2 ** 30, 2),
+                     "p50_by_class_ms": {c: round(float(np.median(v)), 3) for c, v in lat.items() if v}}
+            out["rates"].append(entry)
+            del Cs
+    finally:
+        srv.close()
+    return out
+
+
 def ours(args, dist: Dist):
     import numpy as np
     import torch
@@ -414,6 +480,10 @@ def ours(args, dist: Dist):
         if native:
             batched["fp64"]["frac_of_fp64_peak"] = round(batched["fp64"]["grouped_tflops"] / native["fp64_peak_tflops"], 4)
 
+    serving = None
+    if not args.no_serving:
+        serving = serving_leg(G, torch, args, dev)
+
     peaks, peaks_src = read_peaks()
 
     pairs = info.slices_used * (info.slices_used + 1) // 2
@@ -452,7 +522,7 @@ def ours(args, dist: Dist):
                 "native_fp64": native,
                 "split_vs_native": round(value / dist.world / native["value"], 2) if native else None,
                 "e2e": e2e, "roofline": roofline, "gpu_launches": int(launches), "clocks": clk,
-                "batched": batched}
+                "batched": batched, "serving": serving}
         if not args.no_cpu:
             line["cpu_baseline"] = cpu_baseline(min(n, 4096))
         print(json.dumps(line), flush=True)
