@@ -297,13 +297,6 @@ int gb300_server_submit(gb300_server* srv, const gb300_serve_request* q, uint64_
     g.ldc = q->ldc;
     g.alpha = q->alpha;
     g.beta = q->beta;
-    auto aligned = [](const void* p, int64_t ld) { return reinterpret_cast<uintptr_t>(p) % 16 == 0 && (ld * 8) % 16 == 0; };
-    if (g.k > 0 && (!aligned(g.A, g.lda) || !aligned(g.B, g.ldb))) {
-        delete r;
-        gb::set_error(GB300_ERR_INVALID_ARG, "gb300_server_submit: operands need 16-byte aligned bases and even "
-                                             "leading dimensions");
-        return GB300_ERR_INVALID_ARG;
-    }
     r->sreq.method = q->accuracy;
     r->sreq.target_error = q->target_error;
     r->sreq.slices = 0;

@@ -847,20 +847,65 @@ size_t split_scratch_bytes(const Gemm& g, const SplitGeometry& G) {
     return planes + levels + stats;
 }
 
+// Stored (row-major) shape of the operands of a logical product.
+void stored_a(const Gemm& g, int64_t* rows, int64_t* cols) { *rows = g.ta ? g.k : g.m; *cols = g.ta ? g.m : g.k; }
+void stored_b(const Gemm& g, int64_t* rows, int64_t* cols) { *rows = g.tb ? g.n : g.k; *cols = g.tb ? g.k : g.n; }
+bool tma_ready(const void* p, int64_t ld) { return reinterpret_cast<uintptr_t>(p) % 16 == 0 && (ld * 8) % 16 == 0; }
+
+size_t realign_bytes(const Gemm& g) {
+    if (g.k == 0) return 0;
+    size_t b = 0;
+    int64_t r, c;
+    if (!tma_ready(g.A, g.lda)) { stored_a(g, &r, &c); b += size_t(r) * size_t((c + 1) / 2 * 2) * 8; }
+    if (!tma_ready(g.B, g.ldb)) { stored_b(g, &r, &c); b += size_t(r) * size_t((c + 1) / 2 * 2) * 8; }
+    return b;
+}
+
+// Copy operands whose base or pitch TMA cannot address (16-byte alignment) into the workspace.
+int realign_operands(Gemm& g, Workspace& ws, cudaStream_t st, std::string* err) {
+    if (g.k == 0) return GB300_OK;
+    for (int which = 0; which < 2; ++which) {
+        const void*& p = which == 0 ? g.A : g.B;
+        int64_t& ld = which == 0 ? g.lda : g.ldb;
+        if (tma_ready(p, ld)) continue;
+        int64_t rows, cols;
+        if (which == 0) stored_a(g, &rows, &cols);
+        else stored_b(g, &rows, &cols);
+        const int64_t ldp = (cols + 1) / 2 * 2;
+        void* d = ws.get(which == 0 ? kSlotA : kSlotB, size_t(rows) * size_t(ldp) * 8, err);
+        if (!d) return GB300_ERR_NO_MEMORY;
+        const cudaError_t e = cudaMemcpy2DAsync(d, size_t(ldp) * 8, p, size_t(ld) * 8, size_t(cols) * 8, size_t(rows),
+                                                cudaMemcpyDeviceToDevice, st);
+        if (e != cudaSuccess) {
+            if (err) *err = std::string("operand realignment: ") + cudaGetErrorString(e);
+            return GB300_ERR_CUDA;
+        }
+        p = d;
+        ld = ldp;
+    }
+    return GB300_OK;
+}
+
 }  // namespace
 
 size_t device_product_footprint(const Gemm& g, const SplitRequest& req) {
     Runtime& r = runtime();
+    const size_t extra = realign_bytes(g);
     if (g.k == 0 || req.method == GB300_METHOD_NATIVE || (req.method == GB300_METHOD_AUTO && auto_uses_native(g))) {
         const int splits = g.k > 0 ? native_choose_splits(g.m, g.n, g.k, 8, r.num_sms) : 1;
-        return splits > 1 ? size_t(splits) * size_t(g.m) * size_t(g.n) * 8 : 0;
+        return extra + (splits > 1 ? size_t(splits) * size_t(g.m) * size_t(g.n) * 8 : 0);
     }
-    return split_scratch_bytes(g, split_geometry(g, req, r.num_sms));
+    return extra + split_scratch_bytes(g, split_geometry(g, req, r.num_sms));
 }
 
-int device_product(const Gemm& g, const SplitRequest& req, const LaunchCtl& ctl, cudaStream_t st, Workspace& ws,
+int device_product(const Gemm& g_in, const SplitRequest& req, const LaunchCtl& ctl, cudaStream_t st, Workspace& ws,
                    SplitResult* out, std::string* err) {
     Runtime& r = runtime();
+    Gemm g = g_in;
+    {
+        const int rst = realign_operands(g, ws, st, err);
+        if (rst != GB300_OK) return rst;
+    }
     if (g.k == 0 || req.method == GB300_METHOD_NATIVE || (req.method == GB300_METHOD_AUTO && auto_uses_native(g)))
         return native_product(g, ctl, st, ws, out, err);
 

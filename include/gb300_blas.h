@@ -155,7 +155,8 @@ int gb300_grouped_shape_for(int elem_bytes, int64_t m, int64_t n, int64_t k, int
  * A server admits requests as stream slots and device memory free up (FIFO with backfill under a
  * device-memory budget), runs admitted requests concurrently on their own streams and workspaces,
  * and records per-request latency.  Operands are resident: A, B and C are device (or managed)
- * memory owned by the caller, 16-byte aligned with even leading dimensions.  Blaze has no server;
+ * memory owned by the caller (operands that TMA cannot address in place — odd leading dimension or
+ * a base not 16-byte aligned — are realigned into the request's workspace).  Blaze has no server;
  * each request is the same product as gb300_dgemm_ex with the accuracy class as its method. */
 typedef struct gb300_server_config {
     int64_t memory_budget_bytes;  /* scratch the server may hold (default 150 GiB, capped by free memory) */
