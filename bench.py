@@ -51,6 +51,11 @@ def parse():
     ap.add_argument("--no-batched", action="store_true", help="skip the batched small-product leg")
     ap.add_argument("--batch-count", type=int, default=10000)
     ap.add_argument("--no-serving", action="store_true", help="skip the serving leg")
+    ap.add_argument("--sweep", default="", help="comma list of sweep groups to run instead of the main line: "
+                                                 "square (4096/8192/16384, rr/rc, uniform/spread, native/split S=3..8/"
+                                                 "bf16x3), rect ((M,K,N) = (65536,256,256), (256,65536,256), "
+                                                 "(4096,4096,64), column-major A)")
+    ap.add_argument("--sweep-sizes", default="4096,8192,16384")
     ap.add_argument("--serve-requests", type=int, default=240)
     ap.add_argument("--serve-rates", default="40,160", help="Poisson arrival rates (requests/s) to sweep")
     return ap.parse_args()
@@ -149,6 +154,16 @@ def uniform(n: int, seed: int, lo: float = -1.0, hi: float = 1.0):
     return lo + (hi - lo) * np.random.RandomState(seed).random_sample(n)
 
 
+def spread_values(n: int, seed: int, emin: int = -20, emax: int = 20):
+    """u * 2^e with u uniform in [1,2), a uniform sign and e a uniform integer in [emin, emax]."""
+    import numpy as np
+    rs = np.random.RandomState(seed)
+    u = 1.0 + rs.random_sample(n)
+    e = rs.randint(emin, emax + 1, n)
+    sign = np.where(rs.randint(0, 2, n) == 1, -1.0, 1.0)
+    return sign * np.ldexp(u, e)
+
+
 def batch_sizes(count: int, seed: int, lo: int = 4, hi: int = 256):
     import numpy as np
     u = uniform(3 * count, seed, np.log(lo), np.log(hi))
@@ -189,10 +204,14 @@ def cpu_baseline(size: int, seconds_target: float = 12.0):
                       f"restatement of Blaze's blocked mmm kernel, {threads} OpenMP threads, {total:.1f} s"}
 
 
-def cpu_check_rows(hA, hB, n: int, rows):
-    """Compensated (Dot2) FP64 reference rows of A*B from the oracle: the checker of the GPU results."""
+def cpu_check_rows(hA, hB, n: int, rows, order=101, ta=111, tb=111, m=None, k=None, lda=None, ldb=None):
+    """Compensated (Dot2) FP64 reference rows of op(A)*op(B) from the oracle: the checker of the GPU
+    results (square row-major by default)."""
     import oracle as O
-    return O.product_rows_dot2(O.ROW_MAJOR, O.NO_TRANS, O.NO_TRANS, n, n, n, hA, n, hB, n, rows=rows)
+    m = n if m is None else m
+    k = n if k is None else k
+    return O.product_rows_dot2(order, ta, tb, m, n, k, hA, lda or n, hB, ldb or n, rows=rows)
+
 
 
 def reference_arm(args, dist: Dist):
@@ -528,8 +547,93 @@ def ours(args, dist: Dist):
         print(json.dumps(line), flush=True)
 
 
+def sweep(args):
+    """Accuracy / throughput grid of the product forms (one JSON line per measurement)."""
+    import numpy as np
+    import torch
+
+    import blaze_gb300 as G
+
+    G.device_info()
+    s = torch.cuda.Stream()
+
+    def timed(fn, reps):
+        fn()
+        s.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        for _ in range(reps):
+            fn()
+        e1.record(s)
+        s.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    groups = [g for g in args.sweep.split(",") if g]
+    if "square" in groups:
+        for n in [int(x) for x in args.sweep_sizes.split(",") if x]:
+            for dist in ("uniform", "spread"):
+                hA = uniform(n * n, args.seed) if dist == "uniform" else spread_values(n * n, args.seed)
+                hB = uniform(n * n, args.seed + 1) if dist == "uniform" else spread_values(n * n, args.seed + 1)
+                nA, nB = float(np.linalg.norm(hA)), float(np.linalg.norm(hB))
+                dA = torch.from_numpy(hA).cuda()
+                dB = torch.from_numpy(hB).cuda()
+                dC = torch.empty(n * n, dtype=torch.float64, device="cuda")
+                rows = np.arange(0, n, max(1, n // (32 if n <= 8192 else 16)))
+                for layout, tb in (("rr", 111), ("rc", 112)):
+                    # rc: B stored n x n with k contiguous (Blaze DMatTDMatMultExpr)
+                    P = cpu_check_rows(hA, hB, n, rows, tb=tb)
+                    forms = [("native", 0)] if n <= 8192 or layout == "rr" else []
+                    forms += [("split", 0)] + [("split", S) for S in range(3, 9)] + [("bf16x3", 0)]
+                    for method, S in forms:
+                        o = G.opts(method=method, slices=S, residency=G.PTR_DEVICE, stream=s.cuda_stream,
+                                   synchronous=False)
+                        run = lambda: G.dgemm_ex(101, 111, tb, n, n, n, 1.0, dA, n, dB, n, 0.0, dC, n, o)  # noqa: E731
+                        reps = 1 if method == "native" else (3 if n >= 16384 else 5)
+                        ms = timed(run, reps)
+                        info = G.dgemm_ex(101, 111, tb, n, n, n, 1.0, dA, n, dB, n, 0.0, dC, n,
+                                          G.opts(method=method, slices=S, residency=G.PTR_DEVICE))
+                        C = dC.cpu().numpy().reshape(n, n)
+                        err = float(np.linalg.norm(C[rows] - P) * np.sqrt(n / len(rows)) / (nA * nB))
+                        print(json.dumps({"sweep": "square", "n": n, "layout": layout, "dist": dist, "method": method,
+                                          "slices": info.slices_used, "ms": round(ms, 3),
+                                          "tflops": round(2.0 * n ** 3 / (ms * 1e-3) / 1e12, 3),
+                                          "normwise_error": err, "bound": info.error_bound,
+                                          "target": n * 2.0 ** -53}), flush=True)
+                del dA, dB, dC
+    if "rect" in groups:
+        for (m, k, n) in ((65536, 256, 256), (256, 65536, 256), (4096, 4096, 64)):
+            # column-major A (m x k, ld = m), column-major B and C: Blaze TDMatTDMatMultExpr
+            hA = uniform(m * k, args.seed + 2)
+            hB = uniform(k * n, args.seed + 3)
+            dA = torch.from_numpy(hA).cuda()
+            dB = torch.from_numpy(hB).cuda()
+            dC = torch.empty(m * n, dtype=torch.float64, device="cuda")
+            rows = np.arange(0, m, max(1, m // 64))
+            P = cpu_check_rows(hA, hB, n, rows, order=102, m=m, k=k, lda=m, ldb=k)
+            nA, nB = float(np.linalg.norm(hA)), float(np.linalg.norm(hB))
+            for method in ("native", "split", "bf16x3"):
+                o = G.opts(method=method, residency=G.PTR_DEVICE, stream=s.cuda_stream, synchronous=False)
+                run = lambda: G.dgemm_ex(102, 111, 111, m, n, k, 1.0, dA, m, dB, k, 0.0, dC, m, o)  # noqa: E731
+                ms = timed(run, 3)
+                info = G.dgemm_ex(102, 111, 111, m, n, k, 1.0, dA, m, dB, k, 0.0, dC, m,
+                                  G.opts(method=method, residency=G.PTR_DEVICE))
+                C = dC.cpu().numpy().reshape(n, m).T  # column-major m x n
+                err = float(np.linalg.norm(C[rows] - P) * np.sqrt(m / len(rows)) / (nA * nB))
+                bytes_ = 8.0 * (m * k + k * n + m * n)
+                print(json.dumps({"sweep": "rect", "m": m, "k": k, "n": n, "method": method,
+                                  "slices": info.slices_used, "ms": round(ms, 3),
+                                  "tflops": round(2.0 * m * n * k / (ms * 1e-3) / 1e12, 3),
+                                  "operand_gbs": round(bytes_ / (ms * 1e-3) / 1e9, 1),
+                                  "normwise_error": err, "bound": info.error_bound}), flush=True)
+            del dA, dB, dC
+
+
 def main():
     args = parse()
+    if args.sweep:
+        sweep(args)
+        return
     dist = Dist(args.gpus)
     try:
         if args.impl == "reference":
