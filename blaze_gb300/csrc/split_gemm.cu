@@ -835,7 +835,10 @@ SplitGeometry split_geometry(const Gemm& g, const SplitRequest& req, int num_sms
         const int64_t want = (num_sms + tiles - 1) / tiles;
         kseg = std::min(kseg, std::max<int64_t>(KSEG_UNIT, round_up((G.kpad + want - 1) / want, KSEG_UNIT)));
     }
-    G.kseg = round_up(kseg, TK);
+    // equal segments: persistent CTAs take units in a fixed stride, so unequal segments would give
+    // some CTAs only the long ones
+    const int64_t nseg = (G.kpad + kseg - 1) / kseg;
+    G.kseg = round_up((G.kpad + nseg - 1) / nseg, TK);
     G.nseg = int((G.kpad + G.kseg - 1) / G.kseg);
     return G;
 }
