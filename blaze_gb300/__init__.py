@@ -21,9 +21,9 @@ NoTrans, Trans, ConjTrans = 111, 112, 113
 # gb300_status
 OK, ERR_INVALID_ARG, ERR_CUDA, ERR_NO_MEMORY, ERR_DEVICE_TIMEOUT, ERR_NOT_SUPPORTED, ERR_NO_DEVICE, ERR_ADMISSION = range(8)
 # gb300_method
-METHOD_AUTO, METHOD_NATIVE, METHOD_SPLIT, METHOD_BF16X3, METHOD_BF16 = range(5)
+METHOD_AUTO, METHOD_NATIVE, METHOD_SPLIT, METHOD_BF16X3, METHOD_BF16, METHOD_SPLIT_CRT = range(6)
 METHODS = {"auto": METHOD_AUTO, "native": METHOD_NATIVE, "split": METHOD_SPLIT, "bf16x3": METHOD_BF16X3,
-           "bf16": METHOD_BF16}
+           "bf16": METHOD_BF16, "split_crt": METHOD_SPLIT_CRT}
 # gb300_residency
 PTR_DETECT, PTR_DEVICE, PTR_HOST = range(3)
 

@@ -34,6 +34,7 @@ int default_method() {
             const std::string s(v);
             if (s == "native") g_default_method = GB300_METHOD_NATIVE;
             else if (s == "split") g_default_method = GB300_METHOD_SPLIT;
+            else if (s == "split_crt") g_default_method = GB300_METHOD_SPLIT_CRT;
             else if (s == "bf16x3") g_default_method = GB300_METHOD_BF16X3;
             else if (s == "bf16") g_default_method = GB300_METHOD_BF16;
         }
@@ -90,6 +91,7 @@ const char* method_name(int m) {
         case GB300_METHOD_SPLIT: return "split";
         case GB300_METHOD_BF16X3: return "bf16x3";
         case GB300_METHOD_BF16: return "bf16";
+        case GB300_METHOD_SPLIT_CRT: return "split_crt";
         default: return "auto";
     }
 }
@@ -123,9 +125,9 @@ int gemm_entry(int order, int transA, int transB, int64_t m, int64_t n, int64_t 
     if (ldc < minldc) return fail(GB300_ERR_INVALID_ARG, "parameter 14 (ldc) is too small");
     int method = opts ? opts->method : GB300_METHOD_AUTO;
     if (method == GB300_METHOD_AUTO && opts == nullptr) method = default_method();
-    if (method < GB300_METHOD_AUTO || method > GB300_METHOD_BF16)
+    if (method < GB300_METHOD_AUTO || method > GB300_METHOD_SPLIT_CRT)
         return fail(GB300_ERR_INVALID_ARG, "unknown method " + std::to_string(method));
-    if (!is_double && method == GB300_METHOD_SPLIT)
+    if (!is_double && (method == GB300_METHOD_SPLIT || method == GB300_METHOD_SPLIT_CRT))
         return fail(GB300_ERR_INVALID_ARG, "the split-precision form is defined for double only");
     clear_error();
     if (opts) {
@@ -310,7 +312,7 @@ int gb300_sgemm_ex(int order, int transA, int transB, int64_t m, int64_t n, int6
 
 int gb300_set_default_method(int method) {
     const int prev = gb::default_method();
-    if (method >= GB300_METHOD_AUTO && method <= GB300_METHOD_BF16) gb::g_default_method = method;
+    if (method >= GB300_METHOD_AUTO && method <= GB300_METHOD_SPLIT_CRT) gb::g_default_method = method;
     return prev;
 }
 

@@ -280,7 +280,7 @@ int gb300_server_submit(gb300_server* srv, const gb300_serve_request* q, uint64_
         q->lda < std::max<int64_t>(1, rm ? (tA ? q->m : q->k) : (tA ? q->k : q->m)) ||
         q->ldb < std::max<int64_t>(1, rm ? (tB ? q->k : q->n) : (tB ? q->n : q->k)) ||
         q->ldc < std::max<int64_t>(1, rm ? q->n : q->m) || q->accuracy < GB300_METHOD_AUTO ||
-        q->accuracy > GB300_METHOD_BF16) {
+        q->accuracy > GB300_METHOD_SPLIT_CRT) {
         gb::set_error(GB300_ERR_INVALID_ARG, "gb300_server_submit: invalid request");
         return GB300_ERR_INVALID_ARG;
     }

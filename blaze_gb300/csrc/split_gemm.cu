@@ -79,15 +79,38 @@ constexpr int KSEG_UNIT = 256;          // k-segments are multiples of this
 constexpr uint32_t MAGIC_BITS = 0x4B400000u;  // bits of 1.5 * 2^23
 constexpr float MAGIC = 12582912.0f;
 
-enum Mode : int { kExact = 0, kBf16 = 1, kBf16x3 = 2 };
+enum Mode : int { kExact = 0, kBf16 = 1, kBf16x3 = 2, kCrt = 3 };
+
+// ---- moduli of the CRT (Ozaki scheme II) form ----------------------------------------------------
+// Pairwise coprime moduli <= 257, largest first: a residue in the symmetric range has |r| <= 128,
+// so it is exactly a BF16 and a 256-product group of residue products stays within 2^22 (the same
+// exactness argument as for the digits).  Prime factors: 257; 2; 3,5,17; 11,23; 251; 13,19; 241;
+// 239; 233; 229; 227; 223; 7,31; 211; 199.  Product of all 15: about 2^118.2.
+constexpr int MAX_MODULI = 15;
+__constant__ uint32_t c_mod[MAX_MODULI] = {257, 256, 255, 253, 251, 247, 241, 239, 233, 229, 227, 223, 217, 211, 199};
+// floor(2^32 / p) for the reduction of 32-bit values, and 2^32 mod p for 64-bit values.
+__constant__ uint32_t c_mod_inv32[MAX_MODULI] = {
+    16711935u, 16777216u, 16843009u, 16976155u, 17111423u, 17388531u, 17821441u, 17970574u,
+    18433336u, 18755315u, 18920560u, 19259943u, 19792476u, 20355295u, 21582750u};
+__constant__ uint32_t c_mod_2p32[MAX_MODULI] = {1u, 0u, 1u, 81u, 123u, 139u, 15u, 110u, 8u, 161u, 176u, 7u, 4u, 51u, 46u};
+// log2 of the running products of the moduli (host-side copy for the worst-case plan).
+constexpr double kModLog2[MAX_MODULI] = {8.00562, 8.0, 7.99435, 7.98299, 7.97154, 7.94837, 7.91289, 7.90087,
+                                         7.86419, 7.83920, 7.82655, 7.80090, 7.76155, 7.72110, 7.63662};
 
 // Device-side result of the pre-pass: the slice count and the bound it guarantees.
 struct SplitInfo {
-    int slices;           // S (exact mode); planes per operand otherwise
+    int slices;           // S (digit mode); residue products N (CRT mode); planes per operand otherwise
     int nonfinite;        // inputs contained Inf/NaN
     double bound;         // a-priori normwise bound of the result
     double normA, normB;  // Frobenius norms
     double scaleA, scaleB;// ||2^e||_2, ||2^f||_2
+    // CRT mode
+    int beta;             // operands are rounded to beta-bit integers per row / column
+    int pad;
+    unsigned long long P[2];             // product of the N moduli (lo, hi)
+    unsigned long long M[MAX_MODULI][2]; // P / p_t
+    unsigned long long Pm[4][2];         // 8P, 4P, 2P, P for the final reduction
+    uint32_t y[MAX_MODULI];              // (P / p_t)^-1 mod p_t
 };
 
 // ---- pre-pass ------------------------------------------------------------------------------
@@ -220,7 +243,7 @@ __device__ int block_max_int(int v, int* red) {
 
 __global__ void split_info_kernel(const int* __restrict__ eA, const double* __restrict__ qA, int64_t m,
                                   const int* __restrict__ eB, const double* __restrict__ qB, int64_t n, int64_t k,
-                                  int mode, int fixed_slices, double target, SplitInfo* info) {
+                                  int mode, int fixed_slices, int cap_planes, double target, SplitInfo* info) {
     __shared__ double redd[32];
     __shared__ int redi[32];
     int bad = 0, EA = -100000, EB = -100000;
@@ -260,7 +283,59 @@ __global__ void split_info_kernel(const int* __restrict__ eA, const double* __re
         r.scaleA = (sa > 0) ? ldexp(sqrt(sa), EA) : 0.0;
         r.scaleB = (sb > 0) ? ldexp(sqrt(sb), EB) : 0.0;
         const double rho = (na > 0 && nb > 0) ? sqrt(sa / na) * sqrt(sb / nb) : 0.0;
-        if (mode == kExact) {
+        if (mode == kCrt) {
+            // operands rounded to beta-bit integers: |dA_ip| <= 2^(e_i-beta-1), so
+            // ||dC||_F/(||A|| ||B||) <= 2^(-beta-1)(rA + rB) + 2^(-2beta-2) rA rB + 2^-52 with
+            // rA = sqrt(k) ||2^e|| / ||A|| (and 2^-52 for the final conversion and the alpha scaling)
+            const double rA = (na > 0) ? sqrt(double(k) * sa / na) : 0.0;
+            const double rB = (nb > 0) ? sqrt(double(k) * sb / nb) : 0.0;
+            auto bnd = [&](int b) {
+                return ldexp(1.0, -b - 1) * (rA + rB) + ldexp(1.0, -2 * b - 2) * rA * rB + ldexp(1.0, -52);
+            };
+            int beta = 1;
+            while (beta < 61 && bnd(beta) > target) ++beta;
+            // moduli: product above 2 * k * 2^(2 beta) with one bit to spare
+            const int kbits = 64 - __clzll((long long)(k > 1 ? k - 1 : 1));
+            double need = 2.0 + kbits + 2.0 * beta, have = 0.0;
+            int N = 0;
+            const int nmax = fixed_slices > 0 ? fixed_slices : cap_planes;
+            while (N < nmax && have < need) {
+                have += log2(double(c_mod[N]));
+                ++N;
+            }
+            if (have < need) beta = int(floor((have - 2.0 - kbits) / 2.0));  // the planned moduli cap beta
+            r.slices = N;
+            r.beta = beta;
+            r.bound = bnd(beta);
+            // CRT constants: P, M_t = P / p_t, y_t = M_t^-1 mod p_t
+            unsigned __int128 P = 1;
+            for (int t = 0; t < N; ++t) P *= c_mod[t];
+            r.P[0] = (unsigned long long)P;
+            r.P[1] = (unsigned long long)(P >> 64);
+            for (int t = 0; t < N; ++t) {
+                unsigned __int128 Mt = 1;
+                uint32_t mres = 1;
+                for (int u = 0; u < N; ++u) {
+                    if (u == t) continue;
+                    Mt *= c_mod[u];
+                    mres = (mres * (c_mod[u] % c_mod[t])) % c_mod[t];
+                }
+                r.M[t][0] = (unsigned long long)Mt;
+                r.M[t][1] = (unsigned long long)(Mt >> 64);
+                // inverse of mres modulo p_t (extended Euclid on small numbers)
+                long long a = mres, b = c_mod[t], x0 = 1, x1 = 0;
+                while (b) {
+                    const long long q = a / b, ta = a - q * b, tx = x0 - q * x1;
+                    a = b; b = ta; x0 = x1; x1 = tx;
+                }
+                r.y[t] = uint32_t(((x0 % (long long)c_mod[t]) + c_mod[t]) % c_mod[t]);
+            }
+            for (int i = 0; i < 4; ++i) {
+                const unsigned __int128 v = P << (3 - i);
+                r.Pm[i][0] = (unsigned long long)v;
+                r.Pm[i][1] = (unsigned long long)(v >> 64);
+            }
+        } else if (mode == kExact) {
             int S = fixed_slices;
             if (S <= 0) {
                 S = MAX_SLICES;
@@ -336,6 +411,27 @@ __device__ __forceinline__ void write_planes(const U_t (&V)[8], const bool (&neg
     }
 }
 
+// |round(a * 2^sh)| for a finite double given by its bits (round half up); the result must fit in
+// 62 bits, which the CRT plan guarantees (beta <= 61 and |a| < 2^e).
+__device__ __forceinline__ unsigned long long int_magnitude(unsigned long long bits, int sh_total) {
+    const int eb = int((bits >> 52) & 0x7ff);
+    const unsigned long long mant = bits & 0xfffffffffffffull;
+    const unsigned long long M = eb ? (mant | (1ull << 52)) : mant;
+    const int sh = (eb ? eb : 1) - 1075 + sh_total;
+    if (M == 0) return 0;
+    if (sh >= 0) return M << sh;
+    if (sh > -64) return (M + (1ull << (-sh - 1))) >> (-sh);
+    return 0;
+}
+
+// x mod p for x < 2^32 and p <= 257 with inv = floor(2^32 / p): the quotient estimate is at most
+// one short, so one conditional subtraction finishes the reduction.
+__device__ __forceinline__ uint32_t mod_small(uint32_t x, uint32_t p, uint32_t inv) {
+    const uint32_t q = uint32_t((uint64_t(x) * inv) >> 32);
+    uint32_t r = x - q * p;
+    return r >= p ? r - p : r;
+}
+
 __global__ void slice_kernel(const double* __restrict__ X, int64_t R, int64_t K, int64_t sr, int64_t sp,
                              const int* __restrict__ rexp, const SplitInfo* __restrict__ info, int mode,
                              __nv_bfloat16* __restrict__ planes, int64_t rpad, int64_t kpad) {
@@ -362,7 +458,33 @@ __global__ void slice_kernel(const double* __restrict__ X, int64_t R, int64_t K,
     if (r >= rpad) return;
     const int64_t pstride = rpad * kpad;
     uint16_t* dst = reinterpret_cast<uint16_t*>(planes) + r * kpad + p0 + pp0;
-    if (mode == kExact) {
+    if (mode == kCrt) {
+        const int N = info->slices, beta = info->beta;
+        const int e = (r < R) ? rexp[r] : 0;
+        const bool bad = (e == kNonFinite);
+        unsigned long long U[8];
+        bool neg[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const unsigned long long bits = bad ? 0ull : tile[rr][pp0 + q];
+            neg[q] = (bits >> 63) != 0;
+            U[q] = int_magnitude(bits, beta - e);
+        }
+        for (int t = 0; t < N; ++t) {
+            const uint32_t pm = c_mod[t], inv = c_mod_inv32[t], two32 = c_mod_2p32[t];
+            __align__(16) uint16_t d[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                const uint32_t hi = uint32_t(U[q] >> 32), lo = uint32_t(U[q]);
+                const uint32_t rh = mod_small(hi, pm, inv), rl = mod_small(lo, pm, inv);
+                uint32_t rr_ = mod_small(rh * two32 + rl, pm, inv);
+                int v = int(rr_);
+                if (2 * v > int(pm)) v -= int(pm);  // symmetric range, |v| <= 128
+                d[q] = digit_bf16(neg[q] ? -v : v);
+            }
+            *reinterpret_cast<uint4*>(dst + t * pstride) = *reinterpret_cast<const uint4*>(d);
+        }
+    } else if (mode == kExact) {
         const int S = info->slices;
         const int e = (r < R) ? rexp[r] : 0;
         const bool bad = (e == kNonFinite);
@@ -394,13 +516,14 @@ __global__ void slice_kernel(const double* __restrict__ X, int64_t R, int64_t K,
 }
 
 // ---- level / pair schedule ---------------------------------------------------------------------
-__device__ __forceinline__ int num_levels(int mode, int S) { return mode == kExact ? S : 1; }
+__device__ __forceinline__ int num_levels(int mode, int S) { return (mode == kExact || mode == kCrt) ? S : 1; }
 __device__ __forceinline__ int pairs_in_level(int mode, int L) {
-    return mode == kExact ? L + 1 : (mode == kBf16 ? 1 : 3);
+    return mode == kExact ? L + 1 : (mode == kBf16x3 ? 3 : 1);
 }
 // (A plane, B plane) of pair `i` of level `L`.
 __device__ __forceinline__ void pair_planes(int mode, int L, int i, int& a, int& b) {
     if (mode == kExact) { a = i; b = L - i; }
+    else if (mode == kCrt) { a = L; b = L; }
     else if (mode == kBf16) { a = 0; b = 0; }
     else { a = (i == 2) ? 1 : 0; b = (i == 1) ? 1 : 0; }
 }
@@ -463,8 +586,11 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
     TcBarriers* bars = reinterpret_cast<TcBarriers*>(smem + STAGES * STAGE_BYTES);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
-    constexpr int mode = MODE;
-    const int S = (mode == kExact) ? p.info->slices : 1;
+    // the epilogue's arithmetic is fixed at compile time (exact integer sums or FP32 tiles); the
+    // digit and residue schedules share the exact instantiation and differ only in the plane pairs
+    constexpr int emode = MODE;
+    const int mode = (MODE == kExact) ? p.mode : MODE;
+    const int S = (mode == kExact || mode == kCrt) ? p.info->slices : 1;
     const int nlev = num_levels(mode, S);
     const int units = p.m_tiles * p.n_tiles * p.nseg;
 
@@ -542,7 +668,7 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
                 for (int L = 0; L < nlev && ok; ++L) {
                     const int np = pairs_in_level(mode, L);
                     const int items = np * kbn;
-                    const int gsize = (mode == kExact) ? GROUP_ITEMS : items;
+                    const int gsize = (mode == kExact || mode == kCrt) ? GROUP_ITEMS : items;
                     for (int g0 = 0; g0 < items && ok; g0 += gsize, ++grp) {
                         const int buf = grp & 1;
                         if (grp >= 2 && !mbar_wait(smem_u32(&bars->acc_empty[buf]), ((grp >> 1) - 1) & 1, p.status,
@@ -598,7 +724,7 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
             for (int L = 0; L < nlev && ok; ++L) {
                 const int np = pairs_in_level(mode, L);
                 const int items = np * kbn;
-                const int gsize = (mode == kExact) ? GROUP_ITEMS : items;
+                const int gsize = (mode == kExact || mode == kCrt) ? GROUP_ITEMS : items;
                 uint32_t acc[128];
 #pragma unroll
                 for (int c = 0; c < 128; ++c) acc[c] = 0u;
@@ -617,7 +743,7 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
                         uint32_t v[16];
                         tmem_ld_32x32b_x16(base + uint32_t(c4 * 16), v);
                         tc_wait_ld();
-                        if (mode == kExact) {
+                        if (emode == kExact) {
 #pragma unroll
                             for (int c = 0; c < 16; ++c)
                                 acc[c4 * 16 + c] += __float_as_uint(__uint_as_float(v[c]) + MAGIC);
@@ -634,7 +760,7 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
                 // level sums -> global level plane (row-major, pitch npad)
                 int32_t* dst = p.levels + ((int64_t(seg) * p.max_levels + L) * p.mpad + row) * p.npad +
                                int64_t(tn) * TN + h * 128;
-                const uint32_t bias = (mode == kExact) ? ngroups * MAGIC_BITS : 0u;
+                const uint32_t bias = (emode == kExact) ? ngroups * MAGIC_BITS : 0u;
 #pragma unroll
                 for (int c = 0; c < 128; c += 4) {
                     int4 w;
@@ -710,7 +836,52 @@ __global__ void combine_kernel(const int32_t* __restrict__ levels, int nseg, int
     for (int64_t i = blockIdx.y; i < m; i += gridDim.y) {
     const int64_t off = i * npad + j0;
     double v[COMBINE_COLS];
-    if (mode == kExact) {
+    if (mode == kCrt) {
+        const int N = info->slices;
+        const int ei = eA[i];
+        unsigned __int128 acc[COMBINE_COLS] = {0, 0, 0, 0};
+        for (int t = 0; t < N; ++t) {
+            const uint32_t pm = c_mod[t], inv = c_mod_inv32[t], y = info->y[t];
+            uint32_t c[COMBINE_COLS] = {0, 0, 0, 0};
+            for (int g = 0; g < nseg; ++g) {
+                const int4 q = *reinterpret_cast<const int4*>(levels + (int64_t(g) * max_levels + t) * plane + off);
+                const int tv[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+                for (int cc = 0; cc < COMBINE_COLS; ++cc) {
+                    // residue of the (signed, |v| < 2^31) segment sum in [0, p)
+                    const uint32_t mag = tv[cc] < 0 ? uint32_t(-(int64_t)tv[cc]) : uint32_t(tv[cc]);
+                    uint32_t rsd = mod_small(mag, pm, inv);
+                    if (tv[cc] < 0 && rsd) rsd = pm - rsd;
+                    c[cc] += rsd;
+                }
+            }
+            const unsigned __int128 Mt = ((unsigned __int128)info->M[t][1] << 64) | info->M[t][0];
+#pragma unroll
+            for (int cc = 0; cc < COMBINE_COLS; ++cc) {
+                const uint32_t u = mod_small(mod_small(c[cc], pm, inv) * y, pm, inv);
+                acc[cc] += Mt * u;
+            }
+        }
+        const unsigned __int128 P = ((unsigned __int128)info->P[1] << 64) | info->P[0];
+#pragma unroll
+        for (int cc = 0; cc < COMBINE_COLS; ++cc) {
+            // acc < N*P < 16P: subtract 8P, 4P, 2P, P where they fit
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const unsigned __int128 m = ((unsigned __int128)info->Pm[q][1] << 64) | info->Pm[q][0];
+                if (acc[cc] >= m) acc[cc] -= m;
+            }
+            const int64_t j = j0 + cc;
+            const int fj = (j < n) ? eB[j] : 0;
+            if (ei == kNonFinite || fj == kNonFinite) {
+                v[cc] = __longlong_as_double(0x7ff8000000000000ll);
+            } else {
+                // symmetric residue: the exact product of the scaled integers
+                const __int128 W = (acc[cc] > P / 2) ? (__int128)acc[cc] - (__int128)P : (__int128)acc[cc];
+                v[cc] = int128_to_double_scaled(W, ei + fj - 2 * info->beta);
+            }
+        }
+    } else if (mode == kExact) {
         const int S = info->slices;
         const int ei = eA[i];
         __int128 W[COMBINE_COLS] = {0, 0, 0, 0};
@@ -803,6 +974,25 @@ bool auto_uses_native(const Gemm& g) {
     return work < 256.0 * 256.0 * 256.0 || g.k < 64;
 }
 
+// Moduli the CRT form needs in the worst case for inner dimension k and a normwise target (<= 0:
+// k*2^-53): with |a_i| < 2^e_i, ||A||_F >= ||2^e||/2, so rA, rB <= 2 sqrt(k).  Returns a count above
+// MAX_MODULI when the target is out of reach (the digit form is used then).
+int crt_worst_case_moduli(int64_t k, double target) {
+    if (target <= 0) target = double(k) * 0x1p-53;
+    const double r = 2.0 * std::sqrt(double(std::max<int64_t>(k, 1)));
+    int beta = 1;
+    while (beta < 61 && (std::ldexp(1.0, -beta - 1) * 2 * r + std::ldexp(1.0, -2 * beta - 2) * r * r + 0x1p-52) > target)
+        ++beta;
+    if (beta >= 61) return MAX_MODULI + 1;
+    int kbits = 0;
+    while ((int64_t(1) << kbits) < std::max<int64_t>(k, 2)) ++kbits;
+    const double need = 2.0 + kbits + 2.0 * beta;
+    double have = 0;
+    int N = 0;
+    while (N < MAX_MODULI && have < need) have += kModLog2[N++];
+    return have < need ? MAX_MODULI + 1 : N;
+}
+
 struct SplitGeometry {
     int mode, m_tiles, n_tiles, nseg, kb_total, max_planes, max_levels;
     int64_t mpad, npad, kpad, kseg;
@@ -813,21 +1003,30 @@ SplitGeometry split_geometry(const Gemm& g, const SplitRequest& req, int num_sms
     G.mode = kExact;
     if (req.method == GB300_METHOD_BF16) G.mode = kBf16;
     else if (req.method == GB300_METHOD_BF16X3) G.mode = kBf16x3;
+    else if (req.method == GB300_METHOD_SPLIT_CRT) G.mode = kCrt;
+    else if ((req.method == GB300_METHOD_SPLIT || req.method == GB300_METHOD_AUTO) && req.slices <= 0 &&
+             crt_worst_case_moduli(g.k, req.target_error) <= MAX_MODULI)
+        G.mode = kCrt;
     G.m_tiles = int((g.m + TM - 1) / TM);
     G.n_tiles = int((g.n + TN - 1) / TN);
     G.mpad = int64_t(G.m_tiles) * TM;
     G.npad = int64_t(G.n_tiles) * TN;
     G.kpad = round_up(g.k, TK);
     G.kb_total = int(G.kpad / TK);
-    G.max_planes = (G.mode == kExact) ? (req.slices > 0 ? std::min(req.slices, MAX_SLICES) : MAX_SLICES)
-                                      : (G.mode == kBf16 ? 1 : 2);
-    G.max_levels = (G.mode == kExact) ? G.max_planes : 1;
+    if (G.mode == kCrt)
+        G.max_planes = req.slices > 0 ? std::min(req.slices, MAX_MODULI)
+                                      : std::min(MAX_MODULI, crt_worst_case_moduli(g.k, req.target_error));
+    else
+        G.max_planes = (G.mode == kExact) ? (req.slices > 0 ? std::min(req.slices, MAX_SLICES) : MAX_SLICES)
+                                          : (G.mode == kBf16 ? 1 : 2);
+    G.max_levels = (G.mode == kExact || G.mode == kCrt) ? G.max_planes : 1;
     // k-segments: exactness (int32 level sums) and parallelism for few output tiles; decided from the
     // device's SM count only, so a capped grid computes the same segments (and the same result)
     int64_t kseg = G.kpad;
-    if (G.mode == kExact) {
-        // n_L * (Kseg/256) groups of at most 2^22 each must stay below 2^31
-        const int64_t cap = (int64_t(511) / G.max_planes) * KSEG_UNIT;
+    if (G.mode == kExact || G.mode == kCrt) {
+        // n_L * (Kseg/256) groups of at most 2^22 each must stay below 2^31 (one pair per level in
+        // CRT mode)
+        const int64_t cap = (int64_t(511) / (G.mode == kCrt ? 1 : G.max_planes)) * KSEG_UNIT;
         kseg = std::min(kseg, std::max<int64_t>(cap, KSEG_UNIT));
     }
     const int tiles = G.m_tiles * G.n_tiles;
@@ -846,7 +1045,7 @@ SplitGeometry split_geometry(const Gemm& g, const SplitRequest& req, int num_sms
 size_t split_scratch_bytes(const Gemm& g, const SplitGeometry& G) {
     const size_t planes = size_t(G.max_planes) * (size_t(G.mpad) + size_t(G.npad)) * size_t(G.kpad) * 2;
     const size_t levels = size_t(G.nseg) * G.max_levels * size_t(G.mpad) * size_t(G.npad) * 4;
-    const size_t stats = size_t(g.m + g.n) * (sizeof(int) + sizeof(double) + 32) + 4096;
+    const size_t stats = size_t(g.m + g.n) * (sizeof(int) + sizeof(double) + 32) + 4096 + sizeof(SplitInfo);
     return planes + levels + stats;
 }
 
@@ -931,7 +1130,7 @@ int device_product(const Gemm& g_in, const SplitRequest& req, const LaunchCtl& c
     // statistics block: exponents (int), relative sums of squares (double), SplitInfo
     const int64_t off_sq = round_up((m + n) * int64_t(sizeof(int)), 256);
     const int64_t off_info = round_up(off_sq + (m + n) * int64_t(sizeof(double)), 256);
-    const size_t stat_bytes = size_t(off_info) + 256;
+    const size_t stat_bytes = size_t(off_info) + ((sizeof(SplitInfo) + 255) / 256) * 256;
     auto* stats = static_cast<uint8_t*>(ws.get(kSlotScaleA, stat_bytes, err));
     if (!pa || !pb || !lv || !stats) return GB300_ERR_NO_MEMORY;
     int* eA = reinterpret_cast<int*>(stats);
@@ -957,8 +1156,8 @@ int device_product(const Gemm& g_in, const SplitRequest& req, const LaunchCtl& c
     stats_launch(A, m, a_sr, a_sp, racc, eA, sqA);
     stats_launch(B, n, b_sr, b_sp, racc + m, eB, sqB);
     const double target = req.target_error > 0 ? req.target_error : double(k) * 0x1p-53;
-    split_info_kernel<<<1, 1024, 0, st>>>(eA, sqA, m, eB, sqB, n, k, mode, req.slices > 0 ? max_planes : 0, target,
-                                          info);
+    split_info_kernel<<<1, 1024, 0, st>>>(eA, sqA, m, eB, sqB, n, k, mode, req.slices > 0 ? max_planes : 0,
+                                          max_planes, target, info);
     {
         dim3 grid(unsigned(kpad / 64), unsigned(mpad / 32));
         slice_kernel<<<grid, 256, 0, st>>>(A, m, k, a_sr, a_sp, eA, info, mode, pa, mpad, kpad);
@@ -991,7 +1190,8 @@ int device_product(const Gemm& g_in, const SplitRequest& req, const LaunchCtl& c
     p.inject_stall = ctl.inject_stall;
     const int units = m_tiles * n_tiles * nseg;
     const int grid = std::min(units, req.max_sms > 0 ? std::min(req.max_sms, r.num_sms) : r.num_sms);
-    auto kern = mode == kExact ? tc_gemm_kernel<kExact> : (mode == kBf16 ? tc_gemm_kernel<kBf16> : tc_gemm_kernel<kBf16x3>);
+    auto kern = (mode == kExact || mode == kCrt) ? tc_gemm_kernel<kExact>
+                                                 : (mode == kBf16 ? tc_gemm_kernel<kBf16> : tc_gemm_kernel<kBf16x3>);
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kTcSmem));
     if (e != cudaSuccess) {
         if (err) *err = std::string("tc_gemm_kernel smem attribute: ") + cudaGetErrorString(e);
@@ -1013,7 +1213,10 @@ int device_product(const Gemm& g_in, const SplitRequest& req, const LaunchCtl& c
         if (err) *err = std::string("split-precision launch: ") + cudaGetErrorString(e);
         return GB300_ERR_CUDA;
     }
-    out->method_used = req.method == GB300_METHOD_AUTO ? GB300_METHOD_SPLIT : req.method;
+    out->method_used = mode == kCrt ? GB300_METHOD_SPLIT_CRT
+                                    : (req.method == GB300_METHOD_AUTO || req.method == GB300_METHOD_SPLIT_CRT)
+                                          ? GB300_METHOD_SPLIT
+                                          : req.method;
     out->slices = -1;  // filled in by the caller from the device info when synchronous
     out->error_bound = -1.0;
     out->info_dev = info;

@@ -36,7 +36,11 @@ enum gb300_method {
     GB300_METHOD_NATIVE = 1,  /* native FP64 DFMA (FP32 FFMA for sgemm) */
     GB300_METHOD_SPLIT = 2,   /* Ozaki-style BF16 slices on tcgen05, FP64 recombination (double only) */
     GB300_METHOD_BF16X3 = 3,  /* three BF16 products (hi*hi + hi*lo + lo*hi), FP32 accumulation */
-    GB300_METHOD_BF16 = 4     /* one BF16 product, FP32 accumulation */
+    GB300_METHOD_BF16 = 4,    /* one BF16 product, FP32 accumulation */
+    GB300_METHOD_SPLIT_CRT = 5 /* FP64-accurate, residue (CRT) scheme: operands rounded to beta-bit
+                                  integers per row / column, one BF16 product per modulus, exact
+                                  reconstruction; GB300_METHOD_SPLIT uses it whenever its worst-case
+                                  plan fits 15 moduli and no slice count is requested */
 };
 
 /* Where the operand pointers live. */
@@ -48,14 +52,15 @@ enum gb300_residency {
 
 typedef struct gb300_gemm_opts {
     int method;            /* gb300_method */
-    int slices;            /* GB300_METHOD_SPLIT: slices per operand (0 = choose from target) */
+    int slices;            /* GB300_METHOD_SPLIT: digit slices per operand (0 = choose from target;
+                              a positive count selects the digit scheme); SPLIT_CRT: moduli cap */
     double target_error;   /* GB300_METHOD_SPLIT: normwise bound to reach; <= 0 means k * 2^-53 */
     int residency;         /* gb300_residency */
     void* stream;          /* cudaStream_t to run on; NULL = the library's stream */
     int synchronous;       /* non-zero: return after the result is in C */
     /* outputs */
     int method_used;       /* the form that ran */
-    int slices_used;       /* GB300_METHOD_SPLIT: slices per operand */
+    int slices_used;       /* split forms: digit slices per operand, or moduli (CRT scheme) */
     double error_bound;    /* a-priori normwise bound ||C-AB||_F/(||A||_F||B||_F) of the form
                               that ran (split: computed from the operands' exponents; other forms:
                               the textbook bound of their arithmetic) */

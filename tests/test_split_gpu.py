@@ -49,8 +49,8 @@ LAYOUTS = [(o, a, b) for o in (O.ROW_MAJOR, O.COL_MAJOR) for a in (O.NO_TRANS, O
 def test_split_meets_fp64_bound(order, ta, tb, dist):
     m, n, k = 300, 517, 777
     err, o, _, _ = product(order, ta, tb, m, n, k, dist=dist, pad=3, alpha=1.25, beta=-0.5)
-    assert o.method_used == G.METHOD_SPLIT
-    assert 2 <= o.slices_used <= 10
+    assert o.method_used in (G.METHOD_SPLIT, G.METHOD_SPLIT_CRT)
+    assert 2 <= o.slices_used <= 15
     assert o.error_bound <= k * FP64_BOUND
     assert err <= o.error_bound, (err, o.error_bound)
     assert err <= k * FP64_BOUND
@@ -130,7 +130,7 @@ def test_nonfinite_inputs_poison_their_rows_and_columns():
 def test_auto_picks_a_fp64_accurate_form():
     m = n = k = 512
     err, o, _, _ = product(O.ROW_MAJOR, O.NO_TRANS, O.NO_TRANS, m, n, k, method="auto", seed=17)
-    assert o.method_used in (G.METHOD_SPLIT, G.METHOD_NATIVE)
+    assert o.method_used in (G.METHOD_SPLIT, G.METHOD_SPLIT_CRT, G.METHOD_NATIVE)
     assert err <= k * FP64_BOUND
 
 
@@ -143,3 +143,37 @@ def test_split_stall_reports_timeout_and_recovers():
     assert ei.value.status == G.ERR_DEVICE_TIMEOUT
     G.dgemm_ex(O.ROW_MAJOR, O.NO_TRANS, O.NO_TRANS, m, n, k, 1.0, A, k, B, n, 0.0, C, n, G.opts(method="split"))
     assert np.allclose(C.reshape(m, n), A.reshape(m, k) @ B.reshape(k, n), rtol=1e-12, atol=1e-12)
+
+
+@pytest.mark.parametrize("order,ta,tb", LAYOUTS[::2])
+@pytest.mark.parametrize("dist", ["uniform", "spread"])
+@pytest.mark.parametrize("scheme", ["split_crt", "digits"])
+def test_both_fp64_accurate_schemes(order, ta, tb, dist, scheme):
+    """The residue (CRT) scheme and the digit scheme both meet the FP64 bound on every layout."""
+    m, n, k = 260, 300, 1111
+    if scheme == "digits":
+        # a slice count selects the digit scheme; 7 slices reach the bound for both distributions
+        err, o, _, _ = product(order, ta, tb, m, n, k, dist=dist, seed=21, method="split", slices=7)
+        assert o.method_used == G.METHOD_SPLIT and o.slices_used == 7
+    else:
+        err, o, _, _ = product(order, ta, tb, m, n, k, dist=dist, seed=21, method="split_crt")
+        assert o.method_used == G.METHOD_SPLIT_CRT and 2 <= o.slices_used <= 15
+    assert err <= o.error_bound <= k * FP64_BOUND, (scheme, err, o.error_bound)
+
+
+def test_crt_scheme_is_the_default_split_for_large_k_and_exact_on_integers():
+    m, n, k = 256, 256, 20000
+    A = O.integers(m * k, 31, -1000, 1000)
+    B = O.integers(k * n, 32, -1000, 1000)
+    C = np.zeros(m * n)
+    o = G.dgemm_ex(O.ROW_MAJOR, O.NO_TRANS, O.NO_TRANS, m, n, k, 1.0, A, k, B, n, 0.0, C, n, G.opts(method="split"))
+    assert o.method_used == G.METHOD_SPLIT_CRT
+    exact = A.astype(np.int64).reshape(m, k) @ B.astype(np.int64).reshape(k, n)
+    assert np.array_equal(C.reshape(m, n), exact.astype(np.float64))
+
+
+def test_crt_with_a_moduli_cap_reports_its_weaker_bound():
+    m, n, k = 200, 200, 800
+    err, o, _, _ = product(O.ROW_MAJOR, O.NO_TRANS, O.NO_TRANS, m, n, k, method="split_crt", slices=8, seed=41)
+    assert o.slices_used == 8
+    assert err <= o.error_bound
