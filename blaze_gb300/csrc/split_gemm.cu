@@ -1156,8 +1156,12 @@ int device_product(const Gemm& g_in, const SplitRequest& req, const LaunchCtl& c
     stats_launch(A, m, a_sr, a_sp, racc, eA, sqA);
     stats_launch(B, n, b_sr, b_sp, racc + m, eB, sqB);
     const double target = req.target_error > 0 ? req.target_error : double(k) * 0x1p-53;
-    split_info_kernel<<<1, 1024, 0, st>>>(eA, sqA, m, eB, sqB, n, k, mode, req.slices > 0 ? max_planes : 0,
-                                          max_planes, target, info);
+    split_info_kernel<<<1, 256, 0, st>>>(eA, sqA, m, eB, sqB, n, k, mode, req.slices > 0 ? max_planes : 0,
+                                         max_planes, target, info);
+    if (cudaError_t le = cudaGetLastError(); le != cudaSuccess) {
+        if (err) *err = std::string("split pre-pass launch: ") + cudaGetErrorString(le);
+        return GB300_ERR_CUDA;
+    }
     {
         dim3 grid(unsigned(kpad / 64), unsigned(mpad / 32));
         slice_kernel<<<grid, 256, 0, st>>>(A, m, k, a_sr, a_sp, eA, info, mode, pa, mpad, kpad);
@@ -1165,6 +1169,10 @@ int device_product(const Gemm& g_in, const SplitRequest& req, const LaunchCtl& c
         slice_kernel<<<gridb, 256, 0, st>>>(B, n, k, b_sr, b_sp, eB, info, mode, pb, npad, kpad);
     }
     count_launches(7);
+    if (cudaError_t le = cudaGetLastError(); le != cudaSuccess) {
+        if (err) *err = std::string("split slicing launch: ") + cudaGetErrorString(le);
+        return GB300_ERR_CUDA;
+    }
 
     CUtensorMap tA, tB;
     if (!encode_tmap_2d(&tA, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, pa, uint64_t(max_planes) * mpad, kpad, kpad, TM, TK,
