@@ -93,6 +93,7 @@ __constant__ uint32_t c_mod_inv32[MAX_MODULI] = {
     16711935u, 16777216u, 16843009u, 16976155u, 17111423u, 17388531u, 17821441u, 17970574u,
     18433336u, 18755315u, 18920560u, 19259943u, 19792476u, 20355295u, 21582750u};
 __constant__ uint32_t c_mod_2p32[MAX_MODULI] = {1u, 0u, 1u, 81u, 123u, 139u, 15u, 110u, 8u, 161u, 176u, 7u, 4u, 51u, 46u};
+__constant__ uint32_t c_mod_2p24[MAX_MODULI] = {256u, 0u, 1u, 27u, 125u, 235u, 1u, 133u, 51u, 218u, 100u, 34u, 78u, 184u, 123u};
 // log2 of the running products of the moduli (host-side copy for the worst-case plan).
 constexpr double kModLog2[MAX_MODULI] = {8.00562, 8.0, 7.99435, 7.98299, 7.97154, 7.94837, 7.91289, 7.90087,
                                          7.86419, 7.83920, 7.82655, 7.80090, 7.76155, 7.72110, 7.63662};
@@ -292,8 +293,9 @@ __global__ void split_info_kernel(const int* __restrict__ eA, const double* __re
             auto bnd = [&](int b) {
                 return ldexp(1.0, -b - 1) * (rA + rB) + ldexp(1.0, -2 * b - 2) * rA * rB + ldexp(1.0, -52);
             };
+            // beta <= 55 keeps |A'| < 2^56, the range of the residue extraction
             int beta = 1;
-            while (beta < 61 && bnd(beta) > target) ++beta;
+            while (beta < 55 && bnd(beta) > target) ++beta;
             // moduli: product above 2 * k * 2^(2 beta) with one bit to spare
             const int kbits = 64 - __clzll((long long)(k > 1 ? k - 1 : 1));
             double need = 2.0 + kbits + 2.0 * beta, have = 0.0;
@@ -412,7 +414,7 @@ __device__ __forceinline__ void write_planes(const U_t (&V)[8], const bool (&neg
 }
 
 // |round(a * 2^sh)| for a finite double given by its bits (round half up); the result must fit in
-// 62 bits, which the CRT plan guarantees (beta <= 61 and |a| < 2^e).
+// 56 bits, which the CRT plan guarantees (beta <= 55 and |a| < 2^e).
 __device__ __forceinline__ unsigned long long int_magnitude(unsigned long long bits, int sh_total) {
     const int eb = int((bits >> 52) & 0x7ff);
     const unsigned long long mant = bits & 0xfffffffffffffull;
@@ -470,14 +472,21 @@ __global__ void slice_kernel(const double* __restrict__ X, int64_t R, int64_t K,
             neg[q] = (bits >> 63) != 0;
             U[q] = int_magnitude(bits, beta - e);
         }
+        // U < 2^56 (beta <= 55 in practice): U = hi * 2^24 + lo with hi < 2^32, lo < 2^24, and
+        // U mod p = ((hi mod p) * (2^24 mod p) + lo) mod p, the last sum staying below 2^25
+        uint32_t uhi[8], ulo[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            uhi[q] = uint32_t(U[q] >> 24);
+            ulo[q] = uint32_t(U[q]) & 0xffffffu;
+        }
         for (int t = 0; t < N; ++t) {
-            const uint32_t pm = c_mod[t], inv = c_mod_inv32[t], two32 = c_mod_2p32[t];
+            const uint32_t pm = c_mod[t], inv = c_mod_inv32[t], two24 = c_mod_2p24[t];
             __align__(16) uint16_t d[8];
 #pragma unroll
             for (int q = 0; q < 8; ++q) {
-                const uint32_t hi = uint32_t(U[q] >> 32), lo = uint32_t(U[q]);
-                const uint32_t rh = mod_small(hi, pm, inv), rl = mod_small(lo, pm, inv);
-                uint32_t rr_ = mod_small(rh * two32 + rl, pm, inv);
+                const uint32_t rh = mod_small(uhi[q], pm, inv);
+                uint32_t rr_ = mod_small(rh * two24 + ulo[q], pm, inv);
                 int v = int(rr_);
                 if (2 * v > int(pm)) v -= int(pm);  // symmetric range, |v| <= 128
                 d[q] = digit_bf16(neg[q] ? -v : v);
@@ -757,18 +766,38 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
                     if (lane == 0) mbar_arrive(smem_u32(&bars->acc_empty[buf]));
                 }
                 if (!ok) break;
-                // level sums -> global level plane (row-major, pitch npad)
-                int32_t* dst = p.levels + ((int64_t(seg) * p.max_levels + L) * p.mpad + row) * p.npad +
-                               int64_t(tn) * TN + h * 128;
+                // level sums -> global level plane (row-major, pitch npad); in the residue (CRT)
+                // schedule the sum is reduced modulo the level's modulus and stored as 16 bits
+                const int64_t plane_off = ((int64_t(seg) * p.max_levels + L) * p.mpad + row) * p.npad +
+                                          int64_t(tn) * TN + h * 128;
                 const uint32_t bias = (emode == kExact) ? ngroups * MAGIC_BITS : 0u;
+                if (emode == kExact && mode == kCrt) {
+                    uint16_t* dst = reinterpret_cast<uint16_t*>(p.levels) + plane_off;
+                    const uint32_t pm = c_mod[L], inv = c_mod_inv32[L];
 #pragma unroll
-                for (int c = 0; c < 128; c += 4) {
-                    int4 w;
-                    w.x = int32_t(acc[c + 0] - bias);
-                    w.y = int32_t(acc[c + 1] - bias);
-                    w.z = int32_t(acc[c + 2] - bias);
-                    w.w = int32_t(acc[c + 3] - bias);
-                    *reinterpret_cast<int4*>(dst + c) = w;
+                    for (int c = 0; c < 128; c += 8) {
+                        __align__(16) uint16_t rr[8];
+#pragma unroll
+                        for (int q = 0; q < 8; ++q) {
+                            const int32_t t = int32_t(acc[c + q] - bias);
+                            const uint32_t mag = t < 0 ? uint32_t(-int64_t(t)) : uint32_t(t);
+                            uint32_t rsd = mod_small(mag, pm, inv);
+                            if (t < 0 && rsd) rsd = pm - rsd;
+                            rr[q] = uint16_t(rsd);
+                        }
+                        *reinterpret_cast<uint4*>(dst + c) = *reinterpret_cast<const uint4*>(rr);
+                    }
+                } else {
+                    int32_t* dst = p.levels + plane_off;
+#pragma unroll
+                    for (int c = 0; c < 128; c += 4) {
+                        int4 w;
+                        w.x = int32_t(acc[c + 0] - bias);
+                        w.y = int32_t(acc[c + 1] - bias);
+                        w.z = int32_t(acc[c + 2] - bias);
+                        w.w = int32_t(acc[c + 3] - bias);
+                        *reinterpret_cast<int4*>(dst + c) = w;
+                    }
                 }
             }
         }
@@ -839,29 +868,29 @@ __global__ void combine_kernel(const int32_t* __restrict__ levels, int nseg, int
     if (mode == kCrt) {
         const int N = info->slices;
         const int ei = eA[i];
-        unsigned __int128 acc[COMBINE_COLS] = {0, 0, 0, 0};
+        const uint16_t* res16 = reinterpret_cast<const uint16_t*>(levels);
+        unsigned long long lo[COMBINE_COLS] = {0, 0, 0, 0}, hi[COMBINE_COLS] = {0, 0, 0, 0};
         for (int t = 0; t < N; ++t) {
             const uint32_t pm = c_mod[t], inv = c_mod_inv32[t], y = info->y[t];
             uint32_t c[COMBINE_COLS] = {0, 0, 0, 0};
             for (int g = 0; g < nseg; ++g) {
-                const int4 q = *reinterpret_cast<const int4*>(levels + (int64_t(g) * max_levels + t) * plane + off);
-                const int tv[4] = {q.x, q.y, q.z, q.w};
-#pragma unroll
-                for (int cc = 0; cc < COMBINE_COLS; ++cc) {
-                    // residue of the (signed, |v| < 2^31) segment sum in [0, p)
-                    const uint32_t mag = tv[cc] < 0 ? uint32_t(-(int64_t)tv[cc]) : uint32_t(tv[cc]);
-                    uint32_t rsd = mod_small(mag, pm, inv);
-                    if (tv[cc] < 0 && rsd) rsd = pm - rsd;
-                    c[cc] += rsd;
-                }
+                // four residues in [0, p) of this modulus and segment
+                const uint2 q = *reinterpret_cast<const uint2*>(res16 + (int64_t(g) * max_levels + t) * plane + off);
+                c[0] += q.x & 0xffffu; c[1] += q.x >> 16; c[2] += q.y & 0xffffu; c[3] += q.y >> 16;
             }
-            const unsigned __int128 Mt = ((unsigned __int128)info->M[t][1] << 64) | info->M[t][0];
+            const unsigned long long Mlo = info->M[t][0], Mhi = info->M[t][1];
 #pragma unroll
             for (int cc = 0; cc < COMBINE_COLS; ++cc) {
                 const uint32_t u = mod_small(mod_small(c[cc], pm, inv) * y, pm, inv);
-                acc[cc] += Mt * u;
+                // (hi, lo) += M_t * u with a 64 x 32 bit product per limb
+                const unsigned long long pl = Mlo * u, ph = __umul64hi(Mlo, u) + Mhi * u;
+                lo[cc] += pl;
+                hi[cc] += ph + (lo[cc] < pl ? 1ull : 0ull);
             }
         }
+        unsigned __int128 acc[COMBINE_COLS];
+#pragma unroll
+        for (int cc = 0; cc < COMBINE_COLS; ++cc) acc[cc] = ((unsigned __int128)hi[cc] << 64) | lo[cc];
         const unsigned __int128 P = ((unsigned __int128)info->P[1] << 64) | info->P[0];
 #pragma unroll
         for (int cc = 0; cc < COMBINE_COLS; ++cc) {
@@ -981,9 +1010,9 @@ int crt_worst_case_moduli(int64_t k, double target) {
     if (target <= 0) target = double(k) * 0x1p-53;
     const double r = 2.0 * std::sqrt(double(std::max<int64_t>(k, 1)));
     int beta = 1;
-    while (beta < 61 && (std::ldexp(1.0, -beta - 1) * 2 * r + std::ldexp(1.0, -2 * beta - 2) * r * r + 0x1p-52) > target)
+    while (beta <= 55 && (std::ldexp(1.0, -beta - 1) * 2 * r + std::ldexp(1.0, -2 * beta - 2) * r * r + 0x1p-52) > target)
         ++beta;
-    if (beta >= 61) return MAX_MODULI + 1;
+    if (beta > 55) return MAX_MODULI + 1;
     int kbits = 0;
     while ((int64_t(1) << kbits) < std::max<int64_t>(k, 2)) ++kbits;
     const double need = 2.0 + kbits + 2.0 * beta;
