@@ -133,10 +133,10 @@ struct RowAcc {
     int pad;
 };
 
-__global__ void stats_tile_kernel(const double* __restrict__ X, int64_t R, int64_t K, int64_t sr, int64_t sp,
-                                  RowAcc* __restrict__ acc) {
+__device__ __forceinline__ void stats_tile(const double* __restrict__ X, int64_t R, int64_t K, int64_t sr, int64_t sp,
+                                           RowAcc* __restrict__ acc, int by) {
     __shared__ unsigned long long tile[32][65];
-    const int64_t r0 = int64_t(blockIdx.y) * 32, p0 = int64_t(blockIdx.x) * 64;
+    const int64_t r0 = int64_t(by) * 32, p0 = int64_t(blockIdx.x) * 64;
     const int t = threadIdx.x;  // 256 threads
     const unsigned long long* Xb = reinterpret_cast<const unsigned long long*>(X);
     if (sp == 1) {
@@ -194,10 +194,9 @@ __global__ void stats_tile_kernel(const double* __restrict__ X, int64_t R, int64
     }
 }
 
-__global__ void stats_finalize_kernel(const double* __restrict__ X, int64_t R, int64_t K, int64_t sr, int64_t sp,
-                                      const RowAcc* __restrict__ acc, int* __restrict__ rexp,
-                                      double* __restrict__ rsq) {
-    const int64_t r = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void stats_finalize_row(const double* __restrict__ X, int64_t R, int64_t K, int64_t sr,
+                                                   int64_t sp, const RowAcc* __restrict__ acc, int* __restrict__ rexp,
+                                                   double* __restrict__ rsq, int64_t r) {
     if (r >= R) return;
     const RowAcc a = acc[r];
     if (a.flags & 1) {
@@ -218,6 +217,31 @@ __global__ void stats_finalize_kernel(const double* __restrict__ X, int64_t R, i
     }
     rexp[r] = e;
     rsq[r] = q;
+}
+
+// Both operands of a product go through one launch: blocks with blockIdx.y < yb0 work on A (its
+// rows), the others on B (its columns), so the two passes overlap on the device.
+struct OperandPair {
+    const double* X[2];
+    int64_t R[2], sr[2], sp[2];
+    RowAcc* acc[2];
+    int* rexp[2];
+    double* rsq[2];
+    __nv_bfloat16* planes[2];
+    int64_t rpad[2];
+    unsigned yb0;  // row blocks of A
+};
+
+__global__ void stats_tile_kernel(const OperandPair op, int64_t K) {
+    const int w = blockIdx.y < op.yb0 ? 0 : 1;
+    const int by = w ? int(blockIdx.y - op.yb0) : int(blockIdx.y);
+    stats_tile(op.X[w], op.R[w], K, op.sr[w], op.sp[w], op.acc[w], by);
+}
+
+__global__ void stats_finalize_pair_kernel(const OperandPair op, int64_t K, unsigned xb0) {
+    const int w = blockIdx.x < xb0 ? 0 : 1;
+    const int64_t r = int64_t(w ? blockIdx.x - xb0 : blockIdx.x) * blockDim.x + threadIdx.x;
+    stats_finalize_row(op.X[w], op.R[w], K, op.sr[w], op.sp[w], op.acc[w], op.rexp[w], op.rsq[w], r);
 }
 
 // One block: norms, scale norms, slice count and bound.  Sums are formed relative to the largest
@@ -434,11 +458,11 @@ __device__ __forceinline__ uint32_t mod_small(uint32_t x, uint32_t p, uint32_t i
     return r >= p ? r - p : r;
 }
 
-__global__ void slice_kernel(const double* __restrict__ X, int64_t R, int64_t K, int64_t sr, int64_t sp,
-                             const int* __restrict__ rexp, const SplitInfo* __restrict__ info, int mode,
-                             __nv_bfloat16* __restrict__ planes, int64_t rpad, int64_t kpad) {
+__device__ __forceinline__ void slice_tile(const double* __restrict__ X, int64_t R, int64_t K, int64_t sr, int64_t sp,
+                                           const int* __restrict__ rexp, const SplitInfo* __restrict__ info, int mode,
+                                           __nv_bfloat16* __restrict__ planes, int64_t rpad, int64_t kpad, int by) {
     __shared__ unsigned long long tile[32][65];
-    const int64_t r0 = int64_t(blockIdx.y) * 32, p0 = int64_t(blockIdx.x) * 64;
+    const int64_t r0 = int64_t(by) * 32, p0 = int64_t(blockIdx.x) * 64;
     const int t = threadIdx.x;  // 256 threads
     const unsigned long long* Xb = reinterpret_cast<const unsigned long long*>(X);
     if (sp == 1) {
@@ -522,6 +546,13 @@ __global__ void slice_kernel(const double* __restrict__ X, int64_t R, int64_t K,
         *reinterpret_cast<uint4*>(dst) = *reinterpret_cast<const uint4*>(hi);
         if (mode == kBf16x3) *reinterpret_cast<uint4*>(dst + pstride) = *reinterpret_cast<const uint4*>(lo);
     }
+}
+
+__global__ void slice_kernel(const OperandPair op, int64_t K, const SplitInfo* __restrict__ info, int mode,
+                             int64_t kpad) {
+    const int w = blockIdx.y < op.yb0 ? 0 : 1;
+    const int by = w ? int(blockIdx.y - op.yb0) : int(blockIdx.y);
+    slice_tile(op.X[w], op.R[w], K, op.sr[w], op.sp[w], op.rexp[w], info, mode, op.planes[w], op.rpad[w], kpad, by);
 }
 
 // ---- level / pair schedule ---------------------------------------------------------------------
@@ -869,15 +900,26 @@ __global__ void combine_kernel(const int32_t* __restrict__ levels, int nseg, int
         const int N = info->slices;
         const int ei = eA[i];
         const uint16_t* res16 = reinterpret_cast<const uint16_t*>(levels);
-        unsigned long long lo[COMBINE_COLS] = {0, 0, 0, 0}, hi[COMBINE_COLS] = {0, 0, 0, 0};
-        for (int t = 0; t < N; ++t) {
-            const uint32_t pm = c_mod[t], inv = c_mod_inv32[t], y = info->y[t];
-            uint32_t c[COMBINE_COLS] = {0, 0, 0, 0};
-            for (int g = 0; g < nseg; ++g) {
-                // four residues in [0, p) of this modulus and segment
-                const uint2 q = *reinterpret_cast<const uint2*>(res16 + (int64_t(g) * max_levels + t) * plane + off);
-                c[0] += q.x & 0xffffu; c[1] += q.x >> 16; c[2] += q.y & 0xffffu; c[3] += q.y >> 16;
+        // all residues of the four outputs first (independent loads in flight), then the CRT sum
+        uint2 rq[MAX_MODULI];
+#pragma unroll
+        for (int t = 0; t < MAX_MODULI; ++t) {
+            if (t < N) {
+                rq[t] = *reinterpret_cast<const uint2*>(res16 + int64_t(t) * plane + off);
+                for (int g = 1; g < nseg; ++g) {
+                    // segment residues add up (each < p, sums stay far below 2^16 * nseg)
+                    const uint2 q = *reinterpret_cast<const uint2*>(res16 + (int64_t(g) * max_levels + t) * plane + off);
+                    rq[t].x += q.x;  // lanes hold two 16-bit residues: no carry crosses for nseg < 256
+                    rq[t].y += q.y;
+                }
             }
+        }
+        unsigned long long lo[COMBINE_COLS] = {0, 0, 0, 0}, hi[COMBINE_COLS] = {0, 0, 0, 0};
+#pragma unroll
+        for (int t = 0; t < MAX_MODULI; ++t) {
+            if (t >= N) break;
+            const uint32_t pm = c_mod[t], inv = c_mod_inv32[t], y = info->y[t];
+            const uint32_t c[COMBINE_COLS] = {rq[t].x & 0xffffu, rq[t].x >> 16, rq[t].y & 0xffffu, rq[t].y >> 16};
             const unsigned long long Mlo = info->M[t][0], Mhi = info->M[t][1];
 #pragma unroll
             for (int cc = 0; cc < COMBINE_COLS; ++cc) {
@@ -1177,13 +1219,23 @@ int device_product(const Gemm& g_in, const SplitRequest& req, const LaunchCtl& c
     RowAcc* racc = static_cast<RowAcc*>(ws.get(kSlotScaleB, size_t(m + n) * sizeof(RowAcc), err));
     if (!racc) return GB300_ERR_NO_MEMORY;
     cudaMemsetAsync(racc, 0, size_t(m + n) * sizeof(RowAcc), st);
-    auto stats_launch = [&](const double* X, int64_t R, int64_t sr, int64_t sp, RowAcc* ra, int* ex, double* sq) {
-        dim3 grid(unsigned((k + 63) / 64), unsigned((R + 31) / 32));
-        stats_tile_kernel<<<grid, 256, 0, st>>>(X, R, k, sr, sp, ra);
-        stats_finalize_kernel<<<unsigned((R + 255) / 256), 256, 0, st>>>(X, R, k, sr, sp, ra, ex, sq);
-    };
-    stats_launch(A, m, a_sr, a_sp, racc, eA, sqA);
-    stats_launch(B, n, b_sr, b_sp, racc + m, eB, sqB);
+    OperandPair op;
+    op.X[0] = A; op.X[1] = B;
+    op.R[0] = m; op.R[1] = n;
+    op.sr[0] = a_sr; op.sr[1] = b_sr;
+    op.sp[0] = a_sp; op.sp[1] = b_sp;
+    op.acc[0] = racc; op.acc[1] = racc + m;
+    op.rexp[0] = eA; op.rexp[1] = eB;
+    op.rsq[0] = sqA; op.rsq[1] = sqB;
+    op.planes[0] = pa; op.planes[1] = pb;
+    op.rpad[0] = mpad; op.rpad[1] = npad;
+    op.yb0 = unsigned((m + 31) / 32);
+    {
+        dim3 grid(unsigned((k + 63) / 64), unsigned((m + 31) / 32 + (n + 31) / 32));
+        stats_tile_kernel<<<grid, 256, 0, st>>>(op, k);
+        const unsigned xb0 = unsigned((m + 255) / 256);
+        stats_finalize_pair_kernel<<<xb0 + unsigned((n + 255) / 256), 256, 0, st>>>(op, k, xb0);
+    }
     const double target = req.target_error > 0 ? req.target_error : double(k) * 0x1p-53;
     split_info_kernel<<<1, 256, 0, st>>>(eA, sqA, m, eB, sqB, n, k, mode, req.slices > 0 ? max_planes : 0,
                                          max_planes, target, info);
@@ -1192,12 +1244,12 @@ int device_product(const Gemm& g_in, const SplitRequest& req, const LaunchCtl& c
         return GB300_ERR_CUDA;
     }
     {
-        dim3 grid(unsigned(kpad / 64), unsigned(mpad / 32));
-        slice_kernel<<<grid, 256, 0, st>>>(A, m, k, a_sr, a_sp, eA, info, mode, pa, mpad, kpad);
-        dim3 gridb(unsigned(kpad / 64), unsigned(npad / 32));
-        slice_kernel<<<gridb, 256, 0, st>>>(B, n, k, b_sr, b_sp, eB, info, mode, pb, npad, kpad);
+        OperandPair sp2 = op;
+        sp2.yb0 = unsigned(mpad / 32);
+        dim3 grid(unsigned(kpad / 64), unsigned(mpad / 32 + npad / 32));
+        slice_kernel<<<grid, 256, 0, st>>>(sp2, k, info, mode, kpad);
     }
-    count_launches(7);
+    count_launches(4);
     if (cudaError_t le = cudaGetLastError(); le != cudaSuccess) {
         if (err) *err = std::string("split slicing launch: ") + cudaGetErrorString(le);
         return GB300_ERR_CUDA;
