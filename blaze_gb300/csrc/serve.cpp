@@ -51,6 +51,7 @@ struct ServeRequest {
     Gemm g;
     SplitRequest sreq;
     size_t footprint = 0;
+    size_t need[kSlotCount] = {};
     bool large = false;
     Clock::time_point t_submit, t_start, t_end;
     int slot = -1;
@@ -108,19 +109,24 @@ class Server {
             if (!slots[i].cur) { free_slot = int(i); break; }
         if (free_slot < 0) return false;
         ServeSlot& sl = slots[size_t(free_slot)];
+        // projected bytes of the slot after running r: each buffer grows to the larger of what it
+        // holds and what r needs
+        auto projected = [&](const ServeSlot& x) {
+            size_t t = 0;
+            for (int s = 0; s < kSlotCount; ++s) t += std::max(x.ws.bytes[s], r->need[s]);
+            return t;
+        };
         size_t others = 0;
         for (size_t i = 0; i < slots.size(); ++i)
             if (int(i) != free_slot) others += slots[i].ws.total();
-        size_t mine = std::max(sl.ws.total(), r->footprint);
-        if (others + mine > budget) {
-            // give back memory of idle slots before refusing
+        if (others + projected(sl) > budget) {
+            // give back memory of idle slots (this one included) before refusing
             for (size_t i = 0; i < slots.size(); ++i)
                 if (!slots[i].cur && slots[i].ws.total() > 0) slots[i].ws.release();
             others = 0;
             for (size_t i = 0; i < slots.size(); ++i)
                 if (int(i) != free_slot) others += slots[i].ws.total();
-            mine = std::max(sl.ws.total(), r->footprint);
-            if (others + mine > budget) return false;
+            if (others + projected(sl) > budget) return false;
         }
         launch(r, free_slot);
         return true;
@@ -301,7 +307,9 @@ int gb300_server_submit(gb300_server* srv, const gb300_serve_request* q, uint64_
     r->sreq.target_error = q->target_error;
     r->sreq.slices = 0;
     r->large = std::max(q->m, q->n) >= s->cfg.large_threshold && q->accuracy != GB300_METHOD_NATIVE;
-    r->footprint = (g.m > 0 && g.n > 0) ? gb::device_product_footprint(g, r->sreq) : 0;
+    if (g.m > 0 && g.n > 0) gb::device_product_slot_needs(g, r->sreq, r->need);
+    r->footprint = 0;
+    for (int s_ = 0; s_ < gb::kSlotCount; ++s_) r->footprint += r->need[s_];
     if (cudaEventCreateWithFlags(&r->done, cudaEventDisableTiming) != cudaSuccess) {
         delete r;
         gb::set_error(GB300_ERR_CUDA, "gb300_server_submit: event creation failed");

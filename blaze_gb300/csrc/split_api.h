@@ -35,7 +35,9 @@ struct Workspace;
 int device_product(const Gemm& g, const SplitRequest& req, const LaunchCtl& ctl, cudaStream_t s, Workspace& ws,
                    SplitResult* out, std::string* err);
 
-// Device scratch bytes device_product needs for g (an upper bound used for admission control).
+// Device scratch bytes device_product needs for g (admission control): per workspace slot, rounded
+// the way Workspace::get rounds, and their sum.
+void device_product_slot_needs(const Gemm& g, const SplitRequest& req, size_t need[]);
 size_t device_product_footprint(const Gemm& g, const SplitRequest& req);
 
 }  // namespace gb

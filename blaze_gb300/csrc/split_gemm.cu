@@ -1161,14 +1161,36 @@ int realign_operands(Gemm& g, Workspace& ws, cudaStream_t st, std::string* err) 
 
 }  // namespace
 
-size_t device_product_footprint(const Gemm& g, const SplitRequest& req) {
+void device_product_slot_needs(const Gemm& g, const SplitRequest& req, size_t need[kSlotCount]) {
     Runtime& r = runtime();
-    const size_t extra = realign_bytes(g);
+    for (int i = 0; i < kSlotCount; ++i) need[i] = 0;
+    auto rounded = [](size_t b) { return b == 0 ? size_t(0) : (b + (size_t(2) << 20) - 1) & ~((size_t(2) << 20) - 1); };
+    if (g.k > 0) {
+        int64_t rr, cc;
+        if (!tma_ready(g.A, g.lda)) { stored_a(g, &rr, &cc); need[kSlotA] = rounded(size_t(rr) * size_t((cc + 1) / 2 * 2) * 8); }
+        if (!tma_ready(g.B, g.ldb)) { stored_b(g, &rr, &cc); need[kSlotB] = rounded(size_t(rr) * size_t((cc + 1) / 2 * 2) * 8); }
+    }
     if (g.k == 0 || req.method == GB300_METHOD_NATIVE || (req.method == GB300_METHOD_AUTO && auto_uses_native(g))) {
         const int splits = g.k > 0 ? native_choose_splits(g.m, g.n, g.k, 8, r.num_sms) : 1;
-        return extra + (splits > 1 ? size_t(splits) * size_t(g.m) * size_t(g.n) * 8 : 0);
+        if (splits > 1) need[kSlotWork] = rounded(size_t(splits) * size_t(g.m) * size_t(g.n) * 8);
+        return;
     }
-    return extra + split_scratch_bytes(g, split_geometry(g, req, r.num_sms));
+    const SplitGeometry G = split_geometry(g, req, r.num_sms);
+    need[kSlotSliceA] = rounded(size_t(G.max_planes) * size_t(G.mpad) * size_t(G.kpad) * 2);
+    need[kSlotSliceB] = rounded(size_t(G.max_planes) * size_t(G.npad) * size_t(G.kpad) * 2);
+    need[kSlotLevels] = rounded(size_t(G.nseg) * G.max_levels * size_t(G.mpad) * size_t(G.npad) * 4);
+    const int64_t off_sq = round_up((g.m + g.n) * int64_t(sizeof(int)), 256);
+    const int64_t off_info = round_up(off_sq + (g.m + g.n) * int64_t(sizeof(double)), 256);
+    need[kSlotScaleA] = rounded(size_t(off_info) + ((sizeof(SplitInfo) + 255) / 256) * 256);
+    need[kSlotScaleB] = rounded(size_t(g.m + g.n) * sizeof(RowAcc));
+}
+
+size_t device_product_footprint(const Gemm& g, const SplitRequest& req) {
+    size_t need[kSlotCount];
+    device_product_slot_needs(g, req, need);
+    size_t t = 0;
+    for (int i = 0; i < kSlotCount; ++i) t += need[i];
+    return t;
 }
 
 int device_product(const Gemm& g_in, const SplitRequest& req, const LaunchCtl& ctl, cudaStream_t st, Workspace& ws,
