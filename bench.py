@@ -505,7 +505,8 @@ def ours(args, dist: Dist):
 
     peaks, peaks_src = read_peaks()
 
-    pairs = info.slices_used * (info.slices_used + 1) // 2
+    # tensor products per split product: one per modulus (CRT scheme) or S(S+1)/2 digit pairs
+    pairs = info.slices_used if info.method_used == G.METHOD_SPLIT_CRT else info.slices_used * (info.slices_used + 1) // 2
     tc_flops = pairs * flops  # BF16 tensor operations of the slice products
     tc_ms = ms_tc / max(n_tc, 1)
     achieved = tc_flops / (tc_ms * 1e-3) / 1e12
@@ -518,10 +519,11 @@ def ours(args, dist: Dist):
             traffic = int(tj["dram_bytes_per_launch"])
     except (OSError, ValueError, KeyError):
         traffic = None
-    roofline = {"kernel": "tc_gemm_kernel<exact> (split slice products)", "bound": "tensor",
+    roofline = {"kernel": "tc_gemm_kernel<exact> (" + ("residue products" if info.method_used == G.METHOD_SPLIT_CRT
+                                                    else "digit-slice products") + ")", "bound": "tensor",
                 "achieved": round(achieved, 2), "peak": peak, "unit": "TFLOP/s", "frac": round(achieved / peak, 4),
                 "traffic": traffic, "peak_source": f"bf16_tflops_sustained ({peaks_src})",
-                "work_per_launch": f"{pairs} slice products x 2*{n}^3 BF16 tensor ops",
+                "work_per_launch": f"{pairs} BF16 products x 2*{n}^3 tensor ops",
                 "kernel_ms": round(tc_ms, 3), "kernel_share_of_step": round(tc_ms / ms_step, 4)}
 
     if dist.rank == 0:
@@ -531,7 +533,10 @@ def ours(args, dist: Dist):
                 "data": "synthetic",
                 "config": {"workload": f"dense FP64-accurate GEMM C=A*B, M=N=K={n}, row-major x row-major, "
                                        f"uniform [-1,1] (mt19937 seed {args.seed})",
-                           "method": "split (Ozaki-style BF16 slices on tcgen05, exact int32 slice sums, FP64 "
+                           "method": ("split, residue (CRT) scheme: beta-bit integer scaling, one BF16 tcgen05 product "
+                                      "per modulus with exact int32 sums, exact 128-bit reconstruction")
+                                     if info.method_used == G.METHOD_SPLIT_CRT else
+                                     "split, digit scheme (Ozaki BF16 slices on tcgen05, exact int32 slice sums, FP64 "
                                      "recombination)",
                            "slices": info.slices_used, "target_error": f"k*2^-53 = {n * 2.0 ** -53:.3e}",
                            "l2": "operands larger than L2 (512 MiB each)", "parallelism": "replicas"},

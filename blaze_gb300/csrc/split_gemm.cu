@@ -112,6 +112,12 @@ struct SplitInfo {
     unsigned long long M[MAX_MODULI][2]; // P / p_t
     unsigned long long Pm[4][2];         // 8P, 4P, 2P, P for the final reduction
     uint32_t y[MAX_MODULI];              // (P / p_t)^-1 mod p_t
+    // two-level reconstruction: moduli paired into "super" moduli P_s = p * q (q = 1 for a single)
+    int nsup;
+    uint32_t sp[8], sq[8], sinv[8];      // p, q, p^-1 mod q
+    uint32_t Ps[8], ys[8];               // P_s and (P / P_s)^-1 mod P_s
+    unsigned long long Pinv64[8];        // floor(2^64 / P_s)
+    unsigned long long Ms[8][2];         // P / P_s
 };
 
 // ---- pre-pass ------------------------------------------------------------------------------
@@ -329,7 +335,9 @@ __global__ void split_info_kernel(const int* __restrict__ eA, const double* __re
                 have += log2(double(c_mod[N]));
                 ++N;
             }
-            if (have < need) beta = int(floor((have - 2.0 - kbits) / 2.0));  // the planned moduli cap beta
+            // the moduli chosen may carry more bits than needed: round to as many bits as they allow
+            beta = int(floor((have - 2.0 - kbits) / 2.0));
+            beta = beta > 55 ? 55 : beta;
             r.slices = N;
             r.beta = beta;
             r.bound = bnd(beta);
@@ -360,6 +368,36 @@ __global__ void split_info_kernel(const int* __restrict__ eA, const double* __re
                 const unsigned __int128 v = P << (3 - i);
                 r.Pm[i][0] = (unsigned long long)v;
                 r.Pm[i][1] = (unsigned long long)(v >> 64);
+            }
+            auto inv_mod = [](long long a, long long m) {
+                long long b = m, x0 = 1, x1 = 0;
+                a %= m;
+                while (b) {
+                    const long long q = a / b, ta = a - q * b, tx = x0 - q * x1;
+                    a = b; b = ta; x0 = x1; x1 = tx;
+                }
+                return (long long)(((x0 % m) + m) % m);
+            };
+            r.nsup = (N + 1) / 2;
+            for (int s2 = 0; s2 < r.nsup; ++s2) {
+                const uint32_t pp = c_mod[2 * s2], qq = (2 * s2 + 1 < N) ? c_mod[2 * s2 + 1] : 1u;
+                r.sp[s2] = pp;
+                r.sq[s2] = qq;
+                r.sinv[s2] = qq > 1 ? uint32_t(inv_mod(pp, qq)) : 0u;
+                r.Ps[s2] = pp * qq;
+                r.Pinv64[s2] = ~0ull / (unsigned long long)(pp * qq);
+            }
+            for (int s2 = 0; s2 < r.nsup; ++s2) {
+                unsigned __int128 Ms = 1;
+                unsigned long long mres = 1;
+                for (int u = 0; u < r.nsup; ++u) {
+                    if (u == s2) continue;
+                    Ms *= r.Ps[u];
+                    mres = (mres * (r.Ps[u] % r.Ps[s2])) % r.Ps[s2];
+                }
+                r.Ms[s2][0] = (unsigned long long)Ms;
+                r.Ms[s2][1] = (unsigned long long)(Ms >> 64);
+                r.ys[s2] = uint32_t(inv_mod((long long)mres, (long long)r.Ps[s2]));
             }
         } else if (mode == kExact) {
             int S = fixed_slices;
@@ -914,18 +952,37 @@ __global__ void combine_kernel(const int32_t* __restrict__ levels, int nseg, int
                 }
             }
         }
+        // residue of modulus t for column cc, in [0, p) (segment residues were summed: reduce again)
+        auto res = [&](int t, int cc) -> uint32_t {
+            const uint32_t v = (cc & 1) ? ((cc < 2 ? rq[t].x : rq[t].y) >> 16) : ((cc < 2 ? rq[t].x : rq[t].y) & 0xffffu);
+            return nseg > 1 ? mod_small(v, c_mod[t], c_mod_inv32[t]) : v;
+        };
+        // level 1: pairs (p, q) -> x in [0, pq) with x = c_p + p * ((c_q - c_p) p^-1 mod q)
+        // level 2: sum_s ((x_s * y_s) mod P_s) * (P / P_s), reduced modulo P below
         unsigned long long lo[COMBINE_COLS] = {0, 0, 0, 0}, hi[COMBINE_COLS] = {0, 0, 0, 0};
 #pragma unroll
-        for (int t = 0; t < MAX_MODULI; ++t) {
-            if (t >= N) break;
-            const uint32_t pm = c_mod[t], inv = c_mod_inv32[t], y = info->y[t];
-            const uint32_t c[COMBINE_COLS] = {rq[t].x & 0xffffu, rq[t].x >> 16, rq[t].y & 0xffffu, rq[t].y >> 16};
-            const unsigned long long Mlo = info->M[t][0], Mhi = info->M[t][1];
+        for (int s2 = 0; s2 < (MAX_MODULI + 1) / 2; ++s2) {
+            if (s2 >= info->nsup) break;
+            const uint32_t pp = info->sp[s2], qq = info->sq[s2], pinv = info->sinv[s2], Ps = info->Ps[s2];
+            const uint32_t ys = info->ys[s2];
+            const unsigned long long binv = info->Pinv64[s2], Mlo = info->Ms[s2][0], Mhi = info->Ms[s2][1];
+            const int tq = 2 * s2 + 1;
 #pragma unroll
             for (int cc = 0; cc < COMBINE_COLS; ++cc) {
-                const uint32_t u = mod_small(mod_small(c[cc], pm, inv) * y, pm, inv);
-                // (hi, lo) += M_t * u with a 64 x 32 bit product per limb
-                const unsigned long long pl = Mlo * u, ph = __umul64hi(Mlo, u) + Mhi * u;
+                uint32_t x = res(2 * s2, cc);
+                if (qq > 1) {
+                    const uint32_t cq = res(tq < MAX_MODULI ? tq : 0, cc);
+                    const uint32_t tdiff = cq + 2 * qq - x;  // positive, < 3 * 257
+                    const uint32_t t = mod_small(tdiff * pinv, qq, c_mod_inv32[tq < MAX_MODULI ? tq : 0]);
+                    x += pp * t;
+                }
+                // u = (x * y_s) mod P_s with a 64-bit Barrett step
+                const unsigned long long prod = (unsigned long long)x * ys;
+                const unsigned long long qe = __umul64hi(prod, binv);
+                unsigned long long u = prod - qe * Ps;
+                if (u >= Ps) u -= Ps;
+                const uint32_t uu = uint32_t(u);
+                const unsigned long long pl = Mlo * uu, ph = __umul64hi(Mlo, uu) + Mhi * uu;
                 lo[cc] += pl;
                 hi[cc] += ph + (lo[cc] < pl ? 1ull : 0ull);
             }
