@@ -88,15 +88,31 @@ enum Mode : int { kExact = 0, kBf16 = 1, kBf16x3 = 2, kCrt = 3 };
 // 239; 233; 229; 227; 223; 7,31; 211; 199.  Product of all 15: about 2^118.2.
 constexpr int MAX_MODULI = 15;
 __constant__ uint32_t c_mod[MAX_MODULI] = {257, 256, 255, 253, 251, 247, 241, 239, 233, 229, 227, 223, 217, 211, 199};
-// floor(2^32 / p) for the reduction of 32-bit values, and 2^32 mod p for 64-bit values.
+// floor(2^32 / p) for the reduction of 32-bit values.
 __constant__ uint32_t c_mod_inv32[MAX_MODULI] = {
     16711935u, 16777216u, 16843009u, 16976155u, 17111423u, 17388531u, 17821441u, 17970574u,
     18433336u, 18755315u, 18920560u, 19259943u, 19792476u, 20355295u, 21582750u};
-__constant__ uint32_t c_mod_2p32[MAX_MODULI] = {1u, 0u, 1u, 81u, 123u, 139u, 15u, 110u, 8u, 161u, 176u, 7u, 4u, 51u, 46u};
-__constant__ uint32_t c_mod_2p24[MAX_MODULI] = {256u, 0u, 1u, 27u, 125u, 235u, 1u, 133u, 51u, 218u, 100u, 34u, 78u, 184u, 123u};
 // log2 of the running products of the moduli (host-side copy for the worst-case plan).
 constexpr double kModLog2[MAX_MODULI] = {8.00562, 8.0, 7.99435, 7.98299, 7.97154, 7.94837, 7.91289, 7.90087,
                                          7.86419, 7.83920, 7.82655, 7.80090, 7.76155, 7.72110, 7.63662};
+
+// 2^20 mod p and 2^40 mod p: the slice kernel reduces a 56-bit integer U = u2 2^40 + u1 2^20 + u0
+// as u2 (2^40 mod p) + u1 (2^20 mod p) + u0 < 2^29 with one 32-bit reduction.
+__constant__ uint32_t c_mod_2p20[MAX_MODULI] = {16, 0, 16, 144, 149, 61, 226, 83, 76, 214, 63, 30, 32, 117, 45};
+__constant__ uint32_t c_mod_2p40[MAX_MODULI] = {256, 0, 1, 243, 113, 16, 225, 197, 184, 225, 110, 8, 156, 185, 35};
+
+// CRT reconstruction in two levels.  The N moduli are paired largest with smallest into "super"
+// moduli P_s = p q < 2^16 (a modulus left over, or both of N = 2, stays single with q = 1); a pair's
+// residue follows from one Garner step, and the super residues combine as
+// W = sum_s ((x_s y_s) mod P_s) (P / P_s) with 32-bit limbs.  One record is 64 bytes (four 16-byte
+// loads in the combine kernel).
+struct __align__(16) SuperMod {
+    uint32_t p, q, pinv, pinv32;      // p, q, p^-1 mod q, floor(2^32 / p)
+    uint32_t qinv32, Ps, ys, Psinv32; // floor(2^32 / q), P_s, (P / P_s)^-1 mod P_s, floor(2^32 / P_s)
+    uint32_t M[4];                    // P / P_s, 32-bit limbs (least significant first)
+    float finv;                       // 1 / P_s (FP32)
+    int ia, ib, pad;                  // residue planes of p and q
+};
 
 // Device-side result of the pre-pass: the slice count and the bound it guarantees.
 struct SplitInfo {
@@ -107,17 +123,11 @@ struct SplitInfo {
     double scaleA, scaleB;// ||2^e||_2, ||2^f||_2
     // CRT mode
     int beta;             // operands are rounded to beta-bit integers per row / column
-    int pad;
-    unsigned long long P[2];             // product of the N moduli (lo, hi)
-    unsigned long long M[MAX_MODULI][2]; // P / p_t
-    unsigned long long Pm[4][2];         // 8P, 4P, 2P, P for the final reduction
-    uint32_t y[MAX_MODULI];              // (P / p_t)^-1 mod p_t
-    // two-level reconstruction: moduli paired into "super" moduli P_s = p * q (q = 1 for a single)
-    int nsup;
-    uint32_t sp[8], sq[8], sinv[8];      // p, q, p^-1 mod q
-    uint32_t Ps[8], ys[8];               // P_s and (P / P_s)^-1 mod P_s
-    unsigned long long Pinv64[8];        // floor(2^64 / P_s)
-    unsigned long long Ms[8][2];         // P / P_s
+    int nsup;             // super moduli
+    uint32_t P32[4];      // product of the N moduli, 32-bit limbs
+    float fbias;          // sum_s fl(2^23 / P_s): offset of the FP32 quotient estimate
+    int pad[3];
+    SuperMod sup[8];
 };
 
 // ---- pre-pass ------------------------------------------------------------------------------
@@ -272,6 +282,12 @@ __device__ int block_max_int(int v, int* red) {
     return t;
 }
 
+// 2^x for an integer x <= 0 from the bit pattern (0 below the normal range, where the weight of a
+// row in a norm sum no longer matters)
+__device__ __forceinline__ double pow2i(int x) {
+    return x < -1022 ? 0.0 : __longlong_as_double((long long)(x + 1023) << 52);
+}
+
 __global__ void split_info_kernel(const int* __restrict__ eA, const double* __restrict__ qA, int64_t m,
                                   const int* __restrict__ eB, const double* __restrict__ qB, int64_t n, int64_t k,
                                   int mode, int fixed_slices, int cap_planes, double target, SplitInfo* info) {
@@ -292,13 +308,13 @@ __global__ void split_info_kernel(const int* __restrict__ eA, const double* __re
     double sa = 0, na = 0, sb = 0, nb = 0;
     for (int64_t i = threadIdx.x; i < m; i += blockDim.x) {
         if (eA[i] == kNonFinite || qA[i] <= 0.0) continue;
-        const double w = ldexp(1.0, 2 * (eA[i] - EA));
+        const double w = pow2i(2 * (eA[i] - EA));
         sa += w;
         na += w * qA[i];
     }
     for (int64_t j = threadIdx.x; j < n; j += blockDim.x) {
         if (eB[j] == kNonFinite || qB[j] <= 0.0) continue;
-        const double w = ldexp(1.0, 2 * (eB[j] - EB));
+        const double w = pow2i(2 * (eB[j] - EB));
         sb += w;
         nb += w * qB[j];
     }
@@ -321,7 +337,7 @@ __global__ void split_info_kernel(const int* __restrict__ eA, const double* __re
             const double rA = (na > 0) ? sqrt(double(k) * sa / na) : 0.0;
             const double rB = (nb > 0) ? sqrt(double(k) * sb / nb) : 0.0;
             auto bnd = [&](int b) {
-                return ldexp(1.0, -b - 1) * (rA + rB) + ldexp(1.0, -2 * b - 2) * rA * rB + ldexp(1.0, -52);
+                return pow2i(-b - 1) * (rA + rB) + pow2i(-2 * b - 2) * rA * rB + pow2i(-52);
             };
             // beta <= 55 keeps |A'| < 2^56, the range of the residue extraction
             int beta = 1;
@@ -341,34 +357,10 @@ __global__ void split_info_kernel(const int* __restrict__ eA, const double* __re
             r.slices = N;
             r.beta = beta;
             r.bound = bnd(beta);
-            // CRT constants: P, M_t = P / p_t, y_t = M_t^-1 mod p_t
+            // CRT constants
             unsigned __int128 P = 1;
             for (int t = 0; t < N; ++t) P *= c_mod[t];
-            r.P[0] = (unsigned long long)P;
-            r.P[1] = (unsigned long long)(P >> 64);
-            for (int t = 0; t < N; ++t) {
-                unsigned __int128 Mt = 1;
-                uint32_t mres = 1;
-                for (int u = 0; u < N; ++u) {
-                    if (u == t) continue;
-                    Mt *= c_mod[u];
-                    mres = (mres * (c_mod[u] % c_mod[t])) % c_mod[t];
-                }
-                r.M[t][0] = (unsigned long long)Mt;
-                r.M[t][1] = (unsigned long long)(Mt >> 64);
-                // inverse of mres modulo p_t (extended Euclid on small numbers)
-                long long a = mres, b = c_mod[t], x0 = 1, x1 = 0;
-                while (b) {
-                    const long long q = a / b, ta = a - q * b, tx = x0 - q * x1;
-                    a = b; b = ta; x0 = x1; x1 = tx;
-                }
-                r.y[t] = uint32_t(((x0 % (long long)c_mod[t]) + c_mod[t]) % c_mod[t]);
-            }
-            for (int i = 0; i < 4; ++i) {
-                const unsigned __int128 v = P << (3 - i);
-                r.Pm[i][0] = (unsigned long long)v;
-                r.Pm[i][1] = (unsigned long long)(v >> 64);
-            }
+            for (int l = 0; l < 4; ++l) r.P32[l] = uint32_t(P >> (32 * l));
             auto inv_mod = [](long long a, long long m) {
                 long long b = m, x0 = 1, x1 = 0;
                 a %= m;
@@ -378,26 +370,52 @@ __global__ void split_info_kernel(const int* __restrict__ eA, const double* __re
                 }
                 return (long long)(((x0 % m) + m) % m);
             };
-            r.nsup = (N + 1) / 2;
-            for (int s2 = 0; s2 < r.nsup; ++s2) {
-                const uint32_t pp = c_mod[2 * s2], qq = (2 * s2 + 1 < N) ? c_mod[2 * s2 + 1] : 1u;
-                r.sp[s2] = pp;
-                r.sq[s2] = qq;
-                r.sinv[s2] = qq > 1 ? uint32_t(inv_mod(pp, qq)) : 0u;
-                r.Ps[s2] = pp * qq;
-                r.Pinv64[s2] = ~0ull / (unsigned long long)(pp * qq);
+            // pairs (t, N-1-t): every product stays below 2^16 for N >= 3
+            int ns = 0;
+            if (N == 2) {
+                r.sup[0].ia = 0; r.sup[0].ib = -1;
+                r.sup[1].ia = 1; r.sup[1].ib = -1;
+                ns = 2;
+            } else {
+                for (int t = 0; t < N / 2; ++t) {
+                    r.sup[ns].ia = t;
+                    r.sup[ns].ib = N - 1 - t;
+                    ++ns;
+                }
+                if (N & 1) {
+                    r.sup[ns].ia = N / 2;
+                    r.sup[ns].ib = -1;
+                    ++ns;
+                }
             }
-            for (int s2 = 0; s2 < r.nsup; ++s2) {
+            r.nsup = ns;
+            float fb = 0.f;
+            for (int s = 0; s < ns; ++s) {
+                SuperMod& sm = r.sup[s];
+                sm.p = c_mod[sm.ia];
+                sm.q = sm.ib >= 0 ? c_mod[sm.ib] : 1u;
+                sm.pinv = sm.q > 1 ? uint32_t(inv_mod(sm.p, sm.q)) : 0u;
+                sm.pinv32 = uint32_t(0x100000000ull / sm.p);
+                sm.qinv32 = sm.q > 1 ? uint32_t(0x100000000ull / sm.q) : 0u;
+                sm.Ps = sm.p * sm.q;
+                sm.Psinv32 = uint32_t(0x100000000ull / sm.Ps);
+                sm.finv = 1.0f / float(sm.Ps);
+                sm.pad = 0;
+                if (sm.ib < 0) sm.ib = sm.ia;  // never read as a residue of a second modulus
+                fb += 8388608.0f * sm.finv;
+            }
+            r.fbias = fb;
+            for (int s = 0; s < ns; ++s) {
+                SuperMod& sm = r.sup[s];
                 unsigned __int128 Ms = 1;
                 unsigned long long mres = 1;
-                for (int u = 0; u < r.nsup; ++u) {
-                    if (u == s2) continue;
-                    Ms *= r.Ps[u];
-                    mres = (mres * (r.Ps[u] % r.Ps[s2])) % r.Ps[s2];
+                for (int u = 0; u < ns; ++u) {
+                    if (u == s) continue;
+                    Ms *= r.sup[u].Ps;
+                    mres = (mres * (r.sup[u].Ps % sm.Ps)) % sm.Ps;
                 }
-                r.Ms[s2][0] = (unsigned long long)Ms;
-                r.Ms[s2][1] = (unsigned long long)(Ms >> 64);
-                r.ys[s2] = uint32_t(inv_mod((long long)mres, (long long)r.Ps[s2]));
+                for (int l = 0; l < 4; ++l) sm.M[l] = uint32_t(Ms >> (32 * l));
+                sm.ys = uint32_t(inv_mod((long long)mres, (long long)sm.Ps));
             }
         } else if (mode == kExact) {
             int S = fixed_slices;
@@ -526,34 +544,37 @@ __device__ __forceinline__ void slice_tile(const double* __restrict__ X, int64_t
         const int N = info->slices, beta = info->beta;
         const int e = (r < R) ? rexp[r] : 0;
         const bool bad = (e == kNonFinite);
-        unsigned long long U[8];
-        bool neg[8];
+        // U = |round(a 2^(beta-e))| < 2^56 as u2 2^40 + u1 2^20 + u0; u0 carries an offset of 128 so
+        // that r = (U + 128) mod p gives the residue v = r - 128 in [-128, p - 129], |v| <= 128
+        uint32_t u0[8], u1[8], u2[8], sgn[4];
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
             const unsigned long long bits = bad ? 0ull : tile[rr][pp0 + q];
-            neg[q] = (bits >> 63) != 0;
-            U[q] = int_magnitude(bits, beta - e);
-        }
-        // U < 2^56 (beta <= 55 in practice): U = hi * 2^24 + lo with hi < 2^32, lo < 2^24, and
-        // U mod p = ((hi mod p) * (2^24 mod p) + lo) mod p, the last sum staying below 2^25
-        uint32_t uhi[8], ulo[8];
-#pragma unroll
-        for (int q = 0; q < 8; ++q) {
-            uhi[q] = uint32_t(U[q] >> 24);
-            ulo[q] = uint32_t(U[q]) & 0xffffffu;
+            const unsigned long long U = int_magnitude(bits, beta - e);
+            u0[q] = (uint32_t(U) & 0xfffffu) + 128u;
+            u1[q] = uint32_t(U >> 20) & 0xfffffu;
+            u2[q] = uint32_t(U >> 40);
+            const uint32_t s = uint32_t(bits >> 63);
+            if (q & 1) sgn[q / 2] |= s << 31;
+            else sgn[q / 2] = s << 15;
         }
         for (int t = 0; t < N; ++t) {
-            const uint32_t pm = c_mod[t], inv = c_mod_inv32[t], two24 = c_mod_2p24[t];
-            __align__(16) uint16_t d[8];
+            const uint32_t pm = c_mod[t], inv = c_mod_inv32[t], c20 = c_mod_2p20[t], c40 = c_mod_2p40[t];
+            uint32_t fb[8];
 #pragma unroll
             for (int q = 0; q < 8; ++q) {
-                const uint32_t rh = mod_small(uhi[q], pm, inv);
-                uint32_t rr_ = mod_small(rh * two24 + ulo[q], pm, inv);
-                int v = int(rr_);
-                if (2 * v > int(pm)) v -= int(pm);  // symmetric range, |v| <= 128
-                d[q] = digit_bf16(neg[q] ? -v : v);
+                const uint32_t x = u2[q] * c40 + u1[q] * c20 + u0[q];  // < 2^29
+                uint32_t r = x - __umulhi(x, inv) * pm;
+                r = min(r, r - pm);
+                // float(r - 128) exactly through the 1.5 * 2^23 bias; |r - 128| <= 128 keeps it a BF16
+                fb[q] = __float_as_uint(__uint_as_float(MAGIC_BITS - 128u + r) - MAGIC);
             }
-            *reinterpret_cast<uint4*>(dst + t * pstride) = *reinterpret_cast<const uint4*>(d);
+            uint4 w;
+            w.x = __byte_perm(fb[0], fb[1], 0x7632) ^ sgn[0];
+            w.y = __byte_perm(fb[2], fb[3], 0x7632) ^ sgn[1];
+            w.z = __byte_perm(fb[4], fb[5], 0x7632) ^ sgn[2];
+            w.w = __byte_perm(fb[6], fb[7], 0x7632) ^ sgn[3];
+            *reinterpret_cast<uint4*>(dst + t * pstride) = w;
         }
     } else if (mode == kExact) {
         const int S = info->slices;
@@ -917,6 +938,42 @@ __device__ __forceinline__ double int128_to_double_scaled(__int128 W, int x) {
     return neg ? -v : v;
 }
 
+// The same for W given as two's-complement 64-bit halves, on 64-bit integer operations: normalize
+// the magnitude so that its top bit is bit 127, keep 53 bits, round to nearest even, and write the
+// exponent field by adding (be - 1) << 52 to the 53-bit mantissa (a rounding carry into 2^53 then
+// moves the exponent up by itself).
+__device__ __forceinline__ double i128_to_double_scaled(unsigned long long hi, unsigned long long lo, int x) {
+    const bool neg = (long long)hi < 0;
+    if (neg) {
+        lo = ~lo + 1ull;
+        hi = ~hi + (lo == 0ull ? 1ull : 0ull);
+    }
+    if ((hi | lo) == 0ull) return 0.0;
+    int lz;
+    unsigned long long t, sticky;
+    if (hi) {
+        lz = __clzll((long long)hi);
+        t = lz ? (hi << lz) | (lo >> (64 - lz)) : hi;
+        sticky = lo << lz;
+    } else {
+        const int l2 = __clzll((long long)lo);
+        lz = 64 + l2;
+        t = lo << l2;
+        sticky = 0ull;
+    }
+    // |W| = (t + sticky 2^-64) 2^(64 - lz); mantissa bits 63..11 of t, bit 10 the rounding bit
+    unsigned long long mant = t >> 11;
+    if ((t & 0x400ull) && ((t & 0x3ffull) || sticky || (mant & 1ull))) ++mant;
+    // |W| 2^x ~= mant 2^(75 - lz + x), leading bit 2^(127 - lz + x)
+    const int be = 127 - lz + x + 1023;
+    if (be >= 1 && be + int(mant >> 53) <= 2046) {
+        const unsigned long long bits = ((unsigned long long)(be - 1) << 52) + mant;
+        return __longlong_as_double((long long)(bits | (neg ? (1ull << 63) : 0ull)));
+    }
+    const double v = ldexp(double(mant), 75 - lz + x);
+    return neg ? -v : v;
+}
+
 // C = alpha * 2^(e_i + f_j) * sum_L 2^(-14-8L) * sum_seg T[seg][L] + beta * C   (exact mode)
 // C = alpha * sum_seg P[seg] + beta * C                                         (float modes)
 // Exact mode forms W = sum_L T_L * 2^(8(S-1-L)) exactly in 128-bit integers, so the only roundings
@@ -935,78 +992,90 @@ __global__ void combine_kernel(const int32_t* __restrict__ levels, int nseg, int
     const int64_t off = i * npad + j0;
     double v[COMBINE_COLS];
     if (mode == kCrt) {
-        const int N = info->slices;
+        const int nsup = info->nsup;
         const int ei = eA[i];
         const uint16_t* res16 = reinterpret_cast<const uint16_t*>(levels);
-        // all residues of the four outputs first (independent loads in flight), then the CRT sum
-        uint2 rq[MAX_MODULI];
+        // residues of the four outputs in super-modulus order (all loads in flight before the sums)
+        uint2 rq[16];
 #pragma unroll
-        for (int t = 0; t < MAX_MODULI; ++t) {
-            if (t < N) {
-                rq[t] = *reinterpret_cast<const uint2*>(res16 + int64_t(t) * plane + off);
-                for (int g = 1; g < nseg; ++g) {
-                    // segment residues add up (each < p, sums stay far below 2^16 * nseg)
-                    const uint2 q = *reinterpret_cast<const uint2*>(res16 + (int64_t(g) * max_levels + t) * plane + off);
-                    rq[t].x += q.x;  // lanes hold two 16-bit residues: no carry crosses for nseg < 256
-                    rq[t].y += q.y;
+        for (int s = 0; s < 8; ++s) {
+            if (s < nsup) {
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const int t = h ? info->sup[s].ib : info->sup[s].ia;
+                    uint2 a = *reinterpret_cast<const uint2*>(res16 + int64_t(t) * plane + off);
+                    for (int g = 1; g < nseg; ++g) {
+                        // segment residues add up: each < p, lanes hold two 16-bit residues and
+                        // no carry crosses for nseg < 256
+                        const uint2 b = *reinterpret_cast<const uint2*>(res16 + (int64_t(g) * max_levels + t) * plane + off);
+                        a.x += b.x;
+                        a.y += b.y;
+                    }
+                    rq[2 * s + h] = a;
                 }
             }
         }
-        // residue of modulus t for column cc, in [0, p) (segment residues were summed: reduce again)
-        auto res = [&](int t, int cc) -> uint32_t {
-            const uint32_t v = (cc & 1) ? ((cc < 2 ? rq[t].x : rq[t].y) >> 16) : ((cc < 2 ? rq[t].x : rq[t].y) & 0xffffu);
-            return nseg > 1 ? mod_small(v, c_mod[t], c_mod_inv32[t]) : v;
-        };
-        // level 1: pairs (p, q) -> x in [0, pq) with x = c_p + p * ((c_q - c_p) p^-1 mod q)
-        // level 2: sum_s ((x_s * y_s) mod P_s) * (P / P_s), reduced modulo P below
-        unsigned long long lo[COMBINE_COLS] = {0, 0, 0, 0}, hi[COMBINE_COLS] = {0, 0, 0, 0};
-#pragma unroll
-        for (int s2 = 0; s2 < (MAX_MODULI + 1) / 2; ++s2) {
-            if (s2 >= info->nsup) break;
-            const uint32_t pp = info->sp[s2], qq = info->sq[s2], pinv = info->sinv[s2], Ps = info->Ps[s2];
-            const uint32_t ys = info->ys[s2];
-            const unsigned long long binv = info->Pinv64[s2], Mlo = info->Ms[s2][0], Mhi = info->Ms[s2][1];
-            const int tq = 2 * s2 + 1;
-#pragma unroll
-            for (int cc = 0; cc < COMBINE_COLS; ++cc) {
-                uint32_t x = res(2 * s2, cc);
-                if (qq > 1) {
-                    const uint32_t cq = res(tq < MAX_MODULI ? tq : 0, cc);
-                    const uint32_t tdiff = cq + 2 * qq - x;  // positive, < 3 * 257
-                    const uint32_t t = mod_small(tdiff * pinv, qq, c_mod_inv32[tq < MAX_MODULI ? tq : 0]);
-                    x += pp * t;
-                }
-                // u = (x * y_s) mod P_s with a 64-bit Barrett step
-                const unsigned long long prod = (unsigned long long)x * ys;
-                const unsigned long long qe = __umul64hi(prod, binv);
-                unsigned long long u = prod - qe * Ps;
-                if (u >= Ps) u -= Ps;
-                const uint32_t uu = uint32_t(u);
-                const unsigned long long pl = Mlo * uu, ph = __umul64hi(Mlo, uu) + Mhi * uu;
-                lo[cc] += pl;
-                hi[cc] += ph + (lo[cc] < pl ? 1ull : 0ull);
-            }
-        }
-        unsigned __int128 acc[COMBINE_COLS];
-#pragma unroll
-        for (int cc = 0; cc < COMBINE_COLS; ++cc) acc[cc] = ((unsigned __int128)hi[cc] << 64) | lo[cc];
-        const unsigned __int128 P = ((unsigned __int128)info->P[1] << 64) | info->P[0];
+        // W = sum_s u_s (P / P_s) in four signed 64-bit column sums of 32-bit limb products (each
+        // below 2^48, at most 8 of them), and W / P = sum_s u_s / P_s estimated in FP32
+        long long acc[COMBINE_COLS][4];
+        float fq[COMBINE_COLS];
 #pragma unroll
         for (int cc = 0; cc < COMBINE_COLS; ++cc) {
-            // acc < N*P < 16P: subtract 8P, 4P, 2P, P where they fit
+            fq[cc] = -info->fbias;
 #pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const unsigned __int128 m = ((unsigned __int128)info->Pm[q][1] << 64) | info->Pm[q][0];
-                if (acc[cc] >= m) acc[cc] -= m;
+            for (int l = 0; l < 4; ++l) acc[cc][l] = 0;
+        }
+#pragma unroll
+        for (int s = 0; s < 8; ++s) {
+            if (s >= nsup) break;
+            const uint4* rec = reinterpret_cast<const uint4*>(&info->sup[s]);
+            const uint4 r0 = rec[0], r1 = rec[1], r2 = rec[2], r3 = rec[3];
+            const uint32_t pp = r0.x, qq = r0.y, pinv = r0.z, pinv32 = r0.w;
+            const uint32_t qinv32 = r1.x, Ps = r1.y, ys = r1.z, Psinv32 = r1.w;
+            const float finv = __uint_as_float(r3.x);
+#pragma unroll
+            for (int cc = 0; cc < COMBINE_COLS; ++cc) {
+                const uint2 wa = rq[2 * s], wb = rq[2 * s + 1];
+                const uint32_t ha = cc < 2 ? wa.x : wa.y, hb = cc < 2 ? wb.x : wb.y;
+                uint32_t x = (cc & 1) ? (ha >> 16) : (ha & 0xffffu);
+                if (nseg > 1) x = mod_small(x, pp, pinv32);
+                if (qq > 1) {
+                    // Garner: x + p * (((c_q - x) p^-1) mod q) in [0, p q)
+                    uint32_t cq = (cc & 1) ? (hb >> 16) : (hb & 0xffffu);
+                    if (nseg > 1) cq = mod_small(cq, qq, qinv32);
+                    const uint32_t d = (cq + 2 * qq - x) * pinv;  // < 3 * 257 * 257
+                    x += pp * mod_small(d, qq, qinv32);
+                }
+                // u = (x y_s) mod P_s; x, y_s < P_s < 2^16 keep the product in 32 bits
+                const uint32_t prod = x * ys;
+                uint32_t u = prod - __umulhi(prod, Psinv32) * Ps;
+                u = min(u, u - Ps);
+                fq[cc] = fmaf(__uint_as_float(0x4B000000u | u), finv, fq[cc]);
+                acc[cc][0] += (unsigned long long)u * r2.x;
+                acc[cc][1] += (unsigned long long)u * r2.y;
+                acc[cc][2] += (unsigned long long)u * r2.z;
+                acc[cc][3] += (unsigned long long)u * r2.w;
             }
+        }
+        const uint32_t P0 = info->P32[0], P1 = info->P32[1], P2 = info->P32[2], P3 = info->P32[3];
+#pragma unroll
+        for (int cc = 0; cc < COMBINE_COLS; ++cc) {
+            // W - round(W / P) P is the symmetric residue, the exact product of the scaled integers
+            // (|value| <= P / 4, so the FP32 estimate, off by far less than 1/4, rounds to the right
+            // multiple)
+            const uint32_t qm = __float_as_uint(fq[cc] + MAGIC) - MAGIC_BITS;
+            long long a0 = acc[cc][0] - (long long)((unsigned long long)qm * P0);
+            long long a1 = acc[cc][1] - (long long)((unsigned long long)qm * P1) + (a0 >> 32);
+            long long a2 = acc[cc][2] - (long long)((unsigned long long)qm * P2) + (a1 >> 32);
+            long long a3 = acc[cc][3] - (long long)((unsigned long long)qm * P3) + (a2 >> 32);
             const int64_t j = j0 + cc;
             const int fj = (j < n) ? eB[j] : 0;
             if (ei == kNonFinite || fj == kNonFinite) {
                 v[cc] = __longlong_as_double(0x7ff8000000000000ll);
             } else {
-                // symmetric residue: the exact product of the scaled integers
-                const __int128 W = (acc[cc] > P / 2) ? (__int128)acc[cc] - (__int128)P : (__int128)acc[cc];
-                v[cc] = int128_to_double_scaled(W, ei + fj - 2 * info->beta);
+                const unsigned long long hi = ((unsigned long long)uint32_t(a3) << 32) | uint32_t(a2);
+                const unsigned long long lo = ((unsigned long long)uint32_t(a1) << 32) | uint32_t(a0);
+                v[cc] = i128_to_double_scaled(hi, lo, ei + fj - 2 * info->beta);
             }
         }
     } else if (mode == kExact) {
