@@ -60,6 +60,7 @@
 #include "runtime.h"
 #include "profile.h"
 #include "split_api.h"
+#include "crt_tables.h"
 
 namespace gb {
 namespace {
@@ -101,19 +102,6 @@ constexpr double kModLog2[MAX_MODULI] = {8.00562, 8.0, 7.99435, 7.98299, 7.97154
 __constant__ uint32_t c_mod_2p20[MAX_MODULI] = {16, 0, 16, 144, 149, 61, 226, 83, 76, 214, 63, 30, 32, 117, 45};
 __constant__ uint32_t c_mod_2p40[MAX_MODULI] = {256, 0, 1, 243, 113, 16, 225, 197, 184, 225, 110, 8, 156, 185, 35};
 
-// CRT reconstruction in two levels.  The N moduli are paired largest with smallest into "super"
-// moduli P_s = p q < 2^16 (a modulus left over, or both of N = 2, stays single with q = 1); a pair's
-// residue follows from one Garner step, and the super residues combine as
-// W = sum_s ((x_s y_s) mod P_s) (P / P_s) with 32-bit limbs.  One record is 64 bytes (four 16-byte
-// loads in the combine kernel).
-struct __align__(16) SuperMod {
-    uint32_t p, q, pinv, pinv32;      // p, q, p^-1 mod q, floor(2^32 / p)
-    uint32_t qinv32, Ps, ys, Psinv32; // floor(2^32 / q), P_s, (P / P_s)^-1 mod P_s, floor(2^32 / P_s)
-    uint32_t M[4];                    // P / P_s, 32-bit limbs (least significant first)
-    float finv;                       // 1 / P_s (FP32)
-    int ia, ib, pad;                  // residue planes of p and q
-};
-
 // Device-side result of the pre-pass: the slice count and the bound it guarantees.
 struct SplitInfo {
     int slices;           // S (digit mode); residue products N (CRT mode); planes per operand otherwise
@@ -123,11 +111,6 @@ struct SplitInfo {
     double scaleA, scaleB;// ||2^e||_2, ||2^f||_2
     // CRT mode
     int beta;             // operands are rounded to beta-bit integers per row / column
-    int nsup;             // super moduli
-    uint32_t P32[4];      // product of the N moduli, 32-bit limbs
-    float fbias;          // sum_s fl(2^23 / P_s): offset of the FP32 quotient estimate
-    int pad[3];
-    SuperMod sup[8];
 };
 
 // ---- pre-pass ------------------------------------------------------------------------------
@@ -288,7 +271,7 @@ __device__ __forceinline__ double pow2i(int x) {
     return x < -1022 ? 0.0 : __longlong_as_double((long long)(x + 1023) << 52);
 }
 
-__global__ void split_info_kernel(const int* __restrict__ eA, const double* __restrict__ qA, int64_t m,
+__global__ void __launch_bounds__(1024) split_info_kernel(const int* __restrict__ eA, const double* __restrict__ qA, int64_t m,
                                   const int* __restrict__ eB, const double* __restrict__ qB, int64_t n, int64_t k,
                                   int mode, int fixed_slices, int cap_planes, double target, SplitInfo* info) {
     __shared__ double redd[32];
@@ -345,9 +328,11 @@ __global__ void split_info_kernel(const int* __restrict__ eA, const double* __re
             // moduli: product above 2 * k * 2^(2 beta) with one bit to spare
             const int kbits = 64 - __clzll((long long)(k > 1 ? k - 1 : 1));
             double need = 2.0 + kbits + 2.0 * beta, have = 0.0;
+            // a fixed count is used as given (at least two); otherwise the fewest that carry the
+            // target, within the planes the host sized for
             int N = 0;
-            const int nmax = fixed_slices > 0 ? fixed_slices : cap_planes;
-            while (N < nmax && have < need) {
+            const int nfix = fixed_slices > 0 ? (fixed_slices < 2 ? 2 : fixed_slices) : 0;
+            while (nfix ? N < nfix : (N < 2 || (N < cap_planes && have < need))) {
                 have += log2(double(c_mod[N]));
                 ++N;
             }
@@ -357,66 +342,6 @@ __global__ void split_info_kernel(const int* __restrict__ eA, const double* __re
             r.slices = N;
             r.beta = beta;
             r.bound = bnd(beta);
-            // CRT constants
-            unsigned __int128 P = 1;
-            for (int t = 0; t < N; ++t) P *= c_mod[t];
-            for (int l = 0; l < 4; ++l) r.P32[l] = uint32_t(P >> (32 * l));
-            auto inv_mod = [](long long a, long long m) {
-                long long b = m, x0 = 1, x1 = 0;
-                a %= m;
-                while (b) {
-                    const long long q = a / b, ta = a - q * b, tx = x0 - q * x1;
-                    a = b; b = ta; x0 = x1; x1 = tx;
-                }
-                return (long long)(((x0 % m) + m) % m);
-            };
-            // pairs (t, N-1-t): every product stays below 2^16 for N >= 3
-            int ns = 0;
-            if (N == 2) {
-                r.sup[0].ia = 0; r.sup[0].ib = -1;
-                r.sup[1].ia = 1; r.sup[1].ib = -1;
-                ns = 2;
-            } else {
-                for (int t = 0; t < N / 2; ++t) {
-                    r.sup[ns].ia = t;
-                    r.sup[ns].ib = N - 1 - t;
-                    ++ns;
-                }
-                if (N & 1) {
-                    r.sup[ns].ia = N / 2;
-                    r.sup[ns].ib = -1;
-                    ++ns;
-                }
-            }
-            r.nsup = ns;
-            float fb = 0.f;
-            for (int s = 0; s < ns; ++s) {
-                SuperMod& sm = r.sup[s];
-                sm.p = c_mod[sm.ia];
-                sm.q = sm.ib >= 0 ? c_mod[sm.ib] : 1u;
-                sm.pinv = sm.q > 1 ? uint32_t(inv_mod(sm.p, sm.q)) : 0u;
-                sm.pinv32 = uint32_t(0x100000000ull / sm.p);
-                sm.qinv32 = sm.q > 1 ? uint32_t(0x100000000ull / sm.q) : 0u;
-                sm.Ps = sm.p * sm.q;
-                sm.Psinv32 = uint32_t(0x100000000ull / sm.Ps);
-                sm.finv = 1.0f / float(sm.Ps);
-                sm.pad = 0;
-                if (sm.ib < 0) sm.ib = sm.ia;  // never read as a residue of a second modulus
-                fb += 8388608.0f * sm.finv;
-            }
-            r.fbias = fb;
-            for (int s = 0; s < ns; ++s) {
-                SuperMod& sm = r.sup[s];
-                unsigned __int128 Ms = 1;
-                unsigned long long mres = 1;
-                for (int u = 0; u < ns; ++u) {
-                    if (u == s) continue;
-                    Ms *= r.sup[u].Ps;
-                    mres = (mres * (r.sup[u].Ps % sm.Ps)) % sm.Ps;
-                }
-                for (int l = 0; l < 4; ++l) sm.M[l] = uint32_t(Ms >> (32 * l));
-                sm.ys = uint32_t(inv_mod((long long)mres, (long long)sm.Ps));
-            }
         } else if (mode == kExact) {
             int S = fixed_slices;
             if (S <= 0) {
@@ -981,6 +906,92 @@ __device__ __forceinline__ double i128_to_double_scaled(unsigned long long hi, u
 // Grid: x over groups of 4 consecutive columns (one 16-byte load per level plane), y over rows.
 constexpr int COMBINE_COLS = 4;
 
+// Residue (CRT) reconstruction of four consecutive outputs of one row for N moduli, all constants
+// compile-time (crt_tables.h).  u_s = (c_p A_s + c_q B_s) mod P_s per super modulus (< 2^26 before
+// the reduction), W = sum_s u_s (P / P_s) in signed 64-bit sums of 32-bit limb products (each below
+// 2^48, at most 8 per limb), and the symmetric residue W - round(W / P) P with the quotient from an
+// FP32 estimate of sum_s u_s / P_s: the product of the scaled integers has |value| <= P / 4, so an
+// estimate off by far less than 1/4 picks the right multiple of P.
+template <int N>
+__device__ __forceinline__ void crt_cols(const uint16_t* __restrict__ res16, int64_t plane, int64_t off, int nseg,
+                                         int max_levels, int scale, int ei, const int (&fj)[COMBINE_COLS],
+                                         double (&v)[COMBINE_COLS]) {
+    constexpr CrtTable T = kCrtTables[N - 2];
+    constexpr int NS = T.nsup, LB = T.limbs;
+    uint2 rq[2 * NS];
+#pragma unroll
+    for (int s = 0; s < NS; ++s) {
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int t = h ? T.sup[s].ib : T.sup[s].ia;
+            if (t < 0) continue;
+            uint2 a = *reinterpret_cast<const uint2*>(res16 + int64_t(t) * plane + off);
+            for (int g = 1; g < nseg; ++g) {
+                // segment residues add up: each < p, lanes hold two 16-bit residues and no carry
+                // crosses for nseg < 256
+                const uint2 b = *reinterpret_cast<const uint2*>(res16 + (int64_t(g) * max_levels + t) * plane + off);
+                a.x += b.x;
+                a.y += b.y;
+            }
+            rq[2 * s + h] = a;
+        }
+    }
+    long long acc[COMBINE_COLS][4];
+    float fq[COMBINE_COLS];
+#pragma unroll
+    for (int cc = 0; cc < COMBINE_COLS; ++cc) {
+        fq[cc] = -T.fbias;
+#pragma unroll
+        for (int l = 0; l < 4; ++l) acc[cc][l] = 0;
+    }
+#pragma unroll
+    for (int s = 0; s < NS; ++s) {
+        constexpr uint32_t one = 1u;
+        const CrtSuper& S = T.sup[s];
+#pragma unroll
+        for (int cc = 0; cc < COMBINE_COLS; ++cc) {
+            const uint32_t ha = cc < 2 ? rq[2 * s].x : rq[2 * s].y;
+            uint32_t cp = (cc & 1) ? (ha >> 16) : (ha & 0xffffu);
+            if (nseg > 1) cp = mod_small(cp, S.p, S.pinv32);
+            uint32_t x = cp * S.A;
+            if (S.q > one) {
+                const uint32_t hb = cc < 2 ? rq[2 * s + 1].x : rq[2 * s + 1].y;
+                uint32_t cq = (cc & 1) ? (hb >> 16) : (hb & 0xffffu);
+                if (nseg > 1) cq = mod_small(cq, S.q, S.qinv32);
+                x += cq * S.B;
+            }
+            uint32_t u = x - __umulhi(x, S.Psinv32) * S.Ps;
+            u = min(u, u - S.Ps);
+            fq[cc] = fmaf(__uint_as_float(0x4B000000u | u), S.finv, fq[cc]);
+#pragma unroll
+            for (int l = 0; l < LB; ++l)
+                if (S.M[l]) acc[cc][l] += (unsigned long long)u * S.M[l];
+        }
+    }
+#pragma unroll
+    for (int cc = 0; cc < COMBINE_COLS; ++cc) {
+        const uint32_t qm = __float_as_uint(fq[cc] + MAGIC) - MAGIC_BITS;
+        long long a[4];
+#pragma unroll
+        for (int l = 0; l < LB; ++l) {
+            a[l] = acc[cc][l] - (long long)((unsigned long long)qm * T.P[l]);
+            if (l > 0) a[l] += a[l - 1] >> 32;
+        }
+        unsigned long long hi, lo;
+        if (LB == 1) {
+            lo = (unsigned long long)a[0];
+            hi = (unsigned long long)(a[0] >> 63);
+        } else {
+            lo = ((unsigned long long)a[1] << 32) | uint32_t(a[0]);
+            if (LB == 2) hi = (unsigned long long)(a[1] >> 32);
+            else if (LB == 3) hi = (unsigned long long)a[2];
+            else hi = ((unsigned long long)a[LB - 1] << 32) | uint32_t(a[LB - 2]);
+        }
+        if (ei == kNonFinite || fj[cc] == kNonFinite) v[cc] = __longlong_as_double(0x7ff8000000000000ll);
+        else v[cc] = i128_to_double_scaled(hi, lo, ei + fj[cc] - scale);
+    }
+}
+
 __global__ void combine_kernel(const int32_t* __restrict__ levels, int nseg, int max_levels, int64_t mpad,
                                int64_t npad, int mode, const SplitInfo* __restrict__ info,
                                const int* __restrict__ eA, const int* __restrict__ eB, int64_t m, int64_t n,
@@ -992,91 +1003,22 @@ __global__ void combine_kernel(const int32_t* __restrict__ levels, int nseg, int
     const int64_t off = i * npad + j0;
     double v[COMBINE_COLS];
     if (mode == kCrt) {
-        const int nsup = info->nsup;
         const int ei = eA[i];
+        int fj[COMBINE_COLS];
+#pragma unroll
+        for (int cc = 0; cc < COMBINE_COLS; ++cc) fj[cc] = (j0 + cc < n) ? eB[j0 + cc] : 0;
         const uint16_t* res16 = reinterpret_cast<const uint16_t*>(levels);
-        // residues of the four outputs in super-modulus order (all loads in flight before the sums)
-        uint2 rq[16];
+        const int scale = 2 * info->beta;
+        switch (info->slices) {
+#define GB_CRT_CASE(NN) \
+    case NN: crt_cols<NN>(res16, plane, off, nseg, max_levels, scale, ei, fj, v); break;
+            GB_CRT_CASE(2) GB_CRT_CASE(3) GB_CRT_CASE(4) GB_CRT_CASE(5) GB_CRT_CASE(6) GB_CRT_CASE(7)
+            GB_CRT_CASE(8) GB_CRT_CASE(9) GB_CRT_CASE(10) GB_CRT_CASE(11) GB_CRT_CASE(12) GB_CRT_CASE(13)
+            GB_CRT_CASE(14) GB_CRT_CASE(15)
+#undef GB_CRT_CASE
+            default:
 #pragma unroll
-        for (int s = 0; s < 8; ++s) {
-            if (s < nsup) {
-#pragma unroll
-                for (int h = 0; h < 2; ++h) {
-                    const int t = h ? info->sup[s].ib : info->sup[s].ia;
-                    uint2 a = *reinterpret_cast<const uint2*>(res16 + int64_t(t) * plane + off);
-                    for (int g = 1; g < nseg; ++g) {
-                        // segment residues add up: each < p, lanes hold two 16-bit residues and
-                        // no carry crosses for nseg < 256
-                        const uint2 b = *reinterpret_cast<const uint2*>(res16 + (int64_t(g) * max_levels + t) * plane + off);
-                        a.x += b.x;
-                        a.y += b.y;
-                    }
-                    rq[2 * s + h] = a;
-                }
-            }
-        }
-        // W = sum_s u_s (P / P_s) in four signed 64-bit column sums of 32-bit limb products (each
-        // below 2^48, at most 8 of them), and W / P = sum_s u_s / P_s estimated in FP32
-        long long acc[COMBINE_COLS][4];
-        float fq[COMBINE_COLS];
-#pragma unroll
-        for (int cc = 0; cc < COMBINE_COLS; ++cc) {
-            fq[cc] = -info->fbias;
-#pragma unroll
-            for (int l = 0; l < 4; ++l) acc[cc][l] = 0;
-        }
-#pragma unroll
-        for (int s = 0; s < 8; ++s) {
-            if (s >= nsup) break;
-            const uint4* rec = reinterpret_cast<const uint4*>(&info->sup[s]);
-            const uint4 r0 = rec[0], r1 = rec[1], r2 = rec[2], r3 = rec[3];
-            const uint32_t pp = r0.x, qq = r0.y, pinv = r0.z, pinv32 = r0.w;
-            const uint32_t qinv32 = r1.x, Ps = r1.y, ys = r1.z, Psinv32 = r1.w;
-            const float finv = __uint_as_float(r3.x);
-#pragma unroll
-            for (int cc = 0; cc < COMBINE_COLS; ++cc) {
-                const uint2 wa = rq[2 * s], wb = rq[2 * s + 1];
-                const uint32_t ha = cc < 2 ? wa.x : wa.y, hb = cc < 2 ? wb.x : wb.y;
-                uint32_t x = (cc & 1) ? (ha >> 16) : (ha & 0xffffu);
-                if (nseg > 1) x = mod_small(x, pp, pinv32);
-                if (qq > 1) {
-                    // Garner: x + p * (((c_q - x) p^-1) mod q) in [0, p q)
-                    uint32_t cq = (cc & 1) ? (hb >> 16) : (hb & 0xffffu);
-                    if (nseg > 1) cq = mod_small(cq, qq, qinv32);
-                    const uint32_t d = (cq + 2 * qq - x) * pinv;  // < 3 * 257 * 257
-                    x += pp * mod_small(d, qq, qinv32);
-                }
-                // u = (x y_s) mod P_s; x, y_s < P_s < 2^16 keep the product in 32 bits
-                const uint32_t prod = x * ys;
-                uint32_t u = prod - __umulhi(prod, Psinv32) * Ps;
-                u = min(u, u - Ps);
-                fq[cc] = fmaf(__uint_as_float(0x4B000000u | u), finv, fq[cc]);
-                acc[cc][0] += (unsigned long long)u * r2.x;
-                acc[cc][1] += (unsigned long long)u * r2.y;
-                acc[cc][2] += (unsigned long long)u * r2.z;
-                acc[cc][3] += (unsigned long long)u * r2.w;
-            }
-        }
-        const uint32_t P0 = info->P32[0], P1 = info->P32[1], P2 = info->P32[2], P3 = info->P32[3];
-#pragma unroll
-        for (int cc = 0; cc < COMBINE_COLS; ++cc) {
-            // W - round(W / P) P is the symmetric residue, the exact product of the scaled integers
-            // (|value| <= P / 4, so the FP32 estimate, off by far less than 1/4, rounds to the right
-            // multiple)
-            const uint32_t qm = __float_as_uint(fq[cc] + MAGIC) - MAGIC_BITS;
-            long long a0 = acc[cc][0] - (long long)((unsigned long long)qm * P0);
-            long long a1 = acc[cc][1] - (long long)((unsigned long long)qm * P1) + (a0 >> 32);
-            long long a2 = acc[cc][2] - (long long)((unsigned long long)qm * P2) + (a1 >> 32);
-            long long a3 = acc[cc][3] - (long long)((unsigned long long)qm * P3) + (a2 >> 32);
-            const int64_t j = j0 + cc;
-            const int fj = (j < n) ? eB[j] : 0;
-            if (ei == kNonFinite || fj == kNonFinite) {
-                v[cc] = __longlong_as_double(0x7ff8000000000000ll);
-            } else {
-                const unsigned long long hi = ((unsigned long long)uint32_t(a3) << 32) | uint32_t(a2);
-                const unsigned long long lo = ((unsigned long long)uint32_t(a1) << 32) | uint32_t(a0);
-                v[cc] = i128_to_double_scaled(hi, lo, ei + fj - 2 * info->beta);
-            }
+                for (int cc = 0; cc < COMBINE_COLS; ++cc) v[cc] = __longlong_as_double(0x7ff8000000000000ll);
         }
     } else if (mode == kExact) {
         const int S = info->slices;
@@ -1211,8 +1153,9 @@ SplitGeometry split_geometry(const Gemm& g, const SplitRequest& req, int num_sms
     G.kpad = round_up(g.k, TK);
     G.kb_total = int(G.kpad / TK);
     if (G.mode == kCrt)
-        G.max_planes = req.slices > 0 ? std::min(req.slices, MAX_MODULI)
-                                      : std::min(MAX_MODULI, crt_worst_case_moduli(g.k, req.target_error));
+        // at least two moduli (the reconstruction tables start at N = 2)
+        G.max_planes = req.slices > 0 ? std::max(2, std::min(req.slices, MAX_MODULI))
+                                      : std::max(2, std::min(MAX_MODULI, crt_worst_case_moduli(g.k, req.target_error)));
     else
         G.max_planes = (G.mode == kExact) ? (req.slices > 0 ? std::min(req.slices, MAX_SLICES) : MAX_SLICES)
                                           : (G.mode == kBf16 ? 1 : 2);
@@ -1385,7 +1328,7 @@ int device_product(const Gemm& g_in, const SplitRequest& req, const LaunchCtl& c
         stats_finalize_pair_kernel<<<xb0 + unsigned((n + 255) / 256), 256, 0, st>>>(op, k, xb0);
     }
     const double target = req.target_error > 0 ? req.target_error : double(k) * 0x1p-53;
-    split_info_kernel<<<1, 256, 0, st>>>(eA, sqA, m, eB, sqB, n, k, mode, req.slices > 0 ? max_planes : 0,
+    split_info_kernel<<<1, 1024, 0, st>>>(eA, sqA, m, eB, sqB, n, k, mode, req.slices > 0 ? max_planes : 0,
                                          max_planes, target, info);
     if (cudaError_t le = cudaGetLastError(); le != cudaSuccess) {
         if (err) *err = std::string("split pre-pass launch: ") + cudaGetErrorString(le);

@@ -177,3 +177,34 @@ def test_crt_with_a_moduli_cap_reports_its_weaker_bound():
     err, o, _, _ = product(O.ROW_MAJOR, O.NO_TRANS, O.NO_TRANS, m, n, k, method="split_crt", slices=8, seed=41)
     assert o.slices_used == 8
     assert err <= o.error_bound
+
+
+@pytest.mark.parametrize("slices", [1, 2, 3, 4, 5, 7, 8, 11, 12, 13, 15])
+def test_crt_every_modulus_count_is_exact_on_small_integers(slices):
+    """Each modulus count has its own reconstruction table (1 to 4 result limbs, singles and
+    pairs): with entries in [-3, 3] every count carries the scaled product exactly (one modulus
+    is raised to two)."""
+    m, n, k = 130, 260, 64
+    A = O.integers(m * k, 51 + slices, -3, 3)
+    B = O.integers(k * n, 52 + slices, -3, 3)
+    C = np.zeros(m * n)
+    o = G.dgemm_ex(O.ROW_MAJOR, O.NO_TRANS, O.NO_TRANS, m, n, k, 1.0, A, k, B, n, 0.0, C, n,
+                   G.opts(method="split_crt", slices=slices))
+    assert o.method_used == G.METHOD_SPLIT_CRT
+    assert o.slices_used == max(2, slices)
+    exact = A.astype(np.int64).reshape(m, k) @ B.astype(np.int64).reshape(k, n)
+    assert np.array_equal(C.reshape(m, n), exact.astype(np.float64))
+
+
+def test_crt_segmented_k_residues_are_summed_and_reduced():
+    """Few output tiles make the product split k into segments whose residues the combine kernel
+    adds and reduces again; integer inputs must still come back exact."""
+    m, n, k = 100, 120, 9000
+    A = O.integers(m * k, 61, -500, 500)
+    B = O.integers(k * n, 62, -500, 500)
+    C = np.zeros(m * n)
+    o = G.dgemm_ex(O.ROW_MAJOR, O.NO_TRANS, O.NO_TRANS, m, n, k, 1.0, A, k, B, n, 0.0, C, n,
+                   G.opts(method="split_crt"))
+    assert o.method_used == G.METHOD_SPLIT_CRT
+    exact = A.astype(np.int64).reshape(m, k) @ B.astype(np.int64).reshape(k, n)
+    assert np.array_equal(C.reshape(m, n), exact.astype(np.float64))
