@@ -97,10 +97,23 @@ __constant__ uint32_t c_mod_inv32[MAX_MODULI] = {
 constexpr double kModLog2[MAX_MODULI] = {8.00562, 8.0, 7.99435, 7.98299, 7.97154, 7.94837, 7.91289, 7.90087,
                                          7.86419, 7.83920, 7.82655, 7.80090, 7.76155, 7.72110, 7.63662};
 
-// 2^20 mod p and 2^40 mod p: the slice kernel reduces a 56-bit integer U = u2 2^40 + u1 2^20 + u0
-// as u2 (2^40 mod p) + u1 (2^20 mod p) + u0 < 2^29 with one 32-bit reduction.
-__constant__ uint32_t c_mod_2p20[MAX_MODULI] = {16, 0, 16, 144, 149, 61, 226, 83, 76, 214, 63, 30, 32, 117, 45};
-__constant__ uint32_t c_mod_2p40[MAX_MODULI] = {256, 0, 1, 243, 113, 16, 225, 197, 184, 225, 110, 8, 156, 185, 35};
+// Residues on the FP32 pipe: a 56-bit integer U = sum_i w_i 2^(14 i) (14-bit chunks, i = 0..3) is
+// congruent to x = w_0 + sum_{i>0} w_i K_i with K_i = 2^(14 i) mod p in the symmetric range
+// (|K_i| <= 128), so |x| <= 16383 * 385 < 2^23 and every partial sum is an exact FP32 integer.
+// q = rint(x fl(1/p)) is the nearest integer to x / p: the relative error 2^-24 of fl(1/p) moves
+// x / p by less than 2^23 / p * 2^-24 = 0.5 / p, the smallest distance of x / p from a half
+// integer for odd p (p = 256 is exact), so r = x - p q lies in [-p/2, p/2] and |r| <= 128.
+__constant__ float c_modf[MAX_MODULI] = {257.f, 256.f, 255.f, 253.f, 251.f, 247.f, 241.f, 239.f,
+                                         233.f, 229.f, 227.f, 223.f, 217.f, 211.f, 199.f};
+__constant__ float c_modf_inv[MAX_MODULI] = {
+    0x1.fe01fe0000000p-9f, 0x1.0000000000000p-8f, 0x1.0101020000000p-8f, 0x1.03091c0000000p-8f,
+    0x1.0519800000000p-8f, 0x1.0953f40000000p-8f, 0x1.0fef020000000p-8f, 0x1.12358e0000000p-8f,
+    0x1.1945380000000p-8f, 0x1.1e2ef40000000p-8f, 0x1.20b4700000000p-8f, 0x1.25e2280000000p-8f,
+    0x1.2e025c0000000p-8f, 0x1.3698e00000000p-8f, 0x1.49539e0000000p-8f};
+__constant__ float c_mod_k14[3][MAX_MODULI] = {
+    {-64.f, 0.f, 64.f, -61.f, 69.f, 82.f, -4.f, -107.f, 74.f, -104.f, 40.f, 105.f, -108.f, -74.f, 66.f},
+    {-16.f, 0.f, 16.f, -74.f, -8.f, 55.f, 16.f, -23.f, -116.f, 53.f, 11.f, 98.f, -54.f, -10.f, -22.f},
+    {-4.f, 0.f, 4.f, -40.f, -50.f, 64.f, -64.f, 71.f, 37.f, -16.f, -14.f, 32.f, -27.f, -104.f, -59.f}};
 
 // Device-side result of the pre-pass: the slice count and the bound it guarantees.
 struct SplitInfo {
@@ -255,6 +268,16 @@ __device__ double block_sum(double v, double* red) {
     return t;
 }
 
+__device__ long long block_max_ll(long long v, long long* red) {
+    for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    long long t = red[0];
+    for (int i = 1; i < int(blockDim.x >> 5); ++i) t = max(t, red[i]);
+    return t;
+}
+
 __device__ int block_max_int(int v, int* red) {
     for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
     __syncthreads();
@@ -288,6 +311,14 @@ __global__ void __launch_bounds__(1024) split_info_kernel(const int* __restrict_
     bad = block_max_int(bad, redi);
     EA = block_max_int(EA, redi);
     EB = block_max_int(EB, redi);
+    // largest row / column sum of squares relative to 2^(2e): bounds the norm of a scaled row
+    double QA = 0, QB = 0;
+    for (int64_t i = threadIdx.x; i < m; i += blockDim.x)
+        if (eA[i] != kNonFinite) QA = fmax(QA, qA[i]);
+    for (int64_t j = threadIdx.x; j < n; j += blockDim.x)
+        if (eB[j] != kNonFinite) QB = fmax(QB, qB[j]);
+    QA = __longlong_as_double(block_max_ll(__double_as_longlong(QA), reinterpret_cast<long long*>(redd)));
+    QB = __longlong_as_double(block_max_ll(__double_as_longlong(QB), reinterpret_cast<long long*>(redd)));
     double sa = 0, na = 0, sb = 0, nb = 0;
     for (int64_t i = threadIdx.x; i < m; i += blockDim.x) {
         if (eA[i] == kNonFinite || qA[i] <= 0.0) continue;
@@ -325,23 +356,33 @@ __global__ void __launch_bounds__(1024) split_info_kernel(const int* __restrict_
             // beta <= 55 keeps |A'| < 2^56, the range of the residue extraction
             int beta = 1;
             while (beta < 55 && bnd(beta) > target) ++beta;
-            // moduli: product above 2 * k * 2^(2 beta) with one bit to spare
-            const int kbits = 64 - __clzll((long long)(k > 1 ? k - 1 : 1));
-            double need = 2.0 + kbits + 2.0 * beta, have = 0.0;
+            // The scaled rows satisfy ||A'_i|| <= 2^beta sqrt(Q_A) + sqrt(k)/2 (the rounding adds
+            // at most 1/2 per entry), so by Cauchy-Schwarz every exact product entry T has
+            // |T| <= (2^beta sqrt(Q_A) + sqrt(k)/2)(2^beta sqrt(Q_B) + sqrt(k)/2).  The moduli's
+            // product P must exceed 2.125 |T| (symmetric residues, with room for the FP32 quotient
+            // estimate of the reconstruction); Q carries a 2^-10 allowance for its own rounding.
+            const double hk = 0.5 * sqrt(double(k)), sqa = sqrt(QA * (1.0 + 0x1p-10)), sqb = sqrt(QB * (1.0 + 0x1p-10));
+            auto need = [&](int b) {
+                const double x = ldexp(sqa, b) + hk, y = ldexp(sqb, b) + hk;
+                return 1.0875 + log2(x) + log2(y);
+            };
+            double have = 0.0;
             // a fixed count is used as given (at least two); otherwise the fewest that carry the
             // target, within the planes the host sized for
             int N = 0;
             const int nfix = fixed_slices > 0 ? (fixed_slices < 2 ? 2 : fixed_slices) : 0;
-            while (nfix ? N < nfix : (N < 2 || (N < cap_planes && have < need))) {
+            const double need0 = need(beta);
+            while (nfix ? N < nfix : (N < 2 || (N < cap_planes && have < need0))) {
                 have += log2(double(c_mod[N]));
                 ++N;
             }
             // the moduli chosen may carry more bits than needed: round to as many bits as they allow
-            beta = int(floor((have - 2.0 - kbits) / 2.0));
-            beta = beta > 55 ? 55 : beta;
+            beta = 55;
+            while (beta > -60 && need(beta) > have) --beta;
             r.slices = N;
             r.beta = beta;
-            r.bound = bnd(beta);
+            // too few moduli for even the coarsest rounding: no bound
+            r.bound = need(beta) > have ? __longlong_as_double(0x7ff0000000000000ll) : bnd(beta);
         } else if (mode == kExact) {
             int S = fixed_slices;
             if (S <= 0) {
@@ -469,36 +510,35 @@ __device__ __forceinline__ void slice_tile(const double* __restrict__ X, int64_t
         const int N = info->slices, beta = info->beta;
         const int e = (r < R) ? rexp[r] : 0;
         const bool bad = (e == kNonFinite);
-        // U = |round(a 2^(beta-e))| < 2^56 as u2 2^40 + u1 2^20 + u0; u0 carries an offset of 128 so
-        // that r = (U + 128) mod p gives the residue v = r - 128 in [-128, p - 129], |v| <= 128
-        uint32_t u0[8], u1[8], u2[8], sgn[4];
+        // U = |round(a 2^(beta-e))| < 2^56 in signed FP32 chunks (the sign of a applied to each)
+        float w0[8], w1[8], w2[8], w3[8];
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
             const unsigned long long bits = bad ? 0ull : tile[rr][pp0 + q];
             const unsigned long long U = int_magnitude(bits, beta - e);
-            u0[q] = (uint32_t(U) & 0xfffffu) + 128u;
-            u1[q] = uint32_t(U >> 20) & 0xfffffu;
-            u2[q] = uint32_t(U >> 40);
-            const uint32_t s = uint32_t(bits >> 63);
-            if (q & 1) sgn[q / 2] |= s << 31;
-            else sgn[q / 2] = s << 15;
+            const float sg = (bits >> 63) ? -1.f : 1.f, off = (bits >> 63) ? 8388608.f : -8388608.f;
+            w0[q] = fmaf(__uint_as_float(0x4B000000u | (uint32_t(U) & 0x3fffu)), sg, off);
+            w1[q] = fmaf(__uint_as_float(0x4B000000u | (uint32_t(U >> 14) & 0x3fffu)), sg, off);
+            w2[q] = fmaf(__uint_as_float(0x4B000000u | (uint32_t(U >> 28) & 0x3fffu)), sg, off);
+            w3[q] = fmaf(__uint_as_float(0x4B000000u | uint32_t(U >> 42)), sg, off);
         }
         for (int t = 0; t < N; ++t) {
-            const uint32_t pm = c_mod[t], inv = c_mod_inv32[t], c20 = c_mod_2p20[t], c40 = c_mod_2p40[t];
+            const float pf = c_modf[t], inv = c_modf_inv[t];
+            const float k1 = c_mod_k14[0][t], k2 = c_mod_k14[1][t], k3 = c_mod_k14[2][t];
             uint32_t fb[8];
 #pragma unroll
             for (int q = 0; q < 8; ++q) {
-                const uint32_t x = u2[q] * c40 + u1[q] * c20 + u0[q];  // < 2^29
-                uint32_t r = x - __umulhi(x, inv) * pm;
-                r = min(r, r - pm);
-                // float(r - 128) exactly through the 1.5 * 2^23 bias; |r - 128| <= 128 keeps it a BF16
-                fb[q] = __float_as_uint(__uint_as_float(MAGIC_BITS - 128u + r) - MAGIC);
+                const float x = fmaf(w3[q], k3, fmaf(w2[q], k2, fmaf(w1[q], k1, w0[q])));
+                const float qf = fmaf(x, inv, MAGIC) - MAGIC;
+                // exact symmetric residue, an integer of at most 8 significant bits: its FP32
+                // pattern's upper half is the BF16 pattern
+                fb[q] = __float_as_uint(fmaf(-pf, qf, x));
             }
             uint4 w;
-            w.x = __byte_perm(fb[0], fb[1], 0x7632) ^ sgn[0];
-            w.y = __byte_perm(fb[2], fb[3], 0x7632) ^ sgn[1];
-            w.z = __byte_perm(fb[4], fb[5], 0x7632) ^ sgn[2];
-            w.w = __byte_perm(fb[6], fb[7], 0x7632) ^ sgn[3];
+            w.x = __byte_perm(fb[0], fb[1], 0x7632);
+            w.y = __byte_perm(fb[2], fb[3], 0x7632);
+            w.z = __byte_perm(fb[4], fb[5], 0x7632);
+            w.w = __byte_perm(fb[6], fb[7], 0x7632);
             *reinterpret_cast<uint4*>(dst + t * pstride) = w;
         }
     } else if (mode == kExact) {
@@ -910,8 +950,9 @@ constexpr int COMBINE_COLS = 4;
 // compile-time (crt_tables.h).  u_s = (c_p A_s + c_q B_s) mod P_s per super modulus (< 2^26 before
 // the reduction), W = sum_s u_s (P / P_s) in signed 64-bit sums of 32-bit limb products (each below
 // 2^48, at most 8 per limb), and the symmetric residue W - round(W / P) P with the quotient from an
-// FP32 estimate of sum_s u_s / P_s: the product of the scaled integers has |value| <= P / 4, so an
-// estimate off by far less than 1/4 picks the right multiple of P.
+// FP32 estimate of sum_s u_s / P_s: the product of the scaled integers has |value| < P / 2.125, so
+// W / P lies at least 0.029 from a half integer and an estimate off by less than 0.01 picks the
+// right multiple of P.
 template <int N>
 __device__ __forceinline__ void crt_cols(const uint16_t* __restrict__ res16, int64_t plane, int64_t off, int nseg,
                                          int max_levels, int scale, int ei, const int (&fj)[COMBINE_COLS],
