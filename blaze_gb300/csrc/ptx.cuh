@@ -122,6 +122,16 @@ __device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map
         : "memory");
 }
 
+// Asynchronous 8-byte copy global -> shared (cp.async, L1-allocating); valid == false writes eight
+// zero bytes without reading (src must still be a mapped address).
+__device__ __forceinline__ void cp_async8(uint32_t dst, const void* src, bool valid) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(dst), "l"(src), "r"(valid ? 8 : 0)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+// Wait until at most one committed group of this thread is still in flight.
+__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+
 // Byte offset -> physical byte offset inside a 128-byte-swizzled tile (1024-byte atoms of eight
 // 128-byte rows; the 16-byte chunk index is XORed with the row index modulo 8).  The tile base
 // must be 1024-byte aligned.

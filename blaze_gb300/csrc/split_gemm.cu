@@ -145,63 +145,126 @@ struct RowAcc {
     int pad;
 };
 
-__device__ __forceinline__ void stats_tile(const double* __restrict__ X, int64_t R, int64_t K, int64_t sr, int64_t sp,
-                                           RowAcc* __restrict__ acc, int by) {
-    __shared__ unsigned long long tile[32][65];
-    const int64_t r0 = int64_t(by) * 32, p0 = int64_t(blockIdx.x) * 64;
+// Operands stream through shared memory in tiles of 32 rows x 64 k, TILE_KT tiles per block, with
+// two buffers filled by cp.async: the copies of the next tile are in flight while the current one
+// is processed.
+constexpr int TILE_KT = 8;
+
+// The eight copies of one thread per tile: element (rr0 + i drr, pp0 + i dpp) of the tile,
+// i = 0..7, coalesced along whichever index of X(r, p) = X[r*sr + p*sp] is contiguous (a warp
+// reads 256 consecutive bytes); src points at the first one in tile 0, di and dk step to copy i
+// and to the next tile of 64 k.
+struct TileSrc {
+    const unsigned long long* src;
+    int64_t di, dk;
+    int rr0, pp0, drr, dpp;
+};
+
+__device__ __forceinline__ TileSrc tile_src(const double* X, int64_t sr, int64_t sp, int64_t r0) {
     const int t = threadIdx.x;  // 256 threads
-    const unsigned long long* Xb = reinterpret_cast<const unsigned long long*>(X);
+    TileSrc s;
     if (sp == 1) {
-        for (int e = t; e < 32 * 64; e += 256) {
-            const int rr = e / 64, pp = e % 64;
-            const int64_t r = r0 + rr, p = p0 + pp;
-            tile[rr][pp] = (r < R && p < K) ? Xb[r * sr + p] : 0ull;
-        }
+        s.rr0 = t >> 6; s.drr = 4; s.pp0 = t & 63; s.dpp = 0;
+        s.di = 4 * sr;
+        s.dk = 64;
     } else {
-        for (int e = t; e < 32 * 64; e += 256) {
-            const int pp = e / 32, rr = e % 32;
-            const int64_t r = r0 + rr, p = p0 + pp;
-            tile[rr][pp] = (r < R && p < K) ? Xb[r * sr + p * sp] : 0ull;
-        }
+        s.rr0 = t & 31; s.drr = 0; s.pp0 = t >> 5; s.dpp = 8;
+        s.di = 8 * sp;
+        s.dk = 64 * sp;
     }
-    __syncthreads();
-    const int rr = t / 8, pp0 = (t % 8) * 8;
-    // max |x| and non-finite flag with integer operations on the bit patterns
+    s.src = reinterpret_cast<const unsigned long long*>(X) + (r0 + s.rr0) * sr + int64_t(s.pp0) * sp;
+    return s;
+}
+
+// Issue the copies of tile `it` (k from 64 it) into the buffer at shared address sbuf, where
+// off(rr, pp) places element (rr, pp); zeros outside R x K; one commit group per tile.
+template <typename Off>
+__device__ __forceinline__ void tile_issue(uint32_t sbuf, const TileSrc& s, const double* X, int64_t R, int64_t K,
+                                           int64_t r0, int64_t it, Off off) {
+    const unsigned long long* src = s.src + it * s.dk;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        const int rr = s.rr0 + i * s.drr, pp = s.pp0 + i * s.dpp;
+        const bool ok = r0 + rr < R && it * 64 + pp < K;
+        cp_async8(sbuf + off(rr, pp), ok ? src + i * s.di : reinterpret_cast<const unsigned long long*>(X), ok);
+    }
+    cp_async_commit();
+}
+
+// 2^x in FP32 for x <= 127, 0 below the normal range.
+__device__ __forceinline__ float pow2f_or0(int x) { return x < -126 ? 0.f : __uint_as_float(uint32_t(x + 127) << 23); }
+
+// Row statistics over TILE_KT tiles: thread (rr = t % 32, g = t / 32) keeps, for row rr and the
+// eight k of group g in every tile, the largest |x| (as bits), a non-finite flag and the sum of
+// squares in FP32 relative to its running largest exponent (rescaled exactly by a power of two
+// when a larger exponent arrives); the block folds the eight groups of a row and issues one set
+// of atomics per row.
+__device__ __forceinline__ void stats_rows(const double* __restrict__ X, int64_t R, int64_t K, int64_t sr, int64_t sp,
+                                           RowAcc* __restrict__ acc, int by) {
+    __shared__ __align__(16) unsigned long long tile[2][32][65];
+    __shared__ unsigned long long red_mx[8][32];
+    __shared__ int red_base[8][32], red_bad[8][32];
+    __shared__ float red_sq[8][32];
+    const int t = threadIdx.x, rr = t & 31, g = t >> 5;
+    const int64_t r0 = int64_t(by) * 32;
+    const int64_t ntiles = (K + 63) / 64;
+    const int64_t tb = int64_t(blockIdx.x) * TILE_KT, te = min(ntiles, tb + TILE_KT);
+    const uint32_t s0 = smem_u32(&tile[0][0][0]);
+    constexpr uint32_t BUF = 32 * 65 * 8;
+    auto off = [](int r_, int p_) { return uint32_t(r_ * 65 + p_) * 8u; };
     unsigned long long mx = 0;
-    int bad = 0;
-#pragma unroll
-    for (int q = 0; q < 8; ++q) {
-        const unsigned long long a = tile[rr][pp0 + q] & 0x7fffffffffffffffull;
-        bad |= (a >> 52) == 0x7ff;
-        mx = a > mx ? a : mx;
-    }
-#pragma unroll
-    for (int o = 4; o > 0; o >>= 1) {
-        const unsigned long long y = __shfl_xor_sync(0xffffffffu, mx, o);
-        mx = y > mx ? y : mx;
-        bad |= __shfl_xor_sync(0xffffffffu, bad, o);
-    }
-    // sum of squares in FP32 on values rebased to the tile row's largest exponent (|f| < 2)
-    const int et = int(mx >> 52);  // biased exponent of the tile-row maximum
+    int base = 0, bad = 0;
     float sq = 0.f;
+    const TileSrc ts = tile_src(X, sr, sp, r0);
+    if (tb < te) tile_issue(s0, ts, X, R, K, r0, tb, off);
+    for (int64_t it = tb; it < te; ++it) {
+        const int b = int(it - tb) & 1;
+        if (it + 1 < te) tile_issue(s0 + uint32_t(b ^ 1) * BUF, ts, X, R, K, r0, it + 1, off);
+        else cp_async_commit();  // an empty group keeps the wait count uniform
+        cp_async_wait1();
+        __syncthreads();
 #pragma unroll
-    for (int q = 0; q < 8; ++q) {
-        const unsigned long long a = tile[rr][pp0 + q] & 0x7fffffffffffffffull;
-        const int ea = int(a >> 52);
-        const int fe = ea - et + 127;  // biased float exponent after rebasing
-        const uint32_t fb = (ea == 0 || fe <= 0) ? 0u : (uint32_t(fe) << 23) | uint32_t((a >> 29) & 0x7fffffu);
-        const float f = __uint_as_float(fb);
-        sq = fmaf(f, f, sq);
+        for (int q = 0; q < 8; ++q) {
+            const unsigned long long a = tile[b][rr][8 * g + q] & 0x7fffffffffffffffull;
+            const int ea = int(a >> 52);
+            bad |= ea == 0x7ff;
+            mx = a > mx ? a : mx;
+            if (ea > base) {
+                sq *= pow2f_or0(2 * (base - ea));
+                base = ea;
+            }
+            const int fe = ea - base + 127;  // FP32 exponent of a / 2^(base - 1023)
+            const float f = (ea == 0 || fe <= 0) ? 0.f
+                                                 : __uint_as_float((uint32_t(fe) << 23) | uint32_t((a >> 29) & 0x7fffffu));
+            sq = fmaf(f, f, sq);
+        }
+        __syncthreads();
     }
+    red_mx[g][rr] = mx;
+    red_base[g][rr] = base;
+    red_sq[g][rr] = sq;
+    red_bad[g][rr] = bad;
+    __syncthreads();
+    if (g == 0) {
+        int E = 0, bd = 0;
+        unsigned long long m = 0;
 #pragma unroll
-    for (int o = 4; o > 0; o >>= 1) sq += __shfl_xor_sync(0xffffffffu, sq, o);
-    const int64_t r = r0 + rr;
-    if ((t & 7) == 0 && r < R) {
-        if (bad) atomicOr(&acc[r].flags, 1);
-        if (mx != 0) {
-            atomicMax(&acc[r].maxbits, mx);
-            // sum of squares of the unscaled values: sq * 2^(2*(et - 1023))
-            atomicAdd(&acc[r].sumsq, ldexp(double(sq), 2 * (et - 1023)));
+        for (int i = 0; i < 8; ++i) {
+            E = max(E, red_base[i][rr]);
+            bd |= red_bad[i][rr];
+            m = red_mx[i][rr] > m ? red_mx[i][rr] : m;
+        }
+        float s = 0.f;
+#pragma unroll
+        for (int i = 0; i < 8; ++i) s = fmaf(red_sq[i][rr], pow2f_or0(2 * (red_base[i][rr] - E)), s);
+        const int64_t r = r0 + rr;
+        if (r < R) {
+            if (bd) atomicOr(&acc[r].flags, 1);
+            if (m != 0) {
+                atomicMax(&acc[r].maxbits, m);
+                // sum of squares of the unscaled values: s * 2^(2 (E - 1023))
+                atomicAdd(&acc[r].sumsq, ldexp(double(s), 2 * (E - 1023)));
+            }
         }
     }
 }
@@ -244,10 +307,10 @@ struct OperandPair {
     unsigned yb0;  // row blocks of A
 };
 
-__global__ void stats_tile_kernel(const OperandPair op, int64_t K) {
+__global__ void __launch_bounds__(256, 4) stats_tile_kernel(const OperandPair op, int64_t K) {
     const int w = blockIdx.y < op.yb0 ? 0 : 1;
     const int by = w ? int(blockIdx.y - op.yb0) : int(blockIdx.y);
-    stats_tile(op.X[w], op.R[w], K, op.sr[w], op.sp[w], op.acc[w], by);
+    stats_rows(op.X[w], op.R[w], K, op.sr[w], op.sp[w], op.acc[w], by);
 }
 
 __global__ void stats_finalize_pair_kernel(const OperandPair op, int64_t K, unsigned xb0) {
@@ -480,41 +543,18 @@ __device__ __forceinline__ uint32_t mod_small(uint32_t x, uint32_t p, uint32_t i
     return r >= p ? r - p : r;
 }
 
-__device__ __forceinline__ void slice_tile(const double* __restrict__ X, int64_t R, int64_t K, int64_t sr, int64_t sp,
-                                           const int* __restrict__ rexp, const SplitInfo* __restrict__ info, int mode,
-                                           __nv_bfloat16* __restrict__ planes, int64_t rpad, int64_t kpad, int by) {
-    __shared__ unsigned long long tile[32][65];
-    const int64_t r0 = int64_t(by) * 32, p0 = int64_t(blockIdx.x) * 64;
-    const int t = threadIdx.x;  // 256 threads
-    const unsigned long long* Xb = reinterpret_cast<const unsigned long long*>(X);
-    if (sp == 1) {
-        for (int e = t; e < 32 * 64; e += 256) {
-            const int rr = e / 64, pp = e % 64;
-            const int64_t r = r0 + rr, p = p0 + pp;
-            tile[rr][pp] = (r < R && p < K) ? Xb[r * sr + p] : 0ull;
-        }
-    } else {
-        for (int e = t; e < 32 * 64; e += 256) {
-            const int pp = e / 32, rr = e % 32;
-            const int64_t r = r0 + rr, p = p0 + pp;
-            tile[rr][pp] = (r < R && p < K) ? Xb[r * sr + p * sp] : 0ull;
-        }
-    }
-    __syncthreads();
-    const int rr = t / 8, pp0 = (t % 8) * 8;
-    const int64_t r = r0 + rr;
-    if (r >= rpad) return;
-    const int64_t pstride = rpad * kpad;
-    uint16_t* dst = reinterpret_cast<uint16_t*>(planes) + r * kpad + p0 + pp0;
+// Planes of eight consecutive elements xv of one row (row exponent e, bad: the row holds Inf/NaN)
+// at dst, plane stride pstride; sl = slices (digits) or moduli (CRT), bt = beta (CRT).
+template <int mode>
+__device__ __forceinline__ void slice_emit(const unsigned long long (&xv)[8], int sl, int bt, int e, bool bad,
+                                           uint16_t* __restrict__ dst, int64_t pstride) {
     if (mode == kCrt) {
-        const int N = info->slices, beta = info->beta;
-        const int e = (r < R) ? rexp[r] : 0;
-        const bool bad = (e == kNonFinite);
+        const int N = sl, beta = bt;
         // U = |round(a 2^(beta-e))| < 2^56 in signed FP32 chunks (the sign of a applied to each)
         float w0[8], w1[8], w2[8], w3[8];
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
-            const unsigned long long bits = bad ? 0ull : tile[rr][pp0 + q];
+            const unsigned long long bits = bad ? 0ull : xv[q];
             const unsigned long long U = int_magnitude(bits, beta - e);
             const float sg = (bits >> 63) ? -1.f : 1.f, off = (bits >> 63) ? 8388608.f : -8388608.f;
             w0[q] = fmaf(__uint_as_float(0x4B000000u | (uint32_t(U) & 0x3fffu)), sg, off);
@@ -542,28 +582,26 @@ __device__ __forceinline__ void slice_tile(const double* __restrict__ X, int64_t
             *reinterpret_cast<uint4*>(dst + t * pstride) = w;
         }
     } else if (mode == kExact) {
-        const int S = info->slices;
-        const int e = (r < R) ? rexp[r] : 0;
-        const bool bad = (e == kNonFinite);
+        const int S = sl;
         bool neg[8];
 #pragma unroll
-        for (int q = 0; q < 8; ++q) neg[q] = !bad && (tile[rr][pp0 + q] >> 63) != 0;
+        for (int q = 0; q < 8; ++q) neg[q] = !bad && (xv[q] >> 63) != 0;
         if (S <= 8) {
             unsigned long long V[8];
 #pragma unroll
-            for (int q = 0; q < 8; ++q) V[q] = fixed_point_biased<unsigned long long>(bad ? 0ull : tile[rr][pp0 + q], e, S);
+            for (int q = 0; q < 8; ++q) V[q] = fixed_point_biased<unsigned long long>(bad ? 0ull : xv[q], e, S);
             write_planes(V, neg, S, dst, pstride);
         } else {
             unsigned __int128 V[8];
 #pragma unroll
-            for (int q = 0; q < 8; ++q) V[q] = fixed_point_biased<unsigned __int128>(bad ? 0ull : tile[rr][pp0 + q], e, S);
+            for (int q = 0; q < 8; ++q) V[q] = fixed_point_biased<unsigned __int128>(bad ? 0ull : xv[q], e, S);
             write_planes(V, neg, S, dst, pstride);
         }
     } else {
         __align__(16) __nv_bfloat16 hi[8], lo[8];
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
-            const double x = __longlong_as_double(static_cast<long long>(tile[rr][pp0 + q]));
+            const double x = __longlong_as_double(static_cast<long long>(xv[q]));
             hi[q] = __float2bfloat16_rn(float(x));
             lo[q] = __float2bfloat16_rn(float(x - double(__bfloat162float(hi[q]))));
         }
@@ -572,11 +610,58 @@ __device__ __forceinline__ void slice_tile(const double* __restrict__ X, int64_t
     }
 }
 
-__global__ void slice_kernel(const OperandPair op, int64_t K, const SplitInfo* __restrict__ info, int mode,
-                             int64_t kpad) {
+// Planes of 32 rows over TILE_KT k-tiles.  Thread (rr = t / 8, L = t % 8) handles elements
+// 8L..8L+7 of row rr and writes 16 bytes per plane (a warp: four 128-byte row segments).  The tile
+// buffer keeps rows of 528 bytes with 16-byte chunk c of a row stored at c ^ (c >> 3), so that the
+// eight threads of a row read their chunks 4L + j from eight different bank groups.
+template <int mode>
+__device__ __forceinline__ void slice_rows(const double* __restrict__ X, int64_t R, int64_t K, int64_t sr, int64_t sp,
+                                           const int* __restrict__ rexp, const SplitInfo* __restrict__ info,
+                                           __nv_bfloat16* __restrict__ planes, int64_t rpad, int64_t kpad, int by) {
+    constexpr uint32_t ROWB = 528, BUF = 32 * ROWB;
+    __shared__ __align__(16) unsigned char tbuf[2 * BUF];
+    const int t = threadIdx.x, rr = t >> 3, L = t & 7;
+    const int64_t r0 = int64_t(by) * 32, r = r0 + rr;
+    const int64_t ntiles = kpad / 64;
+    const int64_t tb = int64_t(blockIdx.x) * TILE_KT, te = min(ntiles, tb + TILE_KT);
+    const uint32_t s0 = smem_u32(tbuf);
+    auto off = [](int r_, int p_) {
+        const uint32_t c = uint32_t(p_) >> 1;
+        return uint32_t(r_) * ROWB + ((c ^ (c >> 3)) << 4) + ((uint32_t(p_) & 1u) << 3);
+    };
+    const int sl = (mode == kExact || mode == kCrt) ? info->slices : 0, bt = (mode == kCrt) ? info->beta : 0;
+    const int e = (r < R) ? rexp[r] : 0;
+    const bool bad = (mode == kExact || mode == kCrt) && e == kNonFinite;
+    const int64_t pstride = rpad * kpad;
+    const TileSrc ts = tile_src(X, sr, sp, r0);
+    if (tb < te) tile_issue(s0, ts, X, R, K, r0, tb, off);
+    for (int64_t it = tb; it < te; ++it) {
+        const int b = int(it - tb) & 1;
+        if (it + 1 < te) tile_issue(s0 + uint32_t(b ^ 1) * BUF, ts, X, R, K, r0, it + 1, off);
+        else cp_async_commit();  // an empty group keeps the wait count uniform
+        cp_async_wait1();
+        __syncthreads();
+        unsigned long long xv[8];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const uint32_t c = uint32_t(4 * L + j);
+            const uint4 v = *reinterpret_cast<const uint4*>(tbuf + b * BUF + rr * ROWB + ((c ^ (c >> 3)) << 4));
+            xv[2 * j] = (unsigned long long)v.x | ((unsigned long long)v.y << 32);
+            xv[2 * j + 1] = (unsigned long long)v.z | ((unsigned long long)v.w << 32);
+        }
+        if (r < rpad)
+            slice_emit<mode>(xv, sl, bt, e, bad, reinterpret_cast<uint16_t*>(planes) + r * kpad + it * 64 + 8 * L,
+                             pstride);
+        __syncthreads();
+    }
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(256, 3) slice_kernel(const OperandPair op, int64_t K, const SplitInfo* __restrict__ info,
+                                                       int64_t kpad) {
     const int w = blockIdx.y < op.yb0 ? 0 : 1;
     const int by = w ? int(blockIdx.y - op.yb0) : int(blockIdx.y);
-    slice_tile(op.X[w], op.R[w], K, op.sr[w], op.sp[w], op.rexp[w], info, mode, op.planes[w], op.rpad[w], kpad, by);
+    slice_rows<MODE>(op.X[w], op.R[w], K, op.sr[w], op.sp[w], op.rexp[w], info, op.planes[w], op.rpad[w], kpad, by);
 }
 
 // ---- level / pair schedule ---------------------------------------------------------------------
@@ -1363,7 +1448,7 @@ int device_product(const Gemm& g_in, const SplitRequest& req, const LaunchCtl& c
     op.rpad[0] = mpad; op.rpad[1] = npad;
     op.yb0 = unsigned((m + 31) / 32);
     {
-        dim3 grid(unsigned((k + 63) / 64), unsigned((m + 31) / 32 + (n + 31) / 32));
+        dim3 grid(unsigned(((k + 63) / 64 + TILE_KT - 1) / TILE_KT), unsigned((m + 31) / 32 + (n + 31) / 32));
         stats_tile_kernel<<<grid, 256, 0, st>>>(op, k);
         const unsigned xb0 = unsigned((m + 255) / 256);
         stats_finalize_pair_kernel<<<xb0 + unsigned((n + 255) / 256), 256, 0, st>>>(op, k, xb0);
@@ -1378,8 +1463,10 @@ int device_product(const Gemm& g_in, const SplitRequest& req, const LaunchCtl& c
     {
         OperandPair sp2 = op;
         sp2.yb0 = unsigned(mpad / 32);
-        dim3 grid(unsigned(kpad / 64), unsigned(mpad / 32 + npad / 32));
-        slice_kernel<<<grid, 256, 0, st>>>(sp2, k, info, mode, kpad);
+        dim3 grid(unsigned((kpad / 64 + TILE_KT - 1) / TILE_KT), unsigned(mpad / 32 + npad / 32));
+        auto sk = mode == kCrt ? slice_kernel<kCrt>
+                               : (mode == kExact ? slice_kernel<kExact> : (mode == kBf16 ? slice_kernel<kBf16> : slice_kernel<kBf16x3>));
+        sk<<<grid, 256, 0, st>>>(sp2, k, info, kpad);
     }
     count_launches(4);
     if (cudaError_t le = cudaGetLastError(); le != cudaSuccess) {
