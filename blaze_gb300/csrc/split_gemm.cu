@@ -65,12 +65,14 @@
 namespace gb {
 namespace {
 
-constexpr int TM = 128;                 // tile rows (MMA M)
-constexpr int TN = 256;                 // tile cols (MMA N)
+constexpr int TM = 128;                 // A rows held by each CTA of a pair
+constexpr int TN = 256;                 // tile cols (pair MMA N)
+constexpr int TMP = 2 * TM;             // rows of a CTA pair's tile (pair MMA M = 256)
+constexpr int TNH = TN / 2;             // B rows (tile columns) held by each CTA of the pair
 constexpr int TK = 64;                  // k per item (one 128-byte swizzle row of bf16)
-constexpr int STAGES = 4;
+constexpr int STAGES = 6;
 constexpr int A_BYTES = TM * TK * 2;    // 16 KB
-constexpr int B_BYTES = TN * TK * 2;    // 32 KB
+constexpr int B_BYTES = TNH * TK * 2;   // 16 KB (this CTA's half of the B tile)
 constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
 constexpr int GROUP_ITEMS = 4;          // exact mode: 4 items (256 products) per TMEM drain
 constexpr int EPI_WARPS = 8;
@@ -700,7 +702,11 @@ struct __align__(8) TcBarriers {
     uint32_t tmem_base;
 };
 
-constexpr size_t kTcSmem = size_t(STAGES) * STAGE_BYTES + sizeof(TcBarriers) + 1024;
+// Residue (CRT) level tiles leave through a per-warp staging tile (32 rows x 128 bytes, 128-byte
+// swizzle) and a TMA store: full-line writes instead of 32 rows per store instruction.
+constexpr int OUT_WARP_BYTES = 32 * 128;
+constexpr int OUT_BYTES = EPI_WARPS * OUT_WARP_BYTES;
+constexpr size_t kTcSmem = size_t(STAGES) * STAGE_BYTES + OUT_BYTES + sizeof(TcBarriers) + 1024;
 
 __device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
     uint64_t d = 0;
@@ -712,8 +718,8 @@ __device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
     return d;
 }
 
-// kind::f16 instruction descriptor: BF16 A and B (K-major), FP32 D, M = 128, N = 256.
-constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(TN >> 3) << 17) | (uint32_t(TM >> 4) << 24);
+// kind::f16 instruction descriptor: BF16 A and B (K-major), FP32 D, M = 256 (a CTA pair), N = 256.
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(TN >> 3) << 17) | (uint32_t(TMP >> 4) << 24);
 
 // Work unit u -> (tile m, tile n, segment), grouping 8 m-tiles per band for L2 reuse.
 __device__ __forceinline__ void unit_coords(const TcParams& p, int u, int& tm, int& tn, int& seg) {
@@ -728,12 +734,19 @@ __device__ __forceinline__ void unit_coords(const TcParams& p, int u, int& tm, i
 }
 
 template <int MODE>
-__global__ void __maxnreg__(168)
-tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, const TcParams p) {
+__global__ void __cluster_dims__(2, 1, 1) __maxnreg__(168)
+tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+               const __grid_constant__ CUtensorMap tmC, const TcParams p) {
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-    TcBarriers* bars = reinterpret_cast<TcBarriers*>(smem + STAGES * STAGE_BYTES);
+    uint8_t* out_stage = smem + STAGES * STAGE_BYTES;
+    TcBarriers* bars = reinterpret_cast<TcBarriers*>(out_stage + OUT_BYTES);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    // CTA pair: both CTAs walk the same units; the even CTA issues the pair MMAs, each CTA loads its
+    // 128 rows of A and its half of B and drains its own 128 TMEM lanes
+    const uint32_t rank = cluster_ctarank();
+    const bool leader = rank == 0;
+    const int pair = int(blockIdx.x >> 1), npairs = int(gridDim.x >> 1);
 
     // the epilogue's arithmetic is fixed at compile time (exact integer sums or FP32 tiles); the
     // digit and residue schedules share the exact instantiation and differ only in the plane pairs
@@ -746,23 +759,28 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
     if (threadIdx.x == 0) {
         tma_prefetch_desc(&tmA);
         tma_prefetch_desc(&tmB);
+        if (p.mode == kCrt) tma_prefetch_desc(&tmC);
+        // full: the even CTA's arm plus both CTAs' bytes; empty / acc_full: one pair-MMA commit
+        // (multicast to both CTAs); acc_empty (even CTA): every epilogue warp of both CTAs
         for (int s = 0; s < STAGES; ++s) {
             mbar_init(smem_u32(&bars->full[s]), 1);
             mbar_init(smem_u32(&bars->empty[s]), 1);
         }
         for (int b = 0; b < 2; ++b) {
             mbar_init(smem_u32(&bars->acc_full[b]), 1);
-            mbar_init(smem_u32(&bars->acc_empty[b]), EPI_WARPS);
+            mbar_init(smem_u32(&bars->acc_empty[b]), 2 * EPI_WARPS);
         }
         mbar_init(smem_u32(&bars->drain), 1);
         fence_mbar_init();
     }
     if (warp == 1) {
-        tmem_alloc(smem_u32(&bars->tmem_base), 512);
-        tmem_relinquish();
+        __syncwarp();
+        tmem_alloc_pair(smem_u32(&bars->tmem_base), 512);
+        tmem_relinquish_pair();
     }
     tc_fence_before();
-    __syncthreads();
+    // barriers of both CTAs initialised before any cross-CTA arrival or copy
+    cluster_sync();
     tc_fence_after();
     const uint32_t tmem = bars->tmem_base;
 
@@ -771,7 +789,7 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
         if (lane == 0 && !p.inject_stall) {
             uint32_t it = 0;
             bool ok = true;
-            for (int u = blockIdx.x; u < units && ok; u += gridDim.x) {
+            for (int u = pair; u < units && ok; u += npairs) {
                 int tm, tn, seg;
                 unit_coords(p, u, tm, tn, seg);
                 const int kb0 = seg * p.kb_per_seg;
@@ -789,27 +807,34 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
                             }
                             int a, b;
                             pair_planes(mode, L, i, a, b);
-                            const uint32_t full = smem_u32(&bars->full[s]);
-                            mbar_arrive_expect_tx(full, STAGE_BYTES);
+                            // both CTAs' bytes complete on the even CTA's full barrier, armed there
+                            // for the two halves
+                            const uint32_t full_local = smem_u32(&bars->full[s]);
+                            if (leader) mbar_arrive_expect_tx(full_local, 2 * STAGE_BYTES);
+                            const uint32_t full = mapa_shared(full_local, 0);
                             const uint32_t dst = smem_u32(smem + s * STAGE_BYTES);
                             const int32_t kx = (kb0 + kb) * TK;
-                            tma_load_2d(dst, &tmA, kx, int32_t(a * p.mpad + int64_t(tm) * TM), full);
-                            tma_load_2d(dst + A_BYTES, &tmB, kx, int32_t(b * p.npad + int64_t(tn) * TN), full);
+                            tma_load_2d_pair(dst, &tmA, kx, int32_t(a * p.mpad + int64_t(tm) * TMP + rank * TM), full);
+                            tma_load_2d_pair(dst + A_BYTES, &tmB, kx,
+                                             int32_t(b * p.npad + int64_t(tn) * TN + rank * TNH), full);
                         }
                     }
                 }
             }
-            // drain: the last use of every stage must have landed before the CTA exits
-            const uint32_t first = it > STAGES ? it - STAGES : 0;
-            for (uint32_t j = first; j < it; ++j)
-                mbar_wait_drain(smem_u32(&bars->full[j % STAGES]), (j / STAGES) & 1, p.limit_ns);
+            // drain: the last use of every stage must have landed before the pair exits (the even
+            // CTA's full barriers count the bytes of both)
+            if (leader) {
+                const uint32_t first = it > STAGES ? it - STAGES : 0;
+                for (uint32_t j = first; j < it; ++j)
+                    mbar_wait_drain(smem_u32(&bars->full[j % STAGES]), (j / STAGES) & 1, p.limit_ns);
+            }
         }
     } else if (warp == 1) {
-        // ---------------- MMA issuer ----------------
-        if (lane == 0) {
+        // ---------------- MMA issuer (even CTA of the pair) ----------------
+        if (lane == 0 && leader) {
             uint32_t it = 0, grp = 0;
             bool ok = true, issued_any = false;
-            for (int u = blockIdx.x; u < units && ok; u += gridDim.x) {
+            for (int u = pair; u < units && ok; u += npairs) {
                 int tm, tn, seg;
                 unit_coords(p, u, tm, tn, seg);
                 const int kb0 = seg * p.kb_per_seg;
@@ -841,19 +866,19 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
                             const uint64_t bdesc = sw128_desc(a_addr + A_BYTES);
 #pragma unroll
                             for (int j = 0; j < TK / 16; ++j)
-                                tc_mma_f16(dcol, adesc + uint64_t(2 * j), bdesc + uint64_t(2 * j), kIdesc,
-                                           (x == g0 && j == 0) ? 0u : 1u);
-                            tc_commit(smem_u32(&bars->empty[s]));
+                                tc_mma_f16_pair(dcol, adesc + uint64_t(2 * j), bdesc + uint64_t(2 * j), kIdesc,
+                                                (x == g0 && j == 0) ? 0u : 1u);
+                            tc_commit_pair_mc(smem_u32(&bars->empty[s]), 0x3);
                             issued_any = true;
                         }
                         if (!ok) break;
-                        tc_commit(smem_u32(&bars->acc_full[buf]));
+                        tc_commit_pair_mc(smem_u32(&bars->acc_full[buf]), 0x3);
                     }
                 }
             }
             // drain: every issued MMA completes before TMEM is released
             if (issued_any) {
-                tc_commit(smem_u32(&bars->drain));
+                tc_commit_pair_mc(smem_u32(&bars->drain), 0x1);
                 mbar_wait_drain(smem_u32(&bars->drain), 0, p.limit_ns);
             }
         }
@@ -864,12 +889,15 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
         const uint32_t lane_base = uint32_t(32 * q) << 16;
         uint32_t grp = 0;
         bool ok = true;
-        for (int u = blockIdx.x; u < units && ok; u += gridDim.x) {
+        // the even CTA's accumulator-empty barriers (the MMA issuer waits for both CTAs' drains)
+        const uint32_t acc_empty0 = mapa_shared(smem_u32(&bars->acc_empty[0]), 0);
+        const uint32_t acc_empty1 = mapa_shared(smem_u32(&bars->acc_empty[1]), 0);
+        for (int u = pair; u < units && ok; u += npairs) {
             int tm, tn, seg;
             unit_coords(p, u, tm, tn, seg);
             const int kb0 = seg * p.kb_per_seg;
             const int kbn = min(p.kb_per_seg, p.kb_total - kb0);
-            const int64_t row = int64_t(tm) * TM + 32 * q + lane;
+            const int64_t row = int64_t(tm) * TMP + int64_t(rank) * TM + 32 * q + lane;
             for (int L = 0; L < nlev && ok; ++L) {
                 const int np = pairs_in_level(mode, L);
                 const int items = np * kbn;
@@ -903,7 +931,7 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
                     }
                     tc_fence_before();
                     __syncwarp();
-                    if (lane == 0) mbar_arrive(smem_u32(&bars->acc_empty[buf]));
+                    if (lane == 0) mbar_arrive_cluster(buf ? acc_empty1 : acc_empty0);
                 }
                 if (!ok) break;
                 // level sums -> global level plane (row-major, pitch npad); in the residue (CRT)
@@ -912,20 +940,38 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
                                           int64_t(tn) * TN + h * 128;
                 const uint32_t bias = (emode == kExact) ? ngroups * MAGIC_BITS : 0u;
                 if (emode == kExact && mode == kCrt) {
-                    uint16_t* dst = reinterpret_cast<uint16_t*>(p.levels) + plane_off;
+                    // residues in [0, p) as 16-bit values; two 64-column halves per warp go out
+                    // through the warp's staging tile (row = lane, 16-byte chunk j of a row at
+                    // j ^ (lane % 8): the TMA 128-byte swizzle) and a TMA store
                     const uint32_t pm = c_mod[L], inv = c_mod_inv32[L];
+                    uint8_t* stg = out_stage + (warp - 2) * OUT_WARP_BYTES;
+                    const int32_t ytile = int32_t((int64_t(seg) * p.max_levels + L) * p.mpad + int64_t(tm) * TMP +
+                                                  int64_t(rank) * TM + 32 * q);
 #pragma unroll
-                    for (int c = 0; c < 128; c += 8) {
-                        __align__(16) uint16_t rr[8];
+                    for (int ch = 0; ch < 2; ++ch) {
+                        if (lane == 0) bulk_wait_read0();  // the previous store has read the tile
+                        __syncwarp();
 #pragma unroll
-                        for (int q = 0; q < 8; ++q) {
-                            const int32_t t = int32_t(acc[c + q] - bias);
-                            const uint32_t mag = t < 0 ? uint32_t(-int64_t(t)) : uint32_t(t);
-                            uint32_t rsd = mod_small(mag, pm, inv);
-                            if (t < 0 && rsd) rsd = pm - rsd;
-                            rr[q] = uint16_t(rsd);
+                        for (int j = 0; j < 8; ++j) {
+                            const int c = ch * 64 + j * 8;
+                            __align__(16) uint16_t rr[8];
+#pragma unroll
+                            for (int e = 0; e < 8; ++e) {
+                                const int32_t t = int32_t(acc[c + e] - bias);
+                                const uint32_t mag = t < 0 ? uint32_t(-int64_t(t)) : uint32_t(t);
+                                uint32_t rsd = mod_small(mag, pm, inv);
+                                if (t < 0 && rsd) rsd = pm - rsd;
+                                rr[e] = uint16_t(rsd);
+                            }
+                            *reinterpret_cast<uint4*>(stg + lane * 128 + ((j ^ (lane & 7)) << 4)) =
+                                *reinterpret_cast<const uint4*>(rr);
                         }
-                        *reinterpret_cast<uint4*>(dst + c) = *reinterpret_cast<const uint4*>(rr);
+                        fence_proxy_async_smem();
+                        __syncwarp();
+                        if (lane == 0) {
+                            tma_store_2d(&tmC, int32_t(tn * TN + h * 128 + ch * 64), ytile, smem_u32(stg));
+                            bulk_commit();
+                        }
                     }
                 } else {
                     int32_t* dst = p.levels + plane_off;
@@ -943,11 +989,15 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
         }
     }
 
+    // the residue stores of this thread have completed
+    if (warp >= 2 && lane == 0) bulk_wait0();
     tc_fence_before();
-    __syncthreads();
+    // neither CTA leaves while the pair MMAs, copies or arrivals may still touch its memory
+    cluster_sync();
     if (warp == 1) {
+        __syncwarp();
         tc_fence_after();
-        tmem_dealloc(tmem, 512);
+        tmem_dealloc_pair(tmem, 512);
     }
 }
 
@@ -1272,9 +1322,9 @@ SplitGeometry split_geometry(const Gemm& g, const SplitRequest& req, int num_sms
     else if ((req.method == GB300_METHOD_SPLIT || req.method == GB300_METHOD_AUTO) && req.slices <= 0 &&
              crt_worst_case_moduli(g.k, req.target_error) <= MAX_MODULI)
         G.mode = kCrt;
-    G.m_tiles = int((g.m + TM - 1) / TM);
+    G.m_tiles = int((g.m + TMP - 1) / TMP);  // tiles of a CTA pair (256 rows)
     G.n_tiles = int((g.n + TN - 1) / TN);
-    G.mpad = int64_t(G.m_tiles) * TM;
+    G.mpad = int64_t(G.m_tiles) * TMP;
     G.npad = int64_t(G.n_tiles) * TN;
     G.kpad = round_up(g.k, TK);
     G.kb_total = int(G.kpad / TK);
@@ -1295,9 +1345,9 @@ SplitGeometry split_geometry(const Gemm& g, const SplitRequest& req, int num_sms
         const int64_t cap = (int64_t(511) / (G.mode == kCrt ? 1 : G.max_planes)) * KSEG_UNIT;
         kseg = std::min(kseg, std::max<int64_t>(cap, KSEG_UNIT));
     }
-    const int tiles = G.m_tiles * G.n_tiles;
-    if (tiles < num_sms) {
-        const int64_t want = (num_sms + tiles - 1) / tiles;
+    const int tiles = G.m_tiles * G.n_tiles, pairs = std::max(1, num_sms / 2);
+    if (tiles < pairs) {
+        const int64_t want = (pairs + tiles - 1) / tiles;
         kseg = std::min(kseg, std::max<int64_t>(KSEG_UNIT, round_up((G.kpad + want - 1) / want, KSEG_UNIT)));
     }
     // equal segments: persistent CTAs take units in a fixed stride, so unequal segments would give
@@ -1477,8 +1527,15 @@ int device_product(const Gemm& g_in, const SplitRequest& req, const LaunchCtl& c
     CUtensorMap tA, tB;
     if (!encode_tmap_2d(&tA, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, pa, uint64_t(max_planes) * mpad, kpad, kpad, TM, TK,
                         CU_TENSOR_MAP_SWIZZLE_128B, err) ||
-        !encode_tmap_2d(&tB, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, pb, uint64_t(max_planes) * npad, kpad, kpad, TN, TK,
+        !encode_tmap_2d(&tB, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, pb, uint64_t(max_planes) * npad, kpad, kpad, TNH, TK,
                         CU_TENSOR_MAP_SWIZZLE_128B, err))
+        return GB300_ERR_CUDA;
+
+    // residue planes as a 2-D array of 16-bit values for the epilogue's TMA stores
+    CUtensorMap tC = tA;
+    if (mode == kCrt &&
+        !encode_tmap_2d(&tC, CU_TENSOR_MAP_DATA_TYPE_UINT16, 2, lv, uint64_t(nseg) * max_levels * mpad, npad, npad, 32,
+                        64, CU_TENSOR_MAP_SWIZZLE_128B, err))
         return GB300_ERR_CUDA;
 
     TcParams p;
@@ -1497,7 +1554,9 @@ int device_product(const Gemm& g_in, const SplitRequest& req, const LaunchCtl& c
     p.limit_ns = ctl.wait_limit_ns;
     p.inject_stall = ctl.inject_stall;
     const int units = m_tiles * n_tiles * nseg;
-    const int grid = std::min(units, req.max_sms > 0 ? std::min(req.max_sms, r.num_sms) : r.num_sms);
+    // CTA pairs (clusters of two): at most one pair per unit, at least one pair
+    const int sms = req.max_sms > 0 ? std::min(req.max_sms, r.num_sms) : r.num_sms;
+    const int grid = 2 * std::max(1, std::min(units, sms / 2));
     auto kern = (mode == kExact || mode == kCrt) ? tc_gemm_kernel<kExact>
                                                  : (mode == kBf16 ? tc_gemm_kernel<kBf16> : tc_gemm_kernel<kBf16x3>);
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kTcSmem));
@@ -1507,7 +1566,7 @@ int device_product(const Gemm& g_in, const SplitRequest& req, const LaunchCtl& c
     }
     {
         KernelTimer timer("tc_gemm", st);
-        kern<<<grid, THREADS, kTcSmem, st>>>(tA, tB, p);
+        kern<<<grid, THREADS, kTcSmem, st>>>(tA, tB, tC, p);
     }
     {
         const int64_t colgroups = (n + COMBINE_COLS - 1) / COMBINE_COLS;
