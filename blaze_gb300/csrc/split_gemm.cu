@@ -721,8 +721,14 @@ __device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
 // kind::f16 instruction descriptor: BF16 A and B (K-major), FP32 D, M = 256 (a CTA pair), N = 256.
 constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(TN >> 3) << 17) | (uint32_t(TMP >> 4) << 24);
 
-// Work unit u -> (tile m, tile n, segment), grouping 8 m-tiles per band for L2 reuse.
-__device__ __forceinline__ void unit_coords(const TcParams& p, int u, int& tm, int& tn, int& seg) {
+// Work unit u -> (level, tile m, tile n, segment): one level (a modulus, or the slice pairs of a
+// digit level) of one pair tile, the level varying slowest so that concurrent pairs share the
+// operand planes of one level in L2, with 8 m-tiles per band.  Units of one level have equal
+// lengths, and many small units keep the last wave short.
+__device__ __forceinline__ void unit_coords(const TcParams& p, int u, int& tm, int& tn, int& seg, int& L) {
+    const int per_level = p.m_tiles * p.n_tiles * p.nseg;
+    L = u / per_level;
+    u -= L * per_level;
     seg = u % p.nseg;
     const int t = u / p.nseg;
     const int band = 8;
@@ -754,7 +760,7 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
     const int mode = (MODE == kExact) ? p.mode : MODE;
     const int S = (mode == kExact || mode == kCrt) ? p.info->slices : 1;
     const int nlev = num_levels(mode, S);
-    const int units = p.m_tiles * p.n_tiles * p.nseg;
+    const int units = p.m_tiles * p.n_tiles * p.nseg * nlev;
 
     if (threadIdx.x == 0) {
         tma_prefetch_desc(&tmA);
@@ -790,11 +796,12 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
             uint32_t it = 0;
             bool ok = true;
             for (int u = pair; u < units && ok; u += npairs) {
-                int tm, tn, seg;
-                unit_coords(p, u, tm, tn, seg);
+                int tm, tn, seg, Lu;
+                unit_coords(p, u, tm, tn, seg, Lu);
                 const int kb0 = seg * p.kb_per_seg;
                 const int kbn = min(p.kb_per_seg, p.kb_total - kb0);
-                for (int L = 0; L < nlev && ok; ++L) {
+                {
+                    const int L = Lu;
                     const int np = pairs_in_level(mode, L);
                     for (int kb = 0; kb < kbn && ok; ++kb) {
                         for (int i = 0; i < np; ++i, ++it) {
@@ -835,11 +842,12 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
             uint32_t it = 0, grp = 0;
             bool ok = true, issued_any = false;
             for (int u = pair; u < units && ok; u += npairs) {
-                int tm, tn, seg;
-                unit_coords(p, u, tm, tn, seg);
+                int tm, tn, seg, Lu;
+                unit_coords(p, u, tm, tn, seg, Lu);
                 const int kb0 = seg * p.kb_per_seg;
                 const int kbn = min(p.kb_per_seg, p.kb_total - kb0);
-                for (int L = 0; L < nlev && ok; ++L) {
+                {
+                    const int L = Lu;
                     const int np = pairs_in_level(mode, L);
                     const int items = np * kbn;
                     const int gsize = (mode == kExact || mode == kCrt) ? GROUP_ITEMS : items;
@@ -893,12 +901,13 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
         const uint32_t acc_empty0 = mapa_shared(smem_u32(&bars->acc_empty[0]), 0);
         const uint32_t acc_empty1 = mapa_shared(smem_u32(&bars->acc_empty[1]), 0);
         for (int u = pair; u < units && ok; u += npairs) {
-            int tm, tn, seg;
-            unit_coords(p, u, tm, tn, seg);
+            int tm, tn, seg, Lu;
+            unit_coords(p, u, tm, tn, seg, Lu);
             const int kb0 = seg * p.kb_per_seg;
             const int kbn = min(p.kb_per_seg, p.kb_total - kb0);
             const int64_t row = int64_t(tm) * TMP + int64_t(rank) * TM + 32 * q + lane;
-            for (int L = 0; L < nlev && ok; ++L) {
+            {
+                const int L = Lu;
                 const int np = pairs_in_level(mode, L);
                 const int items = np * kbn;
                 const int gsize = (mode == kExact || mode == kCrt) ? GROUP_ITEMS : items;
@@ -1358,26 +1367,10 @@ SplitGeometry split_geometry(const Gemm& g, const SplitRequest& req, int num_sms
     return G;
 }
 
-size_t split_scratch_bytes(const Gemm& g, const SplitGeometry& G) {
-    const size_t planes = size_t(G.max_planes) * (size_t(G.mpad) + size_t(G.npad)) * size_t(G.kpad) * 2;
-    const size_t levels = size_t(G.nseg) * G.max_levels * size_t(G.mpad) * size_t(G.npad) * 4;
-    const size_t stats = size_t(g.m + g.n) * (sizeof(int) + sizeof(double) + 32) + 4096 + sizeof(SplitInfo);
-    return planes + levels + stats;
-}
-
 // Stored (row-major) shape of the operands of a logical product.
 void stored_a(const Gemm& g, int64_t* rows, int64_t* cols) { *rows = g.ta ? g.k : g.m; *cols = g.ta ? g.m : g.k; }
 void stored_b(const Gemm& g, int64_t* rows, int64_t* cols) { *rows = g.tb ? g.n : g.k; *cols = g.tb ? g.k : g.n; }
 bool tma_ready(const void* p, int64_t ld) { return reinterpret_cast<uintptr_t>(p) % 16 == 0 && (ld * 8) % 16 == 0; }
-
-size_t realign_bytes(const Gemm& g) {
-    if (g.k == 0) return 0;
-    size_t b = 0;
-    int64_t r, c;
-    if (!tma_ready(g.A, g.lda)) { stored_a(g, &r, &c); b += size_t(r) * size_t((c + 1) / 2 * 2) * 8; }
-    if (!tma_ready(g.B, g.ldb)) { stored_b(g, &r, &c); b += size_t(r) * size_t((c + 1) / 2 * 2) * 8; }
-    return b;
-}
 
 // Copy operands whose base or pitch TMA cannot address (16-byte alignment) into the workspace.
 int realign_operands(Gemm& g, Workspace& ws, cudaStream_t st, std::string* err) {
@@ -1553,8 +1546,9 @@ int device_product(const Gemm& g_in, const SplitRequest& req, const LaunchCtl& c
     p.status = ctl.status;
     p.limit_ns = ctl.wait_limit_ns;
     p.inject_stall = ctl.inject_stall;
-    const int units = m_tiles * n_tiles * nseg;
-    // CTA pairs (clusters of two): at most one pair per unit, at least one pair
+    // units: one level of one pair tile and k-segment (the device picks the level count, at most
+    // max_levels); CTA pairs (clusters of two): at most one pair per unit, at least one pair
+    const int units = m_tiles * n_tiles * nseg * max_levels;
     const int sms = req.max_sms > 0 ? std::min(req.max_sms, r.num_sms) : r.num_sms;
     const int grid = 2 * std::max(1, std::min(units, sms / 2));
     auto kern = (mode == kExact || mode == kCrt) ? tc_gemm_kernel<kExact>
