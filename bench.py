@@ -588,8 +588,11 @@ def sweep(args):
                 for layout, tb in (("rr", 111), ("rc", 112)):
                     # rc: B stored n x n with k contiguous (Blaze DMatTDMatMultExpr)
                     P = cpu_check_rows(hA, hB, n, rows, tb=tb)
+                    # native; automatic split (residue scheme); residue scheme with a fixed modulus
+                    # count; digit scheme with a fixed slice count; BF16x3
                     forms = [("native", 0)] if n <= 8192 or layout == "rr" else []
-                    forms += [("split", 0)] + [("split", S) for S in range(3, 9)] + [("bf16x3", 0)]
+                    forms += [("split", 0)] + [("split_crt", N) for N in (6, 8, 10, 12, 14)]
+                    forms += [("split", S) for S in range(3, 9)] + [("bf16x3", 0)]
                     for method, S in forms:
                         o = G.opts(method=method, slices=S, residency=G.PTR_DEVICE, stream=s.cuda_stream,
                                    synchronous=False)
@@ -600,8 +603,10 @@ def sweep(args):
                                           G.opts(method=method, slices=S, residency=G.PTR_DEVICE))
                         C = dC.cpu().numpy().reshape(n, n)
                         err = float(np.linalg.norm(C[rows] - P) * np.sqrt(n / len(rows)) / (nA * nB))
+                        form = {G.METHOD_SPLIT_CRT: "split-residues", G.METHOD_SPLIT: "split-digits"}.get(
+                            info.method_used, method)
                         print(json.dumps({"sweep": "square", "n": n, "layout": layout, "dist": dist, "method": method,
-                                          "slices": info.slices_used, "ms": round(ms, 3),
+                                          "form": form, "slices": info.slices_used, "ms": round(ms, 3),
                                           "tflops": round(2.0 * n ** 3 / (ms * 1e-3) / 1e12, 3),
                                           "normwise_error": err, "bound": info.error_bound,
                                           "target": n * 2.0 ** -53}), flush=True)
@@ -626,7 +631,9 @@ def sweep(args):
                 C = dC.cpu().numpy().reshape(n, m).T  # column-major m x n
                 err = float(np.linalg.norm(C[rows] - P) * np.sqrt(m / len(rows)) / (nA * nB))
                 bytes_ = 8.0 * (m * k + k * n + m * n)
-                print(json.dumps({"sweep": "rect", "m": m, "k": k, "n": n, "method": method,
+                form = {G.METHOD_SPLIT_CRT: "split-residues", G.METHOD_SPLIT: "split-digits"}.get(info.method_used,
+                                                                                                  method)
+                print(json.dumps({"sweep": "rect", "m": m, "k": k, "n": n, "method": method, "form": form,
                                   "slices": info.slices_used, "ms": round(ms, 3),
                                   "tflops": round(2.0 * m * n * k / (ms * 1e-3) / 1e12, 3),
                                   "operand_gbs": round(bytes_ / (ms * 1e-3) / 1e9, 1),
