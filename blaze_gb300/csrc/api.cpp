@@ -177,17 +177,52 @@ int gemm_entry(int order, int transA, int transB, int64_t m, int64_t n, int64_t 
     cudaStream_t s = (opts && opts->stream) ? static_cast<cudaStream_t>(opts->stream) : r.stream;
     const bool sync = any_host || !opts || opts->synchronous;
 
+    LaunchCtl ctl;
+    ctl.status = r.d_status;
+    if (r.inject_stall_count > 0) {
+        --r.inject_stall_count;
+        ctl.inject_stall = 1;
+        ctl.wait_limit_ns = r.inject_limit_ns;
+    }
+    cudaMemsetAsync(r.d_status, 0, sizeof(int), s);
+    int used = method;
+    const void* info_dev = nullptr;
+    cudaError_t e = cudaSuccess;
+
+    // Page-locked host operands of a large FP64-accurate product: row panels of A whose copies in
+    // and out overlap the computation (falls through to staging when the method, shape or memory
+    // does not qualify).
+    bool done = false;
+    if (is_double && product && !devA && !devB && !devC && method != GB300_METHOD_NATIVE) {
+        SplitRequest req;
+        req.method = method;
+        req.slices = opts ? opts->slices : 0;
+        req.target_error = opts ? opts->target_error : 0.0;
+        SplitResult pres;
+        const int pst = device_product_host_panels(g, req, ctl, s, r.ws, &pres, &err);
+        if (pst == GB300_OK) {
+            done = true;
+            used = pres.method_used;
+            info_dev = pres.info_dev;
+        } else if (pst != GB300_ERR_NOT_SUPPORTED) {
+            return fail(pst, err);
+        } else {
+            err.clear();
+        }
+    }
+
     Stored sa{g.A, g.ta ? g.k : g.m, g.ta ? g.m : g.k, g.lda};
     Stored sb{g.B, g.tb ? g.n : g.k, g.tb ? g.k : g.n, g.ldb};
     Stored sc{g.C, g.m, g.n, g.ldc};
     Stored da = sa, db = sb, dc = sc;
+    bool c_staged = false;
+    if (!done) {
     if (product) {
         if (!devA || !aligned_for_tma<T>(sa))
             if (!stage_in<T>(sa, kSlotA, !devA, s, &da, &err)) return fail(GB300_ERR_NO_MEMORY, err);
         if (!devB || !aligned_for_tma<T>(sb))
             if (!stage_in<T>(sb, kSlotB, !devB, s, &db, &err)) return fail(GB300_ERR_NO_MEMORY, err);
     }
-    bool c_staged = false;
     if (!devC) {
         c_staged = true;
         const int64_t ldp = padded_ld(sc.cols, sizeof(T));
@@ -205,18 +240,6 @@ int gemm_entry(int order, int transA, int transB, int64_t m, int64_t n, int64_t 
     g.C = const_cast<void*>(dc.ptr); g.ldc = dc.ld;
 
     // ---- run ----
-    LaunchCtl ctl;
-    ctl.status = r.d_status;
-    if (r.inject_stall_count > 0) {
-        --r.inject_stall_count;
-        ctl.inject_stall = 1;
-        ctl.wait_limit_ns = r.inject_limit_ns;
-    }
-    cudaMemsetAsync(r.d_status, 0, sizeof(int), s);
-
-    int used = method;
-    const void* info_dev = nullptr;
-    cudaError_t e = cudaSuccess;
     if (is_double && product && method != GB300_METHOD_NATIVE) {
         SplitRequest req;
         req.method = method;
@@ -253,6 +276,8 @@ int gemm_entry(int order, int transA, int transB, int64_t m, int64_t n, int64_t 
                               size_t(sc.rows), cudaMemcpyDeviceToHost, s);
         if (e != cudaSuccess) return fail(GB300_ERR_CUDA, std::string("copy of C back: ") + cudaGetErrorString(e));
     }
+    }  // !done
+    if (opts) opts->method_used = used;
     if (sync) {
         e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) return fail(GB300_ERR_CUDA, std::string("kernel failed: ") + cudaGetErrorString(e));

@@ -53,6 +53,11 @@ struct Runtime {
     std::atomic<int64_t> launches{0};
     int inject_stall_count = 0;
     uint64_t inject_limit_ns = 0;
+    // copy streams and events of the panel pipeline for host operands (created on first use)
+    cudaStream_t copy_in = nullptr, copy_out = nullptr;
+    static constexpr int kPipeEvents = 40;
+    cudaEvent_t pipe_ev[kPipeEvents] = {};
+    bool pipe_ready = false;
 };
 
 Runtime& runtime();

@@ -125,7 +125,10 @@ struct SplitInfo {
     double normA, normB;  // Frobenius norms
     double scaleA, scaleB;// ||2^e||_2, ||2^f||_2
     // CRT mode
-    int beta;             // operands are rounded to beta-bit integers per row / column
+    int beta;             // rows of A are rounded to beta-bit integers
+    int beta_b;           // columns of B are rounded to beta_b-bit integers (= beta unless B is sliced
+                          // ahead of A, in the panel pipeline for host operands)
+    double qmaxB;         // largest column sum of squares of B relative to 2^(2f)
 };
 
 // ---- pre-pass ------------------------------------------------------------------------------
@@ -446,6 +449,8 @@ __global__ void __launch_bounds__(1024) split_info_kernel(const int* __restrict_
             while (beta > -60 && need(beta) > have) --beta;
             r.slices = N;
             r.beta = beta;
+            r.beta_b = beta;
+            r.qmaxB = QB;
             // too few moduli for even the coarsest rounding: no bound
             r.bound = need(beta) > have ? __longlong_as_double(0x7ff0000000000000ll) : bnd(beta);
         } else if (mode == kExact) {
@@ -470,6 +475,127 @@ __global__ void __launch_bounds__(1024) split_info_kernel(const int* __restrict_
         }
         *info = r;
     }
+}
+
+// ---- panel pipeline (host operands): B is sliced ahead of A -----------------------------------
+// Block-wide statistics of one operand side from its row exponents e and relative sums of squares
+// q: Inf/NaN flag, largest exponent E, largest q, s = sum 2^(2(e-E)) and nrm = sum 2^(2(e-E)) q.
+struct SideStats {
+    int bad, E;
+    double Q, s, nrm;
+};
+
+__device__ SideStats side_stats(const int* __restrict__ e, const double* __restrict__ q, int64_t count, double* redd,
+                                int* redi) {
+    SideStats r;
+    int bad = 0, E = -100000;
+    double Q = 0;
+    for (int64_t i = threadIdx.x; i < count; i += blockDim.x) {
+        if (e[i] == kNonFinite) bad = 1;
+        else {
+            if (q[i] > 0.0) E = max(E, e[i]);
+            Q = fmax(Q, q[i]);
+        }
+    }
+    r.bad = block_max_int(bad, redi);
+    r.E = block_max_int(E, redi);
+    r.Q = __longlong_as_double(block_max_ll(__double_as_longlong(Q), reinterpret_cast<long long*>(redd)));
+    double sv = 0, nv = 0;
+    for (int64_t i = threadIdx.x; i < count; i += blockDim.x) {
+        if (e[i] == kNonFinite || q[i] <= 0.0) continue;
+        const double w = pow2i(2 * (e[i] - r.E));
+        sv += w;
+        nv += w * q[i];
+    }
+    r.s = block_sum(sv, redd);
+    r.nrm = block_sum(nv, redd);
+    return r;
+}
+
+// B's side alone: its norms, its largest column sum of squares and beta_b, the smallest beta with
+// 2^(-beta-1) r_B <= target / 2 (half of the bound for B's rounding, the other half left to A's);
+// `slices` = the number of residue planes B is sliced into (the host's largest modulus count).
+__global__ void __launch_bounds__(1024) split_side_b_kernel(const int* __restrict__ eB, const double* __restrict__ qB,
+                                                            int64_t n, int64_t k, int planes, double target,
+                                                            SplitInfo* info_b) {
+    __shared__ double redd[32];
+    __shared__ int redi[32];
+    const SideStats b = side_stats(eB, qB, n, redd, redi);
+    if (threadIdx.x == 0) {
+        SplitInfo r;
+        r.nonfinite = b.bad;
+        r.normA = r.scaleA = 0.0;
+        r.normB = (b.nrm > 0) ? ldexp(sqrt(b.nrm), b.E) : 0.0;
+        r.scaleB = (b.s > 0) ? ldexp(sqrt(b.s), b.E) : 0.0;
+        r.qmaxB = b.Q;
+        const double rB = (b.nrm > 0) ? sqrt(double(k) * b.s / b.nrm) : 0.0;
+        int beta = 1;
+        while (beta < 55 && pow2i(-beta - 1) * rB > 0.5 * target) ++beta;
+        r.beta = r.beta_b = beta;
+        r.slices = planes;
+        r.bound = 0.0;
+        *info_b = r;
+    }
+}
+
+// One row panel of A against the pre-sliced B: A's side statistics, then the smallest beta_a with
+// 2^(-beta_a-1) r_A + 2^(-beta_b-1) r_B + 2^(-beta_a-beta_b-2) r_A r_B + 2^-52 <= target, the moduli
+// (as in split_info_kernel, with the two scalings), and beta_a raised to what the moduli carry.
+// The panel's normwise bound is relative to ||A_panel|| ||B||.
+__global__ void __launch_bounds__(1024) split_panel_kernel(const int* __restrict__ eA, const double* __restrict__ qA,
+                                                           int64_t m, int64_t k, int cap_planes, double target,
+                                                           const SplitInfo* __restrict__ info_b, SplitInfo* info) {
+    __shared__ double redd[32];
+    __shared__ int redi[32];
+    const SideStats a = side_stats(eA, qA, m, redd, redi);
+    if (threadIdx.x == 0) {
+        const SplitInfo ib = *info_b;
+        SplitInfo r;
+        r.nonfinite = a.bad | ib.nonfinite;
+        r.normA = (a.nrm > 0) ? ldexp(sqrt(a.nrm), a.E) : 0.0;
+        r.scaleA = (a.s > 0) ? ldexp(sqrt(a.s), a.E) : 0.0;
+        r.normB = ib.normB;
+        r.scaleB = ib.scaleB;
+        r.qmaxB = ib.qmaxB;
+        const double rA = (a.nrm > 0) ? sqrt(double(k) * a.s / a.nrm) : 0.0;
+        const double rB = (ib.normB > 0) ? sqrt(double(k)) * ib.scaleB / ib.normB : 0.0;
+        const int bb = ib.beta_b;
+        auto bnd = [&](int ba) {
+            return pow2i(-ba - 1) * rA + pow2i(-bb - 1) * rB + pow2i(-ba - bb - 2) * rA * rB + pow2i(-52);
+        };
+        int ba = 1;
+        while (ba < 55 && bnd(ba) > target) ++ba;
+        const double hk = 0.5 * sqrt(double(k)), sqa = sqrt(a.Q * (1.0 + 0x1p-10)),
+                     sqb = sqrt(ib.qmaxB * (1.0 + 0x1p-10));
+        const double lb = log2(ldexp(sqb, bb) + hk);
+        auto need = [&](int x) { return 1.0875 + log2(ldexp(sqa, x) + hk) + lb; };
+        double have = 0.0;
+        int N = 0;
+        const double need0 = need(ba);
+        while (N < 2 || (N < cap_planes && have < need0)) {
+            have += log2(double(c_mod[N]));
+            ++N;
+        }
+        ba = 55;
+        while (ba > -60 && need(ba) > have) --ba;
+        r.slices = N;
+        r.beta = ba;
+        r.beta_b = bb;
+        r.bound = need(ba) > have ? __longlong_as_double(0x7ff0000000000000ll) : bnd(ba);
+        *info = r;
+    }
+}
+
+// Summary of the panels for the caller: the largest modulus count and bound.
+__global__ void split_panels_summary_kernel(const SplitInfo* __restrict__ infos, int count, SplitInfo* out) {
+    if (threadIdx.x != 0) return;
+    SplitInfo r = infos[0];
+    for (int i = 1; i < count; ++i) {
+        r.slices = max(r.slices, infos[i].slices);
+        r.bound = fmax(r.bound, infos[i].bound);
+        r.nonfinite |= infos[i].nonfinite;
+    }
+    *out = r;
 }
 
 // Digit planes: planes[a][r][p] (bf16, pitch kpad, plane stride rpad*kpad) for r < rpad, p < kpad;
@@ -617,8 +743,8 @@ __device__ __forceinline__ void slice_emit(const unsigned long long (&xv)[8], in
 // buffer keeps rows of 528 bytes with 16-byte chunk c of a row stored at c ^ (c >> 3), so that the
 // eight threads of a row read their chunks 4L + j from eight different bank groups.
 template <int mode>
-__device__ __forceinline__ void slice_rows(const double* __restrict__ X, int64_t R, int64_t K, int64_t sr, int64_t sp,
-                                           const int* __restrict__ rexp, const SplitInfo* __restrict__ info,
+__device__ __forceinline__ void slice_rows(int which, const double* __restrict__ X, int64_t R, int64_t K, int64_t sr,
+                                           int64_t sp, const int* __restrict__ rexp, const SplitInfo* __restrict__ info,
                                            __nv_bfloat16* __restrict__ planes, int64_t rpad, int64_t kpad, int by) {
     constexpr uint32_t ROWB = 528, BUF = 32 * ROWB;
     __shared__ __align__(16) unsigned char tbuf[2 * BUF];
@@ -631,7 +757,8 @@ __device__ __forceinline__ void slice_rows(const double* __restrict__ X, int64_t
         const uint32_t c = uint32_t(p_) >> 1;
         return uint32_t(r_) * ROWB + ((c ^ (c >> 3)) << 4) + ((uint32_t(p_) & 1u) << 3);
     };
-    const int sl = (mode == kExact || mode == kCrt) ? info->slices : 0, bt = (mode == kCrt) ? info->beta : 0;
+    const int sl = (mode == kExact || mode == kCrt) ? info->slices : 0;
+    const int bt = (mode == kCrt) ? (which ? info->beta_b : info->beta) : 0;
     const int e = (r < R) ? rexp[r] : 0;
     const bool bad = (mode == kExact || mode == kCrt) && e == kNonFinite;
     const int64_t pstride = rpad * kpad;
@@ -663,7 +790,7 @@ __global__ void __launch_bounds__(256, 3) slice_kernel(const OperandPair op, int
                                                        int64_t kpad) {
     const int w = blockIdx.y < op.yb0 ? 0 : 1;
     const int by = w ? int(blockIdx.y - op.yb0) : int(blockIdx.y);
-    slice_rows<MODE>(op.X[w], op.R[w], K, op.sr[w], op.sp[w], op.rexp[w], info, op.planes[w], op.rpad[w], kpad, by);
+    slice_rows<MODE>(w, op.X[w], op.R[w], K, op.sr[w], op.sp[w], op.rexp[w], info, op.planes[w], op.rpad[w], kpad, by);
 }
 
 // ---- level / pair schedule ---------------------------------------------------------------------
@@ -1193,7 +1320,7 @@ __global__ void combine_kernel(const int32_t* __restrict__ levels, int nseg, int
 #pragma unroll
         for (int cc = 0; cc < COMBINE_COLS; ++cc) fj[cc] = (j0 + cc < n) ? eB[j0 + cc] : 0;
         const uint16_t* res16 = reinterpret_cast<const uint16_t*>(levels);
-        const int scale = 2 * info->beta;
+        const int scale = info->beta + info->beta_b;
         switch (info->slices) {
 #define GB_CRT_CASE(NN) \
     case NN: crt_cols<NN>(res16, plane, off, nseg, max_levels, scale, ei, fj, v); break;
@@ -1584,4 +1711,203 @@ int device_product(const Gemm& g_in, const SplitRequest& req, const LaunchCtl& c
     return GB300_OK;
 }
 
+
+namespace {
+bool page_locked(const void* p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost;
+}
+
+bool pipe_init(Runtime& r, std::string* err) {
+    if (r.pipe_ready) return true;
+    if (cudaStreamCreateWithFlags(&r.copy_in, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&r.copy_out, cudaStreamNonBlocking) != cudaSuccess) {
+        if (err) *err = "copy stream creation failed";
+        return false;
+    }
+    for (int i = 0; i < Runtime::kPipeEvents; ++i)
+        if (cudaEventCreateWithFlags(&r.pipe_ev[i], cudaEventDisableTiming) != cudaSuccess) {
+            if (err) *err = "event creation failed";
+            return false;
+        }
+    r.pipe_ready = true;
+    return true;
+}
+}  // namespace
+
+int device_product_host_panels(const Gemm& g, const SplitRequest& req, const LaunchCtl& ctl, cudaStream_t st,
+                               Workspace& ws, SplitResult* out, std::string* err) {
+    Runtime& r = runtime();
+    const int64_t m = g.m, n = g.n, k = g.k;
+    if (k == 0 || req.method == GB300_METHOD_NATIVE || (req.method == GB300_METHOD_AUTO && auto_uses_native(g)) ||
+        req.max_sms > 0)
+        return GB300_ERR_NOT_SUPPORTED;
+    const SplitGeometry G = split_geometry(g, req, r.num_sms);
+    if (G.mode != kCrt) return GB300_ERR_NOT_SUPPORTED;
+    // row panels of about a quarter of A (at least 2048 rows, whole pair tiles), at most 16 panels
+    const int64_t Mp = std::max<int64_t>(2048, round_up((m + 3) / 4, TMP));
+    const int P = int((m + Mp - 1) / Mp);
+    if (P < 2 || P > 16 || !page_locked(g.A) || !page_locked(g.B) || !page_locked(g.C))
+        return GB300_ERR_NOT_SUPPORTED;
+    if (!pipe_init(r, err)) return GB300_ERR_CUDA;
+    Gemm gp = g;
+    gp.m = Mp;
+    const SplitGeometry Gp = split_geometry(gp, req, r.num_sms);
+    const int64_t mpad = Gp.mpad, npad = Gp.npad, kpad = Gp.kpad;
+    const int max_planes = Gp.max_planes, max_levels = Gp.max_levels, nseg = Gp.nseg;
+
+    // device copies of the operands in their stored shapes (dense pitch), C, planes, levels, statistics
+    const int64_t a_rows = g.ta ? k : m, a_cols = g.ta ? m : k;
+    const int64_t b_rows = g.tb ? n : k, b_cols = g.tb ? k : n;
+    auto* dA = static_cast<double*>(ws.get(kSlotA, size_t(a_rows) * size_t(a_cols) * 8, err));
+    auto* dB = static_cast<double*>(ws.get(kSlotB, size_t(b_rows) * size_t(b_cols) * 8, err));
+    auto* dC = static_cast<double*>(ws.get(kSlotC, size_t(m) * size_t(n) * 8, err));
+    auto* pa = static_cast<__nv_bfloat16*>(ws.get(kSlotSliceA, size_t(max_planes) * size_t(mpad) * size_t(kpad) * 2, err));
+    auto* pb = static_cast<__nv_bfloat16*>(ws.get(kSlotSliceB, size_t(max_planes) * size_t(npad) * size_t(kpad) * 2, err));
+    auto* lv = static_cast<int32_t*>(ws.get(kSlotLevels, size_t(nseg) * max_levels * size_t(mpad) * size_t(npad) * 4, err));
+    const int64_t off_sq = round_up((m + n) * int64_t(sizeof(int)), 256);
+    const int64_t off_info = round_up(off_sq + (m + n) * int64_t(sizeof(double)), 256);
+    const size_t info_bytes = size_t(P + 2) * ((sizeof(SplitInfo) + 255) / 256) * 256;
+    auto* stats = static_cast<uint8_t*>(ws.get(kSlotScaleA, size_t(off_info) + info_bytes, err));
+    auto* racc = static_cast<RowAcc*>(ws.get(kSlotScaleB, size_t(m + n) * sizeof(RowAcc), err));
+    if (!dA || !dB || !dC || !pa || !pb || !lv || !stats || !racc) return GB300_ERR_NO_MEMORY;
+    int* eA = reinterpret_cast<int*>(stats);
+    int* eB = eA + m;
+    double* sqA = reinterpret_cast<double*>(stats + off_sq);
+    double* sqB = sqA + m;
+    const size_t info_stride = ((sizeof(SplitInfo) + 255) / 256) * 256;
+    auto info_at = [&](int i) { return reinterpret_cast<SplitInfo*>(stats + off_info + size_t(i) * info_stride); };
+    SplitInfo* infoB = info_at(P);
+    SplitInfo* info_sum = info_at(P + 1);
+    const double target = req.target_error > 0 ? req.target_error : double(k) * 0x1p-53;
+    cudaEvent_t* ev = r.pipe_ev;  // [0] B in, [1..P] panels in, [P+1..2P] panels computed, [2P+1] all out
+    auto cuda_fail = [&](const char* what, cudaError_t e) {
+        if (err) *err = std::string(what) + ": " + cudaGetErrorString(e);
+        return GB300_ERR_CUDA;
+    };
+
+    // ---- B: copy in, statistics, slicing for max_planes moduli with its own beta ----
+    cudaError_t e = cudaMemcpy2DAsync(dB, size_t(b_cols) * 8, g.B, size_t(g.ldb) * 8, size_t(b_cols) * 8,
+                                      size_t(b_rows), cudaMemcpyHostToDevice, r.copy_in);
+    if (e != cudaSuccess) return cuda_fail("copy of B", e);
+    cudaEventRecord(ev[0], r.copy_in);
+    cudaMemsetAsync(racc, 0, size_t(m + n) * sizeof(RowAcc), st);
+    cudaStreamWaitEvent(st, ev[0], 0);
+    const int64_t b_sr = g.tb ? b_cols : 1, b_sp = g.tb ? 1 : b_cols;
+    OperandPair ob;
+    ob.X[0] = dA; ob.X[1] = dB;
+    ob.R[0] = 0; ob.R[1] = n;
+    ob.sr[0] = 1; ob.sr[1] = b_sr;
+    ob.sp[0] = 1; ob.sp[1] = b_sp;
+    ob.acc[0] = racc; ob.acc[1] = racc + m;
+    ob.rexp[0] = eA; ob.rexp[1] = eB;
+    ob.rsq[0] = sqA; ob.rsq[1] = sqB;
+    ob.planes[0] = pa; ob.planes[1] = pb;
+    ob.rpad[0] = 0; ob.rpad[1] = npad;
+    ob.yb0 = 0;
+    const unsigned ktiles = unsigned(((k + 63) / 64 + TILE_KT - 1) / TILE_KT);
+    stats_tile_kernel<<<dim3(ktiles, unsigned((n + 31) / 32)), 256, 0, st>>>(ob, k);
+    stats_finalize_pair_kernel<<<unsigned((n + 255) / 256), 256, 0, st>>>(ob, k, 0u);
+    split_side_b_kernel<<<1, 1024, 0, st>>>(eB, sqB, n, k, max_planes, target, infoB);
+    slice_kernel<kCrt><<<dim3(unsigned((kpad / 64 + TILE_KT - 1) / TILE_KT), unsigned(npad / 32)), 256, 0, st>>>(
+        ob, k, infoB, kpad);
+    count_launches(4);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail("slicing of B", e);
+
+    // ---- tensor maps shared by the panels ----
+    CUtensorMap tA, tB, tC;
+    if (!encode_tmap_2d(&tA, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, pa, uint64_t(max_planes) * mpad, kpad, kpad, TM, TK,
+                        CU_TENSOR_MAP_SWIZZLE_128B, err) ||
+        !encode_tmap_2d(&tB, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, pb, uint64_t(max_planes) * npad, kpad, kpad, TNH, TK,
+                        CU_TENSOR_MAP_SWIZZLE_128B, err) ||
+        !encode_tmap_2d(&tC, CU_TENSOR_MAP_DATA_TYPE_UINT16, 2, lv, uint64_t(nseg) * max_levels * mpad, npad, npad, 32,
+                        64, CU_TENSOR_MAP_SWIZZLE_128B, err))
+        return GB300_ERR_CUDA;
+    e = cudaFuncSetAttribute(tc_gemm_kernel<kExact>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kTcSmem));
+    if (e != cudaSuccess) return cuda_fail("tc_gemm_kernel smem attribute", e);
+
+    // ---- A in row panels: copies run ahead on copy_in; C's rows go back on copy_out ----
+    const double* hA = static_cast<const double*>(g.A);
+    double* hC = static_cast<double*>(g.C);
+    for (int i = 0; i < P; ++i) {
+        const int64_t r0 = int64_t(i) * Mp, mi = std::min(Mp, m - r0);
+        if (g.ta)  // columns r0.. of the stored k x m operand
+            e = cudaMemcpy2DAsync(dA + r0, size_t(a_cols) * 8, hA + r0, size_t(g.lda) * 8, size_t(mi) * 8, size_t(k),
+                                  cudaMemcpyHostToDevice, r.copy_in);
+        else
+            e = cudaMemcpy2DAsync(dA + r0 * a_cols, size_t(a_cols) * 8, hA + r0 * g.lda, size_t(g.lda) * 8,
+                                  size_t(k) * 8, size_t(mi), cudaMemcpyHostToDevice, r.copy_in);
+        if (e == cudaSuccess && g.beta != 0.0)
+            e = cudaMemcpy2DAsync(dC + r0 * n, size_t(n) * 8, hC + r0 * g.ldc, size_t(g.ldc) * 8, size_t(n) * 8,
+                                  size_t(mi), cudaMemcpyHostToDevice, r.copy_in);
+        if (e != cudaSuccess) return cuda_fail("copy of A", e);
+        cudaEventRecord(ev[1 + i], r.copy_in);
+    }
+    const int64_t a_sr = g.ta ? 1 : a_cols, a_sp = g.ta ? a_cols : 1;
+    for (int i = 0; i < P; ++i) {
+        const int64_t r0 = int64_t(i) * Mp, mi = std::min(Mp, m - r0);
+        SplitInfo* info = info_at(i);
+        cudaStreamWaitEvent(st, ev[1 + i], 0);
+        OperandPair oa = ob;
+        oa.X[0] = g.ta ? dA + r0 : dA + r0 * a_cols;
+        oa.R[0] = mi; oa.R[1] = 0;
+        oa.sr[0] = a_sr; oa.sp[0] = a_sp;
+        oa.acc[0] = racc + r0;
+        oa.rexp[0] = eA + r0;
+        oa.rsq[0] = sqA + r0;
+        oa.rpad[0] = mpad;
+        oa.yb0 = unsigned((mi + 31) / 32);
+        stats_tile_kernel<<<dim3(ktiles, oa.yb0), 256, 0, st>>>(oa, k);
+        const unsigned xb0 = unsigned((mi + 255) / 256);
+        stats_finalize_pair_kernel<<<xb0, 256, 0, st>>>(oa, k, xb0);
+        split_panel_kernel<<<1, 1024, 0, st>>>(eA + r0, sqA + r0, mi, k, max_planes, target, infoB, info);
+        oa.yb0 = unsigned(mpad / 32);
+        slice_kernel<kCrt><<<dim3(unsigned((kpad / 64 + TILE_KT - 1) / TILE_KT), oa.yb0), 256, 0, st>>>(oa, k, info, kpad);
+        TcParams tp;
+        tp.mode = kCrt;
+        tp.m_tiles = int((mi + TMP - 1) / TMP);
+        tp.n_tiles = Gp.n_tiles;
+        tp.nseg = nseg;
+        tp.kb_per_seg = int(Gp.kseg / TK);
+        tp.kb_total = Gp.kb_total;
+        tp.mpad = mpad;
+        tp.npad = npad;
+        tp.levels = lv;
+        tp.max_levels = max_levels;
+        tp.info = info;
+        tp.status = ctl.status;
+        tp.limit_ns = ctl.wait_limit_ns;
+        tp.inject_stall = ctl.inject_stall;
+        const int units = tp.m_tiles * tp.n_tiles * nseg * max_levels;
+        const int grid = 2 * std::max(1, std::min(units, r.num_sms / 2));
+        {
+            KernelTimer timer("tc_gemm", st);
+            tc_gemm_kernel<kExact><<<grid, THREADS, kTcSmem, st>>>(tA, tB, tC, tp);
+        }
+        const int64_t colgroups = (n + COMBINE_COLS - 1) / COMBINE_COLS;
+        combine_kernel<<<dim3(unsigned((colgroups + 127) / 128), unsigned(std::min<int64_t>(mi, 65535))), 128, 0, st>>>(
+            lv, nseg, max_levels, mpad, npad, kCrt, info, eA + r0, eB, mi, n, g.alpha, g.beta, dC + r0 * n, n);
+        count_launches(6);
+        if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail("panel launch", e);
+        cudaEventRecord(ev[1 + P + i], st);
+        cudaStreamWaitEvent(r.copy_out, ev[1 + P + i], 0);
+        e = cudaMemcpy2DAsync(hC + r0 * g.ldc, size_t(g.ldc) * 8, dC + r0 * n, size_t(n) * 8, size_t(n) * 8,
+                              size_t(mi), cudaMemcpyDeviceToHost, r.copy_out);
+        if (e != cudaSuccess) return cuda_fail("copy of C back", e);
+    }
+    split_panels_summary_kernel<<<1, 32, 0, st>>>(info_at(0), P, info_sum);
+    count_launches(1);
+    cudaEventRecord(ev[2 * P + 1], r.copy_out);
+    cudaStreamWaitEvent(st, ev[2 * P + 1], 0);  // the call's work ends on st
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail("panel pipeline", e);
+    out->method_used = GB300_METHOD_SPLIT_CRT;
+    out->slices = -1;
+    out->error_bound = -1.0;
+    out->info_dev = info_sum;
+    return GB300_OK;
+}
 }  // namespace gb
