@@ -129,6 +129,7 @@ struct SplitInfo {
     int beta_b;           // columns of B are rounded to beta_b-bit integers (= beta unless B is sliced
                           // ahead of A, in the panel pipeline for host operands)
     double qmaxB;         // largest column sum of squares of B relative to 2^(2f)
+    double qmaxA;         // largest row sum of squares of A relative to 2^(2e) (block pipeline)
 };
 
 // ---- pre-pass ------------------------------------------------------------------------------
@@ -512,88 +513,81 @@ __device__ SideStats side_stats(const int* __restrict__ e, const double* __restr
     return r;
 }
 
-// B's side alone: its norms, its largest column sum of squares and beta_b, the smallest beta with
-// 2^(-beta-1) r_B <= target / 2 (half of the bound for B's rounding, the other half left to A's);
-// `slices` = the number of residue planes B is sliced into (the host's largest modulus count).
-__global__ void __launch_bounds__(1024) split_side_b_kernel(const int* __restrict__ eB, const double* __restrict__ qB,
-                                                            int64_t n, int64_t k, int planes, double target,
-                                                            SplitInfo* info_b) {
+// One operand side of a block of the host pipeline (a row panel of A or a column block of B): its
+// norms and largest relative sum of squares (stored in both the A and the B fields), and the
+// smallest beta with 2^(-beta-1) r <= target / 2: each side takes half of the bound for its own
+// rounding, so the two sides are sliced independently.  `slices` = the planes the side is sliced
+// into (the host's largest modulus count).
+__global__ void __launch_bounds__(1024) split_side_kernel(const int* __restrict__ e, const double* __restrict__ q,
+                                                          int64_t count, int64_t k, int planes, double target,
+                                                          SplitInfo* out) {
     __shared__ double redd[32];
     __shared__ int redi[32];
-    const SideStats b = side_stats(eB, qB, n, redd, redi);
+    const SideStats t = side_stats(e, q, count, redd, redi);
     if (threadIdx.x == 0) {
         SplitInfo r;
-        r.nonfinite = b.bad;
-        r.normA = r.scaleA = 0.0;
-        r.normB = (b.nrm > 0) ? ldexp(sqrt(b.nrm), b.E) : 0.0;
-        r.scaleB = (b.s > 0) ? ldexp(sqrt(b.s), b.E) : 0.0;
-        r.qmaxB = b.Q;
-        const double rB = (b.nrm > 0) ? sqrt(double(k) * b.s / b.nrm) : 0.0;
+        r.nonfinite = t.bad;
+        r.normA = r.normB = (t.nrm > 0) ? ldexp(sqrt(t.nrm), t.E) : 0.0;
+        r.scaleA = r.scaleB = (t.s > 0) ? ldexp(sqrt(t.s), t.E) : 0.0;
+        r.qmaxA = r.qmaxB = t.Q;
+        const double rr = (t.nrm > 0) ? sqrt(double(k) * t.s / t.nrm) : 0.0;
         int beta = 1;
-        while (beta < 55 && pow2i(-beta - 1) * rB > 0.5 * target) ++beta;
+        while (beta < 55 && pow2i(-beta - 1) * rr > 0.5 * target) ++beta;
         r.beta = r.beta_b = beta;
         r.slices = planes;
         r.bound = 0.0;
-        *info_b = r;
+        *out = r;
     }
 }
 
-// One row panel of A against the pre-sliced B: A's side statistics, then the smallest beta_a with
-// 2^(-beta_a-1) r_A + 2^(-beta_b-1) r_B + 2^(-beta_a-beta_b-2) r_A r_B + 2^-52 <= target, the moduli
-// (as in split_info_kernel, with the two scalings), and beta_a raised to what the moduli carry.
-// The panel's normwise bound is relative to ||A_panel|| ||B||.
-__global__ void __launch_bounds__(1024) split_panel_kernel(const int* __restrict__ eA, const double* __restrict__ qA,
-                                                           int64_t m, int64_t k, int cap_planes, double target,
-                                                           const SplitInfo* __restrict__ info_b, SplitInfo* info) {
-    __shared__ double redd[32];
-    __shared__ int redi[32];
-    const SideStats a = side_stats(eA, qA, m, redd, redi);
-    if (threadIdx.x == 0) {
-        const SplitInfo ib = *info_b;
-        SplitInfo r;
-        r.nonfinite = a.bad | ib.nonfinite;
-        r.normA = (a.nrm > 0) ? ldexp(sqrt(a.nrm), a.E) : 0.0;
-        r.scaleA = (a.s > 0) ? ldexp(sqrt(a.s), a.E) : 0.0;
-        r.normB = ib.normB;
-        r.scaleB = ib.scaleB;
-        r.qmaxB = ib.qmaxB;
-        const double rA = (a.nrm > 0) ? sqrt(double(k) * a.s / a.nrm) : 0.0;
-        const double rB = (ib.normB > 0) ? sqrt(double(k)) * ib.scaleB / ib.normB : 0.0;
-        const int bb = ib.beta_b;
-        auto bnd = [&](int ba) {
-            return pow2i(-ba - 1) * rA + pow2i(-bb - 1) * rB + pow2i(-ba - bb - 2) * rA * rB + pow2i(-52);
-        };
-        int ba = 1;
-        while (ba < 55 && bnd(ba) > target) ++ba;
-        const double hk = 0.5 * sqrt(double(k)), sqa = sqrt(a.Q * (1.0 + 0x1p-10)),
-                     sqb = sqrt(ib.qmaxB * (1.0 + 0x1p-10));
-        const double lb = log2(ldexp(sqb, bb) + hk);
-        auto need = [&](int x) { return 1.0875 + log2(ldexp(sqa, x) + hk) + lb; };
-        double have = 0.0;
-        int N = 0;
-        const double need0 = need(ba);
-        while (N < 2 || (N < cap_planes && have < need0)) {
-            have += log2(double(c_mod[N]));
-            ++N;
-        }
-        ba = 55;
-        while (ba > -60 && need(ba) > have) --ba;
-        r.slices = N;
-        r.beta = ba;
-        r.beta_b = bb;
-        r.bound = need(ba) > have ? __longlong_as_double(0x7ff0000000000000ll) : bnd(ba);
-        *info = r;
-    }
-}
-
-// Summary of the panels for the caller: the largest modulus count and bound.
-__global__ void split_panels_summary_kernel(const SplitInfo* __restrict__ infos, int count, SplitInfo* out) {
+// A block (row panel i of A, column block j of B) from the two sides: the moduli that carry
+// (2^beta_a sqrt(Q_A) + sqrt(k)/2)(2^beta_b sqrt(Q_B) + sqrt(k)/2) with the margin of
+// split_info_kernel, and the block's bound 2^(-beta_a-1) r_A + 2^(-beta_b-1) r_B +
+// 2^(-beta_a-beta_b-2) r_A r_B + 2^-52 relative to ||A_i|| ||B_j|| (infinite when even cap_planes
+// moduli are too few).
+__global__ void split_block_kernel(const SplitInfo* __restrict__ ia, const SplitInfo* __restrict__ ib, int64_t k,
+                                   int cap_planes, SplitInfo* out) {
     if (threadIdx.x != 0) return;
-    SplitInfo r = infos[0];
+    const SplitInfo A = *ia, B = *ib;
+    SplitInfo r;
+    r.nonfinite = A.nonfinite | B.nonfinite;
+    r.normA = A.normA;
+    r.scaleA = A.scaleA;
+    r.qmaxA = A.qmaxA;
+    r.normB = B.normB;
+    r.scaleB = B.scaleB;
+    r.qmaxB = B.qmaxB;
+    const double rA = (A.normA > 0) ? sqrt(double(k)) * A.scaleA / A.normA : 0.0;
+    const double rB = (B.normB > 0) ? sqrt(double(k)) * B.scaleB / B.normB : 0.0;
+    const int ba = A.beta, bb = B.beta_b;
+    const double hk = 0.5 * sqrt(double(k));
+    const double need = 1.0875 + log2(ldexp(sqrt(A.qmaxA * (1.0 + 0x1p-10)), ba) + hk) +
+                        log2(ldexp(sqrt(B.qmaxB * (1.0 + 0x1p-10)), bb) + hk);
+    double have = 0.0;
+    int N = 0;
+    while (N < 2 || (N < cap_planes && have < need)) {
+        have += log2(double(c_mod[N]));
+        ++N;
+    }
+    r.slices = N;
+    r.beta = ba;
+    r.beta_b = bb;
+    r.bound = need > have ? __longlong_as_double(0x7ff0000000000000ll)
+                          : pow2i(-ba - 1) * rA + pow2i(-bb - 1) * rB + pow2i(-ba - bb - 2) * rA * rB + pow2i(-52);
+    *out = r;
+}
+
+// Summary of the blocks for the caller: the largest modulus count and bound (infos `stride` bytes
+// apart).
+__global__ void split_panels_summary_kernel(const uint8_t* __restrict__ infos, size_t stride, int count,
+                                            SplitInfo* out) {
+    if (threadIdx.x != 0) return;
+    SplitInfo r = *reinterpret_cast<const SplitInfo*>(infos);
     for (int i = 1; i < count; ++i) {
-        r.slices = max(r.slices, infos[i].slices);
-        r.bound = fmax(r.bound, infos[i].bound);
-        r.nonfinite |= infos[i].nonfinite;
+        const SplitInfo& x = *reinterpret_cast<const SplitInfo*>(infos + size_t(i) * stride);
+        r.slices = max(r.slices, x.slices);
+        r.bound = fmax(r.bound, x.bound);
+        r.nonfinite |= x.nonfinite;
     }
     *out = r;
 }
@@ -1744,20 +1738,26 @@ int device_product_host_panels(const Gemm& g, const SplitRequest& req, const Lau
     Runtime& r = runtime();
     const int64_t m = g.m, n = g.n, k = g.k;
     if (k == 0 || req.method == GB300_METHOD_NATIVE || (req.method == GB300_METHOD_AUTO && auto_uses_native(g)) ||
-        req.max_sms > 0)
+        req.max_sms > 0 || req.slices > 0)
         return GB300_ERR_NOT_SUPPORTED;
     const SplitGeometry G = split_geometry(g, req, r.num_sms);
     if (G.mode != kCrt) return GB300_ERR_NOT_SUPPORTED;
-    // row panels of about a quarter of A (at least 2048 rows, whole pair tiles), at most 16 panels
+    // blocks: row panels of about a quarter of A (at least 2048 rows) and two column blocks of B
+    // (when each has at least 2048 columns), whole pair tiles
     const int64_t Mp = std::max<int64_t>(2048, round_up((m + 3) / 4, TMP));
     const int P = int((m + Mp - 1) / Mp);
+    const int64_t Nq = n >= 4096 ? round_up((n + 1) / 2, TN) : round_up(n, TN);
+    const int Q = int((n + Nq - 1) / Nq);
     if (P < 2 || P > 16 || !page_locked(g.A) || !page_locked(g.B) || !page_locked(g.C))
         return GB300_ERR_NOT_SUPPORTED;
     if (!pipe_init(r, err)) return GB300_ERR_CUDA;
     Gemm gp = g;
     gp.m = Mp;
+    gp.n = Nq;
     const SplitGeometry Gp = split_geometry(gp, req, r.num_sms);
-    const int64_t mpad = Gp.mpad, npad = Gp.npad, kpad = Gp.kpad;
+    const int64_t mpad = Gp.mpad, kpad = Gp.kpad;
+    // B planes block-major: block j holds its max_planes planes of Nq rows, so a block reads like a
+    // whole B of Nq columns (plane stride Nq * kpad)
     const int max_planes = Gp.max_planes, max_levels = Gp.max_levels, nseg = Gp.nseg;
 
     // device copies of the operands in their stored shapes (dense pitch), C, planes, levels, statistics
@@ -1767,73 +1767,38 @@ int device_product_host_panels(const Gemm& g, const SplitRequest& req, const Lau
     auto* dB = static_cast<double*>(ws.get(kSlotB, size_t(b_rows) * size_t(b_cols) * 8, err));
     auto* dC = static_cast<double*>(ws.get(kSlotC, size_t(m) * size_t(n) * 8, err));
     auto* pa = static_cast<__nv_bfloat16*>(ws.get(kSlotSliceA, size_t(max_planes) * size_t(mpad) * size_t(kpad) * 2, err));
-    auto* pb = static_cast<__nv_bfloat16*>(ws.get(kSlotSliceB, size_t(max_planes) * size_t(npad) * size_t(kpad) * 2, err));
-    auto* lv = static_cast<int32_t*>(ws.get(kSlotLevels, size_t(nseg) * max_levels * size_t(mpad) * size_t(npad) * 4, err));
+    const size_t bblock = size_t(max_planes) * size_t(Nq) * size_t(kpad);  // elements per B block
+    auto* pb = static_cast<__nv_bfloat16*>(ws.get(kSlotSliceB, size_t(Q) * bblock * 2, err));
+    auto* lv = static_cast<int32_t*>(ws.get(kSlotLevels, size_t(nseg) * max_levels * size_t(mpad) * size_t(Nq) * 4, err));
     const int64_t off_sq = round_up((m + n) * int64_t(sizeof(int)), 256);
     const int64_t off_info = round_up(off_sq + (m + n) * int64_t(sizeof(double)), 256);
-    const size_t info_bytes = size_t(P + 2) * ((sizeof(SplitInfo) + 255) / 256) * 256;
-    auto* stats = static_cast<uint8_t*>(ws.get(kSlotScaleA, size_t(off_info) + info_bytes, err));
+    const int ninfo = P + Q + P * Q + 1;
+    const size_t info_stride = ((sizeof(SplitInfo) + 255) / 256) * 256;
+    auto* stats = static_cast<uint8_t*>(ws.get(kSlotScaleA, size_t(off_info) + size_t(ninfo) * info_stride, err));
     auto* racc = static_cast<RowAcc*>(ws.get(kSlotScaleB, size_t(m + n) * sizeof(RowAcc), err));
     if (!dA || !dB || !dC || !pa || !pb || !lv || !stats || !racc) return GB300_ERR_NO_MEMORY;
     int* eA = reinterpret_cast<int*>(stats);
     int* eB = eA + m;
     double* sqA = reinterpret_cast<double*>(stats + off_sq);
     double* sqB = sqA + m;
-    const size_t info_stride = ((sizeof(SplitInfo) + 255) / 256) * 256;
     auto info_at = [&](int i) { return reinterpret_cast<SplitInfo*>(stats + off_info + size_t(i) * info_stride); };
-    SplitInfo* infoB = info_at(P);
-    SplitInfo* info_sum = info_at(P + 1);
+    // infos: [0, P) panels of A, [P, P+Q) blocks of B, [P+Q, P+Q+PQ) blocks of C, last: summary
+    SplitInfo* info_sum = info_at(ninfo - 1);
     const double target = req.target_error > 0 ? req.target_error : double(k) * 0x1p-53;
-    cudaEvent_t* ev = r.pipe_ev;  // [0] B in, [1..P] panels in, [P+1..2P] panels computed, [2P+1] all out
+    // events: [0, P) A panels in, [P, P+Q) B blocks in, [P+Q, P+Q+PQ) C blocks computed, last: all out
+    cudaEvent_t* ev = r.pipe_ev;
+    if (P + Q + P * Q + 1 > Runtime::kPipeEvents) return GB300_ERR_NOT_SUPPORTED;
     auto cuda_fail = [&](const char* what, cudaError_t e) {
         if (err) *err = std::string(what) + ": " + cudaGetErrorString(e);
         return GB300_ERR_CUDA;
     };
-
-    // ---- B: copy in, statistics, slicing for max_planes moduli with its own beta ----
-    cudaError_t e = cudaMemcpy2DAsync(dB, size_t(b_cols) * 8, g.B, size_t(g.ldb) * 8, size_t(b_cols) * 8,
-                                      size_t(b_rows), cudaMemcpyHostToDevice, r.copy_in);
-    if (e != cudaSuccess) return cuda_fail("copy of B", e);
-    cudaEventRecord(ev[0], r.copy_in);
-    cudaMemsetAsync(racc, 0, size_t(m + n) * sizeof(RowAcc), st);
-    cudaStreamWaitEvent(st, ev[0], 0);
-    const int64_t b_sr = g.tb ? b_cols : 1, b_sp = g.tb ? 1 : b_cols;
-    OperandPair ob;
-    ob.X[0] = dA; ob.X[1] = dB;
-    ob.R[0] = 0; ob.R[1] = n;
-    ob.sr[0] = 1; ob.sr[1] = b_sr;
-    ob.sp[0] = 1; ob.sp[1] = b_sp;
-    ob.acc[0] = racc; ob.acc[1] = racc + m;
-    ob.rexp[0] = eA; ob.rexp[1] = eB;
-    ob.rsq[0] = sqA; ob.rsq[1] = sqB;
-    ob.planes[0] = pa; ob.planes[1] = pb;
-    ob.rpad[0] = 0; ob.rpad[1] = npad;
-    ob.yb0 = 0;
-    const unsigned ktiles = unsigned(((k + 63) / 64 + TILE_KT - 1) / TILE_KT);
-    stats_tile_kernel<<<dim3(ktiles, unsigned((n + 31) / 32)), 256, 0, st>>>(ob, k);
-    stats_finalize_pair_kernel<<<unsigned((n + 255) / 256), 256, 0, st>>>(ob, k, 0u);
-    split_side_b_kernel<<<1, 1024, 0, st>>>(eB, sqB, n, k, max_planes, target, infoB);
-    slice_kernel<kCrt><<<dim3(unsigned((kpad / 64 + TILE_KT - 1) / TILE_KT), unsigned(npad / 32)), 256, 0, st>>>(
-        ob, k, infoB, kpad);
-    count_launches(4);
-    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail("slicing of B", e);
-
-    // ---- tensor maps shared by the panels ----
-    CUtensorMap tA, tB, tC;
-    if (!encode_tmap_2d(&tA, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, pa, uint64_t(max_planes) * mpad, kpad, kpad, TM, TK,
-                        CU_TENSOR_MAP_SWIZZLE_128B, err) ||
-        !encode_tmap_2d(&tB, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, pb, uint64_t(max_planes) * npad, kpad, kpad, TNH, TK,
-                        CU_TENSOR_MAP_SWIZZLE_128B, err) ||
-        !encode_tmap_2d(&tC, CU_TENSOR_MAP_DATA_TYPE_UINT16, 2, lv, uint64_t(nseg) * max_levels * mpad, npad, npad, 32,
-                        64, CU_TENSOR_MAP_SWIZZLE_128B, err))
-        return GB300_ERR_CUDA;
-    e = cudaFuncSetAttribute(tc_gemm_kernel<kExact>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kTcSmem));
-    if (e != cudaSuccess) return cuda_fail("tc_gemm_kernel smem attribute", e);
-
-    // ---- A in row panels: copies run ahead on copy_in; C's rows go back on copy_out ----
     const double* hA = static_cast<const double*>(g.A);
+    const double* hB = static_cast<const double*>(g.B);
     double* hC = static_cast<double*>(g.C);
-    for (int i = 0; i < P; ++i) {
+
+    // ---- copies in, in the order the blocks need them: A_0, B_0 .. B_{Q-1}, A_1 .. A_{P-1} ----
+    cudaError_t e = cudaSuccess;
+    auto copy_a = [&](int i) {
         const int64_t r0 = int64_t(i) * Mp, mi = std::min(Mp, m - r0);
         if (g.ta)  // columns r0.. of the stored k x m operand
             e = cudaMemcpy2DAsync(dA + r0, size_t(a_cols) * 8, hA + r0, size_t(g.lda) * 8, size_t(mi) * 8, size_t(k),
@@ -1844,70 +1809,149 @@ int device_product_host_panels(const Gemm& g, const SplitRequest& req, const Lau
         if (e == cudaSuccess && g.beta != 0.0)
             e = cudaMemcpy2DAsync(dC + r0 * n, size_t(n) * 8, hC + r0 * g.ldc, size_t(g.ldc) * 8, size_t(n) * 8,
                                   size_t(mi), cudaMemcpyHostToDevice, r.copy_in);
-        if (e != cudaSuccess) return cuda_fail("copy of A", e);
-        cudaEventRecord(ev[1 + i], r.copy_in);
-    }
+        cudaEventRecord(ev[i], r.copy_in);
+    };
+    auto copy_b = [&](int j) {
+        const int64_t c0 = int64_t(j) * Nq, nj = std::min(Nq, n - c0);
+        if (g.tb)  // rows c0.. of the stored n x k operand
+            e = cudaMemcpy2DAsync(dB + c0 * b_cols, size_t(b_cols) * 8, hB + c0 * g.ldb, size_t(g.ldb) * 8,
+                                  size_t(k) * 8, size_t(nj), cudaMemcpyHostToDevice, r.copy_in);
+        else
+            e = cudaMemcpy2DAsync(dB + c0, size_t(b_cols) * 8, hB + c0, size_t(g.ldb) * 8, size_t(nj) * 8, size_t(k),
+                                  cudaMemcpyHostToDevice, r.copy_in);
+        cudaEventRecord(ev[P + j], r.copy_in);
+    };
+    copy_a(0);
+    for (int j = 0; j < Q && e == cudaSuccess; ++j) copy_b(j);
+    for (int i = 1; i < P && e == cudaSuccess; ++i) copy_a(i);
+    if (e != cudaSuccess) return cuda_fail("copy of an operand", e);
+
+    cudaMemsetAsync(racc, 0, size_t(m + n) * sizeof(RowAcc), st);
+    const unsigned ktiles = unsigned(((k + 63) / 64 + TILE_KT - 1) / TILE_KT);
+    const unsigned stiles = unsigned((kpad / 64 + TILE_KT - 1) / TILE_KT);
     const int64_t a_sr = g.ta ? 1 : a_cols, a_sp = g.ta ? a_cols : 1;
+    const int64_t b_sr = g.tb ? b_cols : 1, b_sp = g.tb ? 1 : b_cols;
+    OperandPair base;
+    base.X[0] = dA; base.X[1] = dB;
+    base.R[0] = 0; base.R[1] = 0;
+    base.sr[0] = a_sr; base.sr[1] = b_sr;
+    base.sp[0] = a_sp; base.sp[1] = b_sp;
+    base.acc[0] = racc; base.acc[1] = racc + m;
+    base.rexp[0] = eA; base.rexp[1] = eB;
+    base.rsq[0] = sqA; base.rsq[1] = sqB;
+    base.planes[0] = pa; base.planes[1] = pb;
+    base.rpad[0] = mpad; base.rpad[1] = Nq;
+    base.yb0 = 0;
+    // statistics, side scaling and planes of A's panel i (into the panel plane buffer)
+    auto prep_a = [&](int i) {
+        const int64_t r0 = int64_t(i) * Mp, mi = std::min(Mp, m - r0);
+        OperandPair o = base;
+        o.X[0] = g.ta ? dA + r0 : dA + r0 * a_cols;
+        o.R[0] = mi;
+        o.acc[0] = racc + r0;
+        o.rexp[0] = eA + r0;
+        o.rsq[0] = sqA + r0;
+        o.yb0 = unsigned((mi + 31) / 32);
+        stats_tile_kernel<<<dim3(ktiles, o.yb0), 256, 0, st>>>(o, k);
+        const unsigned xb0 = unsigned((mi + 255) / 256);
+        stats_finalize_pair_kernel<<<xb0, 256, 0, st>>>(o, k, xb0);
+        split_side_kernel<<<1, 1024, 0, st>>>(eA + r0, sqA + r0, mi, k, max_planes, target, info_at(i));
+        o.yb0 = unsigned(mpad / 32);
+        slice_kernel<kCrt><<<dim3(stiles, o.yb0), 256, 0, st>>>(o, k, info_at(i), kpad);
+        count_launches(4);
+    };
+    // statistics, side scaling and planes of B's column block j (rows j*Nq.. of the B planes)
+    auto prep_b = [&](int j) {
+        const int64_t c0 = int64_t(j) * Nq, nj = std::min(Nq, n - c0);
+        OperandPair o = base;
+        o.X[1] = g.tb ? dB + c0 * b_cols : dB + c0;
+        o.R[1] = nj;
+        o.acc[1] = racc + m + c0;
+        o.rexp[1] = eB + c0;
+        o.rsq[1] = sqB + c0;
+        o.planes[1] = pb + size_t(j) * bblock;
+        o.rpad[1] = Nq;
+        o.yb0 = 0;
+        stats_tile_kernel<<<dim3(ktiles, unsigned((nj + 31) / 32)), 256, 0, st>>>(o, k);
+        stats_finalize_pair_kernel<<<unsigned((nj + 255) / 256), 256, 0, st>>>(o, k, 0u);
+        split_side_kernel<<<1, 1024, 0, st>>>(eB + c0, sqB + c0, nj, k, max_planes, target, info_at(P + j));
+        slice_kernel<kCrt><<<dim3(stiles, unsigned(Nq / 32)), 256, 0, st>>>(o, k, info_at(P + j), kpad);
+        count_launches(4);
+    };
+
+    // ---- tensor maps: A panel planes, each B block's planes, the level planes of a block ----
+    CUtensorMap tA, tC, tB[2];  // Q <= 2
+    if (!encode_tmap_2d(&tA, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, pa, uint64_t(max_planes) * mpad, kpad, kpad, TM, TK,
+                        CU_TENSOR_MAP_SWIZZLE_128B, err) ||
+        !encode_tmap_2d(&tC, CU_TENSOR_MAP_DATA_TYPE_UINT16, 2, lv, uint64_t(nseg) * max_levels * mpad, Nq, Nq, 32, 64,
+                        CU_TENSOR_MAP_SWIZZLE_128B, err))
+        return GB300_ERR_CUDA;
+    for (int j = 0; j < Q; ++j)
+        if (!encode_tmap_2d(&tB[j], CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, pb + size_t(j) * bblock,
+                            uint64_t(max_planes) * Nq, kpad, kpad, TNH, TK, CU_TENSOR_MAP_SWIZZLE_128B, err))
+            return GB300_ERR_CUDA;
+    e = cudaFuncSetAttribute(tc_gemm_kernel<kExact>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kTcSmem));
+    if (e != cudaSuccess) return cuda_fail("tc_gemm_kernel smem attribute", e);
+
+    // ---- blocks in row-major order: panel i's planes serve its Q blocks; C goes back per block ----
+    int nb = 0;
     for (int i = 0; i < P; ++i) {
         const int64_t r0 = int64_t(i) * Mp, mi = std::min(Mp, m - r0);
-        SplitInfo* info = info_at(i);
-        cudaStreamWaitEvent(st, ev[1 + i], 0);
-        OperandPair oa = ob;
-        oa.X[0] = g.ta ? dA + r0 : dA + r0 * a_cols;
-        oa.R[0] = mi; oa.R[1] = 0;
-        oa.sr[0] = a_sr; oa.sp[0] = a_sp;
-        oa.acc[0] = racc + r0;
-        oa.rexp[0] = eA + r0;
-        oa.rsq[0] = sqA + r0;
-        oa.rpad[0] = mpad;
-        oa.yb0 = unsigned((mi + 31) / 32);
-        stats_tile_kernel<<<dim3(ktiles, oa.yb0), 256, 0, st>>>(oa, k);
-        const unsigned xb0 = unsigned((mi + 255) / 256);
-        stats_finalize_pair_kernel<<<xb0, 256, 0, st>>>(oa, k, xb0);
-        split_panel_kernel<<<1, 1024, 0, st>>>(eA + r0, sqA + r0, mi, k, max_planes, target, infoB, info);
-        oa.yb0 = unsigned(mpad / 32);
-        slice_kernel<kCrt><<<dim3(unsigned((kpad / 64 + TILE_KT - 1) / TILE_KT), oa.yb0), 256, 0, st>>>(oa, k, info, kpad);
-        TcParams tp;
-        tp.mode = kCrt;
-        tp.m_tiles = int((mi + TMP - 1) / TMP);
-        tp.n_tiles = Gp.n_tiles;
-        tp.nseg = nseg;
-        tp.kb_per_seg = int(Gp.kseg / TK);
-        tp.kb_total = Gp.kb_total;
-        tp.mpad = mpad;
-        tp.npad = npad;
-        tp.levels = lv;
-        tp.max_levels = max_levels;
-        tp.info = info;
-        tp.status = ctl.status;
-        tp.limit_ns = ctl.wait_limit_ns;
-        tp.inject_stall = ctl.inject_stall;
-        const int units = tp.m_tiles * tp.n_tiles * nseg * max_levels;
-        const int grid = 2 * std::max(1, std::min(units, r.num_sms / 2));
-        {
-            KernelTimer timer("tc_gemm", st);
-            tc_gemm_kernel<kExact><<<grid, THREADS, kTcSmem, st>>>(tA, tB, tC, tp);
+        cudaStreamWaitEvent(st, ev[i], 0);
+        prep_a(i);
+        for (int j = 0; j < Q; ++j, ++nb) {
+            const int64_t c0 = int64_t(j) * Nq, nj = std::min(Nq, n - c0);
+            if (i == 0) {
+                cudaStreamWaitEvent(st, ev[P + j], 0);
+                prep_b(j);
+            }
+            SplitInfo* info = info_at(P + Q + nb);
+            split_block_kernel<<<1, 32, 0, st>>>(info_at(i), info_at(P + j), k, max_planes, info);
+            TcParams tp;
+            tp.mode = kCrt;
+            tp.m_tiles = int((mi + TMP - 1) / TMP);
+            tp.n_tiles = int((nj + TN - 1) / TN);
+            tp.nseg = nseg;
+            tp.kb_per_seg = int(Gp.kseg / TK);
+            tp.kb_total = Gp.kb_total;
+            tp.mpad = mpad;
+            tp.npad = Nq;
+            tp.levels = lv;
+            tp.max_levels = max_levels;
+            tp.info = info;
+            tp.status = ctl.status;
+            tp.limit_ns = ctl.wait_limit_ns;
+            tp.inject_stall = ctl.inject_stall;
+            const int units = tp.m_tiles * tp.n_tiles * nseg * max_levels;
+            const int grid = 2 * std::max(1, std::min(units, r.num_sms / 2));
+            {
+                KernelTimer timer("tc_gemm", st);
+                tc_gemm_kernel<kExact><<<grid, THREADS, kTcSmem, st>>>(tA, tB[j], tC, tp);
+            }
+            const int64_t colgroups = (nj + COMBINE_COLS - 1) / COMBINE_COLS;
+            combine_kernel<<<dim3(unsigned((colgroups + 127) / 128), unsigned(std::min<int64_t>(mi, 65535))), 128, 0,
+                             st>>>(lv, nseg, max_levels, mpad, Nq, kCrt, info, eA + r0, eB + c0, mi, nj, g.alpha, g.beta,
+                                   dC + r0 * n + c0, n);
+            count_launches(3);
+            if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail("block launch", e);
+            cudaEventRecord(ev[P + Q + nb], st);
+            cudaStreamWaitEvent(r.copy_out, ev[P + Q + nb], 0);
+            e = cudaMemcpy2DAsync(hC + r0 * g.ldc + c0, size_t(g.ldc) * 8, dC + r0 * n + c0, size_t(n) * 8,
+                                  size_t(nj) * 8, size_t(mi), cudaMemcpyDeviceToHost, r.copy_out);
+            if (e != cudaSuccess) return cuda_fail("copy of C back", e);
         }
-        const int64_t colgroups = (n + COMBINE_COLS - 1) / COMBINE_COLS;
-        combine_kernel<<<dim3(unsigned((colgroups + 127) / 128), unsigned(std::min<int64_t>(mi, 65535))), 128, 0, st>>>(
-            lv, nseg, max_levels, mpad, npad, kCrt, info, eA + r0, eB, mi, n, g.alpha, g.beta, dC + r0 * n, n);
-        count_launches(6);
-        if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail("panel launch", e);
-        cudaEventRecord(ev[1 + P + i], st);
-        cudaStreamWaitEvent(r.copy_out, ev[1 + P + i], 0);
-        e = cudaMemcpy2DAsync(hC + r0 * g.ldc, size_t(g.ldc) * 8, dC + r0 * n, size_t(n) * 8, size_t(n) * 8,
-                              size_t(mi), cudaMemcpyDeviceToHost, r.copy_out);
-        if (e != cudaSuccess) return cuda_fail("copy of C back", e);
     }
-    split_panels_summary_kernel<<<1, 32, 0, st>>>(info_at(0), P, info_sum);
+    split_panels_summary_kernel<<<1, 32, 0, st>>>(reinterpret_cast<const uint8_t*>(info_at(P + Q)), info_stride,
+                                                  P * Q, info_sum);
     count_launches(1);
-    cudaEventRecord(ev[2 * P + 1], r.copy_out);
-    cudaStreamWaitEvent(st, ev[2 * P + 1], 0);  // the call's work ends on st
-    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail("panel pipeline", e);
+    cudaEventRecord(ev[P + Q + P * Q], r.copy_out);
+    cudaStreamWaitEvent(st, ev[P + Q + P * Q], 0);  // the call's work ends on st
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail("block pipeline", e);
     out->method_used = GB300_METHOD_SPLIT_CRT;
     out->slices = -1;
     out->error_bound = -1.0;
     out->info_dev = info_sum;
     return GB300_OK;
 }
+
 }  // namespace gb
