@@ -95,6 +95,11 @@ __constant__ uint32_t c_mod[MAX_MODULI] = {257, 256, 255, 253, 251, 247, 241, 23
 __constant__ uint32_t c_mod_inv32[MAX_MODULI] = {
     16711935u, 16777216u, 16843009u, 16976155u, 17111423u, 17388531u, 17821441u, 17970574u,
     18433336u, 18755315u, 18920560u, 19259943u, 19792476u, 20355295u, 21582750u};
+// log2 of each modulus (device copy: the plan kernels sum these instead of calling log2).
+__constant__ double c_mod_log2[MAX_MODULI] = {
+    8.005624549193879, 8.0, 7.994353436858858, 7.98299357469431, 7.971543553950772, 7.948367231584678,
+    7.912889336229962, 7.900866807980749, 7.864186144654281, 7.839203788096944, 7.826548487290915,
+    7.800899899920305, 7.7615512324444795, 7.721099188707185, 7.636624620543649};
 // log2 of the running products of the moduli (host-side copy for the worst-case plan).
 constexpr double kModLog2[MAX_MODULI] = {8.00562, 8.0, 7.99435, 7.98299, 7.97154, 7.94837, 7.91289, 7.90087,
                                          7.86419, 7.83920, 7.82655, 7.80090, 7.76155, 7.72110, 7.63662};
@@ -442,11 +447,17 @@ __global__ void __launch_bounds__(1024) split_info_kernel(const int* __restrict_
             const int nfix = fixed_slices > 0 ? (fixed_slices < 2 ? 2 : fixed_slices) : 0;
             const double need0 = need(beta);
             while (nfix ? N < nfix : (N < 2 || (N < cap_planes && have < need0))) {
-                have += log2(double(c_mod[N]));
+                have += c_mod_log2[N];
                 ++N;
             }
             // the moduli chosen may carry more bits than needed: round to as many bits as they allow
+            // need(b) exceeds 1.0875 + 2b + log2(sqa sqb): start at the largest b that this allows and
+            // step down (one or two steps)
             beta = 55;
+            if (sqa > 0 && sqb > 0) {
+                const int b0 = int(floor((have - 1.0875 - log2(sqa) - log2(sqb)) / 2.0));
+                beta = b0 < 55 ? (b0 > -60 ? b0 : -60) : 55;
+            }
             while (beta > -60 && need(beta) > have) --beta;
             r.slices = N;
             r.beta = beta;
@@ -566,7 +577,7 @@ __global__ void split_block_kernel(const SplitInfo* __restrict__ ia, const Split
     double have = 0.0;
     int N = 0;
     while (N < 2 || (N < cap_planes && have < need)) {
-        have += log2(double(c_mod[N]));
+        have += c_mod_log2[N];
         ++N;
     }
     r.slices = N;
@@ -1298,7 +1309,7 @@ __device__ __forceinline__ void crt_cols(const uint16_t* __restrict__ res16, int
     }
 }
 
-__global__ void combine_kernel(const int32_t* __restrict__ levels, int nseg, int max_levels, int64_t mpad,
+__global__ void __launch_bounds__(128, 8) combine_kernel(const int32_t* __restrict__ levels, int nseg, int max_levels, int64_t mpad,
                                int64_t npad, int mode, const SplitInfo* __restrict__ info,
                                const int* __restrict__ eA, const int* __restrict__ eB, int64_t m, int64_t n,
                                double alpha, double beta, double* __restrict__ C, int64_t ldc) {
