@@ -94,6 +94,13 @@ def ref_lib():
         R.ref_gemm_d.restype = ct.c_int
         R.ref_gemm_s.argtypes = _gemm_argtypes(_F, ct.c_float)
         R.ref_gemm_s.restype = ct.c_int
+        i64 = ct.c_int64
+        R.ref_gemv_d.argtypes = [ct.c_int, ct.c_int, i64, i64, ct.c_double, _D, i64, _D, ct.c_double, _D]
+        R.ref_gemv_d.restype = ct.c_int
+        R.ref_gemm_z.argtypes = [ct.c_int, ct.c_int, ct.c_int, i64, i64, i64, _D, _D, i64, _D, i64, _D, _D, i64]
+        R.ref_gemm_z.restype = ct.c_int
+        R.ref_trmm_d.argtypes = [ct.c_int] * 5 + [i64, i64, ct.c_double, _D, i64, _D, i64]
+        R.ref_trmm_d.restype = ct.c_int
         _ref = R
     return _ref
 
@@ -228,3 +235,39 @@ def normwise_error(C_logical: np.ndarray, Cref_logical: np.ndarray, normA: float
     num = float(np.sqrt(np.sum(d * d))) * scale
     den = normA * normB
     return num / den if den > 0 else num
+
+
+def _cd(x):
+    return np.ascontiguousarray(x).ctypes.data_as(_D)
+
+
+def ref_gemv(order, transA, m, n, alpha, A, lda, x, beta, y):
+    """y = alpha op(A) x + beta y (unit strides) through Blaze itself; y is updated in place."""
+    R = ref_lib()
+    if R is None:
+        raise RuntimeError("oracle/_ref/libblazeref.so was not built")
+    if R.ref_gemv_d(order, transA, m, n, alpha, _cd(A), lda, _cd(x), beta, y.ctypes.data_as(_D)) != 0:
+        raise RuntimeError("Blaze raised")
+
+
+def ref_zgemm(order, transA, transB, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc):
+    """Complex C = alpha op(A) op(B) + beta C through Blaze itself (complex128 arrays, CBLAS
+    transposes 111 / 112 / 113); C is updated in place."""
+    R = ref_lib()
+    if R is None:
+        raise RuntimeError("oracle/_ref/libblazeref.so was not built")
+    al = np.array([alpha.real, alpha.imag]); be = np.array([beta.real, beta.imag])
+    Ad = np.ascontiguousarray(A).view(np.float64); Bd = np.ascontiguousarray(B).view(np.float64)
+    if R.ref_gemm_z(order, transA, transB, m, n, k, _cd(al), _cd(Ad), lda, _cd(Bd), ldb, _cd(be),
+                    C.view(np.float64).ctypes.data_as(_D), ldc) != 0:
+        raise RuntimeError("Blaze raised")
+
+
+def ref_trmm(order, side, uplo, transA, diag, m, n, alpha, A, lda, B, ldb):
+    """B = alpha op(A) B or alpha B op(A), A triangular, through Blaze itself; B updated in place."""
+    R = ref_lib()
+    if R is None:
+        raise RuntimeError("oracle/_ref/libblazeref.so was not built")
+    if R.ref_trmm_d(order, side, uplo, transA, diag, m, n, alpha, _cd(A), lda, B.ctypes.data_as(_D), ldb) != 0:
+        raise RuntimeError("Blaze raised")
+

@@ -15,6 +15,7 @@
 // serially: its SMP layer rejects some unaligned CustomMatrix views with odd leading dimensions
 // ("Invalid submatrix alignment"), while the serial kernels accept every layout.
 #include <blaze/Math.h>
+#include <complex>
 #include <cstdint>
 #include <cstdio>
 #include <exception>
@@ -89,6 +90,165 @@ int ref_gemm_s(int order, int tA, int tB, int64_t m, int64_t n, int64_t k, float
                int64_t ldc) {
     try {
         dispatch<float>(order, tA, tB, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+    } catch (const std::exception& e) {
+        std::fprintf(stderr, "blaze: %s\n", e.what());
+        return 1;
+    }
+    return 0;
+}
+
+}  // extern "C"
+
+// ---- the neighbouring BLAS routines on the same seam, evaluated by Blaze -----------------------
+namespace {
+
+template <typename T>
+using VView = blaze::CustomVector<T, unaligned, unpadded>;
+
+// y = alpha * op(A) * x + beta * y (unit strides); op(A) is the logical rows x cols view of the
+// CBLAS operand, a CustomMatrix in the storage order (order, trans) describes.
+template <typename T, bool SO>
+void gemv_run(int64_t rows, int64_t cols, T alpha, const T* A, int64_t lda, const T* x, T beta, T* y) {
+    View<T, SO> a(const_cast<T*>(A), rows, cols, lda);
+    VView<T> vx(const_cast<T*>(x), cols);
+    VView<T> vy(y, rows);
+    if (beta == T(0)) {
+        vy = alpha * (a * vx);
+    } else {
+        vy *= beta;
+        vy += alpha * (a * vx);
+    }
+}
+
+template <typename T>
+void gemv_dispatch(int order, int tA, int64_t m, int64_t n, T alpha, const T* A, int64_t lda, const T* x, T beta,
+                   T* y) {
+    const bool rm = (order == 101), ta = (tA != 111);
+    const int64_t rows = ta ? n : m, cols = ta ? m : n;
+    const bool so = rm ? (ta ? columnMajor : rowMajor) : (ta ? rowMajor : columnMajor);
+    if (so == rowMajor) gemv_run<T, rowMajor>(rows, cols, alpha, A, lda, x, beta, y);
+    else gemv_run<T, columnMajor>(rows, cols, alpha, A, lda, x, beta, y);
+}
+
+// Complex C = alpha * op(A) * op(B) + beta * C; op = conj(trans(.)) for CblasConjTrans.
+template <typename T, bool SOC, bool SOA, bool SOB>
+void cgemm_run(int64_t m, int64_t n, int64_t k, bool ca, bool cb, std::complex<T> alpha, const std::complex<T>* A,
+               int64_t lda, const std::complex<T>* B, int64_t ldb, std::complex<T> beta, std::complex<T>* C,
+               int64_t ldc) {
+    using CT = std::complex<T>;
+    View<CT, SOA> a(const_cast<CT*>(A), m, k, lda);
+    View<CT, SOB> b(const_cast<CT*>(B), k, n, ldb);
+    View<CT, SOC> c(C, m, n, ldc);
+    blaze::DynamicMatrix<CT, SOA> aa(a);
+    blaze::DynamicMatrix<CT, SOB> bb(b);
+    if (ca) aa = conj(aa);
+    if (cb) bb = conj(bb);
+    if (beta == CT(0)) {
+        c = alpha * (aa * bb);
+    } else {
+        c *= beta;
+        c += alpha * (aa * bb);
+    }
+}
+
+template <typename T>
+void cgemm_dispatch(int order, int tA, int tB, int64_t m, int64_t n, int64_t k, std::complex<T> alpha,
+                    const std::complex<T>* A, int64_t lda, const std::complex<T>* B, int64_t ldb,
+                    std::complex<T> beta, std::complex<T>* C, int64_t ldc) {
+    const bool rm = (order == 101);
+    const bool ta = (tA != 111), tb = (tB != 111), ca = (tA == 113), cb = (tB == 113);
+    const bool soA = rm ? (ta ? columnMajor : rowMajor) : (ta ? rowMajor : columnMajor);
+    const bool soB = rm ? (tb ? columnMajor : rowMajor) : (tb ? rowMajor : columnMajor);
+#define GB_CASE(SC, SA, SB)                                                                        \
+    if ((rm ? rowMajor : columnMajor) == SC && soA == SA && soB == SB) {                           \
+        cgemm_run<T, SC, SA, SB>(m, n, k, ca, cb, alpha, A, lda, B, ldb, beta, C, ldc);            \
+        return;                                                                                    \
+    }
+    GB_CASE(rowMajor, rowMajor, rowMajor)
+    GB_CASE(rowMajor, rowMajor, columnMajor)
+    GB_CASE(rowMajor, columnMajor, rowMajor)
+    GB_CASE(rowMajor, columnMajor, columnMajor)
+    GB_CASE(columnMajor, rowMajor, rowMajor)
+    GB_CASE(columnMajor, rowMajor, columnMajor)
+    GB_CASE(columnMajor, columnMajor, rowMajor)
+    GB_CASE(columnMajor, columnMajor, columnMajor)
+#undef GB_CASE
+}
+
+// B = alpha * op(A) * B (side Left) or alpha * B * op(A) (side Right), A triangular (only the
+// uplo triangle is read; diag Unit takes ones on the diagonal).  Blaze's own evaluation of a
+// triangular product: the triangle of op(A) through blaze::LowerMatrix / UpperMatrix (and the
+// Uni* adaptors for a unit diagonal), multiplied with Blaze's default kernels.
+template <typename T, bool SO>
+void trmm_run(int side_left, int lower, int ta, int unit, int64_t m, int64_t n, T alpha, const T* A, int64_t lda,
+              T* B, int64_t ldb) {
+    const int64_t ka = side_left ? m : n;
+    View<T, SO> a(const_cast<T*>(A), ka, ka, lda);
+    View<T, SO> b(B, m, n, ldb);
+    blaze::DynamicMatrix<T, SO> t(ka, ka, T(0));
+    for (int64_t i = 0; i < ka; ++i)
+        for (int64_t j = 0; j < ka; ++j) {
+            const bool in = lower ? (j <= i) : (j >= i);
+            if (in) t(i, j) = (unit && i == j) ? T(1) : a(i, j);
+        }
+    blaze::DynamicMatrix<T, SO> op = ta ? blaze::DynamicMatrix<T, SO>(trans(t)) : t;
+    blaze::DynamicMatrix<T, SO> res;
+    const bool low_op = ta ? !lower : lower;
+    if (low_op) {
+        if (unit) {
+            blaze::UniLowerMatrix<blaze::DynamicMatrix<T, SO>> tri(op);
+            res = side_left ? blaze::DynamicMatrix<T, SO>(alpha * (tri * b)) : blaze::DynamicMatrix<T, SO>(alpha * (b * tri));
+        } else {
+            blaze::LowerMatrix<blaze::DynamicMatrix<T, SO>> tri(op);
+            res = side_left ? blaze::DynamicMatrix<T, SO>(alpha * (tri * b)) : blaze::DynamicMatrix<T, SO>(alpha * (b * tri));
+        }
+    } else {
+        if (unit) {
+            blaze::UniUpperMatrix<blaze::DynamicMatrix<T, SO>> tri(op);
+            res = side_left ? blaze::DynamicMatrix<T, SO>(alpha * (tri * b)) : blaze::DynamicMatrix<T, SO>(alpha * (b * tri));
+        } else {
+            blaze::UpperMatrix<blaze::DynamicMatrix<T, SO>> tri(op);
+            res = side_left ? blaze::DynamicMatrix<T, SO>(alpha * (tri * b)) : blaze::DynamicMatrix<T, SO>(alpha * (b * tri));
+        }
+    }
+    b = res;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ref_gemv_d(int order, int tA, int64_t m, int64_t n, double alpha, const double* A, int64_t lda, const double* x,
+               double beta, double* y) {
+    try {
+        gemv_dispatch<double>(order, tA, m, n, alpha, A, lda, x, beta, y);
+    } catch (const std::exception& e) {
+        std::fprintf(stderr, "blaze: %s\n", e.what());
+        return 1;
+    }
+    return 0;
+}
+
+// alpha, beta, A, B, C as interleaved (re, im) doubles
+int ref_gemm_z(int order, int tA, int tB, int64_t m, int64_t n, int64_t k, const double* alpha, const double* A,
+               int64_t lda, const double* B, int64_t ldb, const double* beta, double* C, int64_t ldc) {
+    using CT = std::complex<double>;
+    try {
+        cgemm_dispatch<double>(order, tA, tB, m, n, k, CT(alpha[0], alpha[1]), reinterpret_cast<const CT*>(A), lda,
+                               reinterpret_cast<const CT*>(B), ldb, CT(beta[0], beta[1]), reinterpret_cast<CT*>(C), ldc);
+    } catch (const std::exception& e) {
+        std::fprintf(stderr, "blaze: %s\n", e.what());
+        return 1;
+    }
+    return 0;
+}
+
+int ref_trmm_d(int order, int side, int uplo, int tA, int diag, int64_t m, int64_t n, double alpha, const double* A,
+               int64_t lda, double* B, int64_t ldb) {
+    try {
+        const int left = side == 141, lower = uplo == 122, ta = tA != 111, unit = diag == 132;
+        if (order == 101) trmm_run<double, rowMajor>(left, lower, ta, unit, m, n, alpha, A, lda, B, ldb);
+        else trmm_run<double, columnMajor>(left, lower, ta, unit, m, n, alpha, A, lda, B, ldb);
     } catch (const std::exception& e) {
         std::fprintf(stderr, "blaze: %s\n", e.what());
         return 1;
