@@ -115,6 +115,15 @@ def lib() -> ct.CDLL:
     L.cblas_dgemm_64.restype = None
     L.cblas_sgemm_64.argtypes = [ct.c_int, ct.c_int, ct.c_int, I64, I64, I64, F, VP, I64, VP, I64, F, VP, I64]
     L.cblas_sgemm_64.restype = None
+    for nm, T in (("cblas_dgemv", D), ("cblas_sgemv", F)):
+        getattr(L, nm).argtypes = [ct.c_int, ct.c_int, I32, I32, T, VP, I32, VP, I32, T, VP, I32]
+        getattr(L, nm).restype = None
+    for nm in ("cblas_zgemm", "cblas_cgemm"):
+        getattr(L, nm).argtypes = [ct.c_int, ct.c_int, ct.c_int, I32, I32, I32, VP, VP, I32, VP, I32, VP, VP, I32]
+        getattr(L, nm).restype = None
+    for nm, T in (("cblas_dtrmm", D), ("cblas_strmm", F)):
+        getattr(L, nm).argtypes = [ct.c_int] * 5 + [I32, I32, T, VP, I32, VP, I32]
+        getattr(L, nm).restype = None
     L.gb300_dgemm_ex.argtypes = [ct.c_int, ct.c_int, ct.c_int, I64, I64, I64, D, VP, I64, VP, I64, D, VP, I64,
                                  ct.POINTER(GemmOpts)]
     L.gb300_dgemm_ex.restype = ct.c_int
@@ -255,6 +264,42 @@ def cblas_sgemm(order, transA, transB, m, n, k, alpha, A, lda, B, ldb, beta, C, 
     st, msg = last_error()
     if st != OK:
         raise Gb300Error(st, msg)
+
+
+def _raise_on_error():
+    st, msg = last_error()
+    if st != OK:
+        raise Gb300Error(st, msg)
+
+
+def cblas_gemv(order, transA, m, n, alpha, A, lda, x, incx, beta, y, incy, dtype="d") -> None:
+    """cblas_dgemv (dtype "d") or cblas_sgemv ("s"): y = alpha op(A) x + beta y."""
+    L = lib()
+    L.gb300_clear_error()
+    getattr(L, "cblas_%sgemv" % dtype)(order, transA, m, n, alpha, _addr(A), lda, _addr(x), incx, beta, _addr(y), incy)
+    _raise_on_error()
+
+
+def cblas_zgemm(order, transA, transB, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, single=False) -> None:
+    """cblas_zgemm (complex128 operands) or cblas_cgemm (single=True, complex64): complex
+    C = alpha op(A) op(B) + beta C, transposes 111 / 112 / 113 (conjugate)."""
+    L = lib()
+    import numpy as np
+    ct_t = np.complex64 if single else np.complex128
+    al = np.array([alpha], dtype=ct_t)
+    be = np.array([beta], dtype=ct_t)
+    L.gb300_clear_error()
+    getattr(L, "cblas_cgemm" if single else "cblas_zgemm")(order, transA, transB, m, n, k, al.ctypes.data, _addr(A),
+                                                          lda, _addr(B), ldb, be.ctypes.data, _addr(C), ldc)
+    _raise_on_error()
+
+
+def cblas_trmm(order, side, uplo, transA, diag, m, n, alpha, A, lda, B, ldb, dtype="d") -> None:
+    """cblas_dtrmm / cblas_strmm: B = alpha op(A) B (side 141) or alpha B op(A) (142), A triangular."""
+    L = lib()
+    L.gb300_clear_error()
+    getattr(L, "cblas_%strmm" % dtype)(order, side, uplo, transA, diag, m, n, alpha, _addr(A), lda, _addr(B), ldb)
+    _raise_on_error()
 
 
 def dgemm_native_noalloc(order, transA, transB, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc,

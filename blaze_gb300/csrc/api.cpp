@@ -98,6 +98,8 @@ const char* method_name(int m) {
 
 }  // namespace
 
+int library_default_method() { return default_method(); }
+
 template <typename T>
 int gemm_entry(int order, int transA, int transB, int64_t m, int64_t n, int64_t k, T alpha, const T* A, int64_t lda,
               const T* B, int64_t ldb, T beta, T* C, int64_t ldc, gb300_gemm_opts* opts, const char* routine) {

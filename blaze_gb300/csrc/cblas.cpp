@@ -3,10 +3,11 @@
 // Compiled twice: once with 32-bit integers (the standard names) and once with
 // -DGB300_BLAS_ILP64 (names with a _64 suffix), matching blaze/math/blas/Types.h:56-64.
 //
-// cblas_dgemm / cblas_sgemm run on the GPU (api.cpp).  The remaining routines exist so that every
-// function Blaze's wrappers name (the headers under blaze/math/blas/cblas/) resolves; they compute nothing and
-// record GB300_ERR_NOT_SUPPORTED, so a caller reaching them learns it at once instead of
-// receiving a silent CPU result.
+// cblas_dgemm / cblas_sgemm run on the GPU (api.cpp), and so do cblas_?gemv, cblas_cgemm /
+// cblas_zgemm and cblas_strmm / cblas_dtrmm (api_next.cpp).  The remaining routines exist so that
+// every function Blaze's wrappers name (the headers under blaze/math/blas/cblas/) resolves; they
+// compute nothing and record GB300_ERR_NOT_SUPPORTED, so a caller reaching them learns it at once
+// instead of receiving a silent CPU result.
 #include <string>
 
 #include "../../include/gb300_blas.h"
@@ -17,7 +18,7 @@
 namespace {
 void not_supported(const char* name) {
     gb::set_error(GB300_ERR_NOT_SUPPORTED,
-                  std::string(name) + ": not provided by libgb300blas (only ?gemm runs on the GPU)");
+                  std::string(name) + ": not provided by libgb300blas");
 }
 }  // namespace
 
@@ -51,16 +52,35 @@ __attribute__((visibility("default"))) void gb300_cblas_dgemm_checked(CBLAS_ORDE
 }
 
 // ---- stubs ------------------------------------------------------------------------------------
-void cblas_cgemm(CBLAS_ORDER, CBLAS_TRANSPOSE, CBLAS_TRANSPOSE, gb300_blas_int, gb300_blas_int, gb300_blas_int,
-                 const void*, const void*, gb300_blas_int, const void*, gb300_blas_int, const void*, void*,
-                 gb300_blas_int) { not_supported("cblas_cgemm"); }
-void cblas_zgemm(CBLAS_ORDER, CBLAS_TRANSPOSE, CBLAS_TRANSPOSE, gb300_blas_int, gb300_blas_int, gb300_blas_int,
-                 const void*, const void*, gb300_blas_int, const void*, gb300_blas_int, const void*, void*,
-                 gb300_blas_int) { not_supported("cblas_zgemm"); }
-void cblas_sgemv(CBLAS_ORDER, CBLAS_TRANSPOSE, gb300_blas_int, gb300_blas_int, float, const float*, gb300_blas_int,
-                 const float*, gb300_blas_int, float, float*, gb300_blas_int) { not_supported("cblas_sgemv"); }
-void cblas_dgemv(CBLAS_ORDER, CBLAS_TRANSPOSE, gb300_blas_int, gb300_blas_int, double, const double*, gb300_blas_int,
-                 const double*, gb300_blas_int, double, double*, gb300_blas_int) { not_supported("cblas_dgemv"); }
+// ---- the neighbouring routines on the GPU (api_next.cpp) ----------------------------------------
+void cblas_cgemm(CBLAS_ORDER order, CBLAS_TRANSPOSE transA, CBLAS_TRANSPOSE transB, gb300_blas_int m, gb300_blas_int n,
+                 gb300_blas_int k, const void* alpha, const void* A, gb300_blas_int lda, const void* B,
+                 gb300_blas_int ldb, const void* beta, void* C, gb300_blas_int ldc) {
+    gb::cgemm_entry<float>(int(order), int(transA), int(transB), int64_t(m), int64_t(n), int64_t(k),
+                           static_cast<const float*>(alpha), static_cast<const float*>(A), int64_t(lda),
+                           static_cast<const float*>(B), int64_t(ldb), static_cast<const float*>(beta),
+                           static_cast<float*>(C), int64_t(ldc), "cblas_cgemm");
+}
+void cblas_zgemm(CBLAS_ORDER order, CBLAS_TRANSPOSE transA, CBLAS_TRANSPOSE transB, gb300_blas_int m, gb300_blas_int n,
+                 gb300_blas_int k, const void* alpha, const void* A, gb300_blas_int lda, const void* B,
+                 gb300_blas_int ldb, const void* beta, void* C, gb300_blas_int ldc) {
+    gb::cgemm_entry<double>(int(order), int(transA), int(transB), int64_t(m), int64_t(n), int64_t(k),
+                            static_cast<const double*>(alpha), static_cast<const double*>(A), int64_t(lda),
+                            static_cast<const double*>(B), int64_t(ldb), static_cast<const double*>(beta),
+                            static_cast<double*>(C), int64_t(ldc), "cblas_zgemm");
+}
+void cblas_sgemv(CBLAS_ORDER order, CBLAS_TRANSPOSE transA, gb300_blas_int m, gb300_blas_int n, float alpha,
+                 const float* A, gb300_blas_int lda, const float* x, gb300_blas_int incx, float beta, float* y,
+                 gb300_blas_int incy) {
+    gb::gemv_entry<float>(int(order), int(transA), int64_t(m), int64_t(n), alpha, A, int64_t(lda), x, int64_t(incx), beta,
+                          y, int64_t(incy), "cblas_sgemv");
+}
+void cblas_dgemv(CBLAS_ORDER order, CBLAS_TRANSPOSE transA, gb300_blas_int m, gb300_blas_int n, double alpha,
+                 const double* A, gb300_blas_int lda, const double* x, gb300_blas_int incx, double beta, double* y,
+                 gb300_blas_int incy) {
+    gb::gemv_entry<double>(int(order), int(transA), int64_t(m), int64_t(n), alpha, A, int64_t(lda), x, int64_t(incx),
+                           beta, y, int64_t(incy), "cblas_dgemv");
+}
 void cblas_cgemv(CBLAS_ORDER, CBLAS_TRANSPOSE, gb300_blas_int, gb300_blas_int, const void*, const void*,
                  gb300_blas_int, const void*, gb300_blas_int, const void*, void*, gb300_blas_int) {
     not_supported("cblas_cgemv");
@@ -69,10 +89,18 @@ void cblas_zgemv(CBLAS_ORDER, CBLAS_TRANSPOSE, gb300_blas_int, gb300_blas_int, c
                  gb300_blas_int, const void*, gb300_blas_int, const void*, void*, gb300_blas_int) {
     not_supported("cblas_zgemv");
 }
-void cblas_strmm(CBLAS_ORDER, CBLAS_SIDE, CBLAS_UPLO, CBLAS_TRANSPOSE, CBLAS_DIAG, gb300_blas_int, gb300_blas_int,
-                 float, const float*, gb300_blas_int, float*, gb300_blas_int) { not_supported("cblas_strmm"); }
-void cblas_dtrmm(CBLAS_ORDER, CBLAS_SIDE, CBLAS_UPLO, CBLAS_TRANSPOSE, CBLAS_DIAG, gb300_blas_int, gb300_blas_int,
-                 double, const double*, gb300_blas_int, double*, gb300_blas_int) { not_supported("cblas_dtrmm"); }
+void cblas_strmm(CBLAS_ORDER order, CBLAS_SIDE side, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA, CBLAS_DIAG diag,
+                 gb300_blas_int m, gb300_blas_int n, float alpha, const float* A, gb300_blas_int lda, float* B,
+                 gb300_blas_int ldb) {
+    gb::trmm_entry<float>(int(order), int(side), int(uplo), int(transA), int(diag), int64_t(m), int64_t(n), alpha, A,
+                          int64_t(lda), B, int64_t(ldb), "cblas_strmm");
+}
+void cblas_dtrmm(CBLAS_ORDER order, CBLAS_SIDE side, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA, CBLAS_DIAG diag,
+                 gb300_blas_int m, gb300_blas_int n, double alpha, const double* A, gb300_blas_int lda, double* B,
+                 gb300_blas_int ldb) {
+    gb::trmm_entry<double>(int(order), int(side), int(uplo), int(transA), int(diag), int64_t(m), int64_t(n), alpha, A,
+                           int64_t(lda), B, int64_t(ldb), "cblas_dtrmm");
+}
 void cblas_ctrmm(CBLAS_ORDER, CBLAS_SIDE, CBLAS_UPLO, CBLAS_TRANSPOSE, CBLAS_DIAG, gb300_blas_int, gb300_blas_int,
                  const void*, const void*, gb300_blas_int, void*, gb300_blas_int) { not_supported("cblas_ctrmm"); }
 void cblas_ztrmm(CBLAS_ORDER, CBLAS_SIDE, CBLAS_UPLO, CBLAS_TRANSPOSE, CBLAS_DIAG, gb300_blas_int, gb300_blas_int,

@@ -61,6 +61,20 @@ cudaError_t native_gemm(const Gemm& g, int splits, T* workspace, const LaunchCtl
 // Split count the native kernel uses for a shape on `num_sms` SMs (1 = no split).
 int native_choose_splits(int64_t m, int64_t n, int64_t k, int elem_bytes, int num_sms);
 // The shared implementation behind cblas_?gemm and gb300_?gemm_ex (CBLAS argument conventions).
+// The method cblas_?gemm uses (GB300_DGEMM_METHOD / gb300_set_default_method).
+int library_default_method();
+
+template <typename T>
+int gemv_entry(int order, int transA, int64_t m, int64_t n, T alpha, const T* A, int64_t lda, const T* x,
+               int64_t incx, T beta, T* y, int64_t incy, const char* routine);
+// complex interleaved (re, im) operands, T = double or float; alpha, beta point to two T each
+template <typename T>
+int cgemm_entry(int order, int transA, int transB, int64_t m, int64_t n, int64_t k, const T* alpha, const T* A,
+                int64_t lda, const T* B, int64_t ldb, const T* beta, T* C, int64_t ldc, const char* routine);
+template <typename T>
+int trmm_entry(int order, int side, int uplo, int transA, int diag, int64_t m, int64_t n, T alpha, const T* A,
+               int64_t lda, T* B, int64_t ldb, const char* routine);
+
 template <typename T>
 int gemm_entry(int order, int transA, int transB, int64_t m, int64_t n, int64_t k, T alpha, const T* A, int64_t lda,
                const T* B, int64_t ldb, T beta, T* C, int64_t ldc, gb300_gemm_opts* opts, const char* routine);

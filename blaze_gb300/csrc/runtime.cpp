@@ -105,6 +105,8 @@ int ensure_init(std::string* err) {
     r.num_sms = prop.multiProcessorCount;
     r.ws.stream = r.stream;
     r.ws.d_status = r.d_status;
+    r.aux.stream = r.stream;
+    r.aux.d_status = r.d_status;
     r.inited = true;
     return GB300_OK;
 }

@@ -50,6 +50,8 @@ struct Runtime {
     cudaStream_t stream = nullptr;
     int* d_status = nullptr;       // device status word of the default context
     Workspace ws;                  // default context (stream = `stream`)
+    Workspace aux;                 // operands and intermediates of ?gemv, complex ?gemm, ?trmm
+                                   // (their real products use `ws`)
     std::atomic<int64_t> launches{0};
     int inject_stall_count = 0;
     uint64_t inject_limit_ns = 0;

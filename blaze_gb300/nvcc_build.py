@@ -35,6 +35,8 @@ UNITS = [
     ("profile.cpp", "profile.o", []),
     ("grouped.cu", "grouped.o", []),
     ("serve.cpp", "serve.o", []),
+    ("level23.cu", "level23.o", []),
+    ("api_next.cpp", "api_next.o", []),
 ]
 
 

@@ -102,3 +102,32 @@ def test_no_device_is_reported_not_faked(lib):
                     C.ctypes.data, 2)
     assert G.last_error()[0] == G.ERR_NO_DEVICE
     assert np.all(C == 0.0)  # nothing was computed on the CPU
+
+
+@pytest.mark.parametrize("routine,args,param", [
+    ("gemv", dict(order=99), 1), ("gemv", dict(ta=7), 2), ("gemv", dict(m=-1), 3), ("gemv", dict(n=-1), 4),
+    ("gemv", dict(lda=3), 7), ("gemv", dict(incx=0), 9), ("gemv", dict(incy=0), 12),
+    ("zgemm", dict(order=99), 1), ("zgemm", dict(ta=7), 2), ("zgemm", dict(k=-1), 6), ("zgemm", dict(lda=3), 9),
+    ("zgemm", dict(ldc=3), 14),
+    ("trmm", dict(side=7), 2), ("trmm", dict(uplo=7), 3), ("trmm", dict(ta=7), 4), ("trmm", dict(diag=7), 5),
+    ("trmm", dict(m=-1), 6), ("trmm", dict(lda=3), 10), ("trmm", dict(ldb=3), 12),
+])
+def test_neighbour_routines_name_the_parameter(lib, routine, args, param):
+    a = dict(order=G.RowMajor, ta=G.NoTrans, tb=G.NoTrans, m=8, n=8, k=8, lda=8, ldb=8, ldc=8, incx=1, incy=1,
+             side=141, uplo=121, diag=131)
+    a.update(args)
+    A = np.zeros(128); B = np.zeros(128); C = np.zeros(128)
+    one = np.array([1.0, 0.0]); zero = np.array([0.0, 0.0])
+    lib.gb300_clear_error()
+    if routine == "gemv":
+        lib.cblas_dgemv(a["order"], a["ta"], a["m"], a["n"], 1.0, A.ctypes.data, a["lda"], B.ctypes.data, a["incx"],
+                        0.0, C.ctypes.data, a["incy"])
+    elif routine == "zgemm":
+        lib.cblas_zgemm(a["order"], a["ta"], a["tb"], a["m"], a["n"], a["k"], one.ctypes.data, A.ctypes.data,
+                        a["lda"], B.ctypes.data, a["ldb"], zero.ctypes.data, C.ctypes.data, a["ldc"])
+    else:
+        lib.cblas_dtrmm(a["order"], a["side"], a["uplo"], a["ta"], a["diag"], a["m"], a["n"], 1.0, A.ctypes.data,
+                        a["lda"], B.ctypes.data, a["ldb"])
+    st, msg = G.last_error()
+    assert st == G.ERR_INVALID_ARG
+    assert f"parameter {param} " in msg
