@@ -51,6 +51,7 @@ def parse():
     ap.add_argument("--no-batched", action="store_true", help="skip the batched small-product leg")
     ap.add_argument("--batch-count", type=int, default=10000)
     ap.add_argument("--no-serving", action="store_true", help="skip the serving leg")
+    ap.add_argument("--no-next", action="store_true", help="skip the gemv / zgemm / trmm leg")
     ap.add_argument("--sweep", default="", help="comma list of sweep groups to run instead of the main line: "
                                                  "square (4096/8192/16384, rr/rc, uniform/spread, native/split S=3..8/"
                                                  "bf16x3), rect ((M,K,N) = (65536,256,256), (256,65536,256), "
@@ -339,6 +340,60 @@ def batched_leg(G, torch, args, dev):
     return out
 
 
+def next_leg(G, torch, args):
+    """The BLAS routines next to ?gemm on the same seam, device-resident, each timed as synchronous
+    calls (wall clock per call, launch and synchronisation included): dgemv on a 16384 x 8192
+    matrix (bytes read / time against the measured HBM copy bandwidth), an FP64-accurate zgemm of
+    4096^3 (four split real products; 8 m n k flops) and an FP64-accurate dtrmm (left, lower) of
+    8192 x 8192 (m^2 n flops of a triangular product)."""
+    peaks, _ = read_peaks()
+
+    def wall(fn, reps):
+        fn()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            fn()
+        return (time.perf_counter() - t0) / reps
+
+    out = {}
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(args.seed)
+
+    def dev_uniform(count, dtype=torch.float64):
+        return torch.rand(count, generator=gen, device="cuda", dtype=dtype) * 2 - 1
+
+    m, n = 16384, 8192
+    dA = dev_uniform(m * n)
+    dx = dev_uniform(n)
+    dy = torch.zeros(m, dtype=torch.float64, device="cuda")
+    t = wall(lambda: G.cblas_gemv(101, 111, m, n, 1.0, dA, n, dx, 1, 0.0, dy, 1), 20)
+    ref = dA.view(m, n) @ dx
+    gbs = 8.0 * (m * n + m + n) / t / 1e9
+    out["dgemv"] = {"shape": [m, n], "ms": round(t * 1e3, 4), "gbs": round(gbs, 1),
+                    "frac_of_hbm": round(gbs / float(peaks.get("hbm_gbs", 6800.0)), 3),
+                    "max_rel_diff_vs_torch": float(((dy - ref).abs().max() / ref.abs().max()).item())}
+    del dA, dx, dy, ref
+    k = 4096
+    zA = torch.complex(dev_uniform(k * k), dev_uniform(k * k))
+    zB = torch.complex(dev_uniform(k * k), dev_uniform(k * k))
+    zC = torch.zeros(k * k, dtype=torch.complex128, device="cuda")
+    t = wall(lambda: G.cblas_zgemm(101, 111, 111, k, k, k, 1.0 + 0j, zA, k, zB, k, 0j, zC, k), 3)
+    refz = zA.view(k, k) @ zB.view(k, k)
+    errz = float((torch.linalg.norm(zC.view(k, k) - refz) / (torch.linalg.norm(zA) * torch.linalg.norm(zB))).item())
+    out["zgemm"] = {"n": k, "ms": round(t * 1e3, 3), "tflops": round(8.0 * k ** 3 / t / 1e12, 2),
+                    "normwise_diff_vs_torch": errz, "form": "4 FP64-accurate split real products"}
+    del zA, zB, zC, refz
+    n2 = 8192
+    tA = dev_uniform(n2 * n2)
+    tB = dev_uniform(n2 * n2)
+    t = wall(lambda: G.cblas_trmm(101, 141, 122, 111, 131, n2, n2, 1.0, tA, n2, tB, n2), 3)
+    out["dtrmm"] = {"n": n2, "ms": round(t * 1e3, 3), "tflops": round(float(n2) ** 3 / t / 1e12, 2),
+                    "form": "masked triangle, one FP64-accurate split product"}
+    del tA, tB
+    out["inputs"] = "uniform [-1,1] generated on the device (torch.Generator, the bench seed)"
+    return out
+
+
 def serving_leg(G, torch, args, dev):
     """Poisson stream of square FP64 requests: 70 % n log-uniform in [8,128], 25 % in [512,2048],
     5 % in [4096,8192], accuracy class drawn uniformly from {native FP64, split <= k*2^-53, BF16},
@@ -502,6 +557,9 @@ def ours(args, dist: Dist):
     serving = None
     if not args.no_serving:
         serving = serving_leg(G, torch, args, dev)
+    nxt = None
+    if not args.no_next:
+        nxt = next_leg(G, torch, args)
 
     peaks, peaks_src = read_peaks()
 
@@ -546,7 +604,7 @@ def ours(args, dist: Dist):
                 "native_fp64": native,
                 "split_vs_native": round(value / dist.world / native["value"], 2) if native else None,
                 "e2e": e2e, "roofline": roofline, "gpu_launches": int(launches), "clocks": clk,
-                "batched": batched, "serving": serving}
+                "batched": batched, "serving": serving, "next": nxt}
         if not args.no_cpu:
             line["cpu_baseline"] = cpu_baseline(min(n, 4096))
         print(json.dumps(line), flush=True)
