@@ -64,29 +64,39 @@ def parse():
 
 # ---- distributed plumbing ----------------------------------------------------------------------
 class Dist:
-    def __init__(self, gpus: int):
+    """One process per GPU (torchrun): replicas with no data exchange; the only collectives are the
+    timing barrier and the max over ranks.  NCCL on the GPUs; `backend="gloo"` (or
+    GB300_BENCH_BACKEND=gloo) runs the same collectives on CPU tensors."""
+
+    def __init__(self, gpus: int, backend: str | None = None):
         self.world = int(os.environ.get("WORLD_SIZE", "1"))
         self.rank = int(os.environ.get("RANK", "0"))
         self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.backend = backend or os.environ.get("GB300_BENCH_BACKEND", "nccl")
         self.pg = None
         if self.world > 1:
             import torch.distributed as dist
             import torch
-            torch.cuda.set_device(self.local)
-            dist.init_process_group("nccl")
+            if self.backend == "nccl":
+                torch.cuda.set_device(self.local)
+            dist.init_process_group(self.backend)
             self.pg = dist
+
+    def _device(self):
+        return "cuda" if self.backend == "nccl" else "cpu"
 
     def barrier(self):
         if self.pg:
             import torch
-            self.pg.all_reduce(torch.zeros(1, device="cuda"))
-            torch.cuda.synchronize()
+            self.pg.all_reduce(torch.zeros(1, device=self._device()))
+            if self.backend == "nccl":
+                torch.cuda.synchronize()
 
     def max(self, v: float) -> float:
         if not self.pg:
             return v
         import torch
-        t = torch.tensor([v], dtype=torch.float64, device="cuda")
+        t = torch.tensor([v], dtype=torch.float64, device=self._device())
         self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
         return float(t.item())
 
