@@ -191,9 +191,8 @@ int gemm_entry(int order, int transA, int transB, int64_t m, int64_t n, int64_t 
     const void* info_dev = nullptr;
     cudaError_t e = cudaSuccess;
 
-    // Page-locked host operands of a large FP64-accurate product: row panels of A whose copies in
-    // and out overlap the computation (falls through to staging when the method, shape or memory
-    // does not qualify).
+    // Host operands of a large FP64-accurate product: row panels of A whose copies in and out
+    // overlap the computation (falls through to staging when the method or shape does not qualify).
     bool done = false;
     if (is_double && product && !devA && !devB && !devC && method != GB300_METHOD_NATIVE) {
         SplitRequest req;
@@ -274,8 +273,8 @@ int gemm_entry(int order, int transA, int transB, int64_t m, int64_t n, int64_t 
     if (opts) opts->method_used = used;
 
     if (c_staged) {
-        e = cudaMemcpy2DAsync(C, size_t(ldc) * sizeof(T), dc.ptr, size_t(dc.ld) * sizeof(T), size_t(sc.cols) * sizeof(T),
-                              size_t(sc.rows), cudaMemcpyDeviceToHost, s);
+        e = copy_to_host(C, size_t(ldc) * sizeof(T), dc.ptr, size_t(dc.ld) * sizeof(T), size_t(sc.cols) * sizeof(T),
+                         size_t(sc.rows), s);
         if (e != cudaSuccess) return fail(GB300_ERR_CUDA, std::string("copy of C back: ") + cudaGetErrorString(e));
     }
     }  // !done

@@ -64,8 +64,7 @@ void* stage(const void* p, int64_t rows, int64_t cols, int64_t ld, size_t elem, 
 
 cudaError_t unstage(void* host, const void* dev, int64_t rows, int64_t cols, int64_t ld, size_t elem, cudaStream_t st) {
     if (rows == 0 || cols == 0) return cudaSuccess;
-    return cudaMemcpy2DAsync(host, size_t(ld) * elem, dev, size_t(ld) * elem, size_t(cols) * elem, size_t(rows),
-                             cudaMemcpyDeviceToHost, st);
+    return copy_to_host(host, size_t(ld) * elem, dev, size_t(ld) * elem, size_t(cols) * elem, size_t(rows), st);
 }
 
 // Finish a call: wait for the stream and read the device status word.

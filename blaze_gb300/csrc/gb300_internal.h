@@ -38,6 +38,17 @@ struct LaunchCtl {
     int inject_stall = 0;           // test hook: the TMA producer issues nothing (waits run out)
 };
 
+// Device -> host copy of `rows` rows of `width` bytes: one linear copy when both pitches equal the
+// width, else a pitched copy.  On a Grace host a pitched copy into pageable pages that were never
+// touched runs over ten times slower than a linear one (430 ms against 40 ms for 512 MiB, measured
+// on a GB300); into resident pages the two take the same time.
+inline cudaError_t copy_to_host(void* dst, size_t dpitch, const void* src, size_t spitch, size_t width, size_t rows,
+                                cudaStream_t st) {
+    if (rows <= 1 || (dpitch == width && spitch == width))
+        return cudaMemcpyAsync(dst, src, width * rows, cudaMemcpyDeviceToHost, st);
+    return cudaMemcpy2DAsync(dst, dpitch, src, spitch, width, rows, cudaMemcpyDeviceToHost, st);
+}
+
 // ---- tensor maps ----------------------------------------------------------------------------
 // Encode a 2-D tiled tensor map over a row-major matrix of `rows` x `cols` elements of
 // `dtype` with a row pitch of `ld` elements; the box is box_cols (innermost) x box_rows.

@@ -35,11 +35,11 @@ struct Workspace;
 int device_product(const Gemm& g, const SplitRequest& req, const LaunchCtl& ctl, cudaStream_t s, Workspace& ws,
                    SplitResult* out, std::string* err);
 
-// FP64-accurate product of page-locked host operands in row panels of A: B is copied and sliced once,
-// then each panel's copy in, product and copy of C back run on three streams so that the transfers
-// overlap the computation.  The operands keep the caller's layout (g as for device_product, with host
+// FP64-accurate product of host operands (page-locked or pageable) in row panels of A: B is copied
+// and sliced once, then each panel's copy in, product and copy of C back run on three streams so
+// that the transfers overlap the computation.  The operands keep the caller's layout (g as for device_product, with host
 // pointers); the call's work ends on stream s.  Returns GB300_ERR_NOT_SUPPORTED, with nothing
-// enqueued, when the method, shape or memory does not qualify: the caller then stages the operands
+// enqueued, when the method or shape does not qualify: the caller then stages the operands
 // and calls device_product.
 int device_product_host_panels(const Gemm& g, const SplitRequest& req, const LaunchCtl& ctl, cudaStream_t s,
                                Workspace& ws, SplitResult* out, std::string* err);

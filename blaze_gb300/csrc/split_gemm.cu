@@ -1759,8 +1759,7 @@ int device_product_host_panels(const Gemm& g, const SplitRequest& req, const Lau
     const int P = int((m + Mp - 1) / Mp);
     const int64_t Nq = n >= 4096 ? round_up((n + 1) / 2, TN) : round_up(n, TN);
     const int Q = int((n + Nq - 1) / Nq);
-    if (P < 2 || P > 16 || !page_locked(g.A) || !page_locked(g.B) || !page_locked(g.C))
-        return GB300_ERR_NOT_SUPPORTED;
+    if (P < 2 || P > 16) return GB300_ERR_NOT_SUPPORTED;
     if (!pipe_init(r, err)) return GB300_ERR_CUDA;
     Gemm gp = g;
     gp.m = Mp;
@@ -1832,11 +1831,6 @@ int device_product_host_panels(const Gemm& g, const SplitRequest& req, const Lau
                                   cudaMemcpyHostToDevice, r.copy_in);
         cudaEventRecord(ev[P + j], r.copy_in);
     };
-    copy_a(0);
-    for (int j = 0; j < Q && e == cudaSuccess; ++j) copy_b(j);
-    for (int i = 1; i < P && e == cudaSuccess; ++i) copy_a(i);
-    if (e != cudaSuccess) return cuda_fail("copy of an operand", e);
-
     cudaMemsetAsync(racc, 0, size_t(m + n) * sizeof(RowAcc), st);
     const unsigned ktiles = unsigned(((k + 63) / 64 + TILE_KT - 1) / TILE_KT);
     const unsigned stiles = unsigned((kpad / 64 + TILE_KT - 1) / TILE_KT);
@@ -1905,14 +1899,35 @@ int device_product_host_panels(const Gemm& g, const SplitRequest& req, const Lau
     if (e != cudaSuccess) return cuda_fail("tc_gemm_kernel smem attribute", e);
 
     // ---- blocks in row-major order: panel i's planes serve its Q blocks; C goes back per block ----
+    // Issue order: operands in (A_0, B_0, B_1, then A_i before panel i), panel i's blocks queued,
+    // then panel i-1's blocks of C out.  With page-locked memory every call returns at once; with
+    // pageable memory each copy holds the host thread until it is done, and this order keeps the
+    // GPU busy meanwhile: A_i+1 goes in and panel i-1 comes out while panel i computes.
+    // C goes back per block; a pageable C whose rows are exactly n elements goes back per panel in
+    // one linear copy instead (pitched copies into untouched pageable pages are slow, copy_to_host)
+    const bool c_per_panel = Q > 1 && g.ldc == n && !page_locked(g.C);
+    auto copy_c_out = [&](int i) {
+        const int64_t r0 = int64_t(i) * Mp, mi = std::min(Mp, m - r0);
+        for (int j = 0; j < Q && e == cudaSuccess; ++j) {
+            cudaStreamWaitEvent(r.copy_out, ev[P + Q + i * Q + j], 0);
+            if (c_per_panel && j + 1 < Q) continue;
+            const int64_t c0 = c_per_panel ? 0 : int64_t(j) * Nq, nj = c_per_panel ? n : std::min(Nq, n - c0);
+            e = copy_to_host(hC + r0 * g.ldc + c0, size_t(g.ldc) * 8, dC + r0 * n + c0, size_t(n) * 8, size_t(nj) * 8,
+                             size_t(mi), r.copy_out);
+        }
+    };
     int nb = 0;
     for (int i = 0; i < P; ++i) {
         const int64_t r0 = int64_t(i) * Mp, mi = std::min(Mp, m - r0);
+        copy_a(i);
+        if (e != cudaSuccess) return cuda_fail("copy of an operand", e);
         cudaStreamWaitEvent(st, ev[i], 0);
         prep_a(i);
         for (int j = 0; j < Q; ++j, ++nb) {
             const int64_t c0 = int64_t(j) * Nq, nj = std::min(Nq, n - c0);
             if (i == 0) {
+                copy_b(j);
+                if (e != cudaSuccess) return cuda_fail("copy of an operand", e);
                 cudaStreamWaitEvent(st, ev[P + j], 0);
                 prep_b(j);
             }
@@ -1946,12 +1961,12 @@ int device_product_host_panels(const Gemm& g, const SplitRequest& req, const Lau
             count_launches(3);
             if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail("block launch", e);
             cudaEventRecord(ev[P + Q + nb], st);
-            cudaStreamWaitEvent(r.copy_out, ev[P + Q + nb], 0);
-            e = cudaMemcpy2DAsync(hC + r0 * g.ldc + c0, size_t(g.ldc) * 8, dC + r0 * n + c0, size_t(n) * 8,
-                                  size_t(nj) * 8, size_t(mi), cudaMemcpyDeviceToHost, r.copy_out);
-            if (e != cudaSuccess) return cuda_fail("copy of C back", e);
         }
+        if (i > 0) copy_c_out(i - 1);
+        if (e != cudaSuccess) return cuda_fail("copy of C back", e);
     }
+    copy_c_out(P - 1);
+    if (e != cudaSuccess) return cuda_fail("copy of C back", e);
     split_panels_summary_kernel<<<1, 32, 0, st>>>(reinterpret_cast<const uint8_t*>(info_at(P + Q)), info_stride,
                                                   P * Q, info_sum);
     count_launches(1);
