@@ -51,7 +51,7 @@ def parse():
     ap.add_argument("--no-batched", action="store_true", help="skip the batched small-product leg")
     ap.add_argument("--batch-count", type=int, default=10000)
     ap.add_argument("--no-serving", action="store_true", help="skip the serving leg")
-    ap.add_argument("--no-next", action="store_true", help="skip the gemv / zgemm / trmm leg")
+    ap.add_argument("--no-next", action="store_true", help="skip the gemv / trmv / zgemm / trmm leg")
     ap.add_argument("--sweep", default="", help="comma list of sweep groups to run instead of the main line: "
                                                  "square (4096/8192/16384, rr/rc, uniform/spread, native/split S=3..8/"
                                                  "bf16x3), rect ((M,K,N) = (65536,256,256), (256,65536,256), "
@@ -368,8 +368,9 @@ def next_leg(G, torch, args):
     """The BLAS routines next to ?gemm on the same seam, device-resident, each timed as synchronous
     calls (wall clock per call, launch and synchronisation included): dgemv on a 16384 x 8192
     matrix (bytes read / time against the measured HBM copy bandwidth), an FP64-accurate zgemm of
-    4096^3 (four split real products; 8 m n k flops) and an FP64-accurate dtrmm (left, lower) of
-    8192 x 8192 (m^2 n flops of a triangular product)."""
+    4096^3 (four split real products; 8 m n k flops), an FP64-accurate dtrmm (left, lower) of
+    8192 x 8192 (m^2 n flops of a triangular product), zgemv (conjugate transpose) on 8192 x 8192,
+    dtrmv on a 16384 x 16384 triangle and ztrmm of 4096 x 4096."""
     peaks, _ = read_peaks()
 
     def wall(fn, reps):
@@ -414,6 +415,38 @@ def next_leg(G, torch, args):
     out["dtrmm"] = {"n": n2, "ms": round(t * 1e3, 3), "tflops": round(float(n2) ** 3 / t / 1e12, 2),
                     "form": "masked triangle, one FP64-accurate split product"}
     del tA, tB
+    # complex gemv on 8192 x 8192 (bytes read / time), dtrmv on a 16384 x 16384 lower triangle
+    # (only the triangle is read), ztrmm 4096 x 4096 (4 m^2 n flops of a complex triangular product)
+    m3 = 8192
+    cA = torch.complex(dev_uniform(m3 * m3), dev_uniform(m3 * m3))
+    cx = torch.complex(dev_uniform(m3), dev_uniform(m3))
+    cy = torch.zeros(m3, dtype=torch.complex128, device="cuda")
+    t = wall(lambda: G.cblas_zgemv(101, 113, m3, m3, 1.0 + 0j, cA, m3, cx, 1, 0j, cy, 1), 20)
+    refc = cA.view(m3, m3).conj().T @ cx
+    gbs = 16.0 * (m3 * m3 + 2 * m3) / t / 1e9
+    out["zgemv"] = {"shape": [m3, m3], "op": "conjugate transpose", "ms": round(t * 1e3, 4), "gbs": round(gbs, 1),
+                    "frac_of_hbm": round(gbs / float(peaks.get("hbm_gbs", 6800.0)), 3),
+                    "max_rel_diff_vs_torch": float(((cy - refc).abs().max() / refc.abs().max()).item())}
+    del cA, cx, cy, refc
+    n4 = 16384
+    vA = dev_uniform(n4 * n4)
+    vx = dev_uniform(n4)
+    v0 = vx.clone()
+    t = wall(lambda: (vx.copy_(v0), G.cblas_trmv(101, 122, 111, 131, n4, vA, n4, vx, 1)), 20)
+    refv = torch.tril(vA.view(n4, n4)) @ v0
+    gbs = 8.0 * (n4 * (n4 + 1) / 2 + 2 * n4) / t / 1e9
+    out["dtrmv"] = {"n": n4, "ms": round(t * 1e3, 4), "gbs": round(gbs, 1),
+                    "frac_of_hbm": round(gbs / float(peaks.get("hbm_gbs", 6800.0)), 3),
+                    "bytes": "the lower triangle, x and the result",
+                    "max_rel_diff_vs_torch": float(((vx - refv).abs().max() / refv.abs().max()).item())}
+    del vA, vx, v0, refv
+    n5 = 4096
+    zT = torch.complex(dev_uniform(n5 * n5), dev_uniform(n5 * n5))
+    zB2 = torch.complex(dev_uniform(n5 * n5), dev_uniform(n5 * n5))
+    t = wall(lambda: G.cblas_ztrmm(101, 141, 122, 111, 131, n5, n5, 1.0 + 0j, zT, n5, zB2, n5), 3)
+    out["ztrmm"] = {"n": n5, "ms": round(t * 1e3, 3), "tflops": round(4.0 * float(n5) ** 3 / t / 1e12, 2),
+                    "form": "masked complex triangle, four FP64-accurate split real products"}
+    del zT, zB2
     out["inputs"] = "uniform [-1,1] generated on the device (torch.Generator, the bench seed)"
     return out
 

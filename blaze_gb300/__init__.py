@@ -124,6 +124,15 @@ def lib() -> ct.CDLL:
     for nm, T in (("cblas_dtrmm", D), ("cblas_strmm", F)):
         getattr(L, nm).argtypes = [ct.c_int] * 5 + [I32, I32, T, VP, I32, VP, I32]
         getattr(L, nm).restype = None
+    for nm in ("cblas_zgemv", "cblas_cgemv"):
+        getattr(L, nm).argtypes = [ct.c_int, ct.c_int, I32, I32, VP, VP, I32, VP, I32, VP, VP, I32]
+        getattr(L, nm).restype = None
+    for nm in ("cblas_ztrmm", "cblas_ctrmm"):
+        getattr(L, nm).argtypes = [ct.c_int] * 5 + [I32, I32, VP, VP, I32, VP, I32]
+        getattr(L, nm).restype = None
+    for nm in ("cblas_strmv", "cblas_dtrmv", "cblas_ctrmv", "cblas_ztrmv"):
+        getattr(L, nm).argtypes = [ct.c_int] * 4 + [I32, VP, I32, VP, I32]
+        getattr(L, nm).restype = None
     L.gb300_dgemm_ex.argtypes = [ct.c_int, ct.c_int, ct.c_int, I64, I64, I64, D, VP, I64, VP, I64, D, VP, I64,
                                  ct.POINTER(GemmOpts)]
     L.gb300_dgemm_ex.restype = ct.c_int
@@ -299,6 +308,40 @@ def cblas_trmm(order, side, uplo, transA, diag, m, n, alpha, A, lda, B, ldb, dty
     L = lib()
     L.gb300_clear_error()
     getattr(L, "cblas_%strmm" % dtype)(order, side, uplo, transA, diag, m, n, alpha, _addr(A), lda, _addr(B), ldb)
+    _raise_on_error()
+
+
+def cblas_zgemv(order, transA, m, n, alpha, A, lda, x, incx, beta, y, incy, single=False) -> None:
+    """cblas_zgemv (complex128) or cblas_cgemv (single=True, complex64): complex
+    y = alpha op(A) x + beta y, transposes 111 / 112 / 113 (conjugate)."""
+    L = lib()
+    import numpy as np
+    ct_t = np.complex64 if single else np.complex128
+    al = np.array([alpha], dtype=ct_t)
+    be = np.array([beta], dtype=ct_t)
+    L.gb300_clear_error()
+    getattr(L, "cblas_cgemv" if single else "cblas_zgemv")(order, transA, m, n, al.ctypes.data, _addr(A), lda, _addr(x),
+                                                          incx, be.ctypes.data, _addr(y), incy)
+    _raise_on_error()
+
+
+def cblas_trmv(order, uplo, transA, diag, n, A, lda, x, incx, dtype="d") -> None:
+    """cblas_?trmv, dtype "s", "d", "c" or "z": x = op(A) x with A n x n triangular."""
+    L = lib()
+    L.gb300_clear_error()
+    getattr(L, "cblas_%strmv" % dtype)(order, uplo, transA, diag, n, _addr(A), lda, _addr(x), incx)
+    _raise_on_error()
+
+
+def cblas_ztrmm(order, side, uplo, transA, diag, m, n, alpha, A, lda, B, ldb, single=False) -> None:
+    """cblas_ztrmm (complex128) or cblas_ctrmm (single=True, complex64): complex B = alpha op(A) B
+    (side 141) or alpha B op(A) (142), A triangular."""
+    L = lib()
+    import numpy as np
+    al = np.array([alpha], dtype=np.complex64 if single else np.complex128)
+    L.gb300_clear_error()
+    getattr(L, "cblas_ctrmm" if single else "cblas_ztrmm")(order, side, uplo, transA, diag, m, n, al.ctypes.data,
+                                                          _addr(A), lda, _addr(B), ldb)
     _raise_on_error()
 
 

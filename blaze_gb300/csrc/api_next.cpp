@@ -1,9 +1,12 @@
 // api_next.cpp — the BLAS routines next to ?gemm on Blaze's seam, on the GPU:
 //
-//   cblas_?gemv   y = alpha op(A) x + beta y          blaze/math/blas/cblas/gemv.h:116-235
+//   cblas_?gemv   y = alpha op(A) x + beta y (real and complex)
+//                                                     blaze/math/blas/cblas/gemv.h:116-235
+//   cblas_?trmv   x = op(A) x, A triangular (real and complex)
+//                                                     blaze/math/blas/cblas/trmv.h:111-218
 //   cblas_zgemm / cblas_cgemm  complex C = alpha op(A) op(B) + beta C
 //                                                     blaze/math/blas/cblas/gemm.h:196-256
-//   cblas_?trmm   B = alpha op(A) B or alpha B op(A), A triangular
+//   cblas_?trmm   B = alpha op(A) B or alpha B op(A), A triangular (real and complex)
 //                                                     blaze/math/blas/cblas/trmm.h:116-235
 //
 // Semantics follow CBLAS (argument positions as in xerbla, quick returns, beta == 0 does not read
@@ -11,8 +14,9 @@
 // the real and imaginary parts (conjugate-transpose flips the sign of an imaginary part), each
 // through the library's real product: FP64-accurate split precision for double by default, the
 // native kernel for float.  A triangular product runs on a dense copy of the triangle (zeros
-// elsewhere, ones on a unit diagonal).  Host operands are staged through device buffers;
-// device or managed operands are used in place.
+// elsewhere, ones on a unit diagonal); a triangular matrix x vector product masks the triangle in
+// the matrix x vector kernel itself.  Host operands are staged through device buffers; device or
+// managed operands are used in place (complex ones when 2 * sizeof(T)-aligned, else copied).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -42,11 +46,17 @@ bool on_device(const void* p) {
 }
 
 // aux workspace slots of these routines
-enum AuxSlot : int { kAuxA = 0, kAuxB, kAuxC, kAuxX, kAuxY, kAuxAr, kAuxAi, kAuxBr, kAuxBi, kAuxP };
+enum AuxSlot : int { kAuxA = 0, kAuxB, kAuxC, kAuxX, kAuxY, kAuxAr, kAuxAi, kAuxBr, kAuxBi, kAuxP, kAuxT };
+static_assert(kAuxT < kSlotCount, "aux slots");
+
+// A device or managed operand aligned for `elem`-byte element loads is used in place.
+bool in_place(const void* p, size_t elem) {
+    return on_device(p) && reinterpret_cast<uintptr_t>(p) % elem == 0;
+}
 
 // Device copy of `rows` x `cols` elements (pitch ld, elem bytes each) of a host or device buffer into
-// aux slot `slot` with the same pitch; returns the device pointer (or the buffer itself when it is
-// already on the device).
+// aux slot `slot` with the same pitch; returns the device pointer (or the buffer itself when `dev`:
+// it is used in place).
 void* stage(const void* p, int64_t rows, int64_t cols, int64_t ld, size_t elem, int slot, bool dev, cudaStream_t st,
             std::string* err) {
     if (dev || rows == 0 || cols == 0) return const_cast<void*>(p);
@@ -54,7 +64,7 @@ void* stage(const void* p, int64_t rows, int64_t cols, int64_t ld, size_t elem, 
     void* d = runtime().aux.get(slot, bytes, err);
     if (!d) return nullptr;
     const cudaError_t e = cudaMemcpy2DAsync(d, size_t(ld) * elem, p, size_t(ld) * elem, size_t(cols) * elem,
-                                            size_t(rows), cudaMemcpyHostToDevice, st);
+                                            size_t(rows), cudaMemcpyDefault, st);
     if (e != cudaSuccess) {
         if (err) *err = std::string("operand copy: ") + cudaGetErrorString(e);
         return nullptr;
@@ -62,9 +72,14 @@ void* stage(const void* p, int64_t rows, int64_t cols, int64_t ld, size_t elem, 
     return d;
 }
 
-cudaError_t unstage(void* host, const void* dev, int64_t rows, int64_t cols, int64_t ld, size_t elem, cudaStream_t st) {
+// The staged copy back into the caller's buffer (host, or a device buffer that was not used in
+// place): one linear copy when the rows are contiguous (see copy_to_host).
+cudaError_t unstage(void* dst, const void* dev, int64_t rows, int64_t cols, int64_t ld, size_t elem, cudaStream_t st) {
     if (rows == 0 || cols == 0) return cudaSuccess;
-    return copy_to_host(host, size_t(ld) * elem, dev, size_t(ld) * elem, size_t(cols) * elem, size_t(rows), st);
+    if (rows == 1 || ld == cols)
+        return cudaMemcpyAsync(dst, dev, size_t(rows) * size_t(cols) * elem, cudaMemcpyDefault, st);
+    return cudaMemcpy2DAsync(dst, size_t(ld) * elem, dev, size_t(ld) * elem, size_t(cols) * elem, size_t(rows),
+                             cudaMemcpyDefault, st);
 }
 
 // Finish a call: wait for the stream and read the device status word.
@@ -136,10 +151,18 @@ LaunchCtl fresh_ctl(cudaStream_t st) {
 
 }  // namespace
 
-// ---- gemv --------------------------------------------------------------------------------------
-template <typename T>
-int gemv_entry(int order, int transA, int64_t m, int64_t n, T alpha, const T* A, int64_t lda, const T* x,
-               int64_t incx, T beta, T* y, int64_t incy, const char* routine) {
+// ---- gemv / trmv ------------------------------------------------------------------------------
+namespace {
+// alpha / beta as (re, im) for complex, one value for real
+template <typename T, bool CPLX>
+bool scalar_is(const T* v, T re) {
+    return v[0] == re && (!CPLX || v[1] == T(0));
+}
+}  // namespace
+
+template <typename T, bool CPLX>
+int gemv_any(int order, int transA, int64_t m, int64_t n, const T* alpha, const T* A, int64_t lda, const T* x,
+             int64_t incx, const T* beta, T* y, int64_t incy, const char* routine) {
     auto fail = [&](int st, const std::string& msg) {
         set_error(st, std::string(routine) + ": " + msg);
         return st;
@@ -153,10 +176,12 @@ int gemv_entry(int order, int transA, int64_t m, int64_t n, T alpha, const T* A,
     if (lda < std::max<int64_t>(1, rm ? n : m)) return fail(GB300_ERR_INVALID_ARG, "parameter 7 (lda) is too small");
     if (incx == 0) return fail(GB300_ERR_INVALID_ARG, "parameter 9 (incx) is zero");
     if (incy == 0) return fail(GB300_ERR_INVALID_ARG, "parameter 12 (incy) is zero");
+    if (alpha == nullptr || beta == nullptr) return fail(GB300_ERR_INVALID_ARG, "alpha or beta is NULL");
     clear_error();
-    if (m == 0 || n == 0 || (alpha == T(0) && beta == T(1))) return GB300_OK;
+    const bool alpha0 = scalar_is<T, CPLX>(alpha, T(0));
+    if (m == 0 || n == 0 || (alpha0 && scalar_is<T, CPLX>(beta, T(1)))) return GB300_OK;
     if (y == nullptr) return fail(GB300_ERR_INVALID_ARG, "parameter 11 (y) is NULL");
-    if (alpha != T(0) && (A == nullptr || x == nullptr)) return fail(GB300_ERR_INVALID_ARG, "A or x is NULL");
+    if (!alpha0 && (A == nullptr || x == nullptr)) return fail(GB300_ERR_INVALID_ARG, "A or x is NULL");
 
     Runtime& r = runtime();
     std::lock_guard<std::mutex> lock(r.mu);
@@ -164,51 +189,180 @@ int gemv_entry(int order, int transA, int64_t m, int64_t n, T alpha, const T* A,
     int st = ensure_init(&err);
     if (st != GB300_OK) return fail(st, err);
     cudaStream_t s = r.stream;
-    const LaunchCtl ctl = fresh_ctl(s);
-    (void)ctl;
+    fresh_ctl(s);
 
+    const size_t elem = (CPLX ? 2 : 1) * sizeof(T);
+    const int64_t w = CPLX ? 2 : 1;  // T values per element
     // stored row-major S: A itself (row-major, m x n) or A^T (column-major, n x m)
     const int64_t srows = rm ? m : n, scols = rm ? n : m;
-    // y = S x (rows form) or y = S^T x (cols form)
-    const bool cols_form = rm ? ta : !ta;
     const int64_t xl = ta ? m : n, yl = ta ? n : m;
-    const bool use_a = alpha != T(0);
+    const bool use_a = !alpha0;
     const T* dS = A;
     if (use_a) {
-        dS = static_cast<const T*>(stage(A, srows, scols, lda, sizeof(T), kAuxA, on_device(A), s, &err));
+        dS = static_cast<const T*>(stage(A, srows, scols, lda, elem, kAuxA, in_place(A, elem), s, &err));
         if (!dS) return fail(GB300_ERR_NO_MEMORY, err);
     }
     const int64_t ax = incx < 0 ? -incx : incx, ay = incy < 0 ? -incy : incy;
     const T* dx = x;
     if (use_a) {
-        dx = static_cast<const T*>(stage(x, 1, 1 + (xl - 1) * ax, 1 + (xl - 1) * ax, sizeof(T), kAuxX, on_device(x), s, &err));
+        dx = static_cast<const T*>(stage(x, 1, 1 + (xl - 1) * ax, 1 + (xl - 1) * ax, elem, kAuxX, in_place(x, elem), s, &err));
         if (!dx) return fail(GB300_ERR_NO_MEMORY, err);
     }
-    const bool ydev = on_device(y);
-    T* dy = static_cast<T*>(stage(y, 1, 1 + (yl - 1) * ay, 1 + (yl - 1) * ay, sizeof(T), kAuxY, ydev, s, &err));
+    const bool ydev = in_place(y, elem);
+    T* dy = static_cast<T*>(stage(y, 1, 1 + (yl - 1) * ay, 1 + (yl - 1) * ay, elem, kAuxY, ydev, s, &err));
     if (!dy) return fail(GB300_ERR_NO_MEMORY, err);
     // logical element j of a strided vector: base + j * inc, the base at the far end for inc < 0
-    const T* xb = dx + (incx < 0 ? (xl - 1) * ax : 0);
-    T* yb = dy + (incy < 0 ? (yl - 1) * ay : 0);
-    const int64_t rows = cols_form ? srows : yl, cols = cols_form ? yl : (use_a ? scols : 0);
+    const T* xb = dx + (incx < 0 ? (xl - 1) * ax : 0) * w;
+    T* yb = dy + (incy < 0 ? (yl - 1) * ay : 0) * w;
+    MvForm f;
+    f.cols_form = use_a && (rm ? ta : !ta);  // y = S x (rows form) or y = S^T x (cols form)
+    f.conj = CPLX && transA == CblasConjTrans;
+    const int64_t rows = f.cols_form ? srows : yl, cols = f.cols_form ? yl : (use_a ? scols : 0);
     int slices = 1;
     T* part = nullptr;
-    if (cols_form && use_a) {
-        slices = int(std::max<int64_t>(1, std::min<int64_t>(64, srows / 256)));
-        part = static_cast<T*>(r.aux.get(kAuxP, size_t(slices) * size_t(yl) * sizeof(T), &err));
+    if (f.cols_form) {
+        slices = mv_cols_slices<T, CPLX>(srows, yl);
+        part = static_cast<T*>(r.aux.get(kAuxP, size_t(slices) * size_t(yl) * elem, &err));
         if (!part) return fail(GB300_ERR_NO_MEMORY, err);
     }
-    cudaError_t e = cols_form && use_a
-                        ? launch_gemv<T>(true, srows, yl, alpha, dS, lda, xb, incx, beta, yb, incy, part, slices, s)
-                        : launch_gemv<T>(false, rows, cols, alpha, dS, lda, xb, incx, beta, yb, incy, nullptr, 1, s);
+    cudaError_t e = launch_mv<T, CPLX>(f, rows, cols, alpha, dS, lda, xb, incx, beta, yb, incy, part, slices, s);
     if (e != cudaSuccess) return fail(GB300_ERR_CUDA, std::string("gemv launch: ") + cudaGetErrorString(e));
-    if (!ydev && (e = unstage(y, dy, 1, 1 + (yl - 1) * ay, 1 + (yl - 1) * ay, sizeof(T), s)) != cudaSuccess)
+    if (!ydev && (e = unstage(y, dy, 1, 1 + (yl - 1) * ay, 1 + (yl - 1) * ay, elem, s)) != cudaSuccess)
         return fail(GB300_ERR_CUDA, std::string("copy of y back: ") + cudaGetErrorString(e));
     st = finish(s, &err);
     return st == GB300_OK ? GB300_OK : fail(st, err);
 }
 
+template <typename T>
+int gemv_entry(int order, int transA, int64_t m, int64_t n, T alpha, const T* A, int64_t lda, const T* x,
+               int64_t incx, T beta, T* y, int64_t incy, const char* routine) {
+    return gemv_any<T, false>(order, transA, m, n, &alpha, A, lda, x, incx, &beta, y, incy, routine);
+}
+
+template <typename T>
+int cgemv_entry(int order, int transA, int64_t m, int64_t n, const T* alpha, const T* A, int64_t lda, const T* x,
+                int64_t incx, const T* beta, T* y, int64_t incy, const char* routine) {
+    return gemv_any<T, true>(order, transA, m, n, alpha, A, lda, x, incx, beta, y, incy, routine);
+}
+
+// x = op(A) x with A n x n triangular: the matrix x vector kernel over the triangle only (the
+// other half is not read), into a copy of x's span that then replaces x.
+template <typename T, bool CPLX>
+int trmv_entry(int order, int uplo, int transA, int diag, int64_t n, const T* A, int64_t lda, T* x, int64_t incx,
+               const char* routine) {
+    auto fail = [&](int st, const std::string& msg) {
+        set_error(st, std::string(routine) + ": " + msg);
+        return st;
+    };
+    if (order != CblasRowMajor && order != CblasColMajor) return fail(GB300_ERR_INVALID_ARG, "parameter 1 (order) is invalid");
+    if (uplo != CblasUpper && uplo != CblasLower) return fail(GB300_ERR_INVALID_ARG, "parameter 2 (uplo) is invalid");
+    if (transA != CblasNoTrans && transA != CblasTrans && transA != CblasConjTrans)
+        return fail(GB300_ERR_INVALID_ARG, "parameter 3 (transA) is invalid");
+    if (diag != CblasUnit && diag != CblasNonUnit) return fail(GB300_ERR_INVALID_ARG, "parameter 4 (diag) is invalid");
+    if (n < 0) return fail(GB300_ERR_INVALID_ARG, "parameter 5 (n) is negative");
+    if (lda < std::max<int64_t>(1, n)) return fail(GB300_ERR_INVALID_ARG, "parameter 7 (lda) is too small");
+    if (incx == 0) return fail(GB300_ERR_INVALID_ARG, "parameter 9 (incx) is zero");
+    clear_error();
+    if (n == 0) return GB300_OK;
+    if (A == nullptr || x == nullptr) return fail(GB300_ERR_INVALID_ARG, "A or x is NULL");
+
+    Runtime& r = runtime();
+    std::lock_guard<std::mutex> lock(r.mu);
+    std::string err;
+    int st = ensure_init(&err);
+    if (st != GB300_OK) return fail(st, err);
+    cudaStream_t s = r.stream;
+    fresh_ctl(s);
+
+    const size_t elem = (CPLX ? 2 : 1) * sizeof(T);
+    const int64_t w = CPLX ? 2 : 1;
+    const bool rm = order == CblasRowMajor, ta = transA != CblasNoTrans;
+    MvForm f;
+    f.cols_form = rm ? ta : !ta;
+    // S = A (row-major) or A^T (column-major), whose triangle is the other one
+    f.tri = (rm ? uplo == CblasLower : uplo == CblasUpper) ? 1 : 2;
+    f.unit = diag == CblasUnit;
+    f.conj = CPLX && transA == CblasConjTrans;
+    const T* dS = static_cast<const T*>(stage(A, n, n, lda, elem, kAuxA, in_place(A, elem), s, &err));
+    if (!dS) return fail(GB300_ERR_NO_MEMORY, err);
+    const int64_t ax = incx < 0 ? -incx : incx, span = 1 + (n - 1) * ax;
+    const bool xdev = in_place(x, elem);
+    const T* dx = static_cast<const T*>(stage(x, 1, span, span, elem, kAuxX, xdev, s, &err));
+    T* tmp = static_cast<T*>(r.aux.get(kAuxY, size_t(span) * elem, &err));
+    if (!dx || !tmp) return fail(GB300_ERR_NO_MEMORY, err);
+    cudaError_t e = cudaMemcpyAsync(tmp, dx, size_t(span) * elem, cudaMemcpyDeviceToDevice, s);  // keeps the gaps
+    const int64_t off = (incx < 0 ? (n - 1) * ax : 0) * w;
+    int slices = 1;
+    T* part = nullptr;
+    if (f.cols_form) {
+        slices = mv_cols_slices<T, CPLX>(n, n);
+        part = static_cast<T*>(r.aux.get(kAuxP, size_t(slices) * size_t(n) * elem, &err));
+        if (!part) return fail(GB300_ERR_NO_MEMORY, err);
+    }
+    const T one[2] = {T(1), T(0)}, zero[2] = {T(0), T(0)};
+    if (e == cudaSuccess)
+        e = launch_mv<T, CPLX>(f, n, n, one, dS, lda, dx + off, incx, zero, tmp + off, incx, part, slices, s);
+    if (e != cudaSuccess) return fail(GB300_ERR_CUDA, std::string("trmv launch: ") + cudaGetErrorString(e));
+    if ((e = unstage(x, tmp, 1, span, span, elem, s)) != cudaSuccess)
+        return fail(GB300_ERR_CUDA, std::string("copy of x back: ") + cudaGetErrorString(e));
+    st = finish(s, &err);
+    return st == GB300_OK ? GB300_OK : fail(st, err);
+}
+
 // ---- complex gemm ------------------------------------------------------------------------------
+namespace {
+// C (M x N interleaved complex, device, pitch ldc) = alpha op(A) op(B) + beta C in the logical
+// row-major form.  A and B are device interleaved complex operands in their stored shapes (pitches
+// la, lb); ca / cb conjugate an operand.  product == false (alpha == 0 or k == 0): C = beta C with
+// A and B not read.
+template <typename T>
+int complex_product(int64_t M, int64_t N, int64_t k, bool ta, bool tb, bool ca, bool cb, const T* dA, int64_t la,
+                    const T* dB, int64_t lb, const T* alpha, const T* beta, T* dC, int64_t ldc, bool product,
+                    const LaunchCtl& ctl, cudaStream_t s, std::string* err) {
+    Runtime& r = runtime();
+    int st = GB300_OK;
+    T* Pr = static_cast<T*>(r.aux.get(kAuxP, size_t(2) * size_t(M) * size_t(N) * sizeof(T), err));
+    if (!Pr) return GB300_ERR_NO_MEMORY;
+    T* Pi = Pr + M * N;
+    if (product) {
+        const int64_t ra = ta ? k : M, cA = ta ? M : k;  // stored shapes
+        const int64_t rb = tb ? N : k, cB = tb ? k : N;
+        T* Ar = static_cast<T*>(r.aux.get(kAuxAr, size_t(ra) * size_t(cA) * sizeof(T), err));
+        T* Ai = static_cast<T*>(r.aux.get(kAuxAi, size_t(ra) * size_t(cA) * sizeof(T), err));
+        T* Br = static_cast<T*>(r.aux.get(kAuxBr, size_t(rb) * size_t(cB) * sizeof(T), err));
+        T* Bi = static_cast<T*>(r.aux.get(kAuxBi, size_t(rb) * size_t(cB) * sizeof(T), err));
+        if (!Ar || !Ai || !Br || !Bi) return GB300_ERR_NO_MEMORY;
+        cudaError_t e = launch_split_complex<T>(ra, cA, dA, la, Ar, Ai, s);
+        if (e == cudaSuccess) e = launch_split_complex<T>(rb, cB, dB, lb, Br, Bi, s);
+        if (e != cudaSuccess) {
+            if (err) *err = std::string("complex split: ") + cudaGetErrorString(e);
+            return GB300_ERR_CUDA;
+        }
+        // op(A) = Ar' + i sa Ai', op(B) = Br' + i sb Bi' (sa = -1 for a conjugated operand):
+        // Re = Ar'Br' - sa sb Ai'Bi',  Im = sb Ar'Bi' + sa Ai'Br'
+        const double sa = ca ? -1.0 : 1.0, sb = cb ? -1.0 : 1.0;
+        auto prod = [&](const T* X, const T* Y, T* Z, double al, double be) {
+            Gemm g;
+            g.m = M; g.n = N; g.k = k; g.ta = ta; g.tb = tb;
+            g.A = X; g.lda = cA; g.B = Y; g.ldb = cB; g.C = Z; g.ldc = N;
+            g.alpha = al; g.beta = be;
+            return real_product<T>(g, ctl, s, err);
+        };
+        if ((st = prod(Ar, Br, Pr, 1.0, 0.0)) != GB300_OK || (st = prod(Ai, Bi, Pr, -sa * sb, 1.0)) != GB300_OK ||
+            (st = prod(Ar, Bi, Pi, sb, 0.0)) != GB300_OK || (st = prod(Ai, Br, Pi, sa, 1.0)) != GB300_OK)
+            return st;
+    } else {
+        cudaMemsetAsync(Pr, 0, size_t(2) * size_t(M) * size_t(N) * sizeof(T), s);
+    }
+    const cudaError_t e = launch_complex_epilogue<T>(M, N, Pr, Pi, alpha[0], alpha[1], beta[0], beta[1], dC, ldc, s);
+    if (e != cudaSuccess) {
+        if (err) *err = std::string("complex epilogue: ") + cudaGetErrorString(e);
+        return GB300_ERR_CUDA;
+    }
+    return GB300_OK;
+}
+}  // namespace
+
 template <typename T>
 int cgemm_entry(int order, int transA, int transB, int64_t m, int64_t n, int64_t k, const T* alpha, const T* A,
                 int64_t lda, const T* B, int64_t ldb, const T* beta, T* C, int64_t ldc, const char* routine) {
@@ -228,9 +382,8 @@ int cgemm_entry(int order, int transA, int transB, int64_t m, int64_t n, int64_t
     if (ldb < std::max<int64_t>(1, rm ? (tB ? k : n) : (tB ? n : k))) return fail(GB300_ERR_INVALID_ARG, "parameter 11 (ldb) is too small");
     if (ldc < std::max<int64_t>(1, rm ? n : m)) return fail(GB300_ERR_INVALID_ARG, "parameter 14 (ldc) is too small");
     if (alpha == nullptr || beta == nullptr) return fail(GB300_ERR_INVALID_ARG, "alpha or beta is NULL");
-    const T ar = alpha[0], ai = alpha[1], br = beta[0], bi = beta[1];
     clear_error();
-    const bool alpha0 = ar == T(0) && ai == T(0), beta1 = br == T(1) && bi == T(0);
+    const bool alpha0 = scalar_is<T, true>(alpha, T(0)), beta1 = scalar_is<T, true>(beta, T(1));
     if (m == 0 || n == 0 || ((alpha0 || k == 0) && beta1)) return GB300_OK;
     if (C == nullptr) return fail(GB300_ERR_INVALID_ARG, "parameter 13 (C) is NULL");
     const bool product = !alpha0 && k > 0;
@@ -243,6 +396,7 @@ int cgemm_entry(int order, int transA, int transB, int64_t m, int64_t n, int64_t
     if (st != GB300_OK) return fail(st, err);
     cudaStream_t s = r.stream;
     const LaunchCtl ctl = fresh_ctl(s);
+    const size_t elem = 2 * sizeof(T);
 
     // logical row-major form (C^T = op(B)^T op(A)^T for column-major; conjugation moves along)
     int64_t M = m, N = n;
@@ -255,45 +409,21 @@ int cgemm_entry(int order, int transA, int transB, int64_t m, int64_t n, int64_t
         ta = tB; tb = tA; ca = transB == CblasConjTrans; cb = transA == CblasConjTrans;
         pA = B; pB = A; la = ldb; lb = lda;
     }
-    const int64_t ra = ta ? k : M, cA = ta ? M : k;  // stored shape of the first operand
-    const int64_t rb = tb ? N : k, cB = tb ? k : N;
     // C: row-major M x N (pitch ldc) in either case
-    const bool cdev = on_device(C);
-    T* dC = static_cast<T*>(stage(C, M, N, ldc, 2 * sizeof(T), kAuxC, cdev, s, &err));
+    const bool cdev = in_place(C, elem);
+    T* dC = static_cast<T*>(stage(C, M, N, ldc, elem, kAuxC, cdev, s, &err));
     if (!dC) return fail(GB300_ERR_NO_MEMORY, err);
-    T* Pr = static_cast<T*>(r.aux.get(kAuxP, size_t(2) * size_t(M) * size_t(N) * sizeof(T), &err));
-    if (!Pr) return fail(GB300_ERR_NO_MEMORY, err);
-    T* Pi = Pr + M * N;
+    const T* dA = nullptr;
+    const T* dB = nullptr;
     if (product) {
-        const T* dA = static_cast<const T*>(stage(pA, ra, cA, la, 2 * sizeof(T), kAuxA, on_device(pA), s, &err));
-        const T* dB = static_cast<const T*>(stage(pB, rb, cB, lb, 2 * sizeof(T), kAuxB, on_device(pB), s, &err));
-        T* Ar = static_cast<T*>(r.aux.get(kAuxAr, size_t(ra) * size_t(cA) * sizeof(T), &err));
-        T* Ai = static_cast<T*>(r.aux.get(kAuxAi, size_t(ra) * size_t(cA) * sizeof(T), &err));
-        T* Br = static_cast<T*>(r.aux.get(kAuxBr, size_t(rb) * size_t(cB) * sizeof(T), &err));
-        T* Bi = static_cast<T*>(r.aux.get(kAuxBi, size_t(rb) * size_t(cB) * sizeof(T), &err));
-        if (!dA || !dB || !Ar || !Ai || !Br || !Bi) return fail(GB300_ERR_NO_MEMORY, err);
-        cudaError_t e = launch_split_complex<T>(ra, cA, dA, la, Ar, Ai, s);
-        if (e == cudaSuccess) e = launch_split_complex<T>(rb, cB, dB, lb, Br, Bi, s);
-        if (e != cudaSuccess) return fail(GB300_ERR_CUDA, std::string("complex split: ") + cudaGetErrorString(e));
-        // op(A) = Ar' + i sa Ai', op(B) = Br' + i sb Bi' (sa = -1 for the conjugate transpose):
-        // Re = Ar'Br' - sa sb Ai'Bi',  Im = sb Ar'Bi' + sa Ai'Br'
-        const double sa = ca ? -1.0 : 1.0, sb = cb ? -1.0 : 1.0;
-        auto prod = [&](const T* X, const T* Y, T* Z, double al, double be) {
-            Gemm g;
-            g.m = M; g.n = N; g.k = k; g.ta = ta; g.tb = tb;
-            g.A = X; g.lda = cA; g.B = Y; g.ldb = cB; g.C = Z; g.ldc = N;
-            g.alpha = al; g.beta = be;
-            return real_product<T>(g, ctl, s, &err);
-        };
-        if ((st = prod(Ar, Br, Pr, 1.0, 0.0)) != GB300_OK || (st = prod(Ai, Bi, Pr, -sa * sb, 1.0)) != GB300_OK ||
-            (st = prod(Ar, Bi, Pi, sb, 0.0)) != GB300_OK || (st = prod(Ai, Br, Pi, sa, 1.0)) != GB300_OK)
-            return fail(st, err);
-    } else {
-        cudaMemsetAsync(Pr, 0, size_t(2) * size_t(M) * size_t(N) * sizeof(T), s);
+        dA = static_cast<const T*>(stage(pA, ta ? k : M, ta ? M : k, la, elem, kAuxA, in_place(pA, elem), s, &err));
+        dB = static_cast<const T*>(stage(pB, tb ? N : k, tb ? k : N, lb, elem, kAuxB, in_place(pB, elem), s, &err));
+        if (!dA || !dB) return fail(GB300_ERR_NO_MEMORY, err);
     }
-    cudaError_t e = launch_complex_epilogue<T>(M, N, Pr, Pi, ar, ai, br, bi, dC, ldc, s);
-    if (e != cudaSuccess) return fail(GB300_ERR_CUDA, std::string("complex epilogue: ") + cudaGetErrorString(e));
-    if (!cdev && (e = unstage(C, dC, M, N, ldc, 2 * sizeof(T), s)) != cudaSuccess)
+    st = complex_product<T>(M, N, k, ta, tb, ca, cb, dA, la, dB, lb, alpha, beta, dC, ldc, product, ctl, s, &err);
+    if (st != GB300_OK) return fail(st, err);
+    cudaError_t e;
+    if (!cdev && (e = unstage(C, dC, M, N, ldc, elem, s)) != cudaSuccess)
         return fail(GB300_ERR_CUDA, std::string("copy of C back: ") + cudaGetErrorString(e));
     st = finish(s, &err);
     return st == GB300_OK ? GB300_OK : fail(st, err);
@@ -336,7 +466,7 @@ int trmm_entry(int order, int side, int uplo, int transA, int diag, int64_t m, i
     const int64_t sbr = rm ? m : n, sbc = rm ? n : m;
     const bool lower = rm ? (uplo == CblasLower) : (uplo == CblasUpper);
     const bool sa_left = rm ? left : !left;
-    const bool bdev = on_device(B);
+    const bool bdev = in_place(B, sizeof(T));
     T* dB = static_cast<T*>(stage(B, sbr, sbc, ldb, sizeof(T), kAuxB, bdev, s, &err));
     T* tmp = static_cast<T*>(r.aux.get(kAuxP, size_t(sbr) * size_t(sbc) * sizeof(T), &err));
     if (!dB || !tmp) return fail(GB300_ERR_NO_MEMORY, err);
@@ -346,10 +476,10 @@ int trmm_entry(int order, int side, int uplo, int transA, int diag, int64_t m, i
         g.k = 0;  // B = 0 without reading A
         g.A = dB; g.lda = sbc; g.B = dB; g.ldb = sbc;
     } else {
-        const T* dA = static_cast<const T*>(stage(A, ka, ka, lda, sizeof(T), kAuxA, on_device(A), s, &err));
+        const T* dA = static_cast<const T*>(stage(A, ka, ka, lda, sizeof(T), kAuxA, in_place(A, sizeof(T)), s, &err));
         T* tri = static_cast<T*>(r.aux.get(kAuxAr, size_t(ka) * size_t(ka) * sizeof(T), &err));
         if (!dA || !tri) return fail(GB300_ERR_NO_MEMORY, err);
-        cudaError_t e = launch_triangle<T>(ka, dA, lda, lower, diag == CblasUnit, tri, s);
+        cudaError_t e = launch_triangle<T, false>(ka, dA, lda, lower, diag == CblasUnit, tri, s);
         if (e != cudaSuccess) return fail(GB300_ERR_CUDA, std::string("triangle: ") + cudaGetErrorString(e));
         g.k = ka;
         if (sa_left) {  // SB = op(T) SB
@@ -371,6 +501,78 @@ int trmm_entry(int order, int side, int uplo, int transA, int diag, int64_t m, i
     return st == GB300_OK ? GB300_OK : fail(st, err);
 }
 
+// Complex B = alpha op(A) B or alpha B op(A), A triangular: the masked complex triangle and one
+// complex product (four real products).
+template <typename T>
+int ctrmm_entry(int order, int side, int uplo, int transA, int diag, int64_t m, int64_t n, const T* alpha, const T* A,
+                int64_t lda, T* B, int64_t ldb, const char* routine) {
+    auto fail = [&](int st, const std::string& msg) {
+        set_error(st, std::string(routine) + ": " + msg);
+        return st;
+    };
+    if (order != CblasRowMajor && order != CblasColMajor) return fail(GB300_ERR_INVALID_ARG, "parameter 1 (order) is invalid");
+    if (side != CblasLeft && side != CblasRight) return fail(GB300_ERR_INVALID_ARG, "parameter 2 (side) is invalid");
+    if (uplo != CblasUpper && uplo != CblasLower) return fail(GB300_ERR_INVALID_ARG, "parameter 3 (uplo) is invalid");
+    if (transA != CblasNoTrans && transA != CblasTrans && transA != CblasConjTrans)
+        return fail(GB300_ERR_INVALID_ARG, "parameter 4 (transA) is invalid");
+    if (diag != CblasUnit && diag != CblasNonUnit) return fail(GB300_ERR_INVALID_ARG, "parameter 5 (diag) is invalid");
+    if (m < 0) return fail(GB300_ERR_INVALID_ARG, "parameter 6 (m) is negative");
+    if (n < 0) return fail(GB300_ERR_INVALID_ARG, "parameter 7 (n) is negative");
+    const bool rm = order == CblasRowMajor, left = side == CblasLeft, ta = transA != CblasNoTrans;
+    const int64_t ka = left ? m : n;
+    if (lda < std::max<int64_t>(1, ka)) return fail(GB300_ERR_INVALID_ARG, "parameter 10 (lda) is too small");
+    if (ldb < std::max<int64_t>(1, rm ? n : m)) return fail(GB300_ERR_INVALID_ARG, "parameter 12 (ldb) is too small");
+    if (alpha == nullptr) return fail(GB300_ERR_INVALID_ARG, "parameter 8 (alpha) is NULL");
+    clear_error();
+    if (m == 0 || n == 0) return GB300_OK;
+    const bool alpha0 = scalar_is<T, true>(alpha, T(0));
+    if (B == nullptr || (!alpha0 && A == nullptr)) return fail(GB300_ERR_INVALID_ARG, "A or B is NULL");
+
+    Runtime& r = runtime();
+    std::lock_guard<std::mutex> lock(r.mu);
+    std::string err;
+    int st = ensure_init(&err);
+    if (st != GB300_OK) return fail(st, err);
+    cudaStream_t s = r.stream;
+    const LaunchCtl ctl = fresh_ctl(s);
+    const size_t elem = 2 * sizeof(T);
+
+    // as for the real case: SB = B or B^T in row-major storage, the triangle flips for column-major
+    // and so does the side; a conjugate transpose conjugates the triangle's elements
+    const int64_t sbr = rm ? m : n, sbc = rm ? n : m;
+    const bool lower = rm ? (uplo == CblasLower) : (uplo == CblasUpper);
+    const bool sa_left = rm ? left : !left;
+    const bool conj = transA == CblasConjTrans;
+    const bool bdev = in_place(B, elem);
+    T* dB = static_cast<T*>(stage(B, sbr, sbc, ldb, elem, kAuxB, bdev, s, &err));
+    T* tmp = static_cast<T*>(r.aux.get(kAuxC, size_t(sbr) * size_t(sbc) * elem, &err));
+    if (!dB || !tmp) return fail(GB300_ERR_NO_MEMORY, err);
+    const T zero[2] = {T(0), T(0)};
+    if (alpha0) {
+        st = complex_product<T>(sbr, sbc, 0, false, false, false, false, nullptr, 1, nullptr, 1, alpha, zero, tmp, sbc,
+                                false, ctl, s, &err);
+    } else {
+        const T* dA = static_cast<const T*>(stage(A, ka, ka, lda, elem, kAuxA, in_place(A, elem), s, &err));
+        T* tri = static_cast<T*>(r.aux.get(kAuxT, size_t(ka) * size_t(ka) * elem, &err));
+        if (!dA || !tri) return fail(GB300_ERR_NO_MEMORY, err);
+        cudaError_t e = launch_triangle<T, true>(ka, dA, lda, lower, diag == CblasUnit, tri, s);
+        if (e != cudaSuccess) return fail(GB300_ERR_CUDA, std::string("triangle: ") + cudaGetErrorString(e));
+        if (sa_left)  // SB = op(T) SB
+            st = complex_product<T>(sbr, sbc, ka, ta, false, conj, false, tri, ka, dB, ldb, alpha, zero, tmp, sbc, true,
+                                    ctl, s, &err);
+        else  // SB = SB op(T)
+            st = complex_product<T>(sbr, sbc, ka, false, ta, false, conj, dB, ldb, tri, ka, alpha, zero, tmp, sbc, true,
+                                    ctl, s, &err);
+    }
+    if (st != GB300_OK) return fail(st, err);
+    cudaError_t e = cudaMemcpy2DAsync(bdev ? static_cast<void*>(B) : static_cast<void*>(dB), size_t(ldb) * elem, tmp,
+                                      size_t(sbc) * elem, size_t(sbc) * elem, size_t(sbr), cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess && !bdev) e = unstage(B, dB, sbr, sbc, ldb, elem, s);
+    if (e != cudaSuccess) return fail(GB300_ERR_CUDA, std::string("copy of B back: ") + cudaGetErrorString(e));
+    st = finish(s, &err);
+    return st == GB300_OK ? GB300_OK : fail(st, err);
+}
+
 template int gemv_entry<double>(int, int, int64_t, int64_t, double, const double*, int64_t, const double*, int64_t,
                                 double, double*, int64_t, const char*);
 template int gemv_entry<float>(int, int, int64_t, int64_t, float, const float*, int64_t, const float*, int64_t, float,
@@ -383,4 +585,18 @@ template int trmm_entry<double>(int, int, int, int, int, int64_t, int64_t, doubl
                                 int64_t, const char*);
 template int trmm_entry<float>(int, int, int, int, int, int64_t, int64_t, float, const float*, int64_t, float*, int64_t,
                                const char*);
+template int cgemv_entry<double>(int, int, int64_t, int64_t, const double*, const double*, int64_t, const double*,
+                                 int64_t, const double*, double*, int64_t, const char*);
+template int cgemv_entry<float>(int, int, int64_t, int64_t, const float*, const float*, int64_t, const float*, int64_t,
+                                const float*, float*, int64_t, const char*);
+template int trmv_entry<double, false>(int, int, int, int, int64_t, const double*, int64_t, double*, int64_t,
+                                       const char*);
+template int trmv_entry<float, false>(int, int, int, int, int64_t, const float*, int64_t, float*, int64_t, const char*);
+template int trmv_entry<double, true>(int, int, int, int, int64_t, const double*, int64_t, double*, int64_t,
+                                      const char*);
+template int trmv_entry<float, true>(int, int, int, int, int64_t, const float*, int64_t, float*, int64_t, const char*);
+template int ctrmm_entry<double>(int, int, int, int, int, int64_t, int64_t, const double*, const double*, int64_t,
+                                 double*, int64_t, const char*);
+template int ctrmm_entry<float>(int, int, int, int, int, int64_t, int64_t, const float*, const float*, int64_t, float*,
+                                int64_t, const char*);
 }  // namespace gb

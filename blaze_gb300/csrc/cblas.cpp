@@ -3,8 +3,8 @@
 // Compiled twice: once with 32-bit integers (the standard names) and once with
 // -DGB300_BLAS_ILP64 (names with a _64 suffix), matching blaze/math/blas/Types.h:56-64.
 //
-// cblas_dgemm / cblas_sgemm run on the GPU (api.cpp), and so do cblas_?gemv, cblas_cgemm /
-// cblas_zgemm and cblas_strmm / cblas_dtrmm (api_next.cpp).  The remaining routines exist so that
+// cblas_dgemm / cblas_sgemm run on the GPU (api.cpp), and so do cblas_?gemv, cblas_?trmv,
+// cblas_cgemm / cblas_zgemm and cblas_?trmm, real and complex (api_next.cpp).  The remaining routines exist so that
 // every function Blaze's wrappers name (the headers under blaze/math/blas/cblas/) resolves; they
 // compute nothing and record GB300_ERR_NOT_SUPPORTED, so a caller reaching them learns it at once
 // instead of receiving a silent CPU result.
@@ -81,13 +81,19 @@ void cblas_dgemv(CBLAS_ORDER order, CBLAS_TRANSPOSE transA, gb300_blas_int m, gb
     gb::gemv_entry<double>(int(order), int(transA), int64_t(m), int64_t(n), alpha, A, int64_t(lda), x, int64_t(incx),
                            beta, y, int64_t(incy), "cblas_dgemv");
 }
-void cblas_cgemv(CBLAS_ORDER, CBLAS_TRANSPOSE, gb300_blas_int, gb300_blas_int, const void*, const void*,
-                 gb300_blas_int, const void*, gb300_blas_int, const void*, void*, gb300_blas_int) {
-    not_supported("cblas_cgemv");
+void cblas_cgemv(CBLAS_ORDER order, CBLAS_TRANSPOSE transA, gb300_blas_int m, gb300_blas_int n, const void* alpha,
+                 const void* A, gb300_blas_int lda, const void* x, gb300_blas_int incx, const void* beta, void* y,
+                 gb300_blas_int incy) {
+    gb::cgemv_entry<float>(int(order), int(transA), int64_t(m), int64_t(n), static_cast<const float*>(alpha),
+                           static_cast<const float*>(A), int64_t(lda), static_cast<const float*>(x), int64_t(incx),
+                           static_cast<const float*>(beta), static_cast<float*>(y), int64_t(incy), "cblas_cgemv");
 }
-void cblas_zgemv(CBLAS_ORDER, CBLAS_TRANSPOSE, gb300_blas_int, gb300_blas_int, const void*, const void*,
-                 gb300_blas_int, const void*, gb300_blas_int, const void*, void*, gb300_blas_int) {
-    not_supported("cblas_zgemv");
+void cblas_zgemv(CBLAS_ORDER order, CBLAS_TRANSPOSE transA, gb300_blas_int m, gb300_blas_int n, const void* alpha,
+                 const void* A, gb300_blas_int lda, const void* x, gb300_blas_int incx, const void* beta, void* y,
+                 gb300_blas_int incy) {
+    gb::cgemv_entry<double>(int(order), int(transA), int64_t(m), int64_t(n), static_cast<const double*>(alpha),
+                            static_cast<const double*>(A), int64_t(lda), static_cast<const double*>(x), int64_t(incx),
+                            static_cast<const double*>(beta), static_cast<double*>(y), int64_t(incy), "cblas_zgemv");
 }
 void cblas_strmm(CBLAS_ORDER order, CBLAS_SIDE side, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA, CBLAS_DIAG diag,
                  gb300_blas_int m, gb300_blas_int n, float alpha, const float* A, gb300_blas_int lda, float* B,
@@ -101,18 +107,41 @@ void cblas_dtrmm(CBLAS_ORDER order, CBLAS_SIDE side, CBLAS_UPLO uplo, CBLAS_TRAN
     gb::trmm_entry<double>(int(order), int(side), int(uplo), int(transA), int(diag), int64_t(m), int64_t(n), alpha, A,
                            int64_t(lda), B, int64_t(ldb), "cblas_dtrmm");
 }
-void cblas_ctrmm(CBLAS_ORDER, CBLAS_SIDE, CBLAS_UPLO, CBLAS_TRANSPOSE, CBLAS_DIAG, gb300_blas_int, gb300_blas_int,
-                 const void*, const void*, gb300_blas_int, void*, gb300_blas_int) { not_supported("cblas_ctrmm"); }
-void cblas_ztrmm(CBLAS_ORDER, CBLAS_SIDE, CBLAS_UPLO, CBLAS_TRANSPOSE, CBLAS_DIAG, gb300_blas_int, gb300_blas_int,
-                 const void*, const void*, gb300_blas_int, void*, gb300_blas_int) { not_supported("cblas_ztrmm"); }
-void cblas_strmv(CBLAS_ORDER, CBLAS_UPLO, CBLAS_TRANSPOSE, CBLAS_DIAG, gb300_blas_int, const float*, gb300_blas_int,
-                 float*, gb300_blas_int) { not_supported("cblas_strmv"); }
-void cblas_dtrmv(CBLAS_ORDER, CBLAS_UPLO, CBLAS_TRANSPOSE, CBLAS_DIAG, gb300_blas_int, const double*, gb300_blas_int,
-                 double*, gb300_blas_int) { not_supported("cblas_dtrmv"); }
-void cblas_ctrmv(CBLAS_ORDER, CBLAS_UPLO, CBLAS_TRANSPOSE, CBLAS_DIAG, gb300_blas_int, const void*, gb300_blas_int,
-                 void*, gb300_blas_int) { not_supported("cblas_ctrmv"); }
-void cblas_ztrmv(CBLAS_ORDER, CBLAS_UPLO, CBLAS_TRANSPOSE, CBLAS_DIAG, gb300_blas_int, const void*, gb300_blas_int,
-                 void*, gb300_blas_int) { not_supported("cblas_ztrmv"); }
+void cblas_ctrmm(CBLAS_ORDER order, CBLAS_SIDE side, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA, CBLAS_DIAG diag,
+                 gb300_blas_int m, gb300_blas_int n, const void* alpha, const void* A, gb300_blas_int lda, void* B,
+                 gb300_blas_int ldb) {
+    gb::ctrmm_entry<float>(int(order), int(side), int(uplo), int(transA), int(diag), int64_t(m), int64_t(n),
+                           static_cast<const float*>(alpha), static_cast<const float*>(A), int64_t(lda),
+                           static_cast<float*>(B), int64_t(ldb), "cblas_ctrmm");
+}
+void cblas_ztrmm(CBLAS_ORDER order, CBLAS_SIDE side, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA, CBLAS_DIAG diag,
+                 gb300_blas_int m, gb300_blas_int n, const void* alpha, const void* A, gb300_blas_int lda, void* B,
+                 gb300_blas_int ldb) {
+    gb::ctrmm_entry<double>(int(order), int(side), int(uplo), int(transA), int(diag), int64_t(m), int64_t(n),
+                            static_cast<const double*>(alpha), static_cast<const double*>(A), int64_t(lda),
+                            static_cast<double*>(B), int64_t(ldb), "cblas_ztrmm");
+}
+void cblas_strmv(CBLAS_ORDER order, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA, CBLAS_DIAG diag, gb300_blas_int n,
+                 const float* A, gb300_blas_int lda, float* x, gb300_blas_int incx) {
+    gb::trmv_entry<float, false>(int(order), int(uplo), int(transA), int(diag), int64_t(n), A, int64_t(lda), x,
+                                 int64_t(incx), "cblas_strmv");
+}
+void cblas_dtrmv(CBLAS_ORDER order, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA, CBLAS_DIAG diag, gb300_blas_int n,
+                 const double* A, gb300_blas_int lda, double* x, gb300_blas_int incx) {
+    gb::trmv_entry<double, false>(int(order), int(uplo), int(transA), int(diag), int64_t(n), A, int64_t(lda), x,
+                                  int64_t(incx), "cblas_dtrmv");
+}
+void cblas_ctrmv(CBLAS_ORDER order, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA, CBLAS_DIAG diag, gb300_blas_int n,
+                 const void* A, gb300_blas_int lda, void* x, gb300_blas_int incx) {
+    gb::trmv_entry<float, true>(int(order), int(uplo), int(transA), int(diag), int64_t(n), static_cast<const float*>(A),
+                                int64_t(lda), static_cast<float*>(x), int64_t(incx), "cblas_ctrmv");
+}
+void cblas_ztrmv(CBLAS_ORDER order, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA, CBLAS_DIAG diag, gb300_blas_int n,
+                 const void* A, gb300_blas_int lda, void* x, gb300_blas_int incx) {
+    gb::trmv_entry<double, true>(int(order), int(uplo), int(transA), int(diag), int64_t(n),
+                                 static_cast<const double*>(A), int64_t(lda), static_cast<double*>(x), int64_t(incx),
+                                 "cblas_ztrmv");
+}
 void cblas_strsm(CBLAS_ORDER, CBLAS_SIDE, CBLAS_UPLO, CBLAS_TRANSPOSE, CBLAS_DIAG, gb300_blas_int, gb300_blas_int,
                  float, const float*, gb300_blas_int, float*, gb300_blas_int) { not_supported("cblas_strsm"); }
 void cblas_dtrsm(CBLAS_ORDER, CBLAS_SIDE, CBLAS_UPLO, CBLAS_TRANSPOSE, CBLAS_DIAG, gb300_blas_int, gb300_blas_int,

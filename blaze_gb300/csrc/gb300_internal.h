@@ -85,6 +85,18 @@ int cgemm_entry(int order, int transA, int transB, int64_t m, int64_t n, int64_t
 template <typename T>
 int trmm_entry(int order, int side, int uplo, int transA, int diag, int64_t m, int64_t n, T alpha, const T* A,
                int64_t lda, T* B, int64_t ldb, const char* routine);
+// complex interleaved y = alpha op(A) x + beta y; alpha, beta point to (re, im)
+template <typename T>
+int cgemv_entry(int order, int transA, int64_t m, int64_t n, const T* alpha, const T* A, int64_t lda, const T* x,
+                int64_t incx, const T* beta, T* y, int64_t incy, const char* routine);
+// x = op(A) x, A triangular; CPLX: interleaved complex elements
+template <typename T, bool CPLX>
+int trmv_entry(int order, int uplo, int transA, int diag, int64_t n, const T* A, int64_t lda, T* x, int64_t incx,
+               const char* routine);
+// complex interleaved B = alpha op(A) B or alpha B op(A), A triangular; alpha points to (re, im)
+template <typename T>
+int ctrmm_entry(int order, int side, int uplo, int transA, int diag, int64_t m, int64_t n, const T* alpha, const T* A,
+                int64_t lda, T* B, int64_t ldb, const char* routine);
 
 template <typename T>
 int gemm_entry(int order, int transA, int transB, int64_t m, int64_t n, int64_t k, T alpha, const T* A, int64_t lda,

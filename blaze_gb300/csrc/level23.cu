@@ -1,6 +1,7 @@
-// level23.cu — kernels of the BLAS routines next to ?gemm on Blaze's seam: ?gemv (matrix x vector),
-// complex ?gemm (four real products over split real / imaginary planes) and ?trmm (triangular
-// product through a masked copy of the triangle).  The host entries are in api_next.cpp.
+// level23.cu — kernels of the BLAS routines next to ?gemm on Blaze's seam: ?gemv and ?trmv (matrix x
+// vector, real or complex, a triangle optionally masked), complex ?gemm (four real products over
+// split real / imaginary planes) and ?trmm (triangular product through a masked copy of the
+// triangle).  The host entries are in api_next.cpp.
 //
 // Matrix operands are described in row-major storage (rows x cols, pitch ld); a column-major
 // CBLAS operand is the transpose of its row-major storage, which the host folds into the
@@ -9,6 +10,8 @@
 
 #include <algorithm>
 #include <cstdint>
+#include <cstring>
+#include <type_traits>
 
 #include "gb300_internal.h"
 #include "level23.h"
@@ -17,51 +20,131 @@
 namespace gb {
 namespace {
 
-// ---- gemv ------------------------------------------------------------------------------------
-// y[i] = alpha * sum_j S[i][j] x[j] + beta * y[i] for i < rows: one warp per row, lanes stride over
-// the row (coalesced), a shuffle reduction, FP64 (or FP32) accumulation in the element type.
+// ---- matrix x vector (gemv, trmv) ------------------------------------------------------------
+// Element arithmetic: V = T (real) or Cx<T> (complex, interleaved re / im).
 template <typename T>
-__global__ void gemv_rows_kernel(int64_t rows, int64_t cols, T alpha, const T* __restrict__ S, int64_t ld,
-                                 const T* __restrict__ x, int64_t incx, T beta, T* __restrict__ y, int64_t incy) {
+struct alignas(2 * sizeof(T)) Cx {
+    T re, im;
+};
+
+template <typename V>
+struct Ar {  // real
+    __device__ static V zero() { return V(0); }
+    __device__ static V one() { return V(1); }
+    __device__ static V conj(V a) { return a; }
+    __device__ static V fmadd(V a, V b, V c) { return fma(a, b, c); }
+    __device__ static V mul(V a, V b) { return a * b; }
+    __device__ static V add(V a, V b) { return a + b; }
+    __device__ static bool is_zero(V a) { return a == V(0); }
+    __device__ static V shfl_xor(V a, int o) { return __shfl_xor_sync(0xffffffffu, a, o); }
+    // alpha * acc + beta * y, y not read when beta == 0
+    __device__ static V axpby(V alpha, V acc, V beta, const V* y) {
+        return is_zero(beta) ? alpha * acc : fma(beta, *y, alpha * acc);
+    }
+};
+
+template <typename T>
+struct Ar<Cx<T>> {  // complex
+    using V = Cx<T>;
+    __device__ static V zero() { return V{T(0), T(0)}; }
+    __device__ static V one() { return V{T(1), T(0)}; }
+    __device__ static V conj(V a) { return V{a.re, -a.im}; }
+    __device__ static V fmadd(V a, V b, V c) {
+        return V{fma(a.re, b.re, fma(-a.im, b.im, c.re)), fma(a.re, b.im, fma(a.im, b.re, c.im))};
+    }
+    __device__ static V mul(V a, V b) { return V{a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re}; }
+    __device__ static V add(V a, V b) { return V{a.re + b.re, a.im + b.im}; }
+    __device__ static bool is_zero(V a) { return a.re == T(0) && a.im == T(0); }
+    __device__ static V shfl_xor(V a, int o) {
+        return V{__shfl_xor_sync(0xffffffffu, a.re, o), __shfl_xor_sync(0xffffffffu, a.im, o)};
+    }
+    __device__ static V axpby(V alpha, V acc, V beta, const V* y) {
+        const V t = mul(alpha, acc);
+        return is_zero(beta) ? t : fmadd(beta, *y, t);
+    }
+};
+
+// Element a of S at (i, j) as op sees it: one on a unit diagonal, conjugated for a conjugate
+// transpose (the element is read only off a unit diagonal).
+template <typename V>
+__device__ __forceinline__ V mv_elem(const V* __restrict__ p, bool diag_one, int conj) {
+    if (diag_one) return Ar<V>::one();
+    const V a = *p;
+    return conj ? Ar<V>::conj(a) : a;
+}
+
+// y[i] = alpha * sum_j S[i][j] x[j] + beta * y[i] for i < rows: one warp per row, lanes stride over
+// the row (coalesced; pointers step, no index products per element), a shuffle reduction.
+// tri = 1 (lower) keeps j <= i, tri = 2 (upper) j >= i.  FP64 data is bound by the FP64 pipe here
+// (one FMA per 8-byte element, four per 16-byte complex element), not by HBM; a single
+// accumulator per lane keeps the registers low and the occupancy high, which measured faster than
+// unrolled partial sums or several warps per row.
+template <typename V>
+__global__ void __launch_bounds__(256) mv_rows_kernel(int64_t rows, int64_t cols, V alpha, const V* __restrict__ S,
+                                                      int64_t ld, const V* __restrict__ x, int64_t incx, V beta,
+                                                      V* __restrict__ y, int64_t incy, int tri, int unit, int conj) {
+    using A = Ar<V>;
     const int lane = threadIdx.x & 31;
     const int64_t warps = (int64_t(gridDim.x) * blockDim.x) >> 5;
+    const int64_t xstep = 32 * incx;
     for (int64_t i = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; i < rows; i += warps) {
-        const T* row = S + i * ld;
-        T acc = T(0);
-        for (int64_t j = lane; j < cols; j += 32) acc = fma(row[j], x[j * incx], acc);
+        const int64_t j0 = tri == 2 ? i : 0, j1 = tri == 1 ? min(cols, i + 1) : cols;
+        V acc = A::zero();
+        const V* sp = S + i * ld + j0 + lane;
+        const V* xp = x + (j0 + lane) * incx;
+        for (int64_t j = j0 + lane; j < j1; j += 32, sp += 32, xp += xstep)
+            acc = A::fmadd(mv_elem(sp, unit && j == i, conj), *xp, acc);
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        for (int o = 16; o > 0; o >>= 1) acc = A::add(acc, A::shfl_xor(acc, o));
         if (lane == 0) {
-            T* yi = y + i * incy;
-            *yi = (beta == T(0)) ? alpha * acc : fma(beta, *yi, alpha * acc);
+            V* yi = y + i * incy;
+            *yi = A::axpby(alpha, acc, beta, yi);
         }
     }
 }
 
 // Partial column sums: part[s][j] = sum_{i in slice s} S[i][j] x[i] for j < cols, threads over j
-// (coalesced), slice s of the rows per blockIdx.y.
-template <typename T>
-__global__ void gemv_cols_partial_kernel(int64_t rows, int64_t cols, const T* __restrict__ S, int64_t ld,
-                                         const T* __restrict__ x, int64_t incx, int64_t rows_per_slice,
-                                         T* __restrict__ part) {
+// (coalesced), slice s of the rows per blockIdx.y; tri = 1 (lower) keeps i >= j, tri = 2 (upper)
+// i <= j.
+template <typename V>
+__global__ void __launch_bounds__(256) mv_cols_partial_kernel(int64_t rows, int64_t cols, const V* __restrict__ S,
+                                                              int64_t ld, const V* __restrict__ x, int64_t incx,
+                                                              int64_t rows_per_slice, V* __restrict__ part, int tri,
+                                                              int unit, int conj) {
+    using A = Ar<V>;
     const int64_t j = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (j >= cols) return;
-    const int64_t i0 = int64_t(blockIdx.y) * rows_per_slice, i1 = min(rows, i0 + rows_per_slice);
-    T acc = T(0);
-    for (int64_t i = i0; i < i1; ++i) acc = fma(S[i * ld + j], x[i * incx], acc);
+    int64_t i0 = int64_t(blockIdx.y) * rows_per_slice, i1 = min(rows, i0 + rows_per_slice);
+    if (tri == 1) i0 = max(i0, j);
+    if (tri == 2) i1 = min(i1, j + 1);
+    V acc = A::zero();
+    const V* sp = S + i0 * ld + j;
+    const V* xp = x + i0 * incx;
+    for (int64_t i = i0; i < i1; ++i, sp += ld, xp += incx) acc = A::fmadd(mv_elem(sp, unit && i == j, conj), *xp, acc);
     part[int64_t(blockIdx.y) * cols + j] = acc;
 }
 
-// y[j] = alpha * sum_s part[s][j] + beta * y[j] (slices summed in a fixed order: deterministic).
-template <typename T>
-__global__ void gemv_cols_reduce_kernel(int64_t cols, int slices, const T* __restrict__ part, T alpha, T beta,
-                                        T* __restrict__ y, int64_t incy) {
-    const int64_t j = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (j >= cols) return;
-    T acc = T(0);
-    for (int s = 0; s < slices; ++s) acc += part[int64_t(s) * cols + j];
-    T* yj = y + j * incy;
-    *yj = (beta == T(0)) ? alpha * acc : fma(beta, *yj, alpha * acc);
+// y[j] = alpha * sum_s part[s][j] + beta * y[j]: 32 columns per block, eight threads per column
+// each summing every eighth slice, then the eight sums in a fixed order (deterministic).
+template <typename V>
+__global__ void __launch_bounds__(256) mv_cols_reduce_kernel(int64_t cols, int slices, const V* __restrict__ part,
+                                                             V alpha, V beta, V* __restrict__ y, int64_t incy) {
+    using A = Ar<V>;
+    __shared__ V red[8][32];
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const int64_t j = int64_t(blockIdx.x) * 32 + tx;
+    V acc = A::zero();
+    if (j < cols)
+        for (int s = ty; s < slices; s += 8) acc = A::add(acc, part[int64_t(s) * cols + j]);
+    red[ty][tx] = acc;
+    __syncthreads();
+    if (ty == 0 && j < cols) {
+        V t = red[0][tx];
+#pragma unroll
+        for (int w = 1; w < 8; ++w) t = A::add(t, red[w][tx]);
+        V* yj = y + j * incy;
+        *yj = A::axpby(alpha, t, beta, yj);
+    }
 }
 
 // ---- complex planes --------------------------------------------------------------------------
@@ -102,38 +185,55 @@ __global__ void complex_epilogue_kernel(int64_t rows, int64_t cols, const T* __r
 // ---- triangle --------------------------------------------------------------------------------
 // T (dense n x n, pitch n) = the `lower` (or upper) triangle of A (n x n, pitch lda, row-major
 // storage) with zeros elsewhere and ones on the diagonal when `unit`.
-template <typename T>
-__global__ void triangle_kernel(int64_t n, const T* __restrict__ A, int64_t lda, int lower, int unit,
-                                T* __restrict__ out) {
+template <typename V>
+__global__ void triangle_kernel(int64_t n, const V* __restrict__ A, int64_t lda, int lower, int unit,
+                                V* __restrict__ out) {
     const int64_t total = n * n;
     for (int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; e < total; e += int64_t(gridDim.x) * blockDim.x) {
         const int64_t i = e / n, j = e - i * n;
         const bool in = lower ? (j <= i) : (j >= i);
-        out[e] = !in ? T(0) : ((unit && i == j) ? T(1) : A[i * lda + j]);
+        out[e] = !in ? Ar<V>::zero() : ((unit && i == j) ? Ar<V>::one() : A[i * lda + j]);
     }
 }
 
-unsigned grid_for(int64_t work, int threads, int num_sms) {
+// Blocks for `work` threads of `threads` per block, at most `per_sm` blocks per SM (grid-stride
+// loops take the rest).
+unsigned grid_for(int64_t work, int threads, int num_sms, int per_sm = 16) {
     const int64_t b = (work + threads - 1) / threads;
-    return unsigned(std::max<int64_t>(1, std::min<int64_t>(b, int64_t(num_sms) * 16)));
+    return unsigned(std::max<int64_t>(1, std::min<int64_t>(b, int64_t(num_sms) * per_sm)));
 }
 
 }  // namespace
 
-template <typename T>
-cudaError_t launch_gemv(bool cols_form, int64_t rows, int64_t cols, T alpha, const T* S, int64_t ld, const T* x,
-                        int64_t incx, T beta, T* y, int64_t incy, T* part, int slices, cudaStream_t st) {
+template <typename T, bool CPLX>
+int mv_cols_slices(int64_t rows, int64_t) {
+    // slices of at least 64 rows, at most 128 of them (measured on 8192- and 16384-row operands:
+    // 128 slices beat 32 or 64 by 5 %, 256 gained nothing more)
+    return int(std::max<int64_t>(1, std::min<int64_t>(128, rows / 64)));
+}
+
+template <typename T, bool CPLX>
+cudaError_t launch_mv(const MvForm& f, int64_t rows, int64_t cols, const T* alpha, const T* S, int64_t ld, const T* x,
+                      int64_t incx, const T* beta, T* y, int64_t incy, T* part, int slices, cudaStream_t st) {
+    using V = typename std::conditional<CPLX, Cx<T>, T>::type;
     Runtime& r = runtime();
-    if (!cols_form) {
-        gemv_rows_kernel<T><<<grid_for(rows * 32, 256, r.num_sms), 256, 0, st>>>(rows, cols, alpha, S, ld, x, incx,
-                                                                                beta, y, incy);
+    V al, be;
+    std::memcpy(&al, alpha, sizeof(V));
+    std::memcpy(&be, beta, sizeof(V));
+    const V* vS = reinterpret_cast<const V*>(S);
+    const V* vx = reinterpret_cast<const V*>(x);
+    V* vy = reinterpret_cast<V*>(y);
+    const int tri = f.tri, unit = f.unit ? 1 : 0, conj = f.conj ? 1 : 0;
+    if (!f.cols_form) {
+        mv_rows_kernel<V><<<grid_for(rows * 32, 256, r.num_sms, 8), 256, 0, st>>>(rows, cols, al, vS, ld, vx, incx, be,
+                                                                                  vy, incy, tri, unit, conj);
         count_launches(1);
     } else {
+        V* vp = reinterpret_cast<V*>(part);
         const int64_t per = (rows + slices - 1) / slices;
-        gemv_cols_partial_kernel<T><<<dim3(unsigned((cols + 255) / 256), unsigned(slices)), 256, 0, st>>>(
-            rows, cols, S, ld, x, incx, per, part);
-        gemv_cols_reduce_kernel<T><<<unsigned((cols + 255) / 256), 256, 0, st>>>(cols, slices, part, alpha, beta, y,
-                                                                                   incy);
+        mv_cols_partial_kernel<V><<<dim3(unsigned((cols + 255) / 256), unsigned(slices)), 256, 0, st>>>(
+            rows, cols, vS, ld, vx, incx, per, vp, tri, unit, conj);
+        mv_cols_reduce_kernel<V><<<unsigned((cols + 31) / 32), 256, 0, st>>>(cols, slices, vp, al, be, vy, incy);
         count_launches(2);
     }
     return cudaGetLastError();
@@ -155,18 +255,25 @@ cudaError_t launch_complex_epilogue(int64_t rows, int64_t cols, const T* Pr, con
     return cudaGetLastError();
 }
 
-template <typename T>
+template <typename T, bool CPLX>
 cudaError_t launch_triangle(int64_t n, const T* A, int64_t lda, bool lower, bool unit, T* out, cudaStream_t st) {
-    triangle_kernel<T><<<grid_for(n * n, 256, runtime().num_sms), 256, 0, st>>>(n, A, lda, lower ? 1 : 0, unit ? 1 : 0,
-                                                                               out);
+    using V = typename std::conditional<CPLX, Cx<T>, T>::type;
+    triangle_kernel<V><<<grid_for(n * n, 256, runtime().num_sms), 256, 0, st>>>(
+        n, reinterpret_cast<const V*>(A), lda, lower ? 1 : 0, unit ? 1 : 0, reinterpret_cast<V*>(out));
     count_launches(1);
     return cudaGetLastError();
 }
 
-template cudaError_t launch_gemv<double>(bool, int64_t, int64_t, double, const double*, int64_t, const double*,
-                                         int64_t, double, double*, int64_t, double*, int, cudaStream_t);
-template cudaError_t launch_gemv<float>(bool, int64_t, int64_t, float, const float*, int64_t, const float*, int64_t,
-                                        float, float*, int64_t, float*, int, cudaStream_t);
+#define GB_MV(T, C)                                                                                          \
+    template cudaError_t launch_mv<T, C>(const MvForm&, int64_t, int64_t, const T*, const T*, int64_t, const T*, \
+                                         int64_t, const T*, T*, int64_t, T*, int, cudaStream_t);                \
+    template cudaError_t launch_triangle<T, C>(int64_t, const T*, int64_t, bool, bool, T*, cudaStream_t);         \
+    template int mv_cols_slices<T, C>(int64_t, int64_t);
+GB_MV(double, false)
+GB_MV(double, true)
+GB_MV(float, false)
+GB_MV(float, true)
+#undef GB_MV
 template cudaError_t launch_split_complex<double>(int64_t, int64_t, const double*, int64_t, double*, double*,
                                                   cudaStream_t);
 template cudaError_t launch_split_complex<float>(int64_t, int64_t, const float*, int64_t, float*, float*,
@@ -175,7 +282,5 @@ template cudaError_t launch_complex_epilogue<double>(int64_t, int64_t, const dou
                                                      double, double, double*, int64_t, cudaStream_t);
 template cudaError_t launch_complex_epilogue<float>(int64_t, int64_t, const float*, const float*, float, float, float,
                                                     float, float*, int64_t, cudaStream_t);
-template cudaError_t launch_triangle<double>(int64_t, const double*, int64_t, bool, bool, double*, cudaStream_t);
-template cudaError_t launch_triangle<float>(int64_t, const float*, int64_t, bool, bool, float*, cudaStream_t);
 
 }  // namespace gb

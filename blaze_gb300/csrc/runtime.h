@@ -25,6 +25,7 @@ enum Slot : int {
     kSlotScaleB,       // per-column exponents of B
     kSlotLevels,       // split-precision per-level integer sums
     kSlotMisc,         // small reductions (norms, bounds)
+    kSlotExtra,        // unused by the products; the eleventh buffer of the neighbouring routines
     kSlotCount
 };
 

@@ -126,7 +126,9 @@ void cblas_dgemm(CBLAS_ORDER order, CBLAS_TRANSPOSE transA, CBLAS_TRANSPOSE tran
                  gb300_blas_int lda, const double* B, gb300_blas_int ldb, double beta, double* C,
                  gb300_blas_int ldc);
 
-/* ---- declared for Blaze's other wrappers; stubs (GB300_ERR_NOT_SUPPORTED) ------------------ */
+/* ---- Blaze's other wrappers.  On the GPU: ?gemv, ?trmv, complex ?gemm and ?trmm, real and
+ * complex (complex operands are interleaved (re, im) pairs, alpha / beta point at one pair).
+ * Declared only, stubs that record GB300_ERR_NOT_SUPPORTED: ?trsm, ?axpy and the dot products. */
 /* blaze/math/blas/cblas/gemm.h:201,243 */
 void cblas_cgemm(CBLAS_ORDER order, CBLAS_TRANSPOSE transA, CBLAS_TRANSPOSE transB, gb300_blas_int m,
                  gb300_blas_int n, gb300_blas_int k, const void* alpha, const void* A, gb300_blas_int lda,
@@ -160,7 +162,7 @@ void cblas_ctrmm(CBLAS_ORDER order, CBLAS_SIDE side, CBLAS_UPLO uplo, CBLAS_TRAN
 void cblas_ztrmm(CBLAS_ORDER order, CBLAS_SIDE side, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA, CBLAS_DIAG diag,
                  gb300_blas_int m, gb300_blas_int n, const void* alpha, const void* A, gb300_blas_int lda,
                  void* B, gb300_blas_int ldb);
-/* blaze/math/blas/cblas/trmv.h */
+/* blaze/math/blas/cblas/trmv.h:111,145,181,218 */
 void cblas_strmv(CBLAS_ORDER order, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA, CBLAS_DIAG diag, gb300_blas_int n,
                  const float* A, gb300_blas_int lda, float* x, gb300_blas_int incX);
 void cblas_dtrmv(CBLAS_ORDER order, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA, CBLAS_DIAG diag, gb300_blas_int n,
@@ -169,7 +171,7 @@ void cblas_ctrmv(CBLAS_ORDER order, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA, CBL
                  const void* A, gb300_blas_int lda, void* x, gb300_blas_int incX);
 void cblas_ztrmv(CBLAS_ORDER order, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA, CBLAS_DIAG diag, gb300_blas_int n,
                  const void* A, gb300_blas_int lda, void* x, gb300_blas_int incX);
-/* blaze/math/blas/cblas/trsm.h */
+/* blaze/math/blas/cblas/trsm.h (stubs from here on) */
 void cblas_strsm(CBLAS_ORDER order, CBLAS_SIDE side, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA, CBLAS_DIAG diag,
                  gb300_blas_int m, gb300_blas_int n, float alpha, const float* A, gb300_blas_int lda, float* B,
                  gb300_blas_int ldb);

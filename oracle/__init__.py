@@ -101,6 +101,12 @@ def ref_lib():
         R.ref_gemm_z.restype = ct.c_int
         R.ref_trmm_d.argtypes = [ct.c_int] * 5 + [i64, i64, ct.c_double, _D, i64, _D, i64]
         R.ref_trmm_d.restype = ct.c_int
+        R.ref_gemv_z.argtypes = [ct.c_int, ct.c_int, i64, i64, _D, _D, i64, _D, _D, _D]
+        R.ref_gemv_z.restype = ct.c_int
+        R.ref_trmv.argtypes = [ct.c_int] * 5 + [i64, _D, i64, _D]
+        R.ref_trmv.restype = ct.c_int
+        R.ref_trmm_z.argtypes = [ct.c_int] * 5 + [i64, i64, _D, _D, i64, _D, i64]
+        R.ref_trmm_z.restype = ct.c_int
         _ref = R
     return _ref
 
@@ -271,3 +277,40 @@ def ref_trmm(order, side, uplo, transA, diag, m, n, alpha, A, lda, B, ldb):
     if R.ref_trmm_d(order, side, uplo, transA, diag, m, n, alpha, _cd(A), lda, B.ctypes.data_as(_D), ldb) != 0:
         raise RuntimeError("Blaze raised")
 
+
+def _ref_or_raise():
+    R = ref_lib()
+    if R is None:
+        raise RuntimeError("oracle/_ref/libblazeref.so was not built")
+    return R
+
+
+def ref_zgemv(order, transA, m, n, alpha, A, lda, x, beta, y):
+    """Complex y = alpha op(A) x + beta y (unit strides, complex128, transposes 111 / 112 / 113)
+    through Blaze itself; y is updated in place."""
+    R = _ref_or_raise()
+    al = np.array([alpha.real, alpha.imag]); be = np.array([beta.real, beta.imag])
+    Ad = np.ascontiguousarray(A).view(np.float64); xd = np.ascontiguousarray(x).view(np.float64)
+    if R.ref_gemv_z(order, transA, m, n, _cd(al), _cd(Ad), lda, _cd(xd), _cd(be), y.view(np.float64).ctypes.data_as(_D)) != 0:
+        raise RuntimeError("Blaze raised")
+
+
+def ref_trmv(order, uplo, transA, diag, n, A, lda, x):
+    """x = op(A) x (unit stride), A triangular, through Blaze itself; float64 or complex128; x is
+    updated in place."""
+    R = _ref_or_raise()
+    cplx = int(np.iscomplexobj(x))
+    Ad = np.ascontiguousarray(A).view(np.float64)
+    if R.ref_trmv(cplx, order, uplo, transA, diag, n, _cd(Ad), lda, x.view(np.float64).ctypes.data_as(_D)) != 0:
+        raise RuntimeError("Blaze raised")
+
+
+def ref_ztrmm(order, side, uplo, transA, diag, m, n, alpha, A, lda, B, ldb):
+    """Complex B = alpha op(A) B or alpha B op(A), A triangular, through Blaze itself (complex128);
+    B is updated in place."""
+    R = _ref_or_raise()
+    al = np.array([alpha.real, alpha.imag])
+    Ad = np.ascontiguousarray(A).view(np.float64)
+    if R.ref_trmm_z(order, side, uplo, transA, diag, m, n, _cd(al), _cd(Ad), lda, B.view(np.float64).ctypes.data_as(_D),
+                    ldb) != 0:
+        raise RuntimeError("Blaze raised")

@@ -108,10 +108,20 @@ using VView = blaze::CustomVector<T, unaligned, unpadded>;
 // y = alpha * op(A) * x + beta * y (unit strides); op(A) is the logical rows x cols view of the
 // CBLAS operand, a CustomMatrix in the storage order (order, trans) describes.
 template <typename T, bool SO>
-void gemv_run(int64_t rows, int64_t cols, T alpha, const T* A, int64_t lda, const T* x, T beta, T* y) {
+void gemv_run(int64_t rows, int64_t cols, bool conj_a, T alpha, const T* A, int64_t lda, const T* x, T beta, T* y) {
     View<T, SO> a(const_cast<T*>(A), rows, cols, lda);
     VView<T> vx(const_cast<T*>(x), cols);
     VView<T> vy(y, rows);
+    if (conj_a) {  // conjugate transpose: Blaze's conj() of the transposed view
+        blaze::DynamicMatrix<T, SO> ca(conj(a));
+        if (beta == T(0)) {
+            vy = alpha * (ca * vx);
+        } else {
+            vy *= beta;
+            vy += alpha * (ca * vx);
+        }
+        return;
+    }
     if (beta == T(0)) {
         vy = alpha * (a * vx);
     } else {
@@ -123,11 +133,11 @@ void gemv_run(int64_t rows, int64_t cols, T alpha, const T* A, int64_t lda, cons
 template <typename T>
 void gemv_dispatch(int order, int tA, int64_t m, int64_t n, T alpha, const T* A, int64_t lda, const T* x, T beta,
                    T* y) {
-    const bool rm = (order == 101), ta = (tA != 111);
+    const bool rm = (order == 101), ta = (tA != 111), ca = (tA == 113);
     const int64_t rows = ta ? n : m, cols = ta ? m : n;
     const bool so = rm ? (ta ? columnMajor : rowMajor) : (ta ? rowMajor : columnMajor);
-    if (so == rowMajor) gemv_run<T, rowMajor>(rows, cols, alpha, A, lda, x, beta, y);
-    else gemv_run<T, columnMajor>(rows, cols, alpha, A, lda, x, beta, y);
+    if (so == rowMajor) gemv_run<T, rowMajor>(rows, cols, ca, alpha, A, lda, x, beta, y);
+    else gemv_run<T, columnMajor>(rows, cols, ca, alpha, A, lda, x, beta, y);
 }
 
 // Complex C = alpha * op(A) * op(B) + beta * C; op = conj(trans(.)) for CblasConjTrans.
@@ -175,16 +185,10 @@ void cgemm_dispatch(int order, int tA, int tB, int64_t m, int64_t n, int64_t k, 
 #undef GB_CASE
 }
 
-// B = alpha * op(A) * B (side Left) or alpha * B * op(A) (side Right), A triangular (only the
-// uplo triangle is read; diag Unit takes ones on the diagonal).  Blaze's own evaluation of a
-// triangular product: the triangle of op(A) through blaze::LowerMatrix / UpperMatrix (and the
-// Uni* adaptors for a unit diagonal), multiplied with Blaze's default kernels.
+// op(T) for a triangular A (ka x ka view in storage order SO): only the uplo triangle is read,
+// diag Unit takes ones on the diagonal; op = transpose (ta) and conjugate (ca).
 template <typename T, bool SO>
-void trmm_run(int side_left, int lower, int ta, int unit, int64_t m, int64_t n, T alpha, const T* A, int64_t lda,
-              T* B, int64_t ldb) {
-    const int64_t ka = side_left ? m : n;
-    View<T, SO> a(const_cast<T*>(A), ka, ka, lda);
-    View<T, SO> b(B, m, n, ldb);
+blaze::DynamicMatrix<T, SO> triangle_op(const View<T, SO>& a, int64_t ka, int lower, int ta, int ca, int unit) {
     blaze::DynamicMatrix<T, SO> t(ka, ka, T(0));
     for (int64_t i = 0; i < ka; ++i)
         for (int64_t j = 0; j < ka; ++j) {
@@ -192,26 +196,47 @@ void trmm_run(int side_left, int lower, int ta, int unit, int64_t m, int64_t n, 
             if (in) t(i, j) = (unit && i == j) ? T(1) : a(i, j);
         }
     blaze::DynamicMatrix<T, SO> op = ta ? blaze::DynamicMatrix<T, SO>(trans(t)) : t;
-    blaze::DynamicMatrix<T, SO> res;
-    const bool low_op = ta ? !lower : lower;
+    if (ca) op = conj(op);
+    return op;
+}
+
+// Blaze's own evaluation of a product with a triangular op(T): op(T) held by blaze::LowerMatrix /
+// UpperMatrix (the Uni* adaptors for a unit diagonal), multiplied by f with Blaze's default kernels.
+template <typename T, bool SO, typename F>
+void with_triangle(const blaze::DynamicMatrix<T, SO>& op, bool low_op, int unit, F&& f) {
     if (low_op) {
-        if (unit) {
-            blaze::UniLowerMatrix<blaze::DynamicMatrix<T, SO>> tri(op);
-            res = side_left ? blaze::DynamicMatrix<T, SO>(alpha * (tri * b)) : blaze::DynamicMatrix<T, SO>(alpha * (b * tri));
-        } else {
-            blaze::LowerMatrix<blaze::DynamicMatrix<T, SO>> tri(op);
-            res = side_left ? blaze::DynamicMatrix<T, SO>(alpha * (tri * b)) : blaze::DynamicMatrix<T, SO>(alpha * (b * tri));
-        }
+        if (unit) f(blaze::UniLowerMatrix<blaze::DynamicMatrix<T, SO>>(op));
+        else f(blaze::LowerMatrix<blaze::DynamicMatrix<T, SO>>(op));
     } else {
-        if (unit) {
-            blaze::UniUpperMatrix<blaze::DynamicMatrix<T, SO>> tri(op);
-            res = side_left ? blaze::DynamicMatrix<T, SO>(alpha * (tri * b)) : blaze::DynamicMatrix<T, SO>(alpha * (b * tri));
-        } else {
-            blaze::UpperMatrix<blaze::DynamicMatrix<T, SO>> tri(op);
-            res = side_left ? blaze::DynamicMatrix<T, SO>(alpha * (tri * b)) : blaze::DynamicMatrix<T, SO>(alpha * (b * tri));
-        }
+        if (unit) f(blaze::UniUpperMatrix<blaze::DynamicMatrix<T, SO>>(op));
+        else f(blaze::UpperMatrix<blaze::DynamicMatrix<T, SO>>(op));
     }
+}
+
+// B = alpha * op(A) * B (side Left) or alpha * B * op(A) (side Right), A triangular.
+template <typename T, bool SO>
+void trmm_run(int side_left, int lower, int ta, int ca, int unit, int64_t m, int64_t n, T alpha, const T* A,
+              int64_t lda, T* B, int64_t ldb) {
+    const int64_t ka = side_left ? m : n;
+    View<T, SO> a(const_cast<T*>(A), ka, ka, lda);
+    View<T, SO> b(B, m, n, ldb);
+    const blaze::DynamicMatrix<T, SO> op = triangle_op<T, SO>(a, ka, lower, ta, ca, unit);
+    blaze::DynamicMatrix<T, SO> res;
+    with_triangle<T, SO>(op, ta ? !lower : lower, unit, [&](const auto& tri) {
+        res = side_left ? blaze::DynamicMatrix<T, SO>(alpha * (tri * b)) : blaze::DynamicMatrix<T, SO>(alpha * (b * tri));
+    });
     b = res;
+}
+
+// x = op(A) * x (unit stride), A n x n triangular.
+template <typename T, bool SO>
+void trmv_run(int lower, int ta, int ca, int unit, int64_t n, const T* A, int64_t lda, T* x) {
+    View<T, SO> a(const_cast<T*>(A), n, n, lda);
+    VView<T> vx(x, n);
+    const blaze::DynamicMatrix<T, SO> op = triangle_op<T, SO>(a, n, lower, ta, ca, unit);
+    blaze::DynamicVector<T> res;
+    with_triangle<T, SO>(op, ta ? !lower : lower, unit, [&](const auto& tri) { res = tri * vx; });
+    vx = res;
 }
 
 }  // namespace
@@ -247,8 +272,61 @@ int ref_trmm_d(int order, int side, int uplo, int tA, int diag, int64_t m, int64
                int64_t lda, double* B, int64_t ldb) {
     try {
         const int left = side == 141, lower = uplo == 122, ta = tA != 111, unit = diag == 132;
-        if (order == 101) trmm_run<double, rowMajor>(left, lower, ta, unit, m, n, alpha, A, lda, B, ldb);
-        else trmm_run<double, columnMajor>(left, lower, ta, unit, m, n, alpha, A, lda, B, ldb);
+        if (order == 101) trmm_run<double, rowMajor>(left, lower, ta, 0, unit, m, n, alpha, A, lda, B, ldb);
+        else trmm_run<double, columnMajor>(left, lower, ta, 0, unit, m, n, alpha, A, lda, B, ldb);
+    } catch (const std::exception& e) {
+        std::fprintf(stderr, "blaze: %s\n", e.what());
+        return 1;
+    }
+    return 0;
+}
+
+// complex y = alpha * op(A) * x + beta * y; alpha, beta, A, x, y interleaved (re, im)
+int ref_gemv_z(int order, int tA, int64_t m, int64_t n, const double* alpha, const double* A, int64_t lda,
+               const double* x, const double* beta, double* y) {
+    using CT = std::complex<double>;
+    try {
+        gemv_dispatch<CT>(order, tA, m, n, CT(alpha[0], alpha[1]), reinterpret_cast<const CT*>(A), lda,
+                          reinterpret_cast<const CT*>(x), CT(beta[0], beta[1]), reinterpret_cast<CT*>(y));
+    } catch (const std::exception& e) {
+        std::fprintf(stderr, "blaze: %s\n", e.what());
+        return 1;
+    }
+    return 0;
+}
+
+// x = op(A) * x, A triangular; real (cplx == 0) or interleaved complex doubles
+int ref_trmv(int cplx, int order, int uplo, int tA, int diag, int64_t n, const double* A, int64_t lda, double* x) {
+    using CT = std::complex<double>;
+    try {
+        const int lower = uplo == 122, ta = tA != 111, ca = tA == 113, unit = diag == 132;
+        if (cplx) {
+            const CT* a = reinterpret_cast<const CT*>(A);
+            CT* v = reinterpret_cast<CT*>(x);
+            if (order == 101) trmv_run<CT, rowMajor>(lower, ta, ca, unit, n, a, lda, v);
+            else trmv_run<CT, columnMajor>(lower, ta, ca, unit, n, a, lda, v);
+        } else {
+            if (order == 101) trmv_run<double, rowMajor>(lower, ta, 0, unit, n, A, lda, x);
+            else trmv_run<double, columnMajor>(lower, ta, 0, unit, n, A, lda, x);
+        }
+    } catch (const std::exception& e) {
+        std::fprintf(stderr, "blaze: %s\n", e.what());
+        return 1;
+    }
+    return 0;
+}
+
+// complex B = alpha * op(A) * B or alpha * B * op(A), A triangular; interleaved (re, im)
+int ref_trmm_z(int order, int side, int uplo, int tA, int diag, int64_t m, int64_t n, const double* alpha,
+               const double* A, int64_t lda, double* B, int64_t ldb) {
+    using CT = std::complex<double>;
+    try {
+        const int left = side == 141, lower = uplo == 122, ta = tA != 111, ca = tA == 113, unit = diag == 132;
+        const CT al(alpha[0], alpha[1]);
+        const CT* a = reinterpret_cast<const CT*>(A);
+        CT* b = reinterpret_cast<CT*>(B);
+        if (order == 101) trmm_run<CT, rowMajor>(left, lower, ta, ca, unit, m, n, al, a, lda, b, ldb);
+        else trmm_run<CT, columnMajor>(left, lower, ta, ca, unit, m, n, al, a, lda, b, ldb);
     } catch (const std::exception& e) {
         std::fprintf(stderr, "blaze: %s\n", e.what());
         return 1;

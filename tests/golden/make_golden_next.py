@@ -1,5 +1,5 @@
-"""Generate the golden fixtures of the neighbouring BLAS routines (gemv, complex gemm, trmm) from
-Blaze itself.
+"""Generate the golden fixtures of the neighbouring BLAS routines (gemv, trmv, complex gemm, trmm,
+real and complex) from Blaze itself.
 
 Run in a container that has the reference headers (Blaze is header-only):
 
@@ -9,7 +9,8 @@ Run in a container that has the reference headers (Blaze is header-only):
 Each case is evaluated by Blaze's default (non-BLAS) kernels on blaze::CustomMatrix /
 CustomVector views (oracle/blaze_ref.cpp): y = alpha*op(A)*x + beta*y for gemv; complex
 C = alpha*op(A)*op(B) + beta*C with op in {N, T, conjugate-transpose} for zgemm; B = alpha*op(A)*B or
-alpha*B*op(A) with A triangular (upper/lower, unit/non-unit diagonal) for trmm.  Inputs are not
+alpha*B*op(A) with A triangular (upper/lower, unit/non-unit diagonal) for trmm; x = op(A)*x with A
+triangular for trmv (Blaze's LowerMatrix / UpperMatrix / Uni* adaptors).  Inputs are not
 stored: they are regenerated from their seeds by the oracle's MT19937 generator (checksums kept).
 """
 from __future__ import annotations
@@ -75,6 +76,47 @@ def trmm_cases():
     return out
 
 
+def zgemv_cases():
+    out, seed = [], 11000
+    sizes = [(1, 1), (7, 13), (64, 37), (130, 257)]
+    ab = [(1 + 0j, 0j), (0.5 - 1j, 0j), (1 + 0j, 1 + 0j), (-0.25 + 2j, 0.5 - 0.5j)]
+    for i, (m, n) in enumerate(sizes):
+        for j, (order, ta) in enumerate(itertools.product((O.ROW_MAJOR, O.COL_MAJOR), (O.NO_TRANS, O.TRANS, CONJ))):
+            al, be = ab[(i + j) % 4]
+            out.append((order, ta, m, n, al, be, (i + j) % 2, seed))
+            seed += 3
+    return out
+
+
+def trmv_cases():
+    out, seed = [], 13000
+    for cplx in (0, 1):
+        ops = (O.NO_TRANS, O.TRANS, CONJ) if cplx else (O.NO_TRANS, O.TRANS)
+        combos = list(itertools.product((O.ROW_MAJOR, O.COL_MAJOR), (121, 122), ops, (131, 132)))
+        for i, n in enumerate((1, 7, 64, 130)):
+            for j, (order, uplo, ta, diag) in enumerate(combos):
+                if n > 1 and (i + j) % 2:
+                    continue
+                out.append((cplx, order, uplo, ta, diag, n, j % 2, seed))
+                seed += 2
+    return out
+
+
+def ztrmm_cases():
+    out, seed = [], 15000
+    sizes = [(5, 7), (37, 16), (130, 36)]
+    combos = list(itertools.product((O.ROW_MAJOR, O.COL_MAJOR), (141, 142), (121, 122), (O.NO_TRANS, O.TRANS, CONJ),
+                                    (131, 132)))
+    for i, (m, n) in enumerate(sizes):
+        for j, (order, side, uplo, ta, diag) in enumerate(combos):
+            if (i + j) % 3:
+                continue
+            al = (1 + 0j, -0.75 + 0.5j, 2j)[(i + j) % 3]
+            out.append((order, side, uplo, ta, diag, m, n, al, j % 2, seed))
+            seed += 2
+    return out
+
+
 def stored(order, trans, rows, cols):
     t = trans != O.NO_TRANS
     r, c = (cols, rows) if t else (rows, cols)
@@ -117,6 +159,35 @@ def main():
         arrays[f"trmm{q}_meta"] = np.array([order, side, uplo, ta, diag, m, n, lda, ldb, seed], dtype=np.int64)
         arrays[f"trmm{q}_alpha"] = np.array([al])
         arrays[f"trmm{q}_B"] = B
+    for q, (order, ta, m, n, al, be, pad, seed) in enumerate(zgemv_cases()):
+        r, c = stored(order, O.NO_TRANS, m, n)
+        lda = c + pad
+        A = zvals(r * lda, seed)
+        xl, yl = (m, n) if ta != O.NO_TRANS else (n, m)
+        x = zvals(xl, seed + 1)
+        y = zvals(yl, seed + 2)
+        O.ref_zgemv(order, ta, m, n, al, A, lda, x, be, y)
+        arrays[f"zgemv{q}_meta"] = np.array([order, ta, m, n, lda, seed], dtype=np.int64)
+        arrays[f"zgemv{q}_ab"] = np.array([al, be])
+        arrays[f"zgemv{q}_y"] = y
+    for q, (cplx, order, uplo, ta, diag, n, pad, seed) in enumerate(trmv_cases()):
+        lda = n + pad
+        A = zvals(n * lda, seed) if cplx else O.uniform(n * lda, seed)
+        x = zvals(n, seed + 1) if cplx else O.uniform(n, seed + 1).copy()
+        O.ref_trmv(order, uplo, ta, diag, n, A, lda, x)
+        arrays[f"trmv{q}_meta"] = np.array([cplx, order, uplo, ta, diag, n, lda, seed], dtype=np.int64)
+        arrays[f"trmv{q}_x"] = x
+    for q, (order, side, uplo, ta, diag, m, n, al, pad, seed) in enumerate(ztrmm_cases()):
+        ka = m if side == 141 else n
+        lda = ka + pad
+        rb, cb = stored(order, O.NO_TRANS, m, n)
+        ldb = cb + pad
+        A = zvals(ka * lda, seed)
+        B = zvals(rb * ldb, seed + 1)
+        O.ref_ztrmm(order, side, uplo, ta, diag, m, n, al, A, lda, B, ldb)
+        arrays[f"ztrmm{q}_meta"] = np.array([order, side, uplo, ta, diag, m, n, lda, ldb, seed], dtype=np.int64)
+        arrays[f"ztrmm{q}_alpha"] = np.array([al])
+        arrays[f"ztrmm{q}_B"] = B
     np.savez_compressed(OUT, **arrays)
     print(OUT, len(arrays), "arrays,", os.path.getsize(OUT), "bytes")
 

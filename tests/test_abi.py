@@ -111,6 +111,11 @@ def test_no_device_is_reported_not_faked(lib):
     ("zgemm", dict(ldc=3), 14),
     ("trmm", dict(side=7), 2), ("trmm", dict(uplo=7), 3), ("trmm", dict(ta=7), 4), ("trmm", dict(diag=7), 5),
     ("trmm", dict(m=-1), 6), ("trmm", dict(lda=3), 10), ("trmm", dict(ldb=3), 12),
+    ("zgemv", dict(order=99), 1), ("zgemv", dict(ta=7), 2), ("zgemv", dict(lda=3), 7), ("zgemv", dict(incy=0), 12),
+    ("trmv", dict(order=99), 1), ("trmv", dict(uplo=7), 2), ("trmv", dict(ta=7), 3), ("trmv", dict(diag=7), 4),
+    ("trmv", dict(n=-1), 5), ("trmv", dict(lda=3), 7), ("trmv", dict(incx=0), 9),
+    ("ztrmv", dict(uplo=7), 2), ("ztrmv", dict(lda=3), 7), ("ztrmv", dict(incx=0), 9),
+    ("ztrmm", dict(side=7), 2), ("ztrmm", dict(diag=7), 5), ("ztrmm", dict(lda=3), 10), ("ztrmm", dict(ldb=3), 12),
 ])
 def test_neighbour_routines_name_the_parameter(lib, routine, args, param):
     a = dict(order=G.RowMajor, ta=G.NoTrans, tb=G.NoTrans, m=8, n=8, k=8, lda=8, ldb=8, ldc=8, incx=1, incy=1,
@@ -125,6 +130,15 @@ def test_neighbour_routines_name_the_parameter(lib, routine, args, param):
     elif routine == "zgemm":
         lib.cblas_zgemm(a["order"], a["ta"], a["tb"], a["m"], a["n"], a["k"], one.ctypes.data, A.ctypes.data,
                         a["lda"], B.ctypes.data, a["ldb"], zero.ctypes.data, C.ctypes.data, a["ldc"])
+    elif routine == "zgemv":
+        lib.cblas_zgemv(a["order"], a["ta"], a["m"], a["n"], one.ctypes.data, A.ctypes.data, a["lda"], B.ctypes.data,
+                        a["incx"], zero.ctypes.data, C.ctypes.data, a["incy"])
+    elif routine in ("trmv", "ztrmv"):
+        getattr(lib, "cblas_%s" % ("dtrmv" if routine == "trmv" else "ztrmv"))(
+            a["order"], a["uplo"], a["ta"], a["diag"], a["n"], A.ctypes.data, a["lda"], B.ctypes.data, a["incx"])
+    elif routine == "ztrmm":
+        lib.cblas_ztrmm(a["order"], a["side"], a["uplo"], a["ta"], a["diag"], a["m"], a["n"], one.ctypes.data,
+                        A.ctypes.data, a["lda"], B.ctypes.data, a["ldb"])
     else:
         lib.cblas_dtrmm(a["order"], a["side"], a["uplo"], a["ta"], a["diag"], a["m"], a["n"], 1.0, A.ctypes.data,
                         a["lda"], B.ctypes.data, a["ldb"])
