@@ -51,6 +51,78 @@ __attribute__((visibility("default"))) void gb300_cblas_dgemm_checked(CBLAS_ORDE
     cblas_dgemm(order, transA, transB, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
 }
 
+// Aliases of the routines below for the same throwing wrappers.
+__attribute__((visibility("default"))) void gb300_cblas_sgemv_checked(CBLAS_ORDER order, CBLAS_TRANSPOSE transA,
+    gb300_blas_int m, gb300_blas_int n, float alpha, const float* A, gb300_blas_int lda, const float* x,
+    gb300_blas_int incX, float beta, float* y, gb300_blas_int incY) {
+    cblas_sgemv(order, transA, m, n, alpha, A, lda, x, incX, beta, y, incY);
+}
+__attribute__((visibility("default"))) void gb300_cblas_dgemv_checked(CBLAS_ORDER order, CBLAS_TRANSPOSE transA,
+    gb300_blas_int m, gb300_blas_int n, double alpha, const double* A, gb300_blas_int lda, const double* x,
+    gb300_blas_int incX, double beta, double* y, gb300_blas_int incY) {
+    cblas_dgemv(order, transA, m, n, alpha, A, lda, x, incX, beta, y, incY);
+}
+__attribute__((visibility("default"))) void gb300_cblas_cgemv_checked(CBLAS_ORDER order, CBLAS_TRANSPOSE transA,
+    gb300_blas_int m, gb300_blas_int n, const void* alpha, const void* A, gb300_blas_int lda, const void* x,
+    gb300_blas_int incX, const void* beta, void* y, gb300_blas_int incY) {
+    cblas_cgemv(order, transA, m, n, alpha, A, lda, x, incX, beta, y, incY);
+}
+__attribute__((visibility("default"))) void gb300_cblas_zgemv_checked(CBLAS_ORDER order, CBLAS_TRANSPOSE transA,
+    gb300_blas_int m, gb300_blas_int n, const void* alpha, const void* A, gb300_blas_int lda, const void* x,
+    gb300_blas_int incX, const void* beta, void* y, gb300_blas_int incY) {
+    cblas_zgemv(order, transA, m, n, alpha, A, lda, x, incX, beta, y, incY);
+}
+__attribute__((visibility("default"))) void gb300_cblas_cgemm_checked(CBLAS_ORDER order, CBLAS_TRANSPOSE transA,
+    CBLAS_TRANSPOSE transB, gb300_blas_int m, gb300_blas_int n, gb300_blas_int k, const void* alpha, const void* A,
+    gb300_blas_int lda, const void* B, gb300_blas_int ldb, const void* beta, void* C, gb300_blas_int ldc) {
+    cblas_cgemm(order, transA, transB, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+}
+__attribute__((visibility("default"))) void gb300_cblas_zgemm_checked(CBLAS_ORDER order, CBLAS_TRANSPOSE transA,
+    CBLAS_TRANSPOSE transB, gb300_blas_int m, gb300_blas_int n, gb300_blas_int k, const void* alpha, const void* A,
+    gb300_blas_int lda, const void* B, gb300_blas_int ldb, const void* beta, void* C, gb300_blas_int ldc) {
+    cblas_zgemm(order, transA, transB, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+}
+__attribute__((visibility("default"))) void gb300_cblas_strmm_checked(CBLAS_ORDER order, CBLAS_SIDE side, CBLAS_UPLO
+    uplo, CBLAS_TRANSPOSE transA, CBLAS_DIAG diag, gb300_blas_int m, gb300_blas_int n, float alpha, const float* A,
+    gb300_blas_int lda, float* B, gb300_blas_int ldb) {
+    cblas_strmm(order, side, uplo, transA, diag, m, n, alpha, A, lda, B, ldb);
+}
+__attribute__((visibility("default"))) void gb300_cblas_dtrmm_checked(CBLAS_ORDER order, CBLAS_SIDE side, CBLAS_UPLO
+    uplo, CBLAS_TRANSPOSE transA, CBLAS_DIAG diag, gb300_blas_int m, gb300_blas_int n, double alpha, const double* A,
+    gb300_blas_int lda, double* B, gb300_blas_int ldb) {
+    cblas_dtrmm(order, side, uplo, transA, diag, m, n, alpha, A, lda, B, ldb);
+}
+__attribute__((visibility("default"))) void gb300_cblas_ctrmm_checked(CBLAS_ORDER order, CBLAS_SIDE side, CBLAS_UPLO
+    uplo, CBLAS_TRANSPOSE transA, CBLAS_DIAG diag, gb300_blas_int m, gb300_blas_int n, const void* alpha, const void*
+    A, gb300_blas_int lda, void* B, gb300_blas_int ldb) {
+    cblas_ctrmm(order, side, uplo, transA, diag, m, n, alpha, A, lda, B, ldb);
+}
+__attribute__((visibility("default"))) void gb300_cblas_ztrmm_checked(CBLAS_ORDER order, CBLAS_SIDE side, CBLAS_UPLO
+    uplo, CBLAS_TRANSPOSE transA, CBLAS_DIAG diag, gb300_blas_int m, gb300_blas_int n, const void* alpha, const void*
+    A, gb300_blas_int lda, void* B, gb300_blas_int ldb) {
+    cblas_ztrmm(order, side, uplo, transA, diag, m, n, alpha, A, lda, B, ldb);
+}
+__attribute__((visibility("default"))) void gb300_cblas_strmv_checked(CBLAS_ORDER order, CBLAS_UPLO uplo,
+    CBLAS_TRANSPOSE transA, CBLAS_DIAG diag, gb300_blas_int n, const float* A, gb300_blas_int lda, float* x,
+    gb300_blas_int incX) {
+    cblas_strmv(order, uplo, transA, diag, n, A, lda, x, incX);
+}
+__attribute__((visibility("default"))) void gb300_cblas_dtrmv_checked(CBLAS_ORDER order, CBLAS_UPLO uplo,
+    CBLAS_TRANSPOSE transA, CBLAS_DIAG diag, gb300_blas_int n, const double* A, gb300_blas_int lda, double* x,
+    gb300_blas_int incX) {
+    cblas_dtrmv(order, uplo, transA, diag, n, A, lda, x, incX);
+}
+__attribute__((visibility("default"))) void gb300_cblas_ctrmv_checked(CBLAS_ORDER order, CBLAS_UPLO uplo,
+    CBLAS_TRANSPOSE transA, CBLAS_DIAG diag, gb300_blas_int n, const void* A, gb300_blas_int lda, void* x,
+    gb300_blas_int incX) {
+    cblas_ctrmv(order, uplo, transA, diag, n, A, lda, x, incX);
+}
+__attribute__((visibility("default"))) void gb300_cblas_ztrmv_checked(CBLAS_ORDER order, CBLAS_UPLO uplo,
+    CBLAS_TRANSPOSE transA, CBLAS_DIAG diag, gb300_blas_int n, const void* A, gb300_blas_int lda, void* x,
+    gb300_blas_int incX) {
+    cblas_ztrmv(order, uplo, transA, diag, n, A, lda, x, incX);
+}
+
 // ---- stubs ------------------------------------------------------------------------------------
 // ---- the neighbouring routines on the GPU (api_next.cpp) ----------------------------------------
 void cblas_cgemm(CBLAS_ORDER order, CBLAS_TRANSPOSE transA, CBLAS_TRANSPOSE transB, gb300_blas_int m, gb300_blas_int n,

@@ -9,9 +9,11 @@
  *
  * Implemented on the GPU: cblas_dgemm and cblas_sgemm (the dense matrix-multiplication path,
  * reached from blaze::gemm(), blaze/math/blas/gemm.h:105-131, and blaze/math/blas/cblas/gemm.h:
- * 116-162).  Every other routine that Blaze's wrappers name is declared so that Blaze compiles;
- * the library defines them as stubs that record GB300_ERR_NOT_SUPPORTED (see gb300_last_error())
- * and compute nothing — there is no CPU fallback.
+ * 116-162), and the other routines Blaze's expressions call: cblas_?gemv, cblas_?trmv,
+ * cblas_cgemm / cblas_zgemm and cblas_?trmm.  The remaining routines Blaze's wrappers name
+ * (?trsm, ?axpy, the dot products) are declared so that Blaze compiles; the library defines them
+ * as stubs that record GB300_ERR_NOT_SUPPORTED (see gb300_last_error()) and compute nothing —
+ * there is no CPU fallback.
  *
  * Integer type: `blas_int_t` is int32 unless BLAZE_BLAS_IS_64BIT is set, matching
  * blaze/math/blas/Types.h:56-64.  The library exports the 32-bit ABI under the standard names;
@@ -20,9 +22,9 @@
  *
  * Errors: CBLAS routines return void.  Invalid arguments and device failures are recorded in a
  * thread-local status readable with gb300_last_error() / gb300_last_error_message().
- * Defining GB300_BLAS_THROW before inclusion in C++ wraps cblas_dgemm / cblas_sgemm so that a
- * non-zero status throws std::runtime_error right after the call (the behaviour of Blaze's own
- * BLAZE_THROW_RUNTIME_ERROR, blaze/util/Exception.h).
+ * Defining GB300_BLAS_THROW before inclusion in C++ wraps every routine the library implements so
+ * that a non-zero status throws std::runtime_error right after the call (the behaviour of Blaze's
+ * own BLAZE_THROW_RUNTIME_ERROR, blaze/util/Exception.h).
  */
 #ifndef GB300_CBLAS_H
 #define GB300_CBLAS_H
@@ -101,6 +103,29 @@ void gb300_clear_error(void);
 #define cblas_zdotc_sub cblas_zdotc_sub_64
 #define gb300_cblas_sgemm_checked gb300_cblas_sgemm_checked_64
 #define gb300_cblas_dgemm_checked gb300_cblas_dgemm_checked_64
+#define gb300_cblas_sgemv_checked gb300_cblas_sgemv_checked_64
+#define gb300_cblas_dgemv_checked gb300_cblas_dgemv_checked_64
+#define gb300_cblas_cgemv_checked gb300_cblas_cgemv_checked_64
+#define gb300_cblas_zgemv_checked gb300_cblas_zgemv_checked_64
+#define gb300_cblas_cgemm_checked gb300_cblas_cgemm_checked_64
+#define gb300_cblas_zgemm_checked gb300_cblas_zgemm_checked_64
+#define gb300_cblas_strmm_checked gb300_cblas_strmm_checked_64
+#define gb300_cblas_dtrmm_checked gb300_cblas_dtrmm_checked_64
+#define gb300_cblas_ctrmm_checked gb300_cblas_ctrmm_checked_64
+#define gb300_cblas_ztrmm_checked gb300_cblas_ztrmm_checked_64
+#define gb300_cblas_strmv_checked gb300_cblas_strmv_checked_64
+#define gb300_cblas_dtrmv_checked gb300_cblas_dtrmv_checked_64
+#define gb300_cblas_ctrmv_checked gb300_cblas_ctrmv_checked_64
+#define gb300_cblas_ztrmv_checked gb300_cblas_ztrmv_checked_64
+#endif
+
+/* Under GB300_BLAS_THROW (C++), each routine that runs on the GPU is declared as
+ * gb300_<routine>_checked and <routine> becomes an inline wrapper that throws on a non-zero
+ * status (end of this file). */
+#if defined(__cplusplus) && defined(GB300_BLAS_THROW)
+#define GB300_ENTRY(name) gb300_##name##_checked
+#else
+#define GB300_ENTRY(name) name
 #endif
 
 /* ---- GEMM: implemented on the GPU ---------------------------------------------------------- */
@@ -130,46 +155,46 @@ void cblas_dgemm(CBLAS_ORDER order, CBLAS_TRANSPOSE transA, CBLAS_TRANSPOSE tran
  * complex (complex operands are interleaved (re, im) pairs, alpha / beta point at one pair).
  * Declared only, stubs that record GB300_ERR_NOT_SUPPORTED: ?trsm, ?axpy and the dot products. */
 /* blaze/math/blas/cblas/gemm.h:201,243 */
-void cblas_cgemm(CBLAS_ORDER order, CBLAS_TRANSPOSE transA, CBLAS_TRANSPOSE transB, gb300_blas_int m,
+void GB300_ENTRY(cblas_cgemm)(CBLAS_ORDER order, CBLAS_TRANSPOSE transA, CBLAS_TRANSPOSE transB, gb300_blas_int m,
                  gb300_blas_int n, gb300_blas_int k, const void* alpha, const void* A, gb300_blas_int lda,
                  const void* B, gb300_blas_int ldb, const void* beta, void* C, gb300_blas_int ldc);
-void cblas_zgemm(CBLAS_ORDER order, CBLAS_TRANSPOSE transA, CBLAS_TRANSPOSE transB, gb300_blas_int m,
+void GB300_ENTRY(cblas_zgemm)(CBLAS_ORDER order, CBLAS_TRANSPOSE transA, CBLAS_TRANSPOSE transB, gb300_blas_int m,
                  gb300_blas_int n, gb300_blas_int k, const void* alpha, const void* A, gb300_blas_int lda,
                  const void* B, gb300_blas_int ldb, const void* beta, void* C, gb300_blas_int ldc);
 /* blaze/math/blas/cblas/gemv.h:116,153,193,235 */
-void cblas_sgemv(CBLAS_ORDER order, CBLAS_TRANSPOSE transA, gb300_blas_int m, gb300_blas_int n, float alpha,
+void GB300_ENTRY(cblas_sgemv)(CBLAS_ORDER order, CBLAS_TRANSPOSE transA, gb300_blas_int m, gb300_blas_int n, float alpha,
                  const float* A, gb300_blas_int lda, const float* x, gb300_blas_int incX, float beta, float* y,
                  gb300_blas_int incY);
-void cblas_dgemv(CBLAS_ORDER order, CBLAS_TRANSPOSE transA, gb300_blas_int m, gb300_blas_int n, double alpha,
+void GB300_ENTRY(cblas_dgemv)(CBLAS_ORDER order, CBLAS_TRANSPOSE transA, gb300_blas_int m, gb300_blas_int n, double alpha,
                  const double* A, gb300_blas_int lda, const double* x, gb300_blas_int incX, double beta,
                  double* y, gb300_blas_int incY);
-void cblas_cgemv(CBLAS_ORDER order, CBLAS_TRANSPOSE transA, gb300_blas_int m, gb300_blas_int n,
+void GB300_ENTRY(cblas_cgemv)(CBLAS_ORDER order, CBLAS_TRANSPOSE transA, gb300_blas_int m, gb300_blas_int n,
                  const void* alpha, const void* A, gb300_blas_int lda, const void* x, gb300_blas_int incX,
                  const void* beta, void* y, gb300_blas_int incY);
-void cblas_zgemv(CBLAS_ORDER order, CBLAS_TRANSPOSE transA, gb300_blas_int m, gb300_blas_int n,
+void GB300_ENTRY(cblas_zgemv)(CBLAS_ORDER order, CBLAS_TRANSPOSE transA, gb300_blas_int m, gb300_blas_int n,
                  const void* alpha, const void* A, gb300_blas_int lda, const void* x, gb300_blas_int incX,
                  const void* beta, void* y, gb300_blas_int incY);
 /* blaze/math/blas/cblas/trmm.h:116,153,... */
-void cblas_strmm(CBLAS_ORDER order, CBLAS_SIDE side, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA, CBLAS_DIAG diag,
+void GB300_ENTRY(cblas_strmm)(CBLAS_ORDER order, CBLAS_SIDE side, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA, CBLAS_DIAG diag,
                  gb300_blas_int m, gb300_blas_int n, float alpha, const float* A, gb300_blas_int lda, float* B,
                  gb300_blas_int ldb);
-void cblas_dtrmm(CBLAS_ORDER order, CBLAS_SIDE side, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA, CBLAS_DIAG diag,
+void GB300_ENTRY(cblas_dtrmm)(CBLAS_ORDER order, CBLAS_SIDE side, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA, CBLAS_DIAG diag,
                  gb300_blas_int m, gb300_blas_int n, double alpha, const double* A, gb300_blas_int lda,
                  double* B, gb300_blas_int ldb);
-void cblas_ctrmm(CBLAS_ORDER order, CBLAS_SIDE side, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA, CBLAS_DIAG diag,
+void GB300_ENTRY(cblas_ctrmm)(CBLAS_ORDER order, CBLAS_SIDE side, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA, CBLAS_DIAG diag,
                  gb300_blas_int m, gb300_blas_int n, const void* alpha, const void* A, gb300_blas_int lda,
                  void* B, gb300_blas_int ldb);
-void cblas_ztrmm(CBLAS_ORDER order, CBLAS_SIDE side, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA, CBLAS_DIAG diag,
+void GB300_ENTRY(cblas_ztrmm)(CBLAS_ORDER order, CBLAS_SIDE side, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA, CBLAS_DIAG diag,
                  gb300_blas_int m, gb300_blas_int n, const void* alpha, const void* A, gb300_blas_int lda,
                  void* B, gb300_blas_int ldb);
 /* blaze/math/blas/cblas/trmv.h:111,145,181,218 */
-void cblas_strmv(CBLAS_ORDER order, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA, CBLAS_DIAG diag, gb300_blas_int n,
+void GB300_ENTRY(cblas_strmv)(CBLAS_ORDER order, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA, CBLAS_DIAG diag, gb300_blas_int n,
                  const float* A, gb300_blas_int lda, float* x, gb300_blas_int incX);
-void cblas_dtrmv(CBLAS_ORDER order, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA, CBLAS_DIAG diag, gb300_blas_int n,
+void GB300_ENTRY(cblas_dtrmv)(CBLAS_ORDER order, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA, CBLAS_DIAG diag, gb300_blas_int n,
                  const double* A, gb300_blas_int lda, double* x, gb300_blas_int incX);
-void cblas_ctrmv(CBLAS_ORDER order, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA, CBLAS_DIAG diag, gb300_blas_int n,
+void GB300_ENTRY(cblas_ctrmv)(CBLAS_ORDER order, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA, CBLAS_DIAG diag, gb300_blas_int n,
                  const void* A, gb300_blas_int lda, void* x, gb300_blas_int incX);
-void cblas_ztrmv(CBLAS_ORDER order, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA, CBLAS_DIAG diag, gb300_blas_int n,
+void GB300_ENTRY(cblas_ztrmv)(CBLAS_ORDER order, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA, CBLAS_DIAG diag, gb300_blas_int n,
                  const void* A, gb300_blas_int lda, void* x, gb300_blas_int incX);
 /* blaze/math/blas/cblas/trsm.h (stubs from here on) */
 void cblas_strsm(CBLAS_ORDER order, CBLAS_SIDE side, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA, CBLAS_DIAG diag,
@@ -250,6 +275,86 @@ static inline void cblas_dgemm(CBLAS_ORDER order, CBLAS_TRANSPOSE transA, CBLAS_
                                double beta, double* C, gb300_blas_int ldc) {
     gb300_cblas_dgemm_checked(order, transA, transB, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
     gb300_throw_if_error("cblas_dgemm");
+}
+static inline void cblas_sgemv(CBLAS_ORDER order, CBLAS_TRANSPOSE transA, gb300_blas_int m, gb300_blas_int n, float
+                              alpha, const float* A, gb300_blas_int lda, const float* x, gb300_blas_int incX, float
+                              beta, float* y, gb300_blas_int incY) {
+    gb300_cblas_sgemv_checked(order, transA, m, n, alpha, A, lda, x, incX, beta, y, incY);
+    gb300_throw_if_error("cblas_sgemv");
+}
+static inline void cblas_dgemv(CBLAS_ORDER order, CBLAS_TRANSPOSE transA, gb300_blas_int m, gb300_blas_int n, double
+                              alpha, const double* A, gb300_blas_int lda, const double* x, gb300_blas_int incX, double
+                              beta, double* y, gb300_blas_int incY) {
+    gb300_cblas_dgemv_checked(order, transA, m, n, alpha, A, lda, x, incX, beta, y, incY);
+    gb300_throw_if_error("cblas_dgemv");
+}
+static inline void cblas_cgemv(CBLAS_ORDER order, CBLAS_TRANSPOSE transA, gb300_blas_int m, gb300_blas_int n, const
+                              void* alpha, const void* A, gb300_blas_int lda, const void* x, gb300_blas_int incX,
+                              const void* beta, void* y, gb300_blas_int incY) {
+    gb300_cblas_cgemv_checked(order, transA, m, n, alpha, A, lda, x, incX, beta, y, incY);
+    gb300_throw_if_error("cblas_cgemv");
+}
+static inline void cblas_zgemv(CBLAS_ORDER order, CBLAS_TRANSPOSE transA, gb300_blas_int m, gb300_blas_int n, const
+                              void* alpha, const void* A, gb300_blas_int lda, const void* x, gb300_blas_int incX,
+                              const void* beta, void* y, gb300_blas_int incY) {
+    gb300_cblas_zgemv_checked(order, transA, m, n, alpha, A, lda, x, incX, beta, y, incY);
+    gb300_throw_if_error("cblas_zgemv");
+}
+static inline void cblas_cgemm(CBLAS_ORDER order, CBLAS_TRANSPOSE transA, CBLAS_TRANSPOSE transB, gb300_blas_int m,
+                              gb300_blas_int n, gb300_blas_int k, const void* alpha, const void* A, gb300_blas_int
+                              lda, const void* B, gb300_blas_int ldb, const void* beta, void* C, gb300_blas_int ldc) {
+    gb300_cblas_cgemm_checked(order, transA, transB, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+    gb300_throw_if_error("cblas_cgemm");
+}
+static inline void cblas_zgemm(CBLAS_ORDER order, CBLAS_TRANSPOSE transA, CBLAS_TRANSPOSE transB, gb300_blas_int m,
+                              gb300_blas_int n, gb300_blas_int k, const void* alpha, const void* A, gb300_blas_int
+                              lda, const void* B, gb300_blas_int ldb, const void* beta, void* C, gb300_blas_int ldc) {
+    gb300_cblas_zgemm_checked(order, transA, transB, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+    gb300_throw_if_error("cblas_zgemm");
+}
+static inline void cblas_strmm(CBLAS_ORDER order, CBLAS_SIDE side, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA, CBLAS_DIAG
+                              diag, gb300_blas_int m, gb300_blas_int n, float alpha, const float* A, gb300_blas_int
+                              lda, float* B, gb300_blas_int ldb) {
+    gb300_cblas_strmm_checked(order, side, uplo, transA, diag, m, n, alpha, A, lda, B, ldb);
+    gb300_throw_if_error("cblas_strmm");
+}
+static inline void cblas_dtrmm(CBLAS_ORDER order, CBLAS_SIDE side, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA, CBLAS_DIAG
+                              diag, gb300_blas_int m, gb300_blas_int n, double alpha, const double* A, gb300_blas_int
+                              lda, double* B, gb300_blas_int ldb) {
+    gb300_cblas_dtrmm_checked(order, side, uplo, transA, diag, m, n, alpha, A, lda, B, ldb);
+    gb300_throw_if_error("cblas_dtrmm");
+}
+static inline void cblas_ctrmm(CBLAS_ORDER order, CBLAS_SIDE side, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA, CBLAS_DIAG
+                              diag, gb300_blas_int m, gb300_blas_int n, const void* alpha, const void* A,
+                              gb300_blas_int lda, void* B, gb300_blas_int ldb) {
+    gb300_cblas_ctrmm_checked(order, side, uplo, transA, diag, m, n, alpha, A, lda, B, ldb);
+    gb300_throw_if_error("cblas_ctrmm");
+}
+static inline void cblas_ztrmm(CBLAS_ORDER order, CBLAS_SIDE side, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA, CBLAS_DIAG
+                              diag, gb300_blas_int m, gb300_blas_int n, const void* alpha, const void* A,
+                              gb300_blas_int lda, void* B, gb300_blas_int ldb) {
+    gb300_cblas_ztrmm_checked(order, side, uplo, transA, diag, m, n, alpha, A, lda, B, ldb);
+    gb300_throw_if_error("cblas_ztrmm");
+}
+static inline void cblas_strmv(CBLAS_ORDER order, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA, CBLAS_DIAG diag,
+                              gb300_blas_int n, const float* A, gb300_blas_int lda, float* x, gb300_blas_int incX) {
+    gb300_cblas_strmv_checked(order, uplo, transA, diag, n, A, lda, x, incX);
+    gb300_throw_if_error("cblas_strmv");
+}
+static inline void cblas_dtrmv(CBLAS_ORDER order, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA, CBLAS_DIAG diag,
+                              gb300_blas_int n, const double* A, gb300_blas_int lda, double* x, gb300_blas_int incX) {
+    gb300_cblas_dtrmv_checked(order, uplo, transA, diag, n, A, lda, x, incX);
+    gb300_throw_if_error("cblas_dtrmv");
+}
+static inline void cblas_ctrmv(CBLAS_ORDER order, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA, CBLAS_DIAG diag,
+                              gb300_blas_int n, const void* A, gb300_blas_int lda, void* x, gb300_blas_int incX) {
+    gb300_cblas_ctrmv_checked(order, uplo, transA, diag, n, A, lda, x, incX);
+    gb300_throw_if_error("cblas_ctrmv");
+}
+static inline void cblas_ztrmv(CBLAS_ORDER order, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA, CBLAS_DIAG diag,
+                              gb300_blas_int n, const void* A, gb300_blas_int lda, void* x, gb300_blas_int incX) {
+    gb300_cblas_ztrmv_checked(order, uplo, transA, diag, n, A, lda, x, incX);
+    gb300_throw_if_error("cblas_ztrmv");
 }
 }
 #endif

@@ -1,7 +1,9 @@
 """Compile the Blaze drop-in test program (needs the reference headers; test infrastructure).
 
-    build(kind)   kind = "stub": linked against stub_cblas.cpp (CPU stand-in that logs calls)
-                  kind = "lib":  linked against blaze_gb300/libgb300blas.so
+    build(kind, program)   kind = "stub": linked against stub_cblas.cpp (CPU stand-in that logs calls)
+                           kind = "lib":  linked against blaze_gb300/libgb300blas.so
+                           program = "main" (dropin_main.cpp: ?gemm) or "next" (dropin_next.cpp:
+                           gemv / trmv / complex gemm / trmm through Blaze's expressions)
 Returns the executable path, or None when the Blaze headers are not available here.
 """
 from __future__ import annotations
@@ -23,12 +25,19 @@ def available() -> bool:
     return os.path.isdir(os.path.join(REF, "blaze")) and shutil.which("g++") is not None
 
 
-def build(kind: str) -> str | None:
+# matrix x vector products take Blaze's BLAS kernels (off by default, blaze/config/BLAS.h) from
+# modest sizes on (blaze/config/Thresholds.h)
+NEXT_FLAGS = ["-DBLAZE_USE_BLAS_MATRIX_VECTOR_MULTIPLICATION=1", "-DBLAZE_DMATDVECMULT_THRESHOLD=1000UL",
+              "-DBLAZE_TDMATDVECMULT_THRESHOLD=1000UL", "-DBLAZE_TDVECDMATMULT_THRESHOLD=1000UL",
+              "-DBLAZE_TDVECTDMATMULT_THRESHOLD=1000UL"]
+
+
+def build(kind: str, program: str = "main") -> str | None:
     if not available():
         return None
     os.makedirs(OUT, exist_ok=True)
-    exe = os.path.join(OUT, f"dropin_{kind}")
-    srcs = [os.path.join(HERE, "dropin_main.cpp")]
+    exe = os.path.join(OUT, f"dropin_{kind}" if program == "main" else f"dropin_{program}_{kind}")
+    srcs = [os.path.join(HERE, f"dropin_{program}.cpp")]
     deps = list(srcs) + [os.path.join(ROOT, "include", "gb300_cblas.h")]
     extra = []
     if kind == "stub":
@@ -39,7 +48,8 @@ def build(kind: str) -> str | None:
         extra = ["-L" + lib_dir, "-lgb300blas", "-Wl,-rpath," + lib_dir]
     if os.path.exists(exe) and all(os.path.getmtime(exe) >= os.path.getmtime(d) for d in deps):
         return exe
-    cmd = ["g++", *FLAGS, "-isystem", REF, *srcs, "-o", exe, *extra]
+    flags = FLAGS + (NEXT_FLAGS if program == "next" else [])
+    cmd = ["g++", *flags, "-isystem", REF, *srcs, "-o", exe, *extra]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("Blaze drop-in build failed:\n" + " ".join(cmd) + "\n" + r.stderr[-4000:])

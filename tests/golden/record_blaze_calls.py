@@ -1,8 +1,14 @@
-"""Record the CBLAS calls Blaze itself makes for `C = A*B`, `C += A*B`, `C -= A*B` and
-`C = s*(A*B)` in BLAS mode (all storage-order classes and a CustomMatrix), by running the
-drop-in program of tests/blaze_dropin/ against its logging stub.  Writes
-tests/golden/blaze_calls.txt (one call per line: routine order transA transB m n k alpha lda ldb
-beta ldc), which the GPU tests replay through the real library.  Needs the reference headers.
+"""Record the CBLAS calls Blaze itself makes in BLAS mode, by running the drop-in programs of
+tests/blaze_dropin/ against their logging stub:
+
+- tests/golden/blaze_calls.txt: `C = A*B`, `C += A*B`, `C -= A*B` and `C = s*(A*B)` (all
+  storage-order classes and a CustomMatrix); one call per line: routine order transA transB m n k
+  alpha lda ldb beta ldc;
+- tests/golden/blaze_next_calls.txt: matrix x vector (dense and triangular), complex products and
+  triangular products (dropin_next.cpp); one call per line: the routine name, then its CBLAS
+  arguments in order without the pointers (complex scalars as re,im).
+
+The GPU tests replay both through the real library.  Needs the reference headers.
 """
 import os
 import subprocess
@@ -13,13 +19,14 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(os.path.dirname(HERE), "blaze_dropin"))
 import build as dropin  # noqa: E402
 
-exe = dropin.build("stub")
-if exe is None:
-    raise SystemExit("reference headers not available")
-with tempfile.TemporaryDirectory() as d:
-    log = os.path.join(d, "log.txt")
-    subprocess.run([exe], check=True, env=dict(os.environ, GB300_STUB_LOG=log), capture_output=True)
-    lines = open(log).read().splitlines()
-with open(os.path.join(HERE, "blaze_calls.txt"), "w") as f:
-    f.write("\n".join(lines) + "\n")
-print(f"recorded {len(lines)} calls")
+for program, out in (("main", "blaze_calls.txt"), ("next", "blaze_next_calls.txt")):
+    exe = dropin.build("stub", program)
+    if exe is None:
+        raise SystemExit("reference headers not available")
+    with tempfile.TemporaryDirectory() as d:
+        log = os.path.join(d, "log.txt")
+        subprocess.run([exe], check=True, env=dict(os.environ, GB300_STUB_LOG=log), capture_output=True)
+        lines = open(log).read().splitlines()
+    with open(os.path.join(HERE, out), "w") as f:
+        f.write("\n".join(lines) + "\n")
+    print(f"{out}: recorded {len(lines)} calls")

@@ -44,3 +44,106 @@ def test_replay_blaze_calls(method):
             assert blaze_equal(R, C, 1e-8).all(), c
     finally:
         G.lib().gb300_set_default_method(prev)
+
+
+# ---- the routines next to ?gemm, as Blaze's expressions call them (tests/golden/blaze_next_calls.txt)
+NEXT_CALLS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "blaze_next_calls.txt")
+
+
+def _scalar(tok):
+    if "," in tok:
+        re_, im_ = tok.split(",")
+        return complex(float(re_), float(im_))
+    return float(tok)
+
+
+def _mat(X, order, rows, cols, ld):
+    """The rows x cols matrix stored in X (CBLAS order, leading dimension ld), as a numpy view."""
+    s = X.itemsize
+    if order == O.ROW_MAJOR:
+        return np.lib.stride_tricks.as_strided(X, (rows, cols), (ld * s, s))
+    return np.lib.stride_tricks.as_strided(X, (rows, cols), (s, ld * s))
+
+
+def _op(M, t):
+    return M if t == 111 else (M.T if t == 112 else M.conj().T)
+
+
+def _tri(M, uplo, diag):
+    T = np.tril(M) if uplo == 122 else np.triu(M)
+    if diag == 132:
+        np.fill_diagonal(T, 1.0)
+    return T
+
+
+def _vals(count, seed, kind):
+    if kind == "z":
+        return O.uniform(count, seed) + 1j * O.uniform(count, seed + 7919)
+    v = O.uniform(count, seed)
+    return v.astype(np.float32) if kind == "s" else v
+
+
+def test_replay_blaze_neighbouring_calls():
+    lines = open(NEXT_CALLS).read().splitlines()
+    assert len(lines) == 11
+    for q, ln in enumerate(lines):
+        f = ln.split()
+        name, kind = f[0], f[0][0]
+        eps = 2.0 ** -24 if kind == "s" else 2.0 ** -53
+        if name.endswith("gemv"):
+            order, ta, m, n = (int(v) for v in f[1:5])
+            al, lda, incx, be, incy = _scalar(f[5]), int(f[6]), int(f[7]), _scalar(f[8]), int(f[9])
+            rows = m if order == O.ROW_MAJOR else n
+            A = _vals(rows * lda, 400 + q, kind)
+            xl, yl = (m, n) if ta != 111 else (n, m)
+            x = _vals(xl * abs(incx), 500 + q, kind)
+            y = _vals(yl * abs(incy), 600 + q, kind)
+            ref = al * (_op(_mat(A, order, m, n, lda), ta).astype(np.complex128 if kind == "z" else np.float64)
+                        @ x[::incx]) + be * y[::incy]
+            if kind == "z":
+                G.cblas_zgemv(order, ta, m, n, al, A, lda, x, incx, be, y, incy)
+            else:
+                G.cblas_gemv(order, ta, m, n, al, A, lda, x, incx, be, y, incy, dtype=kind)
+            got = y[::incy]
+            k = xl
+        elif name.endswith("trmv"):
+            order, uplo, ta, diag, n, lda, incx = (int(v) for v in f[1:8])
+            A = _vals(n * lda, 400 + q, kind)
+            x = _vals(n * abs(incx), 500 + q, kind)
+            ref = _op(_tri(np.array(_mat(A, order, n, n, lda)), uplo, diag), ta) @ x[::incx]
+            G.cblas_trmv(order, uplo, ta, diag, n, A, lda, x, incx, dtype=kind)
+            got = x[::incx]
+            k = n
+        elif name.endswith("gemm"):
+            order, ta, tb, m, n, k = (int(v) for v in f[1:7])
+            al, lda, ldb, be, ldc = _scalar(f[7]), int(f[8]), int(f[9]), _scalar(f[10]), int(f[11])
+            ra = (k if ta != 111 else m) if order == O.ROW_MAJOR else (m if ta != 111 else k)
+            rb = (n if tb != 111 else k) if order == O.ROW_MAJOR else (k if tb != 111 else n)
+            rc = m if order == O.ROW_MAJOR else n
+            A = _vals(ra * lda, 400 + q, kind)
+            B = _vals(rb * ldb, 500 + q, kind)
+            C = _vals(rc * ldc, 600 + q, kind)
+            sa = (k, m) if ta != 111 else (m, k)
+            sb = (n, k) if tb != 111 else (k, n)
+            ref = al * (_op(_mat(A, order, *sa, lda), ta) @ _op(_mat(B, order, *sb, ldb), tb)) + \
+                be * np.array(_mat(C, order, m, n, ldc))
+            G.cblas_zgemm(order, ta, tb, m, n, k, al, A, lda, B, ldb, be, C, ldc)
+            got = np.array(_mat(C, order, m, n, ldc))
+        else:  # trmm
+            order, side, uplo, ta, diag, m, n = (int(v) for v in f[1:8])
+            al, lda, ldb = _scalar(f[8]), int(f[9]), int(f[10])
+            ka = m if side == 141 else n
+            A = _vals(ka * lda, 400 + q, kind)
+            rb = m if order == O.ROW_MAJOR else n
+            B = _vals(rb * ldb, 500 + q, kind)
+            T = _op(_tri(np.array(_mat(A, order, ka, ka, lda)), uplo, diag), ta)
+            B0 = np.array(_mat(B, order, m, n, ldb))
+            ref = al * (T @ B0 if side == 141 else B0 @ T)
+            if kind == "z":
+                G.cblas_ztrmm(order, side, uplo, ta, diag, m, n, al, A, lda, B, ldb)
+            else:
+                G.cblas_trmm(order, side, uplo, ta, diag, m, n, al, A, lda, B, ldb, dtype=kind)
+            got = np.array(_mat(B, order, m, n, ldb))
+            k = ka
+        scale = max(float(np.max(np.abs(ref))), 1.0)
+        assert float(np.max(np.abs(got - ref))) <= 4 * k * eps * scale * 8, (q, ln)

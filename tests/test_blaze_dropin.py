@@ -79,3 +79,57 @@ def test_recorded_call_fixture_matches_blaze():
         fresh = open(log).read().splitlines()
     committed = open(os.path.join(HERE, "golden", "blaze_calls.txt")).read().splitlines()
     assert fresh == committed
+
+
+# ---- the routines next to ?gemm, reached through Blaze's own expressions (dropin_next.cpp) ----------
+NEXT_ROUTINES = {  # label -> the CBLAS routine Blaze must call for it
+    "gemv_r": "dgemv", "gemv_c_add": "dgemv", "gemv_t": "dgemv", "sgemv_r": "sgemv", "trmv_lower_r": "dtrmv",
+    "trmv_upper_c": "dtrmv", "ztrmv_lower_r": "ztrmv", "zgemv_r": "zgemv", "zgemm_rr": "zgemm",
+    "dtrmm_lower": "dtrmm", "ztrmm_upper": "ztrmm",
+}
+
+
+def test_blaze_expressions_reach_the_neighbouring_routines(tmp_path):
+    exe = dropin.build("stub", "next")
+    log = tmp_path / "log.txt"
+    out = run(exe, {"GB300_STUB_LOG": str(log)})
+    assert [f[0] for f in out] == list(NEXT_ROUTINES)
+    for fields in out:
+        assert fields[1] == "status=ok", fields
+        tol = 1e-4 if fields[0].startswith("s") else 1e-12
+        assert float(fields[2].split("=")[1]) <= tol, fields
+    calls = [ln.split() for ln in log.read_text().splitlines()]
+    assert [c[0] for c in calls] == list(NEXT_ROUTINES.values())
+    # y += A*x is gemv with beta = 1 (DMatDVecMultExpr's BLAS add-assign kernel); x^T*A is the
+    # transposed gemv; the column-major upper triangle is the row-major lower one's mirror
+    by = dict(zip(NEXT_ROUTINES, calls))
+    assert by["gemv_c_add"][1:3] == ["102", "111"] and float(by["gemv_c_add"][8]) == 1.0
+    assert by["gemv_t"][2] == "112"
+    assert by["trmv_lower_r"][1:5] == ["101", "122", "111", "131"]
+    assert by["trmv_upper_c"][1:5] == ["102", "121", "111", "131"]
+    assert by["dtrmm_lower"][1:6] == ["101", "141", "122", "111", "131"]
+
+
+def test_neighbouring_call_fixture_matches_blaze():
+    exe = dropin.build("stub", "next")
+    import tempfile
+    with tempfile.TemporaryDirectory() as d:
+        log = os.path.join(d, "log.txt")
+        run(exe, {"GB300_STUB_LOG": log})
+        fresh = open(log).read().splitlines()
+    committed = open(os.path.join(HERE, "golden", "blaze_next_calls.txt")).read().splitlines()
+    assert fresh == committed
+
+
+def test_real_library_without_gpu_raises_for_the_neighbouring_routines_too():
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    import blaze_gb300 as G
+    if not os.path.exists(G.LIB_PATH):
+        G.build()
+    exe = dropin.build("lib", "next")
+    out = run(exe, {})
+    assert len(out) == len(NEXT_ROUTINES)
+    assert all(f[1] == "status=exception" for f in out), out
+    assert all("no CUDA device" in " ".join(f) for f in out)
