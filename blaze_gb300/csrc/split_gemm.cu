@@ -332,14 +332,48 @@ __global__ void stats_finalize_pair_kernel(const OperandPair op, int64_t K, unsi
 
 // One block: norms, scale norms, slice count and bound.  Sums are formed relative to the largest
 // row exponent, so the ratio rho = ||2^e|| ||2^f|| / (||A|| ||B||) is finite for any finite input.
+//
+// On GB300 every FP64 warp instruction occupies the narrow FP64 pipe for many cycles whatever the
+// number of active lanes, so these planning kernels keep FP64 work off long serial chains: block
+// sums finish in one warp's shuffles, and the searches below test 32 candidates per instruction.
 __device__ double block_sum(double v, double* red) {
+    __shared__ double total;
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     __syncthreads();
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
     __syncthreads();
-    double t = 0.0;
-    for (int i = 0; i < int(blockDim.x >> 5); ++i) t += red[i];
-    return t;
+    if (threadIdx.x < 32) {
+        double t = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+        if (threadIdx.x == 0) total = t;
+    }
+    __syncthreads();
+    return total;
+}
+
+// Smallest b in [lo, hi] with ok(b), hi + 1 when there is none (ok false, then true as b grows):
+// the 32 lanes of the calling warp test 32 candidates at a time.
+template <typename F>
+__device__ int warp_first_true(int lo, int hi, F ok) {
+    const int lane = threadIdx.x & 31;
+    for (int base = lo; base <= hi; base += 32) {
+        const int b = base + lane;
+        const unsigned m = __ballot_sync(0xffffffffu, b <= hi && ok(b));
+        if (m) return base + __ffs(int(m)) - 1;
+    }
+    return hi + 1;
+}
+
+// Largest b in [lo, hi] with ok(b), lo - 1 when there is none (ok true, then false as b grows).
+template <typename F>
+__device__ int warp_last_true(int lo, int hi, F ok) {
+    const int lane = threadIdx.x & 31;
+    for (int base = hi; base >= lo; base -= 32) {
+        const int b = base - lane;
+        const unsigned m = __ballot_sync(0xffffffffu, b >= lo && ok(b));
+        if (m) return base - (__ffs(int(m)) - 1);
+    }
+    return lo - 1;
 }
 
 __device__ long long block_max_ll(long long v, long long* red) {
@@ -373,26 +407,35 @@ __global__ void __launch_bounds__(1024) split_info_kernel(const int* __restrict_
                                   int mode, int fixed_slices, int cap_planes, double target, SplitInfo* info) {
     __shared__ double redd[32];
     __shared__ int redi[32];
+    // one pass: Inf/NaN flag, largest exponents, largest row / column sums of squares relative to
+    // 2^(2e) (non-negative doubles: their bit patterns order like integers)
     int bad = 0, EA = -100000, EB = -100000;
+    long long QAb = 0, QBb = 0;
     for (int64_t i = threadIdx.x; i < m; i += blockDim.x) {
-        if (eA[i] == kNonFinite) bad = 1;
-        else if (qA[i] > 0.0) EA = max(EA, eA[i]);
+        const int e = eA[i];
+        if (e == kNonFinite) {
+            bad = 1;
+            continue;
+        }
+        const long long qb = __double_as_longlong(qA[i]);
+        if (qb > 0) EA = max(EA, e);
+        QAb = max(QAb, qb);
     }
     for (int64_t j = threadIdx.x; j < n; j += blockDim.x) {
-        if (eB[j] == kNonFinite) bad = 1;
-        else if (qB[j] > 0.0) EB = max(EB, eB[j]);
+        const int e = eB[j];
+        if (e == kNonFinite) {
+            bad = 1;
+            continue;
+        }
+        const long long qb = __double_as_longlong(qB[j]);
+        if (qb > 0) EB = max(EB, e);
+        QBb = max(QBb, qb);
     }
     bad = block_max_int(bad, redi);
     EA = block_max_int(EA, redi);
     EB = block_max_int(EB, redi);
-    // largest row / column sum of squares relative to 2^(2e): bounds the norm of a scaled row
-    double QA = 0, QB = 0;
-    for (int64_t i = threadIdx.x; i < m; i += blockDim.x)
-        if (eA[i] != kNonFinite) QA = fmax(QA, qA[i]);
-    for (int64_t j = threadIdx.x; j < n; j += blockDim.x)
-        if (eB[j] != kNonFinite) QB = fmax(QB, qB[j]);
-    QA = __longlong_as_double(block_max_ll(__double_as_longlong(QA), reinterpret_cast<long long*>(redd)));
-    QB = __longlong_as_double(block_max_ll(__double_as_longlong(QB), reinterpret_cast<long long*>(redd)));
+    const double QA = __longlong_as_double(block_max_ll(QAb, reinterpret_cast<long long*>(redd)));
+    const double QB = __longlong_as_double(block_max_ll(QBb, reinterpret_cast<long long*>(redd)));
     double sa = 0, na = 0, sb = 0, nb = 0;
     for (int64_t i = threadIdx.x; i < m; i += blockDim.x) {
         if (eA[i] == kNonFinite || qA[i] <= 0.0) continue;
@@ -410,7 +453,7 @@ __global__ void __launch_bounds__(1024) split_info_kernel(const int* __restrict_
     na = block_sum(na, redd);
     sb = block_sum(sb, redd);
     nb = block_sum(nb, redd);
-    if (threadIdx.x == 0) {
+    if (threadIdx.x < 32) {  // warp 0 plans; lane 0 writes
         SplitInfo r;
         r.nonfinite = bad;
         r.normA = (na > 0) ? ldexp(sqrt(na), EA) : 0.0;
@@ -427,9 +470,9 @@ __global__ void __launch_bounds__(1024) split_info_kernel(const int* __restrict_
             auto bnd = [&](int b) {
                 return pow2i(-b - 1) * (rA + rB) + pow2i(-2 * b - 2) * rA * rB + pow2i(-52);
             };
-            // beta <= 55 keeps |A'| < 2^56, the range of the residue extraction
-            int beta = 1;
-            while (beta < 55 && bnd(beta) > target) ++beta;
+            // the smallest beta in [1, 55] that meets the target (beta <= 55 keeps |A'| < 2^56, the
+            // range of the residue extraction)
+            int beta = min(55, warp_first_true(1, 54, [&](int b) { return bnd(b) <= target; }));
             // The scaled rows satisfy ||A'_i|| <= 2^beta sqrt(Q_A) + sqrt(k)/2 (the rounding adds
             // at most 1/2 per entry), so by Cauchy-Schwarz every exact product entry T has
             // |T| <= (2^beta sqrt(Q_A) + sqrt(k)/2)(2^beta sqrt(Q_B) + sqrt(k)/2).  The moduli's
@@ -450,15 +493,15 @@ __global__ void __launch_bounds__(1024) split_info_kernel(const int* __restrict_
                 have += c_mod_log2[N];
                 ++N;
             }
-            // the moduli chosen may carry more bits than needed: round to as many bits as they allow
-            // need(b) exceeds 1.0875 + 2b + log2(sqa sqb): start at the largest b that this allows and
-            // step down (one or two steps)
-            beta = 55;
+            // the moduli chosen may carry more bits than needed: round to as many bits as they allow.
+            // need(b) exceeds 1.0875 + 2b + log2(sqa sqb), so no b above b0 qualifies: the largest b
+            // in (-60, b0] with need(b) <= have, -60 when none
+            int bhi = 55;
             if (sqa > 0 && sqb > 0) {
                 const int b0 = int(floor((have - 1.0875 - log2(sqa) - log2(sqb)) / 2.0));
-                beta = b0 < 55 ? (b0 > -60 ? b0 : -60) : 55;
+                bhi = b0 < 55 ? (b0 > -60 ? b0 : -60) : 55;
             }
-            while (beta > -60 && need(beta) > have) --beta;
+            beta = warp_last_true(-59, bhi, [&](int b) { return need(b) <= have; });
             r.slices = N;
             r.beta = beta;
             r.beta_b = beta;
@@ -485,7 +528,7 @@ __global__ void __launch_bounds__(1024) split_info_kernel(const int* __restrict_
             r.slices = 2;
             r.bound = 3.0 * ldexp(1.0, -16) + double(k) * ldexp(1.0, -24);
         }
-        *info = r;
+        if (threadIdx.x == 0) *info = r;
     }
 }
 
@@ -501,17 +544,18 @@ __device__ SideStats side_stats(const int* __restrict__ e, const double* __restr
                                 int* redi) {
     SideStats r;
     int bad = 0, E = -100000;
-    double Q = 0;
+    long long Qb = 0;  // non-negative doubles: their bit patterns order like integers
     for (int64_t i = threadIdx.x; i < count; i += blockDim.x) {
         if (e[i] == kNonFinite) bad = 1;
         else {
-            if (q[i] > 0.0) E = max(E, e[i]);
-            Q = fmax(Q, q[i]);
+            const long long qb = __double_as_longlong(q[i]);
+            if (qb > 0) E = max(E, e[i]);
+            Qb = max(Qb, qb);
         }
     }
     r.bad = block_max_int(bad, redi);
     r.E = block_max_int(E, redi);
-    r.Q = __longlong_as_double(block_max_ll(__double_as_longlong(Q), reinterpret_cast<long long*>(redd)));
+    r.Q = __longlong_as_double(block_max_ll(Qb, reinterpret_cast<long long*>(redd)));
     double sv = 0, nv = 0;
     for (int64_t i = threadIdx.x; i < count; i += blockDim.x) {
         if (e[i] == kNonFinite || q[i] <= 0.0) continue;
@@ -535,19 +579,18 @@ __global__ void __launch_bounds__(1024) split_side_kernel(const int* __restrict_
     __shared__ double redd[32];
     __shared__ int redi[32];
     const SideStats t = side_stats(e, q, count, redd, redi);
-    if (threadIdx.x == 0) {
+    if (threadIdx.x < 32) {  // warp 0 plans; lane 0 writes
         SplitInfo r;
         r.nonfinite = t.bad;
         r.normA = r.normB = (t.nrm > 0) ? ldexp(sqrt(t.nrm), t.E) : 0.0;
         r.scaleA = r.scaleB = (t.s > 0) ? ldexp(sqrt(t.s), t.E) : 0.0;
         r.qmaxA = r.qmaxB = t.Q;
         const double rr = (t.nrm > 0) ? sqrt(double(k) * t.s / t.nrm) : 0.0;
-        int beta = 1;
-        while (beta < 55 && pow2i(-beta - 1) * rr > 0.5 * target) ++beta;
+        const int beta = min(55, warp_first_true(1, 54, [&](int b) { return pow2i(-b - 1) * rr <= 0.5 * target; }));
         r.beta = r.beta_b = beta;
         r.slices = planes;
         r.bound = 0.0;
-        *out = r;
+        if (threadIdx.x == 0) *out = r;
     }
 }
 
@@ -1754,12 +1797,15 @@ int device_product_host_panels(const Gemm& g, const SplitRequest& req, const Lau
     const SplitGeometry G = split_geometry(g, req, r.num_sms);
     if (G.mode != kCrt) return GB300_ERR_NOT_SUPPORTED;
     // blocks: row panels of about a quarter of A (at least 2048 rows) and two column blocks of B
-    // (when each has at least 2048 columns), whole pair tiles
+    // (when each has at least 2048 columns), whole pair tiles.  (Loading A and B alternately in
+    // quarters over a 4 x 4 grid starts the first block earlier but measured 6 % slower end to end
+    // at 8192^3: the copies of C back then share the link with more of the copies in.)
+    const bool c_locked = page_locked(g.C);
     const int64_t Mp = std::max<int64_t>(2048, round_up((m + 3) / 4, TMP));
     const int P = int((m + Mp - 1) / Mp);
     const int64_t Nq = n >= 4096 ? round_up((n + 1) / 2, TN) : round_up(n, TN);
     const int Q = int((n + Nq - 1) / Nq);
-    if (P < 2 || P > 16) return GB300_ERR_NOT_SUPPORTED;
+    if (P < 2 || P > 16 || Q > 2) return GB300_ERR_NOT_SUPPORTED;
     if (!pipe_init(r, err)) return GB300_ERR_CUDA;
     Gemm gp = g;
     gp.m = Mp;
@@ -1776,6 +1822,7 @@ int device_product_host_panels(const Gemm& g, const SplitRequest& req, const Lau
     auto* dA = static_cast<double*>(ws.get(kSlotA, size_t(a_rows) * size_t(a_cols) * 8, err));
     auto* dB = static_cast<double*>(ws.get(kSlotB, size_t(b_rows) * size_t(b_cols) * 8, err));
     auto* dC = static_cast<double*>(ws.get(kSlotC, size_t(m) * size_t(n) * 8, err));
+    // A planes of one panel: a panel's blocks all run before the next panel is sliced
     auto* pa = static_cast<__nv_bfloat16*>(ws.get(kSlotSliceA, size_t(max_planes) * size_t(mpad) * size_t(kpad) * 2, err));
     const size_t bblock = size_t(max_planes) * size_t(Nq) * size_t(kpad);  // elements per B block
     auto* pb = static_cast<__nv_bfloat16*>(ws.get(kSlotSliceB, size_t(Q) * bblock * 2, err));
@@ -1806,7 +1853,7 @@ int device_product_host_panels(const Gemm& g, const SplitRequest& req, const Lau
     const double* hB = static_cast<const double*>(g.B);
     double* hC = static_cast<double*>(g.C);
 
-    // ---- copies in, in the order the blocks need them: A_0, B_0 .. B_{Q-1}, A_1 .. A_{P-1} ----
+    // ---- copies in (issued by `load` below, in its order) ----
     cudaError_t e = cudaSuccess;
     auto copy_a = [&](int i) {
         const int64_t r0 = int64_t(i) * Mp, mi = std::min(Mp, m - r0);
@@ -1898,75 +1945,97 @@ int device_product_host_panels(const Gemm& g, const SplitRequest& req, const Lau
     e = cudaFuncSetAttribute(tc_gemm_kernel<kExact>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kTcSmem));
     if (e != cudaSuccess) return cuda_fail("tc_gemm_kernel smem attribute", e);
 
-    // ---- blocks in row-major order: panel i's planes serve its Q blocks; C goes back per block ----
-    // Issue order: operands in (A_0, B_0, B_1, then A_i before panel i), panel i's blocks queued,
-    // then panel i-1's blocks of C out.  With page-locked memory every call returns at once; with
-    // pageable memory each copy holds the host thread until it is done, and this order keeps the
-    // GPU busy meanwhile: A_i+1 goes in and panel i-1 comes out while panel i computes.
-    // C goes back per block; a pageable C whose rows are exactly n elements goes back per panel in
-    // one linear copy instead (pitched copies into untouched pageable pages are slow, copy_to_host)
-    const bool c_per_panel = Q > 1 && g.ldc == n && !page_locked(g.C);
-    auto copy_c_out = [&](int i) {
+    // ---- operands in, blocks as their operands arrive, C back ----
+    // Load order A_0, B_0 .. B_{Q-1}, A_1 .. A_{P-1}; after each load the blocks it completes are
+    // queued (block (i, j) needs A_i and B_j), so panel i's blocks run together on the panel's
+    // planes.  With page-locked memory every call returns at once; with pageable memory each copy
+    // holds the host thread until it is done, and the order keeps the GPU busy meanwhile: A_i+1
+    // goes in and panel i-1 comes out while panel i computes.  C goes back per block as soon as the
+    // block is done (page-locked C); a pageable C goes back per panel, one linear copy when its rows
+    // are exactly n elements (pitched copies into untouched pageable pages are slow, see
+    // copy_to_host), else per block.
+    const bool c_per_panel = !c_locked && Q > 1 && g.ldc == n;
+    auto block_ev = [&](int i, int j) { return ev[P + Q + i * Q + j]; };
+    auto copy_block_out = [&](int i, int j) {
         const int64_t r0 = int64_t(i) * Mp, mi = std::min(Mp, m - r0);
-        for (int j = 0; j < Q && e == cudaSuccess; ++j) {
-            cudaStreamWaitEvent(r.copy_out, ev[P + Q + i * Q + j], 0);
-            if (c_per_panel && j + 1 < Q) continue;
-            const int64_t c0 = c_per_panel ? 0 : int64_t(j) * Nq, nj = c_per_panel ? n : std::min(Nq, n - c0);
-            e = copy_to_host(hC + r0 * g.ldc + c0, size_t(g.ldc) * 8, dC + r0 * n + c0, size_t(n) * 8, size_t(nj) * 8,
-                             size_t(mi), r.copy_out);
+        const int64_t c0 = int64_t(j) * Nq, nj = std::min(Nq, n - c0);
+        cudaStreamWaitEvent(r.copy_out, block_ev(i, j), 0);
+        e = copy_to_host(hC + r0 * g.ldc + c0, size_t(g.ldc) * 8, dC + r0 * n + c0, size_t(n) * 8, size_t(nj) * 8,
+                         size_t(mi), r.copy_out);
+    };
+    auto copy_panel_out = [&](int i) {
+        if (!c_per_panel) {
+            for (int j = 0; j < Q && e == cudaSuccess; ++j) copy_block_out(i, j);
+            return;
+        }
+        const int64_t r0 = int64_t(i) * Mp, mi = std::min(Mp, m - r0);
+        for (int j = 0; j < Q; ++j) cudaStreamWaitEvent(r.copy_out, block_ev(i, j), 0);
+        e = copy_to_host(hC + r0 * g.ldc, size_t(g.ldc) * 8, dC + r0 * n, size_t(n) * 8, size_t(n) * 8, size_t(mi),
+                         r.copy_out);
+    };
+    auto run_block = [&](int i, int j) {
+        const int64_t r0 = int64_t(i) * Mp, mi = std::min(Mp, m - r0);
+        const int64_t c0 = int64_t(j) * Nq, nj = std::min(Nq, n - c0);
+        SplitInfo* info = info_at(P + Q + i * Q + j);
+        split_block_kernel<<<1, 32, 0, st>>>(info_at(i), info_at(P + j), k, max_planes, info);
+        TcParams tp;
+        tp.mode = kCrt;
+        tp.m_tiles = int((mi + TMP - 1) / TMP);
+        tp.n_tiles = int((nj + TN - 1) / TN);
+        tp.nseg = nseg;
+        tp.kb_per_seg = int(Gp.kseg / TK);
+        tp.kb_total = Gp.kb_total;
+        tp.mpad = mpad;
+        tp.npad = Nq;
+        tp.levels = lv;
+        tp.max_levels = max_levels;
+        tp.info = info;
+        tp.status = ctl.status;
+        tp.limit_ns = ctl.wait_limit_ns;
+        tp.inject_stall = ctl.inject_stall;
+        const int units = tp.m_tiles * tp.n_tiles * nseg * max_levels;
+        const int grid = 2 * std::max(1, std::min(units, r.num_sms / 2));
+        {
+            KernelTimer timer("tc_gemm", st);
+            tc_gemm_kernel<kExact><<<grid, THREADS, kTcSmem, st>>>(tA, tB[j], tC, tp);
+        }
+        const int64_t colgroups = (nj + COMBINE_COLS - 1) / COMBINE_COLS;
+        combine_kernel<<<dim3(unsigned((colgroups + 127) / 128), unsigned(std::min<int64_t>(mi, 65535))), 128, 0,
+                         st>>>(lv, nseg, max_levels, mpad, Nq, kCrt, info, eA + r0, eB + c0, mi, nj, g.alpha, g.beta,
+                               dC + r0 * n + c0, n);
+        count_launches(3);
+        if ((e = cudaGetLastError()) != cudaSuccess) return;
+        cudaEventRecord(block_ev(i, j), st);
+        if (c_locked) copy_block_out(i, j);
+    };
+    bool have_a[16] = {}, have_b[2] = {};
+    auto load = [&](int side, int idx) {
+        if (side == 0) {
+            copy_a(idx);
+            if (e != cudaSuccess) return;
+            cudaStreamWaitEvent(st, ev[idx], 0);
+            prep_a(idx);
+            have_a[idx] = true;
+            for (int j = 0; j < Q && e == cudaSuccess; ++j)
+                if (have_b[j]) run_block(idx, j);
+        } else {
+            copy_b(idx);
+            if (e != cudaSuccess) return;
+            cudaStreamWaitEvent(st, ev[P + idx], 0);
+            prep_b(idx);
+            have_b[idx] = true;
+            for (int i = 0; i < P && e == cudaSuccess; ++i)
+                if (have_a[i]) run_block(i, idx);
         }
     };
-    int nb = 0;
-    for (int i = 0; i < P; ++i) {
-        const int64_t r0 = int64_t(i) * Mp, mi = std::min(Mp, m - r0);
-        copy_a(i);
-        if (e != cudaSuccess) return cuda_fail("copy of an operand", e);
-        cudaStreamWaitEvent(st, ev[i], 0);
-        prep_a(i);
-        for (int j = 0; j < Q; ++j, ++nb) {
-            const int64_t c0 = int64_t(j) * Nq, nj = std::min(Nq, n - c0);
-            if (i == 0) {
-                copy_b(j);
-                if (e != cudaSuccess) return cuda_fail("copy of an operand", e);
-                cudaStreamWaitEvent(st, ev[P + j], 0);
-                prep_b(j);
-            }
-            SplitInfo* info = info_at(P + Q + nb);
-            split_block_kernel<<<1, 32, 0, st>>>(info_at(i), info_at(P + j), k, max_planes, info);
-            TcParams tp;
-            tp.mode = kCrt;
-            tp.m_tiles = int((mi + TMP - 1) / TMP);
-            tp.n_tiles = int((nj + TN - 1) / TN);
-            tp.nseg = nseg;
-            tp.kb_per_seg = int(Gp.kseg / TK);
-            tp.kb_total = Gp.kb_total;
-            tp.mpad = mpad;
-            tp.npad = Nq;
-            tp.levels = lv;
-            tp.max_levels = max_levels;
-            tp.info = info;
-            tp.status = ctl.status;
-            tp.limit_ns = ctl.wait_limit_ns;
-            tp.inject_stall = ctl.inject_stall;
-            const int units = tp.m_tiles * tp.n_tiles * nseg * max_levels;
-            const int grid = 2 * std::max(1, std::min(units, r.num_sms / 2));
-            {
-                KernelTimer timer("tc_gemm", st);
-                tc_gemm_kernel<kExact><<<grid, THREADS, kTcSmem, st>>>(tA, tB[j], tC, tp);
-            }
-            const int64_t colgroups = (nj + COMBINE_COLS - 1) / COMBINE_COLS;
-            combine_kernel<<<dim3(unsigned((colgroups + 127) / 128), unsigned(std::min<int64_t>(mi, 65535))), 128, 0,
-                             st>>>(lv, nseg, max_levels, mpad, Nq, kCrt, info, eA + r0, eB + c0, mi, nj, g.alpha, g.beta,
-                                   dC + r0 * n + c0, n);
-            count_launches(3);
-            if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail("block launch", e);
-            cudaEventRecord(ev[P + Q + nb], st);
-        }
-        if (i > 0) copy_c_out(i - 1);
-        if (e != cudaSuccess) return cuda_fail("copy of C back", e);
+    load(0, 0);
+    for (int j = 0; j < Q && e == cudaSuccess; ++j) load(1, j);
+    for (int i = 1; i < P && e == cudaSuccess; ++i) {
+        load(0, i);
+        if (e == cudaSuccess && !c_locked) copy_panel_out(i - 1);
     }
-    copy_c_out(P - 1);
-    if (e != cudaSuccess) return cuda_fail("copy of C back", e);
+    if (e == cudaSuccess && !c_locked) copy_panel_out(P - 1);
+    if (e != cudaSuccess) return cuda_fail("block pipeline", e);
     split_panels_summary_kernel<<<1, 32, 0, st>>>(reinterpret_cast<const uint8_t*>(info_at(P + Q)), info_stride,
                                                   P * Q, info_sum);
     count_launches(1);
