@@ -33,6 +33,7 @@ struct Ar {  // real
     __device__ static V one() { return V(1); }
     __device__ static V conj(V a) { return a; }
     __device__ static V fmadd(V a, V b, V c) { return fma(a, b, c); }
+    __device__ static V fmadd_conj(V a, V b, V c) { return fma(a, b, c); }
     __device__ static V mul(V a, V b) { return a * b; }
     __device__ static V add(V a, V b) { return a + b; }
     __device__ static bool is_zero(V a) { return a == V(0); }
@@ -52,6 +53,11 @@ struct Ar<Cx<T>> {  // complex
     __device__ static V fmadd(V a, V b, V c) {
         return V{fma(a.re, b.re, fma(-a.im, b.im, c.re)), fma(a.re, b.im, fma(a.im, b.re, c.im))};
     }
+    // conj(a) * b + c with the sign folded into the FMAs (a negation would be one more FP64
+    // instruction per element)
+    __device__ static V fmadd_conj(V a, V b, V c) {
+        return V{fma(a.re, b.re, fma(a.im, b.im, c.re)), fma(a.re, b.im, fma(-a.im, b.re, c.im))};
+    }
     __device__ static V mul(V a, V b) { return V{a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re}; }
     __device__ static V add(V a, V b) { return V{a.re + b.re, a.im + b.im}; }
     __device__ static bool is_zero(V a) { return a.re == T(0) && a.im == T(0); }
@@ -64,13 +70,14 @@ struct Ar<Cx<T>> {  // complex
     }
 };
 
-// Element a of S at (i, j) as op sees it: one on a unit diagonal, conjugated for a conjugate
-// transpose (the element is read only off a unit diagonal).
-template <typename V>
-__device__ __forceinline__ V mv_elem(const V* __restrict__ p, bool diag_one, int conj) {
-    if (diag_one) return Ar<V>::one();
-    const V a = *p;
-    return conj ? Ar<V>::conj(a) : a;
+// acc + op(S[i][j]) * xv for the element at p: one on a unit diagonal (the diagonal's value is not
+// used), conjugated for a conjugate transpose.
+template <typename V, bool CONJ>
+__device__ __forceinline__ V mv_step(const V* __restrict__ p, bool diag_one, V xv, V acc) {
+    // select the operand, then one FMA: a branch between an add and an FMA would have both
+    // evaluated, doubling the FP64 instructions
+    const V a = diag_one ? Ar<V>::one() : *p;
+    return CONJ ? Ar<V>::fmadd_conj(a, xv, acc) : Ar<V>::fmadd(a, xv, acc);
 }
 
 // y[i] = alpha * sum_j S[i][j] x[j] + beta * y[i] for i < rows: one warp per row, lanes stride over
@@ -79,10 +86,10 @@ __device__ __forceinline__ V mv_elem(const V* __restrict__ p, bool diag_one, int
 // (one FMA per 8-byte element, four per 16-byte complex element), not by HBM; a single
 // accumulator per lane keeps the registers low and the occupancy high, which measured faster than
 // unrolled partial sums or several warps per row.
-template <typename V>
+template <typename V, bool CONJ>
 __global__ void __launch_bounds__(256) mv_rows_kernel(int64_t rows, int64_t cols, V alpha, const V* __restrict__ S,
                                                       int64_t ld, const V* __restrict__ x, int64_t incx, V beta,
-                                                      V* __restrict__ y, int64_t incy, int tri, int unit, int conj) {
+                                                      V* __restrict__ y, int64_t incy, int tri, int unit) {
     using A = Ar<V>;
     const int lane = threadIdx.x & 31;
     const int64_t warps = (int64_t(gridDim.x) * blockDim.x) >> 5;
@@ -93,7 +100,7 @@ __global__ void __launch_bounds__(256) mv_rows_kernel(int64_t rows, int64_t cols
         const V* sp = S + i * ld + j0 + lane;
         const V* xp = x + (j0 + lane) * incx;
         for (int64_t j = j0 + lane; j < j1; j += 32, sp += 32, xp += xstep)
-            acc = A::fmadd(mv_elem(sp, unit && j == i, conj), *xp, acc);
+            acc = mv_step<V, CONJ>(sp, unit && j == i, *xp, acc);
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) acc = A::add(acc, A::shfl_xor(acc, o));
         if (lane == 0) {
@@ -106,11 +113,11 @@ __global__ void __launch_bounds__(256) mv_rows_kernel(int64_t rows, int64_t cols
 // Partial column sums: part[s][j] = sum_{i in slice s} S[i][j] x[i] for j < cols, threads over j
 // (coalesced), slice s of the rows per blockIdx.y; tri = 1 (lower) keeps i >= j, tri = 2 (upper)
 // i <= j.
-template <typename V>
+template <typename V, bool CONJ>
 __global__ void __launch_bounds__(256) mv_cols_partial_kernel(int64_t rows, int64_t cols, const V* __restrict__ S,
                                                               int64_t ld, const V* __restrict__ x, int64_t incx,
                                                               int64_t rows_per_slice, V* __restrict__ part, int tri,
-                                                              int unit, int conj) {
+                                                              int unit) {
     using A = Ar<V>;
     const int64_t j = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (j >= cols) return;
@@ -120,7 +127,7 @@ __global__ void __launch_bounds__(256) mv_cols_partial_kernel(int64_t rows, int6
     V acc = A::zero();
     const V* sp = S + i0 * ld + j;
     const V* xp = x + i0 * incx;
-    for (int64_t i = i0; i < i1; ++i, sp += ld, xp += incx) acc = A::fmadd(mv_elem(sp, unit && i == j, conj), *xp, acc);
+    for (int64_t i = i0; i < i1; ++i, sp += ld, xp += incx) acc = mv_step<V, CONJ>(sp, unit && i == j, *xp, acc);
     part[int64_t(blockIdx.y) * cols + j] = acc;
 }
 
@@ -148,38 +155,51 @@ __global__ void __launch_bounds__(256) mv_cols_reduce_kernel(int64_t cols, int s
 }
 
 // ---- complex planes --------------------------------------------------------------------------
+// The element-wise kernels below take rows on blockIdx.y (striding by gridDim.y) and columns on
+// threads (striding by the grid's x extent): no index division per element.
+
 // Interleaved complex rows x cols (pitch ld, in complex elements) -> dense real planes re, im.
 template <typename T>
 __global__ void split_complex_kernel(int64_t rows, int64_t cols, const T* __restrict__ Z, int64_t ld,
                                      T* __restrict__ re, T* __restrict__ im) {
-    const int64_t total = rows * cols;
-    for (int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; e < total; e += int64_t(gridDim.x) * blockDim.x) {
-        const int64_t r = e / cols, c = e - r * cols;
-        const T* z = Z + 2 * (r * ld + c);
-        re[e] = z[0];
-        im[e] = z[1];
-    }
+    for (int64_t r = blockIdx.y; r < rows; r += gridDim.y)
+        for (int64_t c = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; c < cols; c += int64_t(gridDim.x) * blockDim.x) {
+            const T* z = Z + 2 * (r * ld + c);
+            re[r * cols + c] = z[0];
+            im[r * cols + c] = z[1];
+        }
 }
 
-// C (interleaved, pitch ldc) = alpha * (Pr + i Pi) + beta * C for rows x cols (P dense).
+// C (interleaved, pitch ldc) = alpha * (Pr + i Pi) + beta * C for rows x cols (P dense).  With
+// alpha = 1 and beta = 0 (what Blaze passes for C = A * B) the planes are only interleaved: no FP64
+// arithmetic, which on GB300 would bound this kernel by the FP64 pipe.
 template <typename T>
 __global__ void complex_epilogue_kernel(int64_t rows, int64_t cols, const T* __restrict__ Pr, const T* __restrict__ Pi,
                                        T ar, T ai, T br, T bi, T* __restrict__ C, int64_t ldc) {
-    const int64_t total = rows * cols;
     const bool beta0 = (br == T(0) && bi == T(0));
-    for (int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; e < total; e += int64_t(gridDim.x) * blockDim.x) {
-        const int64_t r = e / cols, c = e - r * cols;
-        T* z = C + 2 * (r * ldc + c);
-        const T pr = Pr[e], pi = Pi[e];
-        T cr = ar * pr - ai * pi, ci = ar * pi + ai * pr;
-        if (!beta0) {
-            const T zr = z[0], zi = z[1];
-            cr += br * zr - bi * zi;
-            ci += br * zi + bi * zr;
-        }
-        z[0] = cr;
-        z[1] = ci;
+    const int64_t cstep = int64_t(gridDim.x) * blockDim.x, c0 = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (beta0 && ar == T(1) && ai == T(0)) {  // the branch stays outside the loops: a copy
+        for (int64_t r = blockIdx.y; r < rows; r += gridDim.y)
+            for (int64_t c = c0; c < cols; c += cstep) {
+                T* z = C + 2 * (r * ldc + c);
+                z[0] = Pr[r * cols + c];
+                z[1] = Pi[r * cols + c];
+            }
+        return;
     }
+    for (int64_t r = blockIdx.y; r < rows; r += gridDim.y)
+        for (int64_t c = c0; c < cols; c += cstep) {
+            T* z = C + 2 * (r * ldc + c);
+            const T pr = Pr[r * cols + c], pi = Pi[r * cols + c];
+            T cr = ar * pr - ai * pi, ci = ar * pi + ai * pr;
+            if (!beta0) {
+                const T zr = z[0], zi = z[1];
+                cr += br * zr - bi * zi;
+                ci += br * zi + bi * zr;
+            }
+            z[0] = cr;
+            z[1] = ci;
+        }
 }
 
 // ---- triangle --------------------------------------------------------------------------------
@@ -188,12 +208,19 @@ __global__ void complex_epilogue_kernel(int64_t rows, int64_t cols, const T* __r
 template <typename V>
 __global__ void triangle_kernel(int64_t n, const V* __restrict__ A, int64_t lda, int lower, int unit,
                                 V* __restrict__ out) {
-    const int64_t total = n * n;
-    for (int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; e < total; e += int64_t(gridDim.x) * blockDim.x) {
-        const int64_t i = e / n, j = e - i * n;
-        const bool in = lower ? (j <= i) : (j >= i);
-        out[e] = !in ? Ar<V>::zero() : ((unit && i == j) ? Ar<V>::one() : A[i * lda + j]);
-    }
+    for (int64_t i = blockIdx.y; i < n; i += gridDim.y)
+        for (int64_t j = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; j < n; j += int64_t(gridDim.x) * blockDim.x) {
+            const bool in = lower ? (j <= i) : (j >= i);
+            out[i * n + j] = !in ? Ar<V>::zero() : ((unit && i == j) ? Ar<V>::one() : A[i * lda + j]);
+        }
+}
+
+// Grid of the element-wise kernels: 256-thread blocks over the columns, rows on y, about 16 blocks
+// per SM in all (each block strides over many rows).
+dim3 grid_2d(int64_t rows, int64_t cols) {
+    const int64_t x = std::max<int64_t>(1, std::min<int64_t>((cols + 255) / 256, 64));
+    const int64_t y = std::max<int64_t>(1, std::min<int64_t>(rows, int64_t(runtime().num_sms) * 16 / x));
+    return dim3(unsigned(x), unsigned(y));
 }
 
 // Blocks for `work` threads of `threads` per block, at most `per_sm` blocks per SM (grid-stride
@@ -223,16 +250,19 @@ cudaError_t launch_mv(const MvForm& f, int64_t rows, int64_t cols, const T* alph
     const V* vS = reinterpret_cast<const V*>(S);
     const V* vx = reinterpret_cast<const V*>(x);
     V* vy = reinterpret_cast<V*>(y);
-    const int tri = f.tri, unit = f.unit ? 1 : 0, conj = f.conj ? 1 : 0;
+    const int tri = f.tri, unit = f.unit ? 1 : 0;
+    const bool conj = CPLX && f.conj;
     if (!f.cols_form) {
-        mv_rows_kernel<V><<<grid_for(rows * 32, 256, r.num_sms, 8), 256, 0, st>>>(rows, cols, al, vS, ld, vx, incx, be,
-                                                                                  vy, incy, tri, unit, conj);
+        auto kern = conj ? mv_rows_kernel<V, CPLX> : mv_rows_kernel<V, false>;
+        kern<<<grid_for(rows * 32, 256, r.num_sms, 8), 256, 0, st>>>(rows, cols, al, vS, ld, vx, incx, be, vy, incy, tri,
+                                                                      unit);
         count_launches(1);
     } else {
         V* vp = reinterpret_cast<V*>(part);
         const int64_t per = (rows + slices - 1) / slices;
-        mv_cols_partial_kernel<V><<<dim3(unsigned((cols + 255) / 256), unsigned(slices)), 256, 0, st>>>(
-            rows, cols, vS, ld, vx, incx, per, vp, tri, unit, conj);
+        auto kern = conj ? mv_cols_partial_kernel<V, CPLX> : mv_cols_partial_kernel<V, false>;
+        kern<<<dim3(unsigned((cols + 255) / 256), unsigned(slices)), 256, 0, st>>>(rows, cols, vS, ld, vx, incx, per, vp,
+                                                                                  tri, unit);
         mv_cols_reduce_kernel<V><<<unsigned((cols + 31) / 32), 256, 0, st>>>(cols, slices, vp, al, be, vy, incy);
         count_launches(2);
     }
@@ -241,7 +271,7 @@ cudaError_t launch_mv(const MvForm& f, int64_t rows, int64_t cols, const T* alph
 
 template <typename T>
 cudaError_t launch_split_complex(int64_t rows, int64_t cols, const T* Z, int64_t ld, T* re, T* im, cudaStream_t st) {
-    split_complex_kernel<T><<<grid_for(rows * cols, 256, runtime().num_sms), 256, 0, st>>>(rows, cols, Z, ld, re, im);
+    split_complex_kernel<T><<<grid_2d(rows, cols), 256, 0, st>>>(rows, cols, Z, ld, re, im);
     count_launches(1);
     return cudaGetLastError();
 }
@@ -249,8 +279,7 @@ cudaError_t launch_split_complex(int64_t rows, int64_t cols, const T* Z, int64_t
 template <typename T>
 cudaError_t launch_complex_epilogue(int64_t rows, int64_t cols, const T* Pr, const T* Pi, T ar, T ai, T br, T bi, T* C,
                                    int64_t ldc, cudaStream_t st) {
-    complex_epilogue_kernel<T><<<grid_for(rows * cols, 256, runtime().num_sms), 256, 0, st>>>(rows, cols, Pr, Pi, ar,
-                                                                                             ai, br, bi, C, ldc);
+    complex_epilogue_kernel<T><<<grid_2d(rows, cols), 256, 0, st>>>(rows, cols, Pr, Pi, ar, ai, br, bi, C, ldc);
     count_launches(1);
     return cudaGetLastError();
 }
@@ -258,8 +287,8 @@ cudaError_t launch_complex_epilogue(int64_t rows, int64_t cols, const T* Pr, con
 template <typename T, bool CPLX>
 cudaError_t launch_triangle(int64_t n, const T* A, int64_t lda, bool lower, bool unit, T* out, cudaStream_t st) {
     using V = typename std::conditional<CPLX, Cx<T>, T>::type;
-    triangle_kernel<V><<<grid_for(n * n, 256, runtime().num_sms), 256, 0, st>>>(
-        n, reinterpret_cast<const V*>(A), lda, lower ? 1 : 0, unit ? 1 : 0, reinterpret_cast<V*>(out));
+    triangle_kernel<V><<<grid_2d(n, n), 256, 0, st>>>(n, reinterpret_cast<const V*>(A), lda, lower ? 1 : 0,
+                                                        unit ? 1 : 0, reinterpret_cast<V*>(out));
     count_launches(1);
     return cudaGetLastError();
 }
