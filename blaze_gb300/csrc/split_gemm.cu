@@ -324,10 +324,51 @@ __global__ void __launch_bounds__(256, 4) stats_tile_kernel(const OperandPair op
     stats_rows(op.X[w], op.R[w], K, op.sr[w], op.sp[w], op.acc[w], by);
 }
 
-__global__ void stats_finalize_pair_kernel(const OperandPair op, int64_t K, unsigned xb0) {
+// Per-block summary of the row statistics of one operand side, for split_info_kernel: Inf/NaN
+// flag, largest exponent E of the rows with q > 0 (kNoRows when none), largest q (its bit pattern:
+// non-negative doubles order like integers), s = sum 2^(2(e - E)) and nrm = sum 2^(2(e - E)) q.
+constexpr int kNoRows = -100000;
+struct RowPartial {
+    int bad, E;
+    long long Qbits;
+    double s, nrm;
+};
+
+__device__ double block_sum(double v, double* red);
+__device__ long long block_max_ll(long long v, long long* red);
+__device__ int block_max_int(int v, int* red);
+__device__ __forceinline__ double pow2i(int x);
+
+// blockIdx.x < xb0: rows of A, else columns of B (256 a block); with `part`, each block also
+// writes its RowPartial (part[blockIdx.x]).
+__global__ void __launch_bounds__(256) stats_finalize_pair_kernel(const OperandPair op, int64_t K, unsigned xb0,
+                                                                  RowPartial* __restrict__ part) {
     const int w = blockIdx.x < xb0 ? 0 : 1;
     const int64_t r = int64_t(w ? blockIdx.x - xb0 : blockIdx.x) * blockDim.x + threadIdx.x;
     stats_finalize_row(op.X[w], op.R[w], K, op.sr[w], op.sp[w], op.acc[w], op.rexp[w], op.rsq[w], r);
+    if (part == nullptr) return;  // uniform over the launch
+    __shared__ double redd[32];
+    __shared__ int redi[32];
+    int e = kNoRows, bad = 0;
+    double q = 0.0;
+    if (r < op.R[w]) {
+        e = op.rexp[w][r];
+        q = op.rsq[w][r];
+        if (e == kNonFinite) {
+            bad = 1;
+            e = kNoRows;
+            q = 0.0;
+        }
+    }
+    const long long qb = __double_as_longlong(q);
+    RowPartial pr;
+    pr.bad = block_max_int(bad, redi);
+    pr.E = block_max_int(qb > 0 ? e : kNoRows, redi);
+    pr.Qbits = block_max_ll(qb, reinterpret_cast<long long*>(redd));
+    const double wgt = (qb > 0 && pr.E != kNoRows) ? pow2i(2 * (e - pr.E)) : 0.0;
+    pr.s = block_sum(wgt, redd);
+    pr.nrm = block_sum(wgt * q, redd);
+    if (threadIdx.x == 0) part[blockIdx.x] = pr;
 }
 
 // One block: norms, scale norms, slice count and bound.  Sums are formed relative to the largest
@@ -402,52 +443,46 @@ __device__ __forceinline__ double pow2i(int x) {
     return x < -1022 ? 0.0 : __longlong_as_double((long long)(x + 1023) << 52);
 }
 
-__global__ void __launch_bounds__(1024) split_info_kernel(const int* __restrict__ eA, const double* __restrict__ qA, int64_t m,
-                                  const int* __restrict__ eB, const double* __restrict__ qB, int64_t n, int64_t k,
-                                  int mode, int fixed_slices, int cap_planes, double target, SplitInfo* info) {
+__global__ void __launch_bounds__(1024) split_info_kernel(const RowPartial* __restrict__ part, int nA, int nB, int64_t k,
+                                                           int mode, int fixed_slices, int cap_planes, double target,
+                                                           SplitInfo* info) {
     __shared__ double redd[32];
     __shared__ int redi[32];
-    // one pass: Inf/NaN flag, largest exponents, largest row / column sums of squares relative to
-    // 2^(2e) (non-negative doubles: their bit patterns order like integers)
-    int bad = 0, EA = -100000, EB = -100000;
+    // the per-block partials of A (the first nA) and B: Inf/NaN flag, largest exponents, largest
+    // row / column sums of squares relative to 2^(2e)
+    int bad = 0, EA = kNoRows, EB = kNoRows;
     long long QAb = 0, QBb = 0;
-    for (int64_t i = threadIdx.x; i < m; i += blockDim.x) {
-        const int e = eA[i];
-        if (e == kNonFinite) {
-            bad = 1;
-            continue;
+    for (int i = threadIdx.x; i < nA + nB; i += blockDim.x) {
+        const RowPartial p = part[i];
+        bad |= p.bad;
+        if (i < nA) {
+            EA = max(EA, p.E);
+            QAb = max(QAb, p.Qbits);
+        } else {
+            EB = max(EB, p.E);
+            QBb = max(QBb, p.Qbits);
         }
-        const long long qb = __double_as_longlong(qA[i]);
-        if (qb > 0) EA = max(EA, e);
-        QAb = max(QAb, qb);
-    }
-    for (int64_t j = threadIdx.x; j < n; j += blockDim.x) {
-        const int e = eB[j];
-        if (e == kNonFinite) {
-            bad = 1;
-            continue;
-        }
-        const long long qb = __double_as_longlong(qB[j]);
-        if (qb > 0) EB = max(EB, e);
-        QBb = max(QBb, qb);
     }
     bad = block_max_int(bad, redi);
     EA = block_max_int(EA, redi);
     EB = block_max_int(EB, redi);
     const double QA = __longlong_as_double(block_max_ll(QAb, reinterpret_cast<long long*>(redd)));
     const double QB = __longlong_as_double(block_max_ll(QBb, reinterpret_cast<long long*>(redd)));
+    // the sums relative to the largest exponent: each block's relative to its own, rescaled by an
+    // exact power of two
     double sa = 0, na = 0, sb = 0, nb = 0;
-    for (int64_t i = threadIdx.x; i < m; i += blockDim.x) {
-        if (eA[i] == kNonFinite || qA[i] <= 0.0) continue;
-        const double w = pow2i(2 * (eA[i] - EA));
-        sa += w;
-        na += w * qA[i];
-    }
-    for (int64_t j = threadIdx.x; j < n; j += blockDim.x) {
-        if (eB[j] == kNonFinite || qB[j] <= 0.0) continue;
-        const double w = pow2i(2 * (eB[j] - EB));
-        sb += w;
-        nb += w * qB[j];
+    for (int i = threadIdx.x; i < nA + nB; i += blockDim.x) {
+        const RowPartial p = part[i];
+        if (p.E == kNoRows) continue;
+        if (i < nA) {
+            const double w = pow2i(2 * (p.E - EA));
+            sa += w * p.s;
+            na += w * p.nrm;
+        } else {
+            const double w = pow2i(2 * (p.E - EB));
+            sb += w * p.s;
+            nb += w * p.nrm;
+        }
     }
     sa = block_sum(sa, redd);
     na = block_sum(na, redd);
@@ -1594,7 +1629,8 @@ void device_product_slot_needs(const Gemm& g, const SplitRequest& req, size_t ne
     need[kSlotLevels] = rounded(size_t(G.nseg) * G.max_levels * size_t(G.mpad) * size_t(G.npad) * 4);
     const int64_t off_sq = round_up((g.m + g.n) * int64_t(sizeof(int)), 256);
     const int64_t off_info = round_up(off_sq + (g.m + g.n) * int64_t(sizeof(double)), 256);
-    need[kSlotScaleA] = rounded(size_t(off_info) + ((sizeof(SplitInfo) + 255) / 256) * 256);
+    const size_t off_part = size_t(off_info) + ((sizeof(SplitInfo) + 255) / 256) * 256;
+    need[kSlotScaleA] = rounded(off_part + size_t((g.m + 255) / 256 + (g.n + 255) / 256) * sizeof(RowPartial));
     need[kSlotScaleB] = rounded(size_t(g.m + g.n) * sizeof(RowAcc));
 }
 
@@ -1636,7 +1672,9 @@ int device_product(const Gemm& g_in, const SplitRequest& req, const LaunchCtl& c
     // statistics block: exponents (int), relative sums of squares (double), SplitInfo
     const int64_t off_sq = round_up((m + n) * int64_t(sizeof(int)), 256);
     const int64_t off_info = round_up(off_sq + (m + n) * int64_t(sizeof(double)), 256);
-    const size_t stat_bytes = size_t(off_info) + ((sizeof(SplitInfo) + 255) / 256) * 256;
+    const int64_t off_part = off_info + int64_t((sizeof(SplitInfo) + 255) / 256) * 256;
+    const unsigned xb0 = unsigned((m + 255) / 256), xb1 = unsigned((n + 255) / 256);
+    const size_t stat_bytes = size_t(off_part) + size_t(xb0 + xb1) * sizeof(RowPartial);
     auto* stats = static_cast<uint8_t*>(ws.get(kSlotScaleA, stat_bytes, err));
     if (!pa || !pb || !lv || !stats) return GB300_ERR_NO_MEMORY;
     int* eA = reinterpret_cast<int*>(stats);
@@ -1644,6 +1682,7 @@ int device_product(const Gemm& g_in, const SplitRequest& req, const LaunchCtl& c
     double* sqA = reinterpret_cast<double*>(stats + off_sq);
     double* sqB = sqA + m;
     auto* info = reinterpret_cast<SplitInfo*>(stats + off_info);
+    auto* part = reinterpret_cast<RowPartial*>(stats + off_part);
 
     // operand strides of the logical R x K views
     const int64_t a_sr = g.ta ? 1 : g.lda, a_sp = g.ta ? g.lda : 1;
@@ -1668,11 +1707,10 @@ int device_product(const Gemm& g_in, const SplitRequest& req, const LaunchCtl& c
     {
         dim3 grid(unsigned(((k + 63) / 64 + TILE_KT - 1) / TILE_KT), unsigned((m + 31) / 32 + (n + 31) / 32));
         stats_tile_kernel<<<grid, 256, 0, st>>>(op, k);
-        const unsigned xb0 = unsigned((m + 255) / 256);
-        stats_finalize_pair_kernel<<<xb0 + unsigned((n + 255) / 256), 256, 0, st>>>(op, k, xb0);
+        stats_finalize_pair_kernel<<<xb0 + xb1, 256, 0, st>>>(op, k, xb0, part);
     }
     const double target = req.target_error > 0 ? req.target_error : double(k) * 0x1p-53;
-    split_info_kernel<<<1, 1024, 0, st>>>(eA, sqA, m, eB, sqB, n, k, mode, req.slices > 0 ? max_planes : 0,
+    split_info_kernel<<<1, 1024, 0, st>>>(part, int(xb0), int(xb1), k, mode, req.slices > 0 ? max_planes : 0,
                                          max_planes, target, info);
     if (cudaError_t le = cudaGetLastError(); le != cudaSuccess) {
         if (err) *err = std::string("split pre-pass launch: ") + cudaGetErrorString(le);
@@ -1906,7 +1944,7 @@ int device_product_host_panels(const Gemm& g, const SplitRequest& req, const Lau
         o.yb0 = unsigned((mi + 31) / 32);
         stats_tile_kernel<<<dim3(ktiles, o.yb0), 256, 0, st>>>(o, k);
         const unsigned xb0 = unsigned((mi + 255) / 256);
-        stats_finalize_pair_kernel<<<xb0, 256, 0, st>>>(o, k, xb0);
+        stats_finalize_pair_kernel<<<xb0, 256, 0, st>>>(o, k, xb0, nullptr);
         split_side_kernel<<<1, 1024, 0, st>>>(eA + r0, sqA + r0, mi, k, max_planes, target, info_at(i));
         o.yb0 = unsigned(mpad / 32);
         slice_kernel<kCrt><<<dim3(stiles, o.yb0), 256, 0, st>>>(o, k, info_at(i), kpad);
@@ -1925,7 +1963,7 @@ int device_product_host_panels(const Gemm& g, const SplitRequest& req, const Lau
         o.rpad[1] = Nq;
         o.yb0 = 0;
         stats_tile_kernel<<<dim3(ktiles, unsigned((nj + 31) / 32)), 256, 0, st>>>(o, k);
-        stats_finalize_pair_kernel<<<unsigned((nj + 255) / 256), 256, 0, st>>>(o, k, 0u);
+        stats_finalize_pair_kernel<<<unsigned((nj + 255) / 256), 256, 0, st>>>(o, k, 0u, nullptr);
         split_side_kernel<<<1, 1024, 0, st>>>(eB + c0, sqB + c0, nj, k, max_planes, target, info_at(P + j));
         slice_kernel<kCrt><<<dim3(stiles, unsigned(Nq / 32)), 256, 0, st>>>(o, k, info_at(P + j), kpad);
         count_launches(4);
