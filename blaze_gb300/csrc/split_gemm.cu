@@ -489,19 +489,44 @@ __global__ void __launch_bounds__(1024) split_info_kernel(const RowPartial* __re
     sb = block_sum(sb, redd);
     nb = block_sum(nb, redd);
     if (threadIdx.x < 32) {  // warp 0 plans; lane 0 writes
+        const int lane = threadIdx.x;
+        // Each FP64 function below runs once for the warp with a different argument in each lane
+        // (the cost of one evaluation, same operations as one at a time): lanes 0-3 the norms, 4-5
+        // sqrt(k s / n), 6-7 sqrt(Q (1 + 2^-10)), 8 sqrt(k), 9-10 sqrt(s / n).
+        double num = 0.0, den = 1.0;
+        switch (lane) {
+            case 0: num = na; break;
+            case 1: num = nb; break;
+            case 2: num = sa; break;
+            case 3: num = sb; break;
+            case 4: num = double(k) * sa; den = na > 0 ? na : 1.0; break;
+            case 5: num = double(k) * sb; den = nb > 0 ? nb : 1.0; break;
+            case 6: num = QA * (1.0 + 0x1p-10); break;
+            case 7: num = QB * (1.0 + 0x1p-10); break;
+            case 8: num = double(k); break;
+            case 9: num = sa; den = na > 0 ? na : 1.0; break;
+            case 10: num = sb; den = nb > 0 ? nb : 1.0; break;
+            default: break;
+        }
+        const double root = sqrt(num / den);
+        const double scaled = ldexp(root, (lane == 0 || lane == 2) ? EA : EB);  // lanes 0-3
+        auto from = [&](double v, int l) { return __shfl_sync(0xffffffffu, v, l); };
+        const double nA_ = from(scaled, 0), nB_ = from(scaled, 1), sA_ = from(scaled, 2), sB_ = from(scaled, 3);
+        const double rAk = from(root, 4), rBk = from(root, 5), sqa = from(root, 6), sqb = from(root, 7);
+        const double sqk = from(root, 8), ra = from(root, 9), rb = from(root, 10);
         SplitInfo r;
         r.nonfinite = bad;
-        r.normA = (na > 0) ? ldexp(sqrt(na), EA) : 0.0;
-        r.normB = (nb > 0) ? ldexp(sqrt(nb), EB) : 0.0;
-        r.scaleA = (sa > 0) ? ldexp(sqrt(sa), EA) : 0.0;
-        r.scaleB = (sb > 0) ? ldexp(sqrt(sb), EB) : 0.0;
-        const double rho = (na > 0 && nb > 0) ? sqrt(sa / na) * sqrt(sb / nb) : 0.0;
+        r.normA = (na > 0) ? nA_ : 0.0;
+        r.normB = (nb > 0) ? nB_ : 0.0;
+        r.scaleA = (sa > 0) ? sA_ : 0.0;
+        r.scaleB = (sb > 0) ? sB_ : 0.0;
+        const double rho = (na > 0 && nb > 0) ? ra * rb : 0.0;
         if (mode == kCrt) {
             // operands rounded to beta-bit integers: |dA_ip| <= 2^(e_i-beta-1), so
             // ||dC||_F/(||A|| ||B||) <= 2^(-beta-1)(rA + rB) + 2^(-2beta-2) rA rB + 2^-52 with
             // rA = sqrt(k) ||2^e|| / ||A|| (and 2^-52 for the final conversion and the alpha scaling)
-            const double rA = (na > 0) ? sqrt(double(k) * sa / na) : 0.0;
-            const double rB = (nb > 0) ? sqrt(double(k) * sb / nb) : 0.0;
+            const double rA = (na > 0) ? rAk : 0.0;
+            const double rB = (nb > 0) ? rBk : 0.0;
             auto bnd = [&](int b) {
                 return pow2i(-b - 1) * (rA + rB) + pow2i(-2 * b - 2) * rA * rB + pow2i(-52);
             };
@@ -513,17 +538,20 @@ __global__ void __launch_bounds__(1024) split_info_kernel(const RowPartial* __re
             // |T| <= (2^beta sqrt(Q_A) + sqrt(k)/2)(2^beta sqrt(Q_B) + sqrt(k)/2).  The moduli's
             // product P must exceed 2.125 |T| (symmetric residues, with room for the FP32 quotient
             // estimate of the reconstruction); Q carries a 2^-10 allowance for its own rounding.
-            const double hk = 0.5 * sqrt(double(k)), sqa = sqrt(QA * (1.0 + 0x1p-10)), sqb = sqrt(QB * (1.0 + 0x1p-10));
+            const double hk = 0.5 * sqk;
             auto need = [&](int b) {
                 const double x = ldexp(sqa, b) + hk, y = ldexp(sqb, b) + hk;
                 return 1.0875 + log2(x) + log2(y);
             };
+            // lanes 0-1: the two factors of need(beta); lanes 2-3: log2 sqa and log2 sqb
+            const double lg = log2(ldexp((lane & 1) ? sqb : sqa, lane < 2 ? beta : 0) + (lane < 2 ? hk : 0.0));
+            const double lg0 = from(lg, 0), lg1 = from(lg, 1), lsqa = from(lg, 2), lsqb = from(lg, 3);
             double have = 0.0;
             // a fixed count is used as given (at least two); otherwise the fewest that carry the
             // target, within the planes the host sized for
             int N = 0;
             const int nfix = fixed_slices > 0 ? (fixed_slices < 2 ? 2 : fixed_slices) : 0;
-            const double need0 = need(beta);
+            const double need0 = 1.0875 + lg0 + lg1;  // need(beta)
             while (nfix ? N < nfix : (N < 2 || (N < cap_planes && have < need0))) {
                 have += c_mod_log2[N];
                 ++N;
@@ -533,7 +561,7 @@ __global__ void __launch_bounds__(1024) split_info_kernel(const RowPartial* __re
             // in (-60, b0] with need(b) <= have, -60 when none
             int bhi = 55;
             if (sqa > 0 && sqb > 0) {
-                const int b0 = int(floor((have - 1.0875 - log2(sqa) - log2(sqb)) / 2.0));
+                const int b0 = int(floor((have - 1.0875 - lsqa - lsqb) / 2.0));
                 bhi = b0 < 55 ? (b0 > -60 ? b0 : -60) : 55;
             }
             beta = warp_last_true(-59, bhi, [&](int b) { return need(b) <= have; });
@@ -541,8 +569,10 @@ __global__ void __launch_bounds__(1024) split_info_kernel(const RowPartial* __re
             r.beta = beta;
             r.beta_b = beta;
             r.qmaxB = QB;
-            // too few moduli for even the coarsest rounding: no bound
-            r.bound = need(beta) > have ? __longlong_as_double(0x7ff0000000000000ll) : bnd(beta);
+            // a beta the search found has need(beta) <= have; -60 (none found) was not tested.  Too
+            // few moduli for even the coarsest rounding: no bound
+            const bool fits = beta >= -59 || need(beta) <= have;
+            r.bound = fits ? bnd(beta) : __longlong_as_double(0x7ff0000000000000ll);
         } else if (mode == kExact) {
             int S = fixed_slices;
             if (S <= 0) {
