@@ -65,7 +65,11 @@ struct ServeSlot {
     cudaStream_t stream = nullptr;
     Workspace ws;
     ServeRequest* cur = nullptr;
+    // page-locked landing place of the running request's status word and accuracy record, copied
+    // behind the product on the slot's stream (read once its completion event has fired)
+    uint8_t* host = nullptr;
 };
+constexpr size_t kHostStatus = 0, kHostInfo = 64, kHostBytes = 512;
 
 }  // namespace
 
@@ -152,6 +156,9 @@ class Server {
         r->res.slices = res.slices;
         r->res.error_bound = res.error_bound;
         r->info_dev = res.info_dev;
+        cudaMemcpyAsync(sl.host + kHostStatus, sl.ws.d_status, sizeof(int), cudaMemcpyDeviceToHost, sl.stream);
+        if (r->info_dev && split_info_bytes() <= kHostBytes - kHostInfo)
+            cudaMemcpyAsync(sl.host + kHostInfo, r->info_dev, split_info_bytes(), cudaMemcpyDeviceToHost, sl.stream);
         cudaEventRecord(r->done, sl.stream);
         peak_bytes = std::max(peak_bytes, bytes_held());
         if (st != GB300_OK) r->res.status = st;
@@ -161,15 +168,14 @@ class Server {
         ServeRequest* r = sl.cur;
         r->t_end = Clock::now();
         int status = 0;
-        cudaMemcpy(&status, sl.ws.d_status, sizeof(int), cudaMemcpyDeviceToHost);
+        std::memcpy(&status, sl.host + kHostStatus, sizeof(int));
         if (r->res.status == GB300_OK && status != 0) r->res.status = GB300_ERR_DEVICE_TIMEOUT;
-        if (r->info_dev) {
+        if (r->info_dev && split_info_bytes() <= kHostBytes - kHostInfo) {
             int sl_ = 0;
             double bd = 0;
-            if (split_read_info(r->info_dev, &sl_, &bd)) {
-                r->res.slices = sl_;
-                r->res.error_bound = bd;
-            }
+            split_decode_info(sl.host + kHostInfo, &sl_, &bd);
+            r->res.slices = sl_;
+            r->res.error_bound = bd;
         }
         r->res.queue_ms = ms_between(r->t_submit, r->t_start);
         r->res.latency_ms = ms_between(r->t_submit, r->t_end);
@@ -264,6 +270,7 @@ int gb300_server_create(const gb300_server_config* cfg, gb300_server** out) {
     for (auto& sl : s->slots) {
         cudaError_t e = cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking);
         if (e == cudaSuccess) e = cudaMalloc(&sl.ws.d_status, 64);
+        if (e == cudaSuccess) e = cudaHostAlloc(reinterpret_cast<void**>(&sl.host), gb::kHostBytes, cudaHostAllocDefault);
         if (e != cudaSuccess) {
             gb::set_error(GB300_ERR_CUDA, std::string("gb300_server_create: ") + cudaGetErrorString(e));
             delete s;
@@ -444,6 +451,7 @@ void gb300_server_destroy(gb300_server* srv) {
         if (sl.stream) cudaStreamSynchronize(sl.stream);
         sl.ws.release();
         if (sl.ws.d_status) cudaFree(sl.ws.d_status);
+        if (sl.host) cudaFreeHost(sl.host);
         if (sl.stream) cudaStreamDestroy(sl.stream);
     }
     for (auto& kv : s->reqs) {

@@ -26,6 +26,10 @@ struct SplitResult {
 // Read the slice count and the a-priori bound back from the device copy (after the stream has
 // finished the product).
 bool split_read_info(const void* info_dev, int* slices, double* bound);
+// Size of the device record split_read_info reads, and its decoding from a host copy (the serving
+// loop copies it back asynchronously behind the product).
+size_t split_info_bytes();
+void split_decode_info(const void* info_host, int* slices, double* bound);
 
 struct Workspace;
 

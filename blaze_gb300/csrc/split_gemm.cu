@@ -50,6 +50,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstring>
 #include <cmath>
 #include <string>
 #include <type_traits>
@@ -1549,6 +1550,15 @@ bool split_read_info(const void* info_dev, int* slices, double* bound) {
     *slices = h.slices;
     *bound = h.bound;
     return true;
+}
+
+size_t split_info_bytes() { return sizeof(SplitInfo); }
+
+void split_decode_info(const void* info_host, int* slices, double* bound) {
+    SplitInfo h;
+    std::memcpy(&h, info_host, sizeof(h));
+    *slices = h.slices;
+    *bound = h.bound;
 }
 
 // ---- host orchestration ------------------------------------------------------------------------
