@@ -104,6 +104,7 @@ template <typename T>
 int gemm_entry(int order, int transA, int transB, int64_t m, int64_t n, int64_t k, T alpha, const T* A, int64_t lda,
               const T* B, int64_t ldb, T beta, T* C, int64_t ldc, gb300_gemm_opts* opts, const char* routine) {
     const bool is_double = sizeof(T) == 8;
+    const CallTrace trace(routine, m, n, k);
     auto fail = [&](int st, const std::string& msg) {
         set_error(st, std::string(routine) + ": " + msg);
         return st;

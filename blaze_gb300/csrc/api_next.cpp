@@ -163,6 +163,7 @@ bool scalar_is(const T* v, T re) {
 template <typename T, bool CPLX>
 int gemv_any(int order, int transA, int64_t m, int64_t n, const T* alpha, const T* A, int64_t lda, const T* x,
              int64_t incx, const T* beta, T* y, int64_t incy, const char* routine) {
+    const CallTrace trace(routine, m, n, 1);
     auto fail = [&](int st, const std::string& msg) {
         set_error(st, std::string(routine) + ": " + msg);
         return st;
@@ -250,6 +251,7 @@ int cgemv_entry(int order, int transA, int64_t m, int64_t n, const T* alpha, con
 template <typename T, bool CPLX>
 int trmv_entry(int order, int uplo, int transA, int diag, int64_t n, const T* A, int64_t lda, T* x, int64_t incx,
                const char* routine) {
+    const CallTrace trace(routine, n, n, 1);
     auto fail = [&](int st, const std::string& msg) {
         set_error(st, std::string(routine) + ": " + msg);
         return st;
@@ -366,6 +368,7 @@ int complex_product(int64_t M, int64_t N, int64_t k, bool ta, bool tb, bool ca, 
 template <typename T>
 int cgemm_entry(int order, int transA, int transB, int64_t m, int64_t n, int64_t k, const T* alpha, const T* A,
                 int64_t lda, const T* B, int64_t ldb, const T* beta, T* C, int64_t ldc, const char* routine) {
+    const CallTrace trace(routine, m, n, k);
     auto fail = [&](int st, const std::string& msg) {
         set_error(st, std::string(routine) + ": " + msg);
         return st;
@@ -433,6 +436,7 @@ int cgemm_entry(int order, int transA, int transB, int64_t m, int64_t n, int64_t
 template <typename T>
 int trmm_entry(int order, int side, int uplo, int transA, int diag, int64_t m, int64_t n, T alpha, const T* A,
                int64_t lda, T* B, int64_t ldb, const char* routine) {
+    const CallTrace trace(routine, m, n, side == CblasLeft ? m : n);
     auto fail = [&](int st, const std::string& msg) {
         set_error(st, std::string(routine) + ": " + msg);
         return st;
@@ -506,6 +510,7 @@ int trmm_entry(int order, int side, int uplo, int transA, int diag, int64_t m, i
 template <typename T>
 int ctrmm_entry(int order, int side, int uplo, int transA, int diag, int64_t m, int64_t n, const T* alpha, const T* A,
                 int64_t lda, T* B, int64_t ldb, const char* routine) {
+    const CallTrace trace(routine, m, n, side == CblasLeft ? m : n);
     auto fail = [&](int st, const std::string& msg) {
         set_error(st, std::string(routine) + ": " + msg);
         return st;

@@ -1,9 +1,14 @@
 // runtime.cpp — device state, tensor-map encoding, device buffer pool and error bookkeeping.
 #include "runtime.h"
 
+#include <nvtx3/nvToolsExt.h>
+
+#include <chrono>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <functional>
+#include <thread>
 
 #include "../../include/gb300_blas.h"
 #include "gb300_internal.h"
@@ -43,6 +48,39 @@ EncodeTiledFn encode_fn() {
 Runtime& runtime() {
     static Runtime* r = new Runtime();  // never destroyed: safe at process exit
     return *r;
+}
+
+namespace {
+bool trace_enabled() {
+    static const bool on = [] {
+        const char* v = std::getenv("GB300_BLAS_TRACE");
+        return v && *v && *v != '0';
+    }();
+    return on;
+}
+
+double wall_ms() {
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+unsigned long long thread_tag() { return (unsigned long long)std::hash<std::thread::id>()(std::this_thread::get_id()); }
+}  // namespace
+
+CallTrace::CallTrace(const char* routine, int64_t m, int64_t n, int64_t k) : routine_(routine) {
+    nvtxRangePushA(routine);
+    trace_ = trace_enabled();
+    if (trace_) {
+        std::fprintf(stderr, "libgb300blas: enter %s m=%lld n=%lld k=%lld thread=%llx\n", routine, (long long)m,
+                     (long long)n, (long long)k, thread_tag());
+        t0_ = wall_ms();
+    }
+}
+
+CallTrace::~CallTrace() {
+    if (trace_)
+        std::fprintf(stderr, "libgb300blas: leave %s status=%d ms=%.3f thread=%llx\n", routine_, t_err.status,
+                     wall_ms() - t0_, thread_tag());
+    nvtxRangePop();
 }
 
 void set_error(int status, const std::string& msg) {

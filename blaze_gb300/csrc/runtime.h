@@ -75,6 +75,23 @@ void* pool_get(int s, size_t bytes, std::string* err);
 // Thread-local last error.
 void set_error(int status, const std::string& msg);
 void clear_error();
+
+// One C-ABI call: an NVTX range named after the routine around the whole call (shown by Nsight
+// tools; close to free when none is attached) and, with GB300_BLAS_TRACE=1 in the environment, an
+// enter and a leave line on stderr with the thread, the shape, the call's status and its wall time
+// (the counterpart of Blaze's BLAZE_FUNCTION_TRACE).
+class CallTrace {
+  public:
+    CallTrace(const char* routine, int64_t m, int64_t n, int64_t k);
+    ~CallTrace();
+    CallTrace(const CallTrace&) = delete;
+    CallTrace& operator=(const CallTrace&) = delete;
+
+  private:
+    const char* routine_;
+    double t0_ = 0.0;
+    bool trace_ = false;
+};
 int last_error();
 const char* last_error_message();
 

@@ -145,3 +145,23 @@ def test_neighbour_routines_name_the_parameter(lib, routine, args, param):
     st, msg = G.last_error()
     assert st == G.ERR_INVALID_ARG
     assert f"parameter {param} " in msg
+
+
+def test_call_trace_prints_enter_and_leave():
+    """GB300_BLAS_TRACE=1: one enter and one leave line per call with the routine, the shape and
+    the call's status (here the call fails: argument check, or no device on a CPU host)."""
+    import subprocess
+    import sys
+    code = ("import numpy as np, blaze_gb300 as G\n"
+            "A = np.ones(6); B = np.ones(12); C = np.zeros(8)\n"
+            "G.lib().gb300_clear_error()\n"
+            "G.lib().cblas_dgemm(101, 111, 111, 2, 4, 3, 1.0, A.ctypes.data, 3, B.ctypes.data, 4, 0.0, C.ctypes.data, 4)\n"
+            "G.lib().cblas_dgemm(101, 111, 111, 2, 4, 3, 1.0, A.ctypes.data, 1, B.ctypes.data, 4, 0.0, C.ctypes.data, 4)\n")
+    env = dict(os.environ, GB300_BLAS_TRACE="1")
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, env=env, cwd=ROOT, timeout=120)
+    assert r.returncode == 0, r.stderr
+    lines = [ln for ln in r.stderr.splitlines() if ln.startswith("libgb300blas: ")]
+    enters = [ln for ln in lines if " enter cblas_dgemm m=2 n=4 k=3 " in ln]
+    leaves = [ln for ln in lines if " leave cblas_dgemm status=" in ln]
+    assert len(enters) == 2 and len(leaves) == 2, lines
+    assert "status=1 " in leaves[1]  # the second call: parameter 9 (lda) is too small
