@@ -26,10 +26,10 @@ def available() -> bool:
 
 
 # matrix x vector products take Blaze's BLAS kernels (off by default, blaze/config/BLAS.h) from
-# modest sizes on (blaze/config/Thresholds.h)
+# modest sizes on, and small-area matrix products take them too (blaze/config/Thresholds.h)
 NEXT_FLAGS = ["-DBLAZE_USE_BLAS_MATRIX_VECTOR_MULTIPLICATION=1", "-DBLAZE_DMATDVECMULT_THRESHOLD=1000UL",
               "-DBLAZE_TDMATDVECMULT_THRESHOLD=1000UL", "-DBLAZE_TDVECDMATMULT_THRESHOLD=1000UL",
-              "-DBLAZE_TDVECTDMATMULT_THRESHOLD=1000UL"]
+              "-DBLAZE_TDVECTDMATMULT_THRESHOLD=1000UL", "-DBLAZE_DMATDMATMULT_THRESHOLD=1UL"]
 
 
 def build(kind: str, program: str = "main") -> str | None:

@@ -8,6 +8,8 @@
 //       (blaze/math/expressions/DMatDVecMultExpr.h:1166-1172)
 //   complex y = A*x, C = A*B                                       -> cblas_zgemv, cblas_zgemm
 //   C = L*B, L triangular (DMatDMatMultExpr.h:2026-2033)          -> cblas_dtrmm / cblas_ztrmm
+//   C = A*B of a small area, with -DBLAZE_DMATDMATMULT_THRESHOLD=1 -> cblas_dgemm
+//   C = A*B with B of at most 10 SIMD widths of columns            -> Blaze's own small kernel
 // and prints one line per product:  <label> status=<ok|exception> maxdiff=<|result - reference|>
 // where the reference is a plain loop over the same operands (BLAS bypassed).
 #include <blaze/Math.h>
@@ -169,6 +171,21 @@ int main() {
         fill(U, 22); fill(B, 23);
         C = U * B;
         return mm_diff(U, B, C);
+    });
+    // Blaze's size gates (DMatDMatMultExpr.h:561-569): with the area threshold lowered
+    // (-DBLAZE_DMATDMATMULT_THRESHOLD), a small product (M*N = 3840 < 4900) takes the BLAS kernel;
+    // a product with B.columns() <= 10 SIMD widths stays in Blaze's small kernel (that gate is fixed).
+    report("small_area", [] {
+        blaze::DynamicMatrix<double, rowMajor> A(40, 30), B(30, 96), C;
+        fill(A, 24); fill(B, 25);
+        C = A * B;
+        return mm_diff(A, B, C);
+    });
+    report("skinny_cpu", [] {
+        blaze::DynamicMatrix<double, rowMajor> A(300, 30), B(30, 16), C;
+        fill(A, 26); fill(B, 27);
+        C = A * B;
+        return mm_diff(A, B, C);
     });
     return 0;
 }

@@ -85,7 +85,7 @@ def _vals(count, seed, kind):
 
 def test_replay_blaze_neighbouring_calls():
     lines = open(NEXT_CALLS).read().splitlines()
-    assert len(lines) == 11
+    assert len(lines) == 12
     for q, ln in enumerate(lines):
         f = ln.split()
         name, kind = f[0], f[0][0]
@@ -114,6 +114,16 @@ def test_replay_blaze_neighbouring_calls():
             G.cblas_trmv(order, uplo, ta, diag, n, A, lda, x, incx, dtype=kind)
             got = x[::incx]
             k = n
+        elif name == "dgemm":  # a real product Blaze's lowered area threshold sent to BLAS
+            order, ta, tb, m, n, k = (int(v) for v in f[1:7])
+            al, lda, ldb, be, ldc = float(f[7]), int(f[8]), int(f[9]), float(f[10]), int(f[11])
+            A = _vals(m * lda, 400 + q, kind)
+            B = _vals(k * ldb, 500 + q, kind)
+            C = _vals(m * ldc, 600 + q, kind)
+            ref = al * (np.array(_mat(A, order, m, k, lda)) @ np.array(_mat(B, order, k, n, ldb))) + \
+                be * np.array(_mat(C, order, m, n, ldc))
+            G.cblas_dgemm(order, ta, tb, m, n, k, al, A, lda, B, ldb, be, C, ldc)
+            got = np.array(_mat(C, order, m, n, ldc))
         elif name.endswith("gemm"):
             order, ta, tb, m, n, k = (int(v) for v in f[1:7])
             al, lda, ldb, be, ldc = _scalar(f[7]), int(f[8]), int(f[9]), _scalar(f[10]), int(f[11])
