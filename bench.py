@@ -299,8 +299,8 @@ def e2e_leg(G, hA, hB, n, flops, args, dist):
 
 def batched_leg(G, torch, args, dev):
     """10,000 independent products, M, N, K log-uniform integers in [4, 256], uniform [-1,1],
-    FP64 and FP32: one persistent grouped launch (CUDA graph) against a loop of per-product
-    launches of the native kernel, both device-resident."""
+    FP64 and FP32: one persistent grouped launch (CUDA graph, tile shapes from the autotuner)
+    against a loop of per-product launches of the native kernel, both device-resident."""
     import numpy as np
 
     def build(count, seed, dtype):
@@ -327,6 +327,11 @@ def batched_leg(G, torch, args, dev):
     for name, dtype, esz in (("fp64", np.float64, 8), ("fp32", np.float32, 4)):
         specs, dA, dB, dC = build(args.batch_count, args.seed + 100, dtype)
         probs = G.problems(specs)
+        # the autotuner times every warp-tile shape on a synthetic batch of each size class and
+        # records its cost per padded multiply-add; the plan then picks each product's shape
+        t0 = time.perf_counter()
+        G.grouped_autotune(esz, 1)
+        t_tune = time.perf_counter() - t0
         t0 = time.perf_counter()
         plan = G.GroupedPlan(probs, esz)
         t_plan = time.perf_counter() - t0
@@ -363,7 +368,8 @@ def batched_leg(G, torch, args, dev):
         loop_ms = l0.elapsed_time(l1)
         out[name] = {"grouped_ms": round(ms, 4), "grouped_tflops": round(useful / (ms * 1e-3) / 1e12, 4),
                      "padded_over_useful": round(padded / useful, 4), "tiles": int(ntiles),
-                     "plan_ms": round(t_plan * 1e3, 2), "loop_ms_device": round(loop_ms, 3),
+                     "plan_ms": round(t_plan * 1e3, 2), "autotune_s": round(t_tune, 2),
+                     "loop_ms_device": round(loop_ms, 3),
                      "loop_ms_wall": round(loop_wall * 1e3, 2), "speedup_vs_loop": round(loop_ms / ms, 2),
                      "useful_gflop": round(useful / 1e9, 4)}
         del dA, dB, dC

@@ -155,9 +155,19 @@ constexpr int kMB = 6, kKB = 3;
 int bucket_mn(int x) { return x <= 8 ? 0 : x <= 16 ? 1 : x <= 32 ? 2 : x <= 64 ? 3 : x <= 128 ? 4 : 5; }
 int bucket_k(int x) { return x <= 16 ? 0 : x <= 64 ? 1 : 2; }
 
+// How a plan picks a product's shape, per element type:
+//   kPickModel   no table: the least padded work for the product's own m and n (model_shape);
+//   kPickTable   a loaded table without costs: the shape stored for the product's size class;
+//   kPickCost    autotuned (or a table with costs): for the product's own m, n the shape with the
+//                least (padded multiply-adds) x (the time per padded multiply-add the autotuner
+//                measured for that shape in the product's size class).
+enum PickMode : int { kPickModel = 0, kPickTable = 1, kPickCost = 2 };
+
 struct TuneTable {
     int shape[2][kMB][kMB][kKB];  // [dtype: 0 double, 1 float]
-    bool tuned[2] = {false, false};
+    float cost[2][kMB][kMB][kKB][kNumShapes] = {};  // ns per padded multiply-add, 0 = not measured
+    int mode[2] = {kPickModel, kPickModel};
+    bool tuned_any = false;  // the autotuner ran (or a v2 table was loaded): save as v2
 };
 
 std::mutex g_tune_mu;
@@ -192,10 +202,30 @@ void tune_defaults() {
     g_tune_init = true;
 }
 
-int pick_shape(int dtype_idx, int m, int n, int k) {
+int pick_shape(int dtype_idx, int m, int n, int k, int mode_override = -1) {
     std::lock_guard<std::mutex> lock(g_tune_mu);
     tune_defaults();
-    return g_tune.shape[dtype_idx][bucket_mn(m)][bucket_mn(n)][bucket_k(k)];
+    const int nshapes = dtype_idx == 0 ? max_shape<double>() + 1 : kNumShapes;
+    const int a = bucket_mn(m), b = bucket_mn(n), c = bucket_k(k);
+    switch (mode_override >= 0 ? mode_override : g_tune.mode[dtype_idx]) {
+        case kPickTable: return g_tune.shape[dtype_idx][a][b][c];
+        case kPickCost: {
+            int best = g_tune.shape[dtype_idx][a][b][c];
+            double best_cost = 1e300;
+            for (int s = 0; s < nshapes; ++s) {
+                const float per = g_tune.cost[dtype_idx][a][b][c][s];
+                if (per <= 0.f) continue;
+                const double tr = shape_rows(s), tc = shape_cols(s);
+                const double cost = std::ceil(m / tr) * tr * std::ceil(n / tc) * tc * double(per);
+                if (cost < best_cost) {
+                    best_cost = cost;
+                    best = s;
+                }
+            }
+            return best;
+        }
+        default: return model_shape(m, n, nshapes);
+    }
 }
 
 }  // namespace
@@ -229,7 +259,8 @@ void plan_free(GroupedPlan* p) {
 }
 
 template <typename T>
-int plan_create(const gb300_gemm_problem* probs, int64_t count, int force_shape, GroupedPlan** out, std::string* err) {
+int plan_create(const gb300_gemm_problem* probs, int64_t count, int force_shape, GroupedPlan** out, std::string* err,
+                int policy = -1) {
     Runtime& r = runtime();
     int st = ensure_init(err);
     if (st != GB300_OK) return st;
@@ -269,7 +300,7 @@ int plan_create(const gb300_gemm_problem* probs, int64_t count, int force_shape,
         d.beta = x.beta;
         if (d.m == 0 || d.n == 0) continue;
         if (d.k == 0 || x.alpha == 0.0) d.k = 0;  // C = beta*C through the same kernel
-        d.shape = force_shape >= 0 ? force_shape : pick_shape(didx, d.m, d.n, d.k);
+        d.shape = force_shape >= 0 ? force_shape : pick_shape(didx, d.m, d.n, d.k, policy);
         const int tr = shape_rows(d.shape), tc = shape_cols(d.shape);
         const int mt = (d.m + tr - 1) / tr, nt = (d.n + tc - 1) / tc;
         const int pid = int(hp.size());
@@ -343,47 +374,63 @@ int autotune(int didx, int effort, std::string* err) {
     const int rep_lo[kMB] = {4, 9, 17, 33, 65, 129};
     const int rep_hi[kMB] = {8, 16, 32, 64, 128, 256};
     const int k_lo[kKB] = {4, 17, 65}, k_hi[kKB] = {16, 64, 256};
-    const int batch = std::max(32, 64 * effort);
     uint64_t rng = 0x9E3779B97F4A7C15ull;
     auto rnd = [&](int lo, int hi) {
         rng ^= rng << 13; rng ^= rng >> 7; rng ^= rng << 17;
         return lo + int(rng % uint64_t(hi - lo + 1));
     };
-    // one pool of operand memory large enough for a class batch
-    const size_t maxel = size_t(256) * 256;
-    T *dA = nullptr, *dB = nullptr, *dC = nullptr;
+    // Each class is timed on a batch holding about `work` multiply-adds, so that a plan's run is
+    // long against its launch: a batch of a few tiny products would time the launch, not the shape.
+    const double work = 1.28e8 * std::max(1, effort) * (sizeof(T) == 4 ? 4.0 : 1.0);  // FP32 runs ~30x faster
+    auto class_batch = [&](int a, int b, int c) {
+        const double mean = 0.125 * double(rep_lo[a] + rep_hi[a]) * double(rep_lo[b] + rep_hi[b]) *
+                            double(k_lo[c] + k_hi[c]);
+        // (at most 16384 products: the plan's host-side set-up grows with the count)
+        return int(std::max(64.0, std::min(16384.0, work / mean)));
+    };
+    auto footprint = [&](int a, int b, int c) {  // elements of A, B and C of one product, at most
+        return size_t(rep_hi[a]) * k_hi[c] + size_t(k_hi[c]) * rep_hi[b] + size_t(rep_hi[a]) * rep_hi[b];
+    };
+    size_t pool = 0;
+    for (int a = 0; a < kMB; ++a)
+        for (int b = 0; b < kMB; ++b)
+            for (int c = 0; c < kKB; ++c) pool = std::max(pool, size_t(class_batch(a, b, c)) * footprint(a, b, c));
+    T* dP = nullptr;
     cudaError_t e;
-    if ((e = cudaMalloc(&dA, size_t(batch) * maxel * sizeof(T))) != cudaSuccess ||
-        (e = cudaMalloc(&dB, size_t(batch) * maxel * sizeof(T))) != cudaSuccess ||
-        (e = cudaMalloc(&dC, size_t(batch) * maxel * sizeof(T))) != cudaSuccess) {
-        cudaFree(dA); cudaFree(dB); cudaFree(dC);
+    if ((e = cudaMalloc(&dP, pool * sizeof(T))) != cudaSuccess) {
         if (err) *err = std::string("autotune buffers: ") + cudaGetErrorString(e);
         return GB300_ERR_NO_MEMORY;
     }
-    cudaMemset(dA, 0, size_t(batch) * maxel * sizeof(T));
-    cudaMemset(dB, 0, size_t(batch) * maxel * sizeof(T));
+    cudaMemset(dP, 0, pool * sizeof(T));
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     int table[kMB][kMB][kKB];
+    float costs[kMB][kMB][kKB][kNumShapes] = {};
     for (int a = 0; a < kMB; ++a)
         for (int b = 0; b < kMB; ++b)
             for (int c = 0; c < kKB; ++c) {
+                const int batch = class_batch(a, b, c);
                 std::vector<gb300_gemm_problem> ps(static_cast<size_t>(batch));
+                size_t off = 0;
                 for (int q = 0; q < batch; ++q) {
                     gb300_gemm_problem& x = ps[size_t(q)];
                     std::memset(&x, 0, sizeof(x));
                     x.order = 101; x.transA = 111; x.transB = 111;
                     x.m = rnd(rep_lo[a], rep_hi[a]); x.n = rnd(rep_lo[b], rep_hi[b]); x.k = rnd(k_lo[c], k_hi[c]);
                     x.alpha = 1.0; x.beta = 0.0;
-                    x.A = dA + size_t(q) * maxel; x.lda = x.k;
-                    x.B = dB + size_t(q) * maxel; x.ldb = x.n;
-                    x.C = dC + size_t(q) * maxel; x.ldc = x.n;
+                    x.A = dP + off; x.lda = x.k;
+                    off += size_t(x.m) * size_t(x.k);
+                    x.B = dP + off; x.ldb = x.n;
+                    off += size_t(x.k) * size_t(x.n);
+                    x.C = dP + off; x.ldc = x.n;
+                    off += size_t(x.m) * size_t(x.n);
                 }
                 float best_ms = 1e30f;
                 int best = 0;
                 for (int s = 0; s <= max_shape<T>(); ++s) {
                     GroupedPlan* p = nullptr;
+                    costs[a][b][c][s] = 0.f;
                     if (plan_create<T>(ps.data(), batch, s, &p, err) != GB300_OK) continue;
                     cudaGraphLaunch(p->exec, p->cap_stream);  // warm-up
                     cudaEventRecord(e0, p->cap_stream);
@@ -394,18 +441,74 @@ int autotune(int didx, int effort, std::string* err) {
                     float ms = 0;
                     cudaEventElapsedTime(&ms, e0, e1);
                     count_launches(reps + 1);
+                    // time per padded multiply-add (ns), the shape's efficiency in this class
+                    if (p->padded_flops > 0) costs[a][b][c][s] = float(1e6 * ms / reps / (0.5 * p->padded_flops));
                     plan_free(p);
                     if (ms < best_ms) { best_ms = ms; best = s; }
                 }
                 table[a][b][c] = best;
             }
+    cudaFree(dP);
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mu);
+        tune_defaults();
+        std::memcpy(g_tune.shape[didx], table, sizeof(table));
+        std::memcpy(g_tune.cost[didx], costs, sizeof(costs));
+    }
+    // Which way of picking shapes is faster on a mixed batch (m, n, k log-uniform over all classes):
+    // the measured costs, or the least padded work alone (the better one where one pipe bounds
+    // every shape alike, as the FP64 pipe does).
+    const int vcount = 2048;
+    std::vector<gb300_gemm_problem> vs(static_cast<size_t>(vcount));
+    size_t vtotal = 0;
+    auto logu = [&](int lo, int hi) {
+        const double u = double(rnd(0, 1 << 20)) / double(1 << 20);
+        return int(std::lround(std::exp(std::log(double(lo)) + u * (std::log(double(hi)) - std::log(double(lo))))));
+    };
+    for (auto& x : vs) {
+        std::memset(&x, 0, sizeof(x));
+        x.order = 101; x.transA = 111; x.transB = 111;
+        x.m = logu(4, 256); x.n = logu(4, 256); x.k = logu(4, 256);
+        x.alpha = 1.0; x.beta = 0.0;
+        vtotal += size_t(x.m) * size_t(x.k) + size_t(x.k) * size_t(x.n) + size_t(x.m) * size_t(x.n);
+    }
+    int mode = kPickCost;
+    T* dV = nullptr;
+    if (cudaMalloc(&dV, vtotal * sizeof(T)) == cudaSuccess) {
+        cudaMemset(dV, 0, vtotal * sizeof(T));
+        size_t off = 0;
+        for (auto& x : vs) {
+            x.A = dV + off; x.lda = x.k; off += size_t(x.m) * size_t(x.k);
+            x.B = dV + off; x.ldb = x.n; off += size_t(x.k) * size_t(x.n);
+            x.C = dV + off; x.ldc = x.n; off += size_t(x.m) * size_t(x.n);
+        }
+        float best_ms = 1e30f;
+        for (int pol : {int(kPickCost), int(kPickModel)}) {
+            GroupedPlan* p = nullptr;
+            if (plan_create<T>(vs.data(), vcount, -1, &p, err, pol) != GB300_OK) continue;
+            cudaGraphLaunch(p->exec, p->cap_stream);
+            cudaEventRecord(e0, p->cap_stream);
+            for (int it = 0; it < 5; ++it) cudaGraphLaunch(p->exec, p->cap_stream);
+            cudaEventRecord(e1, p->cap_stream);
+            cudaEventSynchronize(e1);
+            float ms = 0;
+            cudaEventElapsedTime(&ms, e0, e1);
+            count_launches(6);
+            plan_free(p);
+            if (ms < best_ms) {
+                best_ms = ms;
+                mode = pol;
+            }
+        }
+        cudaFree(dV);
+    } else {
+        cudaGetLastError();
+    }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    cudaFree(dA); cudaFree(dB); cudaFree(dC);
     std::lock_guard<std::mutex> lock(g_tune_mu);
-    tune_defaults();
-    std::memcpy(g_tune.shape[didx], table, sizeof(table));
-    g_tune.tuned[didx] = true;
+    g_tune.mode[didx] = mode;
+    g_tune.tuned_any = true;
     return GB300_OK;
 }
 
@@ -514,6 +617,10 @@ int gb300_grouped_autotune(int elem_bytes, int effort) {
     return st;
 }
 
+// Tuning files: "gb300-grouped-tune v1" then one line per class, `dtype m-class n-class k-class
+// shape`; an autotuned table is saved as "gb300-grouped-tune v2", each line followed by the measured
+// ns per padded multiply-add of every shape (0: not measured).  Loading v1 makes plans use the
+// class shapes, loading v2 the measured costs.
 int gb300_grouped_tuning_save(const char* path) {
     std::lock_guard<std::mutex> lock(gb::g_tune_mu);
     gb::tune_defaults();
@@ -522,33 +629,75 @@ int gb300_grouped_tuning_save(const char* path) {
         gb::set_error(GB300_ERR_INVALID_ARG, std::string("gb300_grouped_tuning_save: cannot write ") + path);
         return GB300_ERR_INVALID_ARG;
     }
-    f << "gb300-grouped-tune v1\n";
+    // untuned defaults and loaded class tables save as v1; an autotuned table as v2 with its costs
+    // and the policy the autotuner chose ("mode <double> <float>")
+    const bool costs = gb::g_tune.mode[0] == gb::kPickCost || gb::g_tune.mode[1] == gb::kPickCost ||
+                       gb::g_tune.tuned_any;
+    f << (costs ? "gb300-grouped-tune v2\n" : "gb300-grouped-tune v1\n");
+    if (costs) f << "mode " << gb::g_tune.mode[0] << ' ' << gb::g_tune.mode[1] << '\n';
     for (int d = 0; d < 2; ++d)
         for (int a = 0; a < gb::kMB; ++a)
             for (int b = 0; b < gb::kMB; ++b)
-                for (int c = 0; c < gb::kKB; ++c)
-                    f << d << ' ' << a << ' ' << b << ' ' << c << ' ' << gb::g_tune.shape[d][a][b][c] << '\n';
+                for (int c = 0; c < gb::kKB; ++c) {
+                    f << d << ' ' << a << ' ' << b << ' ' << c << ' ' << gb::g_tune.shape[d][a][b][c];
+                    if (costs)
+                        for (int s = 0; s < gb::kNumShapes; ++s) f << ' ' << gb::g_tune.cost[d][a][b][c][s];
+                    f << '\n';
+                }
     return GB300_OK;
 }
 
 int gb300_grouped_tuning_load(const char* path) {
     std::ifstream f(path);
     std::string head;
-    if (!f || !std::getline(f, head) || head != "gb300-grouped-tune v1") {
+    const bool ok_head = f && std::getline(f, head) && (head == "gb300-grouped-tune v1" || head == "gb300-grouped-tune v2");
+    if (!ok_head) {
         gb::set_error(GB300_ERR_INVALID_ARG, std::string("gb300_grouped_tuning_load: not a tuning file: ") + path);
         return GB300_ERR_INVALID_ARG;
     }
-    std::lock_guard<std::mutex> lock(gb::g_tune_mu);
-    gb::tune_defaults();
-    int d, a, b, c, s;
-    while (f >> d >> a >> b >> c >> s) {
-        if (d < 0 || d > 1 || a < 0 || a >= gb::kMB || b < 0 || b >= gb::kMB || c < 0 || c >= gb::kKB || s < 0 ||
-            s > (d == 0 ? gb::max_shape<double>() : gb::max_shape<float>())) {
+    const bool v2 = head == "gb300-grouped-tune v2";
+    // parse everything first: a malformed file leaves the table as it was
+    gb::TuneTable t;
+    {
+        std::lock_guard<std::mutex> lock(gb::g_tune_mu);
+        gb::tune_defaults();
+        t = gb::g_tune;
+    }
+    std::string line;
+    int modes[2] = {gb::kPickCost, gb::kPickCost};
+    while (std::getline(f, line)) {
+        if (line.empty()) continue;
+        if (v2 && line.rfind("mode ", 0) == 0) {
+            std::istringstream ms(line.substr(5));
+            if (!(ms >> modes[0] >> modes[1]) || modes[0] < 0 || modes[0] > 2 || modes[1] < 0 || modes[1] > 2) {
+                gb::set_error(GB300_ERR_INVALID_ARG, "gb300_grouped_tuning_load: bad mode line");
+                return GB300_ERR_INVALID_ARG;
+            }
+            continue;
+        }
+        std::istringstream ls(line);
+        int d, a, b, c, s;
+        if (!(ls >> d >> a >> b >> c >> s) || d < 0 || d > 1 || a < 0 || a >= gb::kMB || b < 0 || b >= gb::kMB ||
+            c < 0 || c >= gb::kKB || s < 0 || s > (d == 0 ? gb::max_shape<double>() : gb::max_shape<float>())) {
             gb::set_error(GB300_ERR_INVALID_ARG, "gb300_grouped_tuning_load: bad entry");
             return GB300_ERR_INVALID_ARG;
         }
-        gb::g_tune.shape[d][a][b][c] = s;
+        t.shape[d][a][b][c] = s;
+        if (v2)
+            for (int q = 0; q < gb::kNumShapes; ++q) {
+                float v = 0.f;
+                if (!(ls >> v) || !(v >= 0.f)) {
+                    gb::set_error(GB300_ERR_INVALID_ARG, "gb300_grouped_tuning_load: bad cost");
+                    return GB300_ERR_INVALID_ARG;
+                }
+                t.cost[d][a][b][c][q] = v;
+            }
     }
+    t.mode[0] = v2 ? modes[0] : gb::kPickTable;
+    t.mode[1] = v2 ? modes[1] : gb::kPickTable;
+    t.tuned_any = v2;
+    std::lock_guard<std::mutex> lock(gb::g_tune_mu);
+    gb::g_tune = t;
     return GB300_OK;
 }
 

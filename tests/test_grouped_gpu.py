@@ -70,7 +70,13 @@ def test_autotuned_table_keeps_results(torch, tmp_path):
     G.grouped_autotune(8, 1)
     path = tmp_path / "tune.txt"
     G.lib().gb300_grouped_tuning_save(str(path).encode())
+    lines = path.read_text().splitlines()
+    # an autotuned table keeps its measured costs and the shape-picking policy the autotuner chose
+    assert lines[0] == "gb300-grouped-tune v2" and lines[1].startswith("mode ")
+    assert len(lines[2].split()) == 5 + 6
+    before = [G.grouped_shape_for(8, m, n, k) for (m, n, k) in ((5, 9, 30), (100, 20, 300), (250, 40, 7))]
     assert G.lib().gb300_grouped_tuning_load(str(path).encode()) == 0
+    assert [G.grouped_shape_for(8, m, n, k) for (m, n, k) in ((5, 9, 30), (100, 20, 300), (250, 40, 7))] == before
     G.dgemm_grouped(G.problems(specs))
     torch.cuda.synchronize()
     check_batch(specs, dC.cpu().numpy(), reference(specs, A, B, C0), np.float64)
