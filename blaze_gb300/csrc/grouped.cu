@@ -167,6 +167,7 @@ struct TuneTable {
     int shape[2][kMB][kMB][kKB];  // [dtype: 0 double, 1 float]
     float cost[2][kMB][kMB][kKB][kNumShapes] = {};  // ns per padded multiply-add, 0 = not measured
     int mode[2] = {kPickModel, kPickModel};
+    double tile_w[2] = {-1.0, -1.0};  // the model's per-tile weight (the autotuner's choice; -1: default)
     bool tuned_any = false;  // the autotuner ran (or a v2 table was loaded): save as v2
 };
 
@@ -175,14 +176,17 @@ TuneTable g_tune;
 bool g_tune_init = false;
 
 // Default choice (no measurements): the shape with the least padded work, larger tiles on ties.
-int model_shape(int m, int n, int nshapes) {
+// tile_w < 0: the cost is the padded area plus 64 a tile (k left out); tile_w >= 0: the padded
+// multiply-adds (area x k) plus tile_w multiply-adds' worth of overhead a tile.
+int model_shape(int m, int n, int nshapes, int k = 1, double tile_w = -1.0) {
     int best = 0;
     double best_cost = 1e300;
     for (int s = 0; s < nshapes; ++s) {
         const double tr = shape_rows(s), tc = shape_cols(s);
         const double padded = std::ceil(m / tr) * tr * std::ceil(n / tc) * tc;
+        const double tiles = std::ceil(m / tr) * std::ceil(n / tc);
         // a small per-tile overhead favours fewer, larger tiles when the padding is equal
-        const double cost = padded + 64.0 * std::ceil(m / tr) * std::ceil(n / tc);
+        const double cost = tile_w < 0 ? padded + 64.0 * tiles : padded * double(std::max(k, 1)) + tile_w * tiles;
         if (cost < best_cost - 1e-9) {
             best_cost = cost;
             best = s;
@@ -224,7 +228,7 @@ int pick_shape(int dtype_idx, int m, int n, int k, int mode_override = -1) {
             }
             return best;
         }
-        default: return model_shape(m, n, nshapes);
+        default: return model_shape(m, n, nshapes, k, g_tune.tile_w[dtype_idx]);
     }
 }
 
@@ -473,6 +477,7 @@ int autotune(int didx, int effort, std::string* err) {
         vtotal += size_t(x.m) * size_t(x.k) + size_t(x.k) * size_t(x.n) + size_t(x.m) * size_t(x.n);
     }
     int mode = kPickCost;
+    double best_w = -1.0;
     T* dV = nullptr;
     if (cudaMalloc(&dV, vtotal * sizeof(T)) == cudaSuccess) {
         cudaMemset(dV, 0, vtotal * sizeof(T));
@@ -483,7 +488,15 @@ int autotune(int didx, int effort, std::string* err) {
             x.C = dV + off; x.ldc = x.n; off += size_t(x.m) * size_t(x.n);
         }
         float best_ms = 1e30f;
-        for (int pol : {int(kPickCost), int(kPickModel)}) {
+        // candidates: the measured costs, and the model with per-tile weights from none to large
+        const double weights[] = {-1.0, 0.0, 512.0, 2048.0, 8192.0};
+        for (int cand = 0; cand < 6; ++cand) {
+            const int pol = cand == 0 ? int(kPickCost) : int(kPickModel);
+            const double w = cand == 0 ? -1.0 : weights[cand - 1];
+            {
+                std::lock_guard<std::mutex> lock(g_tune_mu);
+                g_tune.tile_w[didx] = w;
+            }
             GroupedPlan* p = nullptr;
             if (plan_create<T>(vs.data(), vcount, -1, &p, err, pol) != GB300_OK) continue;
             cudaGraphLaunch(p->exec, p->cap_stream);
@@ -498,6 +511,7 @@ int autotune(int didx, int effort, std::string* err) {
             if (ms < best_ms) {
                 best_ms = ms;
                 mode = pol;
+                best_w = w;
             }
         }
         cudaFree(dV);
@@ -508,6 +522,7 @@ int autotune(int didx, int effort, std::string* err) {
     cudaEventDestroy(e1);
     std::lock_guard<std::mutex> lock(g_tune_mu);
     g_tune.mode[didx] = mode;
+    g_tune.tile_w[didx] = mode == kPickModel ? best_w : -1.0;
     g_tune.tuned_any = true;
     return GB300_OK;
 }
@@ -634,7 +649,9 @@ int gb300_grouped_tuning_save(const char* path) {
     const bool costs = gb::g_tune.mode[0] == gb::kPickCost || gb::g_tune.mode[1] == gb::kPickCost ||
                        gb::g_tune.tuned_any;
     f << (costs ? "gb300-grouped-tune v2\n" : "gb300-grouped-tune v1\n");
-    if (costs) f << "mode " << gb::g_tune.mode[0] << ' ' << gb::g_tune.mode[1] << '\n';
+    if (costs)
+        f << "mode " << gb::g_tune.mode[0] << ' ' << gb::g_tune.mode[1] << ' ' << gb::g_tune.tile_w[0] << ' '
+          << gb::g_tune.tile_w[1] << '\n';
     for (int d = 0; d < 2; ++d)
         for (int a = 0; a < gb::kMB; ++a)
             for (int b = 0; b < gb::kMB; ++b)
@@ -672,6 +689,11 @@ int gb300_grouped_tuning_load(const char* path) {
             if (!(ms >> modes[0] >> modes[1]) || modes[0] < 0 || modes[0] > 2 || modes[1] < 0 || modes[1] > 2) {
                 gb::set_error(GB300_ERR_INVALID_ARG, "gb300_grouped_tuning_load: bad mode line");
                 return GB300_ERR_INVALID_ARG;
+            }
+            double w0 = -1.0, w1 = -1.0;
+            if (ms >> w0 >> w1) {  // the model's per-tile weights (absent in older v2 files)
+                t.tile_w[0] = w0;
+                t.tile_w[1] = w1;
             }
             continue;
         }
