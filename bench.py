@@ -382,7 +382,8 @@ def next_leg(G, torch, args):
     matrix (bytes read / time against the measured HBM copy bandwidth), an FP64-accurate zgemm of
     4096^3 (four split real products; 8 m n k flops), an FP64-accurate dtrmm (left, lower) of
     8192 x 8192 (m^2 n flops of a triangular product), zgemv (conjugate transpose) on 8192 x 8192,
-    dtrmv on a 16384 x 16384 triangle and ztrmm of 4096 x 4096."""
+    dtrmv on a 16384 x 16384 triangle and ztrmm of 4096 x 4096; sgemm at 8192^3, the residue form
+    at the float target against the native FFMA kernel."""
     peaks, _ = read_peaks()
 
     def wall(fn, reps):
@@ -459,6 +460,23 @@ def next_leg(G, torch, args):
     out["ztrmm"] = {"n": n5, "ms": round(t * 1e3, 3), "tflops": round(4.0 * float(n5) ** 3 / t / 1e12, 2),
                     "form": "masked complex triangle, four FP64-accurate split real products"}
     del zT, zB2
+    # float products (cblas_sgemm) at 8192^3: the residue form at the float target k 2^-24 (auto),
+    # and the native FFMA kernel; normwise error on every 64th row against an FP64 product
+    n6 = 8192
+    fA = dev_uniform(n6 * n6, torch.float32)
+    fB = dev_uniform(n6 * n6, torch.float32)
+    fC = torch.zeros(n6 * n6, dtype=torch.float32, device="cuda")
+    rows = torch.arange(0, n6, 64, device="cuda")
+    ref = fA.view(n6, n6)[rows].double() @ fB.view(n6, n6).double()
+    scale = float(torch.linalg.norm(fA.double()) * torch.linalg.norm(fB.double()))
+    for meth, reps in (("auto", 3), ("native", 1)):
+        o = G.opts(method=meth, residency=G.PTR_DEVICE)
+        t = wall(lambda: G.sgemm_ex(101, 111, 111, n6, n6, n6, 1.0, fA, n6, fB, n6, 0.0, fC, n6, o), reps)
+        err = float(torch.linalg.norm(fC.view(n6, n6)[rows].double() - ref)) * (n6 / len(rows)) ** 0.5 / scale
+        out["sgemm_" + meth] = {"n": n6, "ms": round(t * 1e3, 3), "tflops": round(2.0 * n6 ** 3 / t / 1e12, 2),
+                                "method_used": int(o.method_used), "moduli": int(o.slices_used),
+                                "bound": o.error_bound, "normwise_error": err}
+    del fA, fB, fC, ref
     out["inputs"] = "uniform [-1,1] generated on the device (torch.Generator, the bench seed)"
     return out
 

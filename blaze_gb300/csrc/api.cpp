@@ -130,8 +130,6 @@ int gemm_entry(int order, int transA, int transB, int64_t m, int64_t n, int64_t 
     if (method == GB300_METHOD_AUTO && opts == nullptr) method = default_method();
     if (method < GB300_METHOD_AUTO || method > GB300_METHOD_SPLIT_CRT)
         return fail(GB300_ERR_INVALID_ARG, "unknown method " + std::to_string(method));
-    if (!is_double && (method == GB300_METHOD_SPLIT || method == GB300_METHOD_SPLIT_CRT))
-        return fail(GB300_ERR_INVALID_ARG, "the split-precision form is defined for double only");
     clear_error();
     if (opts) {
         opts->method_used = GB300_METHOD_NATIVE;
@@ -242,13 +240,18 @@ int gemm_entry(int order, int transA, int transB, int64_t m, int64_t n, int64_t 
     g.C = const_cast<void*>(dc.ptr); g.ldc = dc.ld;
 
     // ---- run ----
-    if (is_double && product && method != GB300_METHOD_NATIVE) {
+    // float: the split forms run on double copies at the float target (device_product_float); small
+    // products under `auto` stay on the native kernel, as for double
+    const bool split_path = product && method != GB300_METHOD_NATIVE &&
+                            (is_double || !(method == GB300_METHOD_AUTO && split_auto_uses_native(g)));
+    if (split_path) {
         SplitRequest req;
         req.method = method;
         req.slices = opts ? opts->slices : 0;
         req.target_error = opts ? opts->target_error : 0.0;
         SplitResult res_out;
-        st = device_product(g, req, ctl, s, r.ws, &res_out, &err);
+        st = is_double ? device_product(g, req, ctl, s, r.ws, &res_out, &err)
+                       : device_product_float(g, req, ctl, s, r.ws, r.aux, &res_out, &err);
         if (st != GB300_OK) return fail(st, err);
         used = res_out.method_used;
         info_dev = res_out.info_dev;
@@ -294,7 +297,7 @@ int gemm_entry(int order, int transA, int transB, int64_t m, int64_t n, int64_t 
             double bd = 0;
             if (split_read_info(info_dev, &sl, &bd)) {
                 opts->slices_used = sl;
-                opts->error_bound = bd;
+                opts->error_bound = is_double ? bd : bd + 0x1p-24;  // float: the final rounding
             }
         }
     }

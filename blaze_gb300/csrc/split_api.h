@@ -39,6 +39,15 @@ struct Workspace;
 int device_product(const Gemm& g, const SplitRequest& req, const LaunchCtl& ctl, cudaStream_t s, Workspace& ws,
                    SplitResult* out, std::string* err);
 
+// True when the `auto` method runs a product on the native kernel (small products, short k).
+bool split_auto_uses_native(const Gemm& g);
+
+// The same for float operands (device, float, caller's pitches): widened to double in `conv`
+// (slots 0-2), computed at the float target k 2^-24 unless the request sets one, rounded once to
+// float.  The bound includes the final rounding (2^-24).
+int device_product_float(const Gemm& g, const SplitRequest& req, const LaunchCtl& ctl, cudaStream_t s, Workspace& ws,
+                         Workspace& conv, SplitResult* out, std::string* err);
+
 // FP64-accurate product of host operands (page-locked or pageable) in row panels of A: B is copied
 // and sliced once, then each panel's copy in, product and copy of C back run on three streams so
 // that the transfers overlap the computation.  The operands keep the caller's layout (g as for device_product, with host

@@ -1561,6 +1561,29 @@ void split_decode_info(const void* info_host, int* slices, double* bound) {
     *bound = h.bound;
 }
 
+namespace {
+// dst (rows x cols, pitch ld_d) = src (pitch ld_s), element-wise conversion: rows on blockIdx.y
+// (striding by gridDim.y), columns on threads.
+template <typename S, typename D>
+__global__ void convert_kernel(int64_t rows, int64_t cols, const S* __restrict__ src, int64_t ld_s, D* __restrict__ dst,
+                               int64_t ld_d) {
+    for (int64_t r = blockIdx.y; r < rows; r += gridDim.y)
+        for (int64_t c = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; c < cols; c += int64_t(gridDim.x) * blockDim.x)
+            dst[r * ld_d + c] = D(src[r * ld_s + c]);
+}
+
+template <typename S, typename D>
+cudaError_t launch_convert(int64_t rows, int64_t cols, const S* src, int64_t ld_s, D* dst, int64_t ld_d,
+                           cudaStream_t st) {
+    if (rows <= 0 || cols <= 0) return cudaSuccess;
+    const int64_t x = std::max<int64_t>(1, std::min<int64_t>((cols + 255) / 256, 64));
+    const int64_t y = std::max<int64_t>(1, std::min<int64_t>(rows, int64_t(runtime().num_sms) * 16 / x));
+    convert_kernel<S, D><<<dim3(unsigned(x), unsigned(y)), 256, 0, st>>>(rows, cols, src, ld_s, dst, ld_d);
+    count_launches(1);
+    return cudaGetLastError();
+}
+}  // namespace
+
 // ---- host orchestration ------------------------------------------------------------------------
 namespace {
 
@@ -1726,6 +1749,8 @@ size_t device_product_footprint(const Gemm& g, const SplitRequest& req) {
     return t;
 }
 
+bool split_auto_uses_native(const Gemm& g) { return auto_uses_native(g); }
+
 int device_product(const Gemm& g_in, const SplitRequest& req, const LaunchCtl& ctl, cudaStream_t st, Workspace& ws,
                    SplitResult* out, std::string* err) {
     Runtime& r = runtime();
@@ -1887,6 +1912,45 @@ int device_product(const Gemm& g_in, const SplitRequest& req, const LaunchCtl& c
     return GB300_OK;
 }
 
+
+// A float product through the FP64-accurate machinery: A and B (device, float, the caller's
+// pitches) are widened to double in `conv`'s slots 0 and 1 (exact), C in slot 2 (read only when
+// beta != 0), device_product runs at the float target (k 2^-24 unless the request sets one), and
+// the double result is rounded once to float into C.  The reported bound adds 2^-24 for that final
+// rounding.
+int device_product_float(const Gemm& g, const SplitRequest& req_in, const LaunchCtl& ctl, cudaStream_t st,
+                         Workspace& ws, Workspace& conv, SplitResult* out, std::string* err) {
+    const int64_t a_rows = g.ta ? g.k : g.m, a_cols = g.ta ? g.m : g.k;
+    const int64_t b_rows = g.tb ? g.n : g.k, b_cols = g.tb ? g.k : g.n;
+    const int64_t pa = (a_cols + 1) / 2 * 2, pb = (b_cols + 1) / 2 * 2, pc = (g.n + 1) / 2 * 2;  // 16-byte pitches
+    auto* dA = static_cast<double*>(conv.get(0, size_t(a_rows) * size_t(pa) * 8, err));
+    auto* dB = static_cast<double*>(conv.get(1, size_t(b_rows) * size_t(pb) * 8, err));
+    auto* dC = static_cast<double*>(conv.get(2, size_t(g.m) * size_t(pc) * 8, err));
+    if (!dA || !dB || !dC) return GB300_ERR_NO_MEMORY;
+    cudaError_t e = launch_convert(a_rows, a_cols, static_cast<const float*>(g.A), g.lda, dA, pa, st);
+    if (e == cudaSuccess) e = launch_convert(b_rows, b_cols, static_cast<const float*>(g.B), g.ldb, dB, pb, st);
+    if (e == cudaSuccess && g.beta != 0.0)
+        e = launch_convert(g.m, g.n, static_cast<const float*>(g.C), g.ldc, dC, pc, st);
+    if (e != cudaSuccess) {
+        if (err) *err = std::string("float widening: ") + cudaGetErrorString(e);
+        return GB300_ERR_CUDA;
+    }
+    Gemm g64 = g;
+    g64.A = dA; g64.lda = pa;
+    g64.B = dB; g64.ldb = pb;
+    g64.C = dC; g64.ldc = pc;
+    SplitRequest req = req_in;
+    if (req.target_error <= 0) req.target_error = double(std::max<int64_t>(g.k, 1)) * 0x1p-24;
+    const int st_ = device_product(g64, req, ctl, st, ws, out, err);
+    if (st_ != GB300_OK) return st_;
+    e = launch_convert(g.m, g.n, static_cast<const double*>(dC), pc, static_cast<float*>(g.C), g.ldc, st);
+    if (e != cudaSuccess) {
+        if (err) *err = std::string("float rounding: ") + cudaGetErrorString(e);
+        return GB300_ERR_CUDA;
+    }
+    if (out->error_bound >= 0) out->error_bound += 0x1p-24;
+    return GB300_OK;
+}
 
 namespace {
 bool page_locked(const void* p) {
