@@ -383,7 +383,8 @@ def next_leg(G, torch, args):
     4096^3 (four split real products; 8 m n k flops), an FP64-accurate dtrmm (left, lower) of
     8192 x 8192 (m^2 n flops of a triangular product), zgemv (conjugate transpose) on 8192 x 8192,
     dtrmv on a 16384 x 16384 triangle and ztrmm of 4096 x 4096; sgemm at 8192^3, the residue form
-    at the float target against the native FFMA kernel."""
+    at the float target against the native FFMA kernel; dtrsm 8192 and ztrsm 4096 (square right-hand
+    sides) against cuBLAS's FP64 solve; ddot and daxpy over 2^27 doubles."""
     peaks, _ = read_peaks()
 
     def wall(fn, reps):
@@ -398,7 +399,9 @@ def next_leg(G, torch, args):
     gen.manual_seed(args.seed)
 
     def dev_uniform(count, dtype=torch.float64):
-        return torch.rand(count, generator=gen, device="cuda", dtype=dtype) * 2 - 1
+        v = torch.rand(count, generator=gen, device="cuda", dtype=dtype) * 2 - 1
+        torch.cuda.synchronize()  # the library runs on its own stream
+        return v
 
     m, n = 16384, 8192
     dA = dev_uniform(m * n)
@@ -477,6 +480,58 @@ def next_leg(G, torch, args):
                                 "method_used": int(o.method_used), "moduli": int(o.slices_used),
                                 "bound": o.error_bound, "normwise_error": err}
     del fA, fB, fC, ref
+    # triangular solves: dtrsm (left, lower) with 8192 x 8192 right-hand sides (m^2 n flops) and
+    # ztrsm 4096 (4 m^2 n); the triangle has off-diagonal entries u / n and diagonal 1 + u / 2 (well
+    # conditioned); error against cuBLAS's FP64 solve (torch.linalg.solve_triangular, timed once)
+    for name, n7, cplx, reps in (("dtrsm", 8192, False, 3), ("ztrsm", 4096, True, 3)):
+        def tri_operand():
+            if cplx:
+                T = torch.complex(dev_uniform(n7 * n7), dev_uniform(n7 * n7)).view(n7, n7) / n7
+            else:
+                T = dev_uniform(n7 * n7).view(n7, n7) / n7
+            T.diagonal().copy_(1 + 0.5 * n7 * T.diagonal())
+            return T.contiguous()
+        T = tri_operand()
+        B0 = (torch.complex(dev_uniform(n7 * n7), dev_uniform(n7 * n7)) if cplx else dev_uniform(n7 * n7)).view(n7, n7)
+        X = B0.clone()
+        torch.cuda.synchronize()
+
+        def solve():
+            X.copy_(B0)
+            torch.cuda.synchronize()
+            G.cblas_trsm(101, 141, 122, 111, 131, n7, n7, (1 + 0j) if cplx else 1.0, T, n7, X, n7,
+                         dtype="z" if cplx else "d")
+        scratch = torch.empty_like(B0)
+        t_copy = wall(lambda: (scratch.copy_(B0), torch.cuda.synchronize()), reps)
+        del scratch
+        t = max(wall(solve, reps) - t_copy, 1e-9)  # X holds the last solve
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ref = torch.linalg.solve_triangular(torch.tril(T), B0, upper=False)
+        torch.cuda.synchronize()
+        t_ref = time.perf_counter() - t0
+        err = float((torch.linalg.norm(X - ref) / torch.linalg.norm(ref)).item())
+        fl = (4.0 if cplx else 1.0) * float(n7) ** 3
+        out[name] = {"n": n7, "ms": round(t * 1e3, 3), "tflops": round(fl / t / 1e12, 2),
+                     "cublas_fp64_ms": round(t_ref * 1e3, 2), "cublas_fp64_tflops": round(fl / t_ref / 1e12, 2),
+                     "rel_diff_vs_cublas": err,
+                     "form": "recursive blocked solve: diagonal blocks (512 rows; 256 complex) inverted on the "
+                             "FP64 pipe, products in the FP64-accurate split form"}
+        del T, B0, X, ref
+    # vectors: ddot and daxpy over 2^27 doubles (1 GiB each), bytes moved / time
+    n8 = 1 << 27
+    vx, vy = dev_uniform(n8), dev_uniform(n8)
+    t = wall(lambda: G.cblas_dot(n8, vx, 1, vy, 1), 10)
+    gbs = 16.0 * n8 / t / 1e9
+    r = G.cblas_dot(n8, vx, 1, vy, 1)
+    out["ddot"] = {"n": n8, "ms": round(t * 1e3, 4), "gbs": round(gbs, 1),
+                   "frac_of_hbm": round(gbs / float(peaks.get("hbm_gbs", 6800.0)), 3),
+                   "rel_diff_vs_torch": abs(r - float(torch.dot(vx, vy).item())) / float(torch.sum(torch.abs(vx * vy)))}
+    t = wall(lambda: G.cblas_axpy(n8, 0.5, vx, 1, vy, 1), 10)
+    gbs = 24.0 * n8 / t / 1e9
+    out["daxpy"] = {"n": n8, "ms": round(t * 1e3, 4), "gbs": round(gbs, 1),
+                    "frac_of_hbm": round(gbs / float(peaks.get("hbm_gbs", 6800.0)), 3)}
+    del vx, vy
     out["inputs"] = "uniform [-1,1] generated on the device (torch.Generator, the bench seed)"
     return out
 

@@ -133,6 +133,26 @@ def lib() -> ct.CDLL:
     for nm in ("cblas_strmv", "cblas_dtrmv", "cblas_ctrmv", "cblas_ztrmv"):
         getattr(L, nm).argtypes = [ct.c_int] * 4 + [I32, VP, I32, VP, I32]
         getattr(L, nm).restype = None
+    for nm, T in (("cblas_dtrsm", D), ("cblas_strsm", F)):
+        getattr(L, nm).argtypes = [ct.c_int] * 5 + [I32, I32, T, VP, I32, VP, I32]
+        getattr(L, nm).restype = None
+    for nm in ("cblas_ztrsm", "cblas_ctrsm"):
+        getattr(L, nm).argtypes = [ct.c_int] * 5 + [I32, I32, VP, VP, I32, VP, I32]
+        getattr(L, nm).restype = None
+    for nm, T in (("cblas_daxpy", D), ("cblas_saxpy", F)):
+        getattr(L, nm).argtypes = [I32, T, VP, I32, VP, I32]
+        getattr(L, nm).restype = None
+    for nm in ("cblas_zaxpy", "cblas_caxpy"):
+        getattr(L, nm).argtypes = [I32, VP, VP, I32, VP, I32]
+        getattr(L, nm).restype = None
+    L.cblas_ddot.argtypes = [I32, VP, I32, VP, I32]
+    L.cblas_ddot.restype = D
+    L.cblas_sdot.argtypes = [I32, VP, I32, VP, I32]
+    L.cblas_sdot.restype = F
+    for nm in ("cblas_zdotu_sub", "cblas_zdotc_sub", "cblas_cdotu_sub", "cblas_cdotc_sub",
+               "cblas_zdotu", "cblas_zdotc", "cblas_cdotu", "cblas_cdotc"):
+        getattr(L, nm).argtypes = [I32, VP, I32, VP, I32, VP]
+        getattr(L, nm).restype = None
     L.gb300_dgemm_ex.argtypes = [ct.c_int, ct.c_int, ct.c_int, I64, I64, I64, D, VP, I64, VP, I64, D, VP, I64,
                                  ct.POINTER(GemmOpts)]
     L.gb300_dgemm_ex.restype = ct.c_int
@@ -343,6 +363,51 @@ def cblas_ztrmm(order, side, uplo, transA, diag, m, n, alpha, A, lda, B, ldb, si
     getattr(L, "cblas_ctrmm" if single else "cblas_ztrmm")(order, side, uplo, transA, diag, m, n, al.ctypes.data,
                                                           _addr(A), lda, _addr(B), ldb)
     _raise_on_error()
+
+
+def cblas_trsm(order, side, uplo, transA, diag, m, n, alpha, A, lda, B, ldb, dtype="d") -> None:
+    """cblas_?trsm: B = alpha op(A)^-1 B (side 141) or alpha B op(A)^-1 (142), A triangular.
+    dtype "d" / "s" (alpha a number) or "z" / "c" (alpha a complex number)."""
+    L = lib()
+    import numpy as np
+    L.gb300_clear_error()
+    if dtype in ("z", "c"):
+        al = np.array([alpha], dtype=np.complex128 if dtype == "z" else np.complex64)
+        getattr(L, "cblas_%strsm" % dtype)(order, side, uplo, transA, diag, m, n, al.ctypes.data, _addr(A), lda,
+                                           _addr(B), ldb)
+    else:
+        getattr(L, "cblas_%strsm" % dtype)(order, side, uplo, transA, diag, m, n, alpha, _addr(A), lda, _addr(B), ldb)
+    _raise_on_error()
+
+
+def cblas_axpy(n, alpha, x, incx, y, incy, dtype="d") -> None:
+    """cblas_?axpy: y = alpha x + y (strided; dtype "d", "s", "z" or "c")."""
+    L = lib()
+    import numpy as np
+    L.gb300_clear_error()
+    if dtype in ("z", "c"):
+        al = np.array([alpha], dtype=np.complex128 if dtype == "z" else np.complex64)
+        getattr(L, "cblas_%saxpy" % dtype)(n, al.ctypes.data, _addr(x), incx, _addr(y), incy)
+    else:
+        getattr(L, "cblas_%saxpy" % dtype)(n, alpha, _addr(x), incx, _addr(y), incy)
+    _raise_on_error()
+
+
+def cblas_dot(n, x, incx, y, incy, dtype="d", conj=False, sub=True):
+    """The dot products: cblas_ddot / cblas_sdot (a float), or cblas_?dotu / cblas_?dotc (conj=True)
+    for dtype "z" / "c" (a complex; sub=False calls the value-named form)."""
+    L = lib()
+    import numpy as np
+    L.gb300_clear_error()
+    if dtype in ("d", "s"):
+        r = getattr(L, "cblas_%sdot" % dtype)(n, _addr(x), incx, _addr(y), incy)
+        _raise_on_error()
+        return float(r)
+    out = np.zeros(1, dtype=np.complex128 if dtype == "z" else np.complex64)
+    name = "cblas_%sdot%s%s" % (dtype, "c" if conj else "u", "_sub" if sub else "")
+    getattr(L, name)(n, _addr(x), incx, _addr(y), incy, out.ctypes.data)
+    _raise_on_error()
+    return complex(out[0])
 
 
 def dgemm_native_noalloc(order, transA, transB, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc,

@@ -8,6 +8,11 @@
 //                                                     blaze/math/blas/cblas/gemm.h:196-256
 //   cblas_?trmm   B = alpha op(A) B or alpha B op(A), A triangular (real and complex)
 //                                                     blaze/math/blas/cblas/trmm.h:116-235
+//   cblas_?trsm   B = alpha op(A)^-1 B or alpha B op(A)^-1 (real and complex)
+//                                                     blaze/math/blas/cblas/trsm.h:111-236
+//   cblas_?axpy   y = alpha x + y                     blaze/math/blas/cblas/axpy.h:100-200
+//   cblas_?dot, cblas_?dotu_sub, cblas_?dotc_sub      blaze/math/blas/cblas/dotu.h:97-210,
+//                                                     blaze/math/blas/cblas/dotc.h:97-210
 //
 // Semantics follow CBLAS (argument positions as in xerbla, quick returns, beta == 0 does not read
 // the output, alpha == 0 does not read the inputs).  Complex products are four real products of
@@ -578,6 +583,253 @@ int ctrmm_entry(int order, int side, int uplo, int transA, int diag, int64_t m, 
     return st == GB300_OK ? GB300_OK : fail(st, err);
 }
 
+// ---- axpy and the dot products -----------------------------------------------------------------
+// y = alpha x + y over n elements of strided vectors (CBLAS: n <= 0 or alpha == 0 leave y as it is).
+template <typename T, bool CPLX>
+int axpy_entry(int64_t n, const T* alpha, const T* x, int64_t incx, T* y, int64_t incy, const char* routine) {
+    const CallTrace trace(routine, n, 1, 1);
+    auto fail = [&](int st, const std::string& msg) {
+        set_error(st, std::string(routine) + ": " + msg);
+        return st;
+    };
+    if (alpha == nullptr) return fail(GB300_ERR_INVALID_ARG, "parameter 2 (alpha) is NULL");
+    clear_error();
+    if (n <= 0 || scalar_is<T, CPLX>(alpha, T(0))) return GB300_OK;
+    if (x == nullptr || y == nullptr) return fail(GB300_ERR_INVALID_ARG, "x or y is NULL");
+
+    Runtime& r = runtime();
+    std::lock_guard<std::mutex> lock(r.mu);
+    std::string err;
+    int st = ensure_init(&err);
+    if (st != GB300_OK) return fail(st, err);
+    cudaStream_t s = r.stream;
+    fresh_ctl(s);
+    const size_t elem = (CPLX ? 2 : 1) * sizeof(T);
+    const int64_t w = CPLX ? 2 : 1;
+    const int64_t ax = incx < 0 ? -incx : incx, ay = incy < 0 ? -incy : incy;
+    const int64_t xspan = 1 + (n - 1) * ax, yspan = 1 + (n - 1) * ay;
+    const T* dx = static_cast<const T*>(stage(x, 1, xspan, xspan, elem, kAuxX, in_place(x, elem), s, &err));
+    const bool ydev = in_place(y, elem);
+    T* dy = dx ? static_cast<T*>(stage(y, 1, yspan, yspan, elem, kAuxY, ydev, s, &err)) : nullptr;
+    if (!dx || !dy) return fail(GB300_ERR_NO_MEMORY, err);
+    // logical element 0 sits at the far end of a vector with a negative stride
+    cudaError_t e = launch_axpy<T, CPLX>(n, alpha, dx + (incx < 0 ? (n - 1) * ax : 0) * w, incx,
+                                         dy + (incy < 0 ? (n - 1) * ay : 0) * w, incy, s);
+    if (e != cudaSuccess) return fail(GB300_ERR_CUDA, std::string("axpy launch: ") + cudaGetErrorString(e));
+    if (!ydev && (e = unstage(y, dy, 1, yspan, yspan, elem, s)) != cudaSuccess)
+        return fail(GB300_ERR_CUDA, std::string("copy of y back: ") + cudaGetErrorString(e));
+    st = finish(s, &err);
+    return st == GB300_OK ? GB300_OK : fail(st, err);
+}
+
+// *result = sum_i op(x_i) y_i (op = conjugation when CONJ), summed in double precision in a fixed
+// order and rounded once to T; n <= 0 gives zero.
+template <typename T, bool CPLX, bool CONJ>
+int dot_entry(int64_t n, const T* x, int64_t incx, const T* y, int64_t incy, T* result, const char* routine) {
+    const CallTrace trace(routine, n, 1, 1);
+    auto fail = [&](int st, const std::string& msg) {
+        set_error(st, std::string(routine) + ": " + msg);
+        return st;
+    };
+    if (result == nullptr) return fail(GB300_ERR_INVALID_ARG, "the result pointer is NULL");
+    result[0] = T(0);
+    if (CPLX) result[1] = T(0);
+    clear_error();
+    if (n <= 0) return GB300_OK;
+    if (x == nullptr || y == nullptr) return fail(GB300_ERR_INVALID_ARG, "x or y is NULL");
+
+    Runtime& r = runtime();
+    std::lock_guard<std::mutex> lock(r.mu);
+    std::string err;
+    int st = ensure_init(&err);
+    if (st != GB300_OK) return fail(st, err);
+    cudaStream_t s = r.stream;
+    fresh_ctl(s);
+    const size_t elem = (CPLX ? 2 : 1) * sizeof(T);
+    const int64_t w = CPLX ? 2 : 1;
+    const int64_t ax = incx < 0 ? -incx : incx, ay = incy < 0 ? -incy : incy;
+    const int64_t xspan = 1 + (n - 1) * ax, yspan = 1 + (n - 1) * ay;
+    const T* dx = static_cast<const T*>(stage(x, 1, xspan, xspan, elem, kAuxX, in_place(x, elem), s, &err));
+    const T* dy = dx ? static_cast<const T*>(stage(y, 1, yspan, yspan, elem, kAuxY, in_place(y, elem), s, &err))
+                     : nullptr;
+    const int parts = dot_parts(n);
+    double* part = static_cast<double*>(r.aux.get(kAuxP, size_t(parts + 1) * size_t(w) * sizeof(double), &err));
+    if (!dx || !dy || !part) return fail(GB300_ERR_NO_MEMORY, err);
+    double* out = part + size_t(parts) * size_t(w);
+    cudaError_t e = launch_dot<T, CPLX, CONJ>(n, dx + (incx < 0 ? (n - 1) * ax : 0) * w, incx,
+                                              dy + (incy < 0 ? (n - 1) * ay : 0) * w, incy, part, out, s);
+    if (e != cudaSuccess) return fail(GB300_ERR_CUDA, std::string("dot launch: ") + cudaGetErrorString(e));
+    st = finish(s, &err);
+    if (st != GB300_OK) return fail(st, err);
+    double v[2] = {0.0, 0.0};
+    if ((e = cudaMemcpy(v, out, size_t(w) * sizeof(double), cudaMemcpyDeviceToHost)) != cudaSuccess)
+        return fail(GB300_ERR_CUDA, std::string("copy of the result: ") + cudaGetErrorString(e));
+    result[0] = T(v[0]);
+    if (CPLX) result[1] = T(v[1]);
+    return GB300_OK;
+}
+
+// ---- trsm --------------------------------------------------------------------------------------
+namespace {
+// A triangular system in row-major storage: op(SA) X = SB (left) or X op(SA) = SB (right), X
+// overwriting SB (sbr x sbc, pitch ldb); SA ka x ka (pitch lda), `lower` its stored triangle.
+struct SolveForm {
+    bool left = true, lower = true, trans = false, conj = false, unit = false;
+};
+
+// Recursive blocked solve.  [lo, hi) is a range of op(SA)'s rows and columns whose right-hand sides
+// (rows of SB when left, columns when right) are to be solved.  It is halved at a multiple of the
+// leaf size solve_block().  The half whose unknowns do not depend on the other is solved first, then one
+// product subtracts its contribution from the other half's right-hand sides (alpha = -1,
+// beta = 1), then the other half is solved.  A range of at most one leaf is multiplied by its
+// block's inverse, into `tmp` and copied back.
+template <typename T, bool CPLX>
+int solve_range(const SolveForm& f, int64_t lo, int64_t hi, int64_t sbr, int64_t sbc, const T* SA, int64_t lda,
+                T* SB, int64_t ldb, const T* inv, T* tmp, const LaunchCtl& ctl, cudaStream_t s, std::string* err) {
+    const int64_t w = CPLX ? 2 : 1;
+    const size_t elem = size_t(w) * sizeof(T);
+    const int nb = solve_block(elem);
+    // C (M x N, pitch ldc) = -X Y + C (update) or X Y (leaf); X and Y stored at pitches lx / ly
+    auto product = [&](int64_t M, int64_t N, int64_t K, bool tx, bool ty, bool cx, bool cy, const T* X, int64_t lx,
+                       const T* Y, int64_t ly, bool update, T* C, int64_t ldc) -> int {
+        if (CPLX) {
+            const T one[2] = {T(1), T(0)}, zero[2] = {T(0), T(0)}, minus[2] = {T(-1), T(0)};
+            return complex_product<T>(M, N, K, tx, ty, cx, cy, X, lx, Y, ly, update ? minus : one,
+                                      update ? one : zero, C, ldc, true, ctl, s, err);
+        }
+        Gemm g;
+        g.m = M; g.n = N; g.k = K; g.ta = tx; g.tb = ty;
+        g.A = X; g.lda = lx; g.B = Y; g.ldb = ly; g.C = C; g.ldc = ldc;
+        g.alpha = update ? -1.0 : 1.0;
+        g.beta = update ? 1.0 : 0.0;
+        return real_product<T>(g, ctl, s, err);
+    };
+    // the block of op(SA) at rows i0.., columns j0.. as a product operand (stored transposed when
+    // op transposes)
+    auto block = [&](int64_t i0, int64_t j0) { return SA + (f.trans ? j0 * lda + i0 : i0 * lda + j0) * w; };
+    auto rows_of = [&](int64_t i) { return SB + i * ldb * w; };  // left: right-hand sides are rows
+    auto cols_of = [&](int64_t j) { return SB + j * w; };        // right: they are columns
+    if (hi - lo <= nb) {
+        const int64_t nk = hi - lo;
+        const T* Ib = inv + (lo / nb) * int64_t(nb) * nb * w;
+        int st;
+        cudaError_t e;
+        if (f.left) {
+            if ((st = product(nk, sbc, nk, false, false, false, false, Ib, nb, rows_of(lo), ldb, false, tmp, sbc)) != GB300_OK)
+                return st;
+            e = cudaMemcpy2DAsync(rows_of(lo), size_t(ldb) * elem, tmp, size_t(sbc) * elem, size_t(sbc) * elem,
+                                  size_t(nk), cudaMemcpyDeviceToDevice, s);
+        } else {
+            if ((st = product(sbr, nk, nk, false, false, false, false, cols_of(lo), ldb, Ib, nb, false, tmp, nk)) != GB300_OK)
+                return st;
+            e = cudaMemcpy2DAsync(cols_of(lo), size_t(ldb) * elem, tmp, size_t(nk) * elem, size_t(nk) * elem,
+                                  size_t(sbr), cudaMemcpyDeviceToDevice, s);
+        }
+        if (e != cudaSuccess) {
+            if (err) *err = std::string("solve copy: ") + cudaGetErrorString(e);
+            return GB300_ERR_CUDA;
+        }
+        return GB300_OK;
+    }
+    const int64_t blocks = (hi - lo + nb - 1) / nb, h = lo + int64_t(nb) * ((blocks + 1) / 2);
+    const bool eff_lower = f.lower != f.trans;  // op(SA) lower triangular
+    // the half solved first: the top one when op(SA) is lower and the system is a left one
+    const bool top_first = eff_lower == f.left;
+    auto solve = [&](int64_t a, int64_t b) {
+        return solve_range<T, CPLX>(f, a, b, sbr, sbc, SA, lda, SB, ldb, inv, tmp, ctl, s, err);
+    };
+    int st = top_first ? solve(lo, h) : solve(h, hi);
+    if (st != GB300_OK) return st;
+    if (f.left) {
+        // the other half's rows -= op(SA)[other, first] X[first]
+        st = top_first ? product(hi - h, sbc, h - lo, f.trans, false, f.conj, false, block(h, lo), lda, rows_of(lo), ldb,
+                                 true, rows_of(h), ldb)
+                       : product(h - lo, sbc, hi - h, f.trans, false, f.conj, false, block(lo, h), lda, rows_of(h), ldb,
+                                 true, rows_of(lo), ldb);
+    } else {
+        // the other half's columns -= X[first] op(SA)[first, other]
+        st = top_first ? product(sbr, hi - h, h - lo, false, f.trans, false, f.conj, cols_of(lo), ldb, block(lo, h), lda,
+                                 true, cols_of(h), ldb)
+                       : product(sbr, h - lo, hi - h, false, f.trans, false, f.conj, cols_of(h), ldb, block(h, lo), lda,
+                                 true, cols_of(lo), ldb);
+    }
+    if (st != GB300_OK) return st;
+    return top_first ? solve(h, hi) : solve(lo, h);
+}
+}  // namespace
+
+// B = alpha op(A)^-1 B (left) or alpha B op(A)^-1 (right), A triangular (m x m or n x n): B scaled
+// by alpha, the diagonal blocks of op(A) inverted, then the recursive blocked solve above.
+// alpha == 0 sets B to zero without reading A.
+template <typename T, bool CPLX>
+int trsm_entry(int order, int side, int uplo, int transA, int diag, int64_t m, int64_t n, const T* alpha, const T* A,
+               int64_t lda, T* B, int64_t ldb, const char* routine) {
+    const CallTrace trace(routine, m, n, side == CblasLeft ? m : n);
+    auto fail = [&](int st, const std::string& msg) {
+        set_error(st, std::string(routine) + ": " + msg);
+        return st;
+    };
+    if (order != CblasRowMajor && order != CblasColMajor) return fail(GB300_ERR_INVALID_ARG, "parameter 1 (order) is invalid");
+    if (side != CblasLeft && side != CblasRight) return fail(GB300_ERR_INVALID_ARG, "parameter 2 (side) is invalid");
+    if (uplo != CblasUpper && uplo != CblasLower) return fail(GB300_ERR_INVALID_ARG, "parameter 3 (uplo) is invalid");
+    if (transA != CblasNoTrans && transA != CblasTrans && transA != CblasConjTrans)
+        return fail(GB300_ERR_INVALID_ARG, "parameter 4 (transA) is invalid");
+    if (diag != CblasUnit && diag != CblasNonUnit) return fail(GB300_ERR_INVALID_ARG, "parameter 5 (diag) is invalid");
+    if (m < 0) return fail(GB300_ERR_INVALID_ARG, "parameter 6 (m) is negative");
+    if (n < 0) return fail(GB300_ERR_INVALID_ARG, "parameter 7 (n) is negative");
+    const bool rm = order == CblasRowMajor, left = side == CblasLeft;
+    const int64_t ka = left ? m : n;
+    if (lda < std::max<int64_t>(1, ka)) return fail(GB300_ERR_INVALID_ARG, "parameter 10 (lda) is too small");
+    if (ldb < std::max<int64_t>(1, rm ? n : m)) return fail(GB300_ERR_INVALID_ARG, "parameter 12 (ldb) is too small");
+    if (alpha == nullptr) return fail(GB300_ERR_INVALID_ARG, "parameter 8 (alpha) is NULL");
+    clear_error();
+    if (m == 0 || n == 0) return GB300_OK;
+    const bool alpha0 = scalar_is<T, CPLX>(alpha, T(0));
+    if (B == nullptr || (!alpha0 && A == nullptr)) return fail(GB300_ERR_INVALID_ARG, "A or B is NULL");
+
+    Runtime& r = runtime();
+    std::lock_guard<std::mutex> lock(r.mu);
+    std::string err;
+    int st = ensure_init(&err);
+    if (st != GB300_OK) return fail(st, err);
+    cudaStream_t s = r.stream;
+    const LaunchCtl ctl = fresh_ctl(s);
+    const size_t elem = (CPLX ? 2 : 1) * sizeof(T);
+
+    // row-major storage as for trmm: SB = B or B^T, SA = A or A^T (its triangle flips for
+    // column-major, and so does the side); the transposition and conjugation stay
+    const int64_t sbr = rm ? m : n, sbc = rm ? n : m;
+    SolveForm f;
+    f.left = rm ? left : !left;
+    f.lower = rm ? (uplo == CblasLower) : (uplo == CblasUpper);
+    f.trans = transA != CblasNoTrans;
+    f.conj = CPLX && transA == CblasConjTrans;
+    f.unit = diag == CblasUnit;
+    const bool bdev = in_place(B, elem);
+    T* dB = static_cast<T*>(stage(B, sbr, sbc, ldb, elem, kAuxB, bdev, s, &err));
+    if (!dB) return fail(GB300_ERR_NO_MEMORY, err);
+    cudaError_t e = cudaSuccess;
+    if (alpha0) {
+        e = cudaMemset2DAsync(dB, size_t(ldb) * elem, 0, size_t(sbc) * elem, size_t(sbr), s);
+    } else {
+        const T* dA = static_cast<const T*>(stage(A, ka, ka, lda, elem, kAuxA, in_place(A, elem), s, &err));
+        const int64_t nb = solve_block(elem), nblk = (ka + nb - 1) / nb;
+        T* inv = static_cast<T*>(r.aux.get(kAuxT, size_t(nblk) * size_t(nb) * size_t(nb) * elem, &err));
+        T* tmp = static_cast<T*>(r.aux.get(kAuxC, size_t(f.left ? sbc : sbr) * size_t(std::min<int64_t>(nb, ka)) * elem, &err));
+        if (!dA || !inv || !tmp) return fail(GB300_ERR_NO_MEMORY, err);
+        if (!scalar_is<T, CPLX>(alpha, T(1))) e = launch_scale<T, CPLX>(sbr, sbc, alpha, dB, ldb, s);
+        if (e == cudaSuccess)
+            e = launch_tri_inverse<T, CPLX>(ka, int(nb), dA, lda, f.trans, f.conj, f.lower == f.trans, f.unit, inv, s);
+        if (e != cudaSuccess) return fail(GB300_ERR_CUDA, std::string("trsm launch: ") + cudaGetErrorString(e));
+        if ((st = solve_range<T, CPLX>(f, 0, ka, sbr, sbc, dA, lda, dB, ldb, inv, tmp, ctl, s, &err)) != GB300_OK)
+            return fail(st, err);
+    }
+    if (e == cudaSuccess && !bdev) e = unstage(B, dB, sbr, sbc, ldb, elem, s);
+    if (e != cudaSuccess) return fail(GB300_ERR_CUDA, std::string("copy of B back: ") + cudaGetErrorString(e));
+    st = finish(s, &err);
+    return st == GB300_OK ? GB300_OK : fail(st, err);
+}
+
 template int gemv_entry<double>(int, int, int64_t, int64_t, double, const double*, int64_t, const double*, int64_t,
                                 double, double*, int64_t, const char*);
 template int gemv_entry<float>(int, int, int64_t, int64_t, float, const float*, int64_t, const float*, int64_t, float,
@@ -604,4 +856,25 @@ template int ctrmm_entry<double>(int, int, int, int, int, int64_t, int64_t, cons
                                  double*, int64_t, const char*);
 template int ctrmm_entry<float>(int, int, int, int, int, int64_t, int64_t, const float*, const float*, int64_t, float*,
                                 int64_t, const char*);
+template int axpy_entry<double, false>(int64_t, const double*, const double*, int64_t, double*, int64_t, const char*);
+template int axpy_entry<float, false>(int64_t, const float*, const float*, int64_t, float*, int64_t, const char*);
+template int axpy_entry<double, true>(int64_t, const double*, const double*, int64_t, double*, int64_t, const char*);
+template int axpy_entry<float, true>(int64_t, const float*, const float*, int64_t, float*, int64_t, const char*);
+#define GB_DOT(T, C, J) \
+    template int dot_entry<T, C, J>(int64_t, const T*, int64_t, const T*, int64_t, T*, const char*);
+GB_DOT(double, false, false)
+GB_DOT(float, false, false)
+GB_DOT(double, true, false)
+GB_DOT(double, true, true)
+GB_DOT(float, true, false)
+GB_DOT(float, true, true)
+#undef GB_DOT
+#define GB_TRSM(T, C)                                                                                          \
+    template int trsm_entry<T, C>(int, int, int, int, int, int64_t, int64_t, const T*, const T*, int64_t, T*, \
+                                  int64_t, const char*);
+GB_TRSM(double, false)
+GB_TRSM(float, false)
+GB_TRSM(double, true)
+GB_TRSM(float, true)
+#undef GB_TRSM
 }  // namespace gb

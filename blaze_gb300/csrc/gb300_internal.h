@@ -97,6 +97,16 @@ int trmv_entry(int order, int uplo, int transA, int diag, int64_t n, const T* A,
 template <typename T>
 int ctrmm_entry(int order, int side, int uplo, int transA, int diag, int64_t m, int64_t n, const T* alpha, const T* A,
                 int64_t lda, T* B, int64_t ldb, const char* routine);
+// B = alpha op(A)^-1 B or alpha B op(A)^-1, A triangular; alpha points to one T, or (re, im) for CPLX
+template <typename T, bool CPLX>
+int trsm_entry(int order, int side, int uplo, int transA, int diag, int64_t m, int64_t n, const T* alpha, const T* A,
+               int64_t lda, T* B, int64_t ldb, const char* routine);
+// y = alpha x + y; alpha points to one T, or (re, im) for CPLX
+template <typename T, bool CPLX>
+int axpy_entry(int64_t n, const T* alpha, const T* x, int64_t incx, T* y, int64_t incy, const char* routine);
+// *result = sum_i op(x_i) y_i, op = conjugation when CONJ; result holds one T, or (re, im) for CPLX
+template <typename T, bool CPLX, bool CONJ>
+int dot_entry(int64_t n, const T* x, int64_t incx, const T* y, int64_t incy, T* result, const char* routine);
 
 template <typename T>
 int gemm_entry(int order, int transA, int transB, int64_t m, int64_t n, int64_t k, T alpha, const T* A, int64_t lda,

@@ -1,8 +1,10 @@
-// level23.h — launchers of the ?gemv / ?trmv, complex ?gemm and ?trmm kernels (level23.cu).
+// level23.h — launchers of the kernels of the BLAS routines next to ?gemm: ?gemv / ?trmv, complex
+// ?gemm and ?trmm (level23.cu), ?axpy and the dot products (level1.cu), ?trsm (trsm.cu).
 #pragma once
 
 #include <cuda_runtime.h>
 
+#include <cstddef>
 #include <cstdint>
 
 namespace gb {
@@ -42,5 +44,38 @@ cudaError_t launch_complex_epilogue(int64_t rows, int64_t cols, const T* Pr, con
 // the diagonal when `unit` (CPLX: interleaved complex elements).
 template <typename T, bool CPLX>
 cudaError_t launch_triangle(int64_t n, const T* A, int64_t lda, bool lower, bool unit, T* out, cudaStream_t st);
+
+// ---- level1.cu ---------------------------------------------------------------------------------
+// y[i incy] += alpha x[i incx] for i < n (CPLX: interleaved complex, alpha points at (re, im)); the
+// pointers address logical element 0.  incy == 0 applies the n updates to y[0] in order.
+template <typename T, bool CPLX>
+cudaError_t launch_axpy(int64_t n, const T* alpha, const T* x, int64_t incx, T* y, int64_t incy, cudaStream_t st);
+
+// Block sums of a dot product of length n (the size of `part` in sums).
+int dot_parts(int64_t n);
+
+// out = sum_i op(x_i) y_i in double precision (one double, or re / im for CPLX), op = conjugation
+// when CONJ, summed in a fixed order; `part` holds dot_parts(n) sums (two doubles each for CPLX).
+template <typename T, bool CPLX, bool CONJ>
+cudaError_t launch_dot(int64_t n, const T* x, int64_t incx, const T* y, int64_t incy, double* part, double* out,
+                       cudaStream_t st);
+
+// ---- trsm.cu -----------------------------------------------------------------------------------
+// Rows of the diagonal blocks that a triangular solve inverts (its recursion's leaves) for elements
+// of `elem` bytes: 512, or 256 for complex double, whose inversion would not fit shared memory at
+// 512 rows.  Larger leaves mean fewer, larger products for the same work.
+constexpr int solve_block(size_t elem) { return elem > 8 ? 256 : 512; }
+
+// X (rows x cols, pitch ld) = alpha X.
+template <typename T, bool CPLX>
+cudaError_t launch_scale(int64_t rows, int64_t cols, const T* alpha, T* X, int64_t ld, cudaStream_t st);
+
+// Dense inverses of the diagonal blocks (nb x nb, nb a multiple of 32 up to solve_block(); the last
+// block may be smaller) of the triangular op(SA): SA ka x ka in row-major storage, op = transpose
+// (trans) and conjugation (conj), `upper` when op(SA) is upper triangular, `unit` for a unit
+// diagonal (not read).  Block b's inverse goes to inv + b nb nb (pitch nb).
+template <typename T, bool CPLX>
+cudaError_t launch_tri_inverse(int64_t ka, int nb, const T* SA, int64_t lda, bool trans, bool conj, bool upper,
+                               bool unit, T* inv, cudaStream_t st);
 
 }  // namespace gb

@@ -36,6 +36,8 @@ UNITS = [
     ("grouped.cu", "grouped.o", []),
     ("serve.cpp", "serve.o", []),
     ("level23.cu", "level23.o", []),
+    ("level1.cu", "level1.o", []),
+    ("trsm.cu", "trsm.o", []),
     ("api_next.cpp", "api_next.o", []),
 ]
 

@@ -9,11 +9,10 @@
  *
  * Implemented on the GPU: cblas_dgemm and cblas_sgemm (the dense matrix-multiplication path,
  * reached from blaze::gemm(), blaze/math/blas/gemm.h:105-131, and blaze/math/blas/cblas/gemm.h:
- * 116-162), and the other routines Blaze's expressions call: cblas_?gemv, cblas_?trmv,
- * cblas_cgemm / cblas_zgemm and cblas_?trmm.  The remaining routines Blaze's wrappers name
- * (?trsm, ?axpy, the dot products) are declared so that Blaze compiles; the library defines them
- * as stubs that record GB300_ERR_NOT_SUPPORTED (see gb300_last_error()) and compute nothing —
- * there is no CPU fallback.
+ * 116-162), the other routines Blaze's expressions call (cblas_?gemv, cblas_?trmv, cblas_cgemm /
+ * cblas_zgemm, cblas_?trmm), and the rest of what Blaze's wrappers name: cblas_?trsm (blaze::trsm),
+ * cblas_?axpy (blaze::axpy) and the dot products (blaze::dotu, blaze::dotc).  There is no CPU
+ * fallback.
  *
  * Integer type: `blas_int_t` is int32 unless BLAZE_BLAS_IS_64BIT is set, matching
  * blaze/math/blas/Types.h:56-64.  The library exports the 32-bit ABI under the standard names;
@@ -117,6 +116,24 @@ void gb300_clear_error(void);
 #define gb300_cblas_dtrmv_checked gb300_cblas_dtrmv_checked_64
 #define gb300_cblas_ctrmv_checked gb300_cblas_ctrmv_checked_64
 #define gb300_cblas_ztrmv_checked gb300_cblas_ztrmv_checked_64
+#define gb300_cblas_strsm_checked gb300_cblas_strsm_checked_64
+#define gb300_cblas_saxpy_checked gb300_cblas_saxpy_checked_64
+#define gb300_cblas_dtrsm_checked gb300_cblas_dtrsm_checked_64
+#define gb300_cblas_daxpy_checked gb300_cblas_daxpy_checked_64
+#define gb300_cblas_ctrsm_checked gb300_cblas_ctrsm_checked_64
+#define gb300_cblas_caxpy_checked gb300_cblas_caxpy_checked_64
+#define gb300_cblas_ztrsm_checked gb300_cblas_ztrsm_checked_64
+#define gb300_cblas_zaxpy_checked gb300_cblas_zaxpy_checked_64
+#define gb300_cblas_sdot_checked gb300_cblas_sdot_checked_64
+#define gb300_cblas_ddot_checked gb300_cblas_ddot_checked_64
+#define gb300_cblas_cdotu_sub_checked gb300_cblas_cdotu_sub_checked_64
+#define gb300_cblas_cdotu_checked gb300_cblas_cdotu_checked_64
+#define gb300_cblas_cdotc_sub_checked gb300_cblas_cdotc_sub_checked_64
+#define gb300_cblas_cdotc_checked gb300_cblas_cdotc_checked_64
+#define gb300_cblas_zdotu_sub_checked gb300_cblas_zdotu_sub_checked_64
+#define gb300_cblas_zdotu_checked gb300_cblas_zdotu_checked_64
+#define gb300_cblas_zdotc_sub_checked gb300_cblas_zdotc_sub_checked_64
+#define gb300_cblas_zdotc_checked gb300_cblas_zdotc_checked_64
 #endif
 
 /* Under GB300_BLAS_THROW (C++), each routine that runs on the GPU is declared as
@@ -151,9 +168,9 @@ void cblas_dgemm(CBLAS_ORDER order, CBLAS_TRANSPOSE transA, CBLAS_TRANSPOSE tran
                  gb300_blas_int lda, const double* B, gb300_blas_int ldb, double beta, double* C,
                  gb300_blas_int ldc);
 
-/* ---- Blaze's other wrappers.  On the GPU: ?gemv, ?trmv, complex ?gemm and ?trmm, real and
- * complex (complex operands are interleaved (re, im) pairs, alpha / beta point at one pair).
- * Declared only, stubs that record GB300_ERR_NOT_SUPPORTED: ?trsm, ?axpy and the dot products. */
+/* ---- Blaze's other wrappers, all on the GPU: ?gemv, ?trmv, complex ?gemm, ?trmm, ?trsm, ?axpy
+ * and the dot products, real and complex (complex operands are interleaved (re, im) pairs, alpha /
+ * beta point at one pair). */
 /* blaze/math/blas/cblas/gemm.h:201,243 */
 void GB300_ENTRY(cblas_cgemm)(CBLAS_ORDER order, CBLAS_TRANSPOSE transA, CBLAS_TRANSPOSE transB, gb300_blas_int m,
                  gb300_blas_int n, gb300_blas_int k, const void* alpha, const void* A, gb300_blas_int lda,
@@ -196,49 +213,52 @@ void GB300_ENTRY(cblas_ctrmv)(CBLAS_ORDER order, CBLAS_UPLO uplo, CBLAS_TRANSPOS
                  const void* A, gb300_blas_int lda, void* x, gb300_blas_int incX);
 void GB300_ENTRY(cblas_ztrmv)(CBLAS_ORDER order, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA, CBLAS_DIAG diag, gb300_blas_int n,
                  const void* A, gb300_blas_int lda, void* x, gb300_blas_int incX);
-/* blaze/math/blas/cblas/trsm.h (stubs from here on) */
-void cblas_strsm(CBLAS_ORDER order, CBLAS_SIDE side, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA, CBLAS_DIAG diag,
-                 gb300_blas_int m, gb300_blas_int n, float alpha, const float* A, gb300_blas_int lda, float* B,
-                 gb300_blas_int ldb);
-void cblas_dtrsm(CBLAS_ORDER order, CBLAS_SIDE side, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA, CBLAS_DIAG diag,
-                 gb300_blas_int m, gb300_blas_int n, double alpha, const double* A, gb300_blas_int lda,
-                 double* B, gb300_blas_int ldb);
-void cblas_ctrsm(CBLAS_ORDER order, CBLAS_SIDE side, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA, CBLAS_DIAG diag,
-                 gb300_blas_int m, gb300_blas_int n, const void* alpha, const void* A, gb300_blas_int lda,
-                 void* B, gb300_blas_int ldb);
-void cblas_ztrsm(CBLAS_ORDER order, CBLAS_SIDE side, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA, CBLAS_DIAG diag,
-                 gb300_blas_int m, gb300_blas_int n, const void* alpha, const void* A, gb300_blas_int lda,
-                 void* B, gb300_blas_int ldb);
+/* blaze/math/blas/cblas/trsm.h:115,153,193,234 */
+void GB300_ENTRY(cblas_strsm)(CBLAS_ORDER order, CBLAS_SIDE side, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA,
+    CBLAS_DIAG diag, gb300_blas_int m, gb300_blas_int n, float alpha, const float* A, gb300_blas_int lda, float* B,
+    gb300_blas_int ldb);
 /* blaze/math/blas/cblas/axpy.h:103,133,165,198 */
-void cblas_saxpy(gb300_blas_int n, float alpha, const float* x, gb300_blas_int incX, float* y, gb300_blas_int incY);
-void cblas_daxpy(gb300_blas_int n, double alpha, const double* x, gb300_blas_int incX, double* y,
-                 gb300_blas_int incY);
-void cblas_caxpy(gb300_blas_int n, const void* alpha, const void* x, gb300_blas_int incX, void* y,
-                 gb300_blas_int incY);
-void cblas_zaxpy(gb300_blas_int n, const void* alpha, const void* x, gb300_blas_int incX, void* y,
-                 gb300_blas_int incY);
-/* blaze/math/blas/cblas/dotu.h:99,127 and dotc.h */
-float cblas_sdot(gb300_blas_int n, const float* x, gb300_blas_int incX, const float* y, gb300_blas_int incY);
-double cblas_ddot(gb300_blas_int n, const double* x, gb300_blas_int incX, const double* y, gb300_blas_int incY);
-/* Both forms of the complex dot products: dotu.h / dotc.h reference each under its own branch. */
-void cblas_cdotu_sub(gb300_blas_int n, const void* x, gb300_blas_int incX, const void* y, gb300_blas_int incY,
-                     void* dotu);
-void cblas_zdotu_sub(gb300_blas_int n, const void* x, gb300_blas_int incX, const void* y, gb300_blas_int incY,
-                     void* dotu);
-void cblas_cdotc_sub(gb300_blas_int n, const void* x, gb300_blas_int incX, const void* y, gb300_blas_int incY,
-                     void* dotc);
-void cblas_zdotc_sub(gb300_blas_int n, const void* x, gb300_blas_int incX, const void* y, gb300_blas_int incY,
-                     void* dotc);
-/* The value-returning complex forms exist in some CBLAS flavours; the library exports them with
- * the result written through the trailing pointer (interoperable with the _sub forms). */
-void cblas_cdotu(gb300_blas_int n, const void* x, gb300_blas_int incX, const void* y, gb300_blas_int incY,
-                 void* dotu);
-void cblas_zdotu(gb300_blas_int n, const void* x, gb300_blas_int incX, const void* y, gb300_blas_int incY,
-                 void* dotu);
-void cblas_cdotc(gb300_blas_int n, const void* x, gb300_blas_int incX, const void* y, gb300_blas_int incY,
-                 void* dotc);
-void cblas_zdotc(gb300_blas_int n, const void* x, gb300_blas_int incX, const void* y, gb300_blas_int incY,
-                 void* dotc);
+void GB300_ENTRY(cblas_saxpy)(gb300_blas_int n, float alpha, const float* x, gb300_blas_int incX, float* y,
+    gb300_blas_int incY);
+void GB300_ENTRY(cblas_dtrsm)(CBLAS_ORDER order, CBLAS_SIDE side, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA,
+    CBLAS_DIAG diag, gb300_blas_int m, gb300_blas_int n, double alpha, const double* A, gb300_blas_int lda,
+    double* B, gb300_blas_int ldb);
+void GB300_ENTRY(cblas_daxpy)(gb300_blas_int n, double alpha, const double* x, gb300_blas_int incX, double* y,
+    gb300_blas_int incY);
+void GB300_ENTRY(cblas_ctrsm)(CBLAS_ORDER order, CBLAS_SIDE side, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA,
+    CBLAS_DIAG diag, gb300_blas_int m, gb300_blas_int n, const void* alpha, const void* A, gb300_blas_int lda,
+    void* B, gb300_blas_int ldb);
+void GB300_ENTRY(cblas_caxpy)(gb300_blas_int n, const void* alpha, const void* x, gb300_blas_int incX, void* y,
+    gb300_blas_int incY);
+void GB300_ENTRY(cblas_ztrsm)(CBLAS_ORDER order, CBLAS_SIDE side, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA,
+    CBLAS_DIAG diag, gb300_blas_int m, gb300_blas_int n, const void* alpha, const void* A, gb300_blas_int lda,
+    void* B, gb300_blas_int ldb);
+void GB300_ENTRY(cblas_zaxpy)(gb300_blas_int n, const void* alpha, const void* x, gb300_blas_int incX, void* y,
+    gb300_blas_int incY);
+/* blaze/math/blas/cblas/dotu.h:99,127 and dotc.h:99,127 */
+float GB300_ENTRY(cblas_sdot)(gb300_blas_int n, const float* x, gb300_blas_int incX, const float* y,
+    gb300_blas_int incY);
+double GB300_ENTRY(cblas_ddot)(gb300_blas_int n, const double* x, gb300_blas_int incX, const double* y,
+    gb300_blas_int incY);
+/* Both forms of the complex dot products: dotu.h / dotc.h reference each under its own branch
+ * (the _sub form unless OPENBLAS_VERSION).  The value-returning forms exist in some CBLAS flavours;
+ * the library exports them with the result written through the trailing pointer. */
+void GB300_ENTRY(cblas_cdotu_sub)(gb300_blas_int n, const void* x, gb300_blas_int incX, const void* y,
+    gb300_blas_int incY, void* dotu);
+void GB300_ENTRY(cblas_cdotu)(gb300_blas_int n, const void* x, gb300_blas_int incX, const void* y,
+    gb300_blas_int incY, void* dotu);
+void GB300_ENTRY(cblas_cdotc_sub)(gb300_blas_int n, const void* x, gb300_blas_int incX, const void* y,
+    gb300_blas_int incY, void* dotc);
+void GB300_ENTRY(cblas_cdotc)(gb300_blas_int n, const void* x, gb300_blas_int incX, const void* y,
+    gb300_blas_int incY, void* dotc);
+void GB300_ENTRY(cblas_zdotu_sub)(gb300_blas_int n, const void* x, gb300_blas_int incX, const void* y,
+    gb300_blas_int incY, void* dotu);
+void GB300_ENTRY(cblas_zdotu)(gb300_blas_int n, const void* x, gb300_blas_int incX, const void* y,
+    gb300_blas_int incY, void* dotu);
+void GB300_ENTRY(cblas_zdotc_sub)(gb300_blas_int n, const void* x, gb300_blas_int incX, const void* y,
+    gb300_blas_int incY, void* dotc);
+void GB300_ENTRY(cblas_zdotc)(gb300_blas_int n, const void* x, gb300_blas_int incX, const void* y,
+    gb300_blas_int incY, void* dotc);
 
 #if defined(__GNUC__)
 #pragma GCC visibility pop
@@ -355,6 +375,102 @@ static inline void cblas_ztrmv(CBLAS_ORDER order, CBLAS_UPLO uplo, CBLAS_TRANSPO
                               gb300_blas_int n, const void* A, gb300_blas_int lda, void* x, gb300_blas_int incX) {
     gb300_cblas_ztrmv_checked(order, uplo, transA, diag, n, A, lda, x, incX);
     gb300_throw_if_error("cblas_ztrmv");
+}
+static inline void cblas_strsm(CBLAS_ORDER order, CBLAS_SIDE side, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA,
+    CBLAS_DIAG diag, gb300_blas_int m, gb300_blas_int n, float alpha, const float* A, gb300_blas_int lda, float* B,
+    gb300_blas_int ldb) {
+    gb300_cblas_strsm_checked(order, side, uplo, transA, diag, m, n, alpha, A, lda, B, ldb);
+    gb300_throw_if_error("cblas_strsm");
+}
+static inline void cblas_saxpy(gb300_blas_int n, float alpha, const float* x, gb300_blas_int incX, float* y,
+    gb300_blas_int incY) {
+    gb300_cblas_saxpy_checked(n, alpha, x, incX, y, incY);
+    gb300_throw_if_error("cblas_saxpy");
+}
+static inline void cblas_dtrsm(CBLAS_ORDER order, CBLAS_SIDE side, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA,
+    CBLAS_DIAG diag, gb300_blas_int m, gb300_blas_int n, double alpha, const double* A, gb300_blas_int lda,
+    double* B, gb300_blas_int ldb) {
+    gb300_cblas_dtrsm_checked(order, side, uplo, transA, diag, m, n, alpha, A, lda, B, ldb);
+    gb300_throw_if_error("cblas_dtrsm");
+}
+static inline void cblas_daxpy(gb300_blas_int n, double alpha, const double* x, gb300_blas_int incX, double* y,
+    gb300_blas_int incY) {
+    gb300_cblas_daxpy_checked(n, alpha, x, incX, y, incY);
+    gb300_throw_if_error("cblas_daxpy");
+}
+static inline void cblas_ctrsm(CBLAS_ORDER order, CBLAS_SIDE side, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA,
+    CBLAS_DIAG diag, gb300_blas_int m, gb300_blas_int n, const void* alpha, const void* A, gb300_blas_int lda,
+    void* B, gb300_blas_int ldb) {
+    gb300_cblas_ctrsm_checked(order, side, uplo, transA, diag, m, n, alpha, A, lda, B, ldb);
+    gb300_throw_if_error("cblas_ctrsm");
+}
+static inline void cblas_caxpy(gb300_blas_int n, const void* alpha, const void* x, gb300_blas_int incX, void* y,
+    gb300_blas_int incY) {
+    gb300_cblas_caxpy_checked(n, alpha, x, incX, y, incY);
+    gb300_throw_if_error("cblas_caxpy");
+}
+static inline void cblas_ztrsm(CBLAS_ORDER order, CBLAS_SIDE side, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA,
+    CBLAS_DIAG diag, gb300_blas_int m, gb300_blas_int n, const void* alpha, const void* A, gb300_blas_int lda,
+    void* B, gb300_blas_int ldb) {
+    gb300_cblas_ztrsm_checked(order, side, uplo, transA, diag, m, n, alpha, A, lda, B, ldb);
+    gb300_throw_if_error("cblas_ztrsm");
+}
+static inline void cblas_zaxpy(gb300_blas_int n, const void* alpha, const void* x, gb300_blas_int incX, void* y,
+    gb300_blas_int incY) {
+    gb300_cblas_zaxpy_checked(n, alpha, x, incX, y, incY);
+    gb300_throw_if_error("cblas_zaxpy");
+}
+static inline float cblas_sdot(gb300_blas_int n, const float* x, gb300_blas_int incX, const float* y,
+    gb300_blas_int incY) {
+    const float r = gb300_cblas_sdot_checked(n, x, incX, y, incY);
+    gb300_throw_if_error("cblas_sdot");
+    return r;
+}
+static inline double cblas_ddot(gb300_blas_int n, const double* x, gb300_blas_int incX, const double* y,
+    gb300_blas_int incY) {
+    const double r = gb300_cblas_ddot_checked(n, x, incX, y, incY);
+    gb300_throw_if_error("cblas_ddot");
+    return r;
+}
+static inline void cblas_cdotu_sub(gb300_blas_int n, const void* x, gb300_blas_int incX, const void* y,
+    gb300_blas_int incY, void* dotu) {
+    gb300_cblas_cdotu_sub_checked(n, x, incX, y, incY, dotu);
+    gb300_throw_if_error("cblas_cdotu_sub");
+}
+static inline void cblas_cdotu(gb300_blas_int n, const void* x, gb300_blas_int incX, const void* y,
+    gb300_blas_int incY, void* dotu) {
+    gb300_cblas_cdotu_checked(n, x, incX, y, incY, dotu);
+    gb300_throw_if_error("cblas_cdotu");
+}
+static inline void cblas_cdotc_sub(gb300_blas_int n, const void* x, gb300_blas_int incX, const void* y,
+    gb300_blas_int incY, void* dotc) {
+    gb300_cblas_cdotc_sub_checked(n, x, incX, y, incY, dotc);
+    gb300_throw_if_error("cblas_cdotc_sub");
+}
+static inline void cblas_cdotc(gb300_blas_int n, const void* x, gb300_blas_int incX, const void* y,
+    gb300_blas_int incY, void* dotc) {
+    gb300_cblas_cdotc_checked(n, x, incX, y, incY, dotc);
+    gb300_throw_if_error("cblas_cdotc");
+}
+static inline void cblas_zdotu_sub(gb300_blas_int n, const void* x, gb300_blas_int incX, const void* y,
+    gb300_blas_int incY, void* dotu) {
+    gb300_cblas_zdotu_sub_checked(n, x, incX, y, incY, dotu);
+    gb300_throw_if_error("cblas_zdotu_sub");
+}
+static inline void cblas_zdotu(gb300_blas_int n, const void* x, gb300_blas_int incX, const void* y,
+    gb300_blas_int incY, void* dotu) {
+    gb300_cblas_zdotu_checked(n, x, incX, y, incY, dotu);
+    gb300_throw_if_error("cblas_zdotu");
+}
+static inline void cblas_zdotc_sub(gb300_blas_int n, const void* x, gb300_blas_int incX, const void* y,
+    gb300_blas_int incY, void* dotc) {
+    gb300_cblas_zdotc_sub_checked(n, x, incX, y, incY, dotc);
+    gb300_throw_if_error("cblas_zdotc_sub");
+}
+static inline void cblas_zdotc(gb300_blas_int n, const void* x, gb300_blas_int incX, const void* y,
+    gb300_blas_int incY, void* dotc) {
+    gb300_cblas_zdotc_checked(n, x, incX, y, incY, dotc);
+    gb300_throw_if_error("cblas_zdotc");
 }
 }
 #endif

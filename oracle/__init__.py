@@ -81,6 +81,8 @@ def lib():
         L.orc_fro_norm_s.argtypes = [_F, _I64, _I64, _I64, ct.c_int]
         L.orc_fro_norm_s.restype = ct.c_double
         L.orc_max_threads.restype = ct.c_int
+        L.orc_trsm_left.argtypes = [ct.c_int, ct.c_int, _I64, _I64, _D, _D]
+        L.orc_trsm_left.restype = None
         _lib = L
     return _lib
 
@@ -107,6 +109,10 @@ def ref_lib():
         R.ref_trmv.restype = ct.c_int
         R.ref_trmm_z.argtypes = [ct.c_int] * 5 + [i64, i64, _D, _D, i64, _D, i64]
         R.ref_trmm_z.restype = ct.c_int
+        R.ref_dot.argtypes = [ct.c_int, ct.c_int, i64, _D, _D, _D]
+        R.ref_dot.restype = ct.c_int
+        R.ref_axpy.argtypes = [ct.c_int, i64, _D, _D, _D]
+        R.ref_axpy.restype = ct.c_int
         _ref = R
     return _ref
 
@@ -314,3 +320,87 @@ def ref_ztrmm(order, side, uplo, transA, diag, m, n, alpha, A, lda, B, ldb):
     if R.ref_trmm_z(order, side, uplo, transA, diag, m, n, _cd(al), _cd(Ad), lda, B.view(np.float64).ctypes.data_as(_D),
                     ldb) != 0:
         raise RuntimeError("Blaze raised")
+
+
+def ref_dot(x, y, conj=False):
+    """Blaze's x * y (or conj(x) * y) for unit-stride float64 / complex128 vectors."""
+    R = _ref_or_raise()
+    cplx = int(np.iscomplexobj(x))
+    out = np.zeros(2)
+    xd = np.ascontiguousarray(x).view(np.float64) if cplx else np.ascontiguousarray(x, dtype=np.float64)
+    yd = np.ascontiguousarray(y).view(np.float64) if cplx else np.ascontiguousarray(y, dtype=np.float64)
+    if R.ref_dot(cplx, int(conj), len(x), _cd(xd), _cd(yd), out.ctypes.data_as(_D)) != 0:
+        raise RuntimeError("Blaze raised")
+    return complex(out[0], out[1]) if cplx else float(out[0])
+
+
+def ref_axpy(alpha, x, y):
+    """Blaze's y += alpha * x for unit-stride float64 / complex128 vectors; y updated in place."""
+    R = _ref_or_raise()
+    cplx = int(np.iscomplexobj(y))
+    al = np.array([complex(alpha).real, complex(alpha).imag])
+    xd = np.ascontiguousarray(x).view(np.float64) if cplx else np.ascontiguousarray(x, dtype=np.float64)
+    yd = y.view(np.float64) if cplx else y
+    if R.ref_axpy(cplx, len(x), _cd(al), _cd(xd), yd.ctypes.data_as(_D)) != 0:
+        raise RuntimeError("Blaze raised")
+
+
+# ---- CBLAS-level restatements of the routines next to ?gemm that Blaze has no kernel for -------
+CONJ_TRANS = 113
+
+
+def triangle_logical(order, uplo, transA, diag, ka, A, lda) -> np.ndarray:
+    """op(A) as a dense logical ka x ka array: the `uplo` triangle of the stored A (the other half
+    is not read), ones on a unit diagonal, transposed for 112 and conjugate-transposed for 113."""
+    cplx = np.iscomplexobj(A)
+    flat = np.asarray(A).reshape(-1)
+    idx = np.arange(ka)
+    pos = (idx[:, None] * lda + idx[None, :]) if order == ROW_MAJOR else (idx[None, :] * lda + idx[:, None])
+    full = flat[pos].astype(np.complex128 if cplx else np.float64)
+    keep = np.tril(np.ones((ka, ka), dtype=bool)) if uplo == 122 else np.triu(np.ones((ka, ka), dtype=bool))
+    full = np.where(keep, full, 0)
+    if diag == 132:
+        full[idx, idx] = 1
+    if transA == TRANS:
+        full = full.T
+    elif transA == CONJ_TRANS:
+        full = full.conj().T
+    return np.ascontiguousarray(full)
+
+
+def trsm(order, side, uplo, transA, diag, m, n, alpha, A, lda, B, ldb) -> None:
+    """B = alpha op(A)^-1 B (side 141) or alpha B op(A)^-1 (142) by substitution in the oracle's C
+    restatement (orc_trsm_left), float64 or complex128; B is updated in place."""
+    left = side == 141
+    ka = m if left else n
+    cplx = np.iscomplexobj(B)
+    T = triangle_logical(order, uplo, transA, diag, ka, A, lda)
+    flat = B.reshape(-1)
+    ii, jj = np.arange(m)[:, None], np.arange(n)[None, :]
+    pos = ii * ldb + jj if order == ROW_MAJOR else jj * ldb + ii
+    X = alpha * flat[pos].astype(np.complex128 if cplx else np.float64)  # logical m x n
+    lower = (uplo == 122) == (transA == NO_TRANS)  # op(A) lower triangular
+    if not left:  # X op(A) = B  <=>  op(A)^T X^T = B^T
+        T, X, lower = np.ascontiguousarray(T.T), X.T, not lower
+    X = np.ascontiguousarray(X)
+    Tv, Xv = (T.view(np.float64), X.view(np.float64)) if cplx else (T, X)
+    lib().orc_trsm_left(int(cplx), int(lower), ka, X.shape[1], _cd(Tv), Xv.ctypes.data_as(_D))
+    flat[pos] = X if left else X.T
+
+
+def complex_uniform(count: int, seed: int) -> np.ndarray:
+    """Complex128 values with real parts uniform(seed) and imaginary parts uniform(seed + 7919)."""
+    re = uniform(max(count, 1), seed)[:count]
+    im = uniform(max(count, 1), seed + 7919)[:count]
+    return re + 1j * im
+
+
+def triangular_operands(cplx: bool, ka: int, lda: int, rows_b: int, ldb: int, seed: int):
+    """Seeded operands of a triangular solve: the stored ka x ka square of the triangle (pitch lda;
+    off-diagonal entries u / ka, diagonal 1 + u / 2, u uniform in [-1, 1], well conditioned with or
+    without a unit diagonal) and a solution X0 of rows_b x ldb stored elements."""
+    A = (complex_uniform(ka * lda, seed) if cplx else uniform(ka * lda, seed).copy()) / ka
+    d = np.arange(ka) * (lda + 1)
+    A[d] = 1 + 0.5 * ka * A[d]
+    X0 = complex_uniform(rows_b * ldb, seed + 1) if cplx else uniform(rows_b * ldb, seed + 1).copy()
+    return A, X0

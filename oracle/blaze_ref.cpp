@@ -334,4 +334,51 @@ int ref_trmm_z(int order, int side, int uplo, int tA, int diag, int64_t m, int64
     return 0;
 }
 
+// Dot products as blazetest's BLAS operation test writes them (blazetest/mathtest/blas/
+// OperationTest.h:139-140, 183-184): x * y for dotu, conj(x) * y for dotc, x a row vector;
+// real (cplx == 0) or interleaved complex doubles; the result (re, im) goes to out.
+int ref_dot(int cplx, int conj_x, int64_t n, const double* x, const double* y, double* out) {
+    using CT = std::complex<double>;
+    try {
+        if (cplx) {
+            blaze::CustomVector<CT, unaligned, unpadded, blaze::rowVector> vx(
+                const_cast<CT*>(reinterpret_cast<const CT*>(x)), n);
+            VView<CT> vy(const_cast<CT*>(reinterpret_cast<const CT*>(y)), n);
+            const CT r = conj_x ? CT(conj(vx) * vy) : CT(vx * vy);
+            out[0] = r.real();
+            out[1] = r.imag();
+        } else {
+            blaze::CustomVector<double, unaligned, unpadded, blaze::rowVector> vx(const_cast<double*>(x), n);
+            VView<double> vy(const_cast<double*>(y), n);
+            out[0] = vx * vy;
+            out[1] = 0.0;
+        }
+    } catch (const std::exception& e) {
+        std::fprintf(stderr, "blaze: %s\n", e.what());
+        return 1;
+    }
+    return 0;
+}
+
+// y += alpha * x as blazetest's BLAS operation test checks axpy (OperationTest.h:231-232); real
+// or interleaved complex doubles, alpha (re, im).
+int ref_axpy(int cplx, int64_t n, const double* alpha, const double* x, double* y) {
+    using CT = std::complex<double>;
+    try {
+        if (cplx) {
+            VView<CT> vx(const_cast<CT*>(reinterpret_cast<const CT*>(x)), n);
+            VView<CT> vy(reinterpret_cast<CT*>(y), n);
+            vy += CT(alpha[0], alpha[1]) * vx;
+        } else {
+            VView<double> vx(const_cast<double*>(x), n);
+            VView<double> vy(y, n);
+            vy += alpha[0] * vx;
+        }
+    } catch (const std::exception& e) {
+        std::fprintf(stderr, "blaze: %s\n", e.what());
+        return 1;
+    }
+    return 0;
+}
+
 }  // extern "C"

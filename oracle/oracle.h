@@ -77,6 +77,15 @@ void orc_product_rows_dot2(int order, int transA, int transB, int64_t m, int64_t
 double orc_fro_norm_d(const double* X, int64_t rows, int64_t cols, int64_t ld, int rowmajor);
 double orc_fro_norm_s(const float* X, int64_t rows, int64_t cols, int64_t ld, int rowmajor);
 
+/* ---- triangular solve ---------------------------------------------------------------------- */
+/* T X = X in place, T ka x ka dense row-major lower (lower != 0) or upper triangular with the
+ * diagonal as given, X ka x nrhs row-major; cplx != 0: interleaved complex doubles.  The CBLAS
+ * ?trsm cases reduce to this one (oracle/__init__.py: trsm): a right-side solve X op(A) = B is
+ * op(A)^T X^T = B^T.  ?trsm has no kernel in Blaze itself (blaze/math/blas/cblas/trsm.h hands it
+ * to CBLAS), so this restates the BLAS definition; blazetest's BLAS operation test checks its
+ * result the same way (blazetest/mathtest/blas/OperationTest.h:255-715: A * x == b). */
+void orc_trsm_left(int cplx, int lower, int64_t ka, int64_t nrhs, const double* T, double* X);
+
 /* Number of OpenMP threads available to the oracle. */
 int orc_max_threads(void);
 

@@ -210,3 +210,42 @@ void orc_gemm_blocked_##SUFFIX(int order, int transA, int transB, int64_t m, int
 
 DEFINE_BLOCKED(d, double, KBLOCK_D, LANES_D)
 DEFINE_BLOCKED(s, float, KBLOCK_S, LANES_S)
+
+/* ---- triangular solve (the CBLAS ?trsm definition) ---------------------------------------------
+ * T X = X in place by substitution: T is ka x ka dense row-major, lower (forward substitution) or
+ * upper (back substitution), with its diagonal as given (a unit diagonal is already ones); X is
+ * ka x nrhs row-major.  cplx != 0: both hold interleaved complex doubles.  Row i of X is finished
+ * as X_i = (X_i - sum_{k before i} T_ik X_k) / T_ii, the order of reference BLAS's row-oriented
+ * left-side loops; the complex division is the textbook formula. */
+void orc_trsm_left(int cplx, int lower, int64_t ka, int64_t nrhs, const double* T, double* X) {
+    const int64_t w = cplx ? 2 : 1;
+    for (int64_t s = 0; s < ka; ++s) {
+        const int64_t i = lower ? s : ka - 1 - s;
+        double* xi = X + i * nrhs * w;
+        const int64_t k0 = lower ? 0 : i + 1, k1 = lower ? i : ka;
+        for (int64_t k = k0; k < k1; ++k) {
+            const double* t = T + (i * ka + k) * w;
+            const double* xk = X + k * nrhs * w;
+            if (!cplx) {
+                for (int64_t j = 0; j < nrhs; ++j) xi[j] -= t[0] * xk[j];
+            } else {
+                for (int64_t j = 0; j < nrhs; ++j) {
+                    const double ar = xk[2 * j], ai = xk[2 * j + 1];
+                    xi[2 * j] -= t[0] * ar - t[1] * ai;
+                    xi[2 * j + 1] -= t[0] * ai + t[1] * ar;
+                }
+            }
+        }
+        const double* d = T + (i * ka + i) * w;
+        if (!cplx) {
+            for (int64_t j = 0; j < nrhs; ++j) xi[j] /= d[0];
+        } else {
+            const double den = d[0] * d[0] + d[1] * d[1];
+            for (int64_t j = 0; j < nrhs; ++j) {
+                const double ar = xi[2 * j], ai = xi[2 * j + 1];
+                xi[2 * j] = (ar * d[0] + ai * d[1]) / den;
+                xi[2 * j + 1] = (ai * d[0] - ar * d[1]) / den;
+            }
+        }
+    }
+}

@@ -10,6 +10,8 @@
 //   C = L*B, L triangular (DMatDMatMultExpr.h:2026-2033)          -> cblas_dtrmm / cblas_ztrmm
 //   C = A*B of a small area, with -DBLAZE_DMATDMATMULT_THRESHOLD=1 -> cblas_dgemm
 //   C = A*B with B of at most 10 SIMD widths of columns            -> Blaze's own small kernel
+//   blaze::dotu / dotc / axpy / trsm                               -> cblas_?dot / ?dot?_sub /
+//                                                                     ?axpy / ?trsm
 // and prints one line per product:  <label> status=<ok|exception> maxdiff=<|result - reference|>
 // where the reference is a plain loop over the same operands (BLAS bypassed).
 #include <blaze/Math.h>
@@ -186,6 +188,99 @@ int main() {
         fill(A, 26); fill(B, 27);
         C = A * B;
         return mm_diff(A, B, C);
+    });
+    // blaze::dotu / dotc / axpy / trsm (blaze/math/blas/), the calls blazetest's BLAS operation
+    // test makes (blazetest/mathtest/blas/OperationTest.h): 7-element vectors, 3 x 3 triangular
+    // systems with one and with several right-hand sides, plus larger systems; a storage order of
+    // B that differs from A's makes Blaze pass the transposed triangle (blaze/math/blas/trsm.h:195-199)
+    report("dotu_d", [] {
+        blaze::StaticVector<double, 7, blaze::rowVector> x;
+        blaze::StaticVector<double, 7> y;
+        fillv(x, 28); fillv(y, 29);
+        const double r = blaze::dotu(x, y);
+        double s = 0.0;
+        for (size_t i = 0; i < 7; ++i) s += x[i] * y[i];
+        return std::abs(r - s);
+    });
+    report("dotu_z", [] {
+        blaze::StaticVector<CD, 7, blaze::rowVector> x;
+        blaze::StaticVector<CD, 7> y;
+        fillv(x, 30); fillv(y, 31);
+        const CD r = blaze::dotu(x, y);
+        CD s(0.0);
+        for (size_t i = 0; i < 7; ++i) s += x[i] * y[i];
+        return std::abs(r - s);
+    });
+    report("dotc_z", [] {
+        blaze::StaticVector<CD, 7, blaze::rowVector> x;
+        blaze::StaticVector<CD, 7> y;
+        fillv(x, 32); fillv(y, 33);
+        const CD r = blaze::dotc(x, y);
+        CD s(0.0);
+        for (size_t i = 0; i < 7; ++i) s += std::conj(x[i]) * y[i];
+        return std::abs(r - s);
+    });
+    report("axpy_d", [] {
+        blaze::StaticVector<double, 7, blaze::rowVector> x, y, y0;
+        fillv(x, 34); fillv(y, 35);
+        y0 = y;
+        blaze::axpy(y, x, 0.75);
+        double d = 0.0;
+        for (size_t i = 0; i < 7; ++i) d = std::max(d, std::abs(y[i] - (y0[i] + 0.75 * x[i])));
+        return d;
+    });
+    report("axpy_z", [] {
+        blaze::DynamicVector<CD> x(500), y(500), y0;
+        fillv(x, 36); fillv(y, 37);
+        y0 = y;
+        const CD al(0.5, -2.0);
+        blaze::axpy(y, x, al);
+        double d = 0.0;
+        for (size_t i = 0; i < 500; ++i) d = std::max(d, std::abs(y[i] - (y0[i] + al * x[i])));
+        return d;
+    });
+    report("trsm_lower_vec", [] {
+        blaze::LowerMatrix<blaze::StaticMatrix<double, 3, 3, rowMajor>> A;
+        fill(A, 38);
+        for (size_t i = 0; i < 3; ++i) A(i, i) += 4.0;
+        blaze::StaticVector<double, 3> b, x;
+        fillv(b, 39);
+        x = b;
+        blaze::trsm(A, x, CblasLeft, CblasLower, 1.0);
+        return mv_diff(A, x, b, 1.0, (decltype(b)*)nullptr, 0.0);
+    });
+    report("trsm_upper_right", [] {
+        blaze::UpperMatrix<blaze::StaticMatrix<double, 3, 3, columnMajor>> A;
+        fill(A, 40);
+        for (size_t i = 0; i < 3; ++i) A(i, i) += 4.0;
+        blaze::StaticMatrix<double, 3, 3, columnMajor> B, X;
+        fill(B, 41);
+        X = B;
+        blaze::trsm(A, X, CblasRight, CblasUpper, 1.0);
+        return mm_diff(X, A, B);
+    });
+    report("trsm_mixed", [] {  // A row-major, B column-major: the transposed triangle
+        blaze::LowerMatrix<blaze::DynamicMatrix<double, rowMajor>> A(300);
+        fill(A, 42);
+        for (size_t i = 0; i < 300; ++i) A(i, i) += 300.0;
+        blaze::DynamicMatrix<double, columnMajor> B(300, 24), X, B2;
+        fill(B, 43);
+        X = B;
+        blaze::trsm(A, X, CblasLeft, CblasLower, 2.0);
+        B2 = 2.0 * B;
+        return mm_diff(A, X, B2);
+    });
+    report("ztrsm_lower", [] {
+        blaze::LowerMatrix<blaze::DynamicMatrix<CD, rowMajor>> A(100);
+        fill(A, 44);
+        for (size_t i = 0; i < 100; ++i) A(i, i) += 100.0;
+        blaze::DynamicMatrix<CD, rowMajor> B(100, 16), X, B2;
+        fill(B, 45);
+        X = B;
+        const CD al(0.5, -1.0);
+        blaze::trsm(A, X, CblasLeft, CblasLower, al);
+        B2 = al * B;
+        return mm_diff(A, X, B2);
     });
     return 0;
 }

@@ -1,8 +1,8 @@
 // stub_cblas.cpp — TEST-ONLY stand-in for libgb300blas used to check the Blaze seam on a host
 // without a GPU: it implements the gb300_cblas.h routines Blaze calls on the CPU (plain loops), and
 // logs each call's CBLAS arguments to the file named by GB300_STUB_LOG, so the test can compare
-// them with what Blaze must pass (blaze/math/blas/gemm.h:115-131 and the gemv / trmv / trmm
-// wrappers next to it) and replay them through the real library.
+// them with what Blaze must pass (blaze/math/blas/gemm.h:115-131 and the gemv / trmv / trmm /
+// trsm / axpy / dot wrappers next to it) and replay them through the real library.
 #include <complex>
 #include <cstdarg>
 #include <cstdio>
@@ -156,6 +156,52 @@ void gemm(int order, int ta, int tb, long m, long n, long k, T alpha, const T* A
             c = (beta == T(0)) ? alpha * s : alpha * s + beta * c;
         }
 }
+// B = alpha op(A)^-1 B (left) or alpha B op(A)^-1 (right) by substitution on the logical matrices
+template <typename T>
+void trsm(int order, int side, int uplo, int trans, int diag, long m, long n, T alpha, const T* A, long lda, T* B,
+          long ldb) {
+    const bool left = side == CblasLeft;
+    const long ka = left ? m : n;
+    const bool lower = (uplo == CblasLower) == (trans == CblasNoTrans);  // op(A) lower triangular
+    std::vector<T> X(m * n);
+    for (long i = 0; i < m; ++i)
+        for (long j = 0; j < n; ++j) X[i * n + j] = alpha * at(B, ldb, order, i, j);
+    auto t = [&](long r, long c) { return op_tri(A, lda, order, uplo, trans, diag, r, c); };
+    for (long s = 0; s < ka; ++s) {
+        // left: rows of X in the order op(A) allows; right: columns (X op(A) = B, op(A)^T X^T = B^T)
+        const bool forward = left ? lower : !lower;
+        const long i = forward ? s : ka - 1 - s;
+        const long k0 = forward ? 0 : i + 1, k1 = forward ? i : ka;
+        if (left) {
+            for (long j = 0; j < n; ++j) {
+                T v = X[i * n + j];
+                for (long k = k0; k < k1; ++k) v -= t(i, k) * X[k * n + j];
+                X[i * n + j] = v / t(i, i);
+            }
+        } else {
+            for (long r = 0; r < m; ++r) {
+                T v = X[r * n + i];
+                for (long k = k0; k < k1; ++k) v -= X[r * n + k] * t(k, i);
+                X[r * n + i] = v / t(i, i);
+            }
+        }
+    }
+    for (long i = 0; i < m; ++i)
+        for (long j = 0; j < n; ++j) at(B, ldb, order, i, j) = X[i * n + j];
+}
+
+template <typename T>
+void axpy(long n, T alpha, const T* x, long incx, T* y, long incy) {
+    for (long k = 0; k < n; ++k) vec(y, incy, n, k) += alpha * vec(const_cast<T*>(x), incx, n, k);
+}
+
+template <typename T>
+T dot(long n, const T* x, long incx, const T* y, long incy, bool conj) {
+    T s = T(0);
+    for (long k = 0; k < n; ++k)
+        s += conj_if(vec(const_cast<T*>(x), incx, n, k), conj) * vec(const_cast<T*>(y), incy, n, k);
+    return s;
+}
 }  // namespace
 
 extern "C" {
@@ -289,5 +335,87 @@ void gb300_cblas_cgemm_checked(CBLAS_ORDER order, CBLAS_TRANSPOSE transA, CBLAS_
              long(k), al.real(), al.imag(), long(lda), long(ldb), be.real(), be.imag(), long(ldc));
     cgemm<CF>(order, transA, transB, m, n, k, al, static_cast<const CF*>(A), lda, static_cast<const CF*>(B), ldb, be,
               static_cast<CF*>(C), ldc);
+}
+void gb300_cblas_dtrsm_checked(CBLAS_ORDER order, CBLAS_SIDE side, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA,
+                               CBLAS_DIAG diag, gb300_blas_int m, gb300_blas_int n, double alpha, const double* A,
+                               gb300_blas_int lda, double* B, gb300_blas_int ldb) {
+    log_line("dtrsm %d %d %d %d %d %ld %ld %.17g %ld %ld\n", order, side, uplo, transA, diag, long(m), long(n), alpha,
+             long(lda), long(ldb));
+    trsm<double>(order, side, uplo, transA, diag, m, n, alpha, A, lda, B, ldb);
+}
+void gb300_cblas_strsm_checked(CBLAS_ORDER order, CBLAS_SIDE side, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA,
+                               CBLAS_DIAG diag, gb300_blas_int m, gb300_blas_int n, float alpha, const float* A,
+                               gb300_blas_int lda, float* B, gb300_blas_int ldb) {
+    log_line("strsm %d %d %d %d %d %ld %ld %.9g %ld %ld\n", order, side, uplo, transA, diag, long(m), long(n), alpha,
+             long(lda), long(ldb));
+    trsm<float>(order, side, uplo, transA, diag, m, n, alpha, A, lda, B, ldb);
+}
+void gb300_cblas_ztrsm_checked(CBLAS_ORDER order, CBLAS_SIDE side, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA,
+                               CBLAS_DIAG diag, gb300_blas_int m, gb300_blas_int n, const void* alpha, const void* A,
+                               gb300_blas_int lda, void* B, gb300_blas_int ldb) {
+    const CD al = *static_cast<const CD*>(alpha);
+    log_line("ztrsm %d %d %d %d %d %ld %ld %.17g,%.17g %ld %ld\n", order, side, uplo, transA, diag, long(m), long(n),
+             al.real(), al.imag(), long(lda), long(ldb));
+    trsm<CD>(order, side, uplo, transA, diag, m, n, al, static_cast<const CD*>(A), lda, static_cast<CD*>(B), ldb);
+}
+void gb300_cblas_ctrsm_checked(CBLAS_ORDER order, CBLAS_SIDE side, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transA,
+                               CBLAS_DIAG diag, gb300_blas_int m, gb300_blas_int n, const void* alpha, const void* A,
+                               gb300_blas_int lda, void* B, gb300_blas_int ldb) {
+    const CF al = *static_cast<const CF*>(alpha);
+    log_line("ctrsm %d %d %d %d %d %ld %ld %.9g,%.9g %ld %ld\n", order, side, uplo, transA, diag, long(m), long(n),
+             al.real(), al.imag(), long(lda), long(ldb));
+    trsm<CF>(order, side, uplo, transA, diag, m, n, al, static_cast<const CF*>(A), lda, static_cast<CF*>(B), ldb);
+}
+void gb300_cblas_daxpy_checked(gb300_blas_int n, double alpha, const double* x, gb300_blas_int incX, double* y,
+                               gb300_blas_int incY) {
+    log_line("daxpy %ld %.17g %ld %ld\n", long(n), alpha, long(incX), long(incY));
+    axpy<double>(n, alpha, x, incX, y, incY);
+}
+void gb300_cblas_saxpy_checked(gb300_blas_int n, float alpha, const float* x, gb300_blas_int incX, float* y,
+                               gb300_blas_int incY) {
+    log_line("saxpy %ld %.9g %ld %ld\n", long(n), alpha, long(incX), long(incY));
+    axpy<float>(n, alpha, x, incX, y, incY);
+}
+void gb300_cblas_zaxpy_checked(gb300_blas_int n, const void* alpha, const void* x, gb300_blas_int incX, void* y,
+                               gb300_blas_int incY) {
+    const CD al = *static_cast<const CD*>(alpha);
+    log_line("zaxpy %ld %.17g,%.17g %ld %ld\n", long(n), al.real(), al.imag(), long(incX), long(incY));
+    axpy<CD>(n, al, static_cast<const CD*>(x), incX, static_cast<CD*>(y), incY);
+}
+void gb300_cblas_caxpy_checked(gb300_blas_int n, const void* alpha, const void* x, gb300_blas_int incX, void* y,
+                               gb300_blas_int incY) {
+    const CF al = *static_cast<const CF*>(alpha);
+    log_line("caxpy %ld %.9g,%.9g %ld %ld\n", long(n), al.real(), al.imag(), long(incX), long(incY));
+    axpy<CF>(n, al, static_cast<const CF*>(x), incX, static_cast<CF*>(y), incY);
+}
+double gb300_cblas_ddot_checked(gb300_blas_int n, const double* x, gb300_blas_int incX, const double* y,
+                                gb300_blas_int incY) {
+    log_line("ddot %ld %ld %ld\n", long(n), long(incX), long(incY));
+    return dot<double>(n, x, incX, y, incY, false);
+}
+float gb300_cblas_sdot_checked(gb300_blas_int n, const float* x, gb300_blas_int incX, const float* y,
+                               gb300_blas_int incY) {
+    log_line("sdot %ld %ld %ld\n", long(n), long(incX), long(incY));
+    return dot<float>(n, x, incX, y, incY, false);
+}
+void gb300_cblas_zdotu_sub_checked(gb300_blas_int n, const void* x, gb300_blas_int incX, const void* y,
+                                   gb300_blas_int incY, void* dotu) {
+    log_line("zdotu_sub %ld %ld %ld\n", long(n), long(incX), long(incY));
+    *static_cast<CD*>(dotu) = dot<CD>(n, static_cast<const CD*>(x), incX, static_cast<const CD*>(y), incY, false);
+}
+void gb300_cblas_zdotc_sub_checked(gb300_blas_int n, const void* x, gb300_blas_int incX, const void* y,
+                                   gb300_blas_int incY, void* dotc) {
+    log_line("zdotc_sub %ld %ld %ld\n", long(n), long(incX), long(incY));
+    *static_cast<CD*>(dotc) = dot<CD>(n, static_cast<const CD*>(x), incX, static_cast<const CD*>(y), incY, true);
+}
+void gb300_cblas_cdotu_sub_checked(gb300_blas_int n, const void* x, gb300_blas_int incX, const void* y,
+                                   gb300_blas_int incY, void* dotu) {
+    log_line("cdotu_sub %ld %ld %ld\n", long(n), long(incX), long(incY));
+    *static_cast<CF*>(dotu) = dot<CF>(n, static_cast<const CF*>(x), incX, static_cast<const CF*>(y), incY, false);
+}
+void gb300_cblas_cdotc_sub_checked(gb300_blas_int n, const void* x, gb300_blas_int incX, const void* y,
+                                   gb300_blas_int incY, void* dotc) {
+    log_line("cdotc_sub %ld %ld %ld\n", long(n), long(incX), long(incY));
+    *static_cast<CF*>(dotc) = dot<CF>(n, static_cast<const CF*>(x), incX, static_cast<const CF*>(y), incY, true);
 }
 }

@@ -1,5 +1,5 @@
 """Generate the golden fixtures of the neighbouring BLAS routines (gemv, trmv, complex gemm, trmm,
-real and complex) from Blaze itself.
+trsm, axpy and the dot products, real and complex) from Blaze itself.
 
 Run in a container that has the reference headers (Blaze is header-only):
 
@@ -117,6 +117,54 @@ def ztrmm_cases():
     return out
 
 
+def dot_cases():
+    out, seed = [], 17000
+    for cplx in (0, 1):
+        for conj in ((0, 1) if cplx else (0,)):
+            for n in (1, 3, 7, 100, 1000, 4097):
+                out.append((cplx, conj, n, seed))
+                seed += 2
+    return out
+
+
+def axpy_cases():
+    out, seed = [], 18000
+    for cplx in (0, 1):
+        alphas = (0.5 - 1.25j, -2 + 0j, 1j) if cplx else (1.5, -0.75, 3.0)
+        for i, n in enumerate((1, 7, 257, 1000)):
+            out.append((cplx, n, alphas[i % 3], seed))
+            seed += 2
+    return out
+
+
+def trsm_cases():
+    """blazetest's BLAS operation test solves 3 x 3 triangular systems with one and with several
+    right-hand sides on either side (OperationTest.h:255-715); here also triangles past the 256-row
+    leaves of the GPU's complex double solve (few right-hand sides keep the fixture small)."""
+    out, seed = [], 19000
+    sizes = [(3, 1), (1, 3), (3, 3), (37, 16), (130, 8), (300, 6), (6, 300)]
+    for cplx in (0, 1):
+        ops = (O.NO_TRANS, O.TRANS, CONJ) if cplx else (O.NO_TRANS, O.TRANS)
+        combos = list(itertools.product((O.ROW_MAJOR, O.COL_MAJOR), (141, 142), (121, 122), ops, (131, 132)))
+        alphas = (1 + 0j, 0.5j, -2 + 0j) if cplx else (1.0, -0.5, 2.0)
+        for i, (m, n) in enumerate(sizes):
+            for j, (order, side, uplo, ta, diag) in enumerate(combos):
+                keep = 1 if max(m, n) <= 3 else (4 if max(m, n) < 200 else 8)
+                if (i + j) % keep:
+                    continue
+                out.append((cplx, order, side, uplo, ta, diag, m, n, alphas[(i + j) % 3], j % 2, seed))
+                seed += 2
+    return out
+
+
+def trsm_operands(cplx, ka, lda, m, n, order, pad, seed):
+    """The triangle's stored square and the solution X0 in the storage of B (ldb = columns + pad)."""
+    rb, cb = stored(order, O.NO_TRANS, m, n)
+    ldb = cb + pad
+    A, X0 = O.triangular_operands(bool(cplx), ka, lda, rb, ldb, seed)
+    return A, X0, ldb
+
+
 def stored(order, trans, rows, cols):
     t = trans != O.NO_TRANS
     r, c = (cols, rows) if t else (rows, cols)
@@ -188,6 +236,34 @@ def main():
         arrays[f"ztrmm{q}_meta"] = np.array([order, side, uplo, ta, diag, m, n, lda, ldb, seed], dtype=np.int64)
         arrays[f"ztrmm{q}_alpha"] = np.array([al])
         arrays[f"ztrmm{q}_B"] = B
+    for q, (cplx, conj, n, seed) in enumerate(dot_cases()):
+        x = zvals(n, seed) if cplx else O.uniform(n, seed).copy()
+        y = zvals(n, seed + 1) if cplx else O.uniform(n, seed + 1).copy()
+        arrays[f"dot{q}_meta"] = np.array([cplx, conj, n, seed], dtype=np.int64)
+        arrays[f"dot{q}_r"] = np.array([O.ref_dot(x, y, conj=bool(conj))])
+    for q, (cplx, n, al, seed) in enumerate(axpy_cases()):
+        x = zvals(n, seed) if cplx else O.uniform(n, seed).copy()
+        y = zvals(n, seed + 1) if cplx else O.uniform(n, seed + 1).copy()
+        O.ref_axpy(al, x, y)
+        arrays[f"axpy{q}_meta"] = np.array([cplx, n, seed], dtype=np.int64)
+        arrays[f"axpy{q}_alpha"] = np.array([al])
+        arrays[f"axpy{q}_y"] = y
+    # trsm: Blaze forms B = op(A) X0 (left) or X0 op(A) (right) with its own kernels (the trmm
+    # evaluation above, alpha = 1); solving with alpha (a power of two, so alpha X0 is exact) must
+    # give back alpha X0
+    for q, (cplx, order, side, uplo, ta, diag, m, n, al, pad, seed) in enumerate(trsm_cases()):
+        ka = m if side == 141 else n
+        lda = ka + pad
+        A, X0, ldb = trsm_operands(cplx, ka, lda, m, n, order, pad, seed)
+        B = X0.copy()
+        if cplx:
+            O.ref_ztrmm(order, side, uplo, ta, diag, m, n, 1 + 0j, A, lda, B, ldb)
+        else:
+            O.ref_trmm(order, side, uplo, ta, diag, m, n, 1.0, A, lda, B, ldb)
+        arrays[f"trsm{q}_meta"] = np.array([cplx, order, side, uplo, ta, diag, m, n, lda, ldb, pad, seed],
+                                           dtype=np.int64)
+        arrays[f"trsm{q}_alpha"] = np.array([al])
+        arrays[f"trsm{q}_B"] = B
     np.savez_compressed(OUT, **arrays)
     print(OUT, len(arrays), "arrays,", os.path.getsize(OUT), "bytes")
 

@@ -9,12 +9,16 @@ import oracle as O
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "gemm_golden.npz")
 
-# Blaze's relaxed equality (blaze/math/shims/Equal.h:214-223): |a-b| <= max(acc, acc*|a|) with
-# acc = 1e-8 for double and 1e-6 for float (blaze/util/Limits.h:366,398).
+# Blaze's relaxed equality (blaze/math/shims/Equal.h:214-223; complex values part by part,
+# :406-408): |a-b| <= max(acc, acc*|a|) with acc = 1e-8 for double and 1e-6 for float
+# (blaze/util/Limits.h:366,398).
 BLAZE_ACC = {np.float64: 1e-8, np.float32: 1e-6}
 
 
 def blaze_equal(a: np.ndarray, b: np.ndarray, acc: float) -> np.ndarray:
+    if np.iscomplexobj(a) or np.iscomplexobj(b):  # Blaze compares the real and imaginary parts
+        a, b = np.asarray(a, dtype=np.complex128), np.asarray(b, dtype=np.complex128)
+        return blaze_equal(a.real, b.real, acc) & blaze_equal(a.imag, b.imag, acc)
     a = np.asarray(a, dtype=np.float64)
     b = np.asarray(b, dtype=np.float64)
     return np.abs(a - b) <= np.maximum(acc, acc * np.abs(a))

@@ -86,10 +86,23 @@ def test_quick_returns_do_not_touch_the_device(lib):
     assert G.last_error()[0] == G.OK and np.all(C == 7.0)
 
 
-def test_stub_routines_report_not_supported(lib):
-    lib.gb300_clear_error()
-    lib.cblas_daxpy(4, ct.c_double(1.0), None, 1, None, 1)
-    assert G.last_error()[0] == G.ERR_NOT_SUPPORTED
+def test_level1_and_trsm_need_the_device(lib):
+    """No routine is a stub: axpy, the dot products and trsm validate, then need the GPU; on a
+    host without one they say so and compute nothing."""
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    x = np.arange(4.0); y = np.ones(4)
+    G.lib().gb300_clear_error()
+    G.lib().cblas_daxpy(4, 2.0, x.ctypes.data, 1, y.ctypes.data, 1)
+    assert G.last_error()[0] == G.ERR_NO_DEVICE and np.all(y == 1.0)
+    G.lib().gb300_clear_error()
+    assert G.lib().cblas_ddot(4, x.ctypes.data, 1, y.ctypes.data, 1) == 0.0
+    assert G.last_error()[0] == G.ERR_NO_DEVICE
+    A = np.eye(4); B = np.ones(8)
+    G.lib().gb300_clear_error()
+    G.lib().cblas_dtrsm(101, 141, 122, 111, 131, 4, 2, 1.0, A.ctypes.data, 4, B.ctypes.data, 2)
+    assert G.last_error()[0] == G.ERR_NO_DEVICE and np.all(B == 1.0)
 
 
 def test_no_device_is_reported_not_faked(lib):
@@ -116,6 +129,9 @@ def test_no_device_is_reported_not_faked(lib):
     ("trmv", dict(n=-1), 5), ("trmv", dict(lda=3), 7), ("trmv", dict(incx=0), 9),
     ("ztrmv", dict(uplo=7), 2), ("ztrmv", dict(lda=3), 7), ("ztrmv", dict(incx=0), 9),
     ("ztrmm", dict(side=7), 2), ("ztrmm", dict(diag=7), 5), ("ztrmm", dict(lda=3), 10), ("ztrmm", dict(ldb=3), 12),
+    ("trsm", dict(order=99), 1), ("trsm", dict(side=7), 2), ("trsm", dict(uplo=7), 3), ("trsm", dict(ta=7), 4),
+    ("trsm", dict(diag=7), 5), ("trsm", dict(m=-1), 6), ("trsm", dict(n=-1), 7), ("trsm", dict(lda=3), 10),
+    ("trsm", dict(ldb=3), 12), ("ztrsm", dict(side=7), 2), ("ztrsm", dict(ta=7), 4), ("ztrsm", dict(lda=3), 10),
 ])
 def test_neighbour_routines_name_the_parameter(lib, routine, args, param):
     a = dict(order=G.RowMajor, ta=G.NoTrans, tb=G.NoTrans, m=8, n=8, k=8, lda=8, ldb=8, ldc=8, incx=1, incy=1,
@@ -136,6 +152,12 @@ def test_neighbour_routines_name_the_parameter(lib, routine, args, param):
     elif routine in ("trmv", "ztrmv"):
         getattr(lib, "cblas_%s" % ("dtrmv" if routine == "trmv" else "ztrmv"))(
             a["order"], a["uplo"], a["ta"], a["diag"], a["n"], A.ctypes.data, a["lda"], B.ctypes.data, a["incx"])
+    elif routine == "trsm":
+        lib.cblas_dtrsm(a["order"], a["side"], a["uplo"], a["ta"], a["diag"], a["m"], a["n"], 1.0, A.ctypes.data,
+                        a["lda"], B.ctypes.data, a["ldb"])
+    elif routine == "ztrsm":
+        lib.cblas_ztrsm(a["order"], a["side"], a["uplo"], a["ta"], a["diag"], a["m"], a["n"], one.ctypes.data,
+                        A.ctypes.data, a["lda"], B.ctypes.data, a["ldb"])
     elif routine == "ztrmm":
         lib.cblas_ztrmm(a["order"], a["side"], a["uplo"], a["ta"], a["diag"], a["m"], a["n"], one.ctypes.data,
                         A.ctypes.data, a["lda"], B.ctypes.data, a["ldb"])

@@ -85,7 +85,7 @@ def _vals(count, seed, kind):
 
 def test_replay_blaze_neighbouring_calls():
     lines = open(NEXT_CALLS).read().splitlines()
-    assert len(lines) == 12
+    assert len(lines) == 21
     for q, ln in enumerate(lines):
         f = ln.split()
         name, kind = f[0], f[0][0]
@@ -139,7 +139,35 @@ def test_replay_blaze_neighbouring_calls():
                 be * np.array(_mat(C, order, m, n, ldc))
             G.cblas_zgemm(order, ta, tb, m, n, k, al, A, lda, B, ldb, be, C, ldc)
             got = np.array(_mat(C, order, m, n, ldc))
+        elif "dot" in name:  # ddot, zdotu_sub, zdotc_sub
+            n, incx, incy = (int(v) for v in f[1:4])
+            x = _vals(n * abs(incx), 500 + q, kind)
+            y = _vals(n * abs(incy), 600 + q, kind)
+            xs = x[::incx].conj() if "dotc" in name else x[::incx]
+            ref = np.array([np.sum(xs * y[::incy])])
+            got = np.array([G.cblas_dot(n, x, incx, y, incy, dtype=kind, conj="dotc" in name)])
+            k = n
+        elif name.endswith("axpy"):
+            n, al, incx, incy = int(f[1]), _scalar(f[2]), int(f[3]), int(f[4])
+            x = _vals(n * abs(incx), 500 + q, kind)
+            y = _vals(n * abs(incy), 600 + q, kind)
+            ref = al * x[::incx] + y[::incy]
+            G.cblas_axpy(n, al, x, incx, y, incy, dtype=kind)
+            got = y[::incy]
+            k = 1
+        elif name.endswith("trsm"):
+            order, side, uplo, ta, diag, m, n = (int(v) for v in f[1:8])
+            al, lda, ldb = _scalar(f[8]), int(f[9]), int(f[10])
+            ka = m if side == 141 else n
+            rb = m if order == O.ROW_MAJOR else n
+            A, B = O.triangular_operands(kind == "z", ka, lda, rb, ldb, 700 + q)
+            want = B.copy()
+            O.trsm(order, side, uplo, ta, diag, m, n, al, A, lda, want, ldb)
+            G.cblas_trsm(order, side, uplo, ta, diag, m, n, al, A, lda, B, ldb, dtype=kind)
+            ref, got = np.array(_mat(want, order, m, n, ldb)), np.array(_mat(B, order, m, n, ldb))
+            k = ka
         else:  # trmm
+            assert name.endswith("trmm"), ln
             order, side, uplo, ta, diag, m, n = (int(v) for v in f[1:8])
             al, lda, ldb = _scalar(f[8]), int(f[9]), int(f[10])
             ka = m if side == 141 else n

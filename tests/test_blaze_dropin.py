@@ -86,6 +86,8 @@ NEXT_ROUTINES = {  # label -> the CBLAS routine Blaze must call for it
     "gemv_r": "dgemv", "gemv_c_add": "dgemv", "gemv_t": "dgemv", "sgemv_r": "sgemv", "trmv_lower_r": "dtrmv",
     "trmv_upper_c": "dtrmv", "ztrmv_lower_r": "ztrmv", "zgemv_r": "zgemv", "zgemm_rr": "zgemm",
     "dtrmm_lower": "dtrmm", "ztrmm_upper": "ztrmm", "small_area": "dgemm", "skinny_cpu": None,
+    "dotu_d": "ddot", "dotu_z": "zdotu_sub", "dotc_z": "zdotc_sub", "axpy_d": "daxpy", "axpy_z": "zaxpy",
+    "trsm_lower_vec": "dtrsm", "trsm_upper_right": "dtrsm", "trsm_mixed": "dtrsm", "ztrsm_lower": "ztrsm",
 }
 
 
@@ -110,6 +112,11 @@ def test_blaze_expressions_reach_the_neighbouring_routines(tmp_path):
     assert by["trmv_lower_r"][1:5] == ["101", "122", "111", "131"]
     assert by["trmv_upper_c"][1:5] == ["102", "121", "111", "131"]
     assert by["dtrmm_lower"][1:6] == ["101", "141", "122", "111", "131"]
+    # blaze::trsm: a vector right-hand side is an m x 1 system (ldb = 1 row-major); a column-major B
+    # with a row-major A gets the transposed, flipped triangle (blaze/math/blas/trsm.h:195-199)
+    assert by["trsm_lower_vec"][1:8] == ["101", "141", "122", "111", "131", "3", "1"]
+    assert by["trsm_upper_right"][1:6] == ["102", "142", "121", "111", "131"]
+    assert by["trsm_mixed"][1:6] == ["102", "141", "121", "112", "131"]
 
 
 def test_neighbouring_call_fixture_matches_blaze():

@@ -90,3 +90,56 @@ def test_ztrmm_fixtures(golden):
         for i in range(m if order == O.ROW_MAJOR else n):
             keep[i * ldb:i * ldb + (n if order == O.ROW_MAJOR else m)] = False
         assert np.array_equal(golden[f"ztrmm{q}_B"][keep], B0[keep]), q
+
+
+def test_dot_fixtures(golden):
+    """Blaze's x * y and conj(x) * y against the definition (products summed in double)."""
+    for q in cases(golden, "dot"):
+        cplx, conj, n, seed = (int(v) for v in golden[f"dot{q}_meta"])
+        x = zvals(n, seed) if cplx else O.uniform(n, seed)
+        y = zvals(n, seed + 1) if cplx else O.uniform(n, seed + 1)
+        want = np.sum((x.conj() if conj else x) * y)
+        got = golden[f"dot{q}_r"][0]
+        assert abs(got - want) <= 1e-13 * max(1.0, float(np.sum(np.abs(x) * np.abs(y)))), q
+
+
+def test_axpy_fixtures(golden):
+    for q in cases(golden, "axpy"):
+        cplx, n, seed = (int(v) for v in golden[f"axpy{q}_meta"])
+        al = golden[f"axpy{q}_alpha"][0]
+        x = zvals(n, seed) if cplx else O.uniform(n, seed)
+        y = zvals(n, seed + 1) if cplx else O.uniform(n, seed + 1)
+        assert close(golden[f"axpy{q}_y"], al * x + y), q
+
+
+def trsm_case(golden, q):
+    cplx, order, side, uplo, ta, diag, m, n, lda, ldb, pad, seed = (int(v) for v in golden[f"trsm{q}_meta"])
+    al = golden[f"trsm{q}_alpha"][0]
+    ka = m if side == 141 else n
+    rb = m if order == O.ROW_MAJOR else n
+    A, X0 = O.triangular_operands(bool(cplx), ka, lda, rb, ldb, seed)
+    if not cplx:
+        al = float(al.real)
+    return (cplx, order, side, uplo, ta, diag, m, n, lda, ldb), al, A, X0
+
+
+def test_trsm_fixtures_pin_the_substitution(golden):
+    """Blaze formed B = op(A) X0 (or X0 op(A)) with its own kernels; the oracle's substitution
+    (orc_trsm_left) solving op(A) X = alpha B gives back alpha X0 within Blaze's relaxed equality,
+    the check blazetest's BLAS operation test makes (OperationTest.h:286: A * x == b)."""
+    from helpers import blaze_equal
+    assert len(cases(golden, "trsm")) >= 250
+    for q in cases(golden, "trsm"):
+        (cplx, order, side, uplo, ta, diag, m, n, lda, ldb), al, A, X0 = trsm_case(golden, q)
+        B = golden[f"trsm{q}_B"].copy()
+        O.trsm(order, side, uplo, ta, diag, m, n, al, A, lda, B, ldb)
+        assert blaze_equal(B, trsm_expected(order, m, n, ldb, al, X0), 1e-8).all(), q
+
+
+def trsm_expected(order, m, n, ldb, al, X0):
+    """alpha X0 on B's m x n elements, the padding between rows (or columns) as stored."""
+    E = X0.copy()
+    ii, jj = np.arange(m)[:, None], np.arange(n)[None, :]
+    pos = (ii * ldb + jj) if order == O.ROW_MAJOR else (jj * ldb + ii)
+    E[pos] = al * E[pos]
+    return E
