@@ -1671,9 +1671,13 @@ SplitGeometry split_geometry(const Gemm& g, const SplitRequest& req, int num_sms
         const int64_t cap = (int64_t(511) / (G.mode == kCrt ? 1 : G.max_planes)) * KSEG_UNIT;
         kseg = std::min(kseg, std::max<int64_t>(cap, KSEG_UNIT));
     }
+    // Split k only when at most half the CTA pairs would have a tile, and into as many segments as
+    // still fit one wave of pairs.  With more tiles a split cannot raise the occupancy (the units
+    // spill into a second, partial wave) and it multiplies the residue planes the reconstruction
+    // reads; at 64 tiles on 76 pairs two segments made a 512 x 8192 x 512 product 1.6 times slower.
     const int tiles = G.m_tiles * G.n_tiles, pairs = std::max(1, num_sms / 2);
-    if (tiles < pairs) {
-        const int64_t want = (pairs + tiles - 1) / tiles;
+    if (2 * tiles <= pairs) {
+        const int64_t want = pairs / tiles;
         kseg = std::min(kseg, std::max<int64_t>(KSEG_UNIT, round_up((G.kpad + want - 1) / want, KSEG_UNIT)));
     }
     // equal segments: persistent CTAs take units in a fixed stride, so unequal segments would give

@@ -41,30 +41,35 @@ __global__ void scale_kernel(int64_t rows, int64_t cols, V alpha, V* __restrict_
 // Each block is brought to lower-triangular form L'.  L' is the block itself when op(SA) is lower;
 // when it is upper (`upper`), L' is the block with its rows and columns reversed.  L' is inverted
 // by forward substitution, Y[r][c] = (delta_rc - sum_{j<r} L'[r][j] Y[j][c]) / L'[r][r].
-// blockIdx.x picks a group of 32 columns c, one per lane, and blockIdx.y the block.  The loops are
-// the same for every lane: Y[j][c] = 0 for j < c comes out of the recurrence itself, and a group
-// starts at its first column r0.  So every L' element is one load broadcast to the warp.
 //
-// Row r's sum is split over the kInvWarps warps of the block (warp w takes j = r0 + w, + kInvWarps,
-// ...), which shortens the dependent FMA chain that bounds the kernel kInvWarps-fold.  Warp 0 adds
-// the partial sums in warp order (a fixed order), divides and publishes Y[r] in shared memory
-// ([nb][32], conflict-free) before the next row starts.  A unit diagonal is not read.
+// The work is FP64 FMAs and column c needs about (nb - c)^2 / 2 of them, so the first columns set
+// the kernel's time: on GB300 one SM retires about two FP64 FMAs per clock.  A block of the grid
+// therefore takes only kInvCols columns (blockIdx.x picks the group, blockIdx.y the diagonal block)
+// and spreads each column's sums over 32 chains: lane = column + kInvCols * slice, and warp w with
+// slice s takes j = r0 + 4 w + s, then every 32nd.  The shuffles and then warp 0 add the chains in a
+// fixed order.  Warp 0 scales by the diagonal's reciprocal (computed for all rows up front, so the
+// serial step per row is a multiply) and publishes Y[r] in shared memory before the next row.
+// Y[j][c] = 0 for j < c comes out of the recurrence itself, so the loops are the same for every
+// column of a group, which starts at its first column r0.  A unit diagonal is not read.
 constexpr int kInvWarps = 8;
+constexpr int kInvCols = 8;
 
 template <typename V>
 __global__ void __launch_bounds__(32 * kInvWarps) tri_inverse_kernel(int64_t ka, int nb, const V* __restrict__ SA,
                                                                      int64_t lda, int trans, int conj, int upper,
                                                                      int unit, V* __restrict__ inv) {
     extern __shared__ __align__(16) unsigned char tri_smem[];
-    V* ycol = reinterpret_cast<V*>(tri_smem);  // [nb][32]
-    V* part = ycol + int64_t(nb) * 32;          // [kInvWarps][32]
+    V* ycol = reinterpret_cast<V*>(tri_smem);              // [nb][kInvCols]
+    V* rdiag = ycol + int64_t(nb) * kInvCols;                // [nb]
+    V* part = rdiag + nb;                                    // [kInvWarps][kInvCols]
     using A = Ar<V>;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int cl = lane % kInvCols, slice = lane / kInvCols;  // 4 slices
     const int64_t b0 = int64_t(blockIdx.y) * nb;
     const int nbk = int(min(int64_t(nb), ka - b0));
-    const int r0 = int(blockIdx.x) * 32;
+    const int r0 = int(blockIdx.x) * kInvCols;
     if (r0 >= nbk) return;
-    const int c = r0 + lane;
+    const int c = r0 + cl;
     // L'[r][j] sits at P + r * sr + j * sj
     int64_t sr = trans ? 1 : lda, sj = trans ? lda : 1;
     const V* P = SA + b0 * lda + b0;
@@ -77,37 +82,35 @@ __global__ void __launch_bounds__(32 * kInvWarps) tri_inverse_kernel(int64_t ka,
     // Y[r][c] lands at out[r][c], or at out[nbk-1-r][nbk-1-c] for a reversed (upper) block
     const int64_t o0 = upper ? int64_t(nbk - 1) * (nb + 1) : 0, orow = upper ? -int64_t(nb) : int64_t(nb),
                   ocol = upper ? -1 : 1;
-    if (c < nbk)
-        for (int r = warp; r < r0; r += kInvWarps) out[o0 + r * orow + c * ocol] = A::zero();
+    for (int r = r0 + threadIdx.x; r < nbk; r += blockDim.x) {
+        const V d = unit ? A::one() : (conj ? A::conj(P[r * (sr + sj)]) : P[r * (sr + sj)]);
+        rdiag[r - r0] = A::div(A::one(), d);
+    }
+    // rows above the group: zero (the inverse of a lower triangle is lower)
+    for (int i = threadIdx.x; i < r0 * kInvCols; i += blockDim.x) {
+        const int r = i / kInvCols, cc = r0 + i % kInvCols;
+        if (cc < nbk) out[o0 + r * orow + cc * ocol] = A::zero();
+    }
+    __syncthreads();
+    const int chain = warp * 4 + slice;  // 0..31
+    const int64_t lstep = 32 * sj;
     for (int r = r0; r < nbk; ++r) {
-        // this warp's share of the sum, two chains to overlap the loads
-        V s0 = A::zero(), s1 = A::zero();
-        int j = r0 + warp;
+        V s = A::zero();
+        int j = r0 + chain;
         const V* lp = P + r * sr + j * sj;
-        const V* yp = ycol + (j - r0) * 32 + lane;
-        const int64_t lstep = int64_t(kInvWarps) * sj;
-        for (; j + kInvWarps < r; j += 2 * kInvWarps, lp += 2 * lstep, yp += 64 * kInvWarps) {
-            const V l0 = conj ? A::conj(lp[0]) : lp[0];
-            const V l1 = conj ? A::conj(lp[lstep]) : lp[lstep];
-            s0 = A::fmadd(l0, yp[0], s0);
-            s1 = A::fmadd(l1, yp[32 * kInvWarps], s1);
-        }
-        if (j < r) {
-            const V l0 = conj ? A::conj(lp[0]) : lp[0];
-            s0 = A::fmadd(l0, yp[0], s0);
-        }
-        part[warp * 32 + lane] = A::add(s0, s1);
+        const V* yp = ycol + (j - r0) * kInvCols + cl;
+        for (; j < r; j += 32, lp += lstep, yp += 32 * kInvCols) s = A::fmadd(conj ? A::conj(*lp) : *lp, *yp, s);
+        // the four slices of this warp (lanes cl, cl + 8, cl + 16, cl + 24), then the warps
+        s = A::add(s, A::shfl_xor(s, kInvCols));
+        s = A::add(s, A::shfl_xor(s, 2 * kInvCols));
+        if (slice == 0) part[warp * kInvCols + cl] = s;
         __syncthreads();
-        if (warp == 0) {
-            V sum = part[lane];
+        if (warp == 0 && slice == 0) {
+            V sum = part[cl];
 #pragma unroll
-            for (int w = 1; w < kInvWarps; ++w) sum = A::add(sum, part[w * 32 + lane]);
-            V acc = A::fnmadd(A::one(), sum, (r == c) ? A::one() : A::zero());  // delta_rc - sum
-            if (!unit) {
-                const V* dp = P + r * (sr + sj);
-                acc = A::div(acc, conj ? A::conj(*dp) : *dp);
-            }
-            ycol[(r - r0) * 32 + lane] = acc;
+            for (int w = 1; w < kInvWarps; ++w) sum = A::add(sum, part[w * kInvCols + cl]);
+            const V acc = A::mul(A::fnmadd(A::one(), sum, (r == c) ? A::one() : A::zero()), rdiag[r - r0]);
+            ycol[(r - r0) * kInvCols + cl] = acc;
             if (c < nbk) out[o0 + r * orow + c * ocol] = acc;
         }
         __syncthreads();
@@ -132,15 +135,16 @@ template <typename T, bool CPLX>
 cudaError_t launch_tri_inverse(int64_t ka, int nb, const T* SA, int64_t lda, bool trans, bool conj, bool upper,
                                bool unit, T* inv, cudaStream_t st) {
     using V = typename std::conditional<CPLX, Cx<T>, T>::type;
-    const size_t smem = size_t(nb + kInvWarps) * 32 * sizeof(V);  // Y columns and the partial sums
+    // Y's columns, the diagonal's reciprocals and the partial sums
+    auto smem_for = [](int rows) { return (size_t(rows) * (kInvCols + 1) + kInvWarps * kInvCols) * sizeof(V); };
     constexpr int nb_max = solve_block(sizeof(V));
     static const cudaError_t attr = cudaFuncSetAttribute(tri_inverse_kernel<V>,
                                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                         int((nb_max + kInvWarps) * 32 * sizeof(V)));
+                                                         int(smem_for(nb_max)));
     if (attr != cudaSuccess) return attr;
     if (nb > nb_max || nb % 32 != 0) return cudaErrorInvalidValue;
     const int64_t blocks = (ka + nb - 1) / nb;
-    tri_inverse_kernel<V><<<dim3(unsigned(nb / 32), unsigned(blocks)), 32 * kInvWarps, smem, st>>>(
+    tri_inverse_kernel<V><<<dim3(unsigned(nb / kInvCols), unsigned(blocks)), 32 * kInvWarps, smem_for(nb), st>>>(
         ka, nb, reinterpret_cast<const V*>(SA), lda, trans ? 1 : 0, conj ? 1 : 0, upper ? 1 : 0, unit ? 1 : 0,
         reinterpret_cast<V*>(inv));
     count_launches(1);
