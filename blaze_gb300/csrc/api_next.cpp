@@ -15,10 +15,10 @@
 //                                                     blaze/math/blas/cblas/dotc.h:97-210
 //
 // Semantics follow CBLAS (argument positions as in xerbla, quick returns, beta == 0 does not read
-// the output, alpha == 0 does not read the inputs).  Complex products are four real products of
-// the real and imaginary parts (conjugate-transpose flips the sign of an imaginary part), each
-// through the library's real product: FP64-accurate split precision for double by default, the
-// native kernel for float.  A triangular product runs on a dense copy of the triangle (zeros
+// the output, alpha == 0 does not read the inputs).  A complex product is one real product of the
+// stacked real and imaginary planes, whose four quadrants combine into the result (a conjugate
+// transpose flips the sign of an imaginary part), through the library's real product:
+// FP64-accurate split precision for double by default, the native kernel for float.  A triangular product runs on a dense copy of the triangle (zeros
 // elsewhere, ones on a unit diagonal); a triangular matrix x vector product masks the triangle in
 // the matrix x vector kernel itself.  Host operands are staged through device buffers; device or
 // managed operands are used in place (complex ones when 2 * sizeof(T)-aligned, else copied).
@@ -51,7 +51,7 @@ bool on_device(const void* p) {
 }
 
 // aux workspace slots of these routines
-enum AuxSlot : int { kAuxA = 0, kAuxB, kAuxC, kAuxX, kAuxY, kAuxAr, kAuxAi, kAuxBr, kAuxBi, kAuxP, kAuxT };
+enum AuxSlot : int { kAuxA = 0, kAuxB, kAuxC, kAuxX, kAuxY, kAuxAr, kAuxBr, kAuxP, kAuxT };
 static_assert(kAuxT < kSlotCount, "aux slots");
 
 // A device or managed operand aligned for `elem`-byte element loads is used in place.
@@ -322,46 +322,44 @@ namespace {
 // row-major form.  A and B are device interleaved complex operands in their stored shapes (pitches
 // la, lb); ca / cb conjugate an operand.  product == false (alpha == 0 or k == 0): C = beta C with
 // A and B not read.
+//
+// The four real products are one: the planes are laid out as [op(Ar); op(Ai)] (2M x k) and
+// [op(Br), op(Bi)] (k x 2N), so the library's real product of the two gives all four quadrants
+// (2M x 2N) at once.  Each operand is analysed and sliced once instead of twice, the fixed costs of
+// a product are paid once, and the larger product fills more tiles.  In stored terms, an untransposed
+// A keeps its planes one below the other and a transposed one side by side; for B it is the other
+// way round.  Its error bound is relative to the complex Frobenius norms ||A|| ||B||.
 template <typename T>
 int complex_product(int64_t M, int64_t N, int64_t k, bool ta, bool tb, bool ca, bool cb, const T* dA, int64_t la,
                     const T* dB, int64_t lb, const T* alpha, const T* beta, T* dC, int64_t ldc, bool product,
                     const LaunchCtl& ctl, cudaStream_t s, std::string* err) {
     Runtime& r = runtime();
-    int st = GB300_OK;
-    T* Pr = static_cast<T*>(r.aux.get(kAuxP, size_t(2) * size_t(M) * size_t(N) * sizeof(T), err));
-    if (!Pr) return GB300_ERR_NO_MEMORY;
-    T* Pi = Pr + M * N;
+    T* P = static_cast<T*>(r.aux.get(kAuxP, size_t(4) * size_t(M) * size_t(N) * sizeof(T), err));
+    if (!P) return GB300_ERR_NO_MEMORY;
     if (product) {
         const int64_t ra = ta ? k : M, cA = ta ? M : k;  // stored shapes
         const int64_t rb = tb ? N : k, cB = tb ? k : N;
-        T* Ar = static_cast<T*>(r.aux.get(kAuxAr, size_t(ra) * size_t(cA) * sizeof(T), err));
-        T* Ai = static_cast<T*>(r.aux.get(kAuxAi, size_t(ra) * size_t(cA) * sizeof(T), err));
-        T* Br = static_cast<T*>(r.aux.get(kAuxBr, size_t(rb) * size_t(cB) * sizeof(T), err));
-        T* Bi = static_cast<T*>(r.aux.get(kAuxBi, size_t(rb) * size_t(cB) * sizeof(T), err));
-        if (!Ar || !Ai || !Br || !Bi) return GB300_ERR_NO_MEMORY;
-        cudaError_t e = launch_split_complex<T>(ra, cA, dA, la, Ar, Ai, s);
-        if (e == cudaSuccess) e = launch_split_complex<T>(rb, cB, dB, lb, Br, Bi, s);
+        T* A2 = static_cast<T*>(r.aux.get(kAuxAr, size_t(2) * size_t(ra) * size_t(cA) * sizeof(T), err));
+        T* B2 = static_cast<T*>(r.aux.get(kAuxBr, size_t(2) * size_t(rb) * size_t(cB) * sizeof(T), err));
+        if (!A2 || !B2) return GB300_ERR_NO_MEMORY;
+        const int64_t la2 = ta ? 2 * cA : cA, lb2 = tb ? cB : 2 * cB;
+        cudaError_t e = launch_split_complex<T>(ra, cA, dA, la, A2, ta ? A2 + cA : A2 + ra * cA, la2, s);
+        if (e == cudaSuccess) e = launch_split_complex<T>(rb, cB, dB, lb, B2, tb ? B2 + rb * cB : B2 + cB, lb2, s);
         if (e != cudaSuccess) {
             if (err) *err = std::string("complex split: ") + cudaGetErrorString(e);
             return GB300_ERR_CUDA;
         }
-        // op(A) = Ar' + i sa Ai', op(B) = Br' + i sb Bi' (sa = -1 for a conjugated operand):
-        // Re = Ar'Br' - sa sb Ai'Bi',  Im = sb Ar'Bi' + sa Ai'Br'
-        const double sa = ca ? -1.0 : 1.0, sb = cb ? -1.0 : 1.0;
-        auto prod = [&](const T* X, const T* Y, T* Z, double al, double be) {
-            Gemm g;
-            g.m = M; g.n = N; g.k = k; g.ta = ta; g.tb = tb;
-            g.A = X; g.lda = cA; g.B = Y; g.ldb = cB; g.C = Z; g.ldc = N;
-            g.alpha = al; g.beta = be;
-            return real_product<T>(g, ctl, s, err);
-        };
-        if ((st = prod(Ar, Br, Pr, 1.0, 0.0)) != GB300_OK || (st = prod(Ai, Bi, Pr, -sa * sb, 1.0)) != GB300_OK ||
-            (st = prod(Ar, Bi, Pi, sb, 0.0)) != GB300_OK || (st = prod(Ai, Br, Pi, sa, 1.0)) != GB300_OK)
-            return st;
+        Gemm g;
+        g.m = 2 * M; g.n = 2 * N; g.k = k; g.ta = ta; g.tb = tb;
+        g.A = A2; g.lda = la2; g.B = B2; g.ldb = lb2; g.C = P; g.ldc = 2 * N;
+        g.alpha = 1.0; g.beta = 0.0;
+        const int st = real_product<T>(g, ctl, s, err);
+        if (st != GB300_OK) return st;
     } else {
-        cudaMemsetAsync(Pr, 0, size_t(2) * size_t(M) * size_t(N) * sizeof(T), s);
+        cudaMemsetAsync(P, 0, size_t(4) * size_t(M) * size_t(N) * sizeof(T), s);
     }
-    const cudaError_t e = launch_complex_epilogue<T>(M, N, Pr, Pi, alpha[0], alpha[1], beta[0], beta[1], dC, ldc, s);
+    const cudaError_t e = launch_complex_quadrants<T>(M, N, P, product && ca, product && cb, alpha[0], alpha[1],
+                                                      beta[0], beta[1], dC, ldc, s);
     if (e != cudaSuccess) {
         if (err) *err = std::string("complex epilogue: ") + cudaGetErrorString(e);
         return GB300_ERR_CUDA;
@@ -511,7 +509,7 @@ int trmm_entry(int order, int side, int uplo, int transA, int diag, int64_t m, i
 }
 
 // Complex B = alpha op(A) B or alpha B op(A), A triangular: the masked complex triangle and one
-// complex product (four real products).
+// complex product.
 template <typename T>
 int ctrmm_entry(int order, int side, int uplo, int transA, int diag, int64_t m, int64_t n, const T* alpha, const T* A,
                 int64_t lda, T* B, int64_t ldb, const char* routine) {

@@ -1,7 +1,7 @@
 // level23.cu — kernels of the BLAS routines next to ?gemm on Blaze's seam: ?gemv and ?trmv (matrix x
-// vector, real or complex, a triangle optionally masked), complex ?gemm (four real products over
-// split real / imaginary planes) and ?trmm (triangular product through a masked copy of the
-// triangle).  The host entries are in api_next.cpp.
+// vector, real or complex, a triangle optionally masked), complex ?gemm (one real product of the
+// stacked real / imaginary planes, recombined from its quadrants) and ?trmm (triangular product
+// through a masked copy of the triangle).  The host entries are in api_next.cpp.
 //
 // Matrix operands are described in row-major storage (rows x cols, pitch ld); a column-major
 // CBLAS operand is the transpose of its row-major storage, which the host folds into the
@@ -110,40 +110,45 @@ __global__ void __launch_bounds__(256) mv_cols_reduce_kernel(int64_t cols, int s
 // The element-wise kernels below take rows on blockIdx.y (striding by gridDim.y) and columns on
 // threads (striding by the grid's x extent): no index division per element.
 
-// Interleaved complex rows x cols (pitch ld, in complex elements) -> dense real planes re, im.
+// Interleaved complex rows x cols (pitch ld, in complex elements) -> real planes re, im (pitch
+// out_ld each; the caller places them side by side or one below the other).
 template <typename T>
 __global__ void split_complex_kernel(int64_t rows, int64_t cols, const T* __restrict__ Z, int64_t ld,
-                                     T* __restrict__ re, T* __restrict__ im) {
+                                     T* __restrict__ re, T* __restrict__ im, int64_t out_ld) {
     for (int64_t r = blockIdx.y; r < rows; r += gridDim.y)
         for (int64_t c = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; c < cols; c += int64_t(gridDim.x) * blockDim.x) {
             const T* z = Z + 2 * (r * ld + c);
-            re[r * cols + c] = z[0];
-            im[r * cols + c] = z[1];
+            re[r * out_ld + c] = z[0];
+            im[r * out_ld + c] = z[1];
         }
 }
 
-// C (interleaved, pitch ldc) = alpha * (Pr + i Pi) + beta * C for rows x cols (P dense).  With
-// alpha = 1 and beta = 0 (what Blaze passes for C = A * B) the planes are only interleaved: no FP64
-// arithmetic, which on GB300 would bound this kernel by the FP64 pipe.
-template <typename T>
-__global__ void complex_epilogue_kernel(int64_t rows, int64_t cols, const T* __restrict__ Pr, const T* __restrict__ Pi,
-                                       T ar, T ai, T br, T bi, T* __restrict__ C, int64_t ldc) {
-    const bool beta0 = (br == T(0) && bi == T(0));
-    const int64_t cstep = int64_t(gridDim.x) * blockDim.x, c0 = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (beta0 && ar == T(1) && ai == T(0)) {  // the branch stays outside the loops: a copy
-        for (int64_t r = blockIdx.y; r < rows; r += gridDim.y)
-            for (int64_t c = c0; c < cols; c += cstep) {
-                T* z = C + 2 * (r * ldc + c);
-                z[0] = Pr[r * cols + c];
-                z[1] = Pi[r * cols + c];
-            }
-        return;
-    }
-    for (int64_t r = blockIdx.y; r < rows; r += gridDim.y)
+// C (rows x cols interleaved, pitch ldc) = alpha (Re + i Im) + beta C from the quadrants of the real
+// product P = [op(Ar); op(Ai)] [op(Br), op(Bi)] (2 rows x 2 cols, pitch 2 cols):
+// Re = P00 - SAB P11 and Im = SB (P01 + SAB P10), where SB = -1 conjugates B and SAB = -1 when
+// exactly one operand is conjugated.  The signs are template arguments, so each combination is one
+// FP64 add; with alpha = 1 and beta = 0 (what Blaze passes) nothing else is computed.
+template <typename T, int SAB, int SB>
+__global__ void complex_quadrant_kernel(int64_t rows, int64_t cols, const T* __restrict__ P, T ar, T ai, T br, T bi,
+                                        T* __restrict__ C, int64_t ldc) {
+    const bool plain = ar == T(1) && ai == T(0) && br == T(0) && bi == T(0);
+    const bool beta0 = br == T(0) && bi == T(0);
+    const int64_t ldp = 2 * cols, cstep = int64_t(gridDim.x) * blockDim.x;
+    const int64_t c0 = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    for (int64_t r = blockIdx.y; r < rows; r += gridDim.y) {
+        const T* p0 = P + r * ldp;           // P00 | P01
+        const T* p1 = P + (r + rows) * ldp;  // P10 | P11
         for (int64_t c = c0; c < cols; c += cstep) {
+            const T re = SAB > 0 ? p0[c] - p1[cols + c] : p0[c] + p1[cols + c];
+            const T s = SAB > 0 ? p0[cols + c] + p1[c] : p0[cols + c] - p1[c];
+            const T im = SB > 0 ? s : -s;
             T* z = C + 2 * (r * ldc + c);
-            const T pr = Pr[r * cols + c], pi = Pi[r * cols + c];
-            T cr = ar * pr - ai * pi, ci = ar * pi + ai * pr;
+            if (plain) {
+                z[0] = re;
+                z[1] = im;
+                continue;
+            }
+            T cr = ar * re - ai * im, ci = ar * im + ai * re;
             if (!beta0) {
                 const T zr = z[0], zi = z[1];
                 cr += br * zr - bi * zi;
@@ -152,6 +157,7 @@ __global__ void complex_epilogue_kernel(int64_t rows, int64_t cols, const T* __r
             z[0] = cr;
             z[1] = ci;
         }
+    }
 }
 
 // ---- triangle --------------------------------------------------------------------------------
@@ -222,16 +228,26 @@ cudaError_t launch_mv(const MvForm& f, int64_t rows, int64_t cols, const T* alph
 }
 
 template <typename T>
-cudaError_t launch_split_complex(int64_t rows, int64_t cols, const T* Z, int64_t ld, T* re, T* im, cudaStream_t st) {
-    split_complex_kernel<T><<<grid_2d(rows, cols), 256, 0, st>>>(rows, cols, Z, ld, re, im);
+cudaError_t launch_split_complex(int64_t rows, int64_t cols, const T* Z, int64_t ld, T* re, T* im, int64_t out_ld,
+                                 cudaStream_t st) {
+    split_complex_kernel<T><<<grid_2d(rows, cols), 256, 0, st>>>(rows, cols, Z, ld, re, im, out_ld);
     count_launches(1);
     return cudaGetLastError();
 }
 
 template <typename T>
-cudaError_t launch_complex_epilogue(int64_t rows, int64_t cols, const T* Pr, const T* Pi, T ar, T ai, T br, T bi, T* C,
-                                   int64_t ldc, cudaStream_t st) {
-    complex_epilogue_kernel<T><<<grid_2d(rows, cols), 256, 0, st>>>(rows, cols, Pr, Pi, ar, ai, br, bi, C, ldc);
+cudaError_t launch_complex_quadrants(int64_t rows, int64_t cols, const T* P, bool conj_a, bool conj_b, T ar, T ai,
+                                     T br, T bi, T* C, int64_t ldc, cudaStream_t st) {
+    const dim3 grid = grid_2d(rows, cols);
+    const bool sab_pos = conj_a == conj_b;
+    if (sab_pos && !conj_b)
+        complex_quadrant_kernel<T, 1, 1><<<grid, 256, 0, st>>>(rows, cols, P, ar, ai, br, bi, C, ldc);
+    else if (sab_pos)
+        complex_quadrant_kernel<T, 1, -1><<<grid, 256, 0, st>>>(rows, cols, P, ar, ai, br, bi, C, ldc);
+    else if (!conj_b)
+        complex_quadrant_kernel<T, -1, 1><<<grid, 256, 0, st>>>(rows, cols, P, ar, ai, br, bi, C, ldc);
+    else
+        complex_quadrant_kernel<T, -1, -1><<<grid, 256, 0, st>>>(rows, cols, P, ar, ai, br, bi, C, ldc);
     count_launches(1);
     return cudaGetLastError();
 }
@@ -255,13 +271,13 @@ GB_MV(double, true)
 GB_MV(float, false)
 GB_MV(float, true)
 #undef GB_MV
-template cudaError_t launch_split_complex<double>(int64_t, int64_t, const double*, int64_t, double*, double*,
+template cudaError_t launch_split_complex<double>(int64_t, int64_t, const double*, int64_t, double*, double*, int64_t,
                                                   cudaStream_t);
-template cudaError_t launch_split_complex<float>(int64_t, int64_t, const float*, int64_t, float*, float*,
+template cudaError_t launch_split_complex<float>(int64_t, int64_t, const float*, int64_t, float*, float*, int64_t,
                                                  cudaStream_t);
-template cudaError_t launch_complex_epilogue<double>(int64_t, int64_t, const double*, const double*, double, double,
+template cudaError_t launch_complex_quadrants<double>(int64_t, int64_t, const double*, bool, bool, double, double,
                                                      double, double, double*, int64_t, cudaStream_t);
-template cudaError_t launch_complex_epilogue<float>(int64_t, int64_t, const float*, const float*, float, float, float,
+template cudaError_t launch_complex_quadrants<float>(int64_t, int64_t, const float*, bool, bool, float, float, float,
                                                     float, float*, int64_t, cudaStream_t);
 
 }  // namespace gb

@@ -31,14 +31,19 @@ template <typename T, bool CPLX>
 cudaError_t launch_mv(const MvForm& f, int64_t rows, int64_t cols, const T* alpha, const T* S, int64_t ld, const T* x,
                       int64_t incx, const T* beta, T* y, int64_t incy, T* part, int slices, cudaStream_t st);
 
-// Interleaved complex rows x cols (pitch ld in complex elements) -> dense real planes.
+// Interleaved complex rows x cols (pitch ld in complex elements) -> real planes re and im, each with
+// pitch out_ld (side by side: im = re + cols, out_ld = 2 cols; one below the other: im = re +
+// rows cols, out_ld = cols).
 template <typename T>
-cudaError_t launch_split_complex(int64_t rows, int64_t cols, const T* Z, int64_t ld, T* re, T* im, cudaStream_t st);
+cudaError_t launch_split_complex(int64_t rows, int64_t cols, const T* Z, int64_t ld, T* re, T* im, int64_t out_ld,
+                                 cudaStream_t st);
 
-// C (interleaved, pitch ldc) = (ar + i ai) (Pr + i Pi) + (br + i bi) C.
+// C (rows x cols, interleaved, pitch ldc) = alpha op(A) op(B) + beta C from the real product
+// P = [op(Ar); op(Ai)] [op(Br), op(Bi)] (2 rows x 2 cols, pitch 2 cols) of the planes with the
+// conjugations (conj_a, conj_b) not yet applied; alpha = (ar, ai), beta = (br, bi).
 template <typename T>
-cudaError_t launch_complex_epilogue(int64_t rows, int64_t cols, const T* Pr, const T* Pi, T ar, T ai, T br, T bi, T* C,
-                                   int64_t ldc, cudaStream_t st);
+cudaError_t launch_complex_quadrants(int64_t rows, int64_t cols, const T* P, bool conj_a, bool conj_b, T ar, T ai,
+                                     T br, T bi, T* C, int64_t ldc, cudaStream_t st);
 
 // Dense copy of the lower (or upper) triangle of the n x n row-major A, zeros elsewhere, ones on
 // the diagonal when `unit` (CPLX: interleaved complex elements).
