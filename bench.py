@@ -55,7 +55,8 @@ def parse():
     ap.add_argument("--sweep", default="", help="comma list of sweep groups to run instead of the main line: "
                                                  "square (4096/8192/16384, rr/rc, uniform/spread, native/split S=3..8/"
                                                  "bf16x3), rect ((M,K,N) = (65536,256,256), (256,65536,256), "
-                                                 "(4096,4096,64), column-major A)")
+                                                 "(4096,4096,64), column-major A), trsm (dtrsm at each "
+                                                 "--sweep-sizes, left / right x lower / upper x N / T, and ztrsm)")
     ap.add_argument("--sweep-sizes", default="4096,8192,16384")
     ap.add_argument("--serve-requests", type=int, default=240)
     ap.add_argument("--serve-rates", default="40,160", help="Poisson arrival rates (requests/s) to sweep")
@@ -839,6 +840,52 @@ def sweep(args):
                                   "operand_gbs": round(bytes_ / (ms * 1e-3) / 1e9, 1),
                                   "normwise_error": err, "bound": info.error_bound}), flush=True)
             del dA, dB, dC
+    if "trsm" in groups:
+        # square triangular solves (m = n) with well-conditioned triangles (off-diagonal u / n,
+        # diagonal 1 + u / 2); m^2 n flops (4 m^2 n complex); error against cuBLAS's FP64 solve
+        for n in [int(x) for x in args.sweep_sizes.split(",") if x]:
+            gen = torch.Generator(device="cuda").manual_seed(args.seed)
+            for cplx in (False, True):
+                if cplx and n > 8192:
+                    continue
+                def U():
+                    return torch.rand(n * n, generator=gen, device="cuda", dtype=torch.float64) * 2 - 1
+                T = (torch.complex(U(), U()) if cplx else U()).view(n, n) / n
+                T.diagonal().copy_(1 + 0.5 * n * T.diagonal())
+                B0 = (torch.complex(U(), U()) if cplx else U()).view(n, n)
+                X = torch.empty_like(B0)
+                torch.cuda.synchronize()
+                forms = [(141, 122, 111)] if cplx else [(sd, up, tr) for sd in (141, 142) for up in (122, 121)
+                                                        for tr in (111, 112)]
+                for side, uplo, trans in forms:
+                    def run():
+                        X.copy_(B0)
+                        torch.cuda.synchronize()
+                        G.cblas_trsm(101, side, uplo, trans, 131, n, n, (1 + 0j) if cplx else 1.0, T, n, X, n,
+                                     dtype="z" if cplx else "d")
+                    t_copy = time.perf_counter()  # the refill of X, timed on its own first
+                    for _ in range(3):
+                        X.copy_(B0)
+                        torch.cuda.synchronize()
+                    t_copy = (time.perf_counter() - t_copy) / 3
+                    run()
+                    t0 = time.perf_counter()
+                    for _ in range(3):
+                        run()
+                    t = (time.perf_counter() - t0) / 3 - t_copy  # X holds the last solve
+                    lower = (uplo == 122) == (trans == 111)
+                    opT = (T.transpose(0, 1) if trans == 112 else T)
+                    tri = torch.tril(opT) if lower else torch.triu(opT)
+                    try:  # cuBLAS's solve through torch (its linear-algebra library may be absent)
+                        ref = torch.linalg.solve_triangular(tri, B0, upper=not lower, left=side == 141)
+                        err = float((torch.linalg.norm(X - ref) / torch.linalg.norm(ref)).item())
+                    except RuntimeError:
+                        err = None
+                    fl = (4.0 if cplx else 1.0) * float(n) ** 3
+                    print(json.dumps({"sweep": "trsm", "n": n, "complex": cplx, "side": side, "uplo": uplo,
+                                      "trans": trans, "ms": round(t * 1e3, 3), "tflops": round(fl / t / 1e12, 2),
+                                      "rel_diff_vs_cublas": err}), flush=True)
+                del T, B0, X
 
 
 def main():
