@@ -80,6 +80,7 @@ constexpr int EPI_WARPS = 8;
 constexpr int THREADS = 64 + EPI_WARPS * 32;
 constexpr int MAX_SLICES = 10;
 constexpr int KSEG_UNIT = 256;          // k-segments are multiples of this
+constexpr int kPipeMaxQ = 2;            // column blocks of B in the host-operand pipeline
 constexpr uint32_t MAGIC_BITS = 0x4B400000u;  // bits of 1.5 * 2^23
 constexpr float MAGIC = 12582912.0f;
 
@@ -1992,16 +1993,19 @@ int device_product_host_panels(const Gemm& g, const SplitRequest& req, const Lau
         return GB300_ERR_NOT_SUPPORTED;
     const SplitGeometry G = split_geometry(g, req, r.num_sms);
     if (G.mode != kCrt) return GB300_ERR_NOT_SUPPORTED;
-    // blocks: row panels of about a quarter of A (at least 2048 rows) and two column blocks of B
-    // (when each has at least 2048 columns), whole pair tiles.  (Loading A and B alternately in
-    // quarters over a 4 x 4 grid starts the first block earlier but measured 6 % slower end to end
-    // at 8192^3: the copies of C back then share the link with more of the copies in.)
+    // blocks: row panels of about a quarter of A (at least 2048 rows) and up to kPipeMaxQ column
+    // blocks of B of at least 2048 columns each, whole pair tiles.  Four column blocks at 8192^3
+    // start the first block earlier (A_0 and B_0 are 256 MiB instead of 384) but measured the same
+    // end to end and 1 % slower with pageable memory; loading A and B alternately in quarters over a
+    // 4 x 4 grid measured 6 % slower (the copies of C back then share the link with more of the
+    // copies in).
     const bool c_locked = page_locked(g.C);
     const int64_t Mp = std::max<int64_t>(2048, round_up((m + 3) / 4, TMP));
     const int P = int((m + Mp - 1) / Mp);
-    const int64_t Nq = n >= 4096 ? round_up((n + 1) / 2, TN) : round_up(n, TN);
+    const int64_t Q0 = std::max<int64_t>(1, std::min<int64_t>(kPipeMaxQ, n / 2048));
+    const int64_t Nq = round_up((n + Q0 - 1) / Q0, TN);
     const int Q = int((n + Nq - 1) / Nq);
-    if (P < 2 || P > 16 || Q > 2) return GB300_ERR_NOT_SUPPORTED;
+    if (P < 2 || P > 16 || Q > kPipeMaxQ) return GB300_ERR_NOT_SUPPORTED;
     if (!pipe_init(r, err)) return GB300_ERR_CUDA;
     Gemm gp = g;
     gp.m = Mp;
@@ -2128,7 +2132,7 @@ int device_product_host_panels(const Gemm& g, const SplitRequest& req, const Lau
     };
 
     // ---- tensor maps: A panel planes, each B block's planes, the level planes of a block ----
-    CUtensorMap tA, tC, tB[2];  // Q <= 2
+    CUtensorMap tA, tC, tB[kPipeMaxQ];
     if (!encode_tmap_2d(&tA, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, pa, uint64_t(max_planes) * mpad, kpad, kpad, TM, TK,
                         CU_TENSOR_MAP_SWIZZLE_128B, err) ||
         !encode_tmap_2d(&tC, CU_TENSOR_MAP_DATA_TYPE_UINT16, 2, lv, uint64_t(nseg) * max_levels * mpad, Nq, Nq, 32, 64,
@@ -2205,7 +2209,7 @@ int device_product_host_panels(const Gemm& g, const SplitRequest& req, const Lau
         cudaEventRecord(block_ev(i, j), st);
         if (c_locked) copy_block_out(i, j);
     };
-    bool have_a[16] = {}, have_b[2] = {};
+    bool have_a[16] = {}, have_b[kPipeMaxQ] = {};
     auto load = [&](int side, int idx) {
         if (side == 0) {
             copy_a(idx);

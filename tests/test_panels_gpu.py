@@ -40,9 +40,12 @@ def device_run(order, ta, tb, m, n, k, A, lda, B, ldb, C, ldc, alpha, beta, meth
 
 @pytest.mark.parametrize("memory", ["pinned", "pageable"])
 @pytest.mark.parametrize("ta,tb,n", [(O.NO_TRANS, O.NO_TRANS, 520), (O.TRANS, O.NO_TRANS, 520),
-                                     (O.NO_TRANS, O.TRANS, 4400), (O.TRANS, O.TRANS, 4400)])
+                                     (O.NO_TRANS, O.TRANS, 4400), (O.TRANS, O.TRANS, 4400),
+                                     (O.NO_TRANS, O.NO_TRANS, 6500), (O.TRANS, O.NO_TRANS, 8800)])
 def test_panels_match_the_device_path_and_the_bound(ta, tb, n, memory):
-    m, k = 4608, 900  # three panels: 2048, 2048, 512 rows; n = 4400: two column blocks, 2304 + 2096
+    # three panels: 2048, 2048, 512 rows; two column blocks: n = 4400 2304 + 2096, n = 6500
+    # 3328 + 3172, n = 8800 4608 + 4192
+    m, k = 4608, 900
     alpha, beta = 1.25, -0.5
     lda = (m if ta == O.TRANS else k) + 3
     ldb = (k if tb == O.TRANS else n) + 1
