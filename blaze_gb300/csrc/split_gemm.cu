@@ -445,16 +445,30 @@ __device__ __forceinline__ double pow2i(int x) {
     return x < -1022 ? 0.0 : __longlong_as_double((long long)(x + 1023) << 52);
 }
 
-__global__ void __launch_bounds__(1024) split_info_kernel(const RowPartial* __restrict__ part, int nA, int nB, int64_t k,
-                                                           int mode, int fixed_slices, int cap_planes, double target,
-                                                           SplitInfo* info) {
-    __shared__ double redd[32];
-    __shared__ int redi[32];
+// One warp: the partials are few (one per 256 rows or columns), and the shuffle reductions need no
+// barriers.  A block of 1024 threads spent most of the kernel's 25 us in the barriers and the
+// serial combining steps of nine block-wide reductions.
+__device__ __forceinline__ int warp_max(int v) {
+    for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+__device__ __forceinline__ long long warp_max(long long v) {
+    for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+__device__ __forceinline__ double warp_sum(double v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__global__ void __launch_bounds__(32) split_info_kernel(const RowPartial* __restrict__ part, int nA, int nB, int64_t k,
+                                                         int mode, int fixed_slices, int cap_planes, double target,
+                                                         SplitInfo* info) {
     // the per-block partials of A (the first nA) and B: Inf/NaN flag, largest exponents, largest
     // row / column sums of squares relative to 2^(2e)
     int bad = 0, EA = kNoRows, EB = kNoRows;
     long long QAb = 0, QBb = 0;
-    for (int i = threadIdx.x; i < nA + nB; i += blockDim.x) {
+    for (int i = threadIdx.x; i < nA + nB; i += 32) {
         const RowPartial p = part[i];
         bad |= p.bad;
         if (i < nA) {
@@ -465,15 +479,15 @@ __global__ void __launch_bounds__(1024) split_info_kernel(const RowPartial* __re
             QBb = max(QBb, p.Qbits);
         }
     }
-    bad = block_max_int(bad, redi);
-    EA = block_max_int(EA, redi);
-    EB = block_max_int(EB, redi);
-    const double QA = __longlong_as_double(block_max_ll(QAb, reinterpret_cast<long long*>(redd)));
-    const double QB = __longlong_as_double(block_max_ll(QBb, reinterpret_cast<long long*>(redd)));
+    bad = warp_max(bad);
+    EA = warp_max(EA);
+    EB = warp_max(EB);
+    const double QA = __longlong_as_double(warp_max(QAb));
+    const double QB = __longlong_as_double(warp_max(QBb));
     // the sums relative to the largest exponent: each block's relative to its own, rescaled by an
     // exact power of two
     double sa = 0, na = 0, sb = 0, nb = 0;
-    for (int i = threadIdx.x; i < nA + nB; i += blockDim.x) {
+    for (int i = threadIdx.x; i < nA + nB; i += 32) {
         const RowPartial p = part[i];
         if (p.E == kNoRows) continue;
         if (i < nA) {
@@ -486,10 +500,10 @@ __global__ void __launch_bounds__(1024) split_info_kernel(const RowPartial* __re
             nb += w * p.nrm;
         }
     }
-    sa = block_sum(sa, redd);
-    na = block_sum(na, redd);
-    sb = block_sum(sb, redd);
-    nb = block_sum(nb, redd);
+    sa = warp_sum(sa);
+    na = warp_sum(na);
+    sb = warp_sum(sb);
+    nb = warp_sum(nb);
     if (threadIdx.x < 32) {  // warp 0 plans; lane 0 writes
         const int lane = threadIdx.x;
         // Each FP64 function below runs once for the warp with a different argument in each lane
@@ -1824,7 +1838,7 @@ int device_product(const Gemm& g_in, const SplitRequest& req, const LaunchCtl& c
         stats_finalize_pair_kernel<<<xb0 + xb1, 256, 0, st>>>(op, k, xb0, part);
     }
     const double target = req.target_error > 0 ? req.target_error : double(k) * 0x1p-53;
-    split_info_kernel<<<1, 1024, 0, st>>>(part, int(xb0), int(xb1), k, mode, req.slices > 0 ? max_planes : 0,
+    split_info_kernel<<<1, 32, 0, st>>>(part, int(xb0), int(xb1), k, mode, req.slices > 0 ? max_planes : 0,
                                          max_planes, target, info);
     if (cudaError_t le = cudaGetLastError(); le != cudaSuccess) {
         if (err) *err = std::string("split pre-pass launch: ") + cudaGetErrorString(le);
