@@ -740,7 +740,10 @@ def ours(args, dist: Dist):
                                      "split, digit scheme (Ozaki BF16 slices on tcgen05, exact int32 slice sums, FP64 "
                                      "recombination)",
                            "slices": info.slices_used, "target_error": f"k*2^-53 = {n * 2.0 ** -53:.3e}",
-                           "l2": "operands larger than L2 (512 MiB each)", "parallelism": "replicas"},
+                           "l2": (f"operands larger than L2 ({n * n * 8 >> 20} MiB each)" if n * n * 8 > (129 << 20)
+                                  else f"operands of {n * n * 8 >> 20} MiB each fit L2 (129 MiB): repeated steps "
+                                       "read them from L2"),
+                           "parallelism": "replicas"},
                 "accuracy": {"normwise_error": err, "a_priori_bound": info.error_bound,
                              "target": n * 2.0 ** -53, "oracle": "Dot2 compensated FP64 on every "
                                                                  f"{max(1, n // 32)}th row"},
