@@ -117,15 +117,38 @@ __device__ W block_sum_256(W v) {
     return v;
 }
 
-// part[b] = sum over i in [b chunk, (b + 1) chunk) of op(x_i) y_i.
-template <typename V, bool CONJ>
+// Elements per 16-byte group of a contiguous vector.
+template <typename V>
+__host__ __device__ constexpr int dot_group() { return sizeof(V) >= 16 ? 1 : int(16 / sizeof(V)); }
+
+// part[b] = sum over i in [b chunk, (b + 1) chunk) of op(x_i) y_i.  Contiguous vectors go in groups
+// of G = 16 / sizeof(V) elements: thread t takes groups t, t + 256, ... of its block's chunk (chunk
+// a multiple of G), loaded as one 16-byte vector each when both vectors are 16-byte aligned (VEC)
+// and element by element otherwise, in the same order, so the sum's bits do not depend on the
+// alignment.
+template <typename V, bool CONJ, bool VEC>
 __global__ void __launch_bounds__(256) dot_partial_kernel(int64_t n, const V* __restrict__ x, int64_t incx,
                                                           const V* __restrict__ y, int64_t incy, int64_t chunk,
                                                           typename DotAcc<V, CONJ>::W* __restrict__ part) {
+    constexpr int G = dot_group<V>();
+    struct alignas(16) Group {
+        V v[G];
+    };
     DotAcc<V, CONJ> acc;
     const int64_t i0 = int64_t(blockIdx.x) * chunk, i1 = min(n, i0 + chunk);
     if (incx == 1 && incy == 1) {
-        for (int64_t i = i0 + threadIdx.x; i < i1; i += 256) acc.add(x[i], y[i]);
+        int64_t i = i0 + int64_t(threadIdx.x) * G;
+        for (; i + G <= i1; i += 256 * G) {
+            if (VEC) {
+                const Group a = *reinterpret_cast<const Group*>(x + i), b = *reinterpret_cast<const Group*>(y + i);
+#pragma unroll
+                for (int w = 0; w < G; ++w) acc.add(a.v[w], b.v[w]);
+            } else {
+#pragma unroll
+                for (int w = 0; w < G; ++w) acc.add(x[i + w], y[i + w]);
+            }
+        }
+        for (; i < i1; ++i) acc.add(x[i], y[i]);  // the ragged end of the last group
     } else {
         for (int64_t i = i0 + threadIdx.x; i < i1; i += 256) acc.add(x[i * incx], y[i * incy]);
     }
@@ -172,12 +195,16 @@ cudaError_t launch_dot(int64_t n, const T* x, int64_t incx, const T* y, int64_t 
                        cudaStream_t st) {
     using V = typename std::conditional<CPLX, Cx<T>, T>::type;
     using W = typename DotAcc<V, CONJ>::W;
+    constexpr int G = dot_group<V>();
     const int parts = dot_parts(n);
-    const int64_t chunk = (n + parts - 1) / parts;
-    dot_partial_kernel<V, CONJ><<<unsigned(parts), 256, 0, st>>>(n, reinterpret_cast<const V*>(x), incx,
-                                                                 reinterpret_cast<const V*>(y), incy, chunk,
-                                                                 reinterpret_cast<W*>(part));
-    dot_final_kernel<W><<<1, 256, 0, st>>>(parts, reinterpret_cast<const W*>(part), reinterpret_cast<W*>(out));
+    const int64_t chunk = ((n + parts - 1) / parts + G - 1) / G * G;
+    const bool vec = incx == 1 && incy == 1 && (reinterpret_cast<uintptr_t>(x) % 16) == 0 &&
+                     (reinterpret_cast<uintptr_t>(y) % 16) == 0;
+    auto kern = vec ? dot_partial_kernel<V, CONJ, true> : dot_partial_kernel<V, CONJ, false>;
+    const int blocks = int((n + chunk - 1) / chunk);
+    kern<<<unsigned(blocks), 256, 0, st>>>(n, reinterpret_cast<const V*>(x), incx, reinterpret_cast<const V*>(y), incy,
+                                           chunk, reinterpret_cast<W*>(part));
+    dot_final_kernel<W><<<1, 256, 0, st>>>(blocks, reinterpret_cast<const W*>(part), reinterpret_cast<W*>(out));
     count_launches(2);
     return cudaGetLastError();
 }
