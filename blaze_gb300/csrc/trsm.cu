@@ -45,14 +45,19 @@ __global__ void scale_kernel(int64_t rows, int64_t cols, V alpha, V* __restrict_
 // The work is FP64 FMAs and column c needs about (nb - c)^2 / 2 of them, so the first columns set
 // the kernel's time: on GB300 one SM retires about two FP64 FMAs per clock.  A block of the grid
 // therefore takes only kInvCols columns (blockIdx.x picks the group, blockIdx.y the diagonal block)
-// and spreads each column's sums over 32 chains: lane = column + kInvCols * slice, and warp w with
-// slice s takes j = r0 + 4 w + s, then every 32nd.  The shuffles and then warp 0 add the chains in a
-// fixed order.  Warp 0 scales by the diagonal's reciprocal (computed for all rows up front, so the
+// and spreads each column's sums over kInvChains chains: lane = column + kInvCols * slice, and warp
+// w with slice s takes j = r0 + kInvSlices w + s, then every kInvChains-th.  The shuffles and then
+// warp 0 add the chains in a fixed order.  Those adds cost FP64 instructions every row: with
+// 8-column groups they are 40 % of the kernel's 18.9 M FP64 instructions at 8192 rows (1.71 ms,
+// FP64 pipe 80 % active).  16-column groups halve them but measured slower (1.77-1.87 ms): the
+// heaviest group then does twice the FMAs on one SM.  Warp 0 scales by the diagonal's reciprocal (computed for all rows up front, so the
 // serial step per row is a multiply) and publishes Y[r] in shared memory before the next row.
 // Y[j][c] = 0 for j < c comes out of the recurrence itself, so the loops are the same for every
 // column of a group, which starts at its first column r0.  A unit diagonal is not read.
 constexpr int kInvWarps = 8;
-constexpr int kInvCols = 8;
+constexpr int kInvCols = 8;                      // columns per grid block
+constexpr int kInvSlices = 32 / kInvCols;        // lanes per column in a warp
+constexpr int kInvChains = kInvWarps * kInvSlices;  // FMA chains per column
 
 template <typename V>
 __global__ void __launch_bounds__(32 * kInvWarps) tri_inverse_kernel(int64_t ka, int nb, const V* __restrict__ SA,
@@ -64,7 +69,7 @@ __global__ void __launch_bounds__(32 * kInvWarps) tri_inverse_kernel(int64_t ka,
     V* part = rdiag + nb;                                    // [kInvWarps][kInvCols]
     using A = Ar<V>;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int cl = lane % kInvCols, slice = lane / kInvCols;  // 4 slices
+    const int cl = lane % kInvCols, slice = lane / kInvCols;
     const int64_t b0 = int64_t(blockIdx.y) * nb;
     const int nbk = int(min(int64_t(nb), ka - b0));
     const int r0 = int(blockIdx.x) * kInvCols;
@@ -92,17 +97,18 @@ __global__ void __launch_bounds__(32 * kInvWarps) tri_inverse_kernel(int64_t ka,
         if (cc < nbk) out[o0 + r * orow + cc * ocol] = A::zero();
     }
     __syncthreads();
-    const int chain = warp * 4 + slice;  // 0..31
-    const int64_t lstep = 32 * sj;
+    const int chain = warp * kInvSlices + slice;
+    const int64_t lstep = kInvChains * sj;
     for (int r = r0; r < nbk; ++r) {
         V s = A::zero();
         int j = r0 + chain;
         const V* lp = P + r * sr + j * sj;
         const V* yp = ycol + (j - r0) * kInvCols + cl;
-        for (; j < r; j += 32, lp += lstep, yp += 32 * kInvCols) s = A::fmadd(conj ? A::conj(*lp) : *lp, *yp, s);
-        // the four slices of this warp (lanes cl, cl + 8, cl + 16, cl + 24), then the warps
-        s = A::add(s, A::shfl_xor(s, kInvCols));
-        s = A::add(s, A::shfl_xor(s, 2 * kInvCols));
+        for (; j < r; j += kInvChains, lp += lstep, yp += kInvChains * kInvCols)
+            s = A::fmadd(conj ? A::conj(*lp) : *lp, *yp, s);
+        // the slices of this warp (lanes cl, cl + kInvCols, ...), then the warps
+#pragma unroll
+        for (int o = kInvCols; o < 32; o *= 2) s = A::add(s, A::shfl_xor(s, o));
         if (slice == 0) part[warp * kInvCols + cl] = s;
         __syncthreads();
         if (warp == 0 && slice == 0) {
