@@ -261,3 +261,36 @@ def test_large_dot_deterministic_and_device_resident():
     G.cblas_axpy(n, -2.0, dx, 1, dz, 1)
     torch.cuda.synchronize()
     assert torch.equal(dz, dy - 2.0 * dx)  # 2 x is exact, so y - 2 x rounds once, like the FMA
+
+
+def test_ilp64_entries_compute_the_same():
+    """The _64 symbols (BLAZE_BLAS_IS_64BIT) of the new routines give the 32-bit entries' results."""
+    import ctypes as ct
+    L = G.lib()
+    I64, VP = ct.c_int64, ct.c_void_p
+    L.cblas_ddot_64.argtypes = [I64, VP, I64, VP, I64]
+    L.cblas_ddot_64.restype = ct.c_double
+    L.cblas_daxpy_64.argtypes = [I64, ct.c_double, VP, I64, VP, I64]
+    L.cblas_daxpy_64.restype = None
+    L.cblas_dtrsm_64.argtypes = [ct.c_int] * 5 + [I64, I64, ct.c_double, VP, I64, VP, I64]
+    L.cblas_dtrsm_64.restype = None
+    L.cblas_zdotc_sub_64.argtypes = [I64, VP, I64, VP, I64, VP]
+    L.cblas_zdotc_sub_64.restype = None
+    n = 3001
+    x, y = O.uniform(n, 81).copy(), O.uniform(n, 82).copy()
+    assert L.cblas_ddot_64(n, x.ctypes.data, 1, y.ctypes.data, 1) == G.cblas_dot(n, x, 1, y, 1)
+    y1, y2 = y.copy(), y.copy()
+    L.cblas_daxpy_64(n, -0.5, x.ctypes.data, 1, y1.ctypes.data, 1)
+    G.cblas_axpy(n, -0.5, x, 1, y2, 1)
+    assert np.array_equal(y1, y2)
+    zx, zy = O.complex_uniform(n, 83), O.complex_uniform(n, 84)
+    out = np.zeros(1, dtype=np.complex128)
+    L.cblas_zdotc_sub_64(n, zx.ctypes.data, 1, zy.ctypes.data, 1, out.ctypes.data)
+    assert out[0] == G.cblas_dot(n, zx, 1, zy, 1, dtype="z", conj=True)
+    m, k = 700, 40
+    A, B = O.triangular_operands(False, m, m, m, k, 85)
+    B1, B2 = B.copy(), B.copy()
+    L.cblas_dtrsm_64(101, 141, 122, 111, 131, m, k, 1.5, A.ctypes.data, m, B1.ctypes.data, k)
+    G.cblas_trsm(101, 141, 122, 111, 131, m, k, 1.5, A, m, B2, k)
+    assert np.array_equal(B1, B2)
+    assert G.last_error()[0] == G.OK
