@@ -521,7 +521,7 @@ def next_leg(G, torch, args):
                      "cublas_fp64_ms": round(t_ref * 1e3, 2) if t_ref else None,
                      "cublas_fp64_tflops": round(fl / t_ref / 1e12, 2) if t_ref else None,
                      "rel_diff_vs_cublas": err,
-                     "form": "recursive blocked solve: diagonal blocks (512 rows; 256 complex) inverted on the "
+                     "form": "recursive blocked solve: 512-row diagonal blocks inverted on the "
                              "FP64 pipe, products in the FP64-accurate split form"}
         del T, B0, X
     # vectors: ddot and daxpy over 2^27 doubles (1 GiB each), bytes moved / time

@@ -139,8 +139,8 @@ def axpy_cases():
 
 def trsm_cases():
     """blazetest's BLAS operation test solves 3 x 3 triangular systems with one and with several
-    right-hand sides on either side (OperationTest.h:255-715); here also triangles past the 256-row
-    leaves of the GPU's complex double solve (few right-hand sides keep the fixture small)."""
+    right-hand sides on either side (OperationTest.h:255-715); here also triangles of a few hundred
+    rows (few right-hand sides keep the fixture small)."""
     out, seed = [], 19000
     sizes = [(3, 1), (1, 3), (3, 3), (37, 16), (130, 8), (300, 6), (6, 300)]
     for cplx in (0, 1):

@@ -3,7 +3,7 @@
 - every dot / axpy / trsm case of tests/golden/next_golden.npz (Blaze's own x * y, conj(x) * y,
   y += alpha * x, and triangular systems whose right-hand sides Blaze formed as op(A) X0) within
   Blaze's relaxed equality, the check of blazetest's BLAS operation test;
-- triangular solves past several leaf blocks of the recursion (512 rows; 256 for complex double),
+- triangular solves past several 512-row leaf blocks of the recursion,
   every side / triangle /
   transposition / diagonal, against the oracle's substitution;
 - strided and negative-stride vectors, incy = 0, n <= 0, alpha = 0 (B not read, A may be NULL);
