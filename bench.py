@@ -211,9 +211,16 @@ def cpu_baseline(size: int, seconds_target: float = 12.0):
         if total >= seconds_target or reps >= 8:
             break
     tflops = 2.0 * n ** 3 * reps / total / 1e12
+    # one thread, as blazemark's single-threaded run: one product of half the size (1/8 of the work)
+    h = max(n // 2, 256)
+    t0 = time.perf_counter()
+    O.gemm(O.ROW_MAJOR, O.NO_TRANS, O.NO_TRANS, h, h, h, 1.0, A, h, B, h, 0.0, C, h, nthreads=1)
+    t1 = time.perf_counter() - t0
     return {"value": round(tflops, 5), "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"{reps} product(s) of {n}^3 FP64 (row-major x row-major, uniform [-1,1]) through the oracle's "
-                      f"restatement of Blaze's blocked mmm kernel, {threads} OpenMP threads, {total:.1f} s"}
+                      f"restatement of Blaze's blocked mmm kernel, {threads} OpenMP threads, {total:.1f} s",
+            "single_thread": {"value": round(2.0 * h ** 3 / t1 / 1e12, 5), "unit": UNIT, "cores": 1,
+                              "sample": f"one {h}^3 product, {t1:.1f} s"}}
 
 
 def cpu_check_rows(hA, hB, n: int, rows, order=101, ta=111, tb=111, m=None, k=None, lda=None, ldb=None):
