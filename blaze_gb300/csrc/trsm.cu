@@ -47,14 +47,14 @@ __global__ void scale_kernel(int64_t rows, int64_t cols, V alpha, V* __restrict_
 // therefore takes only kInvCols columns (blockIdx.x picks the group, blockIdx.y the diagonal block)
 // and spreads each column's sums over kInvChains chains: lane = column + kInvCols * slice, and warp
 // w with slice s takes j = r0 + kInvSlices w + s, then every kInvChains-th.  The shuffles and then
-// warp 0 add the chains in a fixed order.  Those adds cost FP64 instructions every row: with
-// 8-column groups they are 40 % of the kernel's 18.9 M FP64 instructions at 8192 rows (1.71 ms,
-// FP64 pipe 80 % active).  16-column groups halve them but measured slower (1.77-1.87 ms): the
-// heaviest group then does twice the FMAs on one SM.  Warp 0 scales by the diagonal's reciprocal (computed for all rows up front, so the
+// warp 0 add the chains in a fixed order.  Those adds cost FP64 instructions every row: with 8
+// warps (32 chains) they were 40 % of the kernel's 18.9 M FP64 instructions at 8192 rows (1.71 ms,
+// FP64 pipe 80 % active).  4 warps (16 chains) measured 1.44-1.53 ms and 2 warps 1.79-1.84 ms;
+// 16-column groups measured 1.77-1.87 ms (the heaviest group then does twice the FMAs on one SM).  Warp 0 scales by the diagonal's reciprocal (computed for all rows up front, so the
 // serial step per row is a multiply) and publishes Y[r] in shared memory before the next row.
 // Y[j][c] = 0 for j < c comes out of the recurrence itself, so the loops are the same for every
 // column of a group, which starts at its first column r0.  A unit diagonal is not read.
-constexpr int kInvWarps = 8;
+constexpr int kInvWarps = 4;
 constexpr int kInvCols = 8;                      // columns per grid block
 constexpr int kInvSlices = 32 / kInvCols;        // lanes per column in a warp
 constexpr int kInvChains = kInvWarps * kInvSlices;  // FMA chains per column
