@@ -723,7 +723,10 @@ def ours(args, dist: Dist):
     tc_flops = pairs * flops  # BF16 tensor operations of the slice products
     tc_ms = ms_tc / max(n_tc, 1)
     achieved = tc_flops / (tc_ms * 1e-3) / 1e12
-    peak = float(peaks.get("bf16_tflops_sustained", peaks.get("bf16_tflops")))
+    # burst peak: the kernel runs about 8 ms inside a 10 ms step, far from the seconds-long loop
+    # the sustained figure is measured over; the sustained ratio is reported beside it
+    peak = float(peaks.get("bf16_tflops"))
+    peak_sus = float(peaks.get("bf16_tflops_sustained", peak))
     traffic = None
     try:
         with open(TRAFFIC_FILE) as f:
@@ -735,7 +738,8 @@ def ours(args, dist: Dist):
     roofline = {"kernel": "tc_gemm_kernel<exact> (" + ("residue products" if info.method_used == G.METHOD_SPLIT_CRT
                                                     else "digit-slice products") + ")", "bound": "tensor",
                 "achieved": round(achieved, 2), "peak": peak, "unit": "TFLOP/s", "frac": round(achieved / peak, 4),
-                "traffic": traffic, "peak_source": f"bf16_tflops_sustained ({peaks_src})",
+                "traffic": traffic, "peak_source": f"bf16_tflops, burst ({peaks_src})",
+                "frac_of_sustained": round(achieved / peak_sus, 4),
                 "work_per_launch": f"{pairs} BF16 products x 2*{n}^3 tensor ops",
                 "kernel_ms": round(tc_ms, 3), "kernel_share_of_step": round(tc_ms / ms_step, 4)}
 

@@ -169,6 +169,7 @@ def lib() -> ct.CDLL:
     L.gb300_device_info.argtypes = [ct.POINTER(ct.c_int), ct.POINTER(I64), ct.POINTER(I64)]
     L.gb300_device_info.restype = ct.c_int
     L.gb300_launch_count.restype = I64
+    L.gb300_pool_bytes.restype = I64
     L.gb300_measure_fp64_peak.argtypes = [ct.POINTER(ct.c_double)]
     L.gb300_measure_fp64_peak.restype = ct.c_int
     L.gb300_synchronize.restype = ct.c_int
@@ -554,6 +555,11 @@ def measure_fp64_peak() -> float:
 
 def launch_count() -> int:
     return int(lib().gb300_launch_count())
+
+
+def pool_bytes() -> int:
+    """Device bytes held by the library's own grow-only buffers."""
+    return int(lib().gb300_pool_bytes())
 
 
 def select_device(ordinal: int) -> None:

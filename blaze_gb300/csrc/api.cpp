@@ -371,6 +371,8 @@ int gb300_device_info(int* num_sms, int64_t* free_bytes, int64_t* total_bytes) {
 
 int64_t gb300_launch_count(void) { return gb::runtime().launches.load(); }
 
+int64_t gb300_pool_bytes(void) { return gb::g_pool_bytes.load(); }
+
 int gb300_select_device(int ordinal) {
     gb::Runtime& r = gb::runtime();
     std::lock_guard<std::mutex> lock(r.mu);

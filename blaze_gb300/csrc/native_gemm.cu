@@ -356,62 +356,53 @@ template cudaError_t native_gemm<float>(const Gemm&, int, float*, const LaunchCt
 //
 //   * The array is a file-scope static __device__ variable of kNoAllocScratchBytes (16 MiB).
 //     Every GPU on which the library's device code is loaded holds it until the process exits.
-//   * Its device address is looked up once per device with cudaGetSymbolAddress, on the first
-//     call made while that device is current; that first call should therefore come before any
-//     stream capture.  Host code must never pass the symbol itself to a kernel: on the host it is
-//     only a stand-in, not a device address.
+//   * Its device address is looked up with cudaGetSymbolAddress on every call, with the call's
+//     device current (a lookup, no allocation), so an address never outlives a context that a
+//     cudaDeviceReset tore down.  The first call on a device also loads this file's device code
+//     there; that first call should therefore come before any stream capture.  Host code must
+//     never pass the symbol itself to a kernel: on the host it is only a stand-in, not a device
+//     address.
 //   * The first 256 bytes hold the kernel status word (cleared before every launch); the rest
 //     holds split-k partial tiles, which the kernel writes in full before reading them.
 //   * All calls share the array, so two calls whose kernels overlapped on the GPU would race on
 //     it.  The entry point therefore serializes its callers with a process-wide lock and returns
-//     only after its kernels have finished on `stream`.
-//   * Products whose split-k partials do not fit are rejected with GB300_ERR_INVALID_ARG; nothing
-//     is allocated, including by the CUDA runtime calls made here.
+//     only after its kernels have finished on `stream`, on the error paths too.
+//   * Products whose split-k partials do not fit are rejected with GB300_ERR_INVALID_ARG before
+//     anything is queued (C is left as it was); nothing is allocated, including by the CUDA
+//     runtime calls made here.
+//   * A, B, C and the stream must belong to the current device (managed memory is accepted).
 namespace gb {
 namespace {
 
 constexpr size_t kNoAllocScratchBytes = size_t(16) << 20;
 constexpr size_t kNoAllocStatusBytes = 256;
-constexpr int kNoAllocMaxDevices = 64;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
 std::mutex g_noalloc_mu;
-void* g_noalloc_addr[kNoAllocMaxDevices] = {};
 
-// Device address of g_noalloc_scratch on the current device (set up on first use per device).
+// Device address of g_noalloc_scratch on the current device.
 int noalloc_scratch(void** out, std::string* err) {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) {
-        *err = std::string("cudaGetDevice: ") + cudaGetErrorString(e);
-        return GB300_ERR_NO_DEVICE;
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || p == nullptr) {
+        cudaGetLastError();
+        *err = std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e);
+        return GB300_ERR_CUDA;
     }
-    if (dev < 0 || dev >= kNoAllocMaxDevices) {
-        *err = "device ordinal " + std::to_string(dev) + " is beyond the supported " + std::to_string(kNoAllocMaxDevices);
-        return GB300_ERR_NO_DEVICE;
-    }
-    if (!g_noalloc_addr[dev]) {
-        void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess || p == nullptr) {
-            cudaGetLastError();
-            *err = std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e);
-            return GB300_ERR_CUDA;
-        }
-        g_noalloc_addr[dev] = p;
-    }
-    *out = g_noalloc_addr[dev];
+    *out = p;
     return GB300_OK;
 }
 
-bool device_resident(const void* p) {
+// Whether p is device memory of device `dev`, or managed memory.
+bool resident_on(const void* p, int dev) {
     cudaPointerAttributes a;
     if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
         cudaGetLastError();
         return false;
     }
-    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+    if (a.type == cudaMemoryTypeManaged) return true;
+    return a.type == cudaMemoryTypeDevice && a.device == dev;
 }
 
 }  // namespace
@@ -440,9 +431,27 @@ extern "C" int gb300_dgemm_native_noalloc(int order, int transA, int transB, int
     if (m == 0 || n == 0) return GB300_OK;
     if ((alpha == 0.0 || k == 0) && beta == 1.0) return GB300_OK;
     const bool product = alpha != 0.0 && k > 0;
-    if (product && (!device_resident(A) || !device_resident(B)))
-        return fail(GB300_ERR_INVALID_ARG, "A and B must be device (or managed) memory");
-    if (!device_resident(C)) return fail(GB300_ERR_INVALID_ARG, "C must be device (or managed) memory");
+
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(GB300_ERR_NO_DEVICE, "no current device");
+    }
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (s != nullptr) {
+        int sdev = -1;
+        if (cudaStreamGetDevice(s, &sdev) != cudaSuccess) {
+            cudaGetLastError();
+            return fail(GB300_ERR_INVALID_ARG, "parameter 15 (stream) is not a valid stream");
+        }
+        if (sdev != dev)
+            return fail(GB300_ERR_INVALID_ARG, "the stream belongs to device " + std::to_string(sdev) +
+                                                   ", not the current device " + std::to_string(dev));
+    }
+    if (product && (!resident_on(A, dev) || !resident_on(B, dev)))
+        return fail(GB300_ERR_INVALID_ARG, "A and B must be device memory of the current device (or managed memory)");
+    if (!resident_on(C, dev))
+        return fail(GB300_ERR_INVALID_ARG, "C must be device memory of the current device (or managed memory)");
 
     Gemm g;
     if (rm) {
@@ -466,13 +475,11 @@ extern "C" int gb300_dgemm_native_noalloc(int order, int transA, int transB, int
 
     std::lock_guard<std::mutex> lock(g_noalloc_mu);
     std::string err;
-    void* scratch = nullptr;
-    int st = noalloc_scratch(&scratch, &err);
-    if (st != GB300_OK) return fail(st, err);
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) {
+        cudaGetLastError();
         return fail(GB300_ERR_NO_DEVICE, "cannot query the SM count");
+    }
     int splits = g.k > 0 ? native_choose_splits(g.m, g.n, g.k, 8, sms) : 1;
     const size_t need = splits > 1 ? size_t(splits) * size_t(g.m) * size_t(g.n) * sizeof(double) : 0;
     if (need > kNoAllocScratchBytes - kNoAllocStatusBytes)
@@ -480,19 +487,40 @@ extern "C" int gb300_dgemm_native_noalloc(int order, int transA, int transB, int
                     "the product needs " + std::to_string(need) + " bytes of split-k scratch; the allocation-free "
                     "entry point holds " + std::to_string(kNoAllocScratchBytes - kNoAllocStatusBytes) +
                     " (use gb300_dgemm_ex)");
+    void* scratch = nullptr;
+    int st = noalloc_scratch(&scratch, &err);
+    if (st != GB300_OK) return fail(st, err);
     auto* status = static_cast<int*>(scratch);
     auto* ws = reinterpret_cast<double*>(static_cast<unsigned char*>(scratch) + kNoAllocStatusBytes);
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
-    cudaError_t e = cudaMemsetAsync(status, 0, sizeof(int), s);
-    if (e != cudaSuccess) return fail(GB300_ERR_CUDA, std::string("status reset: ") + cudaGetErrorString(e));
+
+    // the failure-detection test hook of the other entry points (gb300_debug_inject_stall)
     LaunchCtl ctl;
     ctl.status = status;
+    {
+        Runtime& r = runtime();
+        std::lock_guard<std::mutex> hook(r.mu);
+        if (r.inject_stall_count > 0) {
+            --r.inject_stall_count;
+            ctl.inject_stall = 1;
+            ctl.wait_limit_ns = r.inject_limit_ns;
+        }
+    }
+    // from here on work may be queued: every return waits for the stream first, so that no kernel
+    // of this call still touches the shared array once the lock is released
+    auto fail_after_queue = [&](int st_, const std::string& msg) {
+        cudaStreamSynchronize(s);
+        cudaGetLastError();
+        return fail(st_, msg);
+    };
+    cudaError_t e = cudaMemsetAsync(status, 0, sizeof(int), s);
+    if (e != cudaSuccess) return fail_after_queue(GB300_ERR_CUDA, std::string("status reset: ") + cudaGetErrorString(e));
     e = native_gemm<double>(g, splits, splits > 1 ? ws : nullptr, ctl, s, &err);
-    if (e != cudaSuccess) return fail(GB300_ERR_CUDA, err.empty() ? cudaGetErrorString(e) : err);
+    if (e != cudaSuccess) return fail_after_queue(GB300_ERR_CUDA, err.empty() ? cudaGetErrorString(e) : err);
     int h = 0;
     e = cudaMemcpyAsync(&h, status, sizeof(int), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess) return fail(GB300_ERR_CUDA, std::string("kernel failed: ") + cudaGetErrorString(e));
+    if (e != cudaSuccess)
+        return fail_after_queue(GB300_ERR_CUDA, std::string("kernel failed: ") + cudaGetErrorString(e));
     if (h != 0) return fail(GB300_ERR_DEVICE_TIMEOUT, "a device-side wait ran out (code " + std::to_string(h) + ")");
     return GB300_OK;
 }

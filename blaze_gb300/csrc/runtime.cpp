@@ -149,12 +149,15 @@ int ensure_init(std::string* err) {
     return GB300_OK;
 }
 
+std::atomic<int64_t> g_pool_bytes{0};
+
 void* Workspace::get(int s, size_t n, std::string* err) {
     if (n == 0) n = 256;
     if (bytes[s] >= n) return ptr[s];
     if (ptr[s]) {
         cudaStreamSynchronize(stream);
         cudaFree(ptr[s]);
+        g_pool_bytes.fetch_sub(int64_t(bytes[s]));
         ptr[s] = nullptr;
         bytes[s] = 0;
     }
@@ -169,6 +172,7 @@ void* Workspace::get(int s, size_t n, std::string* err) {
     }
     ptr[s] = p;
     bytes[s] = rounded;
+    g_pool_bytes.fetch_add(int64_t(rounded));
     return p;
 }
 
@@ -181,7 +185,10 @@ size_t Workspace::total() const {
 void Workspace::release() {
     if (stream) cudaStreamSynchronize(stream);
     for (int s = 0; s < kSlotCount; ++s) {
-        if (ptr[s]) cudaFree(ptr[s]);
+        if (ptr[s]) {
+            cudaFree(ptr[s]);
+            g_pool_bytes.fetch_sub(int64_t(bytes[s]));
+        }
         ptr[s] = nullptr;
         bytes[s] = 0;
     }

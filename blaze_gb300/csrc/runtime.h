@@ -65,6 +65,10 @@ struct Runtime {
 
 Runtime& runtime();
 
+// Bytes held by every Workspace of the process (the default context, the neighbouring routines'
+// buffers and the server slots), as allocated by Workspace::get and returned by release().
+extern std::atomic<int64_t> g_pool_bytes;
+
 // Initialise the device state once (thread-safe).  Returns a gb300_status.
 int ensure_init(std::string* err);
 

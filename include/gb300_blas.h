@@ -111,6 +111,11 @@ int gb300_profile_read(const char* prefix, double* total_ms, int64_t* launches);
 /* Count of kernel launches the library has issued in this process (all entry points). */
 int64_t gb300_launch_count(void);
 
+/* Device bytes held by the library's own grow-only buffers in this process (the default context,
+ * the buffers of the routines next to ?gemm and every server slot).  Memory accounting for hosts
+ * that budget device memory; plans of the grouped API are not included. */
+int64_t gb300_pool_bytes(void);
+
 /* Wait until all work the library queued on its own stream has finished. */
 int gb300_synchronize(void);
 
@@ -222,12 +227,16 @@ void gb300_server_destroy(gb300_server* server);
  * memory themselves (a host framework that owns all device memory through its own pool or
  * budget, or a latency-critical loop where cudaMalloc/cudaFree and their implicit device
  * synchronization are not allowed).  It has no counterpart in the reference.
- * Operands and C must be device (or managed) memory with 16-byte aligned bases and even leading
- * dimensions.  The split-k scratch comes from a fixed 16 MiB array compiled into the library (held
- * on every GPU that loads the library until exit); products that need more are rejected with
- * GB300_ERR_INVALID_ARG.  The first call on a device looks up that array's device address, so
- * make it before any stream capture.  Calls share the array: the function serializes its callers
- * and returns after its kernels finished on `stream` (NULL: the legacy default stream). */
+ * Operands and C must be device memory of the current device (or managed memory) with 16-byte
+ * aligned bases and even leading dimensions; a non-NULL `stream` must belong to the current
+ * device.  The split-k scratch comes from a fixed 16 MiB array compiled into the library (held on
+ * every GPU that loads the library until exit); products that need more are rejected with
+ * GB300_ERR_INVALID_ARG before anything is queued, C unchanged.  The array's device address is
+ * looked up on every call; the first call on a device also loads the library's device code there,
+ * so make that first call before any stream capture.  Calls share the array: the function
+ * serializes its callers and returns after its kernels finished on `stream` (NULL: the legacy
+ * default stream), on error paths too.  gb300_debug_inject_stall applies to it like to the other
+ * native launches. */
 int gb300_dgemm_native_noalloc(int order, int transA, int transB, int64_t m, int64_t n, int64_t k,
                                double alpha, const double* A, int64_t lda, const double* B,
                                int64_t ldb, double beta, double* C, int64_t ldc, void* stream);

@@ -37,11 +37,24 @@ def build(quiet: bool = True) -> str:
     return LIB_PATH
 
 
-def build_ref(ref_root: str = "/root/reference") -> str | None:
+def reference_root() -> str | None:
+    """Directory holding the reference's headers (``blaze/``), or None when it is absent.
+
+    The location is the oracle recipe's (``make -C oracle print-ref``; the environment variable
+    BLAZE_REFERENCE_ROOT overrides it)."""
+    root = os.environ.get("BLAZE_REFERENCE_ROOT")
+    if not root:
+        out = subprocess.run(["make", "-s", "-C", HERE, "print-ref"], capture_output=True, text=True)
+        root = out.stdout.strip() if out.returncode == 0 else ""
+    return root if root and os.path.isdir(os.path.join(root, "blaze")) else None
+
+
+def build_ref(ref_root: str | None = None) -> str | None:
     """Compile oracle/_ref/libblazeref.so from the reference headers, if they are present."""
     if os.path.exists(REF_PATH):
         return REF_PATH
-    if not os.path.isdir(os.path.join(ref_root, "blaze")):
+    ref_root = ref_root or reference_root()
+    if ref_root is None:
         return None
     out = subprocess.run(["make", "-C", HERE, "ref", f"REF={ref_root}"], capture_output=True, text=True)
     if out.returncode != 0:

@@ -15,14 +15,25 @@ import subprocess
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 OUT = os.path.join(HERE, "_build")
-REF = os.environ.get("BLAZE_INCLUDE", "/root/reference")
+
+def _reference_root() -> str:
+    import sys
+
+    if ROOT not in sys.path:
+        sys.path.insert(0, ROOT)
+    import oracle
+
+    return oracle.reference_root() or ""
+
+
+REF = _reference_root()
 
 FLAGS = ["-std=c++17", "-O1", "-DBLAZE_BLAS_MODE=1", "-DBLAZE_BLAS_IS_PARALLEL=1",
          "-DBLAZE_BLAS_INCLUDE_FILE=<gb300_cblas.h>", "-DGB300_BLAS_THROW", "-I" + os.path.join(ROOT, "include")]
 
 
 def available() -> bool:
-    return os.path.isdir(os.path.join(REF, "blaze")) and shutil.which("g++") is not None
+    return bool(REF) and os.path.isdir(os.path.join(REF, "blaze")) and shutil.which("g++") is not None
 
 
 # matrix x vector products take Blaze's BLAS kernels (off by default, blaze/config/BLAS.h) from
