@@ -33,11 +33,20 @@ static void mt_seed(mt_state* s, uint32_t seed) {
 
 static uint32_t mt_next(mt_state* s) {
     if (s->idx >= 624) {
-        for (int i = 0; i < 624; ++i) {
-            const uint32_t y = (s->mt[i] & 0x80000000u) | (s->mt[(i + 1) % 624] & 0x7fffffffu);
-            uint32_t v = s->mt[(i + 397) % 624] ^ (y >> 1);
-            if (y & 1u) v ^= 0x9908b0dfu;
-            s->mt[i] = v;
+        /* the recurrence in three index ranges, so that no index needs a modulo */
+        uint32_t* mt = s->mt;
+        int i = 0;
+        for (; i < 624 - 397; ++i) {
+            const uint32_t y = (mt[i] & 0x80000000u) | (mt[i + 1] & 0x7fffffffu);
+            mt[i] = mt[i + 397] ^ (y >> 1) ^ ((y & 1u) ? 0x9908b0dfu : 0u);
+        }
+        for (; i < 623; ++i) {
+            const uint32_t y = (mt[i] & 0x80000000u) | (mt[i + 1] & 0x7fffffffu);
+            mt[i] = mt[i + 397 - 624] ^ (y >> 1) ^ ((y & 1u) ? 0x9908b0dfu : 0u);
+        }
+        {
+            const uint32_t y = (mt[623] & 0x80000000u) | (mt[0] & 0x7fffffffu);
+            mt[623] = mt[396] ^ (y >> 1) ^ ((y & 1u) ? 0x9908b0dfu : 0u);
         }
         s->idx = 0;
     }
