@@ -1,9 +1,13 @@
 """Compile the Blaze drop-in test program (needs the reference headers; test infrastructure).
 
-    build(kind, program)   kind = "stub": linked against stub_cblas.cpp (CPU stand-in that logs calls)
+    build(kind, program, intercept)
+                           kind = "stub": linked against stub_cblas.cpp (CPU stand-in that logs calls)
                            kind = "lib":  linked against blaze_gb300/libgb300blas.so
-                           program = "main" (dropin_main.cpp: ?gemm) or "next" (dropin_next.cpp:
-                           gemv / trmv / complex gemm / trmm through Blaze's expressions)
+                           program = "main" (dropin_main.cpp: ?gemm), "next" (dropin_next.cpp:
+                           gemv / trmv / complex gemm / trmm through Blaze's expressions) or
+                           "gated" (dropin_gated.cpp: the products Blaze's kernel selection keeps
+                           on the CPU)
+                           intercept = True: compiled with include/gb300_blaze.h
 Returns the executable path, or None when the Blaze headers are not available here.
 """
 from __future__ import annotations
@@ -43,13 +47,15 @@ NEXT_FLAGS = ["-DBLAZE_USE_BLAS_MATRIX_VECTOR_MULTIPLICATION=1", "-DBLAZE_DMATDV
               "-DBLAZE_TDVECTDMATMULT_THRESHOLD=1000UL", "-DBLAZE_DMATDMATMULT_THRESHOLD=1UL"]
 
 
-def build(kind: str, program: str = "main") -> str | None:
+def build(kind: str, program: str = "main", intercept: bool = False) -> str | None:
     if not available():
         return None
     os.makedirs(OUT, exist_ok=True)
     exe = os.path.join(OUT, f"dropin_{kind}" if program == "main" else f"dropin_{program}_{kind}")
+    if intercept:
+        exe += "_intercept"
     srcs = [os.path.join(HERE, f"dropin_{program}.cpp")]
-    deps = list(srcs) + [os.path.join(ROOT, "include", "gb300_cblas.h")]
+    deps = list(srcs) + [os.path.join(ROOT, "include", "gb300_cblas.h"), os.path.join(ROOT, "include", "gb300_blaze.h")]
     extra = []
     if kind == "stub":
         srcs.append(os.path.join(HERE, "stub_cblas.cpp"))
@@ -59,7 +65,7 @@ def build(kind: str, program: str = "main") -> str | None:
         extra = ["-L" + lib_dir, "-lgb300blas", "-Wl,-rpath," + lib_dir]
     if os.path.exists(exe) and all(os.path.getmtime(exe) >= os.path.getmtime(d) for d in deps):
         return exe
-    flags = FLAGS + (NEXT_FLAGS if program == "next" else [])
+    flags = FLAGS + (NEXT_FLAGS if program == "next" else []) + (["-DGB300_INTERCEPT"] if intercept else [])
     cmd = ["g++", *flags, "-isystem", REF, *srcs, "-o", exe, *extra]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:

@@ -6,7 +6,10 @@ tests/blaze_dropin/ against their logging stub:
   alpha lda ldb beta ldc;
 - tests/golden/blaze_next_calls.txt: matrix x vector (dense and triangular), complex products and
   triangular products (dropin_next.cpp); one call per line: the routine name, then its CBLAS
-  arguments in order without the pointers (complex scalars as re,im).
+  arguments in order without the pointers (complex scalars as re,im);
+- tests/golden/blaze_gated_calls.txt: the products Blaze's kernel selection keeps on the CPU
+  (dropin_gated.cpp), built with include/gb300_blaze.h, which sends them to ?gemm; the format of
+  blaze_calls.txt.
 
 The GPU tests replay both through the real library.  Needs the reference headers.
 """
@@ -19,8 +22,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(os.path.dirname(HERE), "blaze_dropin"))
 import build as dropin  # noqa: E402
 
-for program, out in (("main", "blaze_calls.txt"), ("next", "blaze_next_calls.txt")):
-    exe = dropin.build("stub", program)
+for program, out, intercept in (("main", "blaze_calls.txt", False), ("next", "blaze_next_calls.txt", False),
+                                ("gated", "blaze_gated_calls.txt", True)):
+    exe = dropin.build("stub", program, intercept)
     if exe is None:
         raise SystemExit("reference headers not available")
     with tempfile.TemporaryDirectory() as d:

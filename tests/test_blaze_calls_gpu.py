@@ -46,6 +46,44 @@ def test_replay_blaze_calls(method):
         G.lib().gb300_set_default_method(prev)
 
 
+# ---- products Blaze's kernel selection keeps on the CPU, sent to ?gemm by include/gb300_blaze.h
+# (tests/golden/blaze_gated_calls.txt, recorded from Blaze with the header)
+GATED_CALLS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "blaze_gated_calls.txt")
+
+
+@pytest.mark.parametrize("method", [G.METHOD_AUTO, G.METHOD_NATIVE, G.METHOD_SPLIT])
+def test_replay_intercepted_blaze_calls(method):
+    lines = open(GATED_CALLS).read().splitlines()
+    assert len(lines) == 14
+    prev = G.lib().gb300_set_default_method(method)
+    try:
+        for i, ln in enumerate(lines):
+            f = ln.split()
+            c = dict(order=int(f[1]), ta=int(f[2]), tb=int(f[3]), m=int(f[4]), n=int(f[5]), k=int(f[6]),
+                     alpha=float(f[7]), lda=int(f[8]), ldb=int(f[9]), beta=float(f[10]), ldc=int(f[11]))
+            dt = np.float32 if f[0] == "sgemm" else np.float64
+            ra, _ = stored_dims(c["order"], c["ta"], c["m"], c["k"])
+            rb, _ = stored_dims(c["order"], c["tb"], c["k"], c["n"])
+            rc, _ = stored_dims(c["order"], O.NO_TRANS, c["m"], c["n"])
+            A = O.uniform(ra * c["lda"], 700 + i, dtype=dt)
+            B = O.uniform(rb * c["ldb"], 800 + i, dtype=dt)
+            C = O.uniform(rc * c["ldc"], 900 + i, dtype=dt)
+            R = C.copy()
+            O.gemm(c["order"], c["ta"], c["tb"], c["m"], c["n"], c["k"], c["alpha"], A, c["lda"], B, c["ldb"],
+                   c["beta"], R, c["ldc"], kernel="default")
+            call = G.cblas_sgemm if dt == np.float32 else G.cblas_dgemm
+            call(c["order"], c["ta"], c["tb"], c["m"], c["n"], c["k"], c["alpha"], A, c["lda"], B, c["ldb"],
+                 c["beta"], C, c["ldc"])
+            if dt == np.float64:
+                assert blaze_equal(R, C, 1e-8).all(), c
+            else:
+                scale = max(1.0, float(np.max(np.abs(R))))
+                assert float(np.max(np.abs(C.astype(np.float64) - R.astype(np.float64)))) <= \
+                    c["k"] * 2.0 ** -22 * scale + 1e-6, c
+    finally:
+        G.lib().gb300_set_default_method(prev)
+
+
 # ---- the routines next to ?gemm, as Blaze's expressions call them (tests/golden/blaze_next_calls.txt)
 NEXT_CALLS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "blaze_next_calls.txt")
 

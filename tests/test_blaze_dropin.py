@@ -145,3 +145,74 @@ def test_real_library_without_gpu_raises_for_the_neighbouring_routines_too():
             assert f[1] == "status=ok", f
         else:
             assert f[1] == "status=exception" and "no CUDA device" in " ".join(f), f
+
+
+# ---- products Blaze's kernel selection keeps on the CPU, and include/gb300_blaze.h (dropin_gated.cpp)
+def _gated_run(intercept, tmp_path):
+    exe = dropin.build("stub", "gated", intercept)
+    log = tmp_path / ("log_i.txt" if intercept else "log_p.txt")
+    out = run(exe, {"GB300_STUB_LOG": str(log)})
+    calls = [ln.split() for ln in log.read_text().splitlines()] if log.exists() else []
+    return out, calls
+
+
+def test_gated_products_stay_on_the_cpu_without_the_interception_header(tmp_path):
+    out, calls = _gated_run(False, tmp_path)
+    for f in out:
+        assert f[1] == "status=ok", f
+    ungated = [f for f in out if f[3] == "gated=0"]
+    assert len(ungated) == 1 and len(out) == 14
+    # only the product Blaze's selection already sends to BLAS makes a call
+    assert len(calls) == 1 and calls[0][0] == "dgemm"
+    assert calls[0][4:7] == [f.split("=")[1] for f in ungated[0][4:7]]
+
+
+def test_interception_header_sends_every_gated_product_to_gemm(tmp_path):
+    out, calls = _gated_run(True, tmp_path)
+    assert len(calls) == len(out) == 14
+    for f, c in zip(out, calls):
+        assert f[1] == "status=ok", f
+        tol = 1e-4 if f[0].startswith("small_float") else 1e-12
+        assert float(f[2].split("=")[1]) <= tol, f
+        assert c[0] == ("sgemm" if f[0].startswith("small_float") else "dgemm"), (f, c)
+        assert c[4:7] == [x.split("=")[1] for x in f[4:7]], (f, c)  # m, n, k as Blaze's gemm() maps them
+    by = {f[0]: c for f, c in zip(out, calls)}
+    # the assignment forms keep Blaze's alpha / beta (the same as its own BLAS kernels)
+    assert (by["small_rr"][7], by["small_rr"][10]) == ("1", "0")
+    assert (by["small_rr/add"][7], by["small_rr/add"][10]) == ("1", "1")
+    assert (by["small_rr/sub"][7], by["small_rr/sub"][10]) == ("-1", "1")
+    assert (by["small_rr/scaled"][7], by["small_rr/scaled"][10]) == ("2.5", "0")
+    # storage orders map like blaze::gemm: order from C, a transposition where an operand's differs
+    assert by["skinny_cr"][1:4] == ["101", "112", "111"]
+    assert by["skinny_cc"][1:4] == ["102", "111", "111"]
+    assert by["small_rc"][1:4] == ["101", "111", "112"]
+    # the intercepted call is the one Blaze itself makes for an ungated product
+    plain_out, plain_calls = _gated_run(False, tmp_path)
+    assert by["large_rr"] == plain_calls[0]
+
+
+def test_gated_call_fixture_matches_blaze():
+    exe = dropin.build("stub", "gated", True)
+    import tempfile
+    with tempfile.TemporaryDirectory() as d:
+        log = os.path.join(d, "log.txt")
+        run(exe, {"GB300_STUB_LOG": log})
+        fresh = open(log).read().splitlines()
+    committed = open(os.path.join(HERE, "golden", "blaze_gated_calls.txt")).read().splitlines()
+    assert fresh == committed
+
+
+def test_intercepted_products_raise_from_the_real_library_without_a_gpu():
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    import blaze_gb300 as G
+    if not os.path.exists(G.LIB_PATH):
+        G.build()
+    exe = dropin.build("lib", "gated", True)
+    out = run(exe, {})
+    assert len(out) == 14
+    # every intercepted product reaches the library (which has no device here), none is computed on
+    # the CPU behind the caller's back
+    for f in out:
+        assert f[1] == "status=exception" and "no CUDA device" in " ".join(f), f
