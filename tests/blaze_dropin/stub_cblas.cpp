@@ -17,14 +17,22 @@ namespace {
 thread_local int t_status = 0;
 thread_local char t_msg[256] = "";
 
+// With GB300_STUB_LOG_PTRS set, a ?gemm line also carries the addresses of A, B and C (hex), from
+// which a test recovers where each call's operands lie inside the caller's matrices.
 void log_call(const char* name, int order, int ta, int tb, long m, long n, long k, double alpha, long lda, long ldb,
-              double beta, long ldc) {
+              double beta, long ldc, const void* A = nullptr, const void* B = nullptr, const void* C = nullptr) {
     const char* path = std::getenv("GB300_STUB_LOG");
     if (!path) return;
+    char line[512];
+    int len = std::snprintf(line, sizeof line, "%s %d %d %d %ld %ld %ld %.17g %ld %ld %.17g %ld", name, order, ta, tb,
+                            m, n, k, alpha, lda, ldb, beta, ldc);
+    if (std::getenv("GB300_STUB_LOG_PTRS"))
+        len += std::snprintf(line + len, sizeof line - size_t(len), " %p %p %p", A, B, C);
+    line[len++] = '\n';
+    // one write per line: concurrent callers (Blaze's OpenMP tiles) append whole lines
     FILE* f = std::fopen(path, "a");
     if (!f) return;
-    std::fprintf(f, "%s %d %d %d %ld %ld %ld %.17g %ld %ld %.17g %ld\n", name, order, ta, tb, m, n, k, alpha, lda, ldb,
-                 beta, ldc);
+    std::fwrite(line, 1, size_t(len), f);
     std::fclose(f);
 }
 
@@ -212,7 +220,7 @@ void gb300_clear_error(void) { t_status = 0; t_msg[0] = 0; }
 void gb300_cblas_dgemm_checked(CBLAS_ORDER order, CBLAS_TRANSPOSE transA, CBLAS_TRANSPOSE transB, gb300_blas_int m,
                                gb300_blas_int n, gb300_blas_int k, double alpha, const double* A, gb300_blas_int lda,
                                const double* B, gb300_blas_int ldb, double beta, double* C, gb300_blas_int ldc) {
-    log_call("dgemm", order, transA, transB, m, n, k, alpha, lda, ldb, beta, ldc);
+    log_call("dgemm", order, transA, transB, m, n, k, alpha, lda, ldb, beta, ldc, A, B, C);
     if (std::getenv("GB300_STUB_FAIL")) {
         t_status = 2;
         std::strcpy(t_msg, "injected failure");
@@ -224,7 +232,7 @@ void gb300_cblas_dgemm_checked(CBLAS_ORDER order, CBLAS_TRANSPOSE transA, CBLAS_
 void gb300_cblas_sgemm_checked(CBLAS_ORDER order, CBLAS_TRANSPOSE transA, CBLAS_TRANSPOSE transB, gb300_blas_int m,
                                gb300_blas_int n, gb300_blas_int k, float alpha, const float* A, gb300_blas_int lda,
                                const float* B, gb300_blas_int ldb, float beta, float* C, gb300_blas_int ldc) {
-    log_call("sgemm", order, transA, transB, m, n, k, alpha, lda, ldb, beta, ldc);
+    log_call("sgemm", order, transA, transB, m, n, k, alpha, lda, ldb, beta, ldc, A, B, C);
     gemm<float>(order, transA, transB, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
 }
 

@@ -84,6 +84,95 @@ def test_replay_intercepted_blaze_calls(method):
         G.lib().gb300_set_default_method(prev)
 
 
+# ---- the reference's own operation test (blazetest dmatdmatmult/MDaMDa.cpp in BLAS and debug mode) ---
+BLAZETEST_CALLS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "blazetest_mdamda_calls.txt")
+
+
+@pytest.mark.parametrize("method", [G.METHOD_AUTO, G.METHOD_NATIVE, G.METHOD_SPLIT])
+def test_replay_blazetest_operation_test_calls(method):
+    lines = open(BLAZETEST_CALLS).read().splitlines()
+    assert len(lines) == 288
+    prev = G.lib().gb300_set_default_method(method)
+    try:
+        for i, ln in enumerate(lines):
+            f = ln.split()
+            c = dict(order=int(f[1]), ta=int(f[2]), tb=int(f[3]), m=int(f[4]), n=int(f[5]), k=int(f[6]),
+                     alpha=float(f[7]), lda=int(f[8]), ldb=int(f[9]), beta=float(f[10]), ldc=int(f[11]))
+            ra, _ = stored_dims(c["order"], c["ta"], c["m"], c["k"])
+            rb, _ = stored_dims(c["order"], c["tb"], c["k"], c["n"])
+            rc, _ = stored_dims(c["order"], O.NO_TRANS, c["m"], c["n"])
+            A = O.uniform(max(ra * c["lda"], 1), 1100 + i)
+            B = O.uniform(max(rb * c["ldb"], 1), 1200 + i)
+            C = O.uniform(max(rc * c["ldc"], 1), 1300 + i)
+            R = C.copy()
+            O.gemm(c["order"], c["ta"], c["tb"], c["m"], c["n"], c["k"], c["alpha"], A, c["lda"], B, c["ldb"],
+                   c["beta"], R, c["ldc"], kernel="default")
+            G.cblas_dgemm(c["order"], c["ta"], c["tb"], c["m"], c["n"], c["k"], c["alpha"], A, c["lda"], B,
+                          c["ldb"], c["beta"], C, c["ldc"])
+            assert blaze_equal(R, C, 1e-8).all(), c
+    finally:
+        G.lib().gb300_set_default_method(prev)
+
+
+# ---- Blaze's OpenMP evaluation (BLAZE_BLAS_IS_PARALLEL=0): concurrent tile calls inside the operands
+SMP_CALLS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "blaze_smp_calls.txt")
+
+
+def test_replay_openmp_tile_calls_concurrently():
+    """Each product's tile calls, as Blaze's OpenMP layer made them (offset pointers inside the
+    whole matrices, their leading dimensions), issued at once from as many host threads; the
+    assembled C against the same calls through the oracle's restatement of Blaze's kernel."""
+    import threading
+
+    products, cur = [], None
+    for ln in open(SMP_CALLS).read().splitlines():
+        f = ln.split()
+        if f[0] == "product":
+            cur = []
+            products.append(cur)
+            continue
+        cur.append(dict(order=int(f[1]), ta=int(f[2]), tb=int(f[3]), m=int(f[4]), n=int(f[5]), k=int(f[6]),
+                        alpha=float(f[7]), lda=int(f[8]), ldb=int(f[9]), beta=float(f[10]), ldc=int(f[11]),
+                        offA=int(f[12]), offB=int(f[13]), offC=int(f[14])))
+    assert len(products) == 5 and all(len(p) == 4 for p in products)
+    for q, tiles in enumerate(products):
+        def extent(c, which):
+            if which == "A":
+                r, _ = stored_dims(c["order"], c["ta"], c["m"], c["k"])
+                return c["offA"] + r * c["lda"]
+            if which == "B":
+                r, _ = stored_dims(c["order"], c["tb"], c["k"], c["n"])
+                return c["offB"] + r * c["ldb"]
+            r, _ = stored_dims(c["order"], O.NO_TRANS, c["m"], c["n"])
+            return c["offC"] + r * c["ldc"]
+        A = O.uniform(max(extent(c, "A") for c in tiles), 1400 + q)
+        B = O.uniform(max(extent(c, "B") for c in tiles), 1500 + q)
+        C = O.uniform(max(extent(c, "C") for c in tiles), 1600 + q)
+        R = C.copy()
+        for c in tiles:
+            O.gemm(c["order"], c["ta"], c["tb"], c["m"], c["n"], c["k"], c["alpha"], A[c["offA"]:], c["lda"],
+                   B[c["offB"]:], c["ldb"], c["beta"], R[c["offC"]:], c["ldc"], kernel="default")
+        errors = []
+        start = threading.Barrier(len(tiles))
+
+        def tile_call(c):
+            try:
+                start.wait()
+                G.cblas_dgemm(c["order"], c["ta"], c["tb"], c["m"], c["n"], c["k"], c["alpha"],
+                              A.ctypes.data + 8 * c["offA"], c["lda"], B.ctypes.data + 8 * c["offB"], c["ldb"],
+                              c["beta"], C.ctypes.data + 8 * c["offC"], c["ldc"])
+            except Exception as e:  # noqa: BLE001
+                errors.append(e)
+
+        threads = [threading.Thread(target=tile_call, args=(c,)) for c in tiles]
+        for t in threads:
+            t.start()
+        for t in threads:
+            t.join()
+        assert not errors, errors
+        assert blaze_equal(R, C, 1e-8).all(), q
+
+
 # ---- the routines next to ?gemm, as Blaze's expressions call them (tests/golden/blaze_next_calls.txt)
 NEXT_CALLS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "blaze_next_calls.txt")
 

@@ -216,3 +216,41 @@ def test_intercepted_products_raise_from_the_real_library_without_a_gpu():
     # the CPU behind the caller's back
     for f in out:
         assert f[1] == "status=exception" and "no CUDA device" in " ".join(f), f
+
+
+# ---- Blaze's OpenMP tiles (dropin_smp.cpp) and the reference's own operation test ----------------
+def test_openmp_tiles_reach_cblas_dgemm_concurrently_inside_the_operands(tmp_path):
+    exe = dropin.build("stub", "smp")
+    log = tmp_path / "log.txt"
+    out = run(exe, {"GB300_STUB_LOG": str(log), "GB300_STUB_LOG_PTRS": "1", "OMP_NUM_THREADS": "4"})
+    assert len(out) == 5
+    for f in out:
+        assert f[1] == "status=ok" and float(f[2].split("=")[1]) <= 1e-12, f
+    lines = dropin.smp_fixture(log.read_text().splitlines())
+    committed = open(os.path.join(HERE, "golden", "blaze_smp_calls.txt")).read().splitlines()
+    assert lines == committed
+    # several tiles per product, each an offset view with the whole matrix's leading dimension
+    tiles = [ln.split() for ln in lines if not ln.startswith("product")]
+    assert len(tiles) == 20
+    assert any(int(t[12]) > 0 for t in tiles) and any(int(t[14]) > 0 for t in tiles)
+    assert all(int(t[11]) != int(t[5] if t[1] == "101" else t[4]) for t in tiles)  # ldc != tile width
+
+
+def test_blazetest_dmatdmatmult_operation_test_passes_through_the_seam(tmp_path):
+    """blazetest's MDaMDa (every storage-order combination and assignment form of DynamicMatrix
+    products) built in BLAS and debug mode against the stub: the test's own checks pass, and the
+    distinct ?gemm calls it makes are the committed fixture the GPU tests replay."""
+    exe = dropin.build_blazetest("double")
+    if exe is None:
+        pytest.skip("blazetest sources are not present")
+    log = tmp_path / "log.txt"
+    r = subprocess.run([exe], capture_output=True, text=True, env=dict(os.environ, GB300_STUB_LOG=str(log)),
+                       timeout=600)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
+    counts = {}
+    for ln in log.read_text().splitlines():
+        counts[ln] = counts.get(ln, 0) + 1
+    fresh = [f"{ln} {counts[ln]}" for ln in sorted(counts)]
+    committed = open(os.path.join(HERE, "golden", "blazetest_mdamda_calls.txt")).read().splitlines()
+    assert fresh == committed
+    assert sum(int(ln.split()[-1]) for ln in committed) == 3672
