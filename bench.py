@@ -233,32 +233,51 @@ def cpu_check_rows(hA, hB, n: int, rows, order=101, ta=111, tb=111, m=None, k=No
 
 
 
+def workload_name(args) -> str:
+    """The benchmark workload, named identically by both arms."""
+    n = args.size
+    return (f"dense FP64-accurate GEMM C=A*B, M=N=K={n}, row-major x row-major, uniform [-1,1] "
+            f"(mt19937 seed {args.seed})")
+
+
 def reference_arm(args, dist: Dist):
+    """The reference's CPU evaluation of the same workload: the oracle's restatement of Blaze's
+    blocked kernel (mmm, blaze/math/dense/MMM.h:105-600) on every host thread.  Each step computes one
+    row panel of the n^3 product (R rows of C from the whole A row panel and all of B), walking down C
+    from step to step, so that the run stays within seconds while timing the workload's own operands
+    and shape; the rate is the panel's 2*R*n*n flops over its time."""
     if dist.rank != 0:
         return
-    size = max(args.size // 2, 256)
     import numpy as np
     import oracle as O
     oracle_threads = O.lib().orc_max_threads()
-    n = size
+    n = args.size
+    R = min(n, 512)
     A = O.uniform(n * n, args.seed)
     B = O.uniform(n * n, args.seed + 1)
-    C = np.zeros(n * n)
-    for _ in range(args.warmup):
-        O.gemm(O.ROW_MAJOR, O.NO_TRANS, O.NO_TRANS, n, n, n, 1.0, A, n, B, n, 0.0, C, n, nthreads=oracle_threads)
+    C = np.zeros(R * n)
+    panels = max(n // R, 1)
+
+    def step(i):
+        r0 = (i % panels) * R
+        O.gemm(O.ROW_MAJOR, O.NO_TRANS, O.NO_TRANS, R, n, n, 1.0, A[r0 * n:], n, B, n, 0.0, C, n,
+               nthreads=oracle_threads)
+
+    for i in range(args.warmup):
+        step(i)
     t0 = time.perf_counter()
-    for _ in range(args.steps):
-        O.gemm(O.ROW_MAJOR, O.NO_TRANS, O.NO_TRANS, n, n, n, 1.0, A, n, B, n, 0.0, C, n, nthreads=oracle_threads)
+    for i in range(args.steps):
+        step(args.warmup + i)
     dt = time.perf_counter() - t0
-    value = 2.0 * n ** 3 * args.steps / dt / 1e12
-    sample = (f"each step one {n}^3 FP64 product (1/8 of the {args.size}^3 workload) through the oracle's "
-              f"restatement of Blaze's blocked mmm kernel on {oracle_threads} host threads (the reference is "
-              f"header-only C++; its own build needs its headers, which the GPU host does not have)")
+    value = 2.0 * R * n * n * args.steps / dt / 1e12
+    sample = (f"each step one {R}-row panel of C (of the {n}^3 product: {R} x {n} x {n} FP64, 1/{panels} of the "
+              f"workload) through the oracle's restatement of Blaze's blocked mmm kernel on {oracle_threads} host "
+              "threads (the reference is header-only C++ and its headers are not on the GPU host)")
     line = {"metric": METRIC, "value": round(value, 5), "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dt / args.steps * 1e3, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"dense FP64 GEMM C=A*B, M=N=K={args.size} (timed on {n}^3 samples), row-major, "
-                                   f"uniform [-1,1] (mt19937 seed {args.seed})", "method": "blaze-cpu"},
+            "config": {"workload": workload_name(args), "method": "blaze-cpu (blocked mmm kernel, FP64)",
+                       "parallelism": "replicas"},
             "cpu_baseline": {"value": round(value, 5), "unit": UNIT, "cores": oracle_threads, "kind": "port",
                              "sample": sample},
             "e2e": {"value": round(value, 5), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -380,8 +399,33 @@ def batched_leg(G, torch, args, dev):
                      "loop_ms_device": round(loop_ms, 3),
                      "loop_ms_wall": round(loop_wall * 1e3, 2), "speedup_vs_loop": round(loop_ms / ms, 2),
                      "useful_gflop": round(useful / 1e9, 4)}
+        if not args.no_cpu:
+            out[name]["cpu_small_kernel"] = batched_cpu_baseline(specs, dA, dB, dC, useful, ms)
         del dA, dB, dC
     return out
+
+
+def batched_cpu_baseline(specs, dA, dB, dC, useful, grouped_ms):
+    """The same product list through the oracle's restatement of Blaze's small kernel
+    (DMatDMatMultExpr.h:864-1878, the kernel Blaze's selection uses for every product of this
+    size), on one host thread and on every host thread (products spread over OpenMP threads)."""
+    import numpy as np
+
+    import oracle as O
+
+    hA, hB = dA.cpu().numpy(), dB.cpu().numpy()
+    desc, ab = O.batch_descriptor(specs)
+    res = {"kind": "port", "kernel": "oracle restatement of Blaze's small kernel (2 rows x 5 SIMD widths, "
+                                    "128-bit vectors)", "host_cores": os.cpu_count()}
+    for nt in (1, os.cpu_count() or 1):
+        C = np.zeros(dC.numel(), dtype=hA.dtype)
+        O.gemm_batch_small(desc, ab, hA, hB, C, nthreads=nt)  # warm (pages, threads)
+        t0 = time.perf_counter()
+        O.gemm_batch_small(desc, ab, hA, hB, C, nthreads=nt)
+        t = time.perf_counter() - t0
+        res[f"threads_{nt}"] = {"ms": round(t * 1e3, 2), "tflops": round(useful / t / 1e12, 5),
+                                "gpu_grouped_speedup": round(t * 1e3 / grouped_ms, 1)}
+    return res
 
 
 def next_leg(G, torch, args):
@@ -748,8 +792,7 @@ def ours(args, dist: Dist):
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step_max, 4),
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
                 "data": "synthetic",
-                "config": {"workload": f"dense FP64-accurate GEMM C=A*B, M=N=K={n}, row-major x row-major, "
-                                       f"uniform [-1,1] (mt19937 seed {args.seed})",
+                "config": {"workload": workload_name(args),
                            "method": ("split, residue (CRT) scheme: beta-bit integer scaling, one BF16 tcgen05 product "
                                       "per modulus with exact int32 sums, exact 128-bit reconstruction")
                                      if info.method_used == G.METHOD_SPLIT_CRT else

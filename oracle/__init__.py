@@ -85,6 +85,11 @@ def lib():
         L.orc_mt19937_raw.argtypes = [ct.c_uint32, ct.POINTER(ct.c_uint32), _I64]
         L.orc_gemm_default_d.argtypes = _gemm_argtypes(_D, ct.c_double)
         L.orc_gemm_default_s.argtypes = _gemm_argtypes(_F, ct.c_float)
+        L.orc_gemm_small_d.argtypes = _gemm_argtypes(_D, ct.c_double)
+        L.orc_gemm_small_s.argtypes = _gemm_argtypes(_F, ct.c_float)
+        _P64 = ct.POINTER(ct.c_int64)
+        L.orc_gemm_batch_small_d.argtypes = [_I64, _P64, _D, _D, _D, _D, ct.c_int]
+        L.orc_gemm_batch_small_s.argtypes = [_I64, _P64, _F, _F, _F, _F, ct.c_int]
         L.orc_gemm_blocked_d.argtypes = _gemm_argtypes(_D, ct.c_double) + [ct.c_int]
         L.orc_gemm_blocked_s.argtypes = _gemm_argtypes(_F, ct.c_float) + [ct.c_int]
         L.orc_product_rows_dot2.argtypes = [ct.c_int, ct.c_int, ct.c_int, _I64, _I64, _I64, _D, _I64,
@@ -191,18 +196,38 @@ def matrix(rows: int, cols: int, seed: int, dist: str = "uniform", dtype=np.floa
 # ---- kernels -------------------------------------------------------------------------------------
 def gemm(order, transA, transB, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, kernel="blocked",
          nthreads: int = 0):
-    """CBLAS-semantics C = alpha*op(A)op(B) + beta*C with the Blaze restatement (in place on C)."""
+    """CBLAS-semantics C = alpha*op(A)op(B) + beta*C with the Blaze restatement (in place on C).
+
+    kernel: "blocked" (mmm), "default" (scalar i-k-j) or "small" (register-blocked small kernel)."""
     L = lib()
-    if C.dtype == np.float64:
-        if kernel == "blocked":
-            L.orc_gemm_blocked_d(order, transA, transB, m, n, k, alpha, _p(A), lda, _p(B), ldb, beta, _p(C), ldc, nthreads)
-        else:
-            L.orc_gemm_default_d(order, transA, transB, m, n, k, alpha, _p(A), lda, _p(B), ldb, beta, _p(C), ldc)
+    sfx = "d" if C.dtype == np.float64 else "s"
+    if kernel == "blocked":
+        getattr(L, "orc_gemm_blocked_" + sfx)(order, transA, transB, m, n, k, alpha, _p(A), lda, _p(B), ldb, beta,
+                                              _p(C), ldc, nthreads)
+    elif kernel in ("default", "small"):
+        getattr(L, f"orc_gemm_{kernel}_" + sfx)(order, transA, transB, m, n, k, alpha, _p(A), lda, _p(B), ldb, beta,
+                                                _p(C), ldc)
     else:
-        if kernel == "blocked":
-            L.orc_gemm_blocked_s(order, transA, transB, m, n, k, alpha, _p(A), lda, _p(B), ldb, beta, _p(C), ldc, nthreads)
-        else:
-            L.orc_gemm_default_s(order, transA, transB, m, n, k, alpha, _p(A), lda, _p(B), ldb, beta, _p(C), ldc)
+        raise ValueError(kernel)
+    return C
+
+
+def batch_descriptor(specs):
+    """(desc, alpha_beta) arrays of a product list for gemm_batch_small: per product order, transA,
+    transB, m, n, k, lda, ldb, ldc and the element offsets offA, offB, offC."""
+    keys = ("order", "transA", "transB", "m", "n", "k", "lda", "ldb", "ldc", "offA", "offB", "offC")
+    desc = np.array([[int(sp[key]) for key in keys] for sp in specs], dtype=np.int64).reshape(-1, 12)
+    ab = np.array([[sp["alpha"], sp["beta"]] for sp in specs], dtype=np.float64).reshape(-1, 2)
+    return np.ascontiguousarray(desc), ab
+
+
+def gemm_batch_small(desc, ab, A, B, C, nthreads: int = 0):
+    """Blaze's small kernel over every product of a batch (in place on C), products spread over
+    nthreads OpenMP threads (<= 0: all)."""
+    L = lib()
+    ab = np.ascontiguousarray(ab, dtype=C.dtype)
+    f = L.orc_gemm_batch_small_d if C.dtype == np.float64 else L.orc_gemm_batch_small_s
+    f(len(desc), desc.ctypes.data_as(ct.POINTER(ct.c_int64)), _p(ab), _p(A), _p(B), _p(C), nthreads)
     return C
 
 

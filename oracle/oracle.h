@@ -59,6 +59,20 @@ void orc_gemm_default_s(int order, int transA, int transB, int64_t m, int64_t n,
                         float alpha, const float* A, int64_t lda, const float* B, int64_t ldb,
                         float beta, float* C, int64_t ldc);
 /* nthreads <= 0 selects the OpenMP default. */
+/* Blaze's register-blocked small kernel (see oracle_blaze.c); same arguments as above. */
+void orc_gemm_small_d(int order, int transA, int transB, int64_t m, int64_t n, int64_t k,
+                      double alpha, const double* A, int64_t lda, const double* B, int64_t ldb,
+                      double beta, double* C, int64_t ldc);
+void orc_gemm_small_s(int order, int transA, int transB, int64_t m, int64_t n, int64_t k,
+                      float alpha, const float* A, int64_t lda, const float* B, int64_t ldb,
+                      float beta, float* C, int64_t ldc);
+/* The small kernel over `count` products: desc holds 12 integers per product (order, transA,
+ * transB, m, n, k, lda, ldb, ldc, and the element offsets of A, B and C in the three buffers),
+ * ab holds alpha and beta per product; products are spread over nthreads (<= 0: all) threads. */
+void orc_gemm_batch_small_d(int64_t count, const int64_t* desc, const double* ab, const double* A,
+                            const double* B, double* C, int nthreads);
+void orc_gemm_batch_small_s(int64_t count, const int64_t* desc, const float* ab, const float* A,
+                            const float* B, float* C, int nthreads);
 void orc_gemm_blocked_d(int order, int transA, int transB, int64_t m, int64_t n, int64_t k,
                         double alpha, const double* A, int64_t lda, const double* B, int64_t ldb,
                         double beta, double* C, int64_t ldc, int nthreads);

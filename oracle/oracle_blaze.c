@@ -12,6 +12,15 @@
  *      The alpha/beta update follows Blaze's scaled/add-assign expressions: the product is
  *      formed first, then C = alpha*P (beta == 0: C is not read) or C = alpha*P + beta*C.
  *
+ *  orc_gemm_small_*     blaze/math/expressions/DMatDMatMultExpr.h:864-1878 (selectSmallAssignKernel,
+ *      row-major C; column-major C through the transposed identity below)
+ *      Column panels of 5, 4, 3, 2 and 1 SIMD widths (then single columns; the width of the
+ *      build target's vectors, 128 bits here), two rows of C at a time, k innermost with one accumulator per output: C(i,j) = A(i,0)*B(0,j), then
+ *      += A(i,k)*B(k,j) for k = 1..K-1 — the same sequential per-element order as the default
+ *      kernel, in the register-blocked loop nest that makes it Blaze's fast path for small and
+ *      skinny products.  orc_gemm_batch_small_* runs it over a list of products (the batched
+ *      configuration's CPU baseline), products spread over OpenMP threads.
+ *
  *  orc_gemm_blocked_*   blaze/math/dense/MMM.h:105-600 (`mmm`, row-major C)
  *      beta == 0 resets C without reading it, beta != 1 scales C (MMM.h:146-151);
  *      k-panels of KBLOCK = MMM_OUTER_BLOCK_SIZE*16/sizeof(T) = 112*16/sizeof(T) columns
@@ -94,6 +103,102 @@ void orc_gemm_default_##SUFFIX(int order, int transA, int transB, int64_t m, int
 
 DEFINE_DEFAULT(d, double)
 DEFINE_DEFAULT(s, float)
+
+/* ---------------------------------------------------------------------------------------------
+ * small (register-blocked) kernel
+ * ------------------------------------------------------------------------------------------- */
+/* One panel of W columns (W a multiple of the lane count, or 1) for rows i0..i0+R-1 (R = 1 or 2);
+ * called with W a literal, so that the loops over the panel have fixed trip counts. */
+#define DEFINE_SMALL(SUFFIX, T, LANES)                                                             \
+static inline __attribute__((always_inline)) void small_panel_##SUFFIX(                          \
+        int tA, int tB, int64_t i0, int R, int64_t j0, const int W, int64_t k, T alpha,          \
+        const T* A, int64_t lda, const T* B, int64_t ldb, T beta, T* C, int64_t ldc) {           \
+    T acc0[5 * LANES], acc1[5 * LANES], bp[5 * LANES];                                           \
+    const int64_t sa = tA ? 1 : lda, pa = tA ? lda : 1; /* A(i,p) = A[i*sa + p*pa] */            \
+    const T* a0 = A + i0 * sa;                                                                   \
+    const T* a1 = A + (i0 + (R > 1 ? 1 : 0)) * sa;                                               \
+    for (int64_t p = 0; p < k; ++p) {                                                            \
+        const T* b;                                                                              \
+        if (!tB) {                                                                               \
+            b = B + p * ldb + j0;                                                                \
+        } else {                                                                                 \
+            for (int w = 0; w < W; ++w) bp[w] = B[(j0 + w) * ldb + p];                           \
+            b = bp;                                                                              \
+        }                                                                                        \
+        const T x0 = a0[p * pa], x1 = a1[p * pa];                                                \
+        if (p == 0) {                                                                            \
+            for (int w = 0; w < W; ++w) { acc0[w] = x0 * b[w]; acc1[w] = x1 * b[w]; }            \
+        } else {                                                                                 \
+            for (int w = 0; w < W; ++w) { acc0[w] += x0 * b[w]; acc1[w] += x1 * b[w]; }          \
+        }                                                                                        \
+    }                                                                                            \
+    for (int r = 0; r < R; ++r) {                                                                \
+        const T* acc = r ? acc1 : acc0;                                                          \
+        T* c = C + (i0 + r) * ldc + j0;                                                          \
+        if (beta == (T)0)                                                                        \
+            for (int w = 0; w < W; ++w) c[w] = alpha * acc[w];                                   \
+        else                                                                                     \
+            for (int w = 0; w < W; ++w) c[w] = alpha * acc[w] + beta * c[w];                     \
+    }                                                                                            \
+}                                                                                                \
+static void small_cols_##SUFFIX(int tA, int tB, int64_t m, int64_t j, const int W, int64_t k,    \
+                                T alpha, const T* A, int64_t lda, const T* B, int64_t ldb,       \
+                                T beta, T* C, int64_t ldc) {                                     \
+    for (int64_t i = 0; i < m; i += 2)                                                           \
+        small_panel_##SUFFIX(tA, tB, i, (i + 2 <= m) ? 2 : 1, j, W, k, alpha, A, lda, B, ldb,    \
+                             beta, C, ldc);                                                      \
+}                                                                                                \
+static void small_rm_##SUFFIX(int tA, int tB, int64_t m, int64_t n, int64_t k, T alpha,          \
+                              const T* A, int64_t lda, const T* B, int64_t ldb, T beta, T* C,    \
+                              int64_t ldc) {                                                     \
+    if (k == 0) {                                                                                \
+        for (int64_t i = 0; i < m; ++i)                                                          \
+            for (int64_t j = 0; j < n; ++j)                                                      \
+                C[i * ldc + j] = beta == (T)0 ? (T)0 : beta * C[i * ldc + j];                     \
+        return;                                                                                  \
+    }                                                                                            \
+    int64_t j = 0;                                                                               \
+    for (; j + 5 * LANES <= n; j += 5 * LANES)                                                   \
+        small_cols_##SUFFIX(tA, tB, m, j, 5 * LANES, k, alpha, A, lda, B, ldb, beta, C, ldc);    \
+    for (; j + 4 * LANES <= n; j += 4 * LANES)                                                   \
+        small_cols_##SUFFIX(tA, tB, m, j, 4 * LANES, k, alpha, A, lda, B, ldb, beta, C, ldc);    \
+    for (; j + 3 * LANES <= n; j += 3 * LANES)                                                   \
+        small_cols_##SUFFIX(tA, tB, m, j, 3 * LANES, k, alpha, A, lda, B, ldb, beta, C, ldc);    \
+    for (; j + 2 * LANES <= n; j += 2 * LANES)                                                   \
+        small_cols_##SUFFIX(tA, tB, m, j, 2 * LANES, k, alpha, A, lda, B, ldb, beta, C, ldc);    \
+    for (; j + LANES <= n; j += LANES)                                                           \
+        small_cols_##SUFFIX(tA, tB, m, j, LANES, k, alpha, A, lda, B, ldb, beta, C, ldc);        \
+    for (; j < n; ++j)                                                                           \
+        small_cols_##SUFFIX(tA, tB, m, j, 1, k, alpha, A, lda, B, ldb, beta, C, ldc);            \
+}                                                                                                \
+void orc_gemm_small_##SUFFIX(int order, int transA, int transB, int64_t m, int64_t n, int64_t k, \
+                             T alpha, const T* A, int64_t lda, const T* B, int64_t ldb, T beta,  \
+                             T* C, int64_t ldc) {                                                \
+    const int tA = (transA != ORC_NO_TRANS), tB = (transB != ORC_NO_TRANS);                      \
+    if (m <= 0 || n <= 0) return;                                                                \
+    if (order == ORC_ROW_MAJOR)                                                                  \
+        small_rm_##SUFFIX(tA, tB, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);                 \
+    else                                                                                         \
+        small_rm_##SUFFIX(tB, tA, n, m, k, alpha, B, ldb, A, lda, beta, C, ldc);                 \
+}                                                                                                \
+void orc_gemm_batch_small_##SUFFIX(int64_t count, const int64_t* desc, const T* ab, const T* A,  \
+                                   const T* B, T* C, int nthreads) {                             \
+    int nt = nthreads > 0 ? nthreads : orc_max_threads();                                        \
+    if (nt < 1) nt = 1;                                                                          \
+    _Pragma("omp parallel for num_threads(nt) schedule(dynamic, 16)")                            \
+    for (int64_t q = 0; q < count; ++q) {                                                        \
+        const int64_t* d = desc + 12 * q;                                                        \
+        orc_gemm_small_##SUFFIX((int)d[0], (int)d[1], (int)d[2], d[3], d[4], d[5], ab[2 * q],    \
+                                A + d[9], d[6], B + d[10], d[7], ab[2 * q + 1], C + d[11], d[8]); \
+    }                                                                                            \
+}
+
+/* Blaze sizes these panels by the SIMD width of the build target; the oracle is built for the
+ * baseline 128-bit vectors of both hosts (SSE2 on x86-64, NEON on Arm): 2 doubles, 4 floats. */
+#define SMALL_LANES_D 2
+#define SMALL_LANES_S 4
+DEFINE_SMALL(d, double, SMALL_LANES_D)
+DEFINE_SMALL(s, float, SMALL_LANES_S)
 
 /* ---------------------------------------------------------------------------------------------
  * blocked (mmm) kernel

@@ -13,9 +13,9 @@ def sizes(count: int, seed: int, lo: int = 4, hi: int = 256) -> np.ndarray:
     return np.clip(np.rint(np.exp(u)).astype(np.int64), lo, hi).reshape(count, 3)
 
 
-def build(torch, count: int, seed: int, dtype=np.float64, layouts: bool = False, alphabeta: bool = False,
-          lo: int = 4, hi: int = 256):
-    """Host operands, device copies and the problem dicts for a batch."""
+def host_batch(count: int, seed: int, dtype=np.float64, layouts: bool = False, alphabeta: bool = False,
+               lo: int = 4, hi: int = 256):
+    """The problem dicts (offsets into one buffer per operand) and the host operands of a batch."""
     mnk = sizes(count, seed, lo, hi)
     rng = np.random.default_rng(seed)
     specs, hostA, hostB, hostC = [], [], [], []
@@ -38,6 +38,13 @@ def build(torch, count: int, seed: int, dtype=np.float64, layouts: bool = False,
     A = O.uniform(offA, seed + 1, dtype=dtype)
     B = O.uniform(offB, seed + 2, dtype=dtype)
     C = O.uniform(offC, seed + 3, dtype=dtype)
+    return specs, A, B, C
+
+
+def build(torch, count: int, seed: int, dtype=np.float64, layouts: bool = False, alphabeta: bool = False,
+          lo: int = 4, hi: int = 256):
+    """Host operands, device copies and the problem dicts for a batch."""
+    specs, A, B, C = host_batch(count, seed, dtype, layouts, alphabeta, lo, hi)
     tdt = torch.float64 if dtype == np.float64 else torch.float32
     dA = torch.from_numpy(A).cuda()
     dB = torch.from_numpy(B).cuda()
@@ -51,13 +58,13 @@ def build(torch, count: int, seed: int, dtype=np.float64, layouts: bool = False,
     return specs, A, B, C, dA, dB, dC
 
 
-def reference(specs, A, B, C0):
-    """The same batch through the oracle's restatement of Blaze's default kernel."""
+def reference(specs, A, B, C0, kernel="default"):
+    """The same batch through the oracle's restatement of Blaze's default (or small) kernel."""
     R = C0.copy()
     for sp in specs:
         a = A[sp["offA"]: sp["offA"] + sp["ra"] * sp["lda"]]
         b = B[sp["offB"]: sp["offB"] + sp["rb"] * sp["ldb"]]
         c = R[sp["offC"]: sp["offC"] + sp["rc"] * sp["ldc"]]
         O.gemm(sp["order"], sp["transA"], sp["transB"], sp["m"], sp["n"], sp["k"], sp["alpha"], a, sp["lda"], b,
-               sp["ldb"], sp["beta"], c, sp["ldc"], kernel="default")
+               sp["ldb"], sp["beta"], c, sp["ldc"], kernel=kernel)
     return R

@@ -33,7 +33,7 @@ def test_golden_inputs_reproduce():
         assert np.isclose(np.sum(C0, dtype=np.float64), c["sumC0"], rtol=0, atol=1e-9 * max(1, C0.size))
 
 
-@pytest.mark.parametrize("kernel", ["blocked", "default"])
+@pytest.mark.parametrize("kernel", ["blocked", "default", "small"])
 def test_port_matches_blaze_golden(kernel):
     """The C restatement reproduces Blaze's results (Blaze's relaxed equality for double,
     a float-rounding bound for float) on every golden case."""
@@ -100,3 +100,34 @@ def test_fro_norm_and_layouts():
             L = O.logical(order, t, lr, lc, A, ld)
             assert abs(float(np.sqrt(np.sum(L * L))) - ref) <= 1e-13 * ref
             del rows, cols
+
+
+def test_small_kernel_sums_like_the_default_kernel():
+    """Blaze's small kernel and its default kernel add each element's products in the same k
+    order; their restatements agree bit for bit on every storage order and ragged shape."""
+    rng = np.random.default_rng(7)
+    for dt in (np.float64, np.float32):
+        for _ in range(40):
+            m, n, k = (int(v) for v in rng.integers(1, 140, 3))
+            order = O.ROW_MAJOR if rng.integers(2) else O.COL_MAJOR
+            ta = O.TRANS if rng.integers(2) else O.NO_TRANS
+            tb = O.TRANS if rng.integers(2) else O.NO_TRANS
+            lda = (k if ta == O.NO_TRANS else m) if order == O.ROW_MAJOR else (m if ta == O.NO_TRANS else k)
+            ldb = (n if tb == O.NO_TRANS else k) if order == O.ROW_MAJOR else (k if tb == O.NO_TRANS else n)
+            ldc = n if order == O.ROW_MAJOR else m
+            A = O.uniform(m * k, 11, dtype=dt); B = O.uniform(k * n, 12, dtype=dt); C0 = O.uniform(m * n, 13, dtype=dt)
+            alpha, beta = (1.0, 0.0) if rng.integers(2) else (-0.5, 1.5)
+            C1, C2 = C0.copy(), C0.copy()
+            O.gemm(order, ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C1, ldc, kernel="small")
+            O.gemm(order, ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C2, ldc, kernel="default")
+            assert np.array_equal(C1, C2), (m, n, k, order, ta, tb)
+
+
+def test_small_kernel_batch_equals_the_single_products():
+    import batched
+    for dt in (np.float64, np.float32):
+        specs, A, B, C0 = batched.host_batch(300, 21, dtype=dt, layouts=True, alphabeta=True)
+        desc, ab = O.batch_descriptor(specs)
+        C1 = O.gemm_batch_small(desc, ab, A, B, C0.copy(), nthreads=4)
+        C2 = batched.reference(specs, A, B, C0, kernel="small")
+        assert np.array_equal(C1, C2)
