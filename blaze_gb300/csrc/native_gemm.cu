@@ -4,7 +4,8 @@
 // reached from DMatDMatMultExpr.h:2021-2037 and its three storage-order siblings), i.e. the work
 // that Blaze's own large kernel `mmm` (blaze/math/dense/MMM.h:105-600) does on the CPU.
 //
-// Design (one CTA per 128x128 tile of C, 256 threads, 8x8 outputs per thread):
+// Design (one CTA per 128x128 tile of C — 256x64 when C has at most 64 columns —, 256 threads,
+// 8x8 outputs per thread):
 //   * operand tiles are staged in shared memory by TMA (cp.async.bulk.tensor) as 128-byte
 //     swizzled boxes, a 4-deep mbarrier pipeline (one "full" barrier with transaction bytes and
 //     one "empty" barrier released by the eight warps per stage);
@@ -34,12 +35,21 @@
 namespace gb {
 namespace {
 
-constexpr int BM = kNativeTileM;
-constexpr int BN = kNativeTileN;
 constexpr int STAGES = 4;
 constexpr int THREADS = 256;
 constexpr int PANEL_BYTES = 128;                         // k-panel depth in bytes
-constexpr int TILE_BYTES = BM * PANEL_BYTES;             // 16 KB per operand per stage
+
+// Tile geometry for a tile of BN_ columns: BM = 16384 / BN rows, so that the 256 threads keep
+// 8 x 8 outputs each; thread (tx, ty) owns rows ty + TY r and columns tx + TX c.
+template <int BN_>
+struct NativeTile {
+    static constexpr int BN = BN_;
+    static constexpr int BM = 16384 / BN_;
+    static constexpr int TX = BN_ / 8, TY = THREADS / TX;
+    static constexpr int A_BYTES = BM * PANEL_BYTES;     // per stage
+    static constexpr int B_BYTES = BN * PANEL_BYTES;
+    static constexpr size_t SMEM = size_t(STAGES) * (A_BYTES + B_BYTES) + 2 * STAGES * 8 + 1024;
+};
 
 template <typename T>
 struct NativeParams {
@@ -76,22 +86,24 @@ __device__ __forceinline__ uint32_t b_off(int kk, int n) {
     return uint32_t((n / E) * BK * PANEL_BYTES) + swz128(uint32_t(kk * PANEL_BYTES + (n % E) * sizeof(T)));
 }
 
-template <typename T, bool TRANS_A, bool TRANS_B>
+template <typename T, bool TRANS_A, bool TRANS_B, int BN_>
 __global__ void __launch_bounds__(THREADS, 1)
 native_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                    const NativeParams<T> p) {
+    using Tile = NativeTile<BN_>;
+    constexpr int BM = Tile::BM, BN = Tile::BN, TX = Tile::TX, TY = Tile::TY;
     constexpr int BK = PANEL_BYTES / sizeof(T);
     constexpr int E = PANEL_BYTES / sizeof(T);
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     // 1024-byte alignment for the swizzle atoms
     uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     uint8_t* tilesA = smem;
-    uint8_t* tilesB = smem + STAGES * TILE_BYTES;
-    NativeBarriers* bars = reinterpret_cast<NativeBarriers*>(smem + 2 * STAGES * TILE_BYTES);
+    uint8_t* tilesB = smem + STAGES * Tile::A_BYTES;
+    NativeBarriers* bars = reinterpret_cast<NativeBarriers*>(smem + STAGES * (Tile::A_BYTES + Tile::B_BYTES));
 
     const int tid = threadIdx.x;
     const int lane = tid & 31;
-    const int tx = tid & 15, ty = tid >> 4;
+    const int tx = tid % TX, ty = tid / TX;
     const int64_t m0 = int64_t(blockIdx.y) * BM;
     const int64_t n0 = int64_t(blockIdx.x) * BN;
     const int64_t kbeg = int64_t(blockIdx.z) * p.k_per_split;
@@ -111,10 +123,10 @@ native_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constan
 
     auto issue = [&](int t, int s) {
         const uint32_t full = smem_u32(&bars->full[s]);
-        mbar_arrive_expect_tx(full, 2 * TILE_BYTES);
+        mbar_arrive_expect_tx(full, Tile::A_BYTES + Tile::B_BYTES);
         const int32_t kx = int32_t(kbeg + int64_t(t) * BK);
-        const uint32_t dA = smem_u32(tilesA + s * TILE_BYTES);
-        const uint32_t dB = smem_u32(tilesB + s * TILE_BYTES);
+        const uint32_t dA = smem_u32(tilesA + s * Tile::A_BYTES);
+        const uint32_t dB = smem_u32(tilesB + s * Tile::B_BYTES);
         if (!TRANS_A) {
             tma_load_2d(dA, &tmA, kx, int32_t(m0), full);
         } else {
@@ -151,15 +163,15 @@ native_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constan
             ok = false;
             break;
         }
-        const uint8_t* As = tilesA + s * TILE_BYTES;
-        const uint8_t* Bs = tilesB + s * TILE_BYTES;
+        const uint8_t* As = tilesA + s * Tile::A_BYTES;
+        const uint8_t* Bs = tilesB + s * Tile::B_BYTES;
 #pragma unroll 4
         for (int kk = 0; kk < BK; ++kk) {
             T a[8], b[8];
 #pragma unroll
-            for (int r = 0; r < 8; ++r) a[r] = *reinterpret_cast<const T*>(As + a_off<T, TRANS_A>(ty + 16 * r, kk));
+            for (int r = 0; r < 8; ++r) a[r] = *reinterpret_cast<const T*>(As + a_off<T, TRANS_A>(ty + TY * r, kk));
 #pragma unroll
-            for (int c = 0; c < 8; ++c) b[c] = *reinterpret_cast<const T*>(Bs + b_off<T, TRANS_B>(kk, tx + 16 * c));
+            for (int c = 0; c < 8; ++c) b[c] = *reinterpret_cast<const T*>(Bs + b_off<T, TRANS_B>(kk, tx + TX * c));
 #pragma unroll
             for (int r = 0; r < 8; ++r)
 #pragma unroll
@@ -193,11 +205,11 @@ native_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constan
         T* w = p.ws + int64_t(blockIdx.z) * p.m * p.n;
 #pragma unroll
         for (int r = 0; r < 8; ++r) {
-            const int64_t i = m0 + ty + 16 * r;
+            const int64_t i = m0 + ty + TY * r;
             if (i >= p.m) continue;
 #pragma unroll
             for (int c = 0; c < 8; ++c) {
-                const int64_t j = n0 + tx + 16 * c;
+                const int64_t j = n0 + tx + TX * c;
                 if (j < p.n) w[i * p.n + j] = acc[r][c];
             }
         }
@@ -205,12 +217,12 @@ native_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constan
     }
 #pragma unroll
     for (int r = 0; r < 8; ++r) {
-        const int64_t i = m0 + ty + 16 * r;
+        const int64_t i = m0 + ty + TY * r;
         if (i >= p.m) continue;
         T* crow = p.C + i * p.ldc;
 #pragma unroll
         for (int c = 0; c < 8; ++c) {
-            const int64_t j = n0 + tx + 16 * c;
+            const int64_t j = n0 + tx + TX * c;
             if (j >= p.n) continue;
             const T v = p.alpha * acc[r][c];
             crow[j] = (p.beta == T(0)) ? v : fma(p.beta, crow[j], v);
@@ -251,47 +263,32 @@ constexpr CUtensorMapDataType tmap_type() {
     return sizeof(T) == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
 }
 
-constexpr size_t kSmemBytes = 2 * STAGES * TILE_BYTES + sizeof(NativeBarriers) + 1024;
-
-template <typename T, bool TA, bool TB>
+template <typename T, bool TA, bool TB, int BN_>
 cudaError_t launch_variant(const CUtensorMap& a, const CUtensorMap& b, const NativeParams<T>& p, dim3 grid,
                            cudaStream_t s) {
-    auto kern = native_gemm_kernel<T, TA, TB>;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kSmemBytes));
+    auto kern = native_gemm_kernel<T, TA, TB, BN_>;
+    constexpr int smem = int(NativeTile<BN_>::SMEM);
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return e;
     {
         KernelTimer timer("native_gemm", s);
-        kern<<<grid, THREADS, kSmemBytes, s>>>(a, b, p);
+        kern<<<grid, THREADS, smem, s>>>(a, b, p);
     }
     count_launches(1);
     return cudaGetLastError();
 }
 
-}  // namespace
+// Columns of the CTA tile: 64 (256 x 64 tiles) for products with at most 64 columns, where a
+// 128-column tile would compute half of its outputs on padding, else 128.
+int native_tile_n(int64_t n) { return n <= 64 ? 64 : 128; }
 
-int native_choose_splits(int64_t m, int64_t n, int64_t k, int elem_bytes, int num_sms) {
-    const int64_t bk = PANEL_BYTES / elem_bytes;
-    const int64_t tiles = ((m + BM - 1) / BM) * ((n + BN - 1) / BN);
-    if (tiles >= num_sms || k < 4 * bk) return 1;
-    // enough splits to cover every SM once, each at least four panels deep
-    int64_t splits = (num_sms + tiles - 1) / tiles;
-    splits = std::min<int64_t>(splits, k / (4 * bk));
-    return int(std::max<int64_t>(splits, 1));
-}
-
-template <typename T>
-cudaError_t native_gemm(const Gemm& g, int splits, T* workspace, const LaunchCtl& ctl, cudaStream_t s,
-                        std::string* err) {
-    if (g.m <= 0 || g.n <= 0) return cudaSuccess;
+template <typename T, int BN_>
+cudaError_t native_gemm_tiled(const Gemm& g, int splits, T* workspace, const LaunchCtl& ctl, cudaStream_t s,
+                              std::string* err) {
+    using Tile = NativeTile<BN_>;
+    constexpr int BM = Tile::BM, BN = Tile::BN;
     const int64_t BK = PANEL_BYTES / sizeof(T);
     const int E = PANEL_BYTES / sizeof(T);
-    if (g.k == 0) {
-        const int64_t total = g.m * g.n;
-        const int blocks = int(std::min<int64_t>((total + 255) / 256, 4096));
-        scale_c_kernel<T><<<blocks, 256, 0, s>>>(g.m, g.n, T(g.beta), static_cast<T*>(g.C), g.ldc);
-        count_launches(1);
-        return cudaGetLastError();
-    }
     CUtensorMap ta, tb;
     const CUtensorMapDataType dt = tmap_type<T>();
     // A: rows x cols as stored (row-major storage, ld = lda)
@@ -327,10 +324,10 @@ cudaError_t native_gemm(const Gemm& g, int splits, T* workspace, const LaunchCtl
     }
     dim3 grid(unsigned((g.n + BN - 1) / BN), unsigned((g.m + BM - 1) / BM), unsigned(splits));
     cudaError_t e;
-    if (!g.ta && !g.tb) e = launch_variant<T, false, false>(ta, tb, p, grid, s);
-    else if (!g.ta && g.tb) e = launch_variant<T, false, true>(ta, tb, p, grid, s);
-    else if (g.ta && !g.tb) e = launch_variant<T, true, false>(ta, tb, p, grid, s);
-    else e = launch_variant<T, true, true>(ta, tb, p, grid, s);
+    if (!g.ta && !g.tb) e = launch_variant<T, false, false, BN_>(ta, tb, p, grid, s);
+    else if (!g.ta && g.tb) e = launch_variant<T, false, true, BN_>(ta, tb, p, grid, s);
+    else if (g.ta && !g.tb) e = launch_variant<T, true, false, BN_>(ta, tb, p, grid, s);
+    else e = launch_variant<T, true, true, BN_>(ta, tb, p, grid, s);
     if (e != cudaSuccess || splits == 1) return e;
     const int64_t total = g.m * g.n;
     const int blocks = int(std::min<int64_t>((total + 255) / 256, 152 * 16));
@@ -338,6 +335,36 @@ cudaError_t native_gemm(const Gemm& g, int splits, T* workspace, const LaunchCtl
                                                    static_cast<T*>(g.C), g.ldc);
     count_launches(1);
     return cudaGetLastError();
+}
+
+}  // namespace
+
+int native_choose_splits(int64_t m, int64_t n, int64_t k, int elem_bytes, int num_sms) {
+    const int64_t bk = PANEL_BYTES / elem_bytes;
+    const int64_t bn = native_tile_n(n), bm = 16384 / bn;
+    const int64_t tiles = ((m + bm - 1) / bm) * ((n + bn - 1) / bn);
+    if (2 * tiles > num_sms || k < 32 * bk) return 1;
+    // as many k-splits as still fit one wave of CTAs (one CTA per SM), each at least 16 panels deep
+    // (four times the stage ring, so that filling the ring stays a small part of a split): a split
+    // count that spills a few CTAs into a second wave doubles the time
+    int64_t splits = num_sms / tiles;
+    splits = std::min<int64_t>(splits, k / (16 * bk));
+    return int(std::max<int64_t>(splits, 1));
+}
+
+template <typename T>
+cudaError_t native_gemm(const Gemm& g, int splits, T* workspace, const LaunchCtl& ctl, cudaStream_t s,
+                        std::string* err) {
+    if (g.m <= 0 || g.n <= 0) return cudaSuccess;
+    if (g.k == 0) {
+        const int64_t total = g.m * g.n;
+        const int blocks = int(std::min<int64_t>((total + 255) / 256, 4096));
+        scale_c_kernel<T><<<blocks, 256, 0, s>>>(g.m, g.n, T(g.beta), static_cast<T*>(g.C), g.ldc);
+        count_launches(1);
+        return cudaGetLastError();
+    }
+    return native_tile_n(g.n) == 64 ? native_gemm_tiled<T, 64>(g, splits, workspace, ctl, s, err)
+                                    : native_gemm_tiled<T, 128>(g, splits, workspace, ctl, s, err);
 }
 
 template cudaError_t native_gemm<double>(const Gemm&, int, double*, const LaunchCtl&, cudaStream_t, std::string*);
