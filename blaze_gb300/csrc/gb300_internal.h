@@ -112,8 +112,13 @@ template <typename T>
 int gemm_entry(int order, int transA, int transB, int64_t m, int64_t n, int64_t k, T alpha, const T* A, int64_t lda,
                const T* B, int64_t ldb, T beta, T* C, int64_t ldc, gb300_gemm_opts* opts, const char* routine);
 
-// Tile edge of the native kernel.
-constexpr int kNativeTileM = 128;
-constexpr int kNativeTileN = 128;
+// Grouped launches of the serving loop (grouped.cu): a lane stages the problem table of a batch of
+// small FP64 products and runs them as one persistent grouped launch on its stream.  A lane's next
+// launch must wait until its previous one has finished.
+struct GroupedLane;
+GroupedLane* grouped_lane_create(cudaStream_t stream, std::string* err);
+void grouped_lane_destroy(GroupedLane* lane);
+int grouped_lane_launch(GroupedLane* lane, const gb300_gemm_problem* probs, int64_t count, double* useful_flops,
+                        std::string* err);
 
 }  // namespace gb

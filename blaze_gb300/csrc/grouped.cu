@@ -85,7 +85,9 @@ __device__ __forceinline__ void warp_tile(const DevProblem& p, int tm, int tn, i
     for (int r = 0; r < R; ++r)
 #pragma unroll
         for (int c = 0; c < C; ++c) acc[r][c] = T(0);
-#pragma unroll 1
+    // unrolled so that the loads of the next k steps issue before this step's multiply-adds retire
+    // (the accumulation order of every output stays k = 0, 1, 2, ...)
+#pragma unroll 2
     for (int kk = 0; kk < p.k; ++kk) {
         T a0[R], b0[C];
 #pragma unroll
@@ -262,17 +264,18 @@ void plan_free(GroupedPlan* p) {
     delete p;
 }
 
+// The device problem table and the flat tile list of a batch (longest tiles first).  Each
+// product's shape depends only on its own (m, n, k) and the tuning state, so a product gets the same
+// tiles — and the same result bits — whatever else is in the batch.
 template <typename T>
-int plan_create(const gb300_gemm_problem* probs, int64_t count, int force_shape, GroupedPlan** out, std::string* err,
-                int policy = -1) {
-    Runtime& r = runtime();
-    int st = ensure_init(err);
-    if (st != GB300_OK) return st;
+int build_tables(const gb300_gemm_problem* probs, int64_t count, int force_shape, int policy,
+                 std::vector<DevProblem>& hp, std::vector<DevTile>& ht, double& useful, double& padded,
+                 std::string* err) {
     const int didx = sizeof(T) == 8 ? 0 : 1;
-    std::vector<DevProblem> hp;
+    hp.clear();
+    ht.clear();
     hp.reserve(size_t(count));
-    std::vector<DevTile> ht;
-    double useful = 0, padded = 0;
+    useful = padded = 0;
     for (int64_t q = 0; q < count; ++q) {
         const gb300_gemm_problem& x = probs[q];
         const bool rm = x.order == 101;
@@ -322,6 +325,29 @@ int plan_create(const gb300_gemm_problem* probs, int64_t count, int force_shape,
         const double wb = double(pb.k) * shape_rows(pb.shape) * shape_cols(pb.shape);
         return wa > wb;
     });
+    return GB300_OK;
+}
+
+// Persistent grid for `ntiles` warp tiles: every SM's resident blocks, or fewer for a short list.
+template <typename T>
+int grouped_grid(int64_t ntiles, int num_sms) {
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, grouped_kernel<T>, 256, 0);
+    per_sm = std::max(per_sm, 1);
+    return int(std::max<int64_t>(1, std::min<int64_t>(int64_t(num_sms) * per_sm, (ntiles + 7) / 8)));
+}
+
+template <typename T>
+int plan_create(const gb300_gemm_problem* probs, int64_t count, int force_shape, GroupedPlan** out, std::string* err,
+                int policy = -1) {
+    Runtime& r = runtime();
+    int st = ensure_init(err);
+    if (st != GB300_OK) return st;
+    std::vector<DevProblem> hp;
+    std::vector<DevTile> ht;
+    double useful = 0, padded = 0;
+    st = build_tables<T>(probs, count, force_shape, policy, hp, ht, useful, padded, err);
+    if (st != GB300_OK) return st;
     auto* p = new GroupedPlan();
     p->elem = sizeof(T);
     p->count = count;
@@ -346,11 +372,7 @@ int plan_create(const gb300_gemm_problem* probs, int64_t count, int force_shape,
         if (err) *err = std::string("grouped plan set-up: ") + cudaGetErrorString(e);
         return GB300_ERR_NO_MEMORY;
     }
-    int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, grouped_kernel<T>, 256, 0);
-    per_sm = std::max(per_sm, 1);
-    const int64_t warps_needed = p->ntiles;
-    p->grid = int(std::max<int64_t>(1, std::min<int64_t>(int64_t(r.num_sms) * per_sm, (warps_needed + 7) / 8)));
+    p->grid = grouped_grid<T>(p->ntiles, r.num_sms);
     // capture: counter reset + persistent kernel
     e = cudaStreamBeginCapture(p->cap_stream, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
@@ -528,6 +550,97 @@ int autotune(int didx, int effort, std::string* err) {
 }
 
 }  // namespace
+
+// ---- lanes: grouped launches of the serving loop ---------------------------------------------
+// A lane owns grow-only page-locked staging and device buffers for the problem table and tile
+// list, so that a batch of small requests goes out as one plain launch (copies, counter reset,
+// persistent kernel) on the lane's stream without allocating once the buffers have grown.  The
+// caller waits for a lane's previous launch to finish before it launches on that lane again.
+struct GroupedLane {
+    cudaStream_t stream = nullptr;
+    void* h_buf = nullptr;
+    size_t h_bytes = 0;
+    void* d_buf = nullptr;
+    size_t d_bytes = 0;
+    int* d_counter = nullptr;
+    std::vector<DevProblem> hp;
+    std::vector<DevTile> ht;
+};
+
+GroupedLane* grouped_lane_create(cudaStream_t stream, std::string* err) {
+    auto* l = new GroupedLane();
+    l->stream = stream;
+    if (cudaMalloc(&l->d_counter, sizeof(int)) != cudaSuccess) {
+        cudaGetLastError();
+        if (err) *err = "grouped lane: counter allocation failed";
+        delete l;
+        return nullptr;
+    }
+    return l;
+}
+
+void grouped_lane_destroy(GroupedLane* l) {
+    if (!l) return;
+    if (l->stream) cudaStreamSynchronize(l->stream);
+    if (l->h_buf) cudaFreeHost(l->h_buf);
+    if (l->d_buf) cudaFree(l->d_buf);
+    if (l->d_counter) cudaFree(l->d_counter);
+    delete l;
+}
+
+int grouped_lane_launch(GroupedLane* l, const gb300_gemm_problem* probs, int64_t count, double* useful_flops,
+                        std::string* err) {
+    double useful = 0, padded = 0;
+    int st = build_tables<double>(probs, count, -1, -1, l->hp, l->ht, useful, padded, err);
+    if (st != GB300_OK) return st;
+    if (useful_flops) *useful_flops = useful;
+    if (l->ht.empty()) return GB300_OK;
+    const size_t pb = l->hp.size() * sizeof(DevProblem), tb = l->ht.size() * sizeof(DevTile);
+    const size_t off_t = (pb + 255) / 256 * 256, need = off_t + tb;
+    auto grow = [](size_t n) { return (n + (size_t(1) << 20) - 1) & ~((size_t(1) << 20) - 1); };
+    if (l->h_bytes < need) {
+        if (l->h_buf) cudaFreeHost(l->h_buf);
+        l->h_buf = nullptr;
+        l->h_bytes = 0;
+        if (cudaHostAlloc(&l->h_buf, grow(need), cudaHostAllocDefault) != cudaSuccess) {
+            cudaGetLastError();
+            if (err) *err = "grouped lane: staging allocation failed";
+            return GB300_ERR_NO_MEMORY;
+        }
+        l->h_bytes = grow(need);
+    }
+    if (l->d_bytes < need) {
+        if (l->d_buf) cudaFree(l->d_buf);
+        l->d_buf = nullptr;
+        l->d_bytes = 0;
+        if (cudaMalloc(&l->d_buf, grow(need)) != cudaSuccess) {
+            cudaGetLastError();
+            if (err) *err = "grouped lane: table allocation failed";
+            return GB300_ERR_NO_MEMORY;
+        }
+        l->d_bytes = grow(need);
+    }
+    auto* h = static_cast<uint8_t*>(l->h_buf);
+    std::memcpy(h, l->hp.data(), pb);
+    std::memcpy(h + off_t, l->ht.data(), tb);
+    auto* d = static_cast<uint8_t*>(l->d_buf);
+    cudaError_t e = cudaMemcpyAsync(d, h, need, cudaMemcpyHostToDevice, l->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(l->d_counter, 0, sizeof(int), l->stream);
+    if (e == cudaSuccess) {
+        const int grid = grouped_grid<double>(int64_t(l->ht.size()), runtime().num_sms);
+        grouped_kernel<double><<<grid, 256, 0, l->stream>>>(reinterpret_cast<const DevProblem*>(d),
+                                                            reinterpret_cast<const DevTile*>(d + off_t),
+                                                            int(l->ht.size()), l->d_counter);
+        count_launches(1);
+        e = cudaGetLastError();
+    }
+    if (e != cudaSuccess) {
+        if (err) *err = std::string("grouped lane launch: ") + cudaGetErrorString(e);
+        return GB300_ERR_CUDA;
+    }
+    return GB300_OK;
+}
+
 }  // namespace gb
 
 // ============================================================================================

@@ -11,12 +11,26 @@
 //     Admission is FIFO with backfill: a smaller request may pass a head request that does not fit
 //     yet, unless the head has waited longer than the aging limit.
 //   * Each slot owns a stream and a grow-only workspace, so admitted requests run concurrently
-//     and their kernels overlap on the device.  While a large tensor-core product runs, a share of
-//     the SMs is kept out of its persistent grid so that small requests keep flowing.
+//     and their kernels overlap on the device.  Large requests (max(m, n) >= large_threshold) run
+//     only on the first `large_slots` slots, whose streams have the lowest priority; the other
+//     slots take the rest at a higher priority and the batch lanes at the highest.  The block
+//     scheduler dispatches pending blocks of higher-priority streams first, so a large native
+//     product with hundreds of waiting CTAs does not hold back the kernels of small and medium
+//     requests launched after it (without priorities their p99 was that product's time).  A large
+//     request waiting for a large slot does not stop others from passing it, and while a large
+//     tensor-core product runs a share of the SMs is also kept out of its persistent grid.
+//   * Small requests (every dimension at most `batch_threshold`) do not take a slot: at each
+//     scheduling step the queued ones are coalesced into one persistent grouped launch (grouped.cu,
+//     FP64) on one of two batch lanes, up to `batch_max` per launch, while the previous launch may
+//     still run on the other lane.  FP64 meets the bound of every accuracy class (k * 2^-53 for
+//     the native and split classes, well below the BF16 classes' bounds), so a small request's
+//     class only decides its reported bound.
 //   * Completion is detected with a CUDA event per request; latency = completion - submission.
 //   * Results do not depend on the mix: the split form accumulates exact integers (its k-segments
-//     depend only on the shape), BF16 forms have a fixed accumulation order per tile, and the
-//     native kernel's split-k choice depends only on the shape.
+//     depend only on the shape), BF16 forms have a fixed accumulation order per tile, the native
+//     kernel's split-k choice depends only on the shape, and a grouped launch gives each product
+//     the warp-tile shape of its own (m, n, k) with a fixed k order per tile, whatever else is in
+//     the batch (a small request alone is a batch of one).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -52,7 +66,8 @@ struct ServeRequest {
     SplitRequest sreq;
     size_t footprint = 0;
     size_t need[kSlotCount] = {};
-    bool large = false;
+    bool large = false;       // a large tensor-core product (reserve_sms applies)
+    int cls = 1;              // size class: 0 small (grouped launches), 1 medium, 2 large
     Clock::time_point t_submit, t_start, t_end;
     int slot = -1;
     int state = 0;  // 0 queued, 1 running, 2 done
@@ -71,12 +86,35 @@ struct ServeSlot {
 };
 constexpr size_t kHostStatus = 0, kHostInfo = 64, kHostBytes = 512;
 
+// A batch lane: a stream, the grouped-launch buffers and the requests of the launch in flight.
+struct BatchLane {
+    cudaStream_t stream = nullptr;
+    GroupedLane* lane = nullptr;
+    cudaEvent_t done = nullptr;
+    std::vector<ServeRequest*> batch;
+    Clock::time_point t_start;
+};
+constexpr int kBatchLanes = 2;
+
+enum Admit : int { kAdmitted = 0, kNoSlot, kNoMemory, kLargeLimit };
+
+double percentile(std::vector<double> l, double p) {
+    if (l.empty()) return 0.0;
+    std::sort(l.begin(), l.end());
+    const double pos = p * double(l.size() - 1);
+    const size_t lo = size_t(pos);
+    const size_t hi = std::min(lo + 1, l.size() - 1);
+    return l[lo] + (l[hi] - l[lo]) * (pos - double(lo));
+}
+
 }  // namespace
 
 class Server {
   public:
     gb300_server_config cfg{};
     std::vector<ServeSlot> slots;
+    std::vector<BatchLane> lanes;
+    std::vector<gb300_gemm_problem> batch_probs;
     std::deque<ServeRequest*> queue;
     std::unordered_map<uint64_t, ServeRequest*> reqs;
     std::mutex mu;
@@ -88,6 +126,8 @@ class Server {
     int num_sms = 0;
     // statistics
     std::vector<double> latencies;
+    std::vector<double> class_lat[3];
+    int64_t grouped_launches = 0, grouped_requests = 0;
     int64_t submitted = 0, completed = 0, rejected = 0, failed = 0;
     double useful_flops = 0;
     Clock::time_point t_first;
@@ -100,18 +140,16 @@ class Server {
         return t;
     }
 
-    bool large_running() const {
-        for (const auto& s : slots)
-            if (s.cur && s.cur->large) return true;
-        return false;
-    }
+    // Slots [0, n_large) take large requests, the others everything else.
+    int n_large = 1;
 
-    // Try to start `r` on a free slot; returns true when launched.
-    bool try_admit(ServeRequest* r) {
+    // Try to start `r` on a free slot of its kind.
+    Admit try_admit(ServeRequest* r) {
         int free_slot = -1;
-        for (size_t i = 0; i < slots.size(); ++i)
+        const size_t lo = r->cls == 2 ? 0 : size_t(n_large), hi = r->cls == 2 ? size_t(n_large) : slots.size();
+        for (size_t i = lo; i < hi; ++i)
             if (!slots[i].cur) { free_slot = int(i); break; }
-        if (free_slot < 0) return false;
+        if (free_slot < 0) return r->cls == 2 ? kLargeLimit : kNoSlot;
         ServeSlot& sl = slots[size_t(free_slot)];
         // projected bytes of the slot after running r: each buffer grows to the larger of what it
         // holds and what r needs
@@ -130,10 +168,70 @@ class Server {
             others = 0;
             for (size_t i = 0; i < slots.size(); ++i)
                 if (int(i) != free_slot) others += slots[i].ws.total();
-            if (others + projected(sl) > budget) return false;
+            if (others + projected(sl) > budget) return kNoMemory;
         }
         launch(r, free_slot);
+        return kAdmitted;
+    }
+
+    // Coalesce queued small requests into one grouped launch on an idle lane.
+    bool launch_batch(BatchLane& ln) {
+        batch_probs.clear();
+        ln.batch.clear();
+        const size_t cap = size_t(std::max(1, cfg.batch_max));
+        for (auto it = queue.begin(); it != queue.end() && ln.batch.size() < cap;) {
+            ServeRequest* r = *it;
+            if (r->cls != 0) {
+                ++it;
+                continue;
+            }
+            gb300_gemm_problem p;
+            p.order = r->req.order; p.transA = r->req.transA; p.transB = r->req.transB;
+            p.m = r->req.m; p.n = r->req.n; p.k = r->req.k;
+            p.alpha = r->req.alpha; p.beta = r->req.beta;
+            p.A = r->req.A; p.lda = r->req.lda; p.B = r->req.B; p.ldb = r->req.ldb;
+            p.C = r->req.C; p.ldc = r->req.ldc;
+            batch_probs.push_back(p);
+            ln.batch.push_back(r);
+            it = queue.erase(it);
+        }
+        if (ln.batch.empty()) return false;
+        ln.t_start = Clock::now();
+        std::string err;
+        const int st = grouped_lane_launch(ln.lane, batch_probs.data(), int64_t(batch_probs.size()), nullptr, &err);
+        for (ServeRequest* r : ln.batch) {
+            r->state = 1;
+            r->t_start = ln.t_start;
+            r->res.status = st;
+            r->res.method_used = GB300_METHOD_NATIVE;
+            r->res.slices = 0;
+            r->res.error_bound = double(std::max<int64_t>(r->req.k, 1)) * 0x1p-53;
+        }
+        cudaEventRecord(ln.done, ln.stream);
+        ++grouped_launches;
+        grouped_requests += int64_t(ln.batch.size());
         return true;
+    }
+
+    void finish(ServeRequest* r) {
+        r->t_end = Clock::now();
+        r->res.queue_ms = ms_between(r->t_submit, r->t_start);
+        r->res.latency_ms = ms_between(r->t_submit, r->t_end);
+        r->res.run_ms = ms_between(r->t_start, r->t_end);
+        r->state = 2;
+        if (r->res.status == GB300_OK) {
+            ++completed;
+            latencies.push_back(r->res.latency_ms);
+            class_lat[r->cls].push_back(r->res.latency_ms);
+            useful_flops += 2.0 * double(r->g.m) * double(r->g.n) * double(r->g.k);
+        } else {
+            ++failed;
+        }
+    }
+
+    void complete_batch(BatchLane& ln) {
+        for (ServeRequest* r : ln.batch) finish(r);
+        ln.batch.clear();
     }
 
     void launch(ServeRequest* r, int si) {
@@ -166,7 +264,6 @@ class Server {
 
     void complete(ServeSlot& sl) {
         ServeRequest* r = sl.cur;
-        r->t_end = Clock::now();
         int status = 0;
         std::memcpy(&status, sl.host + kHostStatus, sizeof(int));
         if (r->res.status == GB300_OK && status != 0) r->res.status = GB300_ERR_DEVICE_TIMEOUT;
@@ -177,17 +274,7 @@ class Server {
             r->res.slices = sl_;
             r->res.error_bound = bd;
         }
-        r->res.queue_ms = ms_between(r->t_submit, r->t_start);
-        r->res.latency_ms = ms_between(r->t_submit, r->t_end);
-        r->res.run_ms = ms_between(r->t_start, r->t_end);
-        r->state = 2;
-        if (r->res.status == GB300_OK) {
-            ++completed;
-            latencies.push_back(r->res.latency_ms);
-            useful_flops += 2.0 * double(r->g.m) * double(r->g.n) * double(r->g.k);
-        } else {
-            ++failed;
-        }
+        finish(r);
         sl.cur = nullptr;
     }
 
@@ -202,23 +289,41 @@ class Server {
                     progressed = true;
                 }
             }
+            for (auto& ln : lanes) {
+                if (!ln.batch.empty() && cudaEventQuery(ln.done) == cudaSuccess) {
+                    complete_batch(ln);
+                    progressed = true;
+                }
+            }
             if (progressed) cv_done.notify_all();
-            // admissions: FIFO with backfill, unless the head has aged past the limit
+            // small requests: one grouped launch per idle lane with everything queued
+            for (auto& ln : lanes)
+                if (ln.batch.empty() && launch_batch(ln)) progressed = true;
+            // admissions: FIFO with backfill, unless the head has aged past the limit; a large
+            // request waiting for a large slot lets the others pass
             const auto now = Clock::now();
             bool head_blocked = false;
+            bool first = true;
             for (auto it = queue.begin(); it != queue.end();) {
                 ServeRequest* r = *it;
                 if (head_blocked) break;
-                if (try_admit(r)) {
+                if (r->cls == 0) {  // waits for a lane
+                    ++it;
+                    continue;
+                }
+                const Admit a = try_admit(r);
+                if (a == kAdmitted) {
                     it = queue.erase(it);
                     progressed = true;
                 } else {
-                    if (it == queue.begin() && ms_between(r->t_submit, now) > cfg.aging_ms) head_blocked = true;
+                    if (first && a != kLargeLimit && ms_between(r->t_submit, now) > cfg.aging_ms) head_blocked = true;
                     ++it;
                 }
+                first = false;
             }
             bool busy = false;
             for (const auto& sl : slots) busy |= (sl.cur != nullptr);
+            for (const auto& ln : lanes) busy |= !ln.batch.empty();
             if (!progressed) {
                 // running work is polled every 20 us; an idle server sleeps until a submission
                 if (busy) cv_work.wait_for(lock, std::chrono::microseconds(20));
@@ -243,6 +348,9 @@ void gb300_server_config_init(gb300_server_config* c) {
     c->reserve_sms = 16;
     c->aging_ms = 50.0;
     c->large_threshold = 2048;
+    c->batch_threshold = 256;
+    c->batch_max = 2048;
+    c->large_slots = 2;
 }
 
 int gb300_server_create(const gb300_server_config* cfg, gb300_server** out) {
@@ -266,9 +374,17 @@ int gb300_server_create(const gb300_server_config* cfg, gb300_server** out) {
     s->budget = size_t(std::max<int64_t>(s->cfg.memory_budget_bytes, 0));
     s->budget = std::min(s->budget, size_t(double(fr) * 0.95));
     s->num_sms = r.num_sms;
+    // at least one slot of each kind
+    if (s->cfg.slots < 2) s->cfg.slots = 2;
+    s->n_large = std::min(std::max(1, s->cfg.large_slots), s->cfg.slots - 1);
+    int prio_least = 0, prio_greatest = 0;
+    cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest);
+    const int prio_mid = prio_greatest < prio_least ? prio_greatest + 1 : prio_greatest;
     s->slots.resize(size_t(s->cfg.slots));
-    for (auto& sl : s->slots) {
-        cudaError_t e = cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking);
+    for (size_t i = 0; i < s->slots.size(); ++i) {
+        auto& sl = s->slots[i];
+        const int prio = int(i) < s->n_large ? prio_least : std::min(prio_mid, prio_least);
+        cudaError_t e = cudaStreamCreateWithPriority(&sl.stream, cudaStreamNonBlocking, prio);
         if (e == cudaSuccess) e = cudaMalloc(&sl.ws.d_status, 64);
         if (e == cudaSuccess) e = cudaHostAlloc(reinterpret_cast<void**>(&sl.host), gb::kHostBytes, cudaHostAllocDefault);
         if (e != cudaSuccess) {
@@ -278,6 +394,18 @@ int gb300_server_create(const gb300_server_config* cfg, gb300_server** out) {
         }
         cudaMemset(sl.ws.d_status, 0, 64);
         sl.ws.stream = sl.stream;
+    }
+    s->lanes.resize(gb::kBatchLanes);
+    for (auto& ln : s->lanes) {
+        cudaError_t e = cudaStreamCreateWithPriority(&ln.stream, cudaStreamNonBlocking, prio_greatest);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ln.done, cudaEventDisableTiming);
+        if (e == cudaSuccess) ln.lane = gb::grouped_lane_create(ln.stream, &err);
+        if (e != cudaSuccess || !ln.lane) {
+            gb::set_error(GB300_ERR_CUDA, "gb300_server_create: batch lane set-up failed " + err);
+            s->worker = std::thread();
+            gb300_server_destroy(reinterpret_cast<gb300_server*>(s));
+            return GB300_ERR_CUDA;
+        }
     }
     s->worker = std::thread([s] { s->loop(); });
     *out = reinterpret_cast<gb300_server*>(s);
@@ -314,7 +442,15 @@ int gb300_server_submit(gb300_server* srv, const gb300_serve_request* q, uint64_
     r->sreq.target_error = q->target_error;
     r->sreq.slices = 0;
     r->large = std::max(q->m, q->n) >= s->cfg.large_threshold && q->accuracy != GB300_METHOD_NATIVE;
-    if (g.m > 0 && g.n > 0) gb::device_product_slot_needs(g, r->sreq, r->need);
+    // small requests of any class run in FP64 grouped launches, unless a split request asks for a
+    // bound below FP64's k * 2^-53
+    const int64_t mx = std::max(q->m, std::max(q->n, q->k));
+    const bool fp64_meets = !(q->accuracy == GB300_METHOD_SPLIT || q->accuracy == GB300_METHOD_SPLIT_CRT) ||
+                            q->target_error <= 0.0 || q->target_error >= double(std::max<int64_t>(q->k, 1)) * 0x1p-53;
+    r->cls = (s->cfg.batch_threshold > 0 && mx <= s->cfg.batch_threshold && fp64_meets)
+                 ? 0
+                 : (std::max(q->m, q->n) >= s->cfg.large_threshold ? 2 : 1);
+    if (g.m > 0 && g.n > 0 && r->cls != 0) gb::device_product_slot_needs(g, r->sreq, r->need);
     r->footprint = 0;
     for (int s_ = 0; s_ < gb::kSlotCount; ++s_) r->footprint += r->need[s_];
     if (cudaEventCreateWithFlags(&r->done, cudaEventDisableTiming) != cudaSuccess) {
@@ -400,22 +536,22 @@ int gb300_server_get_stats(gb300_server* srv, gb300_server_stats* out) {
     out->rejected = s->rejected;
     out->failed = s->failed;
     out->queued = int64_t(s->queue.size());
-    std::vector<double> l = s->latencies;
+    const std::vector<double>& l = s->latencies;
     if (!l.empty()) {
-        std::sort(l.begin(), l.end());
-        auto pct = [&](double p) {
-            const double pos = p * double(l.size() - 1);
-            const size_t lo = size_t(pos);
-            const size_t hi = std::min(lo + 1, l.size() - 1);
-            return l[lo] + (l[hi] - l[lo]) * (pos - double(lo));
-        };
-        out->p50_ms = pct(0.50);
-        out->p99_ms = pct(0.99);
-        out->max_ms = l.back();
+        out->p50_ms = gb::percentile(l, 0.50);
+        out->p99_ms = gb::percentile(l, 0.99);
+        out->max_ms = *std::max_element(l.begin(), l.end());
         double sum = 0;
         for (double v : l) sum += v;
         out->mean_ms = sum / double(l.size());
     }
+    for (int c = 0; c < 3; ++c) {
+        out->class_completed[c] = int64_t(s->class_lat[c].size());
+        out->class_p50_ms[c] = gb::percentile(s->class_lat[c], 0.50);
+        out->class_p99_ms[c] = gb::percentile(s->class_lat[c], 0.99);
+    }
+    out->grouped_launches = s->grouped_launches;
+    out->grouped_mean_batch = s->grouped_launches ? double(s->grouped_requests) / double(s->grouped_launches) : 0.0;
     if (s->any) {
         const double wall = gb::ms_between(s->t_first, gb::Clock::now()) * 1e-3;
         out->wall_s = wall;
@@ -432,6 +568,8 @@ void gb300_server_reset_stats(gb300_server* srv) {
     if (!s) return;
     std::lock_guard<std::mutex> lock(s->mu);
     s->latencies.clear();
+    for (auto& v : s->class_lat) v.clear();
+    s->grouped_launches = s->grouped_requests = 0;
     s->submitted = s->completed = s->rejected = s->failed = 0;
     s->useful_flops = 0;
     s->any = false;
@@ -447,6 +585,11 @@ void gb300_server_destroy(gb300_server* srv) {
         s->cv_work.notify_all();
     }
     if (s->worker.joinable()) s->worker.join();
+    for (auto& ln : s->lanes) {
+        gb::grouped_lane_destroy(ln.lane);
+        if (ln.done) cudaEventDestroy(ln.done);
+        if (ln.stream) cudaStreamDestroy(ln.stream);
+    }
     for (auto& sl : s->slots) {
         if (sl.stream) cudaStreamSynchronize(sl.stream);
         sl.ws.release();

@@ -1,8 +1,10 @@
 """Continuous-batching server on a GB300: every result of a mixed stream (sizes from 8 to 4096,
 the three accuracy classes) is bit-identical when the request runs alone and when it runs in the
-mix with others in flight; results meet their classes' error bounds against the compensated
-oracle; admission honours the memory budget (rejection of requests that can never fit, a peak
-below the budget); latency statistics are reported."""
+mix with others in flight; small requests complete through grouped launches that coalesce many
+of them; results meet their classes' error bounds against the compensated oracle; admission
+honours the memory budget (rejection of requests that can never fit, a peak below the budget);
+large requests never hold more than their share of the slots; latency statistics are reported
+overall and per size class."""
 import numpy as np
 import pytest
 
@@ -37,6 +39,7 @@ def run_alone(srv, torch, reqs):
     for r in reqs:
         n = r["n"]
         dC = torch.zeros(n * n, dtype=torch.float64, device="cuda")
+        torch.cuda.synchronize()  # operands and C are ready when a request is submitted
         t = srv.submit(101, 111, 111, n, n, n, 1.0, r["dA"], n, r["dB"], n, 0.0, dC, n, accuracy=r["cls"])
         res = srv.wait(t)
         assert res.status == 0
@@ -45,11 +48,11 @@ def run_alone(srv, torch, reqs):
 
 
 def run_mix(srv, torch, reqs):
-    dCs, tickets = [], []
-    for r in reqs:
+    dCs = [torch.zeros(r["n"] * r["n"], dtype=torch.float64, device="cuda") for r in reqs]
+    torch.cuda.synchronize()  # operands and C are ready when a request is submitted
+    tickets = []
+    for r, dC in zip(reqs, dCs):
         n = r["n"]
-        dC = torch.zeros(n * n, dtype=torch.float64, device="cuda")
-        dCs.append(dC)
         tickets.append(srv.submit(101, 111, 111, n, n, n, 1.0, r["dA"], n, r["dB"], n, 0.0, dC, n, accuracy=r["cls"]))
     results = [srv.wait(t) for t in tickets]
     assert all(res.status == 0 for res in results)
@@ -77,6 +80,18 @@ def test_results_are_identical_alone_and_in_the_mix(torch):
         assert st.completed == 2 * len(reqs) and st.failed == 0 and st.rejected == 0
         assert 0 < st.p50_ms <= st.p99_ms <= st.max_ms
         assert st.peak_bytes <= st.budget_bytes
+        # small requests (every dimension <= 256) ran in grouped launches: one per request when
+        # alone, several per launch in the mix
+        small = sum(1 for r in reqs if r["n"] <= 256)
+        assert st.class_completed[0] == 2 * small
+        assert st.class_completed[1] + st.class_completed[2] == 2 * (len(reqs) - small)
+        assert small < st.grouped_launches < 2 * small
+        for c in range(3):
+            if st.class_completed[c]:
+                assert 0 < st.class_p50_ms[c] <= st.class_p99_ms[c] <= st.max_ms
+        for r, res in zip(reqs, results):
+            if r["n"] <= 256:
+                assert res.method_used == G.METHOD_NATIVE and res.error_bound == r["n"] * 2.0 ** -53
     finally:
         srv.close()
 
@@ -107,5 +122,58 @@ def test_invalid_requests_are_refused(torch):
         with pytest.raises(G.Gb300Error) as ei:
             srv.submit(101, 111, 111, 8, 8, 8, 1.0, d, 4, d, 8, 0.0, d, 8)  # lda too small
         assert ei.value.status == G.ERR_INVALID_ARG
+    finally:
+        srv.close()
+
+
+def test_small_requests_coalesce_into_grouped_launches(torch):
+    """Many small requests submitted together go out in a few grouped launches, each result equal
+    to the oracle's restatement of Blaze's kernel within Blaze's relaxed equality."""
+    from helpers import blaze_equal
+    srv = G.Server(slots=4, batch_max=512)
+    try:
+        rng = np.random.default_rng(3)
+        reqs = []
+        for i in range(600):
+            m, n, k = (int(v) for v in rng.integers(4, 200, 3))
+            A = O.uniform(m * k, 7000 + 2 * i)
+            B = O.uniform(k * n, 7001 + 2 * i)
+            reqs.append((m, n, k, A, B, torch.from_numpy(A).cuda(), torch.from_numpy(B).cuda(),
+                         torch.zeros(m * n, dtype=torch.float64, device="cuda")))
+        torch.cuda.synchronize()  # operands and C are ready when a request is submitted
+        tickets = [srv.submit(101, 111, 111, m, n, k, 1.0, dA, k, dB, n, 0.0, dC, n, accuracy=CLASSES[i % 3])
+                   for i, (m, n, k, A, B, dA, dB, dC) in enumerate(reqs)]
+        for t in tickets:
+            assert srv.wait(t).status == 0
+        st = srv.stats()
+        assert st.class_completed[0] == 600
+        assert st.grouped_launches < 600 and st.grouped_mean_batch > 1.0
+        for (m, n, k, A, B, dA, dB, dC) in reqs:
+            R = np.zeros(m * n)
+            O.gemm(O.ROW_MAJOR, O.NO_TRANS, O.NO_TRANS, m, n, k, 1.0, A, k, B, n, 0.0, R, n, kernel="default")
+            assert blaze_equal(R, dC.cpu().numpy(), 1e-8).all(), (m, n, k)
+    finally:
+        srv.close()
+
+
+def test_large_requests_leave_slots_for_the_others(torch):
+    """With one large slot, several large products queued ahead of medium ones do not hold the
+    other slots: the medium requests finish before the last large one."""
+    srv = G.Server(slots=4, large_slots=1, large_threshold=2048)
+    try:
+        big, mid = 4096, 600
+        dA = torch.rand(big * big, dtype=torch.float64, device="cuda")
+        Cs = [torch.zeros(big * big, dtype=torch.float64, device="cuda") for _ in range(3)]
+        cm = [torch.zeros(mid * mid, dtype=torch.float64, device="cuda") for _ in range(6)]
+        torch.cuda.synchronize()
+        tl = [srv.submit(101, 111, 111, big, big, big, 1.0, dA, big, dA, big, 0.0, C, big, accuracy="native")
+              for C in Cs]
+        tm = [srv.submit(101, 111, 111, mid, mid, mid, 1.0, dA, mid, dA, mid, 0.0, C, mid, accuracy="split")
+              for C in cm]
+        lm = [srv.wait(t).latency_ms for t in tm]
+        ll = [srv.wait(t).latency_ms for t in tl]
+        assert max(lm) < max(ll), (lm, ll)
+        st = srv.stats()
+        assert st.class_completed[2] == 3 and st.class_completed[1] == 6
     finally:
         srv.close()
