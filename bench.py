@@ -58,8 +58,9 @@ def parse():
                                                  "(4096,4096,64), column-major A), trsm (dtrsm at each "
                                                  "--sweep-sizes, left / right x lower / upper x N / T, and ztrsm)")
     ap.add_argument("--sweep-sizes", default="4096,8192,16384")
-    ap.add_argument("--serve-requests", type=int, default=240)
-    ap.add_argument("--serve-rates", default="40,160", help="Poisson arrival rates (requests/s) to sweep")
+    ap.add_argument("--serve-requests", type=int, default=0,
+                    help="requests per rate (0: three seconds of arrivals, at least 120, at most 1200)")
+    ap.add_argument("--serve-rates", default="20,40,80,160,320,640", help="Poisson arrival rates (requests/s) to sweep")
     return ap.parse_args()
 
 
@@ -531,6 +532,9 @@ def next_leg(G, torch, args):
         out["sgemm_" + meth] = {"n": n6, "ms": round(t * 1e3, 3), "tflops": round(2.0 * n6 ** 3 / t / 1e12, 2),
                                 "method_used": int(o.method_used), "moduli": int(o.slices_used),
                                 "bound": o.error_bound, "normwise_error": err}
+    fp32_peak = G.measure_fp32_peak()
+    out["sgemm_native"]["fp32_peak_tflops"] = round(fp32_peak, 3)
+    out["sgemm_native"]["frac_of_fp32_peak"] = round(out["sgemm_native"]["tflops"] / fp32_peak, 4)
     del fA, fB, fC, ref
     # triangular solves: dtrsm (left, lower) with 8192 x 8192 right-hand sides (m^2 n flops) and
     # ztrsm 4096 (4 m^2 n); the triangle has off-diagonal entries u / n and diagonal 1 + u / 2 (well
@@ -596,7 +600,9 @@ def next_leg(G, torch, args):
 def serving_leg(G, torch, args, dev):
     """Poisson stream of square FP64 requests: 70 % n log-uniform in [8,128], 25 % in [512,2048],
     5 % in [4096,8192], accuracy class drawn uniformly from {native FP64, split <= k*2^-53, BF16},
-    operands resident; admission by a 150 GiB budget.  Reports p50/p99 latency and TFLOP/s per rate."""
+    operands resident; admission by a 150 GiB budget.  The arrival rate is swept up to saturation;
+    per rate: p50/p99 latency overall, per size class (small requests coalesced into grouped
+    launches, medium, large) and per accuracy class, and the aggregate TFLOP/s."""
     import numpy as np
     import threading
 
@@ -608,10 +614,11 @@ def serving_leg(G, torch, args, dev):
     out = {"workload": "Poisson stream, square FP64 n: 70% logU[8,128], 25% logU[512,2048], 5% logU[4096,8192]; "
                        "class uniform over {native, split<=k*2^-53, bf16}; operands resident; budget 150 GiB",
            "rates": []}
-    srv = G.Server(budget_bytes=150 << 30, slots=8, reserve_sms=16, large_threshold=2048)
+    srv = G.Server(budget_bytes=150 << 30, slots=8, reserve_sms=16, large_threshold=2048, batch_threshold=256,
+                   large_slots=2)
     try:
         for rate in [float(x) for x in args.serve_rates.split(",") if x]:
-            nreq = args.serve_requests
+            nreq = args.serve_requests or int(min(1200, max(120, 3 * rate)))
             u = rs.random_sample(nreq)
             n = np.where(u < 0.70, np.exp(rs.uniform(np.log(8), np.log(128), nreq)),
                          np.where(u < 0.95, np.exp(rs.uniform(np.log(512), np.log(2048), nreq)),
@@ -620,6 +627,7 @@ def serving_leg(G, torch, args, dev):
             cls = rs.randint(0, 3, nreq)
             gaps = rs.exponential(1.0 / rate, nreq)
             Cs = [torch.empty(int(x) * int(x), dtype=torch.float64, device=f"cuda:{dev}") for x in n]
+            torch.cuda.synchronize()  # the operand pools are filled before the first submission
             tickets = [None] * nreq
             srv.reset_stats()
             t0 = time.perf_counter()
@@ -644,15 +652,29 @@ def serving_leg(G, torch, args, dev):
                 lat[classes[int(cls[i])]].append(res.latency_ms)
             st = srv.stats()
             flops = float(np.sum(2.0 * n.astype(np.float64) ** 3))
+            sizes = ("small (grouped)", "medium", "large")
             entry = {"rate_per_s": rate, "requests": nreq, "completed": int(st.completed),
                      "rejected": int(st.rejected), "p50_ms": round(st.p50_ms, 3), "p99_ms": round(st.p99_ms, 3),
                      "max_ms": round(st.max_ms, 3), "tflops": round(st.tflops, 3), "wall_s": round(st.wall_s, 3),
                      "useful_tflop": round(flops / 1e12, 3), "peak_gib": round(st.peak_bytes / 2 ** 30, 2),
-                     "p50_by_class_ms": {c: round(float(np.median(v)), 3) for c, v in lat.items() if v}}
+                     "by_size_class": {sizes[c]: {"completed": int(st.class_completed[c]),
+                                                  "p50_ms": round(st.class_p50_ms[c], 3),
+                                                  "p99_ms": round(st.class_p99_ms[c], 3)} for c in range(3)},
+                     "by_accuracy_class": {c: {"p50_ms": round(float(np.median(v)), 3),
+                                               "p99_ms": round(float(np.percentile(v, 99)), 3)}
+                                           for c, v in lat.items() if v},
+                     "grouped_launches": int(st.grouped_launches),
+                     "requests_per_grouped_launch": round(st.grouped_mean_batch, 2)}
             out["rates"].append(entry)
             del Cs
     finally:
         srv.close()
+    if out["rates"]:
+        best = max(out["rates"], key=lambda e: e["tflops"])
+        # throughput stops growing with the arrival rate once the GPU is busy all the time; beyond
+        # that the queue (and the p99) grows instead
+        out["saturation"] = {"rate_per_s": best["rate_per_s"], "tflops": best["tflops"],
+                             "p99_ms": best["p99_ms"]}
     return out
 
 
@@ -752,6 +774,9 @@ def ours(args, dist: Dist):
         batched = batched_leg(G, torch, args, dev)
         if native:
             batched["fp64"]["frac_of_fp64_peak"] = round(batched["fp64"]["grouped_tflops"] / native["fp64_peak_tflops"], 4)
+        fp32_peak = G.measure_fp32_peak()
+        batched["fp32"]["fp32_peak_tflops"] = round(fp32_peak, 3)
+        batched["fp32"]["frac_of_fp32_peak"] = round(batched["fp32"]["grouped_tflops"] / fp32_peak, 4)
 
     serving = None
     if not args.no_serving:

@@ -55,7 +55,8 @@ class GemmProblem(ct.Structure):
 
 class ServerConfig(ct.Structure):
     _fields_ = [("memory_budget_bytes", ct.c_int64), ("slots", ct.c_int), ("reserve_sms", ct.c_int),
-                ("aging_ms", ct.c_double), ("large_threshold", ct.c_int64)]
+                ("aging_ms", ct.c_double), ("large_threshold", ct.c_int64), ("batch_threshold", ct.c_int64),
+                ("batch_max", ct.c_int), ("large_slots", ct.c_int)]
 
 
 class ServeRequest(ct.Structure):
@@ -81,7 +82,10 @@ class ServerStats(ct.Structure):
                 ("failed", ct.c_int64), ("queued", ct.c_int64),
                 ("p50_ms", ct.c_double), ("p99_ms", ct.c_double), ("mean_ms", ct.c_double), ("max_ms", ct.c_double),
                 ("wall_s", ct.c_double), ("tflops", ct.c_double),
-                ("bytes_in_use", ct.c_int64), ("peak_bytes", ct.c_int64), ("budget_bytes", ct.c_int64)]
+                ("bytes_in_use", ct.c_int64), ("peak_bytes", ct.c_int64), ("budget_bytes", ct.c_int64),
+                ("class_completed", ct.c_int64 * 3), ("class_p50_ms", ct.c_double * 3),
+                ("class_p99_ms", ct.c_double * 3), ("grouped_launches", ct.c_int64),
+                ("grouped_mean_batch", ct.c_double)]
 
 
 class Gb300Error(RuntimeError):
@@ -172,6 +176,8 @@ def lib() -> ct.CDLL:
     L.gb300_pool_bytes.restype = I64
     L.gb300_measure_fp64_peak.argtypes = [ct.POINTER(ct.c_double)]
     L.gb300_measure_fp64_peak.restype = ct.c_int
+    L.gb300_measure_fp32_peak.argtypes = [ct.POINTER(ct.c_double)]
+    L.gb300_measure_fp32_peak.restype = ct.c_int
     L.gb300_synchronize.restype = ct.c_int
     L.gb300_dgemm_native_noalloc.argtypes = [ct.c_int, ct.c_int, ct.c_int, I64, I64, I64, D, VP, I64, VP, I64, D,
                                              VP, I64, VP]
@@ -484,7 +490,8 @@ class Server:
     """Continuous-batching request server (gb300_server_*); operands are device-resident."""
 
     def __init__(self, budget_bytes: int | None = None, slots: int | None = None, reserve_sms: int | None = None,
-                 aging_ms: float | None = None, large_threshold: int | None = None):
+                 aging_ms: float | None = None, large_threshold: int | None = None, batch_threshold: int | None = None,
+                 batch_max: int | None = None, large_slots: int | None = None):
         cfg = ServerConfig()
         lib().gb300_server_config_init(ct.byref(cfg))
         if budget_bytes is not None:
@@ -497,6 +504,12 @@ class Server:
             cfg.aging_ms = aging_ms
         if large_threshold is not None:
             cfg.large_threshold = large_threshold
+        if batch_threshold is not None:
+            cfg.batch_threshold = batch_threshold
+        if batch_max is not None:
+            cfg.batch_max = batch_max
+        if large_slots is not None:
+            cfg.large_slots = large_slots
         self.handle = ct.c_void_p()
         check(lib().gb300_server_create(ct.byref(cfg), ct.byref(self.handle)))
 
@@ -550,6 +563,12 @@ def device_info() -> tuple[int, int, int]:
 def measure_fp64_peak() -> float:
     v = ct.c_double(0.0)
     check(lib().gb300_measure_fp64_peak(ct.byref(v)))
+    return v.value
+
+
+def measure_fp32_peak() -> float:
+    v = ct.c_double(0.0)
+    check(lib().gb300_measure_fp32_peak(ct.byref(v)))
     return v.value
 
 

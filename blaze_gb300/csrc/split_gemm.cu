@@ -943,6 +943,7 @@ struct TcParams {
     int64_t mpad, npad;      // padded rows of the A / B planes
     int32_t* levels;         // [nseg][nlevels][mpad][npad] int32 (float modes: fp32 bits)
     int max_levels;          // level dimension of `levels`
+    int band = 8;            // m-tiles per band of the unit order (2..32 measured alike at 8192^3)
     const SplitInfo* info;
     int* status;
     uint64_t limit_ns;
@@ -987,7 +988,7 @@ __device__ __forceinline__ void unit_coords(const TcParams& p, int u, int& tm, i
     u -= L * per_level;
     seg = u % p.nseg;
     const int t = u / p.nseg;
-    const int band = 8;
+    const int band = p.band;
     const int per_band = band * p.n_tiles;
     const int b = t / per_band, r = t % per_band;
     const int rows_in_band = min(band, p.m_tiles - b * band);

@@ -95,6 +95,8 @@ int gb300_device_info(int* num_sms, int64_t* free_bytes, int64_t* total_bytes);
 /* Measure the device's sustained FP64 FMA rate (TFLOP/s) with independent DFMA chains on every
  * SM.  The automatic method choice uses it; benchmarks report it as the FP64 roofline. */
 int gb300_measure_fp64_peak(double* tflops);
+/* The same with FFMA chains: the sustained FP32 rate (TFLOP/s), the roofline of the FP32 kernels. */
+int gb300_measure_fp32_peak(double* tflops);
 
 /* Make `ordinal` the library's device.  Call before the first product of the process (each
  * process of a multi-GPU job owns one device). */
@@ -164,7 +166,14 @@ int gb300_grouped_shape_for(int elem_bytes, int64_t m, int64_t n, int64_t k, int
 /* ---- serving: continuous batching of product requests ---------------------------------------
  * A server admits requests as stream slots and device memory free up (FIFO with backfill under a
  * device-memory budget), runs admitted requests concurrently on their own streams and workspaces,
- * and records per-request latency.  Operands are resident: A, B and C are device (or managed)
+ * and records per-request latency.  Small requests (every dimension at most batch_threshold) are
+ * coalesced: at each scheduling step the queued ones go out together as one persistent grouped
+ * launch in FP64 (which meets the bound of every accuracy class), on one of two batch lanes;
+ * large requests (max(m, n) >= large_threshold) run only on large_slots slots of their own, whose
+ * streams have the lowest priority (the other slots' streams a higher one, the batch lanes' the
+ * highest), so that neither slots nor SMs stay held by them while smaller requests wait.  The server's streams do not wait for work on other
+ * streams: A, B and C must hold their values when a request is submitted (synchronize any copy or
+ * fill still queued for them first).  Operands are resident: A, B and C are device (or managed)
  * memory owned by the caller (operands that TMA cannot address in place — odd leading dimension or
  * a base not 16-byte aligned — are realigned into the request's workspace).  Blaze has no server;
  * each request is the same product as gb300_dgemm_ex with the accuracy class as its method. */
@@ -174,6 +183,9 @@ typedef struct gb300_server_config {
     int reserve_sms;              /* SMs kept out of large tensor-core products for small requests (16) */
     double aging_ms;              /* a queue head older than this stops backfilling (50 ms) */
     int64_t large_threshold;      /* max(m, n) from which a request counts as large (2048) */
+    int64_t batch_threshold;      /* requests with max(m, n, k) <= this run in grouped launches (256; 0: never) */
+    int batch_max;                /* requests per grouped launch at most (2048) */
+    int large_slots;              /* slots kept for large requests, at the lowest stream priority (2) */
 } gb300_server_config;
 
 typedef struct gb300_serve_request {
@@ -206,6 +218,11 @@ typedef struct gb300_server_stats {
     double wall_s;                            /* since the first submission (or the last reset) */
     double tflops;                            /* 2*m*n*k of completed requests / wall_s */
     int64_t bytes_in_use, peak_bytes, budget_bytes;
+    /* per size class: 0 small (grouped launches), 1 medium, 2 large (max(m, n) >= large_threshold) */
+    int64_t class_completed[3];
+    double class_p50_ms[3], class_p99_ms[3];
+    int64_t grouped_launches;                 /* grouped launches issued */
+    double grouped_mean_batch;                /* requests per grouped launch */
 } gb300_server_stats;
 
 typedef struct gb300_server gb300_server;
