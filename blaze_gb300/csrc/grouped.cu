@@ -563,6 +563,7 @@ struct GroupedLane {
     void* d_buf = nullptr;
     size_t d_bytes = 0;
     int* d_counter = nullptr;
+    std::vector<void*> retired;  // outgrown staging buffers: cudaFreeHost would wait for the device
     std::vector<DevProblem> hp;
     std::vector<DevTile> ht;
 };
@@ -581,9 +582,10 @@ GroupedLane* grouped_lane_create(cudaStream_t stream, std::string* err) {
 
 void grouped_lane_destroy(GroupedLane* l) {
     if (!l) return;
+    if (l->d_buf) cudaFreeAsync(l->d_buf, l->stream);
     if (l->stream) cudaStreamSynchronize(l->stream);
     if (l->h_buf) cudaFreeHost(l->h_buf);
-    if (l->d_buf) cudaFree(l->d_buf);
+    for (void* h : l->retired) cudaFreeHost(h);
     if (l->d_counter) cudaFree(l->d_counter);
     delete l;
 }
@@ -599,7 +601,7 @@ int grouped_lane_launch(GroupedLane* l, const gb300_gemm_problem* probs, int64_t
     const size_t off_t = (pb + 255) / 256 * 256, need = off_t + tb;
     auto grow = [](size_t n) { return (n + (size_t(1) << 20) - 1) & ~((size_t(1) << 20) - 1); };
     if (l->h_bytes < need) {
-        if (l->h_buf) cudaFreeHost(l->h_buf);
+        if (l->h_buf) l->retired.push_back(l->h_buf);
         l->h_buf = nullptr;
         l->h_bytes = 0;
         if (cudaHostAlloc(&l->h_buf, grow(need), cudaHostAllocDefault) != cudaSuccess) {
@@ -610,10 +612,11 @@ int grouped_lane_launch(GroupedLane* l, const gb300_gemm_problem* probs, int64_t
         l->h_bytes = grow(need);
     }
     if (l->d_bytes < need) {
-        if (l->d_buf) cudaFree(l->d_buf);
+        // stream-ordered on the lane's stream: growing the table never waits for other streams
+        if (l->d_buf) cudaFreeAsync(l->d_buf, l->stream);
         l->d_buf = nullptr;
         l->d_bytes = 0;
-        if (cudaMalloc(&l->d_buf, grow(need)) != cudaSuccess) {
+        if (cudaMallocAsync(&l->d_buf, grow(need), l->stream) != cudaSuccess) {
             cudaGetLastError();
             if (err) *err = "grouped lane: table allocation failed";
             return GB300_ERR_NO_MEMORY;

@@ -4,8 +4,8 @@
 // reached from DMatDMatMultExpr.h:2021-2037 and its three storage-order siblings), i.e. the work
 // that Blaze's own large kernel `mmm` (blaze/math/dense/MMM.h:105-600) does on the CPU.
 //
-// Design (one CTA per 128x128 tile of C — 256x64 when C has at most 64 columns —, 256 threads,
-// 8x8 outputs per thread):
+// Design (one CTA per 128x128 tile of C — 256x64 when C has at most 64 columns, 64x256 when it has
+// at most 64 rows —, 256 threads, 8x8 outputs per thread):
 //   * operand tiles are staged in shared memory by TMA (cp.async.bulk.tensor) as 128-byte
 //     swizzled boxes, a 4-deep mbarrier pipeline (one "full" barrier with transaction bytes and
 //     one "empty" barrier released by the eight warps per stage);
@@ -278,9 +278,10 @@ cudaError_t launch_variant(const CUtensorMap& a, const CUtensorMap& b, const Nat
     return cudaGetLastError();
 }
 
-// Columns of the CTA tile: 64 (256 x 64 tiles) for products with at most 64 columns, where a
-// 128-column tile would compute half of its outputs on padding, else 128.
-int native_tile_n(int64_t n) { return n <= 64 ? 64 : 128; }
+// Columns of the CTA tile: 64 (256 x 64 tiles) for products with at most 64 columns and 256
+// (64 x 256 tiles) for products with at most 64 rows, where a 128 x 128 tile would compute half of
+// its outputs on padding; else 128.
+int native_tile_n(int64_t m, int64_t n) { return n <= 64 ? 64 : (m <= 64 ? 256 : 128); }
 
 template <typename T, int BN_>
 cudaError_t native_gemm_tiled(const Gemm& g, int splits, T* workspace, const LaunchCtl& ctl, cudaStream_t s,
@@ -341,7 +342,7 @@ cudaError_t native_gemm_tiled(const Gemm& g, int splits, T* workspace, const Lau
 
 int native_choose_splits(int64_t m, int64_t n, int64_t k, int elem_bytes, int num_sms) {
     const int64_t bk = PANEL_BYTES / elem_bytes;
-    const int64_t bn = native_tile_n(n), bm = 16384 / bn;
+    const int64_t bn = native_tile_n(m, n), bm = 16384 / bn;
     const int64_t tiles = ((m + bm - 1) / bm) * ((n + bn - 1) / bn);
     if (2 * tiles > num_sms || k < 32 * bk) return 1;
     // as many k-splits as still fit one wave of CTAs (one CTA per SM), each at least 16 panels deep
@@ -363,8 +364,11 @@ cudaError_t native_gemm(const Gemm& g, int splits, T* workspace, const LaunchCtl
         count_launches(1);
         return cudaGetLastError();
     }
-    return native_tile_n(g.n) == 64 ? native_gemm_tiled<T, 64>(g, splits, workspace, ctl, s, err)
-                                    : native_gemm_tiled<T, 128>(g, splits, workspace, ctl, s, err);
+    switch (native_tile_n(g.m, g.n)) {
+        case 64: return native_gemm_tiled<T, 64>(g, splits, workspace, ctl, s, err);
+        case 256: return native_gemm_tiled<T, 256>(g, splits, workspace, ctl, s, err);
+        default: return native_gemm_tiled<T, 128>(g, splits, workspace, ctl, s, err);
+    }
 }
 
 template cudaError_t native_gemm<double>(const Gemm&, int, double*, const LaunchCtl&, cudaStream_t, std::string*);

@@ -155,8 +155,12 @@ void* Workspace::get(int s, size_t n, std::string* err) {
     if (n == 0) n = 256;
     if (bytes[s] >= n) return ptr[s];
     if (ptr[s]) {
-        cudaStreamSynchronize(stream);
-        cudaFree(ptr[s]);
+        if (stream_ordered) {
+            cudaFreeAsync(ptr[s], stream);
+        } else {
+            cudaStreamSynchronize(stream);
+            cudaFree(ptr[s]);
+        }
         g_pool_bytes.fetch_sub(int64_t(bytes[s]));
         ptr[s] = nullptr;
         bytes[s] = 0;
@@ -164,7 +168,7 @@ void* Workspace::get(int s, size_t n, std::string* err) {
     // round up to 2 MiB so that slowly growing sizes do not reallocate every call
     const size_t rounded = (n + (size_t(2) << 20) - 1) & ~((size_t(2) << 20) - 1);
     void* p = nullptr;
-    cudaError_t e = cudaMalloc(&p, rounded);
+    cudaError_t e = stream_ordered ? cudaMallocAsync(&p, rounded, stream) : cudaMalloc(&p, rounded);
     if (e != cudaSuccess) {
         cudaGetLastError();
         if (err) *err = "device allocation of " + std::to_string(rounded) + " bytes failed: " + cudaGetErrorString(e);
@@ -183,10 +187,11 @@ size_t Workspace::total() const {
 }
 
 void Workspace::release() {
-    if (stream) cudaStreamSynchronize(stream);
+    if (stream && !stream_ordered) cudaStreamSynchronize(stream);
     for (int s = 0; s < kSlotCount; ++s) {
         if (ptr[s]) {
-            cudaFree(ptr[s]);
+            if (stream_ordered) cudaFreeAsync(ptr[s], stream);
+            else cudaFree(ptr[s]);
             g_pool_bytes.fetch_sub(int64_t(bytes[s]));
         }
         ptr[s] = nullptr;

@@ -34,6 +34,10 @@ enum Slot : int {
 // repeated calls of similar size allocate nothing.
 struct Workspace {
     cudaStream_t stream = nullptr;
+    // Stream-ordered buffers (cudaMallocAsync / cudaFreeAsync on `stream`): growing or releasing
+    // them never waits for other streams.  For contexts whose buffers only `stream` uses (the
+    // server's slots); cudaFree would wait for the whole device.
+    bool stream_ordered = false;
     int* d_status = nullptr;       // device status word written by kernels (DeviceStatus)
     void* ptr[kSlotCount] = {};
     size_t bytes[kSlotCount] = {};

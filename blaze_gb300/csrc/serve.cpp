@@ -19,6 +19,11 @@
 //     requests launched after it (without priorities their p99 was that product's time).  A large
 //     request waiting for a large slot does not stop others from passing it, and while a large
 //     tensor-core product runs a share of the SMs is also kept out of its persistent grid.
+//   * Large native requests run as a chain of k-panels (native_panels), which keeps each CTA of
+//     theirs short.
+//   * The scheduler thread never waits for the device: slot workspaces are stream-ordered (growing
+//     one frees and allocates on the slot's stream) and lanes keep outgrown staging buffers, since
+//     cudaFree / cudaFreeHost would wait for every stream, large products included.
 //   * Small requests (every dimension at most `batch_threshold`) do not take a slot: at each
 //     scheduling step the queued ones are coalesced into one persistent grouped launch (grouped.cu,
 //     FP64) on one of two batch lanes, up to `batch_max` per launch, while the previous launch may
@@ -97,6 +102,28 @@ struct BatchLane {
 constexpr int kBatchLanes = 2;
 
 enum Admit : int { kAdmitted = 0, kNoSlot, kNoMemory, kLargeLimit };
+
+// Large native FP64 requests run as a chain of k-panels, C = alpha A_p B_p + C (the first panel
+// with the request's beta), so that a CTA of the native kernel holds its SM for one panel's k loop
+// (about 4 ms at n = 8192 instead of 33 ms): priority decides which stream's blocks take an SM as
+// it frees up, and running CTAs are never preempted.  The panel order is fixed, so the result is
+// the same alone and in the mix; the bound stays k 2^-53.
+constexpr int64_t kServeNativePanel = 1024;
+
+int native_panels(const Gemm& g, const SplitRequest& sreq, const LaunchCtl& ctl, cudaStream_t st, Workspace& ws,
+                  SplitResult* res, std::string* err) {
+    int rc = GB300_OK;
+    for (int64_t k0 = 0; k0 < g.k && rc == GB300_OK; k0 += kServeNativePanel) {
+        Gemm q = g;
+        q.k = std::min(kServeNativePanel, g.k - k0);
+        q.A = static_cast<const double*>(g.A) + (g.ta ? k0 * g.lda : k0);
+        q.B = static_cast<const double*>(g.B) + (g.tb ? k0 : k0 * g.ldb);
+        if (k0 > 0) q.beta = 1.0;
+        rc = device_product(q, sreq, ctl, st, ws, res, err);
+    }
+    res->error_bound = double(g.k) * 0x1p-53;
+    return rc;
+}
 
 double percentile(std::vector<double> l, double p) {
     if (l.empty()) return 0.0;
@@ -248,7 +275,9 @@ class Server {
         std::string err;
         cudaMemsetAsync(sl.ws.d_status, 0, sizeof(int), sl.stream);
         SplitResult res;
-        const int st = device_product(r->g, sreq, ctl, sl.stream, sl.ws, &res, &err);
+        const bool panels = r->cls == 2 && sreq.method == GB300_METHOD_NATIVE && r->g.k > kServeNativePanel;
+        const int st = panels ? native_panels(r->g, sreq, ctl, sl.stream, sl.ws, &res, &err)
+                              : device_product(r->g, sreq, ctl, sl.stream, sl.ws, &res, &err);
         r->res.status = st;
         r->res.method_used = res.method_used;
         r->res.slices = res.slices;
@@ -394,6 +423,8 @@ int gb300_server_create(const gb300_server_config* cfg, gb300_server** out) {
         }
         cudaMemset(sl.ws.d_status, 0, 64);
         sl.ws.stream = sl.stream;
+        // a slot's buffers are only used on its stream: growing them must not wait for the device
+        sl.ws.stream_ordered = true;
     }
     s->lanes.resize(gb::kBatchLanes);
     for (auto& ln : s->lanes) {

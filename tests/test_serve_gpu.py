@@ -171,8 +171,17 @@ def test_large_requests_leave_slots_for_the_others(torch):
         tm = [srv.submit(101, 111, 111, mid, mid, mid, 1.0, dA, mid, dA, mid, 0.0, C, mid, accuracy="split")
               for C in cm]
         lm = [srv.wait(t).latency_ms for t in tm]
-        ll = [srv.wait(t).latency_ms for t in tl]
+        rl = [srv.wait(t) for t in tl]
+        ll = [r.latency_ms for r in rl]
         assert max(lm) < max(ll), (lm, ll)
+        # a large native request runs as a chain of k-panels: still FP64-accurate
+        assert rl[0].method_used == G.METHOD_NATIVE and rl[0].error_bound == big * 2.0 ** -53
+        hA = dA.cpu().numpy()
+        rows = np.arange(0, big, big // 8)
+        P = O.product_rows_dot2(O.ROW_MAJOR, O.NO_TRANS, O.NO_TRANS, big, big, big, hA, big, hA, big, rows=rows)
+        got = Cs[0].view(big, big)[torch.from_numpy(rows).cuda()].cpu().numpy()
+        err = float(np.linalg.norm(got - P) * np.sqrt(big / len(rows)) / np.linalg.norm(hA) ** 2)
+        assert err <= big * 2.0 ** -53, err
         st = srv.stats()
         assert st.class_completed[2] == 3 and st.class_completed[1] == 6
     finally:
