@@ -85,10 +85,7 @@ __device__ __forceinline__ void warp_tile(const DevProblem& p, int tm, int tn, i
     for (int r = 0; r < R; ++r)
 #pragma unroll
         for (int c = 0; c < C; ++c) acc[r][c] = T(0);
-    // unrolled so that the loads of the next k steps issue before this step's multiply-adds retire
-    // (the accumulation order of every output stays k = 0, 1, 2, ...)
-#pragma unroll 2
-    for (int kk = 0; kk < p.k; ++kk) {
+    auto step = [&]() {
         T a0[R], b0[C];
 #pragma unroll
         for (int r = 0; r < R; ++r) a0[r] = (rmask >> r) & 1u ? __ldg(pa + r * a8) : T(0);
@@ -100,6 +97,17 @@ __device__ __forceinline__ void warp_tile(const DevProblem& p, int tm, int tn, i
             for (int c = 0; c < C; ++c) acc[r][c] = fma(a0[r], b0[c], acc[r][c]);
         pa += a_ks;
         pb += b_ks;
+    };
+    // FP64: unrolled so that the loads of the next k step issue before this step's multiply-adds
+    // retire; FP32: not unrolled, which keeps every shape within the 128 registers that let an SM
+    // hold two blocks (latency is hidden by warps instead).  The accumulation order of every output
+    // stays k = 0, 1, 2, ... either way.
+    if constexpr (sizeof(T) == 8) {
+#pragma unroll 2
+        for (int kk = 0; kk < p.k; ++kk) step();
+    } else {
+#pragma unroll 1
+        for (int kk = 0; kk < p.k; ++kk) step();
     }
     T* Cp = static_cast<T*>(p.C);
     const T alpha = T(p.alpha), beta = T(p.beta);
@@ -124,7 +132,7 @@ template <typename T>
 __host__ __device__ constexpr int max_shape() { return sizeof(T) == 8 ? 3 : 5; }
 
 template <typename T>
-__global__ void __launch_bounds__(256, sizeof(T) == 8 ? 2 : 1)
+__global__ void __launch_bounds__(256, 2)
 grouped_kernel(const DevProblem* __restrict__ probs, const DevTile* __restrict__ tiles, int ntiles,
                int* __restrict__ counter) {
     const int lane = threadIdx.x & 31;

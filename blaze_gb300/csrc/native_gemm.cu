@@ -165,17 +165,42 @@ native_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constan
         }
         const uint8_t* As = tilesA + s * Tile::A_BYTES;
         const uint8_t* Bs = tilesB + s * Tile::B_BYTES;
+        if constexpr (sizeof(T) == 4 && !TRANS_A) {
+            // float, k-contiguous A: four consecutive k of a row are one 16-byte swizzle chunk, so
+            // one 128-bit load serves four k steps (a quarter of A's shared-memory wavefronts, the
+            // FFMA form's limit); every output still accumulates k in order
+#pragma unroll 2
+            for (int k4 = 0; k4 < BK; k4 += 4) {
+                float4 a4[8];
+#pragma unroll
+                for (int r = 0; r < 8; ++r) a4[r] = *reinterpret_cast<const float4*>(As + a_off<T, TRANS_A>(ty + TY * r, k4));
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    T b[8];
+#pragma unroll
+                    for (int c = 0; c < 8; ++c)
+                        b[c] = *reinterpret_cast<const T*>(Bs + b_off<T, TRANS_B>(k4 + j, tx + TX * c));
+#pragma unroll
+                    for (int r = 0; r < 8; ++r) {
+                        const T a = j == 0 ? a4[r].x : j == 1 ? a4[r].y : j == 2 ? a4[r].z : a4[r].w;
+#pragma unroll
+                        for (int c = 0; c < 8; ++c) acc[r][c] = fma(a, b[c], acc[r][c]);
+                    }
+                }
+            }
+        } else {
 #pragma unroll 4
-        for (int kk = 0; kk < BK; ++kk) {
-            T a[8], b[8];
+            for (int kk = 0; kk < BK; ++kk) {
+                T a[8], b[8];
 #pragma unroll
-            for (int r = 0; r < 8; ++r) a[r] = *reinterpret_cast<const T*>(As + a_off<T, TRANS_A>(ty + TY * r, kk));
+                for (int r = 0; r < 8; ++r) a[r] = *reinterpret_cast<const T*>(As + a_off<T, TRANS_A>(ty + TY * r, kk));
 #pragma unroll
-            for (int c = 0; c < 8; ++c) b[c] = *reinterpret_cast<const T*>(Bs + b_off<T, TRANS_B>(kk, tx + TX * c));
+                for (int c = 0; c < 8; ++c) b[c] = *reinterpret_cast<const T*>(Bs + b_off<T, TRANS_B>(kk, tx + TX * c));
 #pragma unroll
-            for (int r = 0; r < 8; ++r)
+                for (int r = 0; r < 8; ++r)
 #pragma unroll
-                for (int c = 0; c < 8; ++c) acc[r][c] = fma(a[r], b[c], acc[r][c]);
+                    for (int c = 0; c < 8; ++c) acc[r][c] = fma(a[r], b[c], acc[r][c]);
+            }
         }
         __syncwarp();
         if (lane == 0) mbar_arrive(smem_u32(&bars->empty[s]));
