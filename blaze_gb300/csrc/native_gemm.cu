@@ -104,6 +104,13 @@ native_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constan
     const int tid = threadIdx.x;
     const int lane = tid & 31;
     const int tx = tid % TX, ty = tid / TX;
+    // Float with an n-contiguous B: thread tx owns the 8 consecutive columns 8 tx .. 8 tx + 7, read as
+    // two 16-byte swizzle chunks; B's 32-column boxes lie 4 KB apart, on the same banks, so threads
+    // in odd boxes read their upper chunk first (their columns rotated by four) and one load
+    // instruction spreads over all eight chunk positions.  Otherwise columns tx + TX c.
+    constexpr bool VB = sizeof(T) == 4 && !TRANS_B;
+    const int vbh = VB ? ((tx * 8 / E) & 1) : 0;
+    auto col_of = [&](int c) { return VB ? tx * 8 + ((c + 4 * vbh) & 7) : tx + TX * c; };
     const int64_t m0 = int64_t(blockIdx.y) * BM;
     const int64_t n0 = int64_t(blockIdx.x) * BN;
     const int64_t kbeg = int64_t(blockIdx.z) * p.k_per_split;
@@ -177,9 +184,17 @@ native_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constan
 #pragma unroll
                 for (int j = 0; j < 4; ++j) {
                     T b[8];
+                    if constexpr (VB) {
+                        const float4 lo = *reinterpret_cast<const float4*>(Bs + b_off<T, TRANS_B>(k4 + j, tx * 8 + 4 * vbh));
+                        const float4 hi =
+                            *reinterpret_cast<const float4*>(Bs + b_off<T, TRANS_B>(k4 + j, tx * 8 + 4 * (1 - vbh)));
+                        b[0] = lo.x; b[1] = lo.y; b[2] = lo.z; b[3] = lo.w;
+                        b[4] = hi.x; b[5] = hi.y; b[6] = hi.z; b[7] = hi.w;
+                    } else {
 #pragma unroll
-                    for (int c = 0; c < 8; ++c)
-                        b[c] = *reinterpret_cast<const T*>(Bs + b_off<T, TRANS_B>(k4 + j, tx + TX * c));
+                        for (int c = 0; c < 8; ++c)
+                            b[c] = *reinterpret_cast<const T*>(Bs + b_off<T, TRANS_B>(k4 + j, col_of(c)));
+                    }
 #pragma unroll
                     for (int r = 0; r < 8; ++r) {
                         const T a = j == 0 ? a4[r].x : j == 1 ? a4[r].y : j == 2 ? a4[r].z : a4[r].w;
@@ -195,7 +210,7 @@ native_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constan
 #pragma unroll
                 for (int r = 0; r < 8; ++r) a[r] = *reinterpret_cast<const T*>(As + a_off<T, TRANS_A>(ty + TY * r, kk));
 #pragma unroll
-                for (int c = 0; c < 8; ++c) b[c] = *reinterpret_cast<const T*>(Bs + b_off<T, TRANS_B>(kk, tx + TX * c));
+                for (int c = 0; c < 8; ++c) b[c] = *reinterpret_cast<const T*>(Bs + b_off<T, TRANS_B>(kk, col_of(c)));
 #pragma unroll
                 for (int r = 0; r < 8; ++r)
 #pragma unroll
@@ -234,7 +249,7 @@ native_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constan
             if (i >= p.m) continue;
 #pragma unroll
             for (int c = 0; c < 8; ++c) {
-                const int64_t j = n0 + tx + TX * c;
+                const int64_t j = n0 + col_of(c);
                 if (j < p.n) w[i * p.n + j] = acc[r][c];
             }
         }
@@ -247,7 +262,7 @@ native_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constan
         T* crow = p.C + i * p.ldc;
 #pragma unroll
         for (int c = 0; c < 8; ++c) {
-            const int64_t j = n0 + tx + TX * c;
+            const int64_t j = n0 + col_of(c);
             if (j >= p.n) continue;
             const T v = p.alpha * acc[r][c];
             crow[j] = (p.beta == T(0)) ? v : fma(p.beta, crow[j], v);

@@ -30,7 +30,7 @@
  *      reduced by a horizontal sum and added as C(i,j) += sum*alpha (MMM.h:190-330); when K is
  *      not a multiple of SIMDSIZE the trailing columns are added term by term as
  *      C(i,j) += A2(i,k)*B2(k,j)*alpha (MMM.h:470-575).  SIMDSIZE is 8 doubles / 16 floats
- *      (the AVX-512 width Blaze selects on the survey host).
+ *      (the AVX-512 width Blaze selects on an AVX-512 host).
  *      Column-major C (MMM.h:605-1080) is evaluated through the identity
  *      C^T = op(B)^T op(A)^T, which maps a column-major call onto the row-major kernel.
  *      Rows of C are split across OpenMP threads (Blaze's SMP layer splits C into thread
