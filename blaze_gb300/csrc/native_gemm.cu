@@ -111,6 +111,10 @@ native_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constan
     constexpr bool VB = sizeof(T) == 4 && !TRANS_B;
     const int vbh = VB ? ((tx * 8 / E) & 1) : 0;
     auto col_of = [&](int c) { return VB ? tx * 8 + ((c + 4 * vbh) & 7) : tx + TX * c; };
+    // The same for the rows of a float m-contiguous A: thread ty owns rows 8 ty .. 8 ty + 7.
+    constexpr bool VA = sizeof(T) == 4 && TRANS_A;
+    const int vah = VA ? ((ty * 8 / E) & 1) : 0;
+    auto row_of = [&](int r) { return VA ? ty * 8 + ((r + 4 * vah) & 7) : ty + TY * r; };
     const int64_t m0 = int64_t(blockIdx.y) * BM;
     const int64_t n0 = int64_t(blockIdx.x) * BN;
     const int64_t kbeg = int64_t(blockIdx.z) * p.k_per_split;
@@ -180,11 +184,21 @@ native_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constan
             for (int k4 = 0; k4 < BK; k4 += 4) {
                 float4 a4[8];
 #pragma unroll
-                for (int r = 0; r < 8; ++r) a4[r] = *reinterpret_cast<const float4*>(As + a_off<T, TRANS_A>(ty + TY * r, k4));
+                for (int r = 0; r < 8; ++r) a4[r] = *reinterpret_cast<const float4*>(As + a_off<T, TRANS_A>(row_of(r), k4));
+                // k-contiguous B: its four k steps of a column are one chunk as well
+                float4 b4[TRANS_B ? 8 : 1];
+                if constexpr (TRANS_B) {
+#pragma unroll
+                    for (int c = 0; c < 8; ++c) b4[c] = *reinterpret_cast<const float4*>(Bs + b_off<T, TRANS_B>(k4, col_of(c)));
+                }
 #pragma unroll
                 for (int j = 0; j < 4; ++j) {
                     T b[8];
-                    if constexpr (VB) {
+                    if constexpr (TRANS_B) {
+#pragma unroll
+                        for (int c = 0; c < 8; ++c)
+                            b[c] = j == 0 ? b4[c].x : j == 1 ? b4[c].y : j == 2 ? b4[c].z : b4[c].w;
+                    } else if constexpr (VB) {
                         const float4 lo = *reinterpret_cast<const float4*>(Bs + b_off<T, TRANS_B>(k4 + j, tx * 8 + 4 * vbh));
                         const float4 hi =
                             *reinterpret_cast<const float4*>(Bs + b_off<T, TRANS_B>(k4 + j, tx * 8 + 4 * (1 - vbh)));
@@ -203,14 +217,51 @@ native_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constan
                     }
                 }
             }
+        } else if constexpr (VA && TRANS_B) {
+            // float, m-contiguous A and k-contiguous B: A's rows as two chunks per k step, B's
+            // four k steps of a column as one chunk
+#pragma unroll 2
+            for (int k4 = 0; k4 < BK; k4 += 4) {
+                float4 b4[8];
+#pragma unroll
+                for (int c = 0; c < 8; ++c) b4[c] = *reinterpret_cast<const float4*>(Bs + b_off<T, TRANS_B>(k4, col_of(c)));
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const float4 lo = *reinterpret_cast<const float4*>(As + a_off<T, TRANS_A>(ty * 8 + 4 * vah, k4 + j));
+                    const float4 hi =
+                        *reinterpret_cast<const float4*>(As + a_off<T, TRANS_A>(ty * 8 + 4 * (1 - vah), k4 + j));
+                    const T a[8] = {lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w};
+#pragma unroll
+                    for (int r = 0; r < 8; ++r)
+#pragma unroll
+                        for (int c = 0; c < 8; ++c) {
+                            const T b = j == 0 ? b4[c].x : j == 1 ? b4[c].y : j == 2 ? b4[c].z : b4[c].w;
+                            acc[r][c] = fma(a[r], b, acc[r][c]);
+                        }
+                }
+            }
         } else {
 #pragma unroll 4
             for (int kk = 0; kk < BK; ++kk) {
                 T a[8], b[8];
+                if constexpr (VA) {
+                    const float4 lo = *reinterpret_cast<const float4*>(As + a_off<T, TRANS_A>(ty * 8 + 4 * vah, kk));
+                    const float4 hi = *reinterpret_cast<const float4*>(As + a_off<T, TRANS_A>(ty * 8 + 4 * (1 - vah), kk));
+                    a[0] = lo.x; a[1] = lo.y; a[2] = lo.z; a[3] = lo.w;
+                    a[4] = hi.x; a[5] = hi.y; a[6] = hi.z; a[7] = hi.w;
+                } else {
 #pragma unroll
-                for (int r = 0; r < 8; ++r) a[r] = *reinterpret_cast<const T*>(As + a_off<T, TRANS_A>(ty + TY * r, kk));
+                    for (int r = 0; r < 8; ++r) a[r] = *reinterpret_cast<const T*>(As + a_off<T, TRANS_A>(row_of(r), kk));
+                }
+                if constexpr (VB) {
+                    const float4 lo = *reinterpret_cast<const float4*>(Bs + b_off<T, TRANS_B>(kk, tx * 8 + 4 * vbh));
+                    const float4 hi = *reinterpret_cast<const float4*>(Bs + b_off<T, TRANS_B>(kk, tx * 8 + 4 * (1 - vbh)));
+                    b[0] = lo.x; b[1] = lo.y; b[2] = lo.z; b[3] = lo.w;
+                    b[4] = hi.x; b[5] = hi.y; b[6] = hi.z; b[7] = hi.w;
+                } else {
 #pragma unroll
-                for (int c = 0; c < 8; ++c) b[c] = *reinterpret_cast<const T*>(Bs + b_off<T, TRANS_B>(kk, col_of(c)));
+                    for (int c = 0; c < 8; ++c) b[c] = *reinterpret_cast<const T*>(Bs + b_off<T, TRANS_B>(kk, col_of(c)));
+                }
 #pragma unroll
                 for (int r = 0; r < 8; ++r)
 #pragma unroll
@@ -245,7 +296,7 @@ native_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constan
         T* w = p.ws + int64_t(blockIdx.z) * p.m * p.n;
 #pragma unroll
         for (int r = 0; r < 8; ++r) {
-            const int64_t i = m0 + ty + TY * r;
+            const int64_t i = m0 + row_of(r);
             if (i >= p.m) continue;
 #pragma unroll
             for (int c = 0; c < 8; ++c) {
@@ -257,7 +308,7 @@ native_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constan
     }
 #pragma unroll
     for (int r = 0; r < 8; ++r) {
-        const int64_t i = m0 + ty + TY * r;
+        const int64_t i = m0 + row_of(r);
         if (i >= p.m) continue;
         T* crow = p.C + i * p.ldc;
 #pragma unroll

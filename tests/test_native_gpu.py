@@ -184,3 +184,25 @@ def test_sgemm_larger_normwise():
     ref = A.astype(np.float64).reshape(m, k) @ B.astype(np.float64).reshape(n, k).T
     err = normwise(C.reshape(m, n), ref, float(np.linalg.norm(A.astype(np.float64))), float(np.linalg.norm(B.astype(np.float64))))
     assert err <= k * 2.0 ** -24
+
+
+@pytest.mark.parametrize("ta", [O.NO_TRANS, O.TRANS])
+@pytest.mark.parametrize("tb", [O.NO_TRANS, O.TRANS])
+@pytest.mark.parametrize("m,n,k", [(300, 520, 700), (520, 60, 900), (50, 530, 800)])
+def test_sgemm_native_every_layout_and_tile(ta, tb, m, n, k):
+    """The float kernel reads its shared-memory tiles with 128-bit loads in a layout-dependent
+    way (k, row or column chunks); every transposition and the three tile shapes (C with at most
+    64 columns, at most 64 rows, or neither) against an FP64 product."""
+    A = O.uniform(m * k, 81, dtype=np.float32)
+    B = O.uniform(k * n, 82, dtype=np.float32)
+    C = np.full(m * n, np.nan, dtype=np.float32)
+    lda = m if ta == O.TRANS else k
+    ldb = k if tb == O.TRANS else n
+    G.sgemm_ex(O.ROW_MAJOR, ta, tb, m, n, k, 1.0, A, lda, B, ldb, 0.0, C, n, G.opts(method="native"))
+    opA = A.astype(np.float64).reshape(k, m).T if ta == O.TRANS else A.astype(np.float64).reshape(m, k)
+    opB = B.astype(np.float64).reshape(n, k).T if tb == O.TRANS else B.astype(np.float64).reshape(k, n)
+    ref = opA @ opB
+    err = normwise(C.reshape(m, n), ref, float(np.linalg.norm(A.astype(np.float64))),
+                   float(np.linalg.norm(B.astype(np.float64))))
+    assert err <= k * 2.0 ** -24, err
+    assert np.max(np.abs(C.reshape(m, n) - ref)) <= k * 2.0 ** -22
