@@ -125,6 +125,90 @@ __device__ __forceinline__ void warp_tile(const DevProblem& p, int tm, int tn, i
     }
 }
 
+// FP32 warp tiles stage their operands through shared memory, KC k-steps at a time: a warp reads
+// its A rows and B columns with coalesced loads (the contiguous dimension across lanes) into its own
+// region, then every k step reads them back with broadcast loads.  Read straight from global
+// memory, each k step of an A row costs one cache line per row of the tile for one multiply-add per
+// row and column, which bounds small FP32 tiles by L1 line traffic rather than by the FFMA pipe.
+// Every output still sums k in order, so the results are those of the unstaged tile.
+constexpr int KC = 32;                                   // k-steps per staged block
+constexpr int kStageA = 64 * (KC + 1);                   // up to 64 rows, padded pitch
+constexpr int kStageB = KC * (32 + 1);                   // up to 32 columns, padded pitch
+constexpr int kStageWarp = kStageA + kStageB;            // floats per warp
+constexpr int kStageBytes = 8 * kStageWarp * int(sizeof(float));  // per 256-thread block
+
+template <int R, int C>
+__device__ __forceinline__ void warp_tile_staged(const DevProblem& p, int tm, int tn, int lane, float* __restrict__ sw) {
+    constexpr int TR = 8 * R, TC = 4 * C, PA = KC + 1, PB = TC + 1;
+    float* As = sw;            // As[r * PA + kk]
+    float* Bs = sw + kStageA;  // Bs[kk * PB + c]
+    const int ly = lane >> 2, lx = lane & 3;
+    const int i0 = tm * TR, j0 = tn * TC;
+    const float* A = static_cast<const float*>(p.A);
+    const float* B = static_cast<const float*>(p.B);
+    float acc[R][C];
+#pragma unroll
+    for (int r = 0; r < R; ++r)
+#pragma unroll
+        for (int c = 0; c < C; ++c) acc[r][c] = 0.f;
+    for (int k0 = 0; k0 < p.k; k0 += KC) {
+        const int kc = min(KC, p.k - k0);
+        // A(i, kk) = A[i lda + kk] (k contiguous) or A[kk lda + i] (m contiguous); zeros outside
+        if (!p.ta) {
+            for (int r = 0; r < TR; ++r) {
+                const int i = i0 + r;
+                As[r * PA + lane] = (i < p.m && lane < kc) ? __ldg(A + int64_t(i) * p.lda + k0 + lane) : 0.f;
+            }
+        } else {
+            for (int idx = lane; idx < TR * KC; idx += 32) {
+                const int r = idx % TR, kk = idx / TR, i = i0 + r;
+                As[r * PA + kk] = (i < p.m && kk < kc) ? __ldg(A + int64_t(k0 + kk) * p.lda + i) : 0.f;
+            }
+        }
+        // B(kk, j) = B[kk ldb + j] (n contiguous) or B[j ldb + kk] (k contiguous)
+        if (!p.tb) {
+            for (int idx = lane; idx < KC * TC; idx += 32) {
+                const int c = idx % TC, kk = idx / TC, j = j0 + c;
+                Bs[kk * PB + c] = (j < p.n && kk < kc) ? __ldg(B + int64_t(k0 + kk) * p.ldb + j) : 0.f;
+            }
+        } else {
+            for (int c = 0; c < TC; ++c) {
+                const int j = j0 + c;
+                Bs[lane * PB + c] = (j < p.n && lane < kc) ? __ldg(B + int64_t(j) * p.ldb + k0 + lane) : 0.f;
+            }
+        }
+        __syncwarp();
+#pragma unroll 2
+        for (int kk = 0; kk < kc; ++kk) {
+            float a0[R], b0[C];
+#pragma unroll
+            for (int r = 0; r < R; ++r) a0[r] = As[(ly + 8 * r) * PA + kk];
+#pragma unroll
+            for (int c = 0; c < C; ++c) b0[c] = Bs[kk * PB + lx + 4 * c];
+#pragma unroll
+            for (int r = 0; r < R; ++r)
+#pragma unroll
+                for (int c = 0; c < C; ++c) acc[r][c] = fmaf(a0[r], b0[c], acc[r][c]);
+        }
+        __syncwarp();
+    }
+    float* Cp = static_cast<float*>(p.C);
+    const float alpha = float(p.alpha), beta = float(p.beta);
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const int i = i0 + ly + 8 * r;
+        if (i >= p.m) continue;
+        float* crow = Cp + int64_t(i) * p.ldc;
+#pragma unroll
+        for (int c = 0; c < C; ++c) {
+            const int j = j0 + lx + 4 * c;
+            if (j >= p.n) continue;
+            const float v = alpha * acc[r][c];
+            crow[j] = (beta == 0.f) ? v : fmaf(beta, crow[j], v);
+        }
+    }
+}
+
 // Shapes available per element type: FP64 stops at 16x32 / 32x16 warp tiles (16 accumulators per
 // lane): on the FP64 pipe a larger tile only adds padding, and the smaller register footprint lets an
 // SM hold twice the warps.
@@ -136,6 +220,10 @@ __global__ void __launch_bounds__(256, 2)
 grouped_kernel(const DevProblem* __restrict__ probs, const DevTile* __restrict__ tiles, int ntiles,
                int* __restrict__ counter) {
     const int lane = threadIdx.x & 31;
+    // FP32: the warp's staging region (dynamic shared memory of kStageBytes per block)
+    extern __shared__ float stage_smem[];
+    float* sw = stage_smem + (threadIdx.x >> 5) * kStageWarp;
+    (void)sw;
     int t = 0;
     if (lane == 0) t = atomicAdd(counter, 1);
     t = __shfl_sync(0xffffffffu, t, 0);
@@ -147,17 +235,28 @@ grouped_kernel(const DevProblem* __restrict__ probs, const DevTile* __restrict__
         if (lane == 0) next = atomicAdd(counter, 1);
         const DevTile tl = tiles[t];
         const DevProblem p = probs[tl.prob];
-        switch (p.shape) {
-            case 0: warp_tile<T, 1, 2>(p, tl.tm, tl.tn, lane); break;
-            case 1: warp_tile<T, 2, 4>(p, tl.tm, tl.tn, lane); break;
-            case 2: warp_tile<T, 4, 4>(p, tl.tm, tl.tn, lane); break;
-            case 3: warp_tile<T, 2, 8>(p, tl.tm, tl.tn, lane); break;
-            case 4:
-                if constexpr (max_shape<T>() >= 4) warp_tile<T, 4, 8>(p, tl.tm, tl.tn, lane);
-                break;
-            default:
-                if constexpr (max_shape<T>() >= 5) warp_tile<T, 8, 8>(p, tl.tm, tl.tn, lane);
-                break;
+        if constexpr (sizeof(T) == 4) {
+            switch (p.shape) {
+                case 0: warp_tile_staged<1, 2>(p, tl.tm, tl.tn, lane, sw); break;
+                case 1: warp_tile_staged<2, 4>(p, tl.tm, tl.tn, lane, sw); break;
+                case 2: warp_tile_staged<4, 4>(p, tl.tm, tl.tn, lane, sw); break;
+                case 3: warp_tile_staged<2, 8>(p, tl.tm, tl.tn, lane, sw); break;
+                case 4: warp_tile_staged<4, 8>(p, tl.tm, tl.tn, lane, sw); break;
+                default: warp_tile_staged<8, 8>(p, tl.tm, tl.tn, lane, sw); break;
+            }
+        } else {
+            switch (p.shape) {
+                case 0: warp_tile<T, 1, 2>(p, tl.tm, tl.tn, lane); break;
+                case 1: warp_tile<T, 2, 4>(p, tl.tm, tl.tn, lane); break;
+                case 2: warp_tile<T, 4, 4>(p, tl.tm, tl.tn, lane); break;
+                case 3: warp_tile<T, 2, 8>(p, tl.tm, tl.tn, lane); break;
+                case 4:
+                    if constexpr (max_shape<T>() >= 4) warp_tile<T, 4, 8>(p, tl.tm, tl.tn, lane);
+                    break;
+                default:
+                    if constexpr (max_shape<T>() >= 5) warp_tile<T, 8, 8>(p, tl.tm, tl.tn, lane);
+                    break;
+            }
         }
         t = __shfl_sync(0xffffffffu, next, 0);
     }
@@ -341,11 +440,25 @@ int build_tables(const gb300_gemm_problem* probs, int64_t count, int force_shape
     return GB300_OK;
 }
 
+// Dynamic shared memory of a block: the FP32 staging regions (none for FP64).
+template <typename T>
+int grouped_smem() {
+    if constexpr (sizeof(T) == 4) {
+        static const bool set = [] {
+            return cudaFuncSetAttribute(grouped_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        kStageBytes) == cudaSuccess;
+        }();
+        (void)set;
+        return kStageBytes;
+    }
+    return 0;
+}
+
 // Persistent grid for `ntiles` warp tiles: every SM's resident blocks, or fewer for a short list.
 template <typename T>
 int grouped_grid(int64_t ntiles, int num_sms) {
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, grouped_kernel<T>, 256, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, grouped_kernel<T>, 256, grouped_smem<T>());
     per_sm = std::max(per_sm, 1);
     return int(std::max<int64_t>(1, std::min<int64_t>(int64_t(num_sms) * per_sm, (ntiles + 7) / 8)));
 }
@@ -391,7 +504,8 @@ int plan_create(const gb300_gemm_problem* probs, int64_t count, int force_shape,
     if (e == cudaSuccess) {
         cudaMemsetAsync(p->d_counter, 0, sizeof(int), p->cap_stream);
         if (p->ntiles > 0)
-            grouped_kernel<T><<<p->grid, 256, 0, p->cap_stream>>>(p->d_probs, p->d_tiles, int(p->ntiles), p->d_counter);
+            grouped_kernel<T><<<p->grid, 256, grouped_smem<T>(), p->cap_stream>>>(p->d_probs, p->d_tiles,
+                                                                              int(p->ntiles), p->d_counter);
         e = cudaStreamEndCapture(p->cap_stream, &p->graph);
     }
     if (e == cudaSuccess) e = cudaGraphInstantiate(&p->exec, p->graph, 0);
