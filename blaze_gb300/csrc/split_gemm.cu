@@ -21,11 +21,11 @@
 // so x = sum_s d_s 2^(1-8s) + r_S 2^(1-8S).  Columns of op(B) likewise with exponents f_j.
 // With planes numbered a = s-1, the pair (a, b) has weight 2^(-14-8(a+b)); all pairs with
 // a + b = L form "level" L, L = 0..S-1 (the triangle s + t <= S + 1 of Ozaki's scheme).
-//   Exactness: one TMEM drain group accumulates at most 4 x 64 = 256 products of digits,
-//   |sum| <= 256 * 128^2 = 2^22, which FP32 holds exactly whatever the order of the additions.
-//   The epilogue reads the FP32 integer v, forms bits(v + 1.5*2^23) = 0x4B400000 + v (exact for
-//   |v| <= 2^22) and adds the bit patterns in int32 (wrapping), removing the bias at the end.
-//   A level's int32 sum over a k-segment is bounded by n_L * (Kseg/256) * 2^22 < 2^31.
+//   Exactness: one TMEM drain group accumulates at most 8 x 64 = 512 products of digits,
+//   |sum| <= 512 * 128^2 = 2^23, which FP32 holds exactly whatever the order of the additions
+//   (every partial sum is an integer below 2^24).  The epilogue converts the FP32 integer v with
+//   cvt.rni (exact) and adds it in int32.  A level's int32 sum over a k-segment is bounded by
+//   n_L * Kseg * 2^14 < 2^31.
 //   Error bound (elementwise, scaled units): |dC_ij| <= (S+1) K 2^(-8S); normwise
 //   ||dC||_F / (||A||_F ||B||_F) <= (S+1) K 2^(-8S) ||2^e||_2 ||2^f||_2 / (||A||_F ||B||_F)
 //   plus (S+3) 2^-53 for the FP64 recombination.  The slice count is the smallest S whose bound
@@ -75,7 +75,7 @@ constexpr int STAGES = 6;
 constexpr int A_BYTES = TM * TK * 2;    // 16 KB
 constexpr int B_BYTES = TNH * TK * 2;   // 16 KB (this CTA's half of the B tile)
 constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
-constexpr int GROUP_ITEMS = 4;          // exact mode: 4 items (256 products) per TMEM drain
+constexpr int GROUP_ITEMS = 8;          // exact mode: 8 items (512 products) per TMEM drain
 constexpr int EPI_WARPS = 8;
 constexpr int THREADS = 64 + EPI_WARPS * 32;
 constexpr int MAX_SLICES = 10;
@@ -88,8 +88,9 @@ enum Mode : int { kExact = 0, kBf16 = 1, kBf16x3 = 2, kCrt = 3 };
 
 // ---- moduli of the CRT (Ozaki scheme II) form ----------------------------------------------------
 // Pairwise coprime moduli <= 257, largest first: a residue in the symmetric range has |r| <= 128,
-// so it is exactly a BF16 and a 256-product group of residue products stays within 2^22 (the same
-// exactness argument as for the digits).  Prime factors: 257; 2; 3,5,17; 11,23; 251; 13,19; 241;
+// so it is exactly a BF16 and a 512-product group of residue products stays within 2^23, where
+// every integer and every partial sum is exact in the FP32 accumulator (the same exactness
+// argument as for the digits).  Prime factors: 257; 2; 3,5,17; 11,23; 251; 13,19; 241;
 // 239; 233; 229; 227; 223; 7,31; 211; 199.  Product of all 15: about 2^118.2.
 constexpr int MAX_MODULI = 15;
 __constant__ uint32_t c_mod[MAX_MODULI] = {257, 256, 255, 253, 251, 247, 241, 239, 233, 229, 227, 223, 217, 211, 199};
@@ -1171,8 +1172,7 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
                 uint32_t acc[128];
 #pragma unroll
                 for (int c = 0; c < 128; ++c) acc[c] = 0u;
-                uint32_t ngroups = 0;
-                for (int g0 = 0; g0 < items; g0 += gsize, ++grp, ++ngroups) {
+                for (int g0 = 0; g0 < items; g0 += gsize, ++grp) {
                     const int buf = grp & 1;
                     if (!mbar_wait(smem_u32(&bars->acc_full[buf]), (grp >> 1) & 1, p.status, kDevTimeoutMma,
                                    p.limit_ns)) {
@@ -1187,9 +1187,12 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
                         tmem_ld_32x32b_x16(base + uint32_t(c4 * 16), v);
                         tc_wait_ld();
                         if (emode == kExact) {
+                            // the group sum is an integer of at most 2^23 in magnitude: exact in
+                            // FP32 and exactly converted (adding 1.5 * 2^23 would be exact only
+                            // below 2^22, i.e. for groups of 256 products)
 #pragma unroll
                             for (int c = 0; c < 16; ++c)
-                                acc[c4 * 16 + c] += __float_as_uint(__uint_as_float(v[c]) + MAGIC);
+                                acc[c4 * 16 + c] += uint32_t(__float2int_rn(__uint_as_float(v[c])));
                         } else {
 #pragma unroll
                             for (int c = 0; c < 16; ++c) acc[c4 * 16 + c] = v[c];
@@ -1204,7 +1207,6 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
                 // schedule the sum is reduced modulo the level's modulus and stored as 16 bits
                 const int64_t plane_off = ((int64_t(seg) * p.max_levels + L) * p.mpad + row) * p.npad +
                                           int64_t(tn) * TN + h * 128;
-                const uint32_t bias = (emode == kExact) ? ngroups * MAGIC_BITS : 0u;
                 if (emode == kExact && mode == kCrt) {
                     // residues in [0, p) as 16-bit values; two 64-column halves per warp go out
                     // through the warp's staging tile (row = lane, 16-byte chunk j of a row at
@@ -1223,7 +1225,7 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
                             __align__(16) uint16_t rr[8];
 #pragma unroll
                             for (int e = 0; e < 8; ++e) {
-                                const int32_t t = int32_t(acc[c + e] - bias);
+                                const int32_t t = int32_t(acc[c + e]);
                                 const uint32_t mag = t < 0 ? uint32_t(-int64_t(t)) : uint32_t(t);
                                 uint32_t rsd = mod_small(mag, pm, inv);
                                 if (t < 0 && rsd) rsd = pm - rsd;
@@ -1244,10 +1246,10 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
 #pragma unroll
                     for (int c = 0; c < 128; c += 4) {
                         int4 w;
-                        w.x = int32_t(acc[c + 0] - bias);
-                        w.y = int32_t(acc[c + 1] - bias);
-                        w.z = int32_t(acc[c + 2] - bias);
-                        w.w = int32_t(acc[c + 3] - bias);
+                        w.x = int32_t(acc[c + 0]);
+                        w.y = int32_t(acc[c + 1]);
+                        w.z = int32_t(acc[c + 2]);
+                        w.w = int32_t(acc[c + 3]);
                         *reinterpret_cast<int4*>(dst + c) = w;
                     }
                 }
@@ -1682,7 +1684,7 @@ SplitGeometry split_geometry(const Gemm& g, const SplitRequest& req, int num_sms
     // device's SM count only, so a capped grid computes the same segments (and the same result)
     int64_t kseg = G.kpad;
     if (G.mode == kExact || G.mode == kCrt) {
-        // n_L * (Kseg/256) groups of at most 2^22 each must stay below 2^31 (one pair per level in
+        // n_L * Kseg products of at most 2^14 each must stay below 2^31 (one pair per level in
         // CRT mode)
         const int64_t cap = (int64_t(511) / (G.mode == kCrt ? 1 : G.max_planes)) * KSEG_UNIT;
         kseg = std::min(kseg, std::max<int64_t>(cap, KSEG_UNIT));
