@@ -153,7 +153,11 @@ struct SplitInfo {
 constexpr int kNonFinite = 0x7fff;
 
 struct RowAcc {
-    unsigned long long maxbits;  // bits of max |x| (non-negative doubles order like integers)
+    // max |x| to its high 32 bits (sign, exponent, 20 mantissa bits; non-negative doubles order
+    // like integers), bit 0 set when some value has non-zero low bits: the frexp exponent of the
+    // maximum follows whenever the high word is a normal number, and a row whose high words are
+    // all zero or subnormal is rescanned exactly
+    unsigned long long maxbits;
     double sumsq;
     int flags;                   // 1: non-finite value seen
     int pad;
@@ -209,15 +213,19 @@ __device__ __forceinline__ void tile_issue(uint32_t sbuf, const TileSrc& s, cons
 __device__ __forceinline__ float pow2f_or0(int x) { return x < -126 ? 0.f : __uint_as_float(uint32_t(x + 127) << 23); }
 
 // Row statistics over TILE_KT tiles: thread (rr = t % 32, g = t / 32) keeps, for row rr and the
-// eight k of group g in every tile, the largest |x| (as bits), a non-finite flag and the sum of
-// squares in FP32 relative to its running largest exponent (rescaled exactly by a power of two
-// when a larger exponent arrives); the block folds the eight groups of a row and issues one set
-// of atomics per row.
+// eight k of group g in every tile, the largest high word of |x|, the OR of the low words and the
+// sum of squares in FP32 relative to its running largest exponent `base`: f = |x| 2^(1023 - base)
+// is the high word times 8 (exponent and 20 mantissa bits moved into FP32 position) minus
+// (base - 127) 2^23, one integer multiply-add, valid for exponents above base - 127 (smaller
+// values add less than 2^-252 relative and are dropped; zeros and subnormals always are).  The
+// running sum is rescaled exactly by a power of two when a larger exponent arrives.  The block
+// folds the eight groups of a row and issues one set of atomics per row; an Inf/NaN shows as a
+// largest exponent of 0x7ff.
 __device__ __forceinline__ void stats_rows(const double* __restrict__ X, int64_t R, int64_t K, int64_t sr, int64_t sp,
                                            RowAcc* __restrict__ acc, int by) {
     __shared__ __align__(16) unsigned long long tile[2][32][65];
-    __shared__ unsigned long long red_mx[8][32];
-    __shared__ int red_base[8][32], red_bad[8][32];
+    __shared__ uint32_t red_mx[8][32], red_lo[8][32];
+    __shared__ int red_base[8][32];
     __shared__ float red_sq[8][32];
     const int t = threadIdx.x, rr = t & 31, g = t >> 5;
     const int64_t r0 = int64_t(by) * 32;
@@ -226,8 +234,8 @@ __device__ __forceinline__ void stats_rows(const double* __restrict__ X, int64_t
     const uint32_t s0 = smem_u32(&tile[0][0][0]);
     constexpr uint32_t BUF = 32 * 65 * 8;
     auto off = [](int r_, int p_) { return uint32_t(r_ * 65 + p_) * 8u; };
-    unsigned long long mx = 0;
-    int base = 0, bad = 0;
+    uint32_t mx = 0, lo = 0, cbias = 0;
+    int base = 127;  // f = |x| 2^(1023 - base); values with exponent field 0 never count
     float sq = 0.f;
     const TileSrc ts = tile_src(X, sr, sp, r0);
     if (tb < te) tile_issue(s0, ts, X, R, K, r0, tb, off);
@@ -239,45 +247,45 @@ __device__ __forceinline__ void stats_rows(const double* __restrict__ X, int64_t
         __syncthreads();
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
-            const unsigned long long a = tile[b][rr][8 * g + q] & 0x7fffffffffffffffull;
-            const int ea = int(a >> 52);
-            bad |= ea == 0x7ff;
-            mx = a > mx ? a : mx;
+            const unsigned long long a = tile[b][rr][8 * g + q];
+            const uint32_t hi = uint32_t(a >> 32) & 0x7fffffffu;
+            lo |= uint32_t(a);
+            mx = max(mx, hi);
+            const int ea = int(hi >> 20);
             if (ea > base) {
                 sq *= pow2f_or0(2 * (base - ea));
                 base = ea;
+                cbias = uint32_t(base - 127) << 23;
             }
-            const int fe = ea - base + 127;  // FP32 exponent of a / 2^(base - 1023)
-            const float f = (ea == 0 || fe <= 0) ? 0.f
-                                                 : __uint_as_float((uint32_t(fe) << 23) | uint32_t((a >> 29) & 0x7fffffu));
+            const float f = ea > base - 127 ? __uint_as_float(hi * 8u - cbias) : 0.f;
             sq = fmaf(f, f, sq);
         }
         __syncthreads();
     }
     red_mx[g][rr] = mx;
+    red_lo[g][rr] = lo;
     red_base[g][rr] = base;
     red_sq[g][rr] = sq;
-    red_bad[g][rr] = bad;
     __syncthreads();
     if (g == 0) {
-        int E = 0, bd = 0;
-        unsigned long long m = 0;
+        int E = 0;
+        uint32_t m = 0, l = 0;
 #pragma unroll
         for (int i = 0; i < 8; ++i) {
             E = max(E, red_base[i][rr]);
-            bd |= red_bad[i][rr];
-            m = red_mx[i][rr] > m ? red_mx[i][rr] : m;
+            m = max(m, red_mx[i][rr]);
+            l |= red_lo[i][rr];
         }
         float s = 0.f;
 #pragma unroll
         for (int i = 0; i < 8; ++i) s = fmaf(red_sq[i][rr], pow2f_or0(2 * (red_base[i][rr] - E)), s);
         const int64_t r = r0 + rr;
         if (r < R) {
-            if (bd) atomicOr(&acc[r].flags, 1);
-            if (m != 0) {
-                atomicMax(&acc[r].maxbits, m);
+            if (m >= 0x7ff00000u) atomicOr(&acc[r].flags, 1);
+            if (m != 0 || l != 0) {
+                atomicMax(&acc[r].maxbits, ((unsigned long long)m << 32) | (l != 0 ? 1ull : 0ull));
                 // sum of squares of the unscaled values: s * 2^(2 (E - 1023))
-                atomicAdd(&acc[r].sumsq, ldexp(double(s), 2 * (E - 1023)));
+                if (s > 0.f) atomicAdd(&acc[r].sumsq, ldexp(double(s), 2 * (E - 1023)));
             }
         }
     }
@@ -293,7 +301,17 @@ __device__ __forceinline__ void stats_finalize_row(const double* __restrict__ X,
         rsq[r] = 0.0;
         return;
     }
-    const double mx = __longlong_as_double(static_cast<long long>(a.maxbits));
+    unsigned long long mb = a.maxbits;
+    if (mb != 0 && (mb >> 52) == 0) {
+        // every high word zero or subnormal: the exact maximum decides the exponent
+        mb = 0;
+        for (int64_t p = 0; p < K; ++p) {
+            const unsigned long long v =
+                static_cast<unsigned long long>(__double_as_longlong(X[r * sr + p * sp])) & 0x7fffffffffffffffull;
+            mb = v > mb ? v : mb;
+        }
+    }
+    const double mx = __longlong_as_double(static_cast<long long>(mb));
     int e = 0;
     if (mx > 0.0) frexp(mx, &e);
     double q = ldexp(a.sumsq, -2 * e);

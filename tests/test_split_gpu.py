@@ -208,3 +208,49 @@ def test_crt_segmented_k_residues_are_summed_and_reduced():
     assert o.method_used == G.METHOD_SPLIT_CRT
     exact = A.astype(np.int64).reshape(m, k) @ B.astype(np.int64).reshape(k, n)
     assert np.array_equal(C.reshape(m, n), exact.astype(np.float64))
+
+
+@pytest.mark.parametrize("order,ta,tb", [(O.ROW_MAJOR, O.NO_TRANS, O.NO_TRANS), (O.COL_MAJOR, O.TRANS, O.TRANS)])
+def test_rows_of_extreme_magnitude_keep_their_own_scale(order, ta, tb):
+    """Rows of A and columns of B at the ends of the double range: zero, subnormal values whose high
+    word is zero, subnormals with a non-zero high word, 1e300, 1e-300, one large value among ones.
+    Every output entry is checked against its own row and column scale, so a wrong row exponent
+    cannot hide behind the largest entries."""
+    m, n, k = 64, 96, 300
+    rng = np.random.default_rng(5)
+    Al = rng.uniform(-1, 1, (m, k))
+    Bl = rng.uniform(-1, 1, (k, n))
+    Al[0] = 0.0
+    Al[1] = np.ldexp(np.round(Al[1] * 2 ** 14), -1074)        # low word only
+    Al[2] = np.ldexp(Al[2], -1030)                              # subnormal, high word non-zero
+    Al[3] *= 1e300
+    Al[4] *= 1e-300
+    Al[5, 17] = 1e200
+    Bl[:, 0] = np.ldexp(np.round(Bl[:, 0] * 2 ** 12), -1074)
+    Bl[:, 1] *= 1e-250
+    Bl[:, 2] *= 1e5
+    Bl[:, 3] = 0.0
+
+    def stored(L, trans):
+        X = L.T if trans == O.TRANS else L
+        return np.ascontiguousarray(X if order == O.ROW_MAJOR else X.T).ravel()
+
+    A, B = stored(Al, ta), stored(Bl, tb)
+    ra, ca = stored_dims(order, ta, m, k)
+    rb, cb = stored_dims(order, tb, k, n)
+    lda, ldb = ca, cb
+    ldc = n if order == O.ROW_MAJOR else m
+    C = np.zeros(m * n)
+    o = G.dgemm_ex(order, ta, tb, m, n, k, 1.0, A, lda, B, ldb, 0.0, C, ldc, G.opts(method="split"))
+    assert o.method_used in (G.METHOD_SPLIT, G.METHOD_SPLIT_CRT)
+    out = O.logical(order, O.NO_TRANS, m, n, C, ldc)
+    P = O.product_rows_dot2(order, ta, tb, m, n, k, A, lda, B, ldb)
+    scale = np.outer(np.abs(Al).max(axis=1), np.abs(Bl).max(axis=0)) * k
+    # the rounding of both operands to beta-bit integers bounds an entry's error by about
+    # k 2^(e_i + f_j - beta) with beta near 40 here
+    tol = np.maximum(scale * 2.0 ** -36, 4 * k * 2.0 ** -1074)
+    assert np.isfinite(out).all()
+    bad = np.abs(out - P) > tol
+    assert not bad.any(), [(int(i), int(j), out[i, j], P[i, j]) for i, j in zip(*np.nonzero(bad))][:8]
+    assert np.all(out[0] == 0.0) and np.all(out[:, 3] == 0.0)
+    assert np.count_nonzero(out[1]) > n // 2 and np.count_nonzero(out[:, 0]) > m // 2
