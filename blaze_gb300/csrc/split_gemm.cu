@@ -21,10 +21,11 @@
 // so x = sum_s d_s 2^(1-8s) + r_S 2^(1-8S).  Columns of op(B) likewise with exponents f_j.
 // With planes numbered a = s-1, the pair (a, b) has weight 2^(-14-8(a+b)); all pairs with
 // a + b = L form "level" L, L = 0..S-1 (the triangle s + t <= S + 1 of Ozaki's scheme).
-//   Exactness: one TMEM drain group accumulates at most 8 x 64 = 512 products of digits,
-//   |sum| <= 512 * 128^2 = 2^23, which FP32 holds exactly whatever the order of the additions
-//   (every partial sum is an integer below 2^24).  The epilogue converts the FP32 integer v with
-//   cvt.rni (exact) and adds it in int32.  A level's int32 sum over a k-segment is bounded by
+//   Exactness: one TMEM drain group accumulates at most 16 x 64 = 1024 products of digits,
+//   |product| <= 128^2 = 2^14, so every partial sum is an integer of magnitude at most 2^24, which
+//   FP32 holds exactly (2^24 itself only as the group's final value, when all 1024 products are
+//   largest with one sign).  The epilogue converts the FP32 integer v with cvt.rni (exact) and
+//   adds it in int32.  A level's int32 sum over a k-segment is bounded by
 //   n_L * Kseg * 2^14 < 2^31.
 //   Error bound (elementwise, scaled units): |dC_ij| <= (S+1) K 2^(-8S); normwise
 //   ||dC||_F / (||A||_F ||B||_F) <= (S+1) K 2^(-8S) ||2^e||_2 ||2^f||_2 / (||A||_F ||B||_F)
@@ -75,7 +76,7 @@ constexpr int STAGES = 6;
 constexpr int A_BYTES = TM * TK * 2;    // 16 KB
 constexpr int B_BYTES = TNH * TK * 2;   // 16 KB (this CTA's half of the B tile)
 constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
-constexpr int GROUP_ITEMS = 8;          // exact mode: 8 items (512 products) per TMEM drain
+constexpr int GROUP_ITEMS = 16;         // exact mode: 16 items (1024 products) per TMEM drain
 constexpr int EPI_WARPS = 8;
 constexpr int THREADS = 64 + EPI_WARPS * 32;
 constexpr int MAX_SLICES = 10;
@@ -88,9 +89,9 @@ enum Mode : int { kExact = 0, kBf16 = 1, kBf16x3 = 2, kCrt = 3 };
 
 // ---- moduli of the CRT (Ozaki scheme II) form ----------------------------------------------------
 // Pairwise coprime moduli <= 257, largest first: a residue in the symmetric range has |r| <= 128,
-// so it is exactly a BF16 and a 512-product group of residue products stays within 2^23, where
-// every integer and every partial sum is exact in the FP32 accumulator (the same exactness
-// argument as for the digits).  Prime factors: 257; 2; 3,5,17; 11,23; 251; 13,19; 241;
+// so it is exactly a BF16 and a 1024-product group of residue products stays within 2^24, where
+// every partial sum is an integer exact in the FP32 accumulator (the same exactness argument as
+// for the digits).  Prime factors: 257; 2; 3,5,17; 11,23; 251; 13,19; 241;
 // 239; 233; 229; 227; 223; 7,31; 211; 199.  Product of all 15: about 2^118.2.
 constexpr int MAX_MODULI = 15;
 __constant__ uint32_t c_mod[MAX_MODULI] = {257, 256, 255, 253, 251, 247, 241, 239, 233, 229, 227, 223, 217, 211, 199};
@@ -1205,7 +1206,7 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
                         tmem_ld_32x32b_x16(base + uint32_t(c4 * 16), v);
                         tc_wait_ld();
                         if (emode == kExact) {
-                            // the group sum is an integer of at most 2^23 in magnitude: exact in
+                            // the group sum is an integer of at most 2^24 in magnitude: exact in
                             // FP32 and exactly converted (adding 1.5 * 2^23 would be exact only
                             // below 2^22, i.e. for groups of 256 products)
 #pragma unroll

@@ -254,3 +254,67 @@ def test_rows_of_extreme_magnitude_keep_their_own_scale(order, ta, tb):
     assert not bad.any(), [(int(i), int(j), out[i, j], P[i, j]) for i, j in zip(*np.nonzero(bad))][:8]
     assert np.all(out[0] == 0.0) and np.all(out[:, 3] == 0.0)
     assert np.count_nonzero(out[1]) > n // 2 and np.count_nonzero(out[:, 0]) > m // 2
+
+
+MODULI = [257, 256, 255, 253, 251, 247, 241, 239, 233, 229, 227, 223, 217, 211, 199]
+
+
+def _crt_beta(qa, qb, k, nmod):
+    """The residue plan's rounding exponent for fixed moduli: the largest b whose integer products
+    fit the moduli (the planning kernel's need(b) <= have, in FP64 as there)."""
+    import math
+    have = sum(math.log2(p) for p in MODULI[:nmod])
+    sqa, sqb, hk = math.sqrt(qa * (1 + 2.0 ** -10)), math.sqrt(qb * (1 + 2.0 ** -10)), 0.5 * math.sqrt(k)
+    need = lambda b: 1.0875 + math.log2(math.ldexp(sqa, b) + hk) + math.log2(math.ldexp(sqb, b) + hk)
+    bhi = min(55, math.floor((have - 1.0875 - math.log2(sqa) - math.log2(sqb)) / 2.0))
+    return max(b for b in range(-59, bhi + 1) if need(b) <= have)
+
+
+def test_crt_drain_groups_exact_at_their_largest_sums():
+    """The worst case of the residue products' FP32 accumulation: every 257-residue of one
+    1024-long k block is 128 in both operands (the 256-residues are +-128), so each drain group
+    there sums 128 * 128 products to its largest magnitude.  Block g of k holds values
+    Y / 2^(b0 - 7 + g) with Y = 128 mod 256 * 257, so the block whose exponent equals the plan's
+    beta has exactly those residues; the plan's beta is recovered from the returned bound.  Every
+    entry is exact at that scale, so the result must be the correctly rounded exact product."""
+    from fractions import Fraction
+    m = n = 2048   # 64 pair tiles: k is not split into segments
+    k, blk, nmod = 8192, 1024, 13
+    rng = np.random.default_rng(11)
+
+    def block_values(count, b):
+        lo_t = -(-(2 ** (b - 1) - 128) // 65792)
+        hi_t = (2 ** b - 1 - 128) // 65792
+        return [65792 * int(t) + 128 for t in rng.integers(lo_t, hi_t + 1, count)]
+
+    # a first draft fixes the operand statistics; the block exponents sit at and below its beta
+    b0 = _crt_beta(k * 0.58, k * 0.58, k, nmod)
+    for _ in range(3):
+        exps = [b0 - 7 + g for g in range(k // blk)]
+        ya = [y for g, b in enumerate(exps) for y in block_values(blk, b)]
+        yb = [y for g, b in enumerate(exps) for y in block_values(blk, b)]
+        a = np.array([y / 2.0 ** exps[p // blk] for p, y in enumerate(ya)])
+        b = np.array([y / 2.0 ** exps[p // blk] for p, y in enumerate(yb)])
+        beta = _crt_beta(float(np.sum(a * a)), float(np.sum(b * b)), k, nmod)
+        if beta == b0:
+            break
+        b0 = beta
+    assert beta == b0
+    assert a.max() < 1.0 and a.min() >= 0.5 and b.max() < 1.0 and b.min() >= 0.5  # row exponents 0
+    A = np.tile(a, m)            # m x k, every row a
+    B = np.repeat(b, n)          # k x n, every column b
+    C = np.zeros(m * n)
+    o = G.dgemm_ex(O.ROW_MAJOR, O.NO_TRANS, O.NO_TRANS, m, n, k, 1.0, A, k, B, n, 0.0, C, n,
+                   G.opts(method="split_crt", slices=nmod))
+    assert o.method_used == G.METHOD_SPLIT_CRT and o.slices_used == nmod
+    # the beta that ran, from its bound 2^(-b-1)(rA + rB) + 2^(-2b-2) rA rB + 2^-52
+    rA, rB = np.sqrt(k / np.sum(a * a)), np.sqrt(k / np.sum(b * b))
+    bnd = {bb: 2.0 ** (-bb - 1) * (rA + rB) + 2.0 ** (-2 * bb - 2) * rA * rB + 2.0 ** -52 for bb in range(b0 - 8, b0 + 9)}
+    # (the device's norms come from FP32 sums; bounds of neighbouring exponents differ by 2x)
+    ran = [bb for bb, v in bnd.items() if abs(v - o.error_bound) <= 1e-3 * o.error_bound]
+    assert ran == [b0], (ran, b0, o.error_bound)
+    # exact product: sum_p Y_p Z_p 2^-(2 e_p), correctly rounded
+    top = max(exps)
+    num = sum(ya[p] * yb[p] << (2 * (top - exps[p // blk])) for p in range(k))
+    exact = float(Fraction(num, 2 ** (2 * top)))
+    assert np.all(C == exact), (float(C.min()), float(C.max()), exact)
