@@ -127,19 +127,41 @@ __device__ __forceinline__ void warp_tile(const DevProblem& p, int tm, int tn, i
 
 // FP32 warp tiles stage their operands through shared memory, KC k-steps at a time: a warp reads
 // its A rows and B columns with coalesced loads (the contiguous dimension across lanes) into its own
-// region, then every k step reads them back with broadcast loads.  Read straight from global
-// memory, each k step of an A row costs one cache line per row of the tile for one multiply-add per
-// row and column, which bounds small FP32 tiles by L1 line traffic rather than by the FFMA pipe.
-// Every output still sums k in order, so the results are those of the unstaged tile.
+// region, then every k step reads them back from there.  Read straight from global memory, each k
+// step of an A row costs one cache line per row of the tile for one multiply-add per row and
+// column, which bounds small FP32 tiles by L1 line traffic rather than by the FFMA pipe.  Lane
+// (ly, lx) owns rows ly + 8r and the C contiguous columns lx*C .. lx*C + C-1 of the tile, so a k
+// step reads its B values with 16-byte shared loads (8-byte for C = 2), and one 16-byte load of an
+// A row serves KV = 4 k steps (2 for the 8 x 8 shape, whose accumulators leave fewer registers).
+// Rows of both staging arrays are padded to multiples of 16 bytes; the 16-byte reads of a warp then
+// touch distinct banks (A: rows 36 floats apart land 4 banks apart).  Every output still sums k in
+// order, so the results are those of the unstaged tile.
 constexpr int KC = 32;                                   // k-steps per staged block
-constexpr int kStageA = 64 * (KC + 1);                   // up to 64 rows, padded pitch
-constexpr int kStageB = KC * (32 + 1);                   // up to 32 columns, padded pitch
+constexpr int PA = KC + 4;                               // A row pitch (floats)
+constexpr int kStageA = 64 * PA;                         // up to 64 rows
+constexpr int kStageB = KC * (32 + 4);                   // up to 32 columns, pitch TC + 4
 constexpr int kStageWarp = kStageA + kStageB;            // floats per warp
 constexpr int kStageBytes = 8 * kStageWarp * int(sizeof(float));  // per 256-thread block
 
+// C consecutive floats from 16-byte (or, for C = 2, 8-byte) aligned shared memory.
+template <int C>
+__device__ __forceinline__ void lds_vec(const float* __restrict__ src, float (&v)[C]) {
+    if constexpr (C == 2) {
+        const float2 t = *reinterpret_cast<const float2*>(src);
+        v[0] = t.x; v[1] = t.y;
+    } else {
+#pragma unroll
+        for (int q = 0; q < C / 4; ++q) {
+            const float4 t = *reinterpret_cast<const float4*>(src + 4 * q);
+            v[4 * q] = t.x; v[4 * q + 1] = t.y; v[4 * q + 2] = t.z; v[4 * q + 3] = t.w;
+        }
+    }
+}
+
 template <int R, int C>
 __device__ __forceinline__ void warp_tile_staged(const DevProblem& p, int tm, int tn, int lane, float* __restrict__ sw) {
-    constexpr int TR = 8 * R, TC = 4 * C, PA = KC + 1, PB = TC + 1;
+    constexpr int TR = 8 * R, TC = 4 * C, PB = TC + 4;
+    constexpr int KV = R >= 8 ? 2 : 4;  // k steps per A load
     float* As = sw;            // As[r * PA + kk]
     float* Bs = sw + kStageA;  // Bs[kk * PB + c]
     const int ly = lane >> 2, lx = lane & 3;
@@ -178,17 +200,36 @@ __device__ __forceinline__ void warp_tile_staged(const DevProblem& p, int tm, in
             }
         }
         __syncwarp();
-#pragma unroll 2
-        for (int kk = 0; kk < kc; ++kk) {
-            float a0[R], b0[C];
+        const float* arow = As + ly * PA;
+        const float* bcol = Bs + lx * C;
+        const int kv = kc & ~(KV - 1);
+#pragma unroll 1
+        for (int kk = 0; kk < kv; kk += KV) {
+            float a[R][KV];
 #pragma unroll
-            for (int r = 0; r < R; ++r) a0[r] = As[(ly + 8 * r) * PA + kk];
+            for (int r = 0; r < R; ++r) lds_vec<KV>(arow + 8 * r * PA + kk, a[r]);
 #pragma unroll
-            for (int c = 0; c < C; ++c) b0[c] = Bs[kk * PB + lx + 4 * c];
+            for (int q = 0; q < KV; ++q) {
+                float b[C];
+                lds_vec<C>(bcol + (kk + q) * PB, b);
 #pragma unroll
-            for (int r = 0; r < R; ++r)
+                for (int r = 0; r < R; ++r)
 #pragma unroll
-                for (int c = 0; c < C; ++c) acc[r][c] = fmaf(a0[r], b0[c], acc[r][c]);
+                    for (int c = 0; c < C; ++c) acc[r][c] = fmaf(a[r][q], b[c], acc[r][c]);
+            }
+        }
+        // the last kc % KV steps one at a time (the staged zeros beyond kc are never added, so an
+        // output's sum is exactly that of its k range)
+#pragma unroll 1
+        for (int kk = kv; kk < kc; ++kk) {
+            float b[C];
+            lds_vec<C>(bcol + kk * PB, b);
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                const float a = arow[8 * r * PA + kk];
+#pragma unroll
+                for (int c = 0; c < C; ++c) acc[r][c] = fmaf(a, b[c], acc[r][c]);
+            }
         }
         __syncwarp();
     }
@@ -201,7 +242,7 @@ __device__ __forceinline__ void warp_tile_staged(const DevProblem& p, int tm, in
         float* crow = Cp + int64_t(i) * p.ldc;
 #pragma unroll
         for (int c = 0; c < C; ++c) {
-            const int j = j0 + lx + 4 * c;
+            const int j = j0 + lx * C + c;
             if (j >= p.n) continue;
             const float v = alpha * acc[r][c];
             crow[j] = (beta == 0.f) ? v : fmaf(beta, crow[j], v);
