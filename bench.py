@@ -819,8 +819,11 @@ def ours(args, dist: Dist):
     # tensor products per split product: one per modulus (CRT scheme) or S(S+1)/2 digit pairs
     pairs = info.slices_used if info.method_used == G.METHOD_SPLIT_CRT else info.slices_used * (info.slices_used + 1) // 2
     tc_flops = pairs * flops  # BF16 tensor operations of the slice products
+    # a large product runs its tensor-core work as launches over column parts of C: per launch, the
+    # work is the product's share and the time the launches' average
+    tc_lpp = max(n_tc, 1) / max(args.steps, 1)  # tensor-core launches per product
     tc_ms = ms_tc / max(n_tc, 1)
-    achieved = tc_flops / (tc_ms * 1e-3) / 1e12
+    achieved = tc_flops / tc_lpp / (tc_ms * 1e-3) / 1e12
     # burst peak: the kernel runs about 8 ms inside a 10 ms step, far from the seconds-long loop
     # the sustained figure is measured over; the sustained ratio is reported beside it
     peak = float(peaks.get("bf16_tflops"))
@@ -829,7 +832,8 @@ def ours(args, dist: Dist):
     try:
         with open(TRAFFIC_FILE) as f:
             tj = json.load(f)
-        if int(tj.get("size", 0)) == n and int(tj.get("slices", 0)) == info.slices_used:
+        if (int(tj.get("size", 0)) == n and int(tj.get("slices", 0)) == info.slices_used
+                and int(tj.get("launches_per_product", 1)) == round(tc_lpp)):
             traffic = int(tj["dram_bytes_per_launch"])
     except (OSError, ValueError, KeyError):
         traffic = None
@@ -838,8 +842,10 @@ def ours(args, dist: Dist):
                 "achieved": round(achieved, 2), "peak": peak, "unit": "TFLOP/s", "frac": round(achieved / peak, 4),
                 "traffic": traffic, "peak_source": f"bf16_tflops, burst ({peaks_src})",
                 "frac_of_sustained": round(achieved / peak_sus, 4),
-                "work_per_launch": f"{pairs} BF16 products x 2*{n}^3 tensor ops",
-                "kernel_ms": round(tc_ms, 3), "kernel_share_of_step": round(tc_ms / ms_step, 4)}
+                "work_per_launch": f"{pairs} BF16 products x 2*{n}^3 tensor ops / {round(tc_lpp)} launches",
+                "kernel_ms": round(tc_ms, 3), "kernel_ms_per_product": round(tc_ms * tc_lpp, 3),
+                "launches_per_product": round(tc_lpp, 3),
+                "kernel_share_of_step": round(tc_ms * tc_lpp / ms_step, 4)}
 
     if dist.rank == 0:
         line = {"metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": dist.world,

@@ -9,6 +9,7 @@
 #include <cstdint>
 #include <mutex>
 #include <string>
+#include <vector>
 
 namespace gb {
 
@@ -65,6 +66,10 @@ struct Runtime {
     static constexpr int kPipeEvents = 40;
     cudaEvent_t pipe_ev[kPipeEvents] = {};
     bool pipe_ready = false;
+    // events ordering a split product's two column parts across its two streams (created on
+    // first use, reused)
+    std::mutex part_mu;
+    std::vector<cudaEvent_t> part_events;
 };
 
 Runtime& runtime();

@@ -964,6 +964,7 @@ struct TcParams {
     int32_t* levels;         // [nseg][nlevels][mpad][npad] int32 (float modes: fp32 bits)
     int max_levels;          // level dimension of `levels`
     int band = 8;            // m-tiles per band of the unit order (2..32 measured alike at 8192^3)
+    int tn0 = 0;             // first n-tile of this launch (a product launched in column parts)
     const SplitInfo* info;
     int* status;
     uint64_t limit_ns;
@@ -1013,7 +1014,7 @@ __device__ __forceinline__ void unit_coords(const TcParams& p, int u, int& tm, i
     const int b = t / per_band, r = t % per_band;
     const int rows_in_band = min(band, p.m_tiles - b * band);
     tm = b * band + r % rows_in_band;
-    tn = r / rows_in_band;
+    tn = p.tn0 + r / rows_in_band;
 }
 
 template <int MODE>
@@ -1792,6 +1793,59 @@ size_t device_product_footprint(const Gemm& g, const SplitRequest& req) {
 
 bool split_auto_uses_native(const Gemm& g) { return auto_uses_native(g); }
 
+// A residue product with at least as many pair tiles as SMs runs its tensor-core work as two
+// launches over the two halves of C's column tiles, and the first half's reconstruction runs on a
+// second stream while the tensor cores work on the second half: a reconstruction block (128
+// threads, no shared memory) fits on an SM beside the tensor-core kernel's one CTA.  The second
+// stream belongs to the calling host thread, so concurrent callers (server slots, user threads)
+// never queue behind one another's reconstructions; the ordering events come from a pool.
+struct PartEvents {
+    cudaStream_t aux = nullptr;
+    cudaEvent_t tc0 = nullptr, done0 = nullptr;
+};
+
+struct ThreadPartStream {
+    cudaStream_t s = nullptr;
+    ~ThreadPartStream() {
+        if (s) cudaStreamDestroy(s);  // fails harmlessly once the context is gone at process exit
+    }
+};
+
+static bool part_events_get(PartEvents* pe, std::string* err) {
+    static thread_local ThreadPartStream ts;
+    if (!ts.s && cudaStreamCreateWithFlags(&ts.s, cudaStreamNonBlocking) != cudaSuccess) {
+        ts.s = nullptr;
+        if (err) *err = "part stream creation failed";
+        return false;
+    }
+    Runtime& r = runtime();
+    std::lock_guard<std::mutex> lk(r.part_mu);
+    cudaEvent_t ev[2];
+    for (int i = 0; i < 2; ++i) {
+        if (!r.part_events.empty()) {
+            ev[i] = r.part_events.back();
+            r.part_events.pop_back();
+        } else if (cudaEventCreateWithFlags(&ev[i], cudaEventDisableTiming) != cudaSuccess) {
+            if (i == 1) r.part_events.push_back(ev[0]);
+            if (err) *err = "part event creation failed";
+            return false;
+        }
+    }
+    pe->aux = ts.s;
+    pe->tc0 = ev[0];
+    pe->done0 = ev[1];
+    return true;
+}
+
+// The events go back to the pool once every record and wait on them is enqueued (a wait takes the
+// event's state when it is enqueued, so a later record by another product does not affect it).
+static void part_events_put(const PartEvents& pe) {
+    Runtime& r = runtime();
+    std::lock_guard<std::mutex> lk(r.part_mu);
+    r.part_events.push_back(pe.tc0);
+    r.part_events.push_back(pe.done0);
+}
+
 int device_product(const Gemm& g_in, const SplitRequest& req, const LaunchCtl& ctl, cudaStream_t st, Workspace& ws,
                    SplitResult* out, std::string* err) {
     Runtime& r = runtime();
@@ -1911,9 +1965,7 @@ int device_product(const Gemm& g_in, const SplitRequest& req, const LaunchCtl& c
     p.inject_stall = ctl.inject_stall;
     // units: one level of one pair tile and k-segment (the device picks the level count, at most
     // max_levels); CTA pairs (clusters of two): at most one pair per unit, at least one pair
-    const int units = m_tiles * n_tiles * nseg * max_levels;
     const int sms = req.max_sms > 0 ? std::min(req.max_sms, r.num_sms) : r.num_sms;
-    const int grid = 2 * std::max(1, std::min(units, sms / 2));
     auto kern = (mode == kExact || mode == kCrt) ? tc_gemm_kernel<kExact>
                                                  : (mode == kBf16 ? tc_gemm_kernel<kBf16> : tc_gemm_kernel<kBf16x3>);
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kTcSmem));
@@ -1921,21 +1973,49 @@ int device_product(const Gemm& g_in, const SplitRequest& req, const LaunchCtl& c
         if (err) *err = std::string("tc_gemm_kernel smem attribute: ") + cudaGetErrorString(e);
         return GB300_ERR_CUDA;
     }
-    {
+    auto launch_tc = [&](int tn0, int nt) {
+        TcParams q = p;
+        q.tn0 = tn0;
+        q.n_tiles = nt;
+        const int units = m_tiles * nt * nseg * max_levels;
+        const int grid = 2 * std::max(1, std::min(units, sms / 2));
         KernelTimer timer("tc_gemm", st);
-        kern<<<grid, THREADS, kTcSmem, st>>>(tA, tB, tC, p);
-    }
-    if (mode == kCrt) {
-        const int64_t colgroups = (n + CRT_COMBINE_COLS - 1) / CRT_COMBINE_COLS;
+        kern<<<grid, THREADS, kTcSmem, st>>>(tA, tB, tC, q);
+    };
+    // reconstruction of C's columns [c0, c0 + nc) on stream s
+    auto launch_crt_combine = [&](int64_t c0, int64_t nc, cudaStream_t s) {
+        const int64_t colgroups = (nc + CRT_COMBINE_COLS - 1) / CRT_COMBINE_COLS;
         dim3 cgrid(unsigned((colgroups + 127) / 128), unsigned(std::min<int64_t>(m, 65535)));
-        crt_combine_kernel<CRT_COMBINE_COLS><<<cgrid, 128, 0, st>>>(reinterpret_cast<const uint16_t*>(lv), nseg,
-                                                                     max_levels, mpad, npad, info, eA, eB, m, n,
-                                                                     g.alpha, g.beta, static_cast<double*>(g.C), g.ldc);
+        crt_combine_kernel<CRT_COMBINE_COLS><<<cgrid, 128, 0, s>>>(
+            reinterpret_cast<const uint16_t*>(lv) + c0, nseg, max_levels, mpad, npad, info, eA, eB + c0, m, nc,
+            g.alpha, g.beta, static_cast<double*>(g.C) + c0, g.ldc);
+    };
+    const bool in_parts = mode == kCrt && n_tiles >= 2 && m_tiles * n_tiles >= sms && req.max_sms <= 0;
+    if (in_parts) {
+        PartEvents pe;
+        if (!part_events_get(&pe, err)) return GB300_ERR_CUDA;
+        const int nt0 = n_tiles / 2;
+        const int64_t c0 = int64_t(nt0) * TN;
+        launch_tc(0, nt0);
+        cudaEventRecord(pe.tc0, st);
+        launch_tc(nt0, n_tiles - nt0);
+        cudaStreamWaitEvent(pe.aux, pe.tc0, 0);
+        launch_crt_combine(0, c0, pe.aux);
+        cudaEventRecord(pe.done0, pe.aux);
+        launch_crt_combine(c0, n - c0, st);
+        cudaStreamWaitEvent(st, pe.done0, 0);
+        part_events_put(pe);
+        count_launches(2);
     } else {
-        const int64_t colgroups = (n + COMBINE_COLS - 1) / COMBINE_COLS;
-        dim3 cgrid(unsigned((colgroups + 127) / 128), unsigned(std::min<int64_t>(m, 65535)));
-        combine_kernel<<<cgrid, 128, 0, st>>>(lv, nseg, max_levels, mpad, npad, mode, info, eA, eB, m, n, g.alpha,
-                                              g.beta, static_cast<double*>(g.C), g.ldc);
+        launch_tc(0, n_tiles);
+        if (mode == kCrt) {
+            launch_crt_combine(0, n, st);
+        } else {
+            const int64_t colgroups = (n + COMBINE_COLS - 1) / COMBINE_COLS;
+            dim3 cgrid(unsigned((colgroups + 127) / 128), unsigned(std::min<int64_t>(m, 65535)));
+            combine_kernel<<<cgrid, 128, 0, st>>>(lv, nseg, max_levels, mpad, npad, mode, info, eA, eB, m, n,
+                                                  g.alpha, g.beta, static_cast<double*>(g.C), g.ldc);
+        }
     }
     count_launches(2);
     e = cudaGetLastError();
