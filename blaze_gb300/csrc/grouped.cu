@@ -138,7 +138,7 @@ __device__ __forceinline__ void warp_tile(const DevProblem& p, int tm, int tn, i
 // order, so the results are those of the unstaged tile.
 constexpr int KC = 32;                                   // k-steps per staged block
 constexpr int PA = KC + 4;                               // A row pitch (floats)
-constexpr int kStageA = 64 * PA;                         // up to 64 rows
+constexpr int kStageA = 32 * PA;                         // up to 32 rows (FP32 tiles stop at 32 x 32)
 constexpr int kStageB = KC * (32 + 4);                   // up to 32 columns, pitch TC + 4
 constexpr int kStageWarp = kStageA + kStageB;            // floats per warp
 constexpr int kStageBytes = 8 * kStageWarp * int(sizeof(float));  // per 256-thread block
@@ -252,12 +252,13 @@ __device__ __forceinline__ void warp_tile_staged(const DevProblem& p, int tm, in
 
 // Shapes available per element type: FP64 stops at 16x32 / 32x16 warp tiles (16 accumulators per
 // lane): on the FP64 pipe a larger tile only adds padding, and the smaller register footprint lets an
-// SM hold twice the warps.
+// SM hold twice the warps.  FP32 stops at 32x32 (32 accumulators per lane), so that an SM holds three
+// 256-thread blocks (24 warps) to cover the latency of the staging loads.
 template <typename T>
-__host__ __device__ constexpr int max_shape() { return sizeof(T) == 8 ? 3 : 5; }
+__host__ __device__ constexpr int max_shape() { return sizeof(T) == 8 ? 3 : 4; }
 
 template <typename T>
-__global__ void __launch_bounds__(256, 2)
+__global__ void __launch_bounds__(256, sizeof(T) == 8 ? 2 : 3)
 grouped_kernel(const DevProblem* __restrict__ probs, const DevTile* __restrict__ tiles, int ntiles,
                int* __restrict__ counter) {
     const int lane = threadIdx.x & 31;
@@ -282,8 +283,7 @@ grouped_kernel(const DevProblem* __restrict__ probs, const DevTile* __restrict__
                 case 1: warp_tile_staged<2, 4>(p, tl.tm, tl.tn, lane, sw); break;
                 case 2: warp_tile_staged<4, 4>(p, tl.tm, tl.tn, lane, sw); break;
                 case 3: warp_tile_staged<2, 8>(p, tl.tm, tl.tn, lane, sw); break;
-                case 4: warp_tile_staged<4, 8>(p, tl.tm, tl.tn, lane, sw); break;
-                default: warp_tile_staged<8, 8>(p, tl.tm, tl.tn, lane, sw); break;
+                default: warp_tile_staged<4, 8>(p, tl.tm, tl.tn, lane, sw); break;
             }
         } else {
             switch (p.shape) {
@@ -357,14 +357,15 @@ void tune_defaults() {
         for (int a = 0; a < kMB; ++a)
             for (int b = 0; b < kMB; ++b)
                 for (int c = 0; c < kKB; ++c)
-                    g_tune.shape[d][a][b][c] = model_shape(rep[a], rep[b], d == 0 ? max_shape<double>() + 1 : kNumShapes);
+                    g_tune.shape[d][a][b][c] =
+                        model_shape(rep[a], rep[b], d == 0 ? max_shape<double>() + 1 : max_shape<float>() + 1);
     g_tune_init = true;
 }
 
 int pick_shape(int dtype_idx, int m, int n, int k, int mode_override = -1) {
     std::lock_guard<std::mutex> lock(g_tune_mu);
     tune_defaults();
-    const int nshapes = dtype_idx == 0 ? max_shape<double>() + 1 : kNumShapes;
+    const int nshapes = dtype_idx == 0 ? max_shape<double>() + 1 : max_shape<float>() + 1;
     const int a = bucket_mn(m), b = bucket_mn(n), c = bucket_k(k);
     switch (mode_override >= 0 ? mode_override : g_tune.mode[dtype_idx]) {
         case kPickTable: return g_tune.shape[dtype_idx][a][b][c];
