@@ -318,3 +318,26 @@ def test_crt_drain_groups_exact_at_their_largest_sums():
     num = sum(ya[p] * yb[p] << (2 * (top - exps[p // blk])) for p in range(k))
     exact = float(Fraction(num, 2 ** (2 * top)))
     assert np.all(C == exact), (float(C.min()), float(C.max()), exact)
+
+
+def test_column_parts_join_the_callers_stream():
+    """A large residue product runs its tensor-core work as two column parts and reconstructs the
+    first part on a second stream.  Two asynchronous calls on a user stream (the second with
+    beta = 1, so it reads the first's C) must be complete once that stream alone is synchronised."""
+    torch = pytest.importorskip("torch")
+    m, n, k = 4096, 4096, 512   # 16 x 16 = 256 pair tiles, at least one per SM: two column parts
+    A = O.uniform(m * k, 71)
+    B = O.uniform(k * n, 72)
+    dA, dB = torch.from_numpy(A).cuda(), torch.from_numpy(B).cuda()
+    dC = torch.zeros(m * n, dtype=torch.float64, device="cuda")
+    s = torch.cuda.Stream()
+    torch.cuda.synchronize()
+    o = G.opts(method="split_crt", residency=G.PTR_DEVICE, stream=s.cuda_stream, synchronous=False)
+    G.dgemm_ex(O.ROW_MAJOR, O.NO_TRANS, O.NO_TRANS, m, n, k, 1.0, dA, k, dB, n, 0.0, dC, n, o)
+    G.dgemm_ex(O.ROW_MAJOR, O.NO_TRANS, O.NO_TRANS, m, n, k, 1.0, dA, k, dB, n, 1.0, dC, n, o)
+    s.synchronize()
+    got = dC.cpu().numpy().reshape(m, n)
+    rows = np.arange(0, m, 97)
+    P = O.product_rows_dot2(O.ROW_MAJOR, O.NO_TRANS, O.NO_TRANS, m, n, k, A, k, B, n, rows=rows)
+    err = np.max(np.abs(got[rows] - 2.0 * P))
+    assert err <= 1e-11, err
