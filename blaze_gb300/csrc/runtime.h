@@ -63,7 +63,7 @@ struct Runtime {
     uint64_t inject_limit_ns = 0;
     // copy streams and events of the panel pipeline for host operands (created on first use)
     cudaStream_t copy_in = nullptr, copy_out = nullptr;
-    static constexpr int kPipeEvents = 40;
+    static constexpr int kPipeEvents = 64;
     cudaEvent_t pipe_ev[kPipeEvents] = {};
     bool pipe_ready = false;
     // events ordering a split product's two column parts across its two streams (created on

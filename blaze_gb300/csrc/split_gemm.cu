@@ -1811,13 +1811,19 @@ struct ThreadPartStream {
     }
 };
 
-static bool part_events_get(PartEvents* pe, std::string* err) {
+// The calling host thread's second stream (created on first use).
+static cudaStream_t thread_aux_stream(std::string* err) {
     static thread_local ThreadPartStream ts;
     if (!ts.s && cudaStreamCreateWithFlags(&ts.s, cudaStreamNonBlocking) != cudaSuccess) {
         ts.s = nullptr;
-        if (err) *err = "part stream creation failed";
-        return false;
+        if (err) *err = "second stream creation failed";
     }
+    return ts.s;
+}
+
+static bool part_events_get(PartEvents* pe, std::string* err) {
+    cudaStream_t aux = thread_aux_stream(err);
+    if (!aux) return false;
     Runtime& r = runtime();
     std::lock_guard<std::mutex> lk(r.part_mu);
     cudaEvent_t ev[2];
@@ -1831,7 +1837,7 @@ static bool part_events_get(PartEvents* pe, std::string* err) {
             return false;
         }
     }
-    pe->aux = ts.s;
+    pe->aux = aux;
     pe->tc0 = ev[0];
     pe->done0 = ev[1];
     return true;
@@ -2142,7 +2148,10 @@ int device_product_host_panels(const Gemm& g, const SplitRequest& req, const Lau
     auto* pa = static_cast<__nv_bfloat16*>(ws.get(kSlotSliceA, size_t(max_planes) * size_t(mpad) * size_t(kpad) * 2, err));
     const size_t bblock = size_t(max_planes) * size_t(Nq) * size_t(kpad);  // elements per B block
     auto* pb = static_cast<__nv_bfloat16*>(ws.get(kSlotSliceB, size_t(Q) * bblock * 2, err));
-    auto* lv = static_cast<int32_t*>(ws.get(kSlotLevels, size_t(nseg) * max_levels * size_t(mpad) * size_t(Nq) * 4, err));
+    // level planes of a block, two buffers: block b's reconstruction (on the second stream) reads
+    // buffer b % 2 while block b + 1's tensor-core work writes the other
+    const size_t lv_elems = size_t(nseg) * max_levels * size_t(mpad) * size_t(Nq);
+    auto* lv = static_cast<int32_t*>(ws.get(kSlotLevels, 2 * lv_elems * 4, err));
     const int64_t off_sq = round_up((m + n) * int64_t(sizeof(int)), 256);
     const int64_t off_info = round_up(off_sq + (m + n) * int64_t(sizeof(double)), 256);
     const int ninfo = P + Q + P * Q + 1;
@@ -2158,9 +2167,12 @@ int device_product_host_panels(const Gemm& g, const SplitRequest& req, const Lau
     // infos: [0, P) panels of A, [P, P+Q) blocks of B, [P+Q, P+Q+PQ) blocks of C, last: summary
     SplitInfo* info_sum = info_at(ninfo - 1);
     const double target = req.target_error > 0 ? req.target_error : double(k) * 0x1p-53;
-    // events: [0, P) A panels in, [P, P+Q) B blocks in, [P+Q, P+Q+PQ) C blocks computed, last: all out
+    // events: [0, P) A panels in, [P, P+Q) B blocks in, [P+Q, P+Q+PQ) C blocks computed, next:
+    // all out, then [P+Q+PQ+1, P+Q+2PQ+1) the blocks' tensor-core work done
     cudaEvent_t* ev = r.pipe_ev;
-    if (P + Q + P * Q + 1 > Runtime::kPipeEvents) return GB300_ERR_NOT_SUPPORTED;
+    if (P + Q + 2 * P * Q + 1 > Runtime::kPipeEvents) return GB300_ERR_NOT_SUPPORTED;
+    cudaStream_t aux = thread_aux_stream(err);
+    if (!aux) return GB300_ERR_CUDA;
     auto cuda_fail = [&](const char* what, cudaError_t e) {
         if (err) *err = std::string(what) + ": " + cudaGetErrorString(e);
         return GB300_ERR_CUDA;
@@ -2248,12 +2260,14 @@ int device_product_host_panels(const Gemm& g, const SplitRequest& req, const Lau
     };
 
     // ---- tensor maps: A panel planes, each B block's planes, the level planes of a block ----
-    CUtensorMap tA, tC, tB[kPipeMaxQ];
+    CUtensorMap tA, tC[2], tB[kPipeMaxQ];
     if (!encode_tmap_2d(&tA, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, pa, uint64_t(max_planes) * mpad, kpad, kpad, TM, TK,
-                        CU_TENSOR_MAP_SWIZZLE_128B, err) ||
-        !encode_tmap_2d(&tC, CU_TENSOR_MAP_DATA_TYPE_UINT16, 2, lv, uint64_t(nseg) * max_levels * mpad, Nq, Nq, 32, 64,
                         CU_TENSOR_MAP_SWIZZLE_128B, err))
         return GB300_ERR_CUDA;
+    for (int b = 0; b < 2; ++b)
+        if (!encode_tmap_2d(&tC[b], CU_TENSOR_MAP_DATA_TYPE_UINT16, 2, lv + b * lv_elems,
+                            uint64_t(nseg) * max_levels * mpad, Nq, Nq, 32, 64, CU_TENSOR_MAP_SWIZZLE_128B, err))
+            return GB300_ERR_CUDA;
     for (int j = 0; j < Q; ++j)
         if (!encode_tmap_2d(&tB[j], CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, pb + size_t(j) * bblock,
                             uint64_t(max_planes) * Nq, kpad, kpad, TNH, TK, CU_TENSOR_MAP_SWIZZLE_128B, err))
@@ -2289,9 +2303,19 @@ int device_product_host_panels(const Gemm& g, const SplitRequest& req, const Lau
         e = copy_to_host(hC + r0 * g.ldc, size_t(g.ldc) * 8, dC + r0 * n, size_t(n) * 8, size_t(n) * 8, size_t(mi),
                          r.copy_out);
     };
+    // Block b (in run order) writes level buffer b % 2 on st; its reconstruction runs on the second
+    // stream and records the block's event, which the copies of C wait on; block b + 2 waits for
+    // block b's reconstruction before it overwrites the buffer.
+    int nrun = 0;
+    int run_ij[2 * kPipeMaxQ * 16];  // block index i * Q + j of every block run so far
+    auto tc_done_ev = [&](int blk) { return ev[P + Q + P * Q + 1 + blk]; };
     auto run_block = [&](int i, int j) {
         const int64_t r0 = int64_t(i) * Mp, mi = std::min(Mp, m - r0);
         const int64_t c0 = int64_t(j) * Nq, nj = std::min(Nq, n - c0);
+        const int buf = nrun & 1;
+        int32_t* lvb = lv + buf * lv_elems;
+        if (nrun >= 2) cudaStreamWaitEvent(st, ev[P + Q + run_ij[nrun - 2]], 0);
+        run_ij[nrun++] = i * Q + j;
         SplitInfo* info = info_at(P + Q + i * Q + j);
         split_block_kernel<<<1, 32, 0, st>>>(info_at(i), info_at(P + j), k, max_planes, info);
         TcParams tp;
@@ -2303,7 +2327,7 @@ int device_product_host_panels(const Gemm& g, const SplitRequest& req, const Lau
         tp.kb_total = Gp.kb_total;
         tp.mpad = mpad;
         tp.npad = Nq;
-        tp.levels = lv;
+        tp.levels = lvb;
         tp.max_levels = max_levels;
         tp.info = info;
         tp.status = ctl.status;
@@ -2313,16 +2337,18 @@ int device_product_host_panels(const Gemm& g, const SplitRequest& req, const Lau
         const int grid = 2 * std::max(1, std::min(units, r.num_sms / 2));
         {
             KernelTimer timer("tc_gemm", st);
-            tc_gemm_kernel<kExact><<<grid, THREADS, kTcSmem, st>>>(tA, tB[j], tC, tp);
+            tc_gemm_kernel<kExact><<<grid, THREADS, kTcSmem, st>>>(tA, tB[j], tC[buf], tp);
         }
+        cudaEventRecord(tc_done_ev(i * Q + j), st);
+        cudaStreamWaitEvent(aux, tc_done_ev(i * Q + j), 0);
         const int64_t colgroups = (nj + CRT_COMBINE_COLS - 1) / CRT_COMBINE_COLS;
         crt_combine_kernel<CRT_COMBINE_COLS>
-            <<<dim3(unsigned((colgroups + 127) / 128), unsigned(std::min<int64_t>(mi, 65535))), 128, 0, st>>>(
-                reinterpret_cast<const uint16_t*>(lv), nseg, max_levels, mpad, Nq, info, eA + r0, eB + c0, mi, nj,
+            <<<dim3(unsigned((colgroups + 127) / 128), unsigned(std::min<int64_t>(mi, 65535))), 128, 0, aux>>>(
+                reinterpret_cast<const uint16_t*>(lvb), nseg, max_levels, mpad, Nq, info, eA + r0, eB + c0, mi, nj,
                 g.alpha, g.beta, dC + r0 * n + c0, n);
         count_launches(3);
         if ((e = cudaGetLastError()) != cudaSuccess) return;
-        cudaEventRecord(block_ev(i, j), st);
+        cudaEventRecord(block_ev(i, j), aux);
         if (c_locked) copy_block_out(i, j);
     };
     bool have_a[16] = {}, have_b[kPipeMaxQ] = {};
@@ -2358,6 +2384,7 @@ int device_product_host_panels(const Gemm& g, const SplitRequest& req, const Lau
     count_launches(1);
     cudaEventRecord(ev[P + Q + P * Q], r.copy_out);
     cudaStreamWaitEvent(st, ev[P + Q + P * Q], 0);  // the call's work ends on st
+    if (nrun > 0) cudaStreamWaitEvent(st, ev[P + Q + run_ij[nrun - 1]], 0);  // and so does the second stream's
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail("block pipeline", e);
     out->method_used = GB300_METHOD_SPLIT_CRT;
     out->slices = -1;
