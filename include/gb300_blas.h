@@ -56,7 +56,9 @@ typedef struct gb300_gemm_opts {
                               a positive count selects the digit scheme); SPLIT_CRT: moduli cap */
     double target_error;   /* GB300_METHOD_SPLIT: normwise bound to reach; <= 0 means k * 2^-53 */
     int residency;         /* gb300_residency */
-    void* stream;          /* cudaStream_t to run on; NULL = the library's stream */
+    void* stream;          /* cudaStream_t to run on; NULL = the library's stream.  All of a call's
+                              device work is ordered on it: what the library runs on a second
+                              stream inside the call is joined back to it. */
     int synchronous;       /* non-zero: return after the result is in C */
     /* outputs */
     int method_used;       /* the form that ran */
