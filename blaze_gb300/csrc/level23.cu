@@ -51,6 +51,9 @@ __global__ void __launch_bounds__(256) mv_rows_kernel(int64_t rows, int64_t cols
         V acc = A::zero();
         const V* sp = S + i * ld + j0 + lane;
         const V* xp = x + (j0 + lane) * incx;
+        // unrolled (still one chain per lane, summed in order) so that the next steps' loads issue
+        // ahead of this step's FMA: 2 % faster at 16384 x 8192
+#pragma unroll 4
         for (int64_t j = j0 + lane; j < j1; j += 32, sp += 32, xp += xstep)
             acc = mv_step<V, CONJ>(sp, unit && j == i, *xp, acc);
 #pragma unroll
@@ -79,6 +82,7 @@ __global__ void __launch_bounds__(256) mv_cols_partial_kernel(int64_t rows, int6
     V acc = A::zero();
     const V* sp = S + i0 * ld + j;
     const V* xp = x + i0 * incx;
+#pragma unroll 4
     for (int64_t i = i0; i < i1; ++i, sp += ld, xp += incx) acc = mv_step<V, CONJ>(sp, unit && i == j, *xp, acc);
     part[int64_t(blockIdx.y) * cols + j] = acc;
 }
