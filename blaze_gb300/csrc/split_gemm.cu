@@ -51,10 +51,13 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 #include <cmath>
 #include <string>
 #include <type_traits>
+#include <utility>
+#include <vector>
 
 #include "../../include/gb300_blas.h"
 #include "gb300_internal.h"
@@ -1797,32 +1800,46 @@ bool split_auto_uses_native(const Gemm& g) { return auto_uses_native(g); }
 // launches over the two halves of C's column tiles, and the first half's reconstruction runs on a
 // second stream while the tensor cores work on the second half: a reconstruction block (128
 // threads, no shared memory) fits on an SM beside the tensor-core kernel's one CTA.  The second
-// stream belongs to the calling host thread, so concurrent callers (server slots, user threads)
-// never queue behind one another's reconstructions; the ordering events come from a pool.
+// stream belongs to the pair (calling host thread, caller's stream) and has the caller's stream
+// priority, so concurrent callers (user threads, or the server's slots, launched from its one
+// scheduler thread on their own streams) never queue behind one another's reconstructions; the
+// ordering events come from a pool.
 struct PartEvents {
     cudaStream_t aux = nullptr;
     cudaEvent_t tc0 = nullptr, done0 = nullptr;
 };
 
-struct ThreadPartStream {
-    cudaStream_t s = nullptr;
-    ~ThreadPartStream() {
-        if (s) cudaStreamDestroy(s);  // fails harmlessly once the context is gone at process exit
+struct ThreadAuxStreams {
+    static constexpr size_t kMax = 32;
+    std::vector<std::pair<cudaStream_t, cudaStream_t>> map;  // caller's stream -> second stream
+    ~ThreadAuxStreams() {
+        for (auto& kv : map) cudaStreamDestroy(kv.second);  // fails harmlessly once the context is gone
     }
 };
 
-// The calling host thread's second stream (created on first use).
-static cudaStream_t thread_aux_stream(std::string* err) {
-    static thread_local ThreadPartStream ts;
-    if (!ts.s && cudaStreamCreateWithFlags(&ts.s, cudaStreamNonBlocking) != cudaSuccess) {
-        ts.s = nullptr;
-        if (err) *err = "second stream creation failed";
+// The second stream of the calling host thread for the caller's stream `st` (created on first
+// use; past kMax callers' streams the last one is shared, which orders more but stays correct).
+static cudaStream_t aux_stream_for(cudaStream_t st, std::string* err) {
+    static thread_local ThreadAuxStreams ts;
+    for (auto& kv : ts.map)
+        if (kv.first == st) return kv.second;
+    if (ts.map.size() >= ThreadAuxStreams::kMax) return ts.map.back().second;
+    int prio = 0;
+    if (cudaStreamGetPriority(st, &prio) != cudaSuccess) {
+        cudaGetLastError();
+        prio = 0;
     }
-    return ts.s;
+    cudaStream_t s = nullptr;
+    if (cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, prio) != cudaSuccess) {
+        if (err) *err = "second stream creation failed";
+        return nullptr;
+    }
+    ts.map.emplace_back(st, s);
+    return s;
 }
 
-static bool part_events_get(PartEvents* pe, std::string* err) {
-    cudaStream_t aux = thread_aux_stream(err);
+static bool part_events_get(cudaStream_t st, PartEvents* pe, std::string* err) {
+    cudaStream_t aux = aux_stream_for(st, err);
     if (!aux) return false;
     Runtime& r = runtime();
     std::lock_guard<std::mutex> lk(r.part_mu);
@@ -1999,7 +2016,7 @@ int device_product(const Gemm& g_in, const SplitRequest& req, const LaunchCtl& c
     const bool in_parts = mode == kCrt && n_tiles >= 2 && m_tiles * n_tiles >= sms && req.max_sms <= 0;
     if (in_parts) {
         PartEvents pe;
-        if (!part_events_get(&pe, err)) return GB300_ERR_CUDA;
+        if (!part_events_get(st, &pe, err)) return GB300_ERR_CUDA;
         const int nt0 = n_tiles / 2;
         const int64_t c0 = int64_t(nt0) * TN;
         launch_tc(0, nt0);
@@ -2171,7 +2188,7 @@ int device_product_host_panels(const Gemm& g, const SplitRequest& req, const Lau
     // all out, then [P+Q+PQ+1, P+Q+2PQ+1) the blocks' tensor-core work done
     cudaEvent_t* ev = r.pipe_ev;
     if (P + Q + 2 * P * Q + 1 > Runtime::kPipeEvents) return GB300_ERR_NOT_SUPPORTED;
-    cudaStream_t aux = thread_aux_stream(err);
+    cudaStream_t aux = aux_stream_for(st, err);
     if (!aux) return GB300_ERR_CUDA;
     auto cuda_fail = [&](const char* what, cudaError_t e) {
         if (err) *err = std::string(what) + ": " + cudaGetErrorString(e);
