@@ -1716,10 +1716,15 @@ SplitGeometry split_geometry(const Gemm& g, const SplitRequest& req, int num_sms
     // still fit one wave of pairs.  With more tiles a split cannot raise the occupancy (the units
     // spill into a second, partial wave) and it multiplies the residue planes the reconstruction
     // reads; at 64 tiles on 76 pairs two segments made a 512 x 8192 x 512 product 1.6 times slower.
+    // A segment keeps at least one TMEM drain group of k (1024): a unit of 256 k has about 1.3 us of
+    // products against about 3 us of epilogue (drain, modular reduction, residue store), and every
+    // extra segment adds residue planes for the reconstruction; 1024^3 split into four 256-k
+    // segments took 59 us in the tensor-core kernel and 55 us in the reconstruction.
     const int tiles = G.m_tiles * G.n_tiles, pairs = std::max(1, num_sms / 2);
     if (2 * tiles <= pairs) {
         const int64_t want = pairs / tiles;
-        kseg = std::min(kseg, std::max<int64_t>(KSEG_UNIT, round_up((G.kpad + want - 1) / want, KSEG_UNIT)));
+        constexpr int64_t kMinSeg = int64_t(GROUP_ITEMS) * TK;
+        kseg = std::min(kseg, std::max<int64_t>(kMinSeg, round_up((G.kpad + want - 1) / want, KSEG_UNIT)));
     }
     // equal segments: persistent CTAs take units in a fixed stride, so unequal segments would give
     // some CTAs only the long ones
