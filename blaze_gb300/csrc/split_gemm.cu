@@ -737,6 +737,17 @@ __global__ void split_block_kernel(const SplitInfo* __restrict__ ia, const Split
 
 // Summary of the blocks for the caller: the largest modulus count and bound (infos `stride` bytes
 // apart).
+// The level count of a launch that covers several blocks of one panel: the largest of its blocks'
+// (each block's reconstruction reads its own count of levels; the launch reads only the count).
+__global__ void split_max_slices_kernel(const uint8_t* __restrict__ infos, size_t stride, int count,
+                                        SplitInfo* __restrict__ out) {
+    if (threadIdx.x != 0) return;
+    SplitInfo r = *reinterpret_cast<const SplitInfo*>(infos);
+    for (int i = 1; i < count; ++i)
+        r.slices = max(r.slices, reinterpret_cast<const SplitInfo*>(infos + size_t(i) * stride)->slices);
+    *out = r;
+}
+
 __global__ void split_panels_summary_kernel(const uint8_t* __restrict__ infos, size_t stride, int count,
                                             SplitInfo* out) {
     if (threadIdx.x != 0) return;
@@ -2156,9 +2167,11 @@ int device_product_host_panels(const Gemm& g, const SplitRequest& req, const Lau
     gp.n = Nq;
     const SplitGeometry Gp = split_geometry(gp, req, r.num_sms);
     const int64_t mpad = Gp.mpad, kpad = Gp.kpad;
-    // B planes block-major: block j holds its max_planes planes of Nq rows, so a block reads like a
-    // whole B of Nq columns (plane stride Nq * kpad)
+    // B planes plane-major over the whole width: plane b holds the Q * Nq columns of every column
+    // block (block j at rows j * Nq..), so one tensor map addresses all blocks and one launch can
+    // cover all blocks of a panel
     const int max_planes = Gp.max_planes, max_levels = Gp.max_levels, nseg = Gp.nseg;
+    const int64_t npb = int64_t(Q) * Nq;
 
     // device copies of the operands in their stored shapes (dense pitch), C, planes, levels, statistics
     const int64_t a_rows = g.ta ? k : m, a_cols = g.ta ? m : k;
@@ -2168,15 +2181,14 @@ int device_product_host_panels(const Gemm& g, const SplitRequest& req, const Lau
     auto* dC = static_cast<double*>(ws.get(kSlotC, size_t(m) * size_t(n) * 8, err));
     // A planes of one panel: a panel's blocks all run before the next panel is sliced
     auto* pa = static_cast<__nv_bfloat16*>(ws.get(kSlotSliceA, size_t(max_planes) * size_t(mpad) * size_t(kpad) * 2, err));
-    const size_t bblock = size_t(max_planes) * size_t(Nq) * size_t(kpad);  // elements per B block
-    auto* pb = static_cast<__nv_bfloat16*>(ws.get(kSlotSliceB, size_t(Q) * bblock * 2, err));
-    // level planes of a block, two buffers: block b's reconstruction (on the second stream) reads
-    // buffer b % 2 while block b + 1's tensor-core work writes the other
-    const size_t lv_elems = size_t(nseg) * max_levels * size_t(mpad) * size_t(Nq);
+    auto* pb = static_cast<__nv_bfloat16*>(ws.get(kSlotSliceB, size_t(max_planes) * size_t(npb) * size_t(kpad) * 2, err));
+    // level planes of a launch over the whole width, two buffers: launch L's reconstructions (on the
+    // second stream) read buffer L % 2 while launch L + 1's tensor-core work writes the other
+    const size_t lv_elems = size_t(nseg) * max_levels * size_t(mpad) * size_t(npb);
     auto* lv = static_cast<int32_t*>(ws.get(kSlotLevels, 2 * lv_elems * 4, err));
     const int64_t off_sq = round_up((m + n) * int64_t(sizeof(int)), 256);
     const int64_t off_info = round_up(off_sq + (m + n) * int64_t(sizeof(double)), 256);
-    const int ninfo = P + Q + P * Q + 1;
+    const int ninfo = P + Q + P * Q + P + 1;
     const size_t info_stride = ((sizeof(SplitInfo) + 255) / 256) * 256;
     auto* stats = static_cast<uint8_t*>(ws.get(kSlotScaleA, size_t(off_info) + size_t(ninfo) * info_stride, err));
     auto* racc = static_cast<RowAcc*>(ws.get(kSlotScaleB, size_t(m + n) * sizeof(RowAcc), err));
@@ -2186,11 +2198,12 @@ int device_product_host_panels(const Gemm& g, const SplitRequest& req, const Lau
     double* sqA = reinterpret_cast<double*>(stats + off_sq);
     double* sqB = sqA + m;
     auto info_at = [&](int i) { return reinterpret_cast<SplitInfo*>(stats + off_info + size_t(i) * info_stride); };
-    // infos: [0, P) panels of A, [P, P+Q) blocks of B, [P+Q, P+Q+PQ) blocks of C, last: summary
+    // infos: [0, P) panels of A, [P, P+Q) blocks of B, [P+Q, P+Q+PQ) blocks of C, [P+Q+PQ,
+    // P+Q+PQ+P) the launches over a whole panel (the largest level count of its blocks), last: summary
     SplitInfo* info_sum = info_at(ninfo - 1);
     const double target = req.target_error > 0 ? req.target_error : double(k) * 0x1p-53;
     // events: [0, P) A panels in, [P, P+Q) B blocks in, [P+Q, P+Q+PQ) C blocks computed, next:
-    // all out, then [P+Q+PQ+1, P+Q+2PQ+1) the blocks' tensor-core work done
+    // all out, then [P+Q+PQ+1, P+Q+2PQ+1) the launches' tensor-core work done
     cudaEvent_t* ev = r.pipe_ev;
     if (P + Q + 2 * P * Q + 1 > Runtime::kPipeEvents) return GB300_ERR_NOT_SUPPORTED;
     cudaStream_t aux = aux_stream_for(st, err);
@@ -2242,7 +2255,7 @@ int device_product_host_panels(const Gemm& g, const SplitRequest& req, const Lau
     base.rexp[0] = eA; base.rexp[1] = eB;
     base.rsq[0] = sqA; base.rsq[1] = sqB;
     base.planes[0] = pa; base.planes[1] = pb;
-    base.rpad[0] = mpad; base.rpad[1] = Nq;
+    base.rpad[0] = mpad; base.rpad[1] = npb;
     base.yb0 = 0;
     // statistics, side scaling and planes of A's panel i (into the panel plane buffer)
     auto prep_a = [&](int i) {
@@ -2271,8 +2284,8 @@ int device_product_host_panels(const Gemm& g, const SplitRequest& req, const Lau
         o.acc[1] = racc + m + c0;
         o.rexp[1] = eB + c0;
         o.rsq[1] = sqB + c0;
-        o.planes[1] = pb + size_t(j) * bblock;
-        o.rpad[1] = Nq;
+        o.planes[1] = pb + size_t(j) * size_t(Nq) * size_t(kpad);
+        o.rpad[1] = npb;
         o.yb0 = 0;
         stats_tile_kernel<<<dim3(ktiles, unsigned((nj + 31) / 32)), 256, 0, st>>>(o, k);
         stats_finalize_pair_kernel<<<unsigned((nj + 255) / 256), 256, 0, st>>>(o, k, 0u, nullptr);
@@ -2281,18 +2294,16 @@ int device_product_host_panels(const Gemm& g, const SplitRequest& req, const Lau
         count_launches(4);
     };
 
-    // ---- tensor maps: A panel planes, each B block's planes, the level planes of a block ----
-    CUtensorMap tA, tC[2], tB[kPipeMaxQ];
+    // ---- tensor maps: A panel planes, the B planes, the level planes of a launch ----
+    CUtensorMap tA, tB, tC[2];
     if (!encode_tmap_2d(&tA, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, pa, uint64_t(max_planes) * mpad, kpad, kpad, TM, TK,
+                        CU_TENSOR_MAP_SWIZZLE_128B, err) ||
+        !encode_tmap_2d(&tB, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, pb, uint64_t(max_planes) * npb, kpad, kpad, TNH, TK,
                         CU_TENSOR_MAP_SWIZZLE_128B, err))
         return GB300_ERR_CUDA;
     for (int b = 0; b < 2; ++b)
         if (!encode_tmap_2d(&tC[b], CU_TENSOR_MAP_DATA_TYPE_UINT16, 2, lv + b * lv_elems,
-                            uint64_t(nseg) * max_levels * mpad, Nq, Nq, 32, 64, CU_TENSOR_MAP_SWIZZLE_128B, err))
-            return GB300_ERR_CUDA;
-    for (int j = 0; j < Q; ++j)
-        if (!encode_tmap_2d(&tB[j], CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, pb + size_t(j) * bblock,
-                            uint64_t(max_planes) * Nq, kpad, kpad, TNH, TK, CU_TENSOR_MAP_SWIZZLE_128B, err))
+                            uint64_t(nseg) * max_levels * mpad, npb, npb, 32, 64, CU_TENSOR_MAP_SWIZZLE_128B, err))
             return GB300_ERR_CUDA;
     e = cudaFuncSetAttribute(tc_gemm_kernel<kExact>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kTcSmem));
     if (e != cudaSuccess) return cuda_fail("tc_gemm_kernel smem attribute", e);
@@ -2325,33 +2336,49 @@ int device_product_host_panels(const Gemm& g, const SplitRequest& req, const Lau
         e = copy_to_host(hC + r0 * g.ldc, size_t(g.ldc) * 8, dC + r0 * n, size_t(n) * 8, size_t(n) * 8, size_t(mi),
                          r.copy_out);
     };
-    // Block b (in run order) writes level buffer b % 2 on st; its reconstruction runs on the second
-    // stream and records the block's event, which the copies of C wait on; block b + 2 waits for
-    // block b's reconstruction before it overwrites the buffer.
-    int nrun = 0;
-    int run_ij[2 * kPipeMaxQ * 16];  // block index i * Q + j of every block run so far
-    auto tc_done_ev = [&](int blk) { return ev[P + Q + P * Q + 1 + blk]; };
-    auto run_block = [&](int i, int j) {
+    // Launch L (blocks j0..j1-1 of panel i, one tensor-core launch) writes level buffer L % 2 on st;
+    // each block's reconstruction runs on the second stream and records the block's event, which the
+    // copies of C wait on; launch L + 2 waits for launch L's reconstructions before it overwrites the
+    // buffer.  A panel whose A arrives after all of B runs as one launch (fewer, fuller waves of pair
+    // units than a launch per block), except the last: its blocks' copies back then start one block
+    // earlier; the first panel's blocks run as their B blocks arrive.
+    int nlaunch = 0;
+    int launch_i[16 * kPipeMaxQ], launch_j0[16 * kPipeMaxQ], launch_j1[16 * kPipeMaxQ];
+    auto tc_done_ev = [&](int l) { return ev[P + Q + P * Q + 1 + l]; };
+    auto run_blocks = [&](int i, int j0, int j1) {
         const int64_t r0 = int64_t(i) * Mp, mi = std::min(Mp, m - r0);
-        const int64_t c0 = int64_t(j) * Nq, nj = std::min(Nq, n - c0);
-        const int buf = nrun & 1;
+        const int64_t c0 = int64_t(j0) * Nq, c1 = std::min(n, int64_t(j1) * Nq);
+        const int l = nlaunch++;
+        const int buf = l & 1;
         int32_t* lvb = lv + buf * lv_elems;
-        if (nrun >= 2) cudaStreamWaitEvent(st, ev[P + Q + run_ij[nrun - 2]], 0);
-        run_ij[nrun++] = i * Q + j;
-        SplitInfo* info = info_at(P + Q + i * Q + j);
-        split_block_kernel<<<1, 32, 0, st>>>(info_at(i), info_at(P + j), k, max_planes, info);
+        if (l >= 2)
+            for (int j = launch_j0[l - 2]; j < launch_j1[l - 2]; ++j)
+                cudaStreamWaitEvent(st, block_ev(launch_i[l - 2], j), 0);
+        launch_i[l] = i;
+        launch_j0[l] = j0;
+        launch_j1[l] = j1;
+        for (int j = j0; j < j1; ++j)
+            split_block_kernel<<<1, 32, 0, st>>>(info_at(i), info_at(P + j), k, max_planes, info_at(P + Q + i * Q + j));
+        SplitInfo* linfo = info_at(P + Q + i * Q + j0);
+        if (j1 - j0 > 1) {
+            linfo = info_at(P + Q + P * Q + i);
+            split_max_slices_kernel<<<1, 32, 0, st>>>(reinterpret_cast<const uint8_t*>(info_at(P + Q + i * Q + j0)),
+                                                      info_stride, j1 - j0, linfo);
+            count_launches(1);
+        }
         TcParams tp;
         tp.mode = kCrt;
         tp.m_tiles = int((mi + TMP - 1) / TMP);
-        tp.n_tiles = int((nj + TN - 1) / TN);
+        tp.tn0 = int(c0 / TN);
+        tp.n_tiles = int((c1 - c0 + TN - 1) / TN);
         tp.nseg = nseg;
         tp.kb_per_seg = int(Gp.kseg / TK);
         tp.kb_total = Gp.kb_total;
         tp.mpad = mpad;
-        tp.npad = Nq;
+        tp.npad = npb;
         tp.levels = lvb;
         tp.max_levels = max_levels;
-        tp.info = info;
+        tp.info = linfo;
         tp.status = ctl.status;
         tp.limit_ns = ctl.wait_limit_ns;
         tp.inject_stall = ctl.inject_stall;
@@ -2359,21 +2386,25 @@ int device_product_host_panels(const Gemm& g, const SplitRequest& req, const Lau
         const int grid = 2 * std::max(1, std::min(units, r.num_sms / 2));
         {
             KernelTimer timer("tc_gemm", st);
-            tc_gemm_kernel<kExact><<<grid, THREADS, kTcSmem, st>>>(tA, tB[j], tC[buf], tp);
+            tc_gemm_kernel<kExact><<<grid, THREADS, kTcSmem, st>>>(tA, tB, tC[buf], tp);
         }
-        cudaEventRecord(tc_done_ev(i * Q + j), st);
-        cudaStreamWaitEvent(aux, tc_done_ev(i * Q + j), 0);
-        const int64_t colgroups = (nj + CRT_COMBINE_COLS - 1) / CRT_COMBINE_COLS;
-        crt_combine_kernel<CRT_COMBINE_COLS>
-            <<<dim3(unsigned((colgroups + 127) / 128), unsigned(std::min<int64_t>(mi, 65535))), 128, 0, aux>>>(
-                reinterpret_cast<const uint16_t*>(lvb), nseg, max_levels, mpad, Nq, info, eA + r0, eB + c0, mi, nj,
-                g.alpha, g.beta, dC + r0 * n + c0, n);
-        count_launches(3);
-        if ((e = cudaGetLastError()) != cudaSuccess) return;
-        cudaEventRecord(block_ev(i, j), aux);
-        if (c_locked) copy_block_out(i, j);
+        cudaEventRecord(tc_done_ev(l), st);
+        cudaStreamWaitEvent(aux, tc_done_ev(l), 0);
+        for (int j = j0; j < j1; ++j) {
+            const int64_t cj = int64_t(j) * Nq, nj = std::min(Nq, n - cj);
+            const int64_t colgroups = (nj + CRT_COMBINE_COLS - 1) / CRT_COMBINE_COLS;
+            crt_combine_kernel<CRT_COMBINE_COLS>
+                <<<dim3(unsigned((colgroups + 127) / 128), unsigned(std::min<int64_t>(mi, 65535))), 128, 0, aux>>>(
+                    reinterpret_cast<const uint16_t*>(lvb) + cj, nseg, max_levels, mpad, npb,
+                    info_at(P + Q + i * Q + j), eA + r0, eB + cj, mi, nj, g.alpha, g.beta, dC + r0 * n + cj, n);
+            if ((e = cudaGetLastError()) != cudaSuccess) return;
+            cudaEventRecord(block_ev(i, j), aux);
+            if (c_locked) copy_block_out(i, j);
+        }
+        count_launches(1 + 2 * (j1 - j0));
     };
     bool have_a[16] = {}, have_b[kPipeMaxQ] = {};
+    int nb = 0;  // B blocks in
     auto load = [&](int side, int idx) {
         if (side == 0) {
             copy_a(idx);
@@ -2381,16 +2412,19 @@ int device_product_host_panels(const Gemm& g, const SplitRequest& req, const Lau
             cudaStreamWaitEvent(st, ev[idx], 0);
             prep_a(idx);
             have_a[idx] = true;
-            for (int j = 0; j < Q && e == cudaSuccess; ++j)
-                if (have_b[j]) run_block(idx, j);
+            if (nb == Q && idx + 1 < P) run_blocks(idx, 0, Q);
+            else
+                for (int j = 0; j < Q && e == cudaSuccess; ++j)
+                    if (have_b[j]) run_blocks(idx, j, j + 1);
         } else {
             copy_b(idx);
             if (e != cudaSuccess) return;
             cudaStreamWaitEvent(st, ev[P + idx], 0);
             prep_b(idx);
             have_b[idx] = true;
+            ++nb;
             for (int i = 0; i < P && e == cudaSuccess; ++i)
-                if (have_a[i]) run_block(i, idx);
+                if (have_a[i]) run_blocks(i, idx, idx + 1);
         }
     };
     load(0, 0);
@@ -2406,7 +2440,8 @@ int device_product_host_panels(const Gemm& g, const SplitRequest& req, const Lau
     count_launches(1);
     cudaEventRecord(ev[P + Q + P * Q], r.copy_out);
     cudaStreamWaitEvent(st, ev[P + Q + P * Q], 0);  // the call's work ends on st
-    if (nrun > 0) cudaStreamWaitEvent(st, ev[P + Q + run_ij[nrun - 1]], 0);  // and so does the second stream's
+    for (int l = std::max(0, nlaunch - 2); l < nlaunch; ++l)  // and so does the second stream's
+        for (int j = launch_j0[l]; j < launch_j1[l]; ++j) cudaStreamWaitEvent(st, block_ev(launch_i[l], j), 0);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail("block pipeline", e);
     out->method_used = GB300_METHOD_SPLIT_CRT;
     out->slices = -1;
