@@ -295,15 +295,19 @@ def e2e_leg(G, hA, hB, n, flops, args, dist):
     pC = torch.empty(n * n, dtype=torch.float64).pin_memory()
     G.cblas_dgemm(G.RowMajor, G.NoTrans, G.NoTrans, n, n, n, 1.0, pA, n, pB, n, 0.0, pC, n)  # warm-up
     e2e_steps = max(2, min(args.steps, 10))
-    dist.barrier()
-    per_call = []
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        tc = time.perf_counter()
-        G.cblas_dgemm(G.RowMajor, G.NoTrans, G.NoTrans, n, n, n, 1.0, pA, n, pB, n, 0.0, pC, n)
-        per_call.append(time.perf_counter() - tc)
-    t_e2e = (time.perf_counter() - t0) / e2e_steps
-    t_e2e = dist.max(t_e2e)
+    # three rounds of e2e_steps calls; the value is the median round's mean, so that one call
+    # stalled on the shared host (50-270 ms, about once in 50-100 calls on these boxes, in runs of
+    # this code and of earlier versions alike) does not decide the figure; every round is reported
+    rounds, per_call = [], []
+    for _ in range(3):
+        dist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            tc = time.perf_counter()
+            G.cblas_dgemm(G.RowMajor, G.NoTrans, G.NoTrans, n, n, n, 1.0, pA, n, pB, n, 0.0, pC, n)
+            per_call.append(time.perf_counter() - tc)
+        rounds.append(dist.max((time.perf_counter() - t0) / e2e_steps))
+    t_e2e = sorted(rounds)[1]
     per_call.sort()
     # the same call on pageable buffers (plain malloc'd memory, as a Blaze DynamicMatrix holds)
     qA, qB = hA.numpy(), hB.numpy()
@@ -341,6 +345,8 @@ def e2e_leg(G, hA, hB, n, flops, args, dist):
     return {"value": round(flops * dist.world / t_e2e / 1e12, 4), "unit": UNIT,
             "h2d_bytes_per_step": 2 * n * n * 8, "d2h_bytes_per_step": n * n * 8, "steps": e2e_steps,
             "ms_per_step": round(t_e2e * 1e3, 3), "call": "cblas_dgemm (default method: auto -> split)",
+            "value_of": f"the median of 3 rounds of {e2e_steps} calls (each round's mean per call in rounds_ms)",
+            "rounds_ms": [round(x * 1e3, 3) for x in rounds],
             "ms_per_call_min_median_max": [round(per_call[0] * 1e3, 3), round(per_call[len(per_call) // 2] * 1e3, 3),
                                            round(per_call[-1] * 1e3, 3)],
             "pageable": {"value": round(flops * dist.world / dist.max(pg_call[len(pg_call) // 2]) / 1e12, 4),
